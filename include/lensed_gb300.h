@@ -1,0 +1,193 @@
+/*
+ * lensed_gb300 -- C ABI of the GB300-native Lensed likelihood path.
+ *
+ * The library replaces Lensed's device runtime and kernel assembly
+ * (src/opencl.c, src/kernel.c) and the arithmetic of its likelihood callback
+ * (src/nested.c:17-131) with CUDA for sm_103a.  A context holds one lens
+ * system -- image, weights, optional PSF, pixel coordinate system, quadrature
+ * rule and an ordered object list -- resident on one GPU, plus a program
+ * composed from the object plugins and compiled with NVRTC.  Evaluation is
+ * batched: one call evaluates B candidate parameter vectors.
+ *
+ * Conventions
+ *   - The caller owns every host buffer passed in; the context owns its
+ *     device memory, stream, module and graphs.
+ *   - Functions return LG_OK (0) or a negative LG_ERR_* code and never exit
+ *     the process; lg_last_error() describes the last failure of a context.
+ *   - A context is used by one host thread at a time.  Separate contexts are
+ *     independent.
+ *   - Images are row-major float32 with row 0 at the bottom (FITS order), so
+ *     pixel index k = x + width * y and pixel (x, y) has coordinates
+ *     (rx + sx * x, ry + sy * y) -- kernel/lensed.cl:25.
+ *   - Parameter vectors are in the context's parameter-map order: the free
+ *     parameters first, then the derived ones (fixed by a delta prior), each
+ *     group in object order -- src/lensed.c:106-271.
+ */
+#ifndef LENSED_GB300_H
+#define LENSED_GB300_H
+
+#include <stddef.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define LG_VERSION_MAJOR 0
+#define LG_VERSION_MINOR 1
+
+/* status codes */
+#define LG_OK 0
+#define LG_ERR_INPUT (-1)       /* invalid argument, size, name or prior */
+#define LG_ERR_COMPILE (-2)     /* NVRTC composition or compilation failed */
+#define LG_ERR_CUDA (-3)        /* CUDA runtime / driver error */
+#define LG_ERR_ALLOC (-4)       /* device or host allocation failed */
+#define LG_ERR_TIMEOUT (-5)     /* a bounded device-side wait ran out */
+#define LG_ERR_UNSUPPORTED (-6) /* valid request the library does not do */
+
+/* object kinds (kernel/object.cl:1-6) */
+#define LG_LENS 'L'
+#define LG_SOURCE 'S'
+#define LG_FOREGROUND 'F'
+
+/* parameter types (kernel/object.cl:8-17) */
+#define LG_PARAMETER 0
+#define LG_POSITION_X 1
+#define LG_POSITION_Y 2
+#define LG_RADIUS 3
+#define LG_MAGNITUDE 4
+#define LG_AXIS_RATIO 5
+#define LG_POS_ANGLE 6
+
+/* context flags */
+#define LG_FLAG_STRICT_FP 1 /* no FMA contraction in the composed program */
+#define LG_FLAG_NO_GRAPH 2  /* launch kernels directly instead of graph replay */
+
+typedef struct lg_ctx lg_ctx;
+
+/* The observed data of one lens system.  weight may be NULL only if
+ * lg_make_weight() output is passed instead; psf NULL means no PSF.
+ * pcs = (rx, ry, sx, sy); all zero means the default (1, 1, 1, 1). */
+typedef struct {
+    int width, height;
+    const float* image;  /* width*height */
+    const float* weight; /* width*height inverse variances, 0 = masked */
+    const float* psf;    /* psf_width*psf_height, normalised by lg_create */
+    int psf_width, psf_height;
+    double pcs[4];
+} lg_image_desc;
+
+/* One object of the model, in list order (the order decides the planes:
+ * sources before the first lens are unlensed; foregrounds use the unlensed
+ * position -- src/kernel.c:235-399).
+ *   name    plugin name: sis, sis_plus_shear, nsis, sie, sie_plus_shear, nsie,
+ *           point_mass, epl, epl_plus_shear, sersic, sersic_old, exponential,
+ *           devauc, gauss, sky, or a plugin added with lg_register_plugin
+ *   id      object identifier used in parameter ids "<id>.<param>"
+ *   priors  NULL or one string per plugin parameter in plugin order, each in
+ *           Lensed's prior syntax "[wrap] [image] <value> | unif a b |
+ *           norm m s" (docs/configuration.md); NULL entries keep the
+ *           plugin default (a fixed value where the plugin defines one). */
+typedef struct {
+    const char* name;
+    const char* id;
+    const char* const* priors;
+} lg_object_desc;
+
+typedef struct {
+    const char* rule; /* quadrature rule name, NULL = "g3k7" (src/input/options.c:130-135) */
+    int device;       /* CUDA device ordinal */
+    int max_batch;    /* largest B per call (scratch sizing); 0 = 1024 */
+    int flags;        /* LG_FLAG_* */
+} lg_options;
+
+/* Plugin description for lg_register_plugin (the equivalent of dropping an
+ * objects/<name>.cl file into Lensed).  source is CUDA C++ defining
+ * struct lg_data_<name>, lg_set_<name>(lg_data_<name>*, float...) with the
+ * parameters in order, and lg_deflection_<name> (lens), lg_brightness_<name>
+ * (source) or lg_foreground_<name> (foreground). */
+typedef struct {
+    const char* name;
+    int kind;                   /* LG_LENS / LG_SOURCE / LG_FOREGROUND */
+    int npars;
+    const char* const* par_names;
+    const int* par_types;       /* LG_PARAMETER ... LG_POS_ANGLE */
+    const float* par_bounds;    /* npars x {lower, upper}; {0,0} = unbounded */
+    const float* par_defaults;  /* npars; > 0 or -0.0 means fixed by default */
+    const char* source;
+} lg_plugin_desc;
+
+/* ---------------------------------------------------------------- library */
+const char* lg_version(void);
+int lg_plugin_count(void);
+/* Metadata of plugin i (0 <= i < lg_plugin_count()).  Any output may be NULL. */
+int lg_plugin_info(int i, const char** name, int* kind, int* npars);
+int lg_plugin_param(const char* plugin, int j, const char** name, int* type, float* lower, float* upper,
+                    float* defval);
+int lg_register_plugin(const lg_plugin_desc* desc);
+
+int lg_quad_rule_count(void);
+/* Rule i: name, point count and (if non-NULL) abscissae (size x 2), value
+ * weights and error weights, on the unit pixel [-0.5, 0.5]^2. */
+int lg_quad_rule_info(int i, const char** name, int* size, double* absc, double* weig, double* errw);
+
+/* Weights: weight_map if given, else gain / (image + offset) with a gain map
+ * or a constant gain; then times xweight; then zero where mask != 0
+ * (src/lensed.c:436-486, src/data.c:314-330).  Returns the number of
+ * zero-weight (masked) pixels, or a negative status. */
+long lg_make_weight(const float* image, long n, const float* weight_map, const float* gain, double gain_value,
+                    double offset, const float* xweight, const int* mask, float* weight_out);
+
+/* Compose and compile the program for a model without creating a context or
+ * touching a GPU (configuration check; usable on machines without a GPU). */
+int lg_compile_check(const lg_image_desc* image, const lg_object_desc* objs, int nobjs, const lg_options* opts,
+                     char* log, size_t log_size);
+
+/* ---------------------------------------------------------------- context */
+/* Replaces get_lensed_cl (src/opencl.c:128-191) + main_program
+ * (src/kernel.c:838-879) + the buffer and work-size set-up of
+ * src/lensed.c:652-1112. */
+lg_ctx* lg_create(const lg_image_desc* image, const lg_object_desc* objs, int nobjs, const lg_options* opts,
+                  int* status);
+void lg_destroy(lg_ctx* ctx);
+const char* lg_last_error(const lg_ctx* ctx);
+
+int lg_npars(const lg_ctx* ctx); /* all parameters */
+int lg_ndims(const lg_ctx* ctx); /* free parameters (the sampler's cube) */
+/* Parameter i in map order: id "<obj>.<par>", whether it wraps, its bounds. */
+int lg_param(const lg_ctx* ctx, int i, const char** id, int* wrap, double* lower, double* upper);
+/* Index in object order of the parameter at map position i. */
+int lg_pmap(const lg_ctx* ctx, int i);
+/* Number of pixels with zero weight (for chi^2 per degree of freedom). */
+long lg_masked(const lg_ctx* ctx);
+
+/* Evaluate logL = -chi^2/2 for B parameter vectors (B x npars doubles in map
+ * order, host memory) into logL[B] (host).  Replaces one call of the
+ * reference's loglike() per vector (src/nested.c:63-115): parameter upload,
+ * set_params, render, convolve, chi^2 and its sum.  B <= max_batch. */
+int lg_eval_batch(lg_ctx* ctx, const double* params, int B, double* logL);
+
+/* Same with device pointers on a caller stream (NULL = the context's
+ * stream); returns without synchronising. */
+int lg_eval_batch_device(lg_ctx* ctx, const double* d_params, int B, double* d_logL, void* stream);
+
+/* Unit-cube points (B x ndims, host) -> physical parameters via the priors
+ * (written to phys, B x npars, if not NULL) and logL[B].  Points whose prior
+ * transform leaves the parameter bounds get logL = -inf and phys NaN. */
+int lg_eval_cube_batch(lg_ctx* ctx, const double* cube, int B, double* phys, double* logL);
+
+/* Render one parameter vector (map order) for output: the model (convolved
+ * if there is a PSF), the unconvolved model and the quadrature error
+ * estimate (src/nested.c:175-216).  Any output may be NULL. */
+int lg_render(lg_ctx* ctx, const double* params, float* model, float* raw, float* error);
+
+/* Drop-in for the reference's likelihood callback (src/nested.h:3): ctx is
+ * an lg_ctx*.  cube[0..ndim) holds unit-cube values and is overwritten with
+ * the physical values of all npar parameters (map order); *lnew receives
+ * logL.  On failure *lnew is -inf and lg_last_error() says why. */
+void loglike(double cube[], int* ndim, int* npar, double* lnew, void* ctx);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif /* LENSED_GB300_H */

@@ -1,0 +1,304 @@
+"""lensed_gb300: GB300-native likelihood path of the strong-lensing code Lensed.
+
+The product is the C-ABI library ``liblensed_gb300.so`` (declared in
+``include/lensed_gb300.h``); this module is a thin ctypes binding to it for
+Python callers and tests.  There is no Python or CPU fallback: if the library
+is missing, importing the binding raises.
+
+Typical use::
+
+    import lensed_gb300 as lg
+    ctx = lg.Context(image, weight, objects=[("lens", "sie_plus_shear", priors),
+                                             ("src", "sersic", priors)],
+                     psf=psf, rule="sub5", max_batch=1024)
+    logL = ctx.eval_batch(params)        # (B, npars) physical values, map order
+"""
+from __future__ import annotations
+
+import ctypes as C
+import os
+from typing import Optional, Sequence
+
+import numpy as np
+
+__all__ = ["Context", "LensedError", "lib", "plugins", "plugin_params", "quad_rules", "make_weight",
+           "compile_check", "LIB_PATH"]
+
+LIB_PATH = os.path.join(os.path.dirname(os.path.abspath(__file__)), "liblensed_gb300.so")
+
+LG_OK = 0
+STATUS = {-1: "input", -2: "compile", -3: "cuda", -4: "alloc", -5: "timeout", -6: "unsupported"}
+LG_FLAG_STRICT_FP = 1
+LG_FLAG_NO_GRAPH = 2
+
+
+class LensedError(RuntimeError):
+    def __init__(self, code: int, msg: str):
+        super().__init__(f"[{STATUS.get(code, code)}] {msg}")
+        self.code = code
+
+
+class _ImageDesc(C.Structure):
+    _fields_ = [("width", C.c_int), ("height", C.c_int), ("image", C.POINTER(C.c_float)),
+                ("weight", C.POINTER(C.c_float)), ("psf", C.POINTER(C.c_float)), ("psf_width", C.c_int),
+                ("psf_height", C.c_int), ("pcs", C.c_double * 4)]
+
+
+class _ObjectDesc(C.Structure):
+    _fields_ = [("name", C.c_char_p), ("id", C.c_char_p), ("priors", C.POINTER(C.c_char_p))]
+
+
+class _Options(C.Structure):
+    _fields_ = [("rule", C.c_char_p), ("device", C.c_int), ("max_batch", C.c_int), ("flags", C.c_int)]
+
+
+_lib = None
+
+
+def lib():
+    """Load the native library (raises if it has not been built)."""
+    global _lib
+    if _lib is not None:
+        return _lib
+    if not os.path.exists(LIB_PATH):
+        raise ImportError(f"{LIB_PATH} is missing: run `python -c 'import __graft_entry__ as g; g.build()'`")
+    L = C.CDLL(LIB_PATH)
+    dp, fp, ip, vp = C.POINTER(C.c_double), C.POINTER(C.c_float), C.POINTER(C.c_int), C.c_void_p
+    sig = {
+        "lg_version": (C.c_char_p, []),
+        "lg_plugin_count": (C.c_int, []),
+        "lg_plugin_info": (C.c_int, [C.c_int, C.POINTER(C.c_char_p), ip, ip]),
+        "lg_plugin_param": (C.c_int, [C.c_char_p, C.c_int, C.POINTER(C.c_char_p), ip, fp, fp, fp]),
+        "lg_quad_rule_count": (C.c_int, []),
+        "lg_quad_rule_info": (C.c_int, [C.c_int, C.POINTER(C.c_char_p), ip, dp, dp, dp]),
+        "lg_make_weight": (C.c_long, [fp, C.c_long, fp, fp, C.c_double, C.c_double, fp, ip, fp]),
+        "lg_compile_check": (C.c_int, [C.POINTER(_ImageDesc), C.POINTER(_ObjectDesc), C.c_int,
+                                       C.POINTER(_Options), C.c_char_p, C.c_size_t]),
+        "lg_create": (vp, [C.POINTER(_ImageDesc), C.POINTER(_ObjectDesc), C.c_int, C.POINTER(_Options), ip]),
+        "lg_destroy": (None, [vp]),
+        "lg_last_error": (C.c_char_p, [vp]),
+        "lg_npars": (C.c_int, [vp]),
+        "lg_ndims": (C.c_int, [vp]),
+        "lg_masked": (C.c_long, [vp]),
+        "lg_pmap": (C.c_int, [vp, C.c_int]),
+        "lg_param": (C.c_int, [vp, C.c_int, C.POINTER(C.c_char_p), ip, dp, dp]),
+        "lg_eval_batch": (C.c_int, [vp, dp, C.c_int, dp]),
+        "lg_eval_batch_device": (C.c_int, [vp, vp, C.c_int, vp, vp]),
+        "lg_eval_cube_batch": (C.c_int, [vp, dp, C.c_int, dp, dp]),
+        "lg_render": (C.c_int, [vp, dp, fp, fp, fp]),
+        "loglike": (None, [dp, ip, ip, dp, vp]),
+    }
+    for name, (res, args) in sig.items():
+        f = getattr(L, name)
+        f.restype = res
+        f.argtypes = args
+    _lib = L
+    return L
+
+
+def _f32(a):
+    return None if a is None else np.ascontiguousarray(a, dtype=np.float32)
+
+
+def _p(a, t):
+    return None if a is None else a.ctypes.data_as(C.POINTER(t))
+
+
+def plugins():
+    """List of (name, kind, npars) of the registered object plugins."""
+    L = lib()
+    out = []
+    for i in range(L.lg_plugin_count()):
+        n, k, p = C.c_char_p(), C.c_int(), C.c_int()
+        L.lg_plugin_info(i, C.byref(n), C.byref(k), C.byref(p))
+        out.append((n.value.decode(), chr(k.value), p.value))
+    return out
+
+
+def plugin_params(name: str):
+    """Parameters of a plugin: list of (name, type, lower, upper, default)."""
+    L = lib()
+    out = []
+    j = 0
+    while True:
+        n, t, lo, hi, dv = C.c_char_p(), C.c_int(), C.c_float(), C.c_float(), C.c_float()
+        if L.lg_plugin_param(name.encode(), j, C.byref(n), C.byref(t), C.byref(lo), C.byref(hi), C.byref(dv)):
+            break
+        out.append((n.value.decode(), t.value, lo.value, hi.value, dv.value))
+        j += 1
+    if not out:
+        raise ValueError(f"unknown object: {name}")
+    return out
+
+
+def quad_rules():
+    """Dict name -> (absc (n,2), weights (n,), errors (n,)) from the library."""
+    L = lib()
+    out = {}
+    for i in range(L.lg_quad_rule_count()):
+        n, s = C.c_char_p(), C.c_int()
+        L.lg_quad_rule_info(i, C.byref(n), C.byref(s), None, None, None)
+        a = np.zeros((s.value, 2)); w = np.zeros(s.value); e = np.zeros(s.value)
+        L.lg_quad_rule_info(i, None, None, _p(a, C.c_double), _p(w, C.c_double), _p(e, C.c_double))
+        out[n.value.decode()] = (a, w, e)
+    return out
+
+
+def make_weight(image, weight_map=None, gain=None, gain_value=1.0, offset=0.0, xweight=None, mask=None):
+    """Weights as Lensed builds them; returns (weight, masked_count)."""
+    img = _f32(image)
+    out = np.zeros_like(img)
+    m = None if mask is None else np.ascontiguousarray(mask, dtype=np.int32)
+    wm, g, xw = _f32(weight_map), _f32(gain), _f32(xweight)
+    n = lib().lg_make_weight(_p(img, C.c_float), img.size, _p(wm, C.c_float), _p(g, C.c_float), float(gain_value),
+                             float(offset), _p(xw, C.c_float), _p(m, C.c_int), _p(out, C.c_float))
+    if n < 0:
+        raise LensedError(int(n), "make_weight")
+    return out, int(n)
+
+
+def _objects(objects):
+    """objects: sequence of plugin names, (id, name) or (id, name, priors)."""
+    keep = []
+    arr = (_ObjectDesc * len(objects))()
+    for i, o in enumerate(objects):
+        if isinstance(o, str):
+            oid, name, pri = None, o, None
+        elif len(o) == 2:
+            (oid, name), pri = o, None
+        else:
+            oid, name, pri = o
+        arr[i].name = name.encode()
+        arr[i].id = oid.encode() if oid else None
+        if pri is not None:
+            if isinstance(pri, dict):
+                pnames = [p[0] for p in plugin_params(name)]
+                pri = [pri.get(pn) for pn in pnames]
+            pa = (C.c_char_p * len(pri))(*[(None if v is None else str(v).encode()) for v in pri])
+            keep.append(pa)
+            arr[i].priors = C.cast(pa, C.POINTER(C.c_char_p))
+    return arr, keep
+
+
+def _image_desc(width, height, image, weight, psf, pcs):
+    d = _ImageDesc()
+    d.width, d.height = int(width), int(height)
+    d.image = _p(image, C.c_float)
+    d.weight = _p(weight, C.c_float)
+    if psf is not None:
+        d.psf = _p(psf, C.c_float)
+        d.psf_height, d.psf_width = psf.shape
+    if pcs is not None:
+        for i in range(4):
+            d.pcs[i] = float(pcs[i])
+    return d
+
+
+def _options(rule, device, max_batch, flags):
+    o = _Options()
+    o.rule = rule.encode() if rule else None
+    o.device, o.max_batch, o.flags = int(device), int(max_batch), int(flags)
+    return o
+
+
+def compile_check(width, height, objects, psf=None, rule="g3k7", pcs=None, flags=0):
+    """Compose and compile a model with NVRTC without a GPU; returns the log."""
+    psf_a = _f32(psf)
+    arr, keep = _objects(objects)
+    d = _image_desc(width, height, None, None, psf_a, pcs)
+    buf = C.create_string_buffer(1 << 16)
+    rc = lib().lg_compile_check(C.byref(d), arr, len(objects), C.byref(_options(rule, 0, 0, flags)), buf, len(buf))
+    if rc:
+        raise LensedError(rc, buf.value.decode(errors="replace"))
+    return buf.value.decode(errors="replace")
+
+
+class Context:
+    """One lens system resident on a GPU (wraps lg_create/lg_eval_batch)."""
+
+    def __init__(self, image, weight, objects: Sequence, psf=None, rule: str = "g3k7", pcs=None,
+                 device: int = 0, max_batch: int = 1024, flags: int = 0):
+        L = lib()
+        self._image = _f32(image)
+        self._weight = _f32(weight)
+        self._psf = _f32(psf)
+        h, w = self._image.shape
+        arr, keep = _objects(objects)
+        d = _image_desc(w, h, self._image, self._weight, self._psf, pcs)
+        st = C.c_int()
+        self.h = L.lg_create(C.byref(d), arr, len(objects), C.byref(_options(rule, device, max_batch, flags)),
+                             C.byref(st))
+        if not self.h:
+            raise LensedError(st.value, L.lg_last_error(None).decode(errors="replace"))
+        self.width, self.height = w, h
+        self.npars = L.lg_npars(self.h)
+        self.ndims = L.lg_ndims(self.h)
+        self.max_batch = max_batch
+        self.pmap = [L.lg_pmap(self.h, i) for i in range(self.npars)]
+        self.ids = []
+        for i in range(self.npars):
+            s = C.c_char_p()
+            L.lg_param(self.h, i, C.byref(s), None, None, None)
+            self.ids.append(s.value.decode())
+
+    def close(self):
+        if getattr(self, "h", None):
+            lib().lg_destroy(self.h)
+            self.h = None
+
+    def __del__(self):
+        self.close()
+
+    def _check(self, rc):
+        if rc:
+            raise LensedError(rc, lib().lg_last_error(self.h).decode(errors="replace"))
+
+    @property
+    def masked(self) -> int:
+        return lib().lg_masked(self.h)
+
+    def to_map_order(self, params_obj):
+        """Reorder (..., npars) parameters from object order to map order."""
+        p = np.asarray(params_obj, dtype=np.float64)
+        return p[..., self.pmap]
+
+    def eval_batch(self, params) -> np.ndarray:
+        p = np.ascontiguousarray(np.atleast_2d(params), dtype=np.float64)
+        if p.shape[1] != self.npars:
+            raise ValueError(f"expected {self.npars} parameters, got {p.shape[1]}")
+        out = np.empty(p.shape[0])
+        for b0 in range(0, p.shape[0], self.max_batch):
+            blk = np.ascontiguousarray(p[b0:b0 + self.max_batch])
+            self._check(lib().lg_eval_batch(self.h, _p(blk, C.c_double), blk.shape[0],
+                                            out[b0:b0 + blk.shape[0]].ctypes.data_as(C.POINTER(C.c_double))))
+        return out
+
+    def eval_batch_device(self, d_params: int, B: int, d_logL: int, stream: int = 0) -> None:
+        """Device-pointer variant (e.g. torch tensors' data_ptr()); asynchronous."""
+        self._check(lib().lg_eval_batch_device(self.h, C.c_void_p(d_params), int(B), C.c_void_p(d_logL),
+                                               C.c_void_p(stream) if stream else None))
+
+    def eval_cube(self, cube):
+        u = np.ascontiguousarray(np.atleast_2d(cube), dtype=np.float64)
+        phys = np.empty((u.shape[0], self.npars))
+        out = np.empty(u.shape[0])
+        self._check(lib().lg_eval_cube_batch(self.h, _p(u, C.c_double), u.shape[0], _p(phys, C.c_double),
+                                             _p(out, C.c_double)))
+        return out, phys
+
+    def render(self, params):
+        """(model, raw, error) images for one parameter vector (map order)."""
+        p = np.ascontiguousarray(params, dtype=np.float64)
+        shp = (self.height, self.width)
+        m, r, e = np.empty(shp, np.float32), np.empty(shp, np.float32), np.empty(shp, np.float32)
+        self._check(lib().lg_render(self.h, _p(p, C.c_double), _p(m, C.c_float), _p(r, C.c_float),
+                                    _p(e, C.c_float)))
+        return m, r, e
+
+    def loglike(self, cube):
+        """The reference callback signature: returns (logL, physical params)."""
+        c = np.zeros(self.npars)
+        c[: self.ndims] = cube
+        nd, npar, lnew = C.c_int(self.ndims), C.c_int(self.npars), C.c_double()
+        lib().loglike(_p(c, C.c_double), C.byref(nd), C.byref(npar), C.byref(lnew), C.c_void_p(self.h))
+        return lnew.value, c

@@ -1,0 +1,603 @@
+// Context management, launches and the C ABI of liblensed_gb300.
+//
+// One context = one lens system resident on one GPU (image, weight, PSF,
+// quadrature and the composed program), with scratch sized for max_batch
+// candidates.  An evaluation of B candidates is four launches on the
+// context's stream -- set_params, render, convolve+chi^2 (PSF only), finish
+// -- captured once per B into a CUDA graph together with the parameter
+// upload and the logL read-back, then replayed.  This replaces, per
+// candidate, the reference's map/unmap of the parameter buffer, four OpenCL
+// enqueues, a blocking read of N floats and a host double loop
+// (src/nested.c:63-115).
+
+#include <cuda.h>
+#include <cuda_runtime.h>
+
+#include <cmath>
+#include <cstdio>
+#include <cstring>
+#include <map>
+#include <mutex>
+#include <string>
+#include <vector>
+
+#include "lg_internal.h"
+
+namespace {
+
+// Driver API entry points, resolved through the runtime so the library loads
+// on machines without a CUDA driver (the compile check needs no GPU).
+struct Driver {
+    CUresult (*moduleLoadData)(CUmodule*, const void*) = nullptr;
+    CUresult (*moduleUnload)(CUmodule) = nullptr;
+    CUresult (*moduleGetFunction)(CUfunction*, CUmodule, const char*) = nullptr;
+    CUresult (*moduleGetGlobal)(CUdeviceptr*, size_t*, CUmodule, const char*) = nullptr;
+    CUresult (*funcSetAttribute)(CUfunction, CUfunction_attribute, int) = nullptr;
+    CUresult (*launchKernel)(CUfunction, unsigned, unsigned, unsigned, unsigned, unsigned, unsigned, unsigned,
+                             CUstream, void**, void**) = nullptr;
+    bool ok = false;
+};
+
+std::mutex g_drv_mu;
+Driver g_drv;
+
+template <class F>
+bool resolve(const char* name, F& f)
+{
+    void* p = nullptr;
+    cudaDriverEntryPointQueryResult q;
+    if (cudaGetDriverEntryPointByVersion(name, &p, 12000, cudaEnableDefault, &q) != cudaSuccess ||
+        q != cudaDriverEntryPointSuccess || !p)
+        return false;
+    f = reinterpret_cast<F>(p);
+    return true;
+}
+
+const Driver* driver()
+{
+    std::lock_guard<std::mutex> lk(g_drv_mu);
+    if (!g_drv.ok) {
+        Driver d;
+        bool ok = resolve("cuModuleLoadData", d.moduleLoadData) && resolve("cuModuleUnload", d.moduleUnload) &&
+                  resolve("cuModuleGetFunction", d.moduleGetFunction) &&
+                  resolve("cuModuleGetGlobal", d.moduleGetGlobal) &&
+                  resolve("cuFuncSetAttribute", d.funcSetAttribute) && resolve("cuLaunchKernel", d.launchKernel);
+        if (!ok) return nullptr;
+        d.ok = true;
+        g_drv = d;
+    }
+    return &g_drv;
+}
+
+thread_local std::string g_create_error;
+
+}  // namespace
+
+struct lg_ctx {
+    lg::Model model;
+    lg::Shape shape;
+    int flags = 0;
+    int device = 0;
+    int max_batch = 1024;
+    long N = 0;
+    long masked = 0;
+    bool psf = false;
+    std::string err;
+
+    const Driver* drv = nullptr;
+    CUmodule mod = nullptr;
+    CUfunction f_setp = nullptr, f_rraw = nullptr, f_rchi2 = nullptr, f_rdump = nullptr;
+    CUfunction f_cchi2 = nullptr, f_cdump = nullptr, f_finish = nullptr;
+    size_t model_bytes = 0;
+    int rtiles = 0, ctiles = 0, ctiles_x = 0, ctiles_y = 0, cthreads = 0, csmem = 0;
+
+    cudaStream_t stream = nullptr;
+    float* d_image = nullptr;
+    float* d_weight = nullptr;
+    void* d_models = nullptr;
+    float* d_raw = nullptr;
+    double* d_partials = nullptr;
+    double* d_params = nullptr;
+    double* d_logL = nullptr;
+    float* d_model_out = nullptr;
+    float* d_err_out = nullptr;
+    double* h_params = nullptr;  // pinned staging
+    double* h_logL = nullptr;
+    std::map<int, cudaGraphExec_t> graphs;
+
+    int fail(int code, const std::string& msg)
+    {
+        err = msg;
+        return code;
+    }
+    int cuda(cudaError_t e, const char* what)
+    {
+        if (e == cudaSuccess) return LG_OK;
+        err = std::string(what) + ": " + cudaGetErrorString(e);
+        return LG_ERR_CUDA;
+    }
+    int drvcall(CUresult r, const char* what)
+    {
+        if (r == CUDA_SUCCESS) return LG_OK;
+        err = std::string(what) + ": CUDA driver error " + std::to_string((int)r);
+        return LG_ERR_CUDA;
+    }
+    int launch(CUfunction f, dim3 g, dim3 b, unsigned smem, cudaStream_t s, void** args, const char* what)
+    {
+        return drvcall(drv->launchKernel(f, g.x, g.y, g.z, b.x, b.y, b.z, smem, (CUstream)s, args, nullptr), what);
+    }
+
+    // Enqueue set_params .. finish for B candidates; params and logL are
+    // device pointers.
+    int enqueue(int B, const double* params, double* logL, cudaStream_t s)
+    {
+        int rc;
+        void* a_setp[] = {&params, &B, &d_models};
+        if ((rc = launch(f_setp, dim3((B + 127) / 128), dim3(128), 0, s, a_setp, "set_params"))) return rc;
+        if (psf) {
+            void* a_r[] = {&d_models, &d_raw};
+            if ((rc = launch(f_rraw, dim3(rtiles, B), dim3(shape.rt), 0, s, a_r, "render"))) return rc;
+            void* a_c[] = {&d_raw, &d_image, &d_weight, &d_partials};
+            if ((rc = launch(f_cchi2, dim3(ctiles_x, ctiles_y, B), dim3(shape.ctx / shape.cr, shape.cty), csmem, s,
+                             a_c, "convolve")))
+                return rc;
+            void* a_f[] = {&d_partials, &ctiles, &logL};
+            return launch(f_finish, dim3(B), dim3(256), 0, s, a_f, "finish");
+        }
+        void* a_r[] = {&d_models, &d_image, &d_weight, &d_partials};
+        if ((rc = launch(f_rchi2, dim3(rtiles, B), dim3(shape.rt), 0, s, a_r, "render"))) return rc;
+        void* a_f[] = {&d_partials, &rtiles, &logL};
+        return launch(f_finish, dim3(B), dim3(256), 0, s, a_f, "finish");
+    }
+
+    void release()
+    {
+        for (auto& g : graphs) cudaGraphExecDestroy(g.second);
+        graphs.clear();
+        cudaFree(d_image);
+        cudaFree(d_weight);
+        cudaFree(d_models);
+        cudaFree(d_raw);
+        cudaFree(d_partials);
+        cudaFree(d_params);
+        cudaFree(d_logL);
+        cudaFree(d_model_out);
+        cudaFree(d_err_out);
+        cudaFreeHost(h_params);
+        cudaFreeHost(h_logL);
+        if (mod && drv) drv->moduleUnload(mod);
+        if (stream) cudaStreamDestroy(stream);
+        mod = nullptr;
+        stream = nullptr;
+    }
+};
+
+namespace {
+
+// Launch shape for a model (tile sizes chosen for GB300; see the design
+// notes for the measurements behind them).
+lg::Shape choose_shape(const lg::Model& m)
+{
+    lg::Shape s;
+    if (!m.psf.empty() && m.psfw + 8 > 64) s.cr = 8;
+    return s;
+}
+
+void shape_sizes(const lg::Shape& s, const lg::Model& m, lg_ctx* c)
+{
+    const long N = (long)m.width * m.height;
+    const int rtile = s.rt * s.rppt;
+    c->rtiles = (int)((N + rtile - 1) / rtile);
+    if (!m.psf.empty()) {
+        const int win4 = (s.cr + m.psfw - 1 + 3) / 4 * 4;
+        const int need = s.ctx - s.cr + win4;
+        const int twp = ((need + 27) / 32) * 32 + 4;
+        const int th = s.cty + m.psfh - 1;
+        c->cthreads = (s.ctx / s.cr) * s.cty;
+        c->ctiles_x = (m.width + s.ctx - 1) / s.ctx;
+        c->ctiles_y = (m.height + s.cty - 1) / s.cty;
+        c->ctiles = c->ctiles_x * c->ctiles_y;
+        c->csmem = th * twp * 4;
+    }
+}
+
+int create_impl(lg_ctx* c, const lg_image_desc* img, const lg_object_desc* objs, int nobjs, const lg_options* opts)
+{
+    int rc = lg::build_model(img, objs, nobjs, opts, c->model, c->err);
+    if (rc) return rc;
+    const lg::Model& m = c->model;
+    c->flags = opts ? opts->flags : 0;
+    c->device = opts ? opts->device : 0;
+    c->max_batch = (opts && opts->max_batch > 0) ? opts->max_batch : 1024;
+    if (c->max_batch > 65535) return c->fail(LG_ERR_INPUT, "max_batch above 65535");
+    if (!img->image) return c->fail(LG_ERR_INPUT, "image is required");
+    if (!img->weight) return c->fail(LG_ERR_INPUT, "weight is required (see lg_make_weight)");
+    c->N = (long)m.width * m.height;
+    c->psf = !m.psf.empty();
+    for (long k = 0; k < c->N; ++k)
+        if (img->weight[k] == 0) c->masked++;
+
+    // compose and compile the program (the reference's clBuildProgram,
+    // src/lensed.c:706-776)
+    c->shape = choose_shape(m);
+    shape_sizes(c->shape, m, c);
+    const bool strict = (c->flags & LG_FLAG_STRICT_FP) != 0;
+    std::string src = lg::compose_source(m, c->shape, strict), log;
+    std::vector<char> cubin;
+    if ((rc = lg::compile_program(src, strict, cubin, log))) return c->fail(rc, log);
+
+    if ((rc = c->cuda(cudaSetDevice(c->device), "cudaSetDevice"))) return rc;
+    if ((rc = c->cuda(cudaFree(nullptr), "CUDA context"))) return rc;
+    c->drv = driver();
+    if (!c->drv) return c->fail(LG_ERR_CUDA, "CUDA driver entry points unavailable");
+    if ((rc = c->drvcall(c->drv->moduleLoadData(&c->mod, cubin.data()), "cuModuleLoadData"))) return rc;
+    struct {
+        CUfunction* f;
+        const char* n;
+        bool need;
+    } fns[] = {{&c->f_setp, "lg_set_params_kernel", true}, {&c->f_rraw, "lg_render_raw", true},
+               {&c->f_rchi2, "lg_render_chi2", true},      {&c->f_rdump, "lg_render_dump", true},
+               {&c->f_finish, "lg_finish", true},          {&c->f_cchi2, "lg_conv_chi2", c->psf},
+               {&c->f_cdump, "lg_conv_dump", c->psf}};
+    for (auto& f : fns)
+        if (f.need && (rc = c->drvcall(c->drv->moduleGetFunction(f.f, c->mod, f.n), f.n))) return rc;
+    CUdeviceptr gp;
+    size_t gb;
+    if ((rc = c->drvcall(c->drv->moduleGetGlobal(&gp, &gb, c->mod, "lg_model_bytes"), "lg_model_bytes"))) return rc;
+    unsigned mb = 0;
+    if ((rc = c->cuda(cudaMemcpy(&mb, (void*)gp, sizeof mb, cudaMemcpyDeviceToHost), "model size"))) return rc;
+    c->model_bytes = mb;
+    if (c->psf && c->csmem > 48 * 1024)
+        if ((rc = c->drvcall(c->drv->funcSetAttribute(c->f_cchi2, CU_FUNC_ATTRIBUTE_MAX_DYNAMIC_SHARED_SIZE_BYTES,
+                                                      c->csmem),
+                             "convolve smem")) ||
+            (rc = c->drvcall(c->drv->funcSetAttribute(c->f_cdump, CU_FUNC_ATTRIBUTE_MAX_DYNAMIC_SHARED_SIZE_BYTES,
+                                                      c->csmem),
+                             "convolve smem")))
+            return rc;
+
+    if ((rc = c->cuda(cudaStreamCreateWithFlags(&c->stream, cudaStreamNonBlocking), "stream"))) return rc;
+    const size_t B = (size_t)c->max_batch, N = (size_t)c->N, np = m.pars.size();
+    const size_t ntiles = (size_t)(c->psf ? c->ctiles : c->rtiles);
+    auto alloc = [&](void** p, size_t bytes, const char* what) {
+        cudaError_t e = cudaMalloc(p, bytes);
+        if (e != cudaSuccess) {
+            c->err = std::string("cudaMalloc ") + what + ": " + cudaGetErrorString(e);
+            return LG_ERR_ALLOC;
+        }
+        return LG_OK;
+    };
+    if ((rc = alloc((void**)&c->d_image, N * 4, "image")) || (rc = alloc((void**)&c->d_weight, N * 4, "weight")) ||
+        (rc = alloc(&c->d_models, B * c->model_bytes, "models")) ||
+        (rc = alloc((void**)&c->d_partials, B * ntiles * 8, "partials")) ||
+        (rc = alloc((void**)&c->d_params, B * np * 8, "params")) ||
+        (rc = alloc((void**)&c->d_logL, B * 8, "logL")))
+        return rc;
+    if (c->psf && (rc = alloc((void**)&c->d_raw, B * N * 4, "raw model"))) return rc;
+    if ((rc = c->cuda(cudaMallocHost((void**)&c->h_params, B * np * 8), "pinned params")) ||
+        (rc = c->cuda(cudaMallocHost((void**)&c->h_logL, B * 8), "pinned logL")))
+        return rc;
+    if ((rc = c->cuda(cudaMemcpy(c->d_image, img->image, N * 4, cudaMemcpyHostToDevice), "upload image")) ||
+        (rc = c->cuda(cudaMemcpy(c->d_weight, img->weight, N * 4, cudaMemcpyHostToDevice), "upload weight")))
+        return rc;
+    return LG_OK;
+}
+
+// Graph of upload + evaluation + read-back for B candidates, built on first
+// use and replayed afterwards.
+int graph_for(lg_ctx* c, int B, cudaGraphExec_t* out)
+{
+    auto it = c->graphs.find(B);
+    if (it != c->graphs.end()) {
+        *out = it->second;
+        return LG_OK;
+    }
+    const size_t np = c->model.pars.size();
+    int rc;
+    cudaGraph_t g;
+    if ((rc = c->cuda(cudaStreamBeginCapture(c->stream, cudaStreamCaptureModeThreadLocal), "begin capture")))
+        return rc;
+    int erc = c->cuda(cudaMemcpyAsync(c->d_params, c->h_params, B * np * 8, cudaMemcpyHostToDevice, c->stream),
+                      "params upload");
+    if (!erc) erc = c->enqueue(B, c->d_params, c->d_logL, c->stream);
+    if (!erc)
+        erc = c->cuda(cudaMemcpyAsync(c->h_logL, c->d_logL, B * 8, cudaMemcpyDeviceToHost, c->stream), "logL read");
+    cudaError_t e = cudaStreamEndCapture(c->stream, &g);
+    if (erc) return erc;
+    if ((rc = c->cuda(e, "end capture"))) return rc;
+    cudaGraphExec_t ge;
+    e = cudaGraphInstantiate(&ge, g, 0);
+    cudaGraphDestroy(g);
+    if ((rc = c->cuda(e, "graph instantiate"))) return rc;
+    c->graphs[B] = ge;
+    *out = ge;
+    return LG_OK;
+}
+
+}  // namespace
+
+extern "C" {
+
+const char* lg_version(void) { return "lensed_gb300 0.1 (sm_103a)"; }
+
+int lg_plugin_count(void) { return lg::plugin_count(); }
+
+int lg_plugin_info(int i, const char** name, int* kind, int* npars)
+{
+    const lg::Plugin* p = lg::plugin_at(i);
+    if (!p) return LG_ERR_INPUT;
+    if (name) *name = p->name.c_str();
+    if (kind) *kind = p->kind;
+    if (npars) *npars = (int)p->pars.size();
+    return LG_OK;
+}
+
+int lg_plugin_param(const char* plugin, int j, const char** name, int* type, float* lower, float* upper,
+                    float* defval)
+{
+    const lg::Plugin* p = plugin ? lg::find_plugin(plugin) : nullptr;
+    if (!p || j < 0 || j >= (int)p->pars.size()) return LG_ERR_INPUT;
+    const lg::ParamDef& d = p->pars[j];
+    if (name) *name = d.name.c_str();
+    if (type) *type = d.type;
+    if (lower) *lower = d.lower;
+    if (upper) *upper = d.upper;
+    if (defval) *defval = d.defval;
+    return LG_OK;
+}
+
+int lg_register_plugin(const lg_plugin_desc* desc)
+{
+    std::string err;
+    int rc = lg::register_plugin(desc, err);
+    if (rc) g_create_error = err;
+    return rc;
+}
+
+int lg_quad_rule_count(void) { return lg::quad_rule_count(); }
+
+int lg_quad_rule_info(int i, const char** name, int* size, double* absc, double* weig, double* errw)
+{
+    const lg::QuadRuleData* r = lg::quad_rule_at(i);
+    if (!r) return LG_ERR_INPUT;
+    if (name) *name = r->name;
+    if (size) *size = r->size;
+    for (int n = 0; n < r->size; ++n) {
+        if (absc) {
+            absc[2 * n] = r->absc[n][0];
+            absc[2 * n + 1] = r->absc[n][1];
+        }
+        if (weig) weig[n] = r->weig[n];
+        if (errw) errw[n] = r->errw[n];
+    }
+    return LG_OK;
+}
+
+long lg_make_weight(const float* image, long n, const float* weight_map, const float* gain, double gain_value,
+                    double offset, const float* xweight, const int* mask, float* out)
+{
+    if (!out || n < 0 || (!weight_map && !image)) return LG_ERR_INPUT;
+    long masked = 0;
+    for (long i = 0; i < n; ++i) {
+        float w;
+        if (weight_map) w = weight_map[i];
+        else w = (float)((gain ? (double)gain[i] : (double)(float)gain_value) / ((double)image[i] + offset));
+        if (xweight) w *= xweight[i];
+        if (mask && mask[i]) w = 0;
+        out[i] = w;
+        if (w == 0) ++masked;
+    }
+    return masked;
+}
+
+int lg_compile_check(const lg_image_desc* image, const lg_object_desc* objs, int nobjs, const lg_options* opts,
+                     char* log, size_t log_size)
+{
+    lg::Model m;
+    std::string err;
+    int rc = lg::build_model(image, objs, nobjs, opts, m, err);
+    if (!rc) {
+        const bool strict = opts && (opts->flags & LG_FLAG_STRICT_FP);
+        std::vector<char> cubin;
+        lg::Shape s = choose_shape(m);
+        rc = lg::compile_program(lg::compose_source(m, s, strict), strict, cubin, err);
+    }
+    if (log && log_size) {
+        std::snprintf(log, log_size, "%s", err.c_str());
+    }
+    return rc;
+}
+
+lg_ctx* lg_create(const lg_image_desc* image, const lg_object_desc* objs, int nobjs, const lg_options* opts,
+                  int* status)
+{
+    lg_ctx* c = new (std::nothrow) lg_ctx();
+    if (!c) {
+        if (status) *status = LG_ERR_ALLOC;
+        return nullptr;
+    }
+    int rc = create_impl(c, image, objs, nobjs, opts);
+    if (status) *status = rc;
+    if (rc) {
+        g_create_error = c->err;
+        c->release();
+        delete c;
+        return nullptr;
+    }
+    return c;
+}
+
+void lg_destroy(lg_ctx* c)
+{
+    if (!c) return;
+    cudaSetDevice(c->device);
+    if (c->stream) cudaStreamSynchronize(c->stream);
+    c->release();
+    delete c;
+}
+
+const char* lg_last_error(const lg_ctx* c) { return c ? c->err.c_str() : g_create_error.c_str(); }
+
+int lg_npars(const lg_ctx* c) { return c ? (int)c->model.pars.size() : LG_ERR_INPUT; }
+int lg_ndims(const lg_ctx* c) { return c ? c->model.ndims : LG_ERR_INPUT; }
+long lg_masked(const lg_ctx* c) { return c ? c->masked : LG_ERR_INPUT; }
+
+int lg_pmap(const lg_ctx* c, int i)
+{
+    if (!c || i < 0 || i >= (int)c->model.pmap.size()) return LG_ERR_INPUT;
+    return c->model.pmap[i];
+}
+
+int lg_param(const lg_ctx* c, int i, const char** id, int* wrap, double* lower, double* upper)
+{
+    if (!c || i < 0 || i >= (int)c->model.pmap.size()) return LG_ERR_INPUT;
+    const lg::ParamInfo& p = c->model.pars[c->model.pmap[i]];
+    if (id) *id = p.id.c_str();
+    if (wrap) *wrap = p.prior.wrap;
+    if (lower) *lower = p.has_prior ? p.prior.lower() : -HUGE_VAL;
+    if (upper) *upper = p.has_prior ? p.prior.upper() : HUGE_VAL;
+    return LG_OK;
+}
+
+int lg_eval_batch(lg_ctx* c, const double* params, int B, double* logL)
+{
+    if (!c || !params || !logL || B < 0) return LG_ERR_INPUT;
+    if (B == 0) return LG_OK;
+    if (B > c->max_batch) return c->fail(LG_ERR_INPUT, "batch larger than max_batch");
+    int rc;
+    if ((rc = c->cuda(cudaSetDevice(c->device), "cudaSetDevice"))) return rc;
+    const size_t np = c->model.pars.size();
+    std::memcpy(c->h_params, params, (size_t)B * np * 8);
+    if (c->flags & LG_FLAG_NO_GRAPH) {
+        if ((rc = c->cuda(cudaMemcpyAsync(c->d_params, c->h_params, (size_t)B * np * 8, cudaMemcpyHostToDevice,
+                                          c->stream),
+                          "params upload")))
+            return rc;
+        if ((rc = c->enqueue(B, c->d_params, c->d_logL, c->stream))) return rc;
+        if ((rc = c->cuda(cudaMemcpyAsync(c->h_logL, c->d_logL, (size_t)B * 8, cudaMemcpyDeviceToHost, c->stream),
+                          "logL read")))
+            return rc;
+    } else {
+        cudaGraphExec_t ge;
+        if ((rc = graph_for(c, B, &ge))) return rc;
+        if ((rc = c->cuda(cudaGraphLaunch(ge, c->stream), "graph launch"))) return rc;
+    }
+    if ((rc = c->cuda(cudaStreamSynchronize(c->stream), "evaluate"))) return rc;
+    std::memcpy(logL, c->h_logL, (size_t)B * 8);
+    return LG_OK;
+}
+
+int lg_eval_batch_device(lg_ctx* c, const double* d_params, int B, double* d_logL, void* stream)
+{
+    if (!c || !d_params || !d_logL || B < 0) return LG_ERR_INPUT;
+    if (B == 0) return LG_OK;
+    if (B > c->max_batch) return c->fail(LG_ERR_INPUT, "batch larger than max_batch");
+    int rc;
+    if ((rc = c->cuda(cudaSetDevice(c->device), "cudaSetDevice"))) return rc;
+    return c->enqueue(B, d_params, d_logL, stream ? (cudaStream_t)stream : c->stream);
+}
+
+int lg_eval_cube_batch(lg_ctx* c, const double* cube, int B, double* phys, double* logL)
+{
+    if (!c || !cube || !logL || B < 0) return LG_ERR_INPUT;
+    const lg::Model& m = c->model;
+    const int np = (int)m.pars.size(), nd = m.ndims;
+    for (int i = 0; i < np; ++i)
+        if (!m.pars[m.pmap[i]].has_prior) return c->fail(LG_ERR_INPUT, "missing prior: " + m.pars[m.pmap[i]].id);
+    std::vector<double> p((size_t)B * np);
+    std::vector<char> bad(B, 0);
+    for (int b = 0; b < B; ++b)
+        for (int i = 0; i < np; ++i) {
+            const lg::ParamInfo& par = m.pars[m.pmap[i]];
+            const double u = i < nd ? cube[(size_t)b * nd + i] : 0.5;
+            const double v = par.prior.apply(u);
+            if (par.bounded && (v < par.lower || v > par.upper)) bad[b] = 1;
+            p[(size_t)b * np + i] = v;
+        }
+    for (int b0 = 0; b0 < B; b0 += c->max_batch) {
+        const int nb = std::min(c->max_batch, B - b0);
+        int rc = lg_eval_batch(c, p.data() + (size_t)b0 * np, nb, logL + b0);
+        if (rc) return rc;
+    }
+    for (int b = 0; b < B; ++b) {
+        if (bad[b]) logL[b] = -HUGE_VAL;
+        if (phys)
+            for (int i = 0; i < np; ++i) phys[(size_t)b * np + i] = bad[b] ? NAN : p[(size_t)b * np + i];
+    }
+    return LG_OK;
+}
+
+int lg_render(lg_ctx* c, const double* params, float* model, float* raw, float* error)
+{
+    if (!c || !params) return LG_ERR_INPUT;
+    int rc;
+    if ((rc = c->cuda(cudaSetDevice(c->device), "cudaSetDevice"))) return rc;
+    const size_t N = (size_t)c->N, np = c->model.pars.size();
+    if (!c->d_model_out) {
+        if ((rc = c->cuda(cudaMalloc((void**)&c->d_model_out, N * 4), "render buffer")) ||
+            (rc = c->cuda(cudaMalloc((void**)&c->d_err_out, N * 4), "render buffer")))
+            return rc;
+    }
+    // render to d_model_out (value) and d_err_out (error), convolve the value
+    // into the raw buffer's first image when there is a PSF
+    float* d_val = c->d_model_out;
+    if ((rc = c->cuda(cudaMemcpyAsync(c->d_params, params, np * 8, cudaMemcpyHostToDevice, c->stream), "params")))
+        return rc;
+    int one = 1;
+    void* a_setp[] = {&c->d_params, &one, &c->d_models};
+    if ((rc = c->launch(c->f_setp, dim3(1), dim3(128), 0, c->stream, a_setp, "set_params"))) return rc;
+    void* a_r[] = {&c->d_models, &d_val, &c->d_err_out};
+    if ((rc = c->launch(c->f_rdump, dim3(c->rtiles, 1), dim3(c->shape.rt), 0, c->stream, a_r, "render"))) return rc;
+    if (c->psf) {
+        void* a_c[] = {&d_val, &c->d_raw};
+        if ((rc = c->launch(c->f_cdump, dim3(c->ctiles_x, c->ctiles_y, 1), dim3(c->shape.ctx / c->shape.cr, c->shape.cty),
+                            c->csmem, c->stream, a_c, "convolve")))
+            return rc;
+    }
+    if (raw && (rc = c->cuda(cudaMemcpyAsync(raw, d_val, N * 4, cudaMemcpyDeviceToHost, c->stream), "read raw")))
+        return rc;
+    if (error &&
+        (rc = c->cuda(cudaMemcpyAsync(error, c->d_err_out, N * 4, cudaMemcpyDeviceToHost, c->stream), "read error")))
+        return rc;
+    if (model && (rc = c->cuda(cudaMemcpyAsync(model, c->psf ? c->d_raw : d_val, N * 4, cudaMemcpyDeviceToHost,
+                                               c->stream),
+                               "read model")))
+        return rc;
+    return c->cuda(cudaStreamSynchronize(c->stream), "render");
+}
+
+// src/nested.c:17-131 with the arithmetic moved to the GPU.  The reference
+// redraws a parameter until it falls inside its bounds with the same unit
+// value, which never ends when the first draw is outside; here such a point
+// gets logL = -inf instead.
+void loglike(double cube[], int* ndim, int* npar, double* lnew, void* ctx)
+{
+    lg_ctx* c = static_cast<lg_ctx*>(ctx);
+    *lnew = -HUGE_VAL;
+    if (!c || !cube || !ndim || !npar) return;
+    const lg::Model& m = c->model;
+    if (*npar != (int)m.pars.size() || *ndim != m.ndims) {
+        c->err = "loglike: ndim/npar do not match the context";
+        return;
+    }
+    bool bad = false;
+    for (int i = 0; i < *npar; ++i) {
+        const lg::ParamInfo& par = m.pars[m.pmap[i]];
+        if (!par.has_prior) {
+            c->err = "missing prior: " + par.id;
+            return;
+        }
+        const double unit = i < *ndim ? cube[i] : 0.5;
+        const double phys = par.prior.apply(unit);
+        if (par.bounded && (phys < par.lower || phys > par.upper)) bad = true;
+        cube[i] = phys;
+    }
+    if (bad) {
+        c->err = "loglike: parameter outside its bounds";
+        return;
+    }
+    double l;
+    if (lg_eval_batch(c, cube, 1, &l) == LG_OK) *lnew = l;
+}
+
+}  // extern "C"

@@ -1,0 +1,110 @@
+// Internal declarations shared by the host sources of liblensed_gb300.
+#pragma once
+
+#include <string>
+#include <vector>
+
+#include "lensed_gb300.h"
+
+namespace lg {
+
+// ------------------------------------------------------------------ plugins
+struct ParamDef {
+    std::string name;
+    int type = LG_PARAMETER;
+    float lower = 0, upper = 0;
+    float defval = 0;
+};
+
+struct Plugin {
+    std::string name;
+    int kind = 0;
+    std::vector<ParamDef> pars;
+    std::string source;             // CUDA device source of the plugin
+    std::vector<std::string> deps;  // plugins whose source must come first
+};
+
+const Plugin* find_plugin(const std::string& name);
+int plugin_count();
+const Plugin* plugin_at(int i);
+int register_plugin(const lg_plugin_desc* d, std::string& err);
+
+// Device sources embedded at build time.
+const char* prelude_source();
+const char* kernels_source();
+
+// ------------------------------------------------------------------- priors
+// Lensed's prior plugins (src/prior.c:47-51): delta (pseudo), unif, norm.
+struct Prior {
+    enum Kind { NONE = 0, DELTA, UNIF, NORM } kind = NONE;
+    double a = 0, b = 0;   // delta: a = value; unif: [a, b]; norm: mean a, sigma b
+    bool wrap = false;     // "wrap" keyword
+    bool ipp = false;      // "image" keyword: image-plane prior
+    double apply(double u) const;
+    double lower() const;
+    double upper() const;
+    bool pseudo() const { return kind == DELTA; }
+};
+bool parse_prior(const char* s, Prior& p, std::string& err);
+double norm_quantile(double u);
+
+// ------------------------------------------------------------- quadrature
+struct QuadRuleData {
+    const char* name;
+    const char* info;
+    int size;
+    const double (*absc)[2];
+    const double* weig;
+    const double* errw;
+};
+const QuadRuleData* quad_rule(const char* name);
+int quad_rule_count();
+const QuadRuleData* quad_rule_at(int i);
+
+// ------------------------------------------------------------------ model
+// A parameter of the model, in object order.
+struct ParamInfo {
+    std::string id;       // "<object>.<param>"
+    int object = 0, index = 0, type = 0;
+    double lower = 0, upper = 0;
+    bool bounded = false;
+    Prior prior;
+    bool has_prior = false;
+    bool derived = false;
+};
+
+struct ObjectInfo {
+    std::string id;
+    const Plugin* plugin = nullptr;
+    int par0 = 0;         // first parameter (object order)
+    bool ipp = false;     // (x, y) carry an image-plane prior
+};
+
+struct Model {
+    std::vector<ObjectInfo> objs;
+    std::vector<ParamInfo> pars;  // object order
+    std::vector<int> pmap;        // map position -> object-order index
+    int ndims = 0;
+    int width = 0, height = 0;
+    double pcs[4] = {1, 1, 1, 1};
+    std::vector<float> psf;       // normalised
+    int psfw = 0, psfh = 0;
+    const QuadRuleData* rule = nullptr;
+};
+
+// Build the model from the C-ABI descriptions (priors, bounds, pmap, PSF
+// normalisation); no device work.
+int build_model(const lg_image_desc* img, const lg_object_desc* objs, int nobjs, const lg_options* opts,
+                Model& m, std::string& err);
+
+// Launch-shape parameters baked into the program.
+struct Shape {
+    int rt = 128, rppt = 2;        // render threads / pixels per thread
+    int ctx = 32, cty = 32, cr = 8; // convolution tile and outputs per thread
+};
+
+// Compose the NVRTC source of a model and compile it to a cubin for sm_103a.
+std::string compose_source(const Model& m, const Shape& s, bool strict);
+int compile_program(const std::string& src, bool strict, std::vector<char>& cubin, std::string& log);
+
+}  // namespace lg

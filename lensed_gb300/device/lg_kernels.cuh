@@ -1,0 +1,284 @@
+// Kernels of the composed likelihood program.  Compiled by NVRTC after the
+// prelude, the plugins and the generated model section, which defines:
+//   LG_W, LG_H, LG_N          image size (pixels)
+//   LG_Q                      quadrature points; lg_qq[], lg_ww[] (constant)
+//   LG_RX, LG_RY, LG_SX, LG_SY pixel coordinate system (after the even-PSF shift)
+//   LG_HAS_PSF, LG_PSF_W, LG_PSF_H, lg_psf[] (normalised PSF, constant)
+//   LG_NPARS, lg_model, lg_compute(), lg_set_params(), lg_load_params()
+// and the launch-shape parameters LG_RT, LG_RPPT (render) and LG_CTX, LG_CTY,
+// LG_CR (convolution).
+//
+// Data layout in HBM, per context:
+//   models   lg_model[B]              object data of each candidate
+//   raw      float[B][N]              unconvolved model (PSF path only)
+//   partials double[B][ntiles]        per-tile chi^2 partial sums
+//   logL     double[B]
+//   image, weight float[N]            resident for the context's lifetime
+//
+// The chi^2 of a pixel is w*(m-d)^2 in FP32 as in kernel/lensed.cl:41-55;
+// sums are FP64 (per thread, then a fixed-order block tree, then a
+// fixed-order sum over tiles), so results are deterministic run to run.
+
+#ifndef LG_RT
+#define LG_RT 128
+#endif
+#ifndef LG_RPPT
+#define LG_RPPT 2
+#endif
+#define LG_RTILE (LG_RT * LG_RPPT)
+#define LG_RTILES ((LG_N + LG_RTILE - 1) / LG_RTILE)
+
+// ------------------------------------------------------------ reductions --
+LG_DEV double lg_warp_sum(double v)
+{
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) v += __shfl_down_sync(0xffffffffu, v, o);
+    return v;
+}
+
+// Fixed-order block sum; the result is valid in thread 0.
+template <int NT>
+LG_DEV double lg_block_sum(double v, double* red)
+{
+    const int lane = threadIdx.x & 31, warp = (threadIdx.y * blockDim.x + threadIdx.x) >> 5;
+    v = lg_warp_sum(v);
+    if (lane == 0) red[warp] = v;
+    __syncthreads();
+    double s = 0.0;
+    if (warp == 0 && (threadIdx.y | threadIdx.x) == 0) {
+#pragma unroll
+        for (int i = 0; i < NT / 32; ++i) s += red[i];
+    }
+    return s;
+}
+
+// ------------------------------------------------------------ set_params --
+// One thread per candidate: physical parameters (pmap order, double) ->
+// object data.  src/nested.c:67-77 and the generated set_params of
+// src/kernel.c:114-150.
+extern "C" __global__ void lg_set_params_kernel(const double* __restrict__ params, int B,
+                                                lg_model* __restrict__ models)
+{
+    const int b = blockIdx.x * blockDim.x + threadIdx.x;
+    if (b >= B) return;
+    float p[LG_NPARS];
+    lg_load_params(params + (size_t)b * LG_NPARS, p);
+    lg_model m;
+    lg_set_params(m, p);
+    models[b] = m;
+}
+
+// ---------------------------------------------------------------- render --
+// kernel/lensed.cl:9-39.  Block (tile, candidate); each thread integrates
+// LG_RPPT pixels (strided by LG_RT so loads and stores coalesce) over the
+// quadrature rule.  MODE 0 stores the raw model, MODE 1 reduces the chi^2
+// directly (no PSF), MODE 2 stores value and error for one candidate.
+template <int MODE>
+LG_DEV void lg_render_tile(const lg_model* __restrict__ models, float* __restrict__ out, float* __restrict__ err,
+                           const float* __restrict__ image, const float* __restrict__ weight,
+                           double* __restrict__ partials)
+{
+    const int b = blockIdx.y;
+    const lg_model m = models[b];
+    const int base = blockIdx.x * LG_RTILE + threadIdx.x;
+    float2 xp[LG_RPPT];
+    float v[LG_RPPT], e[LG_RPPT];
+#pragma unroll
+    for (int j = 0; j < LG_RPPT; ++j) {
+        int k = base + j * LG_RT;
+        k = k < LG_N ? k : LG_N - 1;
+        xp[j] = make_float2(LG_RX + LG_SX * (float)(k % LG_W), LG_RY + LG_SY * (float)(k / LG_W));
+        v[j] = 0.0f;
+        e[j] = 0.0f;
+    }
+#pragma unroll 1
+    for (int n = 0; n < LG_Q; ++n) {
+        const float2 q = lg_qq[n];
+        const float2 w = lg_ww[n];
+#pragma unroll
+        for (int j = 0; j < LG_RPPT; ++j) {
+            const float f = lg_compute(m, xp[j] + q);
+            v[j] += w.x * f;
+            if (MODE == 2) e[j] += w.y * f;
+        }
+    }
+    if (MODE == 1) {
+        __shared__ double red[LG_RT / 32];
+        double s = 0.0;
+#pragma unroll
+        for (int j = 0; j < LG_RPPT; ++j) {
+            const int k = base + j * LG_RT;
+            if (k < LG_N) {
+                const float d = v[j] - image[k];
+                s += (double)(weight[k] * d * d);
+            }
+        }
+        s = lg_block_sum<LG_RT>(s, red);
+        if (threadIdx.x == 0) partials[(size_t)b * gridDim.x + blockIdx.x] = s;
+    } else {
+#pragma unroll
+        for (int j = 0; j < LG_RPPT; ++j) {
+            const int k = base + j * LG_RT;
+            if (k < LG_N) {
+                out[(size_t)b * LG_N + k] = v[j];
+                if (MODE == 2) err[(size_t)b * LG_N + k] = e[j];
+            }
+        }
+    }
+}
+
+extern "C" __global__ void __launch_bounds__(LG_RT) lg_render_raw(const lg_model* __restrict__ models,
+                                                                  float* __restrict__ raw)
+{
+    lg_render_tile<0>(models, raw, nullptr, nullptr, nullptr, nullptr);
+}
+
+extern "C" __global__ void __launch_bounds__(LG_RT)
+    lg_render_chi2(const lg_model* __restrict__ models, const float* __restrict__ image,
+                   const float* __restrict__ weight, double* __restrict__ partials)
+{
+    lg_render_tile<1>(models, nullptr, nullptr, image, weight, partials);
+}
+
+extern "C" __global__ void __launch_bounds__(LG_RT)
+    lg_render_dump(const lg_model* __restrict__ models, float* __restrict__ value, float* __restrict__ error)
+{
+    lg_render_tile<2>(models, value, error, nullptr, nullptr, nullptr);
+}
+
+// -------------------------------------------------------------- convolve --
+// kernel/lensed.cl:56-103: out(x, y) = sum_j sum_i psf[j][i] *
+// in(clamp(y + OY - j), clamp(x + OX - i)) with OX = PW-1-PW/2,
+// OY = PH-1-PH/2, rows j outer, columns i inner (the reference's order).
+// A block computes an LG_CTX x LG_CTY output tile from a clamped halo tile in
+// shared memory; each thread owns LG_CR consecutive outputs of one row and
+// slides a register window of LG_CR + PW - 1 inputs along each PSF row.
+#if LG_HAS_PSF
+#ifndef LG_CTX
+#define LG_CTX 32
+#endif
+#ifndef LG_CTY
+#define LG_CTY 32
+#endif
+#ifndef LG_CR
+#define LG_CR 8
+#endif
+#define LG_OX (LG_PSF_W - 1 - LG_PSF_W / 2)
+#define LG_OY (LG_PSF_H - 1 - LG_PSF_H / 2)
+#define LG_WIN4 ((LG_CR + LG_PSF_W - 1 + 3) / 4 * 4)
+#define LG_TW_NEED (LG_CTX - LG_CR + LG_WIN4)
+// row pitch = 4 (mod 32) words: the float4 loads of a quarter warp (two
+// rows of four threads) then fall in distinct banks
+#define LG_TWP (((LG_TW_NEED + 27) / 32) * 32 + 4)
+#define LG_TH (LG_CTY + LG_PSF_H - 1)
+#define LG_CTHREADS ((LG_CTX / LG_CR) * LG_CTY)
+#define LG_CTILES_X ((LG_W + LG_CTX - 1) / LG_CTX)
+#define LG_CTILES_Y ((LG_H + LG_CTY - 1) / LG_CTY)
+#define LG_CTILES (LG_CTILES_X * LG_CTILES_Y)
+#define LG_CSMEM (LG_TH * LG_TWP * 4)
+
+template <int MODE>
+LG_DEV void lg_conv_tile(const float* __restrict__ raw, float* __restrict__ out, const float* __restrict__ image,
+                         const float* __restrict__ weight, double* __restrict__ partials)
+{
+    extern __shared__ float4 lg_smem4[];
+    float* tile = reinterpret_cast<float*>(lg_smem4);
+    const int b = blockIdx.z;
+    const float* src = raw + (size_t)b * LG_N;
+    const int X0 = blockIdx.x * LG_CTX, Y0 = blockIdx.y * LG_CTY;
+    const int br = Y0 + LG_OY - (LG_PSF_H - 1), bc = X0 + LG_OX - (LG_PSF_W - 1);
+    const int tid = threadIdx.y * blockDim.x + threadIdx.x;
+    for (int i = tid; i < LG_TH * LG_TWP; i += LG_CTHREADS) {
+        const int r = i / LG_TWP, c = i - r * LG_TWP;
+        int gy = br + r, gx = bc + c;
+        gy = gy < 0 ? 0 : (gy > LG_H - 1 ? LG_H - 1 : gy);
+        gx = gx < 0 ? 0 : (gx > LG_W - 1 ? LG_W - 1 : gx);
+        tile[i] = src[gy * LG_W + gx];
+    }
+    __syncthreads();
+    const int lx0 = threadIdx.x * LG_CR, ly = threadIdx.y;
+    float acc[LG_CR];
+#pragma unroll
+    for (int o = 0; o < LG_CR; ++o) acc[o] = 0.0f;
+#pragma unroll 1
+    for (int j = 0; j < LG_PSF_H; ++j) {
+        const float4* row = reinterpret_cast<const float4*>(tile + (ly + LG_PSF_H - 1 - j) * LG_TWP + lx0);
+        float win[LG_WIN4];
+#pragma unroll
+        for (int t = 0; t < LG_WIN4 / 4; ++t) {
+            const float4 q = row[t];
+            win[4 * t + 0] = q.x;
+            win[4 * t + 1] = q.y;
+            win[4 * t + 2] = q.z;
+            win[4 * t + 3] = q.w;
+        }
+        const float* prow = lg_psf + j * LG_PSF_W;
+#pragma unroll
+        for (int i = 0; i < LG_PSF_W; ++i) {
+            const float p = prow[i];
+#pragma unroll
+            for (int o = 0; o < LG_CR; ++o) acc[o] += p * win[o + LG_PSF_W - 1 - i];
+        }
+    }
+    const int gy = Y0 + ly;
+    if (MODE == 1) {
+        __shared__ double red[LG_CTHREADS / 32];
+        double s = 0.0;
+        if (gy < LG_H) {
+#pragma unroll
+            for (int o = 0; o < LG_CR; ++o) {
+                const int gx = X0 + lx0 + o;
+                if (gx < LG_W) {
+                    const int k = gy * LG_W + gx;
+                    const float d = acc[o] - image[k];
+                    s += (double)(weight[k] * d * d);
+                }
+            }
+        }
+        s = lg_block_sum<LG_CTHREADS>(s, red);
+        if (tid == 0) partials[(size_t)b * LG_CTILES + blockIdx.y * LG_CTILES_X + blockIdx.x] = s;
+    } else if (gy < LG_H) {
+#pragma unroll
+        for (int o = 0; o < LG_CR; ++o) {
+            const int gx = X0 + lx0 + o;
+            if (gx < LG_W) out[(size_t)b * LG_N + gy * LG_W + gx] = acc[o];
+        }
+    }
+}
+
+extern "C" __global__ void __launch_bounds__(LG_CTHREADS)
+    lg_conv_chi2(const float* __restrict__ raw, const float* __restrict__ image, const float* __restrict__ weight,
+                 double* __restrict__ partials)
+{
+    lg_conv_tile<1>(raw, nullptr, image, weight, partials);
+}
+
+extern "C" __global__ void __launch_bounds__(LG_CTHREADS) lg_conv_dump(const float* __restrict__ raw,
+                                                                       float* __restrict__ out)
+{
+    lg_conv_tile<0>(raw, out, nullptr, nullptr, nullptr);
+}
+#endif
+
+// ---------------------------------------------------------------- finish --
+// logL[b] = -chi2/2 (src/nested.c:106-115) from the per-tile partials, in
+// a fixed order.
+extern "C" __global__ void __launch_bounds__(256)
+    lg_finish(const double* __restrict__ partials, int ntiles, double* __restrict__ logL)
+{
+    __shared__ double red[8];
+    const int b = blockIdx.x;
+    double s = 0.0;
+    for (int t = threadIdx.x; t < ntiles; t += 256) s += partials[(size_t)b * ntiles + t];
+    s = lg_block_sum<256>(s, red);
+    if (threadIdx.x == 0) logL[b] = -0.5 * s;
+}
+
+// Sizes the host reads back after loading the module.
+extern "C" __device__ const unsigned lg_model_bytes = sizeof(lg_model);
+extern "C" __device__ const int lg_render_tiles = LG_RTILES;
+#if LG_HAS_PSF
+extern "C" __device__ const int lg_conv_tiles = LG_CTILES;
+extern "C" __device__ const int lg_conv_smem = LG_CSMEM;
+extern "C" __device__ const int lg_conv_threads = LG_CTHREADS;
+#endif

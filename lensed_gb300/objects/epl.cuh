@@ -1,0 +1,50 @@
+// Elliptical power-law lens (Tessore & Metcalf 2015).  Parameters
+// (objects/epl.cl:5-13): x, y, r, t (2-D convergence slope, 0..2), q, pa.
+// The angular part is the ten-term recursion of the hypergeometric series;
+// the radial part is n * R^(1 - t) in the elliptical radius R.
+struct lg_data_epl {
+    float2 x;
+    mat22 m;   // rotate, make elliptical, scale by 1/r
+    mat22 w;   // rotate back
+    float t, f, n;
+};
+LG_DEV void lg_epl_setup(lg_data_epl* o, float x1, float x2, float r, float t, float q, float pa)
+{
+    float c = cosf(pa * LG_DEG2RAD);
+    float s = sinf(pa * LG_DEG2RAD);
+    o->x = make_float2(x1, x2);
+    o->m = (1 / r / sqrtf(q)) * make_mat22(q * c, q * s, -s, c);
+    o->w = make_mat22(c, -s, s, c);
+    o->t = t;
+    o->f = (1 - q) / (1 + q);
+    o->n = 2 * r * sqrtf(q) / (1 + q);
+}
+LG_DEV void lg_set_epl(lg_data_epl* o, float x1, float x2, float r, float t, float q, float pa)
+{
+    lg_epl_setup(o, x1, x2, r, t, q, pa);
+}
+// Deflection in the rotated frame for the elliptical coordinates x.
+LG_DEV float2 lg_epl_frame(const lg_data_epl* __restrict__ o, float2 x)
+{
+    const float T = 2 - o->t;
+    const float f = o->f;
+    float r = length(x);
+    float phi = atan2f(x.y, x.x);
+    float s, c, s2, c2;
+    sincosf(phi, &s, &c);
+    sincosf(2 * phi, &s2, &c2);
+    mat22 R = make_mat22(c2, -s2, s2, c2);
+    float2 A = make_float2(c, s);
+    float2 a = A;
+#pragma unroll
+    for (int k = 1; k <= 10; ++k) {
+        A = (-f * (2 * k - T) / (2 * k + T)) * mv22(R, A);
+        a += A;
+    }
+    a *= o->n * powf(r, 1 - o->t);
+    return mv22(o->w, a);
+}
+LG_DEV float2 lg_deflection_epl(const lg_data_epl* __restrict__ o, float2 x)
+{
+    return lg_epl_frame(o, mv22(o->m, x - o->x));
+}

@@ -1,0 +1,224 @@
+"""Parity of the CUDA path (through the C ABI) with the CPU oracle.
+
+Tolerances (FP32 ray-shooting, FP64 reduction):
+  * model images: relative error <= 1e-5 on pixels above 1e-6 of the peak,
+    absolute error <= 1e-6 * peak below that floor;
+  * logL: |logL_gpu - logL_oracle32| <= 1e-3;
+  * the FP32 paths' distance to the FP64 oracle is reported, not bounded
+    tighter than the FP32 budget.
+"""
+import numpy as np
+import pytest
+
+import lensed_gb300 as lg
+from lensed_gb300 import quadrature, workloads
+from oracle.oracle import Oracle
+
+pytestmark = pytest.mark.gpu
+
+IMG_REL, LOGL_ABS = 1e-5, 1e-3
+
+
+def image_err(got, want):
+    got = np.asarray(got, np.float64)
+    want = np.asarray(want, np.float64)
+    peak = np.abs(want).max()
+    big = np.abs(want) > 1e-6 * peak
+    rel = (np.abs(got - want)[big] / np.abs(want[big])).max() if big.any() else 0.0
+    small = np.abs(got - want)[~big].max() / peak if (~big).any() else 0.0
+    return rel, small
+
+
+def assert_image_close(got, want, what=""):
+    rel, small = image_err(got, want)
+    assert rel <= IMG_REL and small <= 1e-6, (what, rel, small)
+
+
+PLUGIN_CASES = [
+    (["sis", "sersic"], [20.3, 18.7, 8.0] + [21.0, 18.0, 3.0, -2.0, 1.5, 0.8, 20.0]),
+    (["sis_plus_shear", "sersic"], [20.3, 18.7, 8.0, 0.05, -0.03] + [21.0, 18.0, 3.0, -2.0, 1.5, 0.8, 20.0]),
+    (["nsis", "exponential"], [20.3, 18.7, 8.0, 1.5] + [21.0, 18.0, 3.0, -2.0, 0.8, 20.0]),
+    (["sie", "devauc"], [20.3, 18.7, 8.0, 0.7, 35.0] + [21.0, 18.0, 3.0, -2.0, 0.8, 20.0]),
+    (["sie_plus_shear", "gauss"], [20.3, 18.7, 8.0, 0.7, 35.0, 0.05, -0.03] + [21.0, 18.0, 3.0, -2.0, 0.8, 20.0]),
+    (["nsie", "sersic_old"], [20.3, 18.7, 8.0, 1.2, 0.7, 35.0] + [21.0, 18.0, 3.0, -2.0, 2.5, 0.8, 20.0]),
+    (["point_mass", "sersic"], [20.3, 18.7, 6.0] + [21.0, 18.0, 3.0, -2.0, 1.5, 0.8, 20.0]),
+    (["epl", "sersic"], [20.3, 18.7, 8.0, 0.8, 0.7, 35.0] + [21.0, 18.0, 3.0, -2.0, 1.5, 0.8, 20.0]),
+    (["epl_plus_shear", "sersic"], [20.3, 18.7, 8.0, 1.2, 0.7, 35.0, 0.05, -0.03] + [21.0, 18.0, 3.0, -2.0, 1.5, 0.8, 20.0]),
+    (["sky"], [10.0, 0.3, -0.2]),
+    (["sersic", "sie", "sersic", "sky"], [15.0, 25.0, 2.0, -1.0, 3.0, 0.6, 100.0, 20.3, 18.7, 8.0, 0.7, 35.0,
+                                          21.0, 18.0, 3.0, -2.0, 1.5, 0.8, 20.0, 10.0, 0.1, 0.2]),
+]
+
+
+def make_ctx(plugins, W, H, psf=None, rule="g3k7", image=None, weight=None, pcs=None, max_batch=64, flags=0,
+             priors=None):
+    if image is None:
+        image = np.zeros((H, W), np.float32)
+    if weight is None:
+        weight = np.ones((H, W), np.float32)
+    objs = [(f"o{i}", p, None if priors is None else priors[i]) for i, p in enumerate(plugins)]
+    return lg.Context(image, weight, objs, psf=psf, rule=rule, pcs=pcs, max_batch=max_batch, flags=flags)
+
+
+@pytest.mark.parametrize("case", range(len(PLUGIN_CASES)))
+def test_render_matches_oracle_per_plugin(native, case):
+    plugins, params = PLUGIN_CASES[case]
+    W, H = 41, 37  # non-square, odd: catches index mix-ups
+    pcs = (2.0, -1.0, 1.0, 1.0)
+    ctx = make_ctx(plugins, W, H, rule="gm75", pcs=pcs)
+    model, raw, err = ctx.render(ctx.to_map_order(params))
+    o = Oracle(plugins, W, H, quadrature.rule("gm75"), pcs=pcs, precision=32)
+    v, e, _ = o.render(params)
+    assert_image_close(raw, v, plugins)
+    assert np.array_equal(model, raw)  # no PSF: the model is the raw render
+    assert np.abs(err - e).max() <= 1e-5 * np.abs(v).max() + 1e-7, plugins
+
+
+def test_reference_images_on_gpu(native, golden):
+    rule = quadrature.rule("g3k7")
+    for case in [str(c) for c in golden["cases"]]:
+        plugins = [str(p) for p in golden[f"{case}__plugins"]]
+        params = golden[f"{case}__params"]
+        ctx = make_ctx(plugins, 100, 100, rule="g3k7")
+        _, raw, _ = ctx.render(ctx.to_map_order(params))
+        want = Oracle(plugins, 100, 100, rule, precision=32).render(params)[0]
+        assert_image_close(raw, want, case)
+        ref = golden[f"{case}__image"].astype(np.float64)
+        big = np.abs(ref) > 1e-6 * np.abs(ref).max()
+        assert (np.abs(raw - ref)[big] / np.abs(ref[big])).max() <= 2e-4, case
+        ctx.close()
+
+
+@pytest.mark.parametrize("psf_size", [7, 8, 15])
+def test_psf_convolution_matches_oracle(native, psf_size):
+    plugins, params = PLUGIN_CASES[4]
+    W, H = 45, 52
+    psf = workloads.psf_gauss_wings(psf_size, 2.0)
+    if psf_size == 8:
+        psf = psf[:, :7].copy()  # even height, odd width: one-axis half-pixel shift
+    ctx = make_ctx(plugins, W, H, psf=psf, rule="sub2")
+    model, raw, _ = ctx.render(ctx.to_map_order(params))
+    o = Oracle(plugins, W, H, quadrature.rule("sub2"), psf=psf, precision=32)
+    v, _, c = o.render(params)
+    assert_image_close(raw, v, "raw")
+    assert_image_close(model, c, "convolved")
+
+
+def _loglike_case(system, B, seed=0):
+    ctx = lg.Context(system.image, system.weight, system.objects, psf=system.psf, rule=system.rule,
+                     max_batch=max(B, 8))
+    cand = workloads.draw_candidates(system, B, seed=seed)
+    got = ctx.eval_batch(ctx.to_map_order(cand))
+    o32 = Oracle(system.plugins, system.width, system.height, quadrature.rule(system.rule), psf=system.psf,
+                 image=system.image, weight=system.weight, precision=32, threads=16)
+    o64 = Oracle(system.plugins, system.width, system.height, quadrature.rule(system.rule), psf=system.psf,
+                 image=system.image, weight=system.weight, precision=64, threads=16)
+    want32, want64 = o32.loglike(cand), o64.loglike(cand)
+    return ctx, cand, got, want32, want64
+
+
+def test_loglike_small_workload(native):
+    ctx, cand, got, w32, w64 = _loglike_case(workloads.small(), 16)
+    d32 = np.abs(got - w32).max()
+    print(f"small: max|dlogL| vs FP32 oracle {d32:.3g}, vs FP64 oracle {np.abs(got - w64).max():.3g}, "
+          f"FP32 oracle vs FP64 {np.abs(w32 - w64).max():.3g}")
+    assert d32 <= LOGL_ABS
+
+
+def test_loglike_config2_full_size(native):
+    """256^2, SIE+shear, bulge + disk + sky, 25x25 PSF, 25-point rule, 10% mask."""
+    ctx, cand, got, w32, w64 = _loglike_case(workloads.config2(), 6)
+    d32 = np.abs(got - w32).max()
+    print(f"config2: logL {got[:3]} max|dlogL| vs FP32 oracle {d32:.3g}, vs FP64 oracle "
+          f"{np.abs(got - w64).max():.3g}, FP32 oracle vs FP64 {np.abs(w32 - w64).max():.3g}")
+    assert d32 <= LOGL_ABS
+    assert ctx.masked == int((ctx._weight == 0).sum())
+
+
+def test_batch_equals_single_and_is_deterministic(native):
+    s = workloads.config2()
+    ctx = lg.Context(s.image, s.weight, s.objects, psf=s.psf, rule=s.rule, max_batch=64)
+    cand = ctx.to_map_order(workloads.draw_candidates(s, 64, seed=3))
+    a = ctx.eval_batch(cand)
+    b = ctx.eval_batch(cand)
+    assert np.array_equal(a, b)
+    single = np.array([ctx.eval_batch(cand[i:i + 1])[0] for i in range(0, 64, 9)])
+    assert np.array_equal(single, a[::9])
+    rev = ctx.eval_batch(cand[::-1].copy())
+    assert np.array_equal(rev[::-1], a)
+
+
+def test_graph_and_direct_launch_agree(native):
+    s = workloads.small()
+    cand = workloads.draw_candidates(s, 32, seed=4)
+    a = lg.Context(s.image, s.weight, s.objects, rule=s.rule, max_batch=32)
+    b = lg.Context(s.image, s.weight, s.objects, rule=s.rule, max_batch=32, flags=lg.LG_FLAG_NO_GRAPH)
+    assert np.array_equal(a.eval_batch(a.to_map_order(cand)), b.eval_batch(b.to_map_order(cand)))
+
+
+def test_strict_fp_mode_matches_oracle_more_tightly(native):
+    s = workloads.small()
+    cand = workloads.draw_candidates(s, 8, seed=5)
+    ctx = lg.Context(s.image, s.weight, s.objects, rule=s.rule, max_batch=8, flags=lg.LG_FLAG_STRICT_FP)
+    got = ctx.eval_batch(ctx.to_map_order(cand))
+    want = Oracle(s.plugins, s.width, s.height, quadrature.rule(s.rule), image=s.image, weight=s.weight,
+                  precision=32, threads=16).loglike(cand)
+    assert np.abs(got - want).max() <= LOGL_ABS
+
+
+def test_image_plane_prior_parity(native):
+    W = H = 48
+    psf = None
+    plugins = ["sie", "sersic"]
+    params = [24.3, 23.8, 9.0, 0.75, 40.0, 14.0, 30.0, 2.0, -1.0, 2.0, 0.8, 30.0]
+    priors = [{"x": "unif 20 28", "y": "unif 20 28", "r": "unif 5 12", "q": "unif 0.5 0.95", "pa": "unif 0 180"},
+              {"x": "image unif 10 20", "y": "image unif 25 35", "r": "unif 1 3", "mag": "unif -3 0",
+               "n": "unif 1 4", "q": "unif 0.5 1", "pa": "unif 0 180"}]
+    ctx = make_ctx(plugins, W, H, psf=psf, rule="sub3", priors=priors)
+    _, raw, _ = ctx.render(ctx.to_map_order(params))
+    o = Oracle([("sie", 0), ("sersic", 1)], W, H, quadrature.rule("sub3"), precision=32)
+    assert_image_close(raw, o.render(params)[0], "ipp")
+
+
+def test_cube_transform_and_reference_callback(native):
+    s = workloads.small()
+    ctx = lg.Context(s.image, s.weight, s.objects, rule=s.rule, max_batch=16)
+    rng = np.random.Generator(np.random.PCG64(9))
+    cube = rng.random(size=(5, ctx.ndims))
+    ll, phys = ctx.eval_cube(cube)
+    direct = ctx.eval_batch(phys)
+    assert np.array_equal(ll, direct)
+    l1, p1 = ctx.loglike(cube[0])
+    assert l1 == ll[0] and np.array_equal(p1, phys[0])
+    # derived (fixed) parameters sit after the free ones
+    assert ctx.ndims == ctx.npars - 2
+
+
+def test_bad_calls_return_status_and_context_survives(native):
+    import ctypes as C
+
+    s = workloads.small()
+    ctx = lg.Context(s.image, s.weight, s.objects, rule=s.rule, max_batch=4)
+    cand = np.ascontiguousarray(ctx.to_map_order(workloads.draw_candidates(s, 5, seed=1)))
+    out = np.zeros(5)
+    dp = C.POINTER(C.c_double)
+    rc = lg.lib().lg_eval_batch(ctx.h, cand.ctypes.data_as(dp), 5, out.ctypes.data_as(dp))
+    assert rc == -1 and b"max_batch" in lg.lib().lg_last_error(ctx.h)
+    ok = ctx.eval_batch(cand[:4])
+    assert np.all(np.isfinite(ok))
+
+
+def test_non_finite_parameters_follow_the_reference(native):
+    """A non-finite lens deflection sends the ray away (src/kernel.c:86-91);
+    a NaN source parameter gives a NaN likelihood, as on the CPU."""
+    s = workloads.small()
+    ctx = lg.Context(s.image, s.weight, s.objects, rule=s.rule, max_batch=4)
+    o = Oracle(s.plugins, s.width, s.height, quadrature.rule(s.rule), image=s.image, weight=s.weight,
+               precision=32, threads=16)
+    p = np.tile(s.truth, (2, 1))
+    p[0, 0] = np.nan          # lens x
+    p[1, 8] = np.nan          # source magnitude
+    got = ctx.eval_batch(ctx.to_map_order(p))
+    want = o.loglike(p)
+    assert np.isfinite(got[0]) and abs(got[0] - want[0]) <= LOGL_ABS
+    assert np.isnan(got[1]) and np.isnan(want[1])
