@@ -1,0 +1,353 @@
+#!/usr/bin/env python
+"""Benchmark: logL evaluations per second of the batched GB300 likelihood.
+
+Workload (default ``config2``): a 256x256 float32 mock, SIE + external shear
+lens, Sersic bulge + exponential disk sources, sky foreground, 25x25
+Gaussian-plus-wings PSF, 25-point (5x5) pixel quadrature, 10% random mask,
+1024 candidate parameter vectors per launch.  One step = one evaluation of
+the whole batch (set_params -> render -> convolve + chi^2 -> logL).
+
+Arms
+  default            the CUDA path.  ``value``: device-resident parameters,
+                     CUDA-event timing of K steps on the launching stream.
+                     ``e2e``: the public C-ABI call ``lg_eval_batch`` with host
+                     parameters and host logL (H2D + D2H inside the timing).
+  --impl reference   the reference algorithm on the host CPU: the
+                     reference's own sources compiled here if that build is
+                     present (oracle/_ref), else the C++ restatement (oracle),
+                     with all host threads, one candidate per step as the
+                     reference's callback does.
+
+Multi-GPU: one process per GPU under torchrun; each rank evaluates its own
+batch (replicas, weak scaling; no collective on the data path); the JSON
+``value`` is the total over ranks divided by the slowest rank's time.
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import os
+import subprocess
+import sys
+import tempfile
+import threading
+import time
+
+import numpy as np
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+METRIC = "logL evals/s"
+UNIT = "evals/s"
+
+# Source-level FP32 operation count per ray of each plugin's evaluation
+# (add/sub/mul/div/sqrt = 1, each libm-class call = 1), counted from the
+# plugin formulas; plus per-ray overheads of compute() and the quadrature
+# loop.  Used for the algorithmic FLOPs of the render kernel.
+RAY_FLOPS = {
+    "sis": 12, "sis_plus_shear": 20, "nsis": 10, "sie": 26, "sie_plus_shear": 34, "nsie": 30,
+    "point_mass": 9, "epl": 172, "epl_plus_shear": 180, "sersic": 17, "sersic_old": 17, "exponential": 15,
+    "devauc": 16, "gauss": 16, "sky": 6,
+}
+RAY_OVERHEAD = 4 + 8  # x + qq, ww*f + acc; per lens plane: a += .., finiteness test and y -= a
+
+
+def ray_flops(plugins):
+    return sum(RAY_FLOPS[p] for p in plugins) + RAY_OVERHEAD + sum(1 for p in plugins if p not in RAY_FLOPS)
+
+
+def workload(name):
+    from lensed_gb300 import workloads
+
+    if name == "config2":
+        return workloads.config2(), 1024
+    if name == "small":
+        return workloads.small(), 1
+    if name == "large":
+        return workloads.large(), 256
+    raise SystemExit(f"unknown workload {name}")
+
+
+def describe(s, B):
+    return {
+        "workload": f"{s.name}: {s.width}x{s.height} float32, objects " + "+".join(s.plugins)
+                    + (f", {s.psf.shape[0]}x{s.psf.shape[1]} PSF" if s.psf is not None else ", no PSF")
+                    + f", rule {s.rule}" + (", 10% mask" if s.mask is not None else ""),
+        "batch": B,
+        "params": int(s.truth.size),
+        "l2": "per-step working set larger than L2 (raw model images B x N x 4 B = "
+              f"{B * s.width * s.height * 4 / 2**20:.0f} MiB written and re-read)" if s.psf is not None
+              else "inputs resident; no L2 flush (compute-bound)",
+        "data": "synthetic seeded mock (no public dataset)",
+    }
+
+
+class Clocks:
+    """nvidia-smi sampler running during the timed region."""
+
+    Q = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,clocks_event_reasons.hw_slowdown,"
+         "clocks_event_reasons.hw_thermal_slowdown,clocks_event_reasons.sw_thermal_slowdown,"
+         "clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, device):
+        self.device = device
+        self.proc = None
+        self.path = None
+
+    def start(self):
+        try:
+            fd, self.path = tempfile.mkstemp(suffix=".csv")
+            os.close(fd)
+            self.proc = subprocess.Popen(["nvidia-smi", f"--id={self.device}", f"--query-gpu={self.Q}",
+                                          "--format=csv,noheader,nounits", "-lms", "200"],
+                                         stdout=open(self.path, "w"), stderr=subprocess.DEVNULL)
+        except Exception:
+            self.proc = None
+
+    def stop(self):
+        if not self.proc:
+            return None
+        self.proc.terminate()
+        try:
+            self.proc.wait(timeout=5)
+        except Exception:
+            self.proc.kill()
+        sm, mx, reasons = [], [], set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for line in open(self.path):
+            f = [x.strip() for x in line.split(",")]
+            if len(f) < 9:
+                continue
+            try:
+                sm.append(float(f[1]))
+                mx.append(float(f[2]))
+            except ValueError:
+                continue
+            for n, v in zip(names, f[5:9]):
+                if v.lower().startswith("active"):
+                    reasons.add(n)
+        os.unlink(self.path)
+        if not sm:
+            return None
+        return {"sm_mhz": float(np.median(sm)), "sm_max_mhz": float(max(mx)), "reasons": sorted(reasons),
+                "samples": len(sm)}
+
+
+def dist_setup(n_gpus):
+    rank = int(os.environ.get("RANK", "0"))
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    dist = None
+    if world > 1:
+        import torch
+        import torch.distributed as dist
+
+        torch.cuda.set_device(local)
+        dist.init_process_group("nccl")
+    return rank, world, local, dist
+
+
+def cpu_oracle(s, threads, precision=32):
+    from lensed_gb300 import quadrature
+    from oracle.oracle import Oracle
+
+    return Oracle(s.plugins, s.width, s.height, quadrature.rule(s.rule), psf=s.psf, image=s.image,
+                  weight=s.weight, precision=precision, threads=threads)
+
+
+def ref_impl():
+    """The reference-built CPU implementation if present, else the restatement."""
+    try:
+        from oracle import ref as R
+
+        if R.available():
+            return "reference", R
+    except Exception:
+        pass
+    return "port", None
+
+
+def cpu_rate(s, cand, threads, budget_s=12.0, kind="port", ref=None):
+    """Evaluate candidates one at a time on the host until the budget is spent."""
+    o = ref.Reference(s, threads) if ref is not None else cpu_oracle(s, threads)
+    o.loglike(cand[:1])  # warm-up
+    n, t0 = 0, time.perf_counter()
+    while True:
+        o.loglike(cand[n % len(cand): n % len(cand) + 1])
+        n += 1
+        dt = time.perf_counter() - t0
+        if (dt > budget_s and n >= 2) or n >= 200:
+            break
+    return n / dt, n, dt
+
+
+def run_reference(args):
+    rank = int(os.environ.get("RANK", "0"))
+    if rank != 0:
+        return
+    from lensed_gb300 import workloads
+
+    s, B = workload(args.workload)
+    cand = workloads.draw_candidates(s, 64, seed=1)
+    threads = os.cpu_count() or 1
+    kind, R = ref_impl()
+    o = R.Reference(s, threads) if R is not None else cpu_oracle(s, threads)
+    for i in range(args.warmup):
+        o.loglike(cand[i % 64: i % 64 + 1])
+    t0 = time.perf_counter()
+    for i in range(args.steps):
+        o.loglike(cand[i % 64: i % 64 + 1])
+    dt = time.perf_counter() - t0
+    v = args.steps / dt
+    sample = f"{args.steps} candidates, one logL per step, {threads} threads (OpenMP over pixels)"
+    line = {"impl": "reference", "metric": METRIC, "value": v, "unit": UNIT, "n_gpus": 0, "steps": args.steps,
+            "warmup": args.warmup, "ms_per_step": 1e3 * dt / args.steps, "higher_is_better": True,
+            "scaling": "weak", "vs_baseline": None, "dtype": "f32 (f64 chi^2 sum)", "data": "synthetic",
+            "config": describe(s, 1),
+            "cpu_baseline": {"value": v, "unit": UNIT, "cores": threads, "kind": kind, "sample": sample},
+            "e2e": {"value": v, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
+    print(json.dumps(line), flush=True)
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=100)
+    ap.add_argument("--warmup", type=int, default=5)
+    ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
+    ap.add_argument("--workload", default="config2")
+    ap.add_argument("--batch", type=int, default=0)
+    ap.add_argument("--no-cpu-baseline", action="store_true")
+    args = ap.parse_args()
+    args.warmup = max(args.warmup, 3)
+    if args.impl == "reference":
+        return run_reference(args)
+
+    import torch
+
+    import lensed_gb300 as lg
+    from lensed_gb300 import workloads
+
+    rank, world, local, dist = dist_setup(args.gpus)
+    torch.cuda.set_device(local)
+    s, B = workload(args.workload)
+    if args.batch:
+        B = args.batch
+    ctx = lg.Context(s.image, s.weight, s.objects, psf=s.psf, rule=s.rule, device=local, max_batch=B)
+    cand = ctx.to_map_order(workloads.draw_candidates(s, B, seed=1 + rank))
+    d_params = torch.from_numpy(np.ascontiguousarray(cand)).to(f"cuda:{local}")
+    d_logL = torch.empty(B, dtype=torch.float64, device=f"cuda:{local}")
+    stream = torch.cuda.current_stream()
+    sh = stream.cuda_stream
+
+    def step():
+        ctx.eval_batch_device(d_params.data_ptr(), B, d_logL.data_ptr(), sh)
+
+    for _ in range(args.warmup):
+        step()
+    torch.cuda.synchronize()
+    clocks = Clocks(local)
+    clocks.start()
+    time.sleep(0.3)
+    if dist:
+        dist.barrier()
+    torch.cuda.synchronize()
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    e0.record(stream)
+    for _ in range(args.steps):
+        step()
+    e1.record(stream)
+    torch.cuda.synchronize()
+    if dist:
+        dist.barrier()
+    ms = e0.elapsed_time(e1)
+    clk = clocks.stop()
+    if dist:
+        t = torch.tensor([ms], device=f"cuda:{local}")
+        dist.all_reduce(t, op=dist.ReduceOp.MAX)
+        ms = float(t.item())
+    value = world * B * args.steps / (ms / 1e3)
+    logL_gpu = d_logL.cpu().numpy()
+
+    # per-stage device times (the reference's --profile stages), averaged
+    stage = np.zeros(4)
+    nprof = 5
+    for _ in range(nprof):
+        stage += ctx.profile(d_params.data_ptr(), B, d_logL.data_ptr())
+    stage /= nprof
+
+    # end to end through the public C ABI with host buffers
+    hp = np.ascontiguousarray(cand)
+    for _ in range(2):
+        ctx.eval_batch(hp)
+    ne2e = max(3, min(args.steps, 50))
+    t0 = time.perf_counter()
+    for _ in range(ne2e):
+        ll_host = ctx.eval_batch(hp)
+    e2e_dt = (time.perf_counter() - t0) / ne2e
+    e2e = world * B / e2e_dt
+    if dist:
+        t = torch.tensor([e2e_dt], device=f"cuda:{local}")
+        dist.all_reduce(t, op=dist.ReduceOp.MAX)
+        e2e = world * B / float(t.item())
+
+    # plain mode: one candidate per call with a host sync (the reference flow)
+    plain = None
+    if rank == 0:
+        n1 = 200
+        t0 = time.perf_counter()
+        for i in range(n1):
+            ctx.eval_batch(hp[i % B: i % B + 1])
+        plain = n1 / (time.perf_counter() - t0)
+
+    # roofline of the dominant kernel
+    N, Q = s.width * s.height, len(lg.quad_rules()[s.rule][1])
+    render_flops = B * N * Q * ray_flops(s.plugins)
+    conv_flops = 2.0 * B * N * (s.psf.size if s.psf is not None else 0)
+    try:
+        peak_fp32 = lg.measure_fp32_peak(local)
+    except Exception:
+        peak_fp32 = None
+    nominal = 152 * 128 * 2 * 2070e6 / 1e12
+    dom = "render" if stage[1] >= stage[2] else "convolve"
+    if dom == "render":
+        ach = render_flops / (stage[1] * 1e-3) / 1e12
+    else:
+        ach = conv_flops / (stage[2] * 1e-3) / 1e12
+    peak = peak_fp32 or nominal
+    roof = {"kernel": "lg_render_raw" if dom == "render" and s.psf is not None else
+            ("lg_render_chi2" if dom == "render" else "lg_conv_chi2"),
+            "bound": "fp32", "achieved": ach, "peak": peak, "unit": "TFLOP/s", "frac": ach / peak,
+            "peak_source": "measured FP32 FMA probe (lg_measure_fp32_peak) on this GPU" if peak_fp32 else
+                           "nominal 152 SM x 128 lanes x 2 flop x 2070 MHz",
+            "nominal_peak": nominal, "traffic": None,
+            "algorithmic_flops_per_launch": render_flops if dom == "render" else conv_flops,
+            "stage_ms": {"set_params": float(stage[0]), "render": float(stage[1]), "convolve": float(stage[2]),
+                         "finish": float(stage[3])},
+            "convolve_tflops": (conv_flops / (stage[2] * 1e-3) / 1e12) if stage[2] > 0 else None,
+            "rays_per_s": B * N * Q / (stage[1] * 1e-3)}
+
+    line = {"metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
+            "warmup": args.warmup, "ms_per_step": ms / args.steps, "higher_is_better": True, "scaling": "weak",
+            "vs_baseline": None, "dtype": "f32 (f64 chi^2 reduction)", "data": "synthetic",
+            "config": describe(s, B), "gpu_launches": 4 * args.steps,
+            "e2e": {"value": e2e, "unit": UNIT, "h2d_bytes_per_step": int(hp.nbytes), "d2h_bytes_per_step": 8 * B},
+            "plain_evals_per_s": plain, "roofline": roof}
+    if clk:
+        line["clocks"] = clk
+    if rank == 0 and world == 1 and not args.no_cpu_baseline:
+        threads = os.cpu_count() or 1
+        kind, R = ref_impl()
+        v, n, dt = cpu_rate(s, workloads.draw_candidates(s, 8, seed=1), threads, kind=kind, ref=R)
+        line["cpu_baseline"] = {"value": v, "unit": UNIT, "cores": threads, "kind": kind,
+                                "sample": f"{n} candidates of the same workload, one at a time, {dt:.1f} s"}
+    if rank == 0:
+        print(json.dumps(line), flush=True)
+    if dist:
+        dist.destroy_process_group()
+    ctx.close()
+
+
+if __name__ == "__main__":
+    main()

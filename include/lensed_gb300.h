@@ -180,6 +180,16 @@ int lg_eval_cube_batch(lg_ctx* ctx, const double* cube, int B, double* phys, dou
  * estimate (src/nested.c:175-216).  Any output may be NULL. */
 int lg_render(lg_ctx* ctx, const double* params, float* model, float* raw, float* error);
 
+/* Device times (ms) of the four stages of one evaluation of B candidates
+ * with device pointers: set_params, render, convolve (0 without a PSF) and
+ * the chi^2 finish -- the counterpart of the reference's --profile table
+ * (src/nested.c:21-40, src/profile.c:36-83). */
+int lg_eval_profile(lg_ctx* ctx, const double* d_params, int B, double* d_logL, float* stage_ms);
+
+/* Measured FP32 FMA throughput (TFLOP/s) of a device, for roofline
+ * denominators. */
+int lg_measure_fp32_peak(int device, double* tflops);
+
 /* Drop-in for the reference's likelihood callback (src/nested.h:3): ctx is
  * an lg_ctx*.  cube[0..ndim) holds unit-cube values and is overwritten with
  * the physical values of all npar parameters (map order); *lnew receives

@@ -86,6 +86,8 @@ def lib():
         "lg_eval_batch_device": (C.c_int, [vp, vp, C.c_int, vp, vp]),
         "lg_eval_cube_batch": (C.c_int, [vp, dp, C.c_int, dp, dp]),
         "lg_render": (C.c_int, [vp, dp, fp, fp, fp]),
+        "lg_eval_profile": (C.c_int, [vp, vp, C.c_int, vp, fp]),
+        "lg_measure_fp32_peak": (C.c_int, [C.c_int, dp]),
         "loglike": (None, [dp, ip, ip, dp, vp]),
     }
     for name, (res, args) in sig.items():
@@ -142,6 +144,15 @@ def quad_rules():
         L.lg_quad_rule_info(i, None, None, _p(a, C.c_double), _p(w, C.c_double), _p(e, C.c_double))
         out[n.value.decode()] = (a, w, e)
     return out
+
+
+def measure_fp32_peak(device: int = 0) -> float:
+    """Measured FP32 FMA throughput of the device in TFLOP/s."""
+    v = C.c_double()
+    rc = lib().lg_measure_fp32_peak(device, C.byref(v))
+    if rc:
+        raise LensedError(rc, "fp32 peak probe")
+    return v.value
 
 
 def make_weight(image, weight_map=None, gain=None, gain_value=1.0, offset=0.0, xweight=None, mask=None):
@@ -277,6 +288,13 @@ class Context:
         """Device-pointer variant (e.g. torch tensors' data_ptr()); asynchronous."""
         self._check(lib().lg_eval_batch_device(self.h, C.c_void_p(d_params), int(B), C.c_void_p(d_logL),
                                                C.c_void_p(stream) if stream else None))
+
+    def profile(self, d_params: int, B: int, d_logL: int):
+        """Device ms of (set_params, render, convolve, finish) for one evaluation."""
+        ms = np.zeros(4, np.float32)
+        self._check(lib().lg_eval_profile(self.h, C.c_void_p(d_params), int(B), C.c_void_p(d_logL),
+                                          _p(ms, C.c_float)))
+        return ms
 
     def eval_cube(self, cube):
         u = np.ascontiguousarray(np.atleast_2d(cube), dtype=np.float64)

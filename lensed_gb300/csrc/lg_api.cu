@@ -128,26 +128,36 @@ struct lg_ctx {
     }
 
     // Enqueue set_params .. finish for B candidates; params and logL are
-    // device pointers.
-    int enqueue(int B, const double* params, double* logL, cudaStream_t s)
+    // device pointers.  With ev != NULL, ev[0..4] are recorded before
+    // set_params, render, convolve and finish and after finish.
+    int enqueue(int B, const double* params, double* logL, cudaStream_t s, cudaEvent_t* ev = nullptr)
     {
         int rc;
+        auto mark = [&](int i) { return ev ? cuda(cudaEventRecord(ev[i], s), "event") : LG_OK; };
         void* a_setp[] = {&params, &B, &d_models};
-        if ((rc = launch(f_setp, dim3((B + 127) / 128), dim3(128), 0, s, a_setp, "set_params"))) return rc;
+        if ((rc = mark(0)) || (rc = launch(f_setp, dim3((B + 127) / 128), dim3(128), 0, s, a_setp, "set_params")) ||
+            (rc = mark(1)))
+            return rc;
         if (psf) {
             void* a_r[] = {&d_models, &d_raw};
-            if ((rc = launch(f_rraw, dim3(rtiles, B), dim3(shape.rt), 0, s, a_r, "render"))) return rc;
+            if ((rc = launch(f_rraw, dim3(rtiles, B), dim3(shape.rt), 0, s, a_r, "render")) || (rc = mark(2)))
+                return rc;
             void* a_c[] = {&d_raw, &d_image, &d_weight, &d_partials};
             if ((rc = launch(f_cchi2, dim3(ctiles_x, ctiles_y, B), dim3(shape.ctx / shape.cr, shape.cty), csmem, s,
-                             a_c, "convolve")))
+                             a_c, "convolve")) ||
+                (rc = mark(3)))
                 return rc;
             void* a_f[] = {&d_partials, &ctiles, &logL};
-            return launch(f_finish, dim3(B), dim3(256), 0, s, a_f, "finish");
+            if ((rc = launch(f_finish, dim3(B), dim3(256), 0, s, a_f, "finish"))) return rc;
+            return mark(4);
         }
         void* a_r[] = {&d_models, &d_image, &d_weight, &d_partials};
-        if ((rc = launch(f_rchi2, dim3(rtiles, B), dim3(shape.rt), 0, s, a_r, "render"))) return rc;
+        if ((rc = launch(f_rchi2, dim3(rtiles, B), dim3(shape.rt), 0, s, a_r, "render")) || (rc = mark(2)) ||
+            (rc = mark(3)))
+            return rc;
         void* a_f[] = {&d_partials, &rtiles, &logL};
-        return launch(f_finish, dim3(B), dim3(256), 0, s, a_f, "finish");
+        if ((rc = launch(f_finish, dim3(B), dim3(256), 0, s, a_f, "finish"))) return rc;
+        return mark(4);
     }
 
     void release()
@@ -564,6 +574,77 @@ int lg_render(lg_ctx* c, const double* params, float* model, float* raw, float* 
                                "read model")))
         return rc;
     return c->cuda(cudaStreamSynchronize(c->stream), "render");
+}
+
+// Per-stage device times of one evaluation, the counterpart of the
+// reference's --profile event table (src/nested.c:21-40, src/profile.c).
+int lg_eval_profile(lg_ctx* c, const double* d_params, int B, double* d_logL, float* stage_ms)
+{
+    if (!c || !d_params || !d_logL || !stage_ms || B <= 0) return LG_ERR_INPUT;
+    if (B > c->max_batch) return c->fail(LG_ERR_INPUT, "batch larger than max_batch");
+    int rc;
+    if ((rc = c->cuda(cudaSetDevice(c->device), "cudaSetDevice"))) return rc;
+    cudaEvent_t ev[5] = {};
+    for (auto& e : ev)
+        if ((rc = c->cuda(cudaEventCreate(&e), "event"))) return rc;
+    rc = c->enqueue(B, d_params, d_logL, c->stream, ev);
+    if (!rc) rc = c->cuda(cudaStreamSynchronize(c->stream), "profile");
+    for (int i = 0; i < 4 && !rc; ++i) rc = c->cuda(cudaEventElapsedTime(&stage_ms[i], ev[i], ev[i + 1]), "elapsed");
+    for (auto& e : ev) cudaEventDestroy(e);
+    return rc;
+}
+
+}  // extern "C"
+
+// FP32 FMA throughput probe: eight independent FMA chains per thread.
+__global__ void lg_fma_probe(float* out, float a, float b, int iters)
+{
+    float x0 = threadIdx.x * 1e-7f, x1 = x0 + 1e-7f, x2 = x0 + 2e-7f, x3 = x0 + 3e-7f;
+    float x4 = x0 + 4e-7f, x5 = x0 + 5e-7f, x6 = x0 + 6e-7f, x7 = x0 + 7e-7f;
+    for (int i = 0; i < iters; ++i) {
+#pragma unroll
+        for (int k = 0; k < 16; ++k) {
+            x0 = fmaf(x0, a, b); x1 = fmaf(x1, a, b); x2 = fmaf(x2, a, b); x3 = fmaf(x3, a, b);
+            x4 = fmaf(x4, a, b); x5 = fmaf(x5, a, b); x6 = fmaf(x6, a, b); x7 = fmaf(x7, a, b);
+        }
+    }
+    const float s = ((x0 + x1) + (x2 + x3)) + ((x4 + x5) + (x6 + x7));
+    if (s == 12345.0f) out[blockIdx.x * blockDim.x + threadIdx.x] = s;
+}
+
+extern "C" {
+
+// Measured FP32 FMA throughput of the current device in TFLOP/s (2 flops per
+// FMA); the denominator of the ray-shooting roofline.
+int lg_measure_fp32_peak(int device, double* tflops)
+{
+    if (!tflops) return LG_ERR_INPUT;
+    if (cudaSetDevice(device) != cudaSuccess) return LG_ERR_CUDA;
+    int sms = 0;
+    cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, device);
+    float* out = nullptr;
+    const int threads = 256, blocks = sms * 8, iters = 4096;
+    if (cudaMalloc(&out, (size_t)threads * blocks * 4) != cudaSuccess) return LG_ERR_ALLOC;
+    cudaEvent_t e0, e1;
+    cudaEventCreate(&e0);
+    cudaEventCreate(&e1);
+    float best = 1e30f;
+    for (int rep = 0; rep < 4; ++rep) {
+        cudaEventRecord(e0);
+        lg_fma_probe<<<blocks, threads>>>(out, 0.999999f, 1e-6f, iters);
+        cudaEventRecord(e1);
+        cudaEventSynchronize(e1);
+        float ms = 0;
+        cudaEventElapsedTime(&ms, e0, e1);
+        if (rep > 0 && ms < best) best = ms;
+    }
+    cudaError_t e = cudaGetLastError();
+    cudaEventDestroy(e0);
+    cudaEventDestroy(e1);
+    cudaFree(out);
+    if (e != cudaSuccess) return LG_ERR_CUDA;
+    *tflops = 2.0 * 8 * 16 * (double)iters * threads * blocks / (best * 1e-3) / 1e12;
+    return LG_OK;
 }
 
 // src/nested.c:17-131 with the arithmetic moved to the GPU.  The reference

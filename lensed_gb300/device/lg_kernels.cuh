@@ -40,12 +40,13 @@ LG_DEV double lg_warp_sum(double v)
 template <int NT>
 LG_DEV double lg_block_sum(double v, double* red)
 {
-    const int lane = threadIdx.x & 31, warp = (threadIdx.y * blockDim.x + threadIdx.x) >> 5;
+    const int tid = threadIdx.y * blockDim.x + threadIdx.x;
+    const int lane = tid & 31, warp = tid >> 5;
     v = lg_warp_sum(v);
     if (lane == 0) red[warp] = v;
     __syncthreads();
     double s = 0.0;
-    if (warp == 0 && (threadIdx.y | threadIdx.x) == 0) {
+    if (tid == 0) {
 #pragma unroll
         for (int i = 0; i < NT / 32; ++i) s += red[i];
     }
