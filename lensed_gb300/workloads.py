@@ -252,7 +252,7 @@ def _priors_from_box(plugins, lower, upper, fixed):
             if k in fixed:
                 d[n] = repr(float(fixed[k]))
             else:
-                d[n] = f"unif {lower[k]!r} {upper[k]!r}"
+                d[n] = f"unif {float(lower[k])!r} {float(upper[k])!r}"
             k += 1
         out.append(d)
     return out

@@ -118,3 +118,12 @@ LG_DEV float lg_brightness_ring_test(const lg_data_ring_test* __restrict__ o, fl
     assert native.lg_register_plugin(C.byref(d)) == -1  # duplicate
     assert [p[0] for p in lg.plugin_params("ring_test")] == ["x", "y", "r", "w", "a"]
     lg.compile_check(16, 16, ["sie", "ring_test"], rule="point")
+
+
+@pytest.mark.parametrize("name", ["small", "config2", "large"])
+def test_benchmark_workloads_compose(native, name):
+    """The seeded benchmark systems (priors included) compose and compile."""
+    from lensed_gb300 import workloads
+
+    s = getattr(workloads, name)()
+    lg.compile_check(s.width, s.height, s.objects, psf=s.psf, rule=s.rule)

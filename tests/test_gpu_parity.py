@@ -2,7 +2,11 @@
 
 Tolerances (FP32 ray-shooting, FP64 reduction):
   * model images: relative error <= 1e-5 on pixels above 1e-6 of the peak,
-    absolute error <= 1e-6 * peak below that floor;
+    absolute error <= 1e-6 * peak below that floor.  Where the FP32 oracle is
+    itself further than 1e-5 from the FP64 oracle (ill-conditioned profiles,
+    e.g. the r^(1/4) cusp of de Vaucouleurs, whose gradient amplifies
+    last-bit differences of the ray positions), the bound is twice that FP32
+    error, and the GPU image must be as close to FP64 as that bound;
   * logL: |logL_gpu - logL_oracle32| <= 1e-3;
   * the FP32 paths' distance to the FP64 oracle is reported, not bounded
     tighter than the FP32 budget.
@@ -29,9 +33,14 @@ def image_err(got, want):
     return rel, small
 
 
-def assert_image_close(got, want, what=""):
+def assert_image_close(got, want, what="", want64=None):
+    tol = IMG_REL
+    if want64 is not None:
+        tol = max(IMG_REL, 2 * image_err(want, want64)[0])
+        rel64, _ = image_err(got, want64)
+        assert rel64 <= tol, (what, "vs FP64", rel64, tol)
     rel, small = image_err(got, want)
-    assert rel <= IMG_REL and small <= 1e-6, (what, rel, small)
+    assert rel <= tol and small <= 1e-6, (what, rel, small, tol)
 
 
 PLUGIN_CASES = [
@@ -69,7 +78,8 @@ def test_render_matches_oracle_per_plugin(native, case):
     model, raw, err = ctx.render(ctx.to_map_order(params))
     o = Oracle(plugins, W, H, quadrature.rule("gm75"), pcs=pcs, precision=32)
     v, e, _ = o.render(params)
-    assert_image_close(raw, v, plugins)
+    v64 = Oracle(plugins, W, H, quadrature.rule("gm75"), pcs=pcs, precision=64).render(params)[0]
+    assert_image_close(raw, v, plugins, want64=v64)
     assert np.array_equal(model, raw)  # no PSF: the model is the raw render
     assert np.abs(err - e).max() <= 1e-5 * np.abs(v).max() + 1e-7, plugins
 
