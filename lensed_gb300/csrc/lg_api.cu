@@ -85,7 +85,8 @@ struct lg_ctx {
     std::string err;
 
     const Driver* drv = nullptr;
-    CUmodule mod = nullptr;
+    CUmodule mod = nullptr;      // evaluation module
+    CUmodule mod_set = nullptr;  // set_params module
     CUfunction f_setp = nullptr, f_rraw = nullptr, f_rchi2 = nullptr, f_rdump = nullptr;
     CUfunction f_cchi2 = nullptr, f_cdump = nullptr, f_finish = nullptr;
     size_t model_bytes = 0;
@@ -176,6 +177,8 @@ struct lg_ctx {
         cudaFreeHost(h_params);
         cudaFreeHost(h_logL);
         if (mod && drv) drv->moduleUnload(mod);
+        if (mod_set && drv) drv->moduleUnload(mod_set);
+        mod_set = nullptr;
         if (stream) cudaStreamDestroy(stream);
         mod = nullptr;
         stream = nullptr;
@@ -227,33 +230,41 @@ int create_impl(lg_ctx* c, const lg_image_desc* img, const lg_object_desc* objs,
     for (long k = 0; k < c->N; ++k)
         if (img->weight[k] == 0) c->masked++;
 
-    // compose and compile the program (the reference's clBuildProgram,
+    // compose and compile the programs (the reference's clBuildProgram,
     // src/lensed.c:706-776)
     c->shape = choose_shape(m);
     shape_sizes(c->shape, m, c);
     const bool strict = (c->flags & LG_FLAG_STRICT_FP) != 0;
-    std::string src = lg::compose_source(m, c->shape, strict), log;
-    std::vector<char> cubin;
-    if ((rc = lg::compile_program(src, strict, cubin, log))) return c->fail(rc, log);
+    std::string log;
+    std::vector<char> cubin, cubin_set;
+    if ((rc = lg::compile_program(lg::compose_source(m, c->shape, strict, lg::Part::EVAL), !strict, cubin, log)))
+        return c->fail(rc, log);
+    if ((rc = lg::compile_program(lg::compose_source(m, c->shape, strict, lg::Part::SET), false, cubin_set, log)))
+        return c->fail(rc, log);
 
     if ((rc = c->cuda(cudaSetDevice(c->device), "cudaSetDevice"))) return rc;
     if ((rc = c->cuda(cudaFree(nullptr), "CUDA context"))) return rc;
     c->drv = driver();
     if (!c->drv) return c->fail(LG_ERR_CUDA, "CUDA driver entry points unavailable");
-    if ((rc = c->drvcall(c->drv->moduleLoadData(&c->mod, cubin.data()), "cuModuleLoadData"))) return rc;
+    if ((rc = c->drvcall(c->drv->moduleLoadData(&c->mod, cubin.data()), "cuModuleLoadData")) ||
+        (rc = c->drvcall(c->drv->moduleLoadData(&c->mod_set, cubin_set.data()), "cuModuleLoadData")))
+        return rc;
+    if ((rc = c->drvcall(c->drv->moduleGetFunction(&c->f_setp, c->mod_set, "lg_set_params_kernel"),
+                         "lg_set_params_kernel")))
+        return rc;
     struct {
         CUfunction* f;
         const char* n;
         bool need;
-    } fns[] = {{&c->f_setp, "lg_set_params_kernel", true}, {&c->f_rraw, "lg_render_raw", true},
-               {&c->f_rchi2, "lg_render_chi2", true},      {&c->f_rdump, "lg_render_dump", true},
-               {&c->f_finish, "lg_finish", true},          {&c->f_cchi2, "lg_conv_chi2", c->psf},
-               {&c->f_cdump, "lg_conv_dump", c->psf}};
+    } fns[] = {{&c->f_rraw, "lg_render_raw", true},  {&c->f_rchi2, "lg_render_chi2", true},
+               {&c->f_rdump, "lg_render_dump", true}, {&c->f_finish, "lg_finish", true},
+               {&c->f_cchi2, "lg_conv_chi2", c->psf}, {&c->f_cdump, "lg_conv_dump", c->psf}};
     for (auto& f : fns)
         if (f.need && (rc = c->drvcall(c->drv->moduleGetFunction(f.f, c->mod, f.n), f.n))) return rc;
     CUdeviceptr gp;
     size_t gb;
-    if ((rc = c->drvcall(c->drv->moduleGetGlobal(&gp, &gb, c->mod, "lg_model_bytes"), "lg_model_bytes"))) return rc;
+    if ((rc = c->drvcall(c->drv->moduleGetGlobal(&gp, &gb, c->mod_set, "lg_model_bytes"), "lg_model_bytes")))
+        return rc;
     unsigned mb = 0;
     if ((rc = c->cuda(cudaMemcpy(&mb, (void*)gp, sizeof mb, cudaMemcpyDeviceToHost), "model size"))) return rc;
     c->model_bytes = mb;
@@ -410,7 +421,8 @@ int lg_compile_check(const lg_image_desc* image, const lg_object_desc* objs, int
         const bool strict = opts && (opts->flags & LG_FLAG_STRICT_FP);
         std::vector<char> cubin;
         lg::Shape s = choose_shape(m);
-        rc = lg::compile_program(lg::compose_source(m, s, strict), strict, cubin, err);
+        rc = lg::compile_program(lg::compose_source(m, s, strict, lg::Part::EVAL), !strict, cubin, err);
+        if (!rc) rc = lg::compile_program(lg::compose_source(m, s, strict, lg::Part::SET), false, cubin, err);
     }
     if (log && log_size) {
         std::snprintf(log, log_size, "%s", err.c_str());

@@ -32,6 +32,8 @@ int register_plugin(const lg_plugin_desc* d, std::string& err);
 // Device sources embedded at build time.
 const char* prelude_source();
 const char* kernels_source();
+const char* set_kernel_source();
+const char* crmath_source();
 
 // ------------------------------------------------------------------- priors
 // Lensed's prior plugins (src/prior.c:47-51): delta (pseudo), unif, norm.
@@ -103,8 +105,12 @@ struct Shape {
     int ctx = 32, cty = 32, cr = 8; // convolution tile and outputs per thread
 };
 
-// Compose the NVRTC source of a model and compile it to a cubin for sm_103a.
-std::string compose_source(const Model& m, const Shape& s, bool strict);
-int compile_program(const std::string& src, bool strict, std::vector<char>& cubin, std::string& log);
+// Compose the NVRTC sources of a model and compile them to cubins for
+// sm_103a.  The set_params module always uses the double-evaluated
+// elementary functions and no FMA contraction; the evaluation module uses
+// them only in strict mode.
+enum class Part { SET, EVAL };
+std::string compose_source(const Model& m, const Shape& s, bool strict, Part part);
+int compile_program(const std::string& src, bool fmad, std::vector<char>& cubin, std::string& log);
 
 }  // namespace lg

@@ -113,21 +113,37 @@ void emit_set_params(std::ostringstream& o, const Model& m)
 
 }  // namespace
 
-std::string compose_source(const Model& m, const Shape& s, bool strict)
+std::string compose_source(const Model& m, const Shape& s, bool strict, Part part)
 {
+    const bool set = part == Part::SET;
     std::ostringstream o;
-    o << "// Lensed likelihood program composed for:";
+    o << "// Lensed likelihood program (" << (set ? "set_params" : "evaluation") << " module) composed for:";
     for (const auto& ob : m.objs) o << " " << ob.id << "=" << ob.plugin->name;
     o << "\n// image " << m.width << "x" << m.height << ", rule " << m.rule->name << " (" << m.rule->size
       << " points), PSF " << m.psfw << "x" << m.psfh << (strict ? ", strict FP" : "") << "\n\n";
     o << "#define LG_RT " << s.rt << "\n#define LG_RPPT " << s.rppt << "\n";
     o << "#define LG_CTX " << s.ctx << "\n#define LG_CTY " << s.cty << "\n#define LG_CR " << s.cr << "\n\n";
     o << prelude_source() << "\n";
+    if (set || strict) o << crmath_source() << "\n";
     std::set<std::string> done;
     for (const auto& ob : m.objs) emit_plugin(o, ob.plugin, done);
 
     o << "// ---- model section\n";
     o << "#define LG_W " << m.width << "\n#define LG_H " << m.height << "\n#define LG_N (LG_W * LG_H)\n";
+    o << "#define LG_NPARS " << m.pars.size() << "\n";
+    o << "struct lg_model {\n";
+    for (size_t i = 0; i < m.objs.size(); ++i)
+        o << "    lg_data_" << m.objs[i].plugin->name << " o" << i << ";  // " << m.objs[i].id << "\n";
+    o << "};\n\n";
+    if (set) {
+        emit_set_params(o, m);
+        // parameter upload order: params[pmap[i]] = cube[i] (src/nested.c:70-71)
+        o << "LG_DEV void lg_load_params(const double* __restrict__ src, float* p)\n{\n";
+        for (size_t i = 0; i < m.pmap.size(); ++i) o << "    p[" << m.pmap[i] << "] = (float)src[" << i << "];\n";
+        o << "}\n\n";
+        o << set_kernel_source() << "\n";
+        return o.str();
+    }
     // pixel coordinate system, shifted by half a pixel for even PSF sizes
     // (src/lensed.c:871-891); stored in float as the reference's float4 pcs
     double rx = m.pcs[0], ry = m.pcs[1];
@@ -157,22 +173,12 @@ std::string compose_source(const Model& m, const Shape& s, bool strict)
     } else {
         o << "#define LG_HAS_PSF 0\n";
     }
-    o << "#define LG_NPARS " << m.pars.size() << "\n\n";
-    o << "struct lg_model {\n";
-    for (size_t i = 0; i < m.objs.size(); ++i)
-        o << "    lg_data_" << m.objs[i].plugin->name << " o" << i << ";  // " << m.objs[i].id << "\n";
-    o << "};\n\n";
     emit_compute(o, m);
-    emit_set_params(o, m);
-    // parameter upload order: params[pmap[i]] = cube[i] (src/nested.c:70-71)
-    o << "LG_DEV void lg_load_params(const double* __restrict__ src, float* p)\n{\n";
-    for (size_t i = 0; i < m.pmap.size(); ++i) o << "    p[" << m.pmap[i] << "] = (float)src[" << i << "];\n";
-    o << "}\n\n";
     o << kernels_source() << "\n";
     return o.str();
 }
 
-int compile_program(const std::string& src, bool strict, std::vector<char>& cubin, std::string& log)
+int compile_program(const std::string& src, bool fmad, std::vector<char>& cubin, std::string& log)
 {
     nvrtcProgram prog;
     nvrtcResult r = nvrtcCreateProgram(&prog, src.c_str(), "lensed_model.cu", 0, nullptr, nullptr);
@@ -183,7 +189,7 @@ int compile_program(const std::string& src, bool strict, std::vector<char>& cubi
     std::vector<const char*> opts = {"--gpu-architecture=sm_103a", "-std=c++17", "--generate-line-info",
                                      "--prec-div=true", "--prec-sqrt=true", "--ftz=false",
                                      "-diag-suppress=177"};
-    opts.push_back(strict ? "--fmad=false" : "--fmad=true");
+    opts.push_back(fmad ? "--fmad=true" : "--fmad=false");
     r = nvrtcCompileProgram(prog, (int)opts.size(), opts.data());
     size_t n = 0;
     nvrtcGetProgramLogSize(prog, &n);

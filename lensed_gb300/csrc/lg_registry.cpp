@@ -21,6 +21,8 @@ namespace lg {
 
 const char* prelude_source() { return LG_EMBED_PRELUDE; }
 const char* kernels_source() { return LG_EMBED_KERNELS; }
+const char* set_kernel_source() { return LG_EMBED_SET_KERNEL; }
+const char* crmath_source() { return LG_EMBED_CRMATH; }
 
 namespace {
 

@@ -4,7 +4,7 @@
 //   LG_Q                      quadrature points; lg_qq[], lg_ww[] (constant)
 //   LG_RX, LG_RY, LG_SX, LG_SY pixel coordinate system (after the even-PSF shift)
 //   LG_HAS_PSF, LG_PSF_W, LG_PSF_H, lg_psf[] (normalised PSF, constant)
-//   LG_NPARS, lg_model, lg_compute(), lg_set_params(), lg_load_params()
+//   LG_NPARS, lg_model, lg_compute()
 // and the launch-shape parameters LG_RT, LG_RPPT (render) and LG_CTX, LG_CTY,
 // LG_CR (convolution).
 //
@@ -51,22 +51,6 @@ LG_DEV double lg_block_sum(double v, double* red)
         for (int i = 0; i < NT / 32; ++i) s += red[i];
     }
     return s;
-}
-
-// ------------------------------------------------------------ set_params --
-// One thread per candidate: physical parameters (pmap order, double) ->
-// object data.  src/nested.c:67-77 and the generated set_params of
-// src/kernel.c:114-150.
-extern "C" __global__ void lg_set_params_kernel(const double* __restrict__ params, int B,
-                                                lg_model* __restrict__ models)
-{
-    const int b = blockIdx.x * blockDim.x + threadIdx.x;
-    if (b >= B) return;
-    float p[LG_NPARS];
-    lg_load_params(params + (size_t)b * LG_NPARS, p);
-    lg_model m;
-    lg_set_params(m, p);
-    models[b] = m;
 }
 
 // ---------------------------------------------------------------- render --
@@ -276,7 +260,7 @@ extern "C" __global__ void __launch_bounds__(256)
 }
 
 // Sizes the host reads back after loading the module.
-extern "C" __device__ const unsigned lg_model_bytes = sizeof(lg_model);
+extern "C" __device__ const unsigned lg_model_bytes_eval = sizeof(lg_model);
 extern "C" __device__ const int lg_render_tiles = LG_RTILES;
 #if LG_HAS_PSF
 extern "C" __device__ const int lg_conv_tiles = LG_CTILES;

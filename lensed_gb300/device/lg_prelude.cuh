@@ -58,6 +58,42 @@ LG_DEV mat22 operator/(mat22 m, float s) { return make_mat22(m.a / s, m.b / s, m
 // matrix-vector product: (dot(row0, v), dot(row1, v))
 LG_DEV float2 mv22(mat22 m, float2 v) { return make_float2(m.a * v.x + m.b * v.y, m.c * v.x + m.d * v.y); }
 
+// Correctly rounded single-precision elementary functions: evaluated in
+// double precision and rounded once to float.  set_params always uses them
+// (and strict mode uses them per ray), so that the FP32 result is defined by
+// IEEE arithmetic alone and not by a particular float math library.
+LG_DEV float lg_cr_expf(float x) { return (float)exp((double)x); }
+LG_DEV float lg_cr_exp2f(float x) { return (float)exp2((double)x); }
+LG_DEV float lg_cr_expm1f(float x) { return (float)expm1((double)x); }
+LG_DEV float lg_cr_logf(float x) { return (float)log((double)x); }
+LG_DEV float lg_cr_log2f(float x) { return (float)log2((double)x); }
+LG_DEV float lg_cr_log10f(float x) { return (float)log10((double)x); }
+LG_DEV float lg_cr_log1pf(float x) { return (float)log1p((double)x); }
+LG_DEV float lg_cr_powf(float x, float y) { return (float)pow((double)x, (double)y); }
+LG_DEV float lg_cr_sinf(float x) { return (float)sin((double)x); }
+LG_DEV float lg_cr_cosf(float x) { return (float)cos((double)x); }
+LG_DEV float lg_cr_tanf(float x) { return (float)tan((double)x); }
+LG_DEV void lg_cr_sincosf(float x, float* s, float* c)
+{
+    *s = (float)sin((double)x);
+    *c = (float)cos((double)x);
+}
+LG_DEV float lg_cr_asinf(float x) { return (float)asin((double)x); }
+LG_DEV float lg_cr_acosf(float x) { return (float)acos((double)x); }
+LG_DEV float lg_cr_atanf(float x) { return (float)atan((double)x); }
+LG_DEV float lg_cr_atan2f(float y, float x) { return (float)atan2((double)y, (double)x); }
+LG_DEV float lg_cr_sinhf(float x) { return (float)sinh((double)x); }
+LG_DEV float lg_cr_coshf(float x) { return (float)cosh((double)x); }
+LG_DEV float lg_cr_tanhf(float x) { return (float)tanh((double)x); }
+LG_DEV float lg_cr_asinhf(float x) { return (float)asinh((double)x); }
+LG_DEV float lg_cr_acoshf(float x) { return (float)acosh((double)x); }
+LG_DEV float lg_cr_atanhf(float x) { return (float)atanh((double)x); }
+LG_DEV float lg_cr_tgammaf(float x) { return (float)tgamma((double)x); }
+LG_DEV float lg_cr_lgammaf(float x) { return (float)lgamma((double)x); }
+LG_DEV float lg_cr_cbrtf(float x) { return (float)cbrt((double)x); }
+LG_DEV float lg_cr_erff(float x) { return (float)erf((double)x); }
+LG_DEV float lg_cr_erfcf(float x) { return (float)erfc((double)x); }
+
 // Apply a lens plane's summed deflection to a ray if it is finite; rays with
 // a non-finite deflection are sent far away (src/kernel.c:86-91).
 LG_DEV void lg_deflect(float2& y, float2 a)

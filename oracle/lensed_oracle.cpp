@@ -104,6 +104,34 @@ template <class T> struct Obj {
 // FP32 oracle, the same decimal in double precision for the FP64 oracle.
 template <class T> inline T lit(float f, double d) { return sizeof(T) == 4 ? T(f) : T(d); }
 
+// Elementary functions.  CR: evaluated in double precision and rounded
+// once to T (correctly rounded except within a double ulp of a float
+// rounding boundary); LM: the C library's function in T itself.  set_params
+// always uses CR; the per-ray evaluation uses CR in strict mode (the same
+// semantics as the GPU's strict mode) and LM otherwise.
+template <class T> struct CR {
+    static T exp(T x) { return T(std::exp((double)x)); }
+    static T log(T x) { return T(std::log((double)x)); }
+    static T pow(T x, T y) { return T(std::pow((double)x, (double)y)); }
+    static T sin(T x) { return T(std::sin((double)x)); }
+    static T cos(T x) { return T(std::cos((double)x)); }
+    static T atan(T x) { return T(std::atan((double)x)); }
+    static T atanh(T x) { return T(std::atanh((double)x)); }
+    static T atan2(T y, T x) { return T(std::atan2((double)y, (double)x)); }
+    static T tgamma(T x) { return T(std::tgamma((double)x)); }
+};
+int g_cr_eval = 1;
+template <class T> struct EM {
+    static T exp(T x) { return g_cr_eval ? CR<T>::exp(x) : std::exp(x); }
+    static T log(T x) { return g_cr_eval ? CR<T>::log(x) : std::log(x); }
+    static T pow(T x, T y) { return g_cr_eval ? CR<T>::pow(x, y) : std::pow(x, y); }
+    static T sin(T x) { return g_cr_eval ? CR<T>::sin(x) : std::sin(x); }
+    static T cos(T x) { return g_cr_eval ? CR<T>::cos(x) : std::cos(x); }
+    static T atan(T x) { return g_cr_eval ? CR<T>::atan(x) : std::atan(x); }
+    static T atanh(T x) { return g_cr_eval ? CR<T>::atanh(x) : std::atanh(x); }
+    static T atan2(T y, T x) { return g_cr_eval ? CR<T>::atan2(y, x) : std::atan2(y, x); }
+};
+
 template <class T> using DeflFn = V2<T> (*)(const Obj<T>&, V2<T>);
 template <class T> using BrightFn = T (*)(const Obj<T>&, V2<T>);
 template <class T> using SetFn = void (*)(Obj<T>&, const T*);
@@ -139,13 +167,13 @@ template <class T> V2<T> defl_sie(const Obj<T>& o, V2<T> x)
     x = x - o.x;
     V2<T> y = mv22(o.m, x);
     T r = o.e / std::sqrt(o.q2 * y.x * y.x + y.y * y.y);
-    y = o.d * V2<T>{std::atan(y.x * r), std::atanh(y.y * r)};
+    y = o.d * V2<T>{EM<T>::atan(y.x * r), EM<T>::atanh(y.y * r)};
     return mv22(o.w, y);
 }
 template <class T> void set_sie_common(Obj<T>& o, T x, T y, T r, T q, T pa)
 {
-    T c = std::cos(pa * K<T>::DEG2RAD);
-    T s = std::sin(pa * K<T>::DEG2RAD);
+    T c = CR<T>::cos(pa * K<T>::DEG2RAD);
+    T s = CR<T>::sin(pa * K<T>::DEG2RAD);
     o.x = {x, y};
     o.m = {c, s, -s, c};
     o.w = {c, -s, s, c};
@@ -161,13 +189,13 @@ template <class T> V2<T> defl_sie_plus_shear(const Obj<T>& o, V2<T> x)
     x = x - o.x;
     V2<T> y = mv22(o.m, x);
     T r = o.e / std::sqrt(o.q2 * y.x * y.x + y.y * y.y);
-    y = o.d * V2<T>{std::atan(y.x * r), std::atanh(y.y * r)};
+    y = o.d * V2<T>{EM<T>::atan(y.x * r), EM<T>::atanh(y.y * r)};
     return mv22(o.w, y) + mv22(o.g, x);
 }
 template <class T> void set_sie_plus_shear(Obj<T>& o, const T* p)
 {
-    T c = std::cos(p[4] * K<T>::DEG2RAD);
-    T s = std::sin(p[4] * K<T>::DEG2RAD);
+    T c = CR<T>::cos(p[4] * K<T>::DEG2RAD);
+    T s = CR<T>::sin(p[4] * K<T>::DEG2RAD);
     o.x = {p[0], p[1]};
     o.m = {c, s, -s, c};
     o.w = {c, -s, s, c};
@@ -183,13 +211,13 @@ template <class T> V2<T> defl_nsie(const Obj<T>& o, V2<T> x)
     x = x - o.x;
     V2<T> y = mv22(o.m, x);
     T r = std::sqrt(o.q2 * y.x * y.x + y.y * y.y);
-    y = o.d * V2<T>{std::atan(y.x * o.e / (o.rc + r)), std::atanh(y.y * o.e / (o.rc * o.q2 + r))};
+    y = o.d * V2<T>{EM<T>::atan(y.x * o.e / (o.rc + r)), EM<T>::atanh(y.y * o.e / (o.rc * o.q2 + r))};
     return mv22(o.w, y);
 }
 template <class T> void set_nsie(Obj<T>& o, const T* p)
 {
-    T c = std::cos(p[5] * K<T>::DEG2RAD);
-    T s = std::sin(p[5] * K<T>::DEG2RAD);
+    T c = CR<T>::cos(p[5] * K<T>::DEG2RAD);
+    T s = CR<T>::sin(p[5] * K<T>::DEG2RAD);
     T q = p[4];
     o.x = {p[0], p[1]};
     o.m = {c, s, -s, c};
@@ -215,9 +243,9 @@ template <class T> V2<T> epl_core(const Obj<T>& o, V2<T> x)
     const T TT = T(2) - o.tt;
     const T f = o.f;
     T r = length(x);
-    T phi = std::atan2(x.y, x.x);
-    T s = std::sin(phi), c = std::cos(phi);
-    T s2 = std::sin(T(2) * phi), c2 = std::cos(T(2) * phi);
+    T phi = EM<T>::atan2(x.y, x.x);
+    T s = EM<T>::sin(phi), c = EM<T>::cos(phi);
+    T s2 = EM<T>::sin(T(2) * phi), c2 = EM<T>::cos(T(2) * phi);
     M22<T> R = {c2, -s2, s2, c2};
     V2<T> A = {c, s};
     V2<T> a = A;
@@ -226,13 +254,13 @@ template <class T> V2<T> epl_core(const Obj<T>& o, V2<T> x)
         A = coef * mv22(R, A);
         a = a + A;
     }
-    a = (o.n * std::pow(r, T(1) - o.tt)) * a;
+    a = (o.n * EM<T>::pow(r, T(1) - o.tt)) * a;
     return mv22(o.w, a);
 }
 template <class T> V2<T> defl_epl(const Obj<T>& o, V2<T> x) { return epl_core(o, mv22(o.m, x - o.x)); }
 template <class T> void set_epl_common(Obj<T>& o, const T* p)
 {
-    T s = std::sin(p[5] * K<T>::DEG2RAD), c = std::cos(p[5] * K<T>::DEG2RAD);
+    T s = CR<T>::sin(p[5] * K<T>::DEG2RAD), c = CR<T>::cos(p[5] * K<T>::DEG2RAD);
     T r = p[2], q = p[4];
     o.x = {p[0], p[1]};
     o.m = (T(1) / r / std::sqrt(q)) * M22<T>{q * c, q * s, -s, c};
@@ -260,7 +288,7 @@ template <class T> void set_epl_plus_shear(Obj<T>& o, const T* p)
 template <class T> T bright_sersic(const Obj<T>& o, V2<T> x)
 {
     V2<T> y = mv22(o.t, x - o.x);
-    return std::exp(o.log0 - std::exp(o.log1 + o.mexp * std::log(dot(y, y))));
+    return EM<T>::exp(o.log0 - EM<T>::exp(o.log1 + o.mexp * EM<T>::log(dot(y, y))));
 }
 template <class T> void set_sersic(Obj<T>& o, const T* p)
 {
@@ -271,13 +299,13 @@ template <class T> void set_sersic(Obj<T>& o, const T* p)
               + T(131) / (T(1148175) * (n * n * n)) - T(2194697) / (T(30690717750.0) * (n * n * n * n))
         : lit<T>(0.01945f, 0.01945) - lit<T>(0.8902f, 0.8902) * n + lit<T>(10.95f, 10.95) * (n * n)
               - lit<T>(19.67f, 19.67) * (n * n * n) + lit<T>(13.43f, 13.43) * (n * n * n * n);
-    T c = std::cos(a * K<T>::DEG2RAD);
-    T s = std::sin(a * K<T>::DEG2RAD);
+    T c = CR<T>::cos(a * K<T>::DEG2RAD);
+    T s = CR<T>::sin(a * K<T>::DEG2RAD);
     o.x = {x, y};
     o.t = M22<T>{q * c, q * s, -s, c} / std::sqrt(q);
-    o.log0 = -lit<T>(0.4f, 0.4) * mag * K<T>::LOG_10 + T(2) * n * std::log(b) - K<T>::LOG_PI - T(2) * std::log(r)
-           - std::log(std::tgamma(T(2) * n + T(1)));
-    o.log1 = std::log(b) - std::log(r) / n;
+    o.log0 = -lit<T>(0.4f, 0.4) * mag * K<T>::LOG_10 + T(2) * n * CR<T>::log(b) - K<T>::LOG_PI - T(2) * CR<T>::log(r)
+           - CR<T>::log(CR<T>::tgamma(T(2) * n + T(1)));
+    o.log1 = CR<T>::log(b) - CR<T>::log(r) / n;
     o.mexp = T(0.5) / n;
 }
 
@@ -287,60 +315,60 @@ template <class T> void set_sersic_old(Obj<T>& o, const T* p)
 {
     T x = p[0], y = p[1], r = p[2], mag = p[3], n = p[4], q = p[5], a = p[6];
     T b = lit<T>(1.9992f, 1.9992) * n - lit<T>(0.3271f, 0.3271);
-    T c = std::cos(a * K<T>::DEG2RAD);
-    T s = std::sin(a * K<T>::DEG2RAD);
+    T c = CR<T>::cos(a * K<T>::DEG2RAD);
+    T s = CR<T>::sin(a * K<T>::DEG2RAD);
     o.x = {x, y};
     o.t = M22<T>{q * c, q * s, -s, c} / std::sqrt(q);
-    o.log0 = -lit<T>(0.4f, 0.4) * mag * K<T>::LOG_10 + T(2) * n * std::log(b) - K<T>::LOG_PI - T(2) * std::log(r)
-           - std::log(std::tgamma(T(2) * n + T(1)));
-    o.log1 = std::log(b) - std::log(r) / n;
+    o.log0 = -lit<T>(0.4f, 0.4) * mag * K<T>::LOG_10 + T(2) * n * CR<T>::log(b) - K<T>::LOG_PI - T(2) * CR<T>::log(r)
+           - CR<T>::log(CR<T>::tgamma(T(2) * n + T(1)));
+    o.log1 = CR<T>::log(b) - CR<T>::log(r) / n;
     o.mexp = T(0.5) / n;
 }
 
 // objects/exponential.cl:21-43
 template <class T> T bright_exponential(const Obj<T>& o, V2<T> x)
 {
-    return o.norm * std::exp(-length(mv22(o.t, x - o.x)) / o.rs);
+    return o.norm * EM<T>::exp(-length(mv22(o.t, x - o.x)) / o.rs);
 }
 template <class T> void set_exponential(Obj<T>& o, const T* p)
 {
-    T c = std::cos(p[5] * K<T>::DEG2RAD), s = std::sin(p[5] * K<T>::DEG2RAD);
+    T c = CR<T>::cos(p[5] * K<T>::DEG2RAD), s = CR<T>::sin(p[5] * K<T>::DEG2RAD);
     T rs = p[2], q = p[4];
     o.x = {p[0], p[1]};
     o.t = {q * c, q * s, -s, c};
     o.rs = rs;
-    o.norm = std::exp(-lit<T>(0.4f, 0.4) * p[3] * K<T>::LOG_10) * T(0.5) / K<T>::PI / rs / rs / q;
+    o.norm = CR<T>::exp(-lit<T>(0.4f, 0.4) * p[3] * K<T>::LOG_10) * T(0.5) / K<T>::PI / rs / rs / q;
 }
 
 // objects/devauc.cl:26-48
 template <class T> T bright_devauc(const Obj<T>& o, V2<T> x)
 {
-    return o.norm * std::exp(-K<T>::DEVAUC_B * std::sqrt(std::sqrt(length(mv22(o.t, x - o.x)) / o.rs)));
+    return o.norm * EM<T>::exp(-K<T>::DEVAUC_B * std::sqrt(std::sqrt(length(mv22(o.t, x - o.x)) / o.rs)));
 }
 template <class T> void set_devauc(Obj<T>& o, const T* p)
 {
-    T c = std::cos(p[5] * K<T>::DEG2RAD), s = std::sin(p[5] * K<T>::DEG2RAD);
+    T c = CR<T>::cos(p[5] * K<T>::DEG2RAD), s = CR<T>::sin(p[5] * K<T>::DEG2RAD);
     T r = p[2], q = p[4];
     o.x = {p[0], p[1]};
     o.t = {q * c, q * s, -s, c};
     o.rs = r;
-    o.norm = std::exp(-lit<T>(0.4f, 0.4) * p[3] * K<T>::LOG_10) / K<T>::PI / r / r / q * K<T>::DEVAUC_C;
+    o.norm = CR<T>::exp(-lit<T>(0.4f, 0.4) * p[3] * K<T>::LOG_10) / K<T>::PI / r / r / q * K<T>::DEVAUC_C;
 }
 
 // objects/gauss.cl:21-41
 template <class T> T bright_gauss(const Obj<T>& o, V2<T> x)
 {
     V2<T> y = mv22(o.t, x - o.x);
-    return o.norm * std::exp(-T(0.5) * dot(y, y) / o.s2);
+    return o.norm * EM<T>::exp(-T(0.5) * dot(y, y) / o.s2);
 }
 template <class T> void set_gauss(Obj<T>& o, const T* p)
 {
-    T c = std::cos(p[5] * K<T>::DEG2RAD), s = std::sin(p[5] * K<T>::DEG2RAD);
+    T c = CR<T>::cos(p[5] * K<T>::DEG2RAD), s = CR<T>::sin(p[5] * K<T>::DEG2RAD);
     T sigma = p[2], q = p[4];
     o.x = {p[0], p[1]};
     o.t = {q * c, q * s, -s, c};
     o.s2 = sigma * sigma;
-    o.norm = std::exp(-lit<T>(0.4f, 0.4) * p[3] * K<T>::LOG_10) * T(0.5) / K<T>::PI / o.s2 / q;
+    o.norm = CR<T>::exp(-lit<T>(0.4f, 0.4) * p[3] * K<T>::LOG_10) * T(0.5) / K<T>::PI / o.s2 / q;
 }
 
 // objects/sky.cl:16-25 (evaluated at the unlensed position)
@@ -441,6 +469,13 @@ template <class T> struct Model {
     // image-plane prior deflection of (x, y) through earlier lens planes.
     void set_params(const T* params, std::vector<Obj<T>>& d) const
     {
+        // image-plane deflections inside set_params use the double-evaluated
+        // functions too, whatever the per-ray mode
+        struct Restore {
+            int v;
+            ~Restore() { g_cr_eval = v; }
+        } restore{g_cr_eval};
+        g_cr_eval = 1;
         d.assign(nobjs, Obj<T>{});
         int trigger = 0, plane = 0;
         std::vector<T> args;
@@ -605,6 +640,11 @@ int lo_plugin_index(const char* name)
         if (std::strcmp(PLUGINS[i].name, name) == 0) return i;
     return -1;
 }
+// Per-ray elementary functions of the FP32 oracle: 1 = double-evaluated
+// (strict semantics, the default), 0 = the C library's float functions.
+// Process-wide.
+void lo_set_eval_cr(int on) { g_cr_eval = on ? 1 : 0; }
+
 int lo_plugin_npars(int id) { return (id >= 0 && id < NPLUGINS) ? PLUGINS[id].npars : -1; }
 int lo_plugin_kind(int id) { return (id >= 0 && id < NPLUGINS) ? PLUGINS[id].kind : -1; }
 

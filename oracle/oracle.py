@@ -10,6 +10,9 @@ from ``oracle/lensed_oracle.cpp`` on first use if it is missing.
   width, height, pcs, rule (QuadRule), psf (2-D array or None),
   image / weight (2-D arrays, needed for logL)
   precision 32 (FP32 oracle) or 64 (FP64 oracle)
+  math      FP32 per-ray elementary functions: "cr" (evaluated in double and
+            rounded once: the strict semantics, the default) or "libm" (the C
+            library's float functions).  set_params always uses "cr".
 """
 from __future__ import annotations
 
@@ -55,6 +58,7 @@ def lib():
         L.lo_set_threads.argtypes = [C.c_void_p, C.c_int]
         L.lo_render.argtypes = [C.c_void_p, dp, dp, dp, dp]
         L.lo_loglike_batch.argtypes = [C.c_void_p, dp, C.c_int, dp]
+        L.lo_set_eval_cr.argtypes = [C.c_int]
         L.lo_make_weight.argtypes = [fp, C.c_long, fp, fp, C.c_double, C.c_double, fp, ip, fp]
         _lib = L
     return _lib
@@ -75,7 +79,11 @@ def plugin_npars(name: str) -> int:
 class Oracle:
     def __init__(self, objects: Sequence, width: int, height: int, rule, pcs=(1.0, 1.0, 1.0, 1.0),
                  psf: Optional[np.ndarray] = None, image: Optional[np.ndarray] = None,
-                 weight: Optional[np.ndarray] = None, precision: int = 32, threads: int = 1):
+                 weight: Optional[np.ndarray] = None, precision: int = 32, threads: int = 1,
+                 math: str = "cr"):
+        if math not in ("cr", "libm"):
+            raise ValueError("math must be 'cr' or 'libm'")
+        self.math = math
         L = lib()
         names, ipps = [], []
         for o in objects:
@@ -123,6 +131,7 @@ class Oracle:
         """Return (value, error, convolved-or-None) as (H, W) float64 arrays."""
         p = np.ascontiguousarray(params, dtype=np.float64)
         assert p.size == self.npars
+        lib().lo_set_eval_cr(1 if self.math == "cr" else 0)
         v = np.zeros(self.N); e = np.zeros(self.N)
         c = np.zeros(self.N) if self.has_psf else None
         lib().lo_render(self.h, _ptr(p, C.c_double), _ptr(v, C.c_double), _ptr(e, C.c_double), _ptr(c, C.c_double))
@@ -134,6 +143,7 @@ class Oracle:
         p = np.ascontiguousarray(np.atleast_2d(params), dtype=np.float64)
         assert p.shape[1] == self.npars
         out = np.zeros(p.shape[0])
+        lib().lo_set_eval_cr(1 if self.math == "cr" else 0)
         rc = lib().lo_loglike_batch(self.h, _ptr(p, C.c_double), p.shape[0], _ptr(out, C.c_double))
         if rc:
             raise ValueError("oracle: image and weight are needed for logL")

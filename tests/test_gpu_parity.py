@@ -1,6 +1,12 @@
 """Parity of the CUDA path (through the C ABI) with the CPU oracle.
 
-Tolerances (FP32 ray-shooting, FP64 reduction):
+The FP32 reference semantics is IEEE single-precision arithmetic in the
+reference's operation order with elementary functions evaluated in double
+and rounded once (oracle math="cr").  set_params always follows it on the
+GPU.  Strict mode (LG_FLAG_STRICT_FP) follows it per ray too and must match
+the oracle to the last bit except for rare double-rounding coincidences:
+images within 2 ulp (1.2e-7 relative), |dlogL| <= 1e-6.  The default fast
+mode uses CUDA's single-precision functions per ray; its tolerances:
   * model images: relative error <= 1e-5 on pixels above 1e-6 of the peak,
     absolute error <= 1e-6 * peak below that floor.  Where the FP32 oracle is
     itself further than 1e-5 from the FP64 oracle (ill-conditioned profiles,
@@ -81,7 +87,23 @@ def test_render_matches_oracle_per_plugin(native, case):
     v64 = Oracle(plugins, W, H, quadrature.rule("gm75"), pcs=pcs, precision=64).render(params)[0]
     assert_image_close(raw, v, plugins, want64=v64)
     assert np.array_equal(model, raw)  # no PSF: the model is the raw render
-    assert np.abs(err - e).max() <= 1e-5 * np.abs(v).max() + 1e-7, plugins
+    tol = max(IMG_REL, 2 * image_err(v, v64)[0])
+    assert np.abs(err - e).max() <= tol * np.abs(v).max() + 1e-7, plugins
+
+
+@pytest.mark.parametrize("case", range(len(PLUGIN_CASES)))
+def test_strict_render_matches_oracle_bitwise(native, case):
+    plugins, params = PLUGIN_CASES[case]
+    W, H = 41, 37
+    pcs = (2.0, -1.0, 1.0, 1.0)
+    ctx = make_ctx(plugins, W, H, rule="gm75", pcs=pcs, flags=lg.LG_FLAG_STRICT_FP)
+    _, raw, err = ctx.render(ctx.to_map_order(params))
+    v, e, _ = Oracle(plugins, W, H, quadrature.rule("gm75"), pcs=pcs, precision=32).render(params)
+    same = raw == v.astype(np.float32)
+    rel = np.abs(raw - v) / np.maximum(np.abs(v), 1e-30)
+    print(f"strict {plugins}: {100 * same.mean():.4f}% identical pixels, max rel {rel.max():.3g}")
+    assert rel.max() <= 1.2e-7 * 2
+    assert same.mean() >= 0.999
 
 
 def test_reference_images_on_gpu(native, golden):
@@ -127,22 +149,38 @@ def _loglike_case(system, B, seed=0):
     return ctx, cand, got, want32, want64
 
 
+def _report(name, got, w32, w64):
+    d32 = np.abs(got - w32)
+    print(f"{name}: |dlogL| vs FP32 oracle max {d32.max():.3g} (per candidate {np.array2string(d32, precision=2)}), "
+          f"vs FP64 oracle max {np.abs(got - w64).max():.3g}, FP32 oracle vs FP64 max {np.abs(w32 - w64).max():.3g}")
+    return d32
+
+
 def test_loglike_small_workload(native):
     ctx, cand, got, w32, w64 = _loglike_case(workloads.small(), 16)
-    d32 = np.abs(got - w32).max()
-    print(f"small: max|dlogL| vs FP32 oracle {d32:.3g}, vs FP64 oracle {np.abs(got - w64).max():.3g}, "
-          f"FP32 oracle vs FP64 {np.abs(w32 - w64).max():.3g}")
-    assert d32 <= LOGL_ABS
+    d32 = _report("small fast", got, w32, w64)
+    assert d32.max() <= LOGL_ABS
 
 
 def test_loglike_config2_full_size(native):
     """256^2, SIE+shear, bulge + disk + sky, 25x25 PSF, 25-point rule, 10% mask."""
-    ctx, cand, got, w32, w64 = _loglike_case(workloads.config2(), 6)
-    d32 = np.abs(got - w32).max()
-    print(f"config2: logL {got[:3]} max|dlogL| vs FP32 oracle {d32:.3g}, vs FP64 oracle "
-          f"{np.abs(got - w64).max():.3g}, FP32 oracle vs FP64 {np.abs(w32 - w64).max():.3g}")
-    assert d32 <= LOGL_ABS
+    ctx, cand, got, w32, w64 = _loglike_case(workloads.config2(), 8)
+    d32 = _report("config2 fast", got, w32, w64)
+    assert d32.max() <= LOGL_ABS
     assert ctx.masked == int((ctx._weight == 0).sum())
+
+
+@pytest.mark.parametrize("name", ["small", "config2"])
+def test_loglike_strict_mode_bitwise(native, name):
+    s = getattr(workloads, name)()
+    ctx = lg.Context(s.image, s.weight, s.objects, psf=s.psf, rule=s.rule, max_batch=8, flags=lg.LG_FLAG_STRICT_FP)
+    cand = workloads.draw_candidates(s, 8, seed=5)
+    got = ctx.eval_batch(ctx.to_map_order(cand))
+    o = Oracle(s.plugins, s.width, s.height, quadrature.rule(s.rule), psf=s.psf, image=s.image, weight=s.weight,
+               precision=32, threads=16)
+    want = o.loglike(cand)
+    d = _report(f"{name} strict", got, want, want)
+    assert d.max() <= 1e-6
 
 
 def test_batch_equals_single_and_is_deterministic(native):
@@ -164,16 +202,6 @@ def test_graph_and_direct_launch_agree(native):
     a = lg.Context(s.image, s.weight, s.objects, rule=s.rule, max_batch=32)
     b = lg.Context(s.image, s.weight, s.objects, rule=s.rule, max_batch=32, flags=lg.LG_FLAG_NO_GRAPH)
     assert np.array_equal(a.eval_batch(a.to_map_order(cand)), b.eval_batch(b.to_map_order(cand)))
-
-
-def test_strict_fp_mode_matches_oracle_more_tightly(native):
-    s = workloads.small()
-    cand = workloads.draw_candidates(s, 8, seed=5)
-    ctx = lg.Context(s.image, s.weight, s.objects, rule=s.rule, max_batch=8, flags=lg.LG_FLAG_STRICT_FP)
-    got = ctx.eval_batch(ctx.to_map_order(cand))
-    want = Oracle(s.plugins, s.width, s.height, quadrature.rule(s.rule), image=s.image, weight=s.weight,
-                  precision=32, threads=16).loglike(cand)
-    assert np.abs(got - want).max() <= LOGL_ABS
 
 
 def test_image_plane_prior_parity(native):
