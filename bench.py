@@ -152,8 +152,9 @@ def cpu_oracle(s, threads, precision=32):
     from lensed_gb300 import quadrature
     from oracle.oracle import Oracle
 
+    # the C library's float functions per ray: the natural CPU implementation
     return Oracle(s.plugins, s.width, s.height, quadrature.rule(s.rule), psf=s.psf, image=s.image,
-                  weight=s.weight, precision=precision, threads=threads)
+                  weight=s.weight, precision=precision, threads=threads, math="libm")
 
 
 def ref_impl():
@@ -238,7 +239,8 @@ def main():
     cand = ctx.to_map_order(workloads.draw_candidates(s, B, seed=1 + rank))
     d_params = torch.from_numpy(np.ascontiguousarray(cand)).to(f"cuda:{local}")
     d_logL = torch.empty(B, dtype=torch.float64, device=f"cuda:{local}")
-    stream = torch.cuda.current_stream()
+    # a dedicated stream: the context's kernels and the timing events share it
+    stream = torch.cuda.Stream(device=f"cuda:{local}")
     sh = stream.cuda_stream
 
     def step():
@@ -247,6 +249,8 @@ def main():
     for _ in range(args.warmup):
         step()
     torch.cuda.synchronize()
+    if not np.all(np.isfinite(d_logL.cpu().numpy())):
+        raise SystemExit("non-finite logL in warm-up")
     clocks = Clocks(local)
     clocks.start()
     time.sleep(0.3)
