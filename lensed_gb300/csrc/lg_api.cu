@@ -73,6 +73,11 @@ thread_local std::string g_create_error;
 
 }  // namespace
 
+namespace lg {
+// Message returned by lg_last_error(NULL) on this thread.
+void set_global_error(const char* msg) { g_create_error = msg ? msg : ""; }
+}  // namespace lg
+
 struct lg_ctx {
     lg::Model model;
     lg::Shape shape;
@@ -237,10 +242,10 @@ int create_impl(lg_ctx* c, const lg_image_desc* img, const lg_object_desc* objs,
     const bool strict = (c->flags & LG_FLAG_STRICT_FP) != 0;
     std::string log;
     std::vector<char> cubin, cubin_set;
-    if ((rc = lg::compile_program(lg::compose_source(m, c->shape, strict, lg::Part::EVAL), !strict, cubin, log)))
-        return c->fail(rc, log);
-    if ((rc = lg::compile_program(lg::compose_source(m, c->shape, strict, lg::Part::SET), false, cubin_set, log)))
-        return c->fail(rc, log);
+    rc = lg::compile_program(lg::compose_source(m, c->shape, strict, lg::Part::EVAL), !strict, cubin, log);
+    if (rc) return c->fail(rc, log);
+    rc = lg::compile_program(lg::compose_source(m, c->shape, strict, lg::Part::SET), false, cubin_set, log);
+    if (rc) return c->fail(rc, log);
 
     if ((rc = c->cuda(cudaSetDevice(c->device), "cudaSetDevice"))) return rc;
     if ((rc = c->cuda(cudaFree(nullptr), "CUDA context"))) return rc;
