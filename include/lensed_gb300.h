@@ -190,6 +190,26 @@ int lg_eval_profile(lg_ctx* ctx, const double* d_params, int B, double* d_logL, 
  * denominators. */
 int lg_measure_fp32_peak(int device, double* tflops);
 
+/* Capacity of the static scratch of lg_loglike_images_noalloc, in partial
+ * sums (doubles): 512 KiB held on every GPU that loads the library. */
+#define LG_NOALLOC_MAX_PARTIALS 65536
+
+/* logL[b] = -chi^2/2 of B model images (d_models: B x n_pixels floats) against
+ * one image and weight map (n_pixels floats each), all device pointers, on
+ * the given stream (NULL = default stream), returning without synchronising.
+ * No counterpart in the reference: it is the likelihood path's chi^2
+ * reduction for callers that cannot allocate device memory (a host framework
+ * that owns the GPU's memory through its own pool, or code running where new
+ * allocations are not allowed).  It allocates nothing: its scratch is a
+ * static device array of LG_NOALLOC_MAX_PARTIALS doubles shared by all calls,
+ * so calls that overlap on the GPU race and must be serialised by the caller.
+ * The first call on a device looks up the array's device address; make that
+ * first call before any stream capture.  B is limited to 65535; larger B, null
+ * pointers or non-positive sizes return LG_ERR_INPUT (message in
+ * lg_last_error(NULL)). */
+int lg_loglike_images_noalloc(const float* d_image, const float* d_weight, const float* d_models, long n_pixels,
+                              int B, double* d_logL, void* stream);
+
 /* Drop-in for the reference's likelihood callback (src/nested.h:3): ctx is
  * an lg_ctx*.  cube[0..ndim) holds unit-cube values and is overwritten with
  * the physical values of all npar parameters (map order); *lnew receives

@@ -88,6 +88,7 @@ def lib():
         "lg_render": (C.c_int, [vp, dp, fp, fp, fp]),
         "lg_eval_profile": (C.c_int, [vp, vp, C.c_int, vp, fp]),
         "lg_measure_fp32_peak": (C.c_int, [C.c_int, dp]),
+        "lg_loglike_images_noalloc": (C.c_int, [vp, vp, vp, C.c_long, C.c_int, vp, vp]),
         "loglike": (None, [dp, ip, ip, dp, vp]),
     }
     for name, (res, args) in sig.items():
