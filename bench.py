@@ -225,6 +225,7 @@ def main():
     ap.add_argument("--workload", default="config2")
     ap.add_argument("--batch", type=int, default=0)
     ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--flags", type=int, default=0, help="lg_options.flags (1 strict, 4 IEEE div/sqrt)")
     args = ap.parse_args()
     args.warmup = max(args.warmup, 3)
     if args.impl == "reference":
@@ -240,7 +241,8 @@ def main():
     s, B = workload(args.workload)
     if args.batch:
         B = args.batch
-    ctx = lg.Context(s.image, s.weight, s.objects, psf=s.psf, rule=s.rule, device=local, max_batch=B)
+    ctx = lg.Context(s.image, s.weight, s.objects, psf=s.psf, rule=s.rule, device=local, max_batch=B,
+                     flags=args.flags)
     cand = ctx.to_map_order(workloads.draw_candidates(s, B, seed=1 + rank))
     d_params = torch.from_numpy(np.ascontiguousarray(cand)).to(f"cuda:{local}")
     d_logL = torch.empty(B, dtype=torch.float64, device=f"cuda:{local}")

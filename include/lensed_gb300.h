@@ -61,6 +61,7 @@ extern "C" {
 /* context flags */
 #define LG_FLAG_STRICT_FP 1 /* no FMA contraction in the composed program */
 #define LG_FLAG_NO_GRAPH 2  /* launch kernels directly instead of graph replay */
+#define LG_FLAG_IEEE_DIV 4  /* fast mode with IEEE division and square root per ray */
 
 typedef struct lg_ctx lg_ctx;
 

@@ -30,6 +30,7 @@ LG_OK = 0
 STATUS = {-1: "input", -2: "compile", -3: "cuda", -4: "alloc", -5: "timeout", -6: "unsupported"}
 LG_FLAG_STRICT_FP = 1
 LG_FLAG_NO_GRAPH = 2
+LG_FLAG_IEEE_DIV = 4
 
 
 class LensedError(RuntimeError):

@@ -242,7 +242,11 @@ int create_impl(lg_ctx* c, const lg_image_desc* img, const lg_object_desc* objs,
     const bool strict = (c->flags & LG_FLAG_STRICT_FP) != 0;
     std::string log;
     std::vector<char> cubin, cubin_set;
-    rc = lg::compile_program(lg::compose_source(m, c->shape, strict, lg::Part::EVAL), !strict, cubin, log);
+    // fast mode: hardware-approximate division and square root per ray
+    // (<= 2 ulp, as the reference's -cl-fast-relaxed-math build allows)
+    // unless LG_FLAG_IEEE_DIV; strict mode and set_params stay IEEE
+    const bool ieee = strict || (c->flags & LG_FLAG_IEEE_DIV);
+    rc = lg::compile_program(lg::compose_source(m, c->shape, strict, lg::Part::EVAL), !strict, cubin, log, ieee);
     if (rc) return c->fail(rc, log);
     rc = lg::compile_program(lg::compose_source(m, c->shape, strict, lg::Part::SET), false, cubin_set, log);
     if (rc) return c->fail(rc, log);
@@ -426,7 +430,8 @@ int lg_compile_check(const lg_image_desc* image, const lg_object_desc* objs, int
         const bool strict = opts && (opts->flags & LG_FLAG_STRICT_FP);
         std::vector<char> cubin;
         lg::Shape s = choose_shape(m);
-        rc = lg::compile_program(lg::compose_source(m, s, strict, lg::Part::EVAL), !strict, cubin, err);
+        const bool ieee = strict || (opts->flags & LG_FLAG_IEEE_DIV);
+        rc = lg::compile_program(lg::compose_source(m, s, strict, lg::Part::EVAL), !strict, cubin, err, ieee);
         if (!rc) rc = lg::compile_program(lg::compose_source(m, s, strict, lg::Part::SET), false, cubin, err);
     }
     if (log && log_size) {

@@ -111,6 +111,7 @@ struct Shape {
 // them only in strict mode.
 enum class Part { SET, EVAL };
 std::string compose_source(const Model& m, const Shape& s, bool strict, Part part);
-int compile_program(const std::string& src, bool fmad, std::vector<char>& cubin, std::string& log);
+int compile_program(const std::string& src, bool fmad, std::vector<char>& cubin, std::string& log,
+                    bool ieee_divsqrt = true);
 
 }  // namespace lg

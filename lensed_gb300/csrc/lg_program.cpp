@@ -178,7 +178,8 @@ std::string compose_source(const Model& m, const Shape& s, bool strict, Part par
     return o.str();
 }
 
-int compile_program(const std::string& src, bool fmad, std::vector<char>& cubin, std::string& log)
+int compile_program(const std::string& src, bool fmad, std::vector<char>& cubin, std::string& log,
+                    bool ieee_divsqrt)
 {
     nvrtcProgram prog;
     nvrtcResult r = nvrtcCreateProgram(&prog, src.c_str(), "lensed_model.cu", 0, nullptr, nullptr);
@@ -187,8 +188,9 @@ int compile_program(const std::string& src, bool fmad, std::vector<char>& cubin,
         return LG_ERR_COMPILE;
     }
     std::vector<const char*> opts = {"--gpu-architecture=sm_103a", "-std=c++17", "--generate-line-info",
-                                     "--prec-div=true", "--prec-sqrt=true", "--ftz=false",
-                                     "-diag-suppress=177"};
+                                     "--ftz=false", "-diag-suppress=177"};
+    opts.push_back(ieee_divsqrt ? "--prec-div=true" : "--prec-div=false");
+    opts.push_back(ieee_divsqrt ? "--prec-sqrt=true" : "--prec-sqrt=false");
     opts.push_back(fmad ? "--fmad=true" : "--fmad=false");
     r = nvrtcCompileProgram(prog, (int)opts.size(), opts.data());
     size_t n = 0;

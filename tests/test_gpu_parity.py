@@ -182,6 +182,19 @@ def test_loglike_config2_full_size(native):
     assert ctx.masked == int((ctx._weight == 0).sum())
 
 
+def test_loglike_config2_fast_ieee_division(native):
+    """Fast mode with IEEE division and square root (LG_FLAG_IEEE_DIV)."""
+    s = workloads.config2()
+    ctx = lg.Context(s.image, s.weight, s.objects, psf=s.psf, rule=s.rule, max_batch=8, flags=lg.LG_FLAG_IEEE_DIV)
+    cand = workloads.draw_candidates(s, 8, seed=0)
+    got = ctx.eval_batch(ctx.to_map_order(cand))
+    o = Oracle(s.plugins, s.width, s.height, quadrature.rule(s.rule), psf=s.psf, image=s.image, weight=s.weight,
+               precision=32, threads=16)
+    want = o.loglike(cand)
+    d = _report("config2 fast ieee-div", got, want, want)
+    assert np.all(d <= logl_tol(want))
+
+
 @pytest.mark.parametrize("name", ["small", "config2"])
 def test_loglike_strict_mode_bitwise(native, name):
     s = getattr(workloads, name)()
