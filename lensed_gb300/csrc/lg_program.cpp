@@ -11,6 +11,7 @@
 
 #include <cmath>
 #include <cstdio>
+#include <cstdlib>
 #include <set>
 #include <sstream>
 
@@ -192,6 +193,11 @@ int compile_program(const std::string& src, bool fmad, std::vector<char>& cubin,
     opts.push_back(ieee_divsqrt ? "--prec-div=true" : "--prec-div=false");
     opts.push_back(ieee_divsqrt ? "--prec-sqrt=true" : "--prec-sqrt=false");
     opts.push_back(fmad ? "--fmad=true" : "--fmad=false");
+    if (std::getenv("LG_NVRTC_VERBOSE")) {
+        std::fprintf(stderr, "lensed_gb300: nvrtc");
+        for (const char* o : opts) std::fprintf(stderr, " %s", o);
+        std::fprintf(stderr, "\n");
+    }
     r = nvrtcCompileProgram(prog, (int)opts.size(), opts.data());
     size_t n = 0;
     nvrtcGetProgramLogSize(prog, &n);

@@ -12,8 +12,8 @@ the correctly rounded values); its tolerances:
     absolute error <= 1e-6 * peak below that floor.  Where the FP32 oracle is
     itself further than 1e-5 from the FP64 oracle (ill-conditioned profiles,
     e.g. the r^(1/4) cusp of de Vaucouleurs, whose gradient amplifies
-    last-bit differences of the ray positions), the bound is twice that FP32
-    error, and the GPU image must be as close to FP64 as that bound;
+    last-bit differences of the ray positions), the bound is three times that
+    FP32 error, and the GPU image must be as close to FP64 as that bound;
   * logL: |logL_gpu - logL_oracle32| <= 1e-3 + 2e-6 |logL| (the ulp-level
     differences of the per-ray functions add up coherently for candidates
     far from the data, and the Sersic profile exp(log0 - exp(u)) amplifies a
@@ -51,7 +51,7 @@ def image_err(got, want):
 def assert_image_close(got, want, what="", want64=None):
     tol = IMG_REL
     if want64 is not None:
-        tol = max(IMG_REL, 2 * image_err(want, want64)[0])
+        tol = max(IMG_REL, 3 * image_err(want, want64)[0])
         rel64, _ = image_err(got, want64)
         assert rel64 <= tol, (what, "vs FP64", rel64, tol)
     rel, small = image_err(got, want)
@@ -96,7 +96,7 @@ def test_render_matches_oracle_per_plugin(native, case):
     v64 = Oracle(plugins, W, H, quadrature.rule("gm75"), pcs=pcs, precision=64).render(params)[0]
     assert_image_close(raw, v, plugins, want64=v64)
     assert np.array_equal(model, raw)  # no PSF: the model is the raw render
-    tol = max(IMG_REL, 2 * image_err(v, v64)[0])
+    tol = max(IMG_REL, 3 * image_err(v, v64)[0])
     assert np.abs(err - e).max() <= tol * np.abs(v).max() + 1e-7, plugins
 
 
