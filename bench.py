@@ -66,7 +66,44 @@ def workload(name):
         return workloads.small(), 1
     if name == "large":
         return workloads.large(), 256
+    if name == "systems":
+        return workloads.systems(), 256
     raise SystemExit(f"unknown workload {name}")
+
+
+def run_systems(args):
+    """16 systems of uneven sizes, 256 candidates each, one batch per step
+    through lg_systems_eval (host buffers in and out: value = e2e)."""
+    import lensed_gb300 as lg
+    from lensed_gb300 import workloads
+
+    syst, per = workload("systems")
+    S = lg.Systems([(s.image, s.weight, s.psf, None) for s in syst], syst[0].objects, capacity=[per] * len(syst),
+                   rule="g3k7", flags=args.flags)
+    params = []
+    for s in syst:
+        ctx = lg.Context(s.image, s.weight, s.objects, psf=s.psf, rule=s.rule, max_batch=1)
+        params.append(ctx.to_map_order(workloads.draw_candidates(s, per, seed=1)))
+        ctx.close()
+    for _ in range(args.warmup):
+        S.eval(params)
+    t0 = time.perf_counter()
+    for _ in range(args.steps):
+        out = S.eval(params)
+    dt = (time.perf_counter() - t0) / args.steps
+    total = per * len(syst)
+    assert all(np.all(np.isfinite(o)) for o in out)
+    pix = sum(s.width * s.height for s in syst) / len(syst)
+    line = {"metric": METRIC, "value": total / dt, "unit": UNIT, "n_gpus": 1, "steps": args.steps,
+            "warmup": args.warmup, "ms_per_step": dt * 1e3, "higher_is_better": True, "scaling": "weak",
+            "vs_baseline": None, "dtype": "f32 (f64 chi^2 reduction)", "data": "synthetic",
+            "config": {"workload": f"{len(syst)} systems, sizes " + ",".join(str(s.width) for s in syst)
+                       + f" (mean {pix:.0f} px), epl_plus_shear+sersic+sky, odd PSFs 15-31, rule g3k7",
+                       "batch": total, "per_system": per},
+            "gpu_launches": 4 * args.steps,
+            "e2e": {"value": total / dt, "unit": UNIT,
+                    "h2d_bytes_per_step": int(sum(p.nbytes for p in params)), "d2h_bytes_per_step": 8 * total}}
+    print(json.dumps(line), flush=True)
 
 
 def describe(s, B):
@@ -230,6 +267,8 @@ def main():
     args.warmup = max(args.warmup, 3)
     if args.impl == "reference":
         return run_reference(args)
+    if args.workload == "systems":
+        return run_systems(args)
 
     import torch
 

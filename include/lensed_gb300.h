@@ -211,6 +211,24 @@ int lg_measure_fp32_peak(int device, double* tflops);
 int lg_loglike_images_noalloc(const float* d_image, const float* d_weight, const float* d_models, long n_pixels,
                               int B, double* d_logL, void* stream);
 
+/* ---------------------------------------------------------------- systems */
+/* A batch of lens systems of uneven image and PSF sizes that share the
+ * object list (plugins, priors, parameter map) and quadrature rule,
+ * evaluated together: one persistent launch per stage over (system,
+ * candidate, tile) work units, replayed from one CUDA graph for any per-call
+ * candidate counts up to capacity[s].  The counterpart of running one
+ * reference process (src/lensed.c) per system. */
+typedef struct lg_systems lg_systems;
+lg_systems* lg_systems_create(const lg_image_desc* images, int nsys, const lg_object_desc* objs, int nobjs,
+                              const lg_options* opts, const int* capacity, int* status);
+void lg_systems_destroy(lg_systems* S);
+const char* lg_systems_last_error(const lg_systems* S);
+int lg_systems_npars(const lg_systems* S);
+/* params: counts[0] vectors of system 0, then counts[1] of system 1, ...
+ * (npars doubles each, map order); logL receives sum(counts) values in the
+ * same order.  Each system's values equal those of its own lg_ctx. */
+int lg_systems_eval(lg_systems* S, const double* params, const int* counts, double* logL);
+
 /* Drop-in for the reference's likelihood callback (src/nested.h:3): ctx is
  * an lg_ctx*.  cube[0..ndim) holds unit-cube values and is overwritten with
  * the physical values of all npar parameters (map order); *lnew receives

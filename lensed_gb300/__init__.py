@@ -21,7 +21,7 @@ from typing import Optional, Sequence
 
 import numpy as np
 
-__all__ = ["Context", "LensedError", "lib", "plugins", "plugin_params", "quad_rules", "make_weight",
+__all__ = ["Context", "Systems", "LensedError", "lib", "plugins", "plugin_params", "quad_rules", "make_weight",
            "compile_check", "LIB_PATH"]
 
 LIB_PATH = os.path.join(os.path.dirname(os.path.abspath(__file__)), "liblensed_gb300.so")
@@ -90,6 +90,12 @@ def lib():
         "lg_eval_profile": (C.c_int, [vp, vp, C.c_int, vp, fp]),
         "lg_measure_fp32_peak": (C.c_int, [C.c_int, dp]),
         "lg_loglike_images_noalloc": (C.c_int, [vp, vp, vp, C.c_long, C.c_int, vp, vp]),
+        "lg_systems_create": (vp, [C.POINTER(_ImageDesc), C.c_int, C.POINTER(_ObjectDesc), C.c_int,
+                                   C.POINTER(_Options), ip, ip]),
+        "lg_systems_destroy": (None, [vp]),
+        "lg_systems_last_error": (C.c_char_p, [vp]),
+        "lg_systems_npars": (C.c_int, [vp]),
+        "lg_systems_eval": (C.c_int, [vp, dp, ip, dp]),
         "loglike": (None, [dp, ip, ip, dp, vp]),
     }
     for name, (res, args) in sig.items():
@@ -224,6 +230,54 @@ def compile_check(width, height, objects, psf=None, rule="g3k7", pcs=None, flags
     if rc:
         raise LensedError(rc, buf.value.decode(errors="replace"))
     return buf.value.decode(errors="replace")
+
+
+class Systems:
+    """A batch of lens systems sharing the objects (wraps lg_systems_*).
+
+    systems: sequence of (image, weight, psf-or-None, pcs-or-None);
+    capacity: max candidates per system per call."""
+
+    def __init__(self, systems, objects: Sequence, capacity, rule: str = "g3k7", device: int = 0,
+                 flags: int = 0):
+        L = lib()
+        self._keep = []
+        descs = (_ImageDesc * len(systems))()
+        for i, (img, wht, psf, pcs) in enumerate(systems):
+            a, w = _f32(img), _f32(wht)
+            p = _f32(psf)
+            self._keep += [a, w, p]
+            descs[i] = _image_desc(a.shape[1], a.shape[0], a, w, p, pcs)
+        arr, keep = _objects(objects)
+        self._keep += [arr, keep]
+        cap = np.ascontiguousarray(capacity, dtype=np.int32)
+        self.capacity = cap
+        st = C.c_int()
+        self.h = L.lg_systems_create(descs, len(systems), arr, len(objects),
+                                     C.byref(_options(rule, device, 0, flags)), _p(cap, C.c_int), C.byref(st))
+        if not self.h:
+            raise LensedError(st.value, L.lg_last_error(None).decode(errors="replace"))
+        self.nsys = len(systems)
+        self.npars = L.lg_systems_npars(self.h)
+
+    def close(self):
+        if getattr(self, "h", None):
+            lib().lg_systems_destroy(self.h)
+            self.h = None
+
+    def __del__(self):
+        self.close()
+
+    def eval(self, params_list):
+        """params_list: per system a (count, npars) array in map order."""
+        counts = np.array([len(p) for p in params_list], dtype=np.int32)
+        flat = np.ascontiguousarray(np.concatenate([np.asarray(p, np.float64).reshape(-1, self.npars)
+                                                    for p in params_list]))
+        out = np.empty(int(counts.sum()))
+        rc = lib().lg_systems_eval(self.h, _p(flat, C.c_double), _p(counts, C.c_int), _p(out, C.c_double))
+        if rc:
+            raise LensedError(rc, lib().lg_systems_last_error(self.h).decode(errors="replace"))
+        return np.split(out, np.cumsum(counts)[:-1])
 
 
 class Context:

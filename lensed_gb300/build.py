@@ -43,12 +43,14 @@ def write_embed() -> str:
     kernels = open(os.path.join(PKG, "device", "lg_kernels.cuh")).read()
     setk = open(os.path.join(PKG, "device", "lg_set_kernel.cuh")).read()
     crmath = open(os.path.join(PKG, "device", "lg_crmath_on.cuh")).read()
+    multi = open(os.path.join(PKG, "device", "lg_multi_kernels.cuh")).read()
     objs = sorted(glob.glob(os.path.join(PKG, "objects", "*.cuh")))
     lines = ["// generated by lensed_gb300/build.py: device sources for NVRTC", ""]
     lines.append(f"static const char LG_EMBED_PRELUDE[] = {_raw(prelude)};")
     lines.append(f"static const char LG_EMBED_KERNELS[] = {_raw(kernels)};")
     lines.append(f"static const char LG_EMBED_SET_KERNEL[] = {_raw(setk)};")
     lines.append(f"static const char LG_EMBED_CRMATH[] = {_raw(crmath)};")
+    lines.append(f"static const char LG_EMBED_MULTI[] = {_raw(multi)};")
     lines.append("struct lg_embedded_object { const char* name; const char* text; };")
     lines.append("static const lg_embedded_object LG_EMBED_OBJECTS[] = {")
     for p in objs:

@@ -23,21 +23,9 @@
 
 #include "lg_internal.h"
 
+namespace lg {
+
 namespace {
-
-// Driver API entry points, resolved through the runtime so the library loads
-// on machines without a CUDA driver (the compile check needs no GPU).
-struct Driver {
-    CUresult (*moduleLoadData)(CUmodule*, const void*) = nullptr;
-    CUresult (*moduleUnload)(CUmodule) = nullptr;
-    CUresult (*moduleGetFunction)(CUfunction*, CUmodule, const char*) = nullptr;
-    CUresult (*moduleGetGlobal)(CUdeviceptr*, size_t*, CUmodule, const char*) = nullptr;
-    CUresult (*funcSetAttribute)(CUfunction, CUfunction_attribute, int) = nullptr;
-    CUresult (*launchKernel)(CUfunction, unsigned, unsigned, unsigned, unsigned, unsigned, unsigned, unsigned,
-                             CUstream, void**, void**) = nullptr;
-    bool ok = false;
-};
-
 std::mutex g_drv_mu;
 Driver g_drv;
 
@@ -52,6 +40,7 @@ bool resolve(const char* name, F& f)
     f = reinterpret_cast<F>(p);
     return true;
 }
+}  // namespace
 
 const Driver* driver()
 {
@@ -61,13 +50,20 @@ const Driver* driver()
         bool ok = resolve("cuModuleLoadData", d.moduleLoadData) && resolve("cuModuleUnload", d.moduleUnload) &&
                   resolve("cuModuleGetFunction", d.moduleGetFunction) &&
                   resolve("cuModuleGetGlobal", d.moduleGetGlobal) &&
-                  resolve("cuFuncSetAttribute", d.funcSetAttribute) && resolve("cuLaunchKernel", d.launchKernel);
+                  resolve("cuFuncSetAttribute", d.funcSetAttribute) && resolve("cuLaunchKernel", d.launchKernel) &&
+                  resolve("cuOccupancyMaxActiveBlocksPerMultiprocessor", d.occupancy);
         if (!ok) return nullptr;
         d.ok = true;
         g_drv = d;
     }
     return &g_drv;
 }
+
+}  // namespace lg
+
+namespace {
+using lg::Driver;
+using lg::driver;
 
 thread_local std::string g_create_error;
 

@@ -6,7 +6,25 @@
 
 #include "lensed_gb300.h"
 
+#include <cuda.h>
+
 namespace lg {
+
+// Driver API entry points, resolved through the runtime so the library loads
+// on machines without a CUDA driver (the compile check needs no GPU).
+struct Driver {
+    CUresult (*moduleLoadData)(CUmodule*, const void*) = nullptr;
+    CUresult (*moduleUnload)(CUmodule) = nullptr;
+    CUresult (*moduleGetFunction)(CUfunction*, CUmodule, const char*) = nullptr;
+    CUresult (*moduleGetGlobal)(CUdeviceptr*, size_t*, CUmodule, const char*) = nullptr;
+    CUresult (*funcSetAttribute)(CUfunction, CUfunction_attribute, int) = nullptr;
+    CUresult (*launchKernel)(CUfunction, unsigned, unsigned, unsigned, unsigned, unsigned, unsigned, unsigned,
+                             CUstream, void**, void**) = nullptr;
+    CUresult (*occupancy)(int*, CUfunction, int, size_t) = nullptr;
+    bool ok = false;
+};
+const Driver* driver();
+void set_global_error(const char* msg);
 
 // ------------------------------------------------------------------ plugins
 struct ParamDef {
@@ -34,6 +52,7 @@ const char* prelude_source();
 const char* kernels_source();
 const char* set_kernel_source();
 const char* crmath_source();
+const char* multi_kernels_source();
 
 // ------------------------------------------------------------------- priors
 // Lensed's prior plugins (src/prior.c:47-51): delta (pseudo), unif, norm.
@@ -111,6 +130,10 @@ struct Shape {
 // them only in strict mode.
 enum class Part { SET, EVAL };
 std::string compose_source(const Model& m, const Shape& s, bool strict, Part part);
+// Evaluation module for a batch of systems sharing m's objects and rule; the
+// PSF shapes (w, h) present in the batch get their own convolution code.
+std::string compose_multi_source(const Model& m, const std::vector<std::pair<int, int>>& psf_shapes,
+                                 const Shape& s, bool strict);
 int compile_program(const std::string& src, bool fmad, std::vector<char>& cubin, std::string& log,
                     bool ieee_divsqrt = true);
 

@@ -179,6 +179,43 @@ std::string compose_source(const Model& m, const Shape& s, bool strict, Part par
     return o.str();
 }
 
+std::string compose_multi_source(const Model& m, const std::vector<std::pair<int, int>>& psf_shapes,
+                                 const Shape& s, bool strict)
+{
+    std::ostringstream o;
+    o << "// Lensed likelihood program (multi-system evaluation module) composed for:";
+    for (const auto& ob : m.objs) o << " " << ob.id << "=" << ob.plugin->name;
+    o << "\n// rule " << m.rule->name << " (" << m.rule->size << " points)" << (strict ? ", strict FP" : "")
+      << "\n\n";
+    o << "#define LG_RT " << s.rt << "\n#define LG_RPPT " << s.rppt << "\n";
+    o << "#define LG_CTX " << s.ctx << "\n#define LG_CTY " << s.cty << "\n#define LG_CR " << s.cr << "\n\n";
+    o << prelude_source() << "\n";
+    if (strict) o << crmath_source() << "\n";
+    std::set<std::string> done;
+    for (const auto& ob : m.objs) emit_plugin(o, ob.plugin, done);
+    o << "// ---- model section\n#define LG_NPARS " << m.pars.size() << "\n";
+    o << "struct lg_model {\n";
+    for (size_t i = 0; i < m.objs.size(); ++i)
+        o << "    lg_data_" << m.objs[i].plugin->name << " o" << i << ";  // " << m.objs[i].id << "\n";
+    o << "};\n\n";
+    const int nq = m.rule->size;
+    o << "#define LG_Q " << nq << "\n";
+    o << "__constant__ float2 lg_qq[LG_Q] = {";
+    for (int n = 0; n < nq; ++n)
+        o << (n ? ", " : "") << "{" << hexf((float)(m.pcs[2] * m.rule->absc[n][0])) << ", "
+          << hexf((float)(m.pcs[3] * m.rule->absc[n][1])) << "}";
+    o << "};\n__constant__ float2 lg_ww[LG_Q] = {";
+    for (int n = 0; n < nq; ++n)
+        o << (n ? ", " : "") << "{" << hexf((float)m.rule->weig[n]) << ", " << hexf((float)m.rule->errw[n]) << "}";
+    o << "};\n";
+    emit_compute(o, m);
+    o << "#define LG_PSF_SHAPES";
+    for (const auto& ps : psf_shapes) o << " LG_PSF_CASE(" << ps.first << ", " << ps.second << ")";
+    o << "\n";
+    o << multi_kernels_source() << "\n";
+    return o.str();
+}
+
 int compile_program(const std::string& src, bool fmad, std::vector<char>& cubin, std::string& log,
                     bool ieee_divsqrt)
 {

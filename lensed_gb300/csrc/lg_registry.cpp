@@ -23,6 +23,7 @@ const char* prelude_source() { return LG_EMBED_PRELUDE; }
 const char* kernels_source() { return LG_EMBED_KERNELS; }
 const char* set_kernel_source() { return LG_EMBED_SET_KERNEL; }
 const char* crmath_source() { return LG_EMBED_CRMATH; }
+const char* multi_kernels_source() { return LG_EMBED_MULTI; }
 
 namespace {
 

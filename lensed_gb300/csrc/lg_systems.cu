@@ -1,0 +1,398 @@
+// A batch of lens systems of uneven image and PSF sizes evaluated together:
+// the counterpart of running one Lensed process per system, for samplers
+// that advance many systems at once.
+//
+// All systems share the object list (plugins, priors, parameter map) and the
+// quadrature rule.  Per call, the candidate counts of the systems may change;
+// a small plan (per-system counts and work-unit offsets) is uploaded inside
+// the CUDA graph, so one graph -- upload, set_params, persistent render,
+// persistent convolution + chi^2, finish, read-back -- is captured once and
+// replayed for any counts within the capacities given at creation.
+
+#include <cuda.h>
+#include <cuda_runtime.h>
+
+#include <algorithm>
+#include <cstring>
+#include <set>
+#include <string>
+#include <vector>
+
+#include "lg_internal.h"
+
+namespace {
+
+// mirrors of the device structs in device/lg_multi_kernels.cuh
+struct SysInfo {
+    int W, H, N, pw, ph;
+    int rtiles, ctiles_x, ctiles_y, ctiles;
+    int psf_off;
+    float rx, ry, sx, sy;
+    long long img_off;
+};
+struct SysPlan {
+    int count, cand0;
+    long long r_unit0, c_unit0, raw0, part0;
+};
+
+}  // namespace
+
+struct lg_systems {
+    int nsys = 0, flags = 0, device = 0;
+    bool psf = false;
+    std::string err;
+    std::vector<lg::Model> models;
+    lg::Shape shape;
+    std::vector<int> cap;      // capacity (max candidates) per system
+    int max_total = 0;
+    std::vector<SysInfo> info;
+    std::vector<long long> raw0, part0;
+    size_t model_bytes = 0;
+
+    const lg::Driver* drv = nullptr;
+    CUmodule mod = nullptr, mod_set = nullptr;
+    CUfunction f_setp = nullptr, f_render = nullptr, f_conv = nullptr, f_finish = nullptr;
+    int grid_render = 0, grid_conv = 0, grid_finish = 0, csmem = 0;
+
+    cudaStream_t stream = nullptr;
+    float *d_images = nullptr, *d_weights = nullptr, *d_psfs = nullptr, *d_raw = nullptr;
+    void* d_models = nullptr;
+    double *d_partials = nullptr, *d_params = nullptr, *d_logL = nullptr;
+    SysInfo* d_info = nullptr;
+    SysPlan* d_plan = nullptr;
+    long long* d_hdr = nullptr;
+    double *h_params = nullptr, *h_logL = nullptr;
+    SysPlan* h_plan = nullptr;
+    long long* h_hdr = nullptr;
+    cudaGraphExec_t graph = nullptr;
+
+    int fail(int code, const std::string& m)
+    {
+        err = m;
+        return code;
+    }
+    int cuda(cudaError_t e, const char* what)
+    {
+        if (e == cudaSuccess) return LG_OK;
+        err = std::string(what) + ": " + cudaGetErrorString(e);
+        return LG_ERR_CUDA;
+    }
+    int drvcall(CUresult r, const char* what)
+    {
+        if (r == CUDA_SUCCESS) return LG_OK;
+        err = std::string(what) + ": CUDA driver error " + std::to_string((int)r);
+        return LG_ERR_CUDA;
+    }
+    int launch(CUfunction f, dim3 g, dim3 b, unsigned smem, void** args, const char* what)
+    {
+        return drvcall(drv->launchKernel(f, g.x, g.y, g.z, b.x, b.y, b.z, smem, (CUstream)stream, args, nullptr),
+                       what);
+    }
+    void release()
+    {
+        if (graph) cudaGraphExecDestroy(graph);
+        graph = nullptr;
+        void* dev[] = {d_images, d_weights, d_psfs, d_raw, d_models, d_partials, d_params, d_logL, d_info, d_plan,
+                       d_hdr};
+        for (void* p : dev) cudaFree(p);
+        void* host[] = {h_params, h_logL, h_plan, h_hdr};
+        for (void* p : host) cudaFreeHost(p);
+        if (mod && drv) drv->moduleUnload(mod);
+        if (mod_set && drv) drv->moduleUnload(mod_set);
+        if (stream) cudaStreamDestroy(stream);
+        mod = mod_set = nullptr;
+        stream = nullptr;
+    }
+};
+
+namespace {
+
+int create_systems(lg_systems* S, const lg_image_desc* images, int nsys, const lg_object_desc* objs, int nobjs,
+                   const lg_options* opts, const int* capacity)
+{
+    if (!images || nsys <= 0 || nsys > 4096 || !capacity) return S->fail(LG_ERR_INPUT, "invalid system list");
+    S->nsys = nsys;
+    S->flags = opts ? opts->flags : 0;
+    S->device = opts ? opts->device : 0;
+    S->models.resize(nsys);
+    int rc;
+    for (int s = 0; s < nsys; ++s) {
+        if ((rc = lg::build_model(&images[s], objs, nobjs, opts, S->models[s], S->err))) {
+            S->err = "system " + std::to_string(s) + ": " + S->err;
+            return rc;
+        }
+        if (!images[s].image || !images[s].weight)
+            return S->fail(LG_ERR_INPUT, "system " + std::to_string(s) + ": image and weight are required");
+        if (capacity[s] < 0 || capacity[s] > 65535) return S->fail(LG_ERR_INPUT, "invalid capacity");
+    }
+    const lg::Model& m0 = S->models[0];
+    S->psf = !m0.psf.empty();
+    for (int s = 1; s < nsys; ++s) {
+        const lg::Model& m = S->models[s];
+        if (!m.psf.empty() != S->psf) return S->fail(LG_ERR_UNSUPPORTED, "all systems need a PSF, or none");
+        if (m.pcs[2] != m0.pcs[2] || m.pcs[3] != m0.pcs[3])
+            return S->fail(LG_ERR_UNSUPPORTED, "systems must share the pixel scale (quadrature offsets)");
+        if (m.pmap != m0.pmap) return S->fail(LG_ERR_UNSUPPORTED, "systems must share the parameter map");
+    }
+    S->cap.assign(capacity, capacity + nsys);
+    for (int c : S->cap) S->max_total += c;
+    if (S->max_total <= 0 || S->max_total > 1 << 20) return S->fail(LG_ERR_INPUT, "invalid total capacity");
+
+    // static layout: images, PSFs, raw models and partials by capacity
+    const lg::Shape& sh = S->shape;
+    std::set<std::pair<int, int>> shapes;
+    long long img = 0, raw = 0, part = 0;
+    int psf_off = 0, csmem = 0;
+    for (int s = 0; s < nsys; ++s) {
+        const lg::Model& m = S->models[s];
+        SysInfo I{};
+        I.W = m.width;
+        I.H = m.height;
+        I.N = m.width * m.height;
+        I.pw = m.psfw;
+        I.ph = m.psfh;
+        I.rtiles = (I.N + sh.rt * sh.rppt - 1) / (sh.rt * sh.rppt);
+        I.ctiles_x = (I.W + sh.ctx - 1) / sh.ctx;
+        I.ctiles_y = (I.H + sh.cty - 1) / sh.cty;
+        I.ctiles = I.ctiles_x * I.ctiles_y;
+        I.psf_off = psf_off;
+        double rx = m.pcs[0], ry = m.pcs[1];
+        if (S->psf) {
+            if (m.psfw % 2 == 0) rx += 0.5;  // src/lensed.c:884-891
+            if (m.psfh % 2 == 0) ry += 0.5;
+            shapes.insert({m.psfw, m.psfh});
+            const int win4 = (sh.cr + m.psfw - 1 + 3) / 4 * 4;
+            const int twp = ((sh.ctx - sh.cr + win4 + 27) / 32) * 32 + 4;
+            csmem = std::max(csmem, ((sh.cty + m.psfh - 1) * twp + m.psfw * m.psfh) * 4);
+            psf_off += m.psfw * m.psfh;
+        }
+        I.rx = (float)rx;
+        I.ry = (float)ry;
+        I.sx = (float)m.pcs[2];
+        I.sy = (float)m.pcs[3];
+        I.img_off = img;
+        img += I.N;
+        S->raw0.push_back(raw);
+        S->part0.push_back(part);
+        raw += (long long)S->cap[s] * I.N;
+        part += (long long)S->cap[s] * (S->psf ? I.ctiles : I.rtiles);
+        S->info.push_back(I);
+    }
+    S->csmem = csmem;
+
+    // programs
+    const bool strict = (S->flags & LG_FLAG_STRICT_FP) != 0;
+    const bool ieee = strict || (S->flags & LG_FLAG_IEEE_DIV);
+    std::vector<std::pair<int, int>> shape_list(shapes.begin(), shapes.end());
+    std::vector<char> cubin, cubin_set;
+    std::string log;
+    rc = lg::compile_program(lg::compose_multi_source(m0, shape_list, sh, strict), !strict, cubin, log, ieee);
+    if (rc) return S->fail(rc, log);
+    rc = lg::compile_program(lg::compose_source(m0, sh, strict, lg::Part::SET), false, cubin_set, log);
+    if (rc) return S->fail(rc, log);
+    if ((rc = S->cuda(cudaSetDevice(S->device), "cudaSetDevice")) || (rc = S->cuda(cudaFree(nullptr), "context")))
+        return rc;
+    S->drv = lg::driver();
+    if (!S->drv) return S->fail(LG_ERR_CUDA, "CUDA driver entry points unavailable");
+    if ((rc = S->drvcall(S->drv->moduleLoadData(&S->mod, cubin.data()), "cuModuleLoadData")) ||
+        (rc = S->drvcall(S->drv->moduleLoadData(&S->mod_set, cubin_set.data()), "cuModuleLoadData")) ||
+        (rc = S->drvcall(S->drv->moduleGetFunction(&S->f_setp, S->mod_set, "lg_set_params_kernel"), "set_params")) ||
+        (rc = S->drvcall(S->drv->moduleGetFunction(&S->f_render, S->mod,
+                                                   S->psf ? "lg_multi_render_raw" : "lg_multi_render_chi2"),
+                         "render")) ||
+        (rc = S->drvcall(S->drv->moduleGetFunction(&S->f_conv, S->mod, "lg_multi_conv_chi2"), "convolve")) ||
+        (rc = S->drvcall(S->drv->moduleGetFunction(&S->f_finish, S->mod, "lg_multi_finish"), "finish")))
+        return rc;
+    CUdeviceptr gp;
+    size_t gb;
+    unsigned mb = 0;
+    if ((rc = S->drvcall(S->drv->moduleGetGlobal(&gp, &gb, S->mod_set, "lg_model_bytes"), "model size")) ||
+        (rc = S->cuda(cudaMemcpy(&mb, (void*)gp, sizeof mb, cudaMemcpyDeviceToHost), "model size")))
+        return rc;
+    S->model_bytes = mb;
+    if (S->csmem > 48 * 1024 &&
+        (rc = S->drvcall(S->drv->funcSetAttribute(S->f_conv, CU_FUNC_ATTRIBUTE_MAX_DYNAMIC_SHARED_SIZE_BYTES,
+                                                  S->csmem),
+                         "convolve smem")))
+        return rc;
+    // persistent grids: every SM filled to its occupancy
+    int sms = 0, occ_r = 0, occ_c = 0;
+    cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, S->device);
+    if ((rc = S->drvcall(S->drv->occupancy(&occ_r, S->f_render, sh.rt, 0), "occupancy")) ||
+        (rc = S->drvcall(S->drv->occupancy(&occ_c, S->f_conv, (sh.ctx / sh.cr) * sh.cty, S->csmem), "occupancy")))
+        return rc;
+    S->grid_render = sms * std::max(occ_r, 1);
+    S->grid_conv = sms * std::max(occ_c, 1);
+    S->grid_finish = sms * 4;
+
+    if ((rc = S->cuda(cudaStreamCreateWithFlags(&S->stream, cudaStreamNonBlocking), "stream"))) return rc;
+    const size_t np = m0.pars.size();
+    auto alloc = [&](void** p, size_t bytes, const char* what) {
+        cudaError_t e = cudaMalloc(p, bytes ? bytes : 16);
+        if (e != cudaSuccess) {
+            S->err = std::string("cudaMalloc ") + what + ": " + cudaGetErrorString(e);
+            return LG_ERR_ALLOC;
+        }
+        return LG_OK;
+    };
+    if ((rc = alloc((void**)&S->d_images, img * 4, "images")) || (rc = alloc((void**)&S->d_weights, img * 4, "weights")) ||
+        (rc = alloc((void**)&S->d_psfs, std::max(psf_off, 1) * 4, "psfs")) ||
+        (rc = alloc((void**)&S->d_raw, S->psf ? raw * 4 : 0, "raw")) ||
+        (rc = alloc(&S->d_models, (size_t)S->max_total * S->model_bytes, "models")) ||
+        (rc = alloc((void**)&S->d_partials, part * 8, "partials")) ||
+        (rc = alloc((void**)&S->d_params, (size_t)S->max_total * np * 8, "params")) ||
+        (rc = alloc((void**)&S->d_logL, (size_t)S->max_total * 8, "logL")) ||
+        (rc = alloc((void**)&S->d_info, nsys * sizeof(SysInfo), "info")) ||
+        (rc = alloc((void**)&S->d_plan, nsys * sizeof(SysPlan), "plan")) ||
+        (rc = alloc((void**)&S->d_hdr, 4 * sizeof(long long), "header")))
+        return rc;
+    if ((rc = S->cuda(cudaMallocHost((void**)&S->h_params, (size_t)S->max_total * np * 8), "pinned")) ||
+        (rc = S->cuda(cudaMallocHost((void**)&S->h_logL, (size_t)S->max_total * 8), "pinned")) ||
+        (rc = S->cuda(cudaMallocHost((void**)&S->h_plan, nsys * sizeof(SysPlan)), "pinned")) ||
+        (rc = S->cuda(cudaMallocHost((void**)&S->h_hdr, 4 * sizeof(long long)), "pinned")))
+        return rc;
+    std::memset(S->h_params, 0, (size_t)S->max_total * np * 8);
+    for (int s = 0; s < nsys; ++s) {
+        const SysInfo& I = S->info[s];
+        if ((rc = S->cuda(cudaMemcpy(S->d_images + I.img_off, images[s].image, (size_t)I.N * 4,
+                                     cudaMemcpyHostToDevice),
+                          "upload")) ||
+            (rc = S->cuda(cudaMemcpy(S->d_weights + I.img_off, images[s].weight, (size_t)I.N * 4,
+                                     cudaMemcpyHostToDevice),
+                          "upload")))
+            return rc;
+        if (S->psf &&
+            (rc = S->cuda(cudaMemcpy(S->d_psfs + I.psf_off, S->models[s].psf.data(), S->models[s].psf.size() * 4,
+                                     cudaMemcpyHostToDevice),
+                          "upload")))
+            return rc;
+    }
+    if ((rc = S->cuda(cudaMemcpy(S->d_info, S->info.data(), nsys * sizeof(SysInfo), cudaMemcpyHostToDevice),
+                      "upload")) ||
+        (rc = S->cuda(cudaMemset(S->d_params, 0, (size_t)S->max_total * np * 8), "clear")))
+        return rc;
+    return LG_OK;
+}
+
+int enqueue_systems(lg_systems* S)
+{
+    const size_t np = S->models[0].pars.size();
+    int rc;
+    if ((rc = S->cuda(cudaMemcpyAsync(S->d_params, S->h_params, (size_t)S->max_total * np * 8,
+                                      cudaMemcpyHostToDevice, S->stream),
+                      "params")) ||
+        (rc = S->cuda(cudaMemcpyAsync(S->d_plan, S->h_plan, S->nsys * sizeof(SysPlan), cudaMemcpyHostToDevice,
+                                      S->stream),
+                      "plan")) ||
+        (rc = S->cuda(cudaMemcpyAsync(S->d_hdr, S->h_hdr, 4 * sizeof(long long), cudaMemcpyHostToDevice,
+                                      S->stream),
+                      "header")))
+        return rc;
+    int total = S->max_total;
+    void* a_setp[] = {&S->d_params, &total, &S->d_models};
+    if ((rc = S->launch(S->f_setp, dim3((total + 127) / 128), dim3(128), 0, a_setp, "set_params"))) return rc;
+    if (S->psf) {
+        void* a_r[] = {&S->d_models, &S->d_info, &S->d_plan, &S->d_hdr, &S->d_raw};
+        if ((rc = S->launch(S->f_render, dim3(S->grid_render), dim3(S->shape.rt), 0, a_r, "render"))) return rc;
+        void* a_c[] = {&S->d_raw, &S->d_info, &S->d_plan, &S->d_hdr, &S->d_images, &S->d_weights, &S->d_psfs,
+                       &S->d_partials};
+        if ((rc = S->launch(S->f_conv, dim3(S->grid_conv), dim3(S->shape.ctx / S->shape.cr, S->shape.cty),
+                            S->csmem, a_c, "convolve")))
+            return rc;
+    } else {
+        void* a_r[] = {&S->d_models, &S->d_info, &S->d_plan, &S->d_hdr, &S->d_images, &S->d_weights,
+                       &S->d_partials};
+        if ((rc = S->launch(S->f_render, dim3(S->grid_render), dim3(S->shape.rt), 0, a_r, "render"))) return rc;
+    }
+    int with_psf = S->psf ? 1 : 0;
+    void* a_f[] = {&S->d_partials, &S->d_info, &S->d_plan, &S->d_hdr, &with_psf, &S->d_logL};
+    if ((rc = S->launch(S->f_finish, dim3(S->grid_finish), dim3(256), 0, a_f, "finish"))) return rc;
+    return S->cuda(cudaMemcpyAsync(S->h_logL, S->d_logL, (size_t)S->max_total * 8, cudaMemcpyDeviceToHost,
+                                   S->stream),
+                   "logL");
+}
+
+}  // namespace
+
+extern "C" {
+
+lg_systems* lg_systems_create(const lg_image_desc* images, int nsys, const lg_object_desc* objs, int nobjs,
+                              const lg_options* opts, const int* capacity, int* status)
+{
+    lg_systems* S = new (std::nothrow) lg_systems();
+    if (!S) {
+        if (status) *status = LG_ERR_ALLOC;
+        return nullptr;
+    }
+    int rc = create_systems(S, images, nsys, objs, nobjs, opts, capacity);
+    if (status) *status = rc;
+    if (rc) {
+        lg::set_global_error(S->err.c_str());
+        S->release();
+        delete S;
+        return nullptr;
+    }
+    return S;
+}
+
+void lg_systems_destroy(lg_systems* S)
+{
+    if (!S) return;
+    cudaSetDevice(S->device);
+    if (S->stream) cudaStreamSynchronize(S->stream);
+    S->release();
+    delete S;
+}
+
+const char* lg_systems_last_error(const lg_systems* S) { return S ? S->err.c_str() : ""; }
+
+int lg_systems_npars(const lg_systems* S) { return S ? (int)S->models[0].pars.size() : LG_ERR_INPUT; }
+
+int lg_systems_eval(lg_systems* S, const double* params, const int* counts, double* logL)
+{
+    if (!S || !params || !counts || !logL) return LG_ERR_INPUT;
+    int rc;
+    if ((rc = S->cuda(cudaSetDevice(S->device), "cudaSetDevice"))) return rc;
+    const size_t np = S->models[0].pars.size();
+    long long ru = 0, cu = 0;
+    int total = 0;
+    for (int s = 0; s < S->nsys; ++s) {
+        if (counts[s] < 0 || counts[s] > S->cap[s])
+            return S->fail(LG_ERR_INPUT, "system " + std::to_string(s) + ": count outside [0, capacity]");
+        SysPlan& P = S->h_plan[s];
+        P.count = counts[s];
+        P.cand0 = total;
+        P.r_unit0 = ru;
+        P.c_unit0 = cu;
+        P.raw0 = S->raw0[s];
+        P.part0 = S->part0[s];
+        ru += (long long)counts[s] * S->info[s].rtiles;
+        cu += (long long)counts[s] * S->info[s].ctiles;
+        total += counts[s];
+    }
+    if (total == 0) return LG_OK;
+    S->h_hdr[0] = ru;
+    S->h_hdr[1] = S->psf ? cu : 0;
+    S->h_hdr[2] = total;
+    S->h_hdr[3] = S->nsys;
+    std::memcpy(S->h_params, params, (size_t)total * np * 8);
+    if (!S->graph) {
+        cudaGraph_t g;
+        if ((rc = S->cuda(cudaStreamBeginCapture(S->stream, cudaStreamCaptureModeThreadLocal), "capture")))
+            return rc;
+        int erc = enqueue_systems(S);
+        cudaError_t e = cudaStreamEndCapture(S->stream, &g);
+        if (erc) return erc;
+        if ((rc = S->cuda(e, "end capture"))) return rc;
+        e = cudaGraphInstantiate(&S->graph, g, 0);
+        cudaGraphDestroy(g);
+        if ((rc = S->cuda(e, "graph instantiate"))) return rc;
+    }
+    if ((rc = S->cuda(cudaGraphLaunch(S->graph, S->stream), "graph launch")) ||
+        (rc = S->cuda(cudaStreamSynchronize(S->stream), "evaluate")))
+        return rc;
+    std::memcpy(logL, S->h_logL, (size_t)total * 8);
+    return LG_OK;
+}
+
+}  // extern "C"

@@ -1,0 +1,277 @@
+// Persistent kernels for a batch of lens systems of uneven sizes that share
+// the object list and the quadrature rule.  Composed by NVRTC after the
+// prelude, the plugins, the model struct, lg_compute and the quadrature
+// table; the distinct PSF shapes of the batch are listed in LG_PSF_SHAPES
+// (a sequence of LG_PSF_CASE(w, h) entries), and LG_MAX_PSF bounds them.
+//
+// Work is split into units -- (system, candidate, tile) -- enumerated
+// system by system; a fixed grid of blocks strides over them, so one launch
+// covers every image size and the launch shape does not depend on the
+// per-call candidate counts (which live in device memory).  Per-pixel
+// arithmetic and summation orders are those of the single-system kernels, so
+// each system's logL is identical to its own context's.
+
+#ifndef LG_RT
+#define LG_RT 128
+#endif
+#ifndef LG_RPPT
+#define LG_RPPT 2
+#endif
+#define LG_RTILE (LG_RT * LG_RPPT)
+#ifndef LG_CTX
+#define LG_CTX 32
+#endif
+#ifndef LG_CTY
+#define LG_CTY 32
+#endif
+#ifndef LG_CR
+#define LG_CR 8
+#endif
+#define LG_CTHREADS ((LG_CTX / LG_CR) * LG_CTY)
+
+// static description of a system
+struct lg_sysinfo {
+    int W, H, N, pw, ph;
+    int rtiles, ctiles_x, ctiles_y, ctiles;
+    int psf_off;
+    float rx, ry, sx, sy;
+    long long img_off;
+};
+
+// per-call placement of a system's candidates
+struct lg_sysplan {
+    int count, cand0;
+    long long r_unit0, c_unit0, raw0, part0;
+};
+
+// header: [0] render units, [1] convolution units, [2] candidates, [3] systems
+LG_DEV int lg_find_system(const lg_sysplan* __restrict__ plan, int nsys, long long u, bool conv)
+{
+    int s = 0;
+    while (s + 1 < nsys && (conv ? plan[s + 1].c_unit0 : plan[s + 1].r_unit0) <= u) ++s;
+    return s;
+}
+
+LG_DEV double lg_warp_sum(double v)
+{
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) v += __shfl_down_sync(0xffffffffu, v, o);
+    return v;
+}
+
+// Fixed-order block sum, valid in thread 0; red must hold NT/32 doubles.
+template <int NT>
+LG_DEV double lg_block_sum(double v, double* red)
+{
+    const int tid = threadIdx.y * blockDim.x + threadIdx.x;
+    const int lane = tid & 31, warp = tid >> 5;
+    v = lg_warp_sum(v);
+    if (lane == 0) red[warp] = v;
+    __syncthreads();
+    double s = 0.0;
+    if (tid == 0) {
+#pragma unroll
+        for (int i = 0; i < NT / 32; ++i) s += red[i];
+    }
+    __syncthreads();
+    return s;
+}
+
+// ------------------------------------------------------------- render --
+// WITH_PSF: store raw models; else reduce the chi^2 of each tile directly.
+template <bool WITH_PSF>
+LG_DEV void lg_multi_render_body(const lg_model* __restrict__ models, const lg_sysinfo* __restrict__ info,
+                                 const lg_sysplan* __restrict__ plan, const long long* __restrict__ hdr,
+                                 float* __restrict__ raw, const float* __restrict__ images,
+                                 const float* __restrict__ weights, double* __restrict__ partials)
+{
+    __shared__ double red[LG_RT / 32];
+    const long long U = hdr[0];
+    const int nsys = (int)hdr[3];
+    for (long long u = blockIdx.x; u < U; u += gridDim.x) {
+        const int s = lg_find_system(plan, nsys, u, false);
+        const lg_sysinfo I = info[s];
+        const lg_sysplan P = plan[s];
+        const long long local = u - P.r_unit0;
+        const int b = (int)(local / I.rtiles), t = (int)(local - (long long)b * I.rtiles);
+        const lg_model m = models[P.cand0 + b];
+        const int base = t * LG_RTILE + threadIdx.x;
+        float2 xp[LG_RPPT];
+        float v[LG_RPPT];
+#pragma unroll
+        for (int j = 0; j < LG_RPPT; ++j) {
+            int k = base + j * LG_RT;
+            k = k < I.N ? k : I.N - 1;
+            xp[j] = make_float2(I.rx + I.sx * (float)(k % I.W), I.ry + I.sy * (float)(k / I.W));
+            v[j] = 0.0f;
+        }
+#pragma unroll 1
+        for (int n = 0; n < LG_Q; ++n) {
+            const float2 q = lg_qq[n];
+            const float2 w = lg_ww[n];
+#pragma unroll
+            for (int j = 0; j < LG_RPPT; ++j) v[j] += w.x * lg_compute(m, xp[j] + q);
+        }
+        if (WITH_PSF) {
+#pragma unroll
+            for (int j = 0; j < LG_RPPT; ++j) {
+                const int k = base + j * LG_RT;
+                if (k < I.N) raw[P.raw0 + (long long)b * I.N + k] = v[j];
+            }
+        } else {
+            double acc = 0.0;
+#pragma unroll
+            for (int j = 0; j < LG_RPPT; ++j) {
+                const int k = base + j * LG_RT;
+                if (k < I.N) {
+                    const float d = v[j] - images[I.img_off + k];
+                    acc += (double)(weights[I.img_off + k] * d * d);
+                }
+            }
+            acc = lg_block_sum<LG_RT>(acc, red);
+            if (threadIdx.x == 0) partials[P.part0 + (long long)b * I.rtiles + t] = acc;
+        }
+    }
+}
+
+extern "C" __global__ void __launch_bounds__(LG_RT)
+    lg_multi_render_raw(const lg_model* __restrict__ models, const lg_sysinfo* __restrict__ info,
+                        const lg_sysplan* __restrict__ plan, const long long* __restrict__ hdr, float* __restrict__ raw)
+{
+    lg_multi_render_body<true>(models, info, plan, hdr, raw, nullptr, nullptr, nullptr);
+}
+
+extern "C" __global__ void __launch_bounds__(LG_RT)
+    lg_multi_render_chi2(const lg_model* __restrict__ models, const lg_sysinfo* __restrict__ info,
+                         const lg_sysplan* __restrict__ plan, const long long* __restrict__ hdr,
+                         const float* __restrict__ images, const float* __restrict__ weights,
+                         double* __restrict__ partials)
+{
+    lg_multi_render_body<false>(models, info, plan, hdr, nullptr, images, weights, partials);
+}
+
+// ----------------------------------------------------------- convolve --
+// One 32x32 output tile of one candidate of one system, for a PSF shape
+// known at compile time (same order and clamping as the single-system
+// kernel, kernel/lensed.cl:56-103); the PSF is staged in shared memory.
+template <int PW, int PH>
+LG_DEV double lg_multi_conv_unit(const float* __restrict__ src, const float* __restrict__ psf_g, int W, int H,
+                                 int X0, int Y0, const float* __restrict__ image, const float* __restrict__ weight,
+                                 float* smem)
+{
+    constexpr int OX = PW - 1 - PW / 2, OY = PH - 1 - PH / 2;
+    constexpr int WIN4 = (LG_CR + PW - 1 + 3) / 4 * 4;
+    constexpr int NEED = LG_CTX - LG_CR + WIN4;
+    constexpr int TWP = ((NEED + 27) / 32) * 32 + 4;
+    constexpr int TH = LG_CTY + PH - 1;
+    float* tile = smem;
+    float* psf = smem + TH * TWP;
+    const int tid = threadIdx.y * blockDim.x + threadIdx.x;
+    const int br = Y0 + OY - (PH - 1), bc = X0 + OX - (PW - 1);
+    for (int i = tid; i < TH * TWP; i += LG_CTHREADS) {
+        const int r = i / TWP, c = i - r * TWP;
+        int gy = br + r, gx = bc + c;
+        gy = gy < 0 ? 0 : (gy > H - 1 ? H - 1 : gy);
+        gx = gx < 0 ? 0 : (gx > W - 1 ? W - 1 : gx);
+        tile[i] = src[gy * W + gx];
+    }
+    for (int i = tid; i < PW * PH; i += LG_CTHREADS) psf[i] = psf_g[i];
+    __syncthreads();
+    const int lx0 = threadIdx.x * LG_CR, ly = threadIdx.y;
+    float acc[LG_CR];
+#pragma unroll
+    for (int o = 0; o < LG_CR; ++o) acc[o] = 0.0f;
+#pragma unroll 1
+    for (int j = 0; j < PH; ++j) {
+        const float4* row = reinterpret_cast<const float4*>(tile + (ly + PH - 1 - j) * TWP + lx0);
+        float win[WIN4];
+#pragma unroll
+        for (int t = 0; t < WIN4 / 4; ++t) {
+            const float4 q = row[t];
+            win[4 * t + 0] = q.x;
+            win[4 * t + 1] = q.y;
+            win[4 * t + 2] = q.z;
+            win[4 * t + 3] = q.w;
+        }
+        const float* prow = psf + j * PW;
+#pragma unroll
+        for (int i = 0; i < PW; ++i) {
+            const float p = prow[i];
+#pragma unroll
+            for (int o = 0; o < LG_CR; ++o) acc[o] += p * win[o + PW - 1 - i];
+        }
+    }
+    double s = 0.0;
+    const int gy = Y0 + ly;
+    if (gy < H) {
+#pragma unroll
+        for (int o = 0; o < LG_CR; ++o) {
+            const int gx = X0 + lx0 + o;
+            if (gx < W) {
+                const int k = gy * W + gx;
+                const float d = acc[o] - image[k];
+                s += (double)(weight[k] * d * d);
+            }
+        }
+    }
+    return s;
+}
+
+extern "C" __global__ void __launch_bounds__(LG_CTHREADS)
+    lg_multi_conv_chi2(const float* __restrict__ raw, const lg_sysinfo* __restrict__ info,
+                       const lg_sysplan* __restrict__ plan, const long long* __restrict__ hdr,
+                       const float* __restrict__ images, const float* __restrict__ weights,
+                       const float* __restrict__ psfs, double* __restrict__ partials)
+{
+    extern __shared__ float4 lg_msmem4[];
+    float* smem = reinterpret_cast<float*>(lg_msmem4);
+    __shared__ double red[LG_CTHREADS / 32];
+    const long long U = hdr[1];
+    const int nsys = (int)hdr[3];
+    for (long long u = blockIdx.x; u < U; u += gridDim.x) {
+        const int s = lg_find_system(plan, nsys, u, true);
+        const lg_sysinfo I = info[s];
+        const lg_sysplan P = plan[s];
+        const long long local = u - P.c_unit0;
+        const int b = (int)(local / I.ctiles), t = (int)(local - (long long)b * I.ctiles);
+        const int ty = t / I.ctiles_x, tx = t - ty * I.ctiles_x;
+        const float* src = raw + P.raw0 + (long long)b * I.N;
+        const float* img = images + I.img_off;
+        const float* wht = weights + I.img_off;
+        const float* psf = psfs + I.psf_off;
+        double acc = 0.0;
+        switch (I.pw * 1024 + I.ph) {
+#define LG_PSF_CASE(w, h)                                                                                 \
+    case (w) * 1024 + (h):                                                                               \
+        acc = lg_multi_conv_unit<w, h>(src, psf, I.W, I.H, tx * LG_CTX, ty * LG_CTY, img, wht, smem);    \
+        break;
+            LG_PSF_SHAPES
+#undef LG_PSF_CASE
+        default:
+            break;
+        }
+        acc = lg_block_sum<LG_CTHREADS>(acc, red);
+        if (threadIdx.x == 0 && threadIdx.y == 0) partials[P.part0 + (long long)b * I.ctiles + t] = acc;
+    }
+}
+
+// ------------------------------------------------------------- finish --
+// logL of every candidate from its partials, in a fixed order.
+extern "C" __global__ void __launch_bounds__(256)
+    lg_multi_finish(const double* __restrict__ partials, const lg_sysinfo* __restrict__ info,
+                    const lg_sysplan* __restrict__ plan, const long long* __restrict__ hdr, int with_psf,
+                    double* __restrict__ logL)
+{
+    __shared__ double red[8];
+    const int C = (int)hdr[2], nsys = (int)hdr[3];
+    for (int c = blockIdx.x; c < C; c += gridDim.x) {
+        int s = 0;
+        while (s + 1 < nsys && plan[s + 1].cand0 <= c) ++s;
+        const int n = with_psf ? info[s].ctiles : info[s].rtiles;
+        const double* p = partials + plan[s].part0 + (long long)(c - plan[s].cand0) * n;
+        double acc = 0.0;
+        for (int t = threadIdx.x; t < n; t += 256) acc += p[t];
+        acc = lg_block_sum<256>(acc, red);
+        if (threadIdx.x == 0) logL[c] = -0.5 * acc;
+    }
+}

@@ -127,3 +127,17 @@ def test_benchmark_workloads_compose(native, name):
 
     s = getattr(workloads, name)()
     lg.compile_check(s.width, s.height, s.objects, psf=s.psf, rule=s.rule)
+
+
+def test_systems_program_composes_without_gpu(native):
+    """lg_systems_create compiles its programs before touching the GPU: on a
+    machine without one it must fail with a CUDA error, not a compile error."""
+    from lensed_gb300 import workloads
+    import torch
+
+    if torch.cuda.is_available():
+        pytest.skip("GPU present: covered by the GPU tests")
+    syst = workloads.systems(count=3)
+    with pytest.raises(lg.LensedError) as e:
+        lg.Systems([(s.image, s.weight, s.psf, None) for s in syst], syst[0].objects, capacity=[4, 4, 4])
+    assert e.value.code == -3, str(e.value)
