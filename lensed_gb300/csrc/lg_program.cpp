@@ -230,6 +230,14 @@ int compile_program(const std::string& src, bool fmad, std::vector<char>& cubin,
     opts.push_back(ieee_divsqrt ? "--prec-div=true" : "--prec-div=false");
     opts.push_back(ieee_divsqrt ? "--prec-sqrt=true" : "--prec-sqrt=false");
     opts.push_back(fmad ? "--fmad=true" : "--fmad=false");
+    if (const char* dump = std::getenv("LG_NVRTC_DUMP")) {
+        static int seq = 0;
+        std::string path = std::string(dump) + "." + std::to_string(seq++) + ".cu";
+        if (FILE* f = std::fopen(path.c_str(), "w")) {
+            std::fputs(src.c_str(), f);
+            std::fclose(f);
+        }
+    }
     if (std::getenv("LG_NVRTC_VERBOSE")) {
         std::fprintf(stderr, "lensed_gb300: nvrtc");
         for (const char* o : opts) std::fprintf(stderr, " %s", o);
