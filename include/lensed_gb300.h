@@ -229,6 +229,68 @@ int lg_systems_npars(const lg_systems* S);
  * same order.  Each system's values equal those of its own lg_ctx. */
 int lg_systems_eval(lg_systems* S, const double* params, const int* counts, double* logL);
 
+/* ------------------------------------------------------- nested sampling */
+/* The sampler that replaces MultiNest's role (src/lensed.c:1236-1288):
+ * nested sampling over the unit cube with one enlarged bounding ellipsoid
+ * (Mukherjee, Parkinson & Liddle 2006), proposals drawn and evaluated in
+ * batches, FP64 log-sum-exp evidence; optionally a learned coupling-flow
+ * proposal trained on the live points (the ellipsoid stays the fallback). */
+#define LG_PROPOSAL_ELLIPSOID 0
+#define LG_PROPOSAL_FLOW 1
+
+typedef struct {
+    int nlive;      /* live points (reference option nlive) */
+    double tol;     /* stop when the live points can raise ln Z by less than tol */
+    double efr;     /* ellipsoid volume enlargement factor 1/efr */
+    int batch;      /* proposals per batched likelihood call */
+    int seed;       /* random seed (-1: from the clock) */
+    long maxiter;   /* 0: unlimited */
+    int proposal;   /* LG_PROPOSAL_* */
+    int flow_every; /* retrain the flow every this many replacements */
+} lg_nested_options;
+
+typedef struct {
+    double logz, logz_err, information, max_logl;
+    long ncall, niter, nsamples, n_flow_proposals, n_ellipsoid_proposals;
+    double wall_s;
+    double* mean;          /* ndims, caller-owned, or NULL: posterior means (cube) */
+    double* std;           /* ndims, or NULL */
+    double* samples;       /* max_samples x ndims, or NULL: dead + final live points */
+    double* sample_logwt;  /* max_samples, or NULL: log posterior weights */
+    long max_samples;
+} lg_nested_result;
+
+/* Learned proposal: affine coupling layers with MLP conditioners, trained by
+ * maximum likelihood on the live points with hand-written CUDA kernels. */
+typedef struct {
+    int layers;     /* coupling layers (default 8) */
+    int width;      /* hidden units (default 128) */
+    int hidden;     /* hidden layers per conditioner (default 2) */
+    int epochs;     /* training epochs per retraining (default 200) */
+    int batch;      /* training batch (default 256) */
+    double lr;      /* Adam learning rate (default 1e-3) */
+    double expand;  /* latent radius enlargement over the live points (default 1.1) */
+} lg_flow_options;
+
+typedef int (*lg_batch_loglike)(void* user, const double* cube, int B, double* logL);
+
+lg_nested_options lg_nested_defaults(void);
+lg_flow_options lg_flow_defaults(void);
+int lg_nested_sample(int ndims, lg_batch_loglike fn, void* user, const lg_nested_options* opts,
+                     lg_nested_result* result);
+/* Loss and gradient of a flow with the given parameters on n points
+ * (standardised coordinates), for gradient checks; bf16 = 0 keeps hidden
+ * activations in FP32. */
+long lg_flow_nparams(int d, int layers, int width, int hidden);
+int lg_flow_loss_grad(int device, int d, int layers, int width, int hidden, int bf16, const float* params,
+                      const float* x, int n, float* loss, float* grad);
+/* lg_nested_sample with the learned proposal on the given CUDA device. */
+int lg_nested_sample_flow(int ndims, lg_batch_loglike fn, void* user, const lg_nested_options* opts,
+                          const lg_flow_options* flow, int device, lg_nested_result* result);
+/* Nested sampling of a context's posterior (cube -> priors -> GPU logL). */
+int lg_nested_run(lg_ctx* ctx, const lg_nested_options* opts, const lg_flow_options* flow,
+                  lg_nested_result* result);
+
 /* Drop-in for the reference's likelihood callback (src/nested.h:3): ctx is
  * an lg_ctx*.  cube[0..ndim) holds unit-cube values and is overwritten with
  * the physical values of all npar parameters (map order); *lnew receives

@@ -49,6 +49,29 @@ class _ObjectDesc(C.Structure):
     _fields_ = [("name", C.c_char_p), ("id", C.c_char_p), ("priors", C.POINTER(C.c_char_p))]
 
 
+class NestedOptions(C.Structure):
+    _fields_ = [("nlive", C.c_int), ("tol", C.c_double), ("efr", C.c_double), ("batch", C.c_int),
+                ("seed", C.c_int), ("maxiter", C.c_long), ("proposal", C.c_int), ("flow_every", C.c_int)]
+
+
+class NestedResult(C.Structure):
+    _fields_ = [("logz", C.c_double), ("logz_err", C.c_double), ("information", C.c_double),
+                ("max_logl", C.c_double), ("ncall", C.c_long), ("niter", C.c_long), ("nsamples", C.c_long),
+                ("n_flow_proposals", C.c_long), ("n_ellipsoid_proposals", C.c_long), ("wall_s", C.c_double),
+                ("mean", C.POINTER(C.c_double)), ("std", C.POINTER(C.c_double)),
+                ("samples", C.POINTER(C.c_double)), ("sample_logwt", C.POINTER(C.c_double)),
+                ("max_samples", C.c_long)]
+
+
+class FlowOptions(C.Structure):
+    _fields_ = [("layers", C.c_int), ("width", C.c_int), ("hidden", C.c_int), ("epochs", C.c_int),
+                ("batch", C.c_int), ("lr", C.c_double), ("expand", C.c_double)]
+
+
+BATCH_LOGLIKE = C.CFUNCTYPE(C.c_int, C.c_void_p, C.POINTER(C.c_double), C.c_int, C.POINTER(C.c_double))
+PROPOSAL_ELLIPSOID, PROPOSAL_FLOW = 0, 1
+
+
 class _Options(C.Structure):
     _fields_ = [("rule", C.c_char_p), ("device", C.c_int), ("max_batch", C.c_int), ("flags", C.c_int)]
 
@@ -96,6 +119,17 @@ def lib():
         "lg_systems_last_error": (C.c_char_p, [vp]),
         "lg_systems_npars": (C.c_int, [vp]),
         "lg_systems_eval": (C.c_int, [vp, dp, ip, dp]),
+        "lg_nested_defaults": (NestedOptions, []),
+        "lg_flow_defaults": (FlowOptions, []),
+        "lg_nested_sample": (C.c_int, [C.c_int, BATCH_LOGLIKE, vp, C.POINTER(NestedOptions),
+                                       C.POINTER(NestedResult)]),
+        "lg_nested_sample_flow": (C.c_int, [C.c_int, BATCH_LOGLIKE, vp, C.POINTER(NestedOptions),
+                                            C.POINTER(FlowOptions), C.c_int, C.POINTER(NestedResult)]),
+        "lg_nested_run": (C.c_int, [vp, C.POINTER(NestedOptions), C.POINTER(FlowOptions),
+                                    C.POINTER(NestedResult)]),
+        "lg_flow_nparams": (C.c_long, [C.c_int, C.c_int, C.c_int, C.c_int]),
+        "lg_flow_loss_grad": (C.c_int, [C.c_int, C.c_int, C.c_int, C.c_int, C.c_int, C.c_int, fp, fp, C.c_int,
+                                        fp, fp]),
         "loglike": (None, [dp, ip, ip, dp, vp]),
     }
     for name, (res, args) in sig.items():
@@ -161,6 +195,97 @@ def measure_fp32_peak(device: int = 0) -> float:
     if rc:
         raise LensedError(rc, "fp32 peak probe")
     return v.value
+
+
+def _nested_opts(**kw):
+    o = lib().lg_nested_defaults()
+    for k, v in kw.items():
+        if not hasattr(o, k):
+            raise TypeError(f"unknown nested option {k}")
+        setattr(o, k, v)
+    return o
+
+
+def _flow_opts(**kw):
+    o = lib().lg_flow_defaults()
+    for k, v in kw.items():
+        if not hasattr(o, k):
+            raise TypeError(f"unknown flow option {k}")
+        setattr(o, k, v)
+    return o
+
+
+def _result(nd, max_samples):
+    r = NestedResult()
+    arrays = {"mean": np.zeros(nd), "std": np.zeros(nd), "samples": np.zeros((max_samples, nd)),
+              "logwt": np.zeros(max_samples)}
+    r.mean, r.std = _p(arrays["mean"], C.c_double), _p(arrays["std"], C.c_double)
+    r.samples, r.sample_logwt = _p(arrays["samples"], C.c_double), _p(arrays["logwt"], C.c_double)
+    r.max_samples = max_samples
+    return r, arrays
+
+
+def _pack(r, arrays):
+    n = min(r.nsamples, r.max_samples)
+    return {"logz": r.logz, "logz_err": r.logz_err, "information": r.information, "max_logl": r.max_logl,
+            "ncall": r.ncall, "niter": r.niter, "nsamples": r.nsamples, "wall_s": r.wall_s,
+            "n_flow_proposals": r.n_flow_proposals, "n_ellipsoid_proposals": r.n_ellipsoid_proposals,
+            "mean": arrays["mean"], "std": arrays["std"], "samples": arrays["samples"][:n],
+            "logwt": arrays["logwt"][:n]}
+
+
+def nested_sample(loglike, ndims: int, max_samples: int = 200000, **opts):
+    """Nested sampling of a batched log-likelihood over the unit cube.
+
+    loglike(cube) receives a (B, ndims) array and returns B log-likelihoods."""
+    err = []
+
+    def cb(_user, cube, B, out):
+        try:
+            x = np.ctypeslib.as_array(cube, shape=(B, ndims))
+            res = np.asarray(loglike(x.copy()), dtype=np.float64)
+            np.ctypeslib.as_array(out, shape=(B,))[:] = res
+            return 0
+        except Exception as e:  # reported after the call
+            err.append(e)
+            return -1
+
+    f = BATCH_LOGLIKE(cb)
+    o = _nested_opts(**opts)
+    r, arrays = _result(ndims, max_samples)
+    rc = lib().lg_nested_sample(ndims, f, None, C.byref(o), C.byref(r))
+    if err:
+        raise err[0]
+    if rc:
+        raise LensedError(rc, lib().lg_last_error(None).decode(errors="replace"))
+    return _pack(r, arrays)
+
+
+def nested_sample_flow(loglike, ndims: int, max_samples: int = 200000, flow: dict | None = None, device: int = 0,
+                       **opts):
+    """nested_sample with the learned coupling-flow proposal (needs a GPU)."""
+    err = []
+
+    def cb(_user, cube, B, out):
+        try:
+            x = np.ctypeslib.as_array(cube, shape=(B, ndims))
+            np.ctypeslib.as_array(out, shape=(B,))[:] = np.asarray(loglike(x.copy()), dtype=np.float64)
+            return 0
+        except Exception as e:
+            err.append(e)
+            return -1
+
+    f = BATCH_LOGLIKE(cb)
+    o = _nested_opts(**opts)
+    o.proposal = PROPOSAL_FLOW
+    fo = _flow_opts(**(flow or {}))
+    r, arrays = _result(ndims, max_samples)
+    rc = lib().lg_nested_sample_flow(ndims, f, None, C.byref(o), C.byref(fo), device, C.byref(r))
+    if err:
+        raise err[0]
+    if rc:
+        raise LensedError(rc, lib().lg_last_error(None).decode(errors="replace"))
+    return _pack(r, arrays)
 
 
 def make_weight(image, weight_map=None, gain=None, gain_value=1.0, offset=0.0, xweight=None, mask=None):
@@ -368,6 +493,14 @@ class Context:
         self._check(lib().lg_render(self.h, _p(p, C.c_double), _p(m, C.c_float), _p(r, C.c_float),
                                     _p(e, C.c_float)))
         return m, r, e
+
+    def nested(self, max_samples: int = 200000, flow: dict | None = None, **opts):
+        """Nested sampling of this context's posterior (unit-cube means/samples)."""
+        o = _nested_opts(**opts)
+        fo = _flow_opts(**(flow or {}))
+        r, arrays = _result(self.ndims, max_samples)
+        self._check(lib().lg_nested_run(self.h, C.byref(o), C.byref(fo), C.byref(r)))
+        return _pack(r, arrays)
 
     def loglike(self, cube):
         """The reference callback signature: returns (logL, physical params)."""

@@ -186,6 +186,9 @@ struct lg_ctx {
     }
 };
 
+int lg::ctx_device(const lg_ctx* c) { return c ? c->device : 0; }
+int lg::ctx_max_batch(const lg_ctx* c) { return c ? c->max_batch : 0; }
+
 namespace {
 
 // Launch shape for a model (tile sizes chosen for GB300; see the design

@@ -25,6 +25,8 @@ struct Driver {
 };
 const Driver* driver();
 void set_global_error(const char* msg);
+int ctx_device(const lg_ctx* c);
+int ctx_max_batch(const lg_ctx* c);
 
 // ------------------------------------------------------------------ plugins
 struct ParamDef {

@@ -1,0 +1,395 @@
+// Nested sampling over the unit cube with batched likelihood calls.
+//
+// Lensed delegates sampling to MultiNest (src/lensed.c:1236-1288, external
+// Fortran, not part of the reference).  This file provides the sampler the
+// likelihood path needs in its place, written from the published method:
+// nested sampling (Skilling 2004/2006) with live points bounded by one
+// enlarged ellipsoid (Mukherjee, Parkinson & Liddle 2006; the single-
+// ellipsoid case of Feroz & Hobson 2008).  Proposals are drawn in batches and
+// evaluated with one batched likelihood call; every evaluated proposal is
+// kept in a pool and used, in draw order, for later replacements while its
+// logL exceeds the moving threshold (a draw uniform in the ellipsoid is still
+// uniform in the ellipsoid after the threshold rises).
+//
+// The evidence is accumulated as a log-sum-exp in double precision, with
+// Skilling's information H and the error sqrt(H / nlive).  A learned
+// proposal (lg_flow.cu) can replace the ellipsoid; the ellipsoid remains the
+// fallback and the judge of the learned sampler.
+
+#include <algorithm>
+#include <chrono>
+#include <cmath>
+#include <cstdint>
+#include <cstring>
+#include <limits>
+#include <memory>
+#include <string>
+#include <vector>
+
+#include "lg_internal.h"
+#include "lg_nested.h"
+
+namespace lg {
+
+// Bounding ellipsoid of a set of points: centre, Cholesky factor of the
+// covariance scaled so that every point lies inside.
+struct Ellipsoid {
+    int d = 0;
+    std::vector<double> mu, L;  // L lower triangular, row-major d x d
+    double scale = 1;           // (x-mu)^T C^-1 (x-mu) <= scale defines the boundary
+
+    bool fit(const std::vector<double>& pts, int n, int dim, double enlarge_volume)
+    {
+        d = dim;
+        mu.assign(d, 0);
+        for (int i = 0; i < n; ++i)
+            for (int k = 0; k < d; ++k) mu[k] += pts[(size_t)i * d + k];
+        for (auto& m : mu) m /= n;
+        std::vector<double> C((size_t)d * d, 0);
+        for (int i = 0; i < n; ++i)
+            for (int a = 0; a < d; ++a) {
+                const double xa = pts[(size_t)i * d + a] - mu[a];
+                for (int b = 0; b <= a; ++b) C[(size_t)a * d + b] += xa * (pts[(size_t)i * d + b] - mu[b]);
+            }
+        for (int a = 0; a < d; ++a)
+            for (int b = 0; b <= a; ++b) C[(size_t)a * d + b] /= n;
+        // Cholesky with a small diagonal floor for degenerate point sets
+        L.assign((size_t)d * d, 0);
+        for (int a = 0; a < d; ++a) {
+            for (int b = 0; b <= a; ++b) {
+                double s = C[(size_t)a * d + b];
+                for (int k = 0; k < b; ++k) s -= L[(size_t)a * d + k] * L[(size_t)b * d + k];
+                if (a == b) {
+                    if (s <= 1e-30) s = 1e-30;
+                    L[(size_t)a * d + a] = std::sqrt(s);
+                } else {
+                    L[(size_t)a * d + b] = s / L[(size_t)b * d + b];
+                }
+            }
+        }
+        double kmax = 0;
+        std::vector<double> y(d);
+        for (int i = 0; i < n; ++i) {
+            kmax = std::max(kmax, mahalanobis(&pts[(size_t)i * d], y));
+        }
+        scale = kmax * std::pow(enlarge_volume, 2.0 / d);
+        return std::isfinite(scale) && scale > 0;
+    }
+    double mahalanobis(const double* x, std::vector<double>& y) const
+    {
+        double m = 0;
+        for (int a = 0; a < d; ++a) {
+            double s = x[a] - mu[a];
+            for (int k = 0; k < a; ++k) s -= L[(size_t)a * d + k] * y[k];
+            y[a] = s / L[(size_t)a * d + a];
+            m += y[a] * y[a];
+        }
+        return m;
+    }
+    // uniform draw inside the ellipsoid
+    void sample(Rng& r, double* x, std::vector<double>& u) const
+    {
+        double n2 = 0;
+        for (int a = 0; a < d; ++a) {
+            u[a] = r.normal();
+            n2 += u[a] * u[a];
+        }
+        const double rad = std::pow(r.uniform(), 1.0 / d) / std::sqrt(n2) * std::sqrt(scale);
+        for (int a = 0; a < d; ++a) {
+            double s = 0;
+            for (int k = 0; k <= a; ++k) s += L[(size_t)a * d + k] * u[k];
+            x[a] = mu[a] + rad * s;
+        }
+    }
+    // log volume of the ellipsoid (for diagnostics)
+    double log_volume() const
+    {
+        double lv = 0.5 * d * std::log(M_PI) - std::lgamma(0.5 * d + 1) + 0.5 * d * std::log(scale);
+        for (int a = 0; a < d; ++a) lv += std::log(L[(size_t)a * d + a]);
+        return lv;
+    }
+};
+
+namespace {
+
+double logaddexp(double a, double b)
+{
+    if (a == -HUGE_VAL) return b;
+    if (b == -HUGE_VAL) return a;
+    const double m = std::max(a, b);
+    return m + std::log(std::exp(a - m) + std::exp(b - m));
+}
+
+}  // namespace
+
+int nested_sample(int nd, lg_batch_loglike fn, void* user, const lg_nested_options* o, lg_nested_result* res,
+                  Proposal* learned, std::string& err)
+{
+    const auto t0 = std::chrono::steady_clock::now();
+    lg_nested_options opt = lg_nested_defaults();
+    if (o) opt = *o;
+    if (nd <= 0 || !fn || !res || opt.nlive < nd + 1 || opt.batch <= 0) {
+        err = "nested sampling: invalid arguments (nlive must exceed the dimension)";
+        return LG_ERR_INPUT;
+    }
+    const int nl = opt.nlive, B = opt.batch;
+    Rng rng((uint64_t)(opt.seed < 0 ? std::chrono::steady_clock::now().time_since_epoch().count() : opt.seed));
+    std::vector<double> live((size_t)nl * nd), llive(nl);
+    std::vector<double> buf((size_t)B * nd), lbuf(B);
+    long ncall = 0;
+    auto evaluate = [&](const double* x, int n, double* l) {
+        int rc = fn(user, x, n, l);
+        ncall += n;
+        return rc;
+    };
+    // initial live points: uniform in the cube
+    for (int i0 = 0; i0 < nl; i0 += B) {
+        const int n = std::min(B, nl - i0);
+        for (size_t k = 0; k < (size_t)n * nd; ++k) buf[k] = rng.uniform();
+        if (int rc = evaluate(buf.data(), n, lbuf.data())) {
+            err = "likelihood callback failed";
+            return rc;
+        }
+        for (int i = 0; i < n; ++i) {
+            std::memcpy(&live[(size_t)(i0 + i) * nd], &buf[(size_t)i * nd], nd * sizeof(double));
+            llive[i0 + i] = std::isnan(lbuf[i]) ? -HUGE_VAL : lbuf[i];
+        }
+    }
+    // dead points
+    std::vector<double> dead_x;
+    std::vector<double> dead_l, dead_lw;
+    double logz = -HUGE_VAL, H = 0, logx = 0;
+    const double dlogx = 1.0 / nl;
+    const double lw_step = std::log1p(-std::exp(-dlogx));  // log(1 - e^{-1/nl})
+    // pool of evaluated proposals, used in draw order
+    std::vector<double> pool_x;
+    std::vector<double> pool_l;
+    size_t pool_pos = 0;
+    Ellipsoid ell;
+    std::vector<double> u(nd), y(nd);
+    long iter = 0, since_train = 0, n_flow = 0, n_ell = 0;
+    bool use_flow = false;
+    int status = LG_OK;
+    for (;; ++iter) {
+        if (opt.maxiter > 0 && iter >= opt.maxiter) break;
+        int imin = 0;
+        double lmax = -HUGE_VAL;
+        for (int i = 0; i < nl; ++i) {
+            if (llive[i] < llive[imin]) imin = i;
+            lmax = std::max(lmax, llive[i]);
+        }
+        // termination: the live points can still add at most X * Lmax
+        if (iter > 0 && logaddexp(logz, logx + lmax) - logz < opt.tol) break;
+        const double lmin = llive[imin];
+        const double lw = logx + lw_step + lmin;
+        const double lznew = logaddexp(logz, lw);
+        H = (lmin == -HUGE_VAL ? 0 : std::exp(lw - lznew) * lmin) +
+            (logz == -HUGE_VAL ? 0 : std::exp(logz - lznew) * (H + logz)) - lznew;
+        logz = lznew;
+        logx -= dlogx;
+        dead_x.insert(dead_x.end(), &live[(size_t)imin * nd], &live[(size_t)imin * nd] + nd);
+        dead_l.push_back(lmin);
+        dead_lw.push_back(lw);
+        // learned proposal: (re)train every flow_every replacements
+        if (learned && opt.flow_every > 0 && since_train >= opt.flow_every) {
+            since_train = 0;
+            use_flow = learned->train(live.data(), nl, nd) == LG_OK;
+            pool_x.clear();
+            pool_l.clear();
+            pool_pos = 0;
+        }
+        // replacement: next pool point above the threshold, else a new batch
+        bool replaced = false;
+        for (int attempt = 0; attempt < 100000 && !replaced; ++attempt) {
+            while (pool_pos < pool_l.size() && !(pool_l[pool_pos] > lmin)) ++pool_pos;
+            if (pool_pos < pool_l.size()) {
+                std::memcpy(&live[(size_t)imin * nd], &pool_x[pool_pos * nd], nd * sizeof(double));
+                llive[imin] = pool_l[pool_pos];
+                ++pool_pos;
+                replaced = true;
+                break;
+            }
+            // propose a batch
+            int n = 0;
+            if (use_flow) {
+                n = learned->propose(live.data(), nl, nd, buf.data(), B, rng.next());
+                if (n <= 0) use_flow = false;
+                else n_flow += n;
+            }
+            if (!use_flow) {
+                // the ellipsoid bounds the live points other than the one leaving
+                std::vector<double> others;
+                others.reserve((size_t)(nl - 1) * nd);
+                for (int i = 0; i < nl; ++i)
+                    if (i != imin) others.insert(others.end(), &live[(size_t)i * nd], &live[(size_t)i * nd] + nd);
+                if (!ell.fit(others, nl - 1, nd, 1.0 / opt.efr)) {
+                    err = "nested sampling: degenerate live points";
+                    return LG_ERR_INPUT;
+                }
+                long tries = 0;
+                while (n < B && tries < 1000L * B) {
+                    ++tries;
+                    double* x = &buf[(size_t)n * nd];
+                    ell.sample(rng, x, u);
+                    bool in = true;
+                    for (int a = 0; a < nd && in; ++a) in = x[a] >= 0 && x[a] <= 1;
+                    if (in) ++n;
+                }
+                n_ell += n;
+                if (n == 0) {
+                    err = "nested sampling: ellipsoid left the unit cube";
+                    return LG_ERR_INPUT;
+                }
+            }
+            if (int rc = evaluate(buf.data(), n, lbuf.data())) {
+                err = "likelihood callback failed";
+                return rc;
+            }
+            pool_x.assign(buf.begin(), buf.begin() + (size_t)n * nd);
+            pool_l.assign(lbuf.begin(), lbuf.begin() + n);
+            for (auto& v : pool_l)
+                if (std::isnan(v)) v = -HUGE_VAL;
+            pool_pos = 0;
+        }
+        if (!replaced) {
+            status = LG_ERR_TIMEOUT;
+            err = "nested sampling: no replacement found above the threshold";
+            break;
+        }
+        ++since_train;
+    }
+    // remaining live points share the last prior volume
+    const double lwl = logx - std::log((double)nl);
+    for (int i = 0; i < nl; ++i) {
+        const double lw = lwl + llive[i];
+        const double lznew = logaddexp(logz, lw);
+        H = (llive[i] == -HUGE_VAL ? 0 : std::exp(lw - lznew) * llive[i]) +
+            (logz == -HUGE_VAL ? 0 : std::exp(logz - lznew) * (H + logz)) - lznew;
+        logz = lznew;
+        dead_x.insert(dead_x.end(), &live[(size_t)i * nd], &live[(size_t)i * nd] + nd);
+        dead_l.push_back(llive[i]);
+        dead_lw.push_back(lw);
+    }
+    // posterior moments in the cube
+    const size_t ns = dead_l.size();
+    std::vector<double> mean(nd, 0), m2(nd, 0);
+    double wsum = 0, lmax = -HUGE_VAL;
+    for (size_t i = 0; i < ns; ++i) {
+        const double w = std::exp(dead_lw[i] - logz);
+        wsum += w;
+        lmax = std::max(lmax, dead_l[i]);
+        for (int a = 0; a < nd; ++a) {
+            mean[a] += w * dead_x[i * nd + a];
+            m2[a] += w * dead_x[i * nd + a] * dead_x[i * nd + a];
+        }
+    }
+    res->logz = logz;
+    res->logz_err = std::sqrt(std::max(H, 0.0) / nl);
+    res->information = H;
+    res->max_logl = lmax;
+    res->ncall = ncall;
+    res->niter = iter;
+    res->nsamples = (long)ns;
+    res->n_flow_proposals = n_flow;
+    res->n_ellipsoid_proposals = n_ell;
+    res->wall_s = std::chrono::duration<double>(std::chrono::steady_clock::now() - t0).count();
+    if (res->mean && res->std)
+        for (int a = 0; a < nd; ++a) {
+            res->mean[a] = mean[a] / wsum;
+            res->std[a] = std::sqrt(std::max(m2[a] / wsum - res->mean[a] * res->mean[a], 0.0));
+        }
+    if (res->samples && res->sample_logwt && res->max_samples > 0) {
+        const size_t n = std::min(ns, (size_t)res->max_samples);
+        std::memcpy(res->samples, dead_x.data(), n * nd * sizeof(double));
+        for (size_t i = 0; i < n; ++i) res->sample_logwt[i] = dead_lw[i] - logz;
+    }
+    return status;
+}
+
+}  // namespace lg
+
+extern "C" {
+
+lg_nested_options lg_nested_defaults(void)
+{
+    lg_nested_options o;
+    std::memset(&o, 0, sizeof o);
+    o.nlive = 300;     // src/input/options.c: nlive default
+    o.tol = 0.1;       // src/input/options.c: tol default
+    o.efr = 0.8;       // ellipsoid volume enlargement 1/efr
+    o.batch = 1024;
+    o.seed = 1;
+    o.maxiter = 0;
+    o.proposal = LG_PROPOSAL_ELLIPSOID;
+    o.flow_every = 1000;
+    return o;
+}
+
+int lg_nested_sample(int ndims, lg_batch_loglike fn, void* user, const lg_nested_options* opts,
+                     lg_nested_result* result)
+{
+    std::string err;
+    int rc = lg::nested_sample(ndims, fn, user, opts, result, nullptr, err);
+    if (rc) lg::set_global_error(err.c_str());
+    return rc;
+}
+
+}  // extern "C"
+
+namespace {
+
+struct CtxUser {
+    lg_ctx* ctx;
+    int max_batch;
+};
+
+int ctx_loglike(void* user, const double* cube, int B, double* logL)
+{
+    CtxUser* u = static_cast<CtxUser*>(user);
+    for (int b0 = 0; b0 < B; b0 += u->max_batch) {
+        const int n = std::min(u->max_batch, B - b0);
+        const int nd = lg_ndims(u->ctx);
+        int rc = lg_eval_cube_batch(u->ctx, cube + (size_t)b0 * nd, n, nullptr, logL + b0);
+        if (rc) return rc;
+    }
+    return LG_OK;
+}
+
+}  // namespace
+
+extern "C" int lg_nested_run(lg_ctx* ctx, const lg_nested_options* opts, const lg_flow_options* flow,
+                             lg_nested_result* result)
+{
+    if (!ctx || !result) return LG_ERR_INPUT;
+    lg_nested_options o = opts ? *opts : lg_nested_defaults();
+    CtxUser u{ctx, lg::ctx_max_batch(ctx)};
+    if (o.batch > u.max_batch) o.batch = u.max_batch;
+    std::string err;
+    std::unique_ptr<lg::Proposal> prop;
+    if (o.proposal == LG_PROPOSAL_FLOW) {
+        prop.reset(lg::make_flow_proposal(lg::ctx_device(ctx), lg_ndims(ctx), flow, err));
+        if (!prop) {
+            lg::set_global_error(err.c_str());
+            return LG_ERR_ALLOC;
+        }
+    }
+    int rc = lg::nested_sample(lg_ndims(ctx), ctx_loglike, &u, &o, result, prop.get(), err);
+    if (rc) lg::set_global_error(err.c_str());
+    return rc;
+}
+
+extern "C" int lg_nested_sample_flow(int ndims, lg_batch_loglike fn, void* user, const lg_nested_options* opts,
+                                     const lg_flow_options* flow, int device, lg_nested_result* result)
+{
+    std::string err;
+    std::unique_ptr<lg::Proposal> prop(lg::make_flow_proposal(device, ndims, flow, err));
+    if (!prop) {
+        lg::set_global_error(err.c_str());
+        return LG_ERR_ALLOC;
+    }
+    lg_nested_options o = opts ? *opts : lg_nested_defaults();
+    o.proposal = LG_PROPOSAL_FLOW;
+    int rc = lg::nested_sample(ndims, fn, user, &o, result, prop.get(), err);
+    if (rc) lg::set_global_error(err.c_str());
+    return rc;
+}

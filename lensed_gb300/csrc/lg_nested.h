@@ -1,0 +1,68 @@
+// Internal interface between the nested sampler and its learned proposal.
+#pragma once
+
+#include <cmath>
+#include <cstdint>
+#include <string>
+
+#include "lensed_gb300.h"
+
+namespace lg {
+
+// xoshiro256** (Blackman & Vigna 2018) seeded by splitmix64.
+struct Rng {
+    uint64_t s[4];
+    explicit Rng(uint64_t seed)
+    {
+        uint64_t z = seed + 0x9E3779B97F4A7C15ull;
+        for (auto& v : s) {
+            z += 0x9E3779B97F4A7C15ull;
+            uint64_t x = z;
+            x = (x ^ (x >> 30)) * 0xBF58476D1CE4E5B9ull;
+            x = (x ^ (x >> 27)) * 0x94D049BB133111EBull;
+            v = x ^ (x >> 31);
+        }
+    }
+    static uint64_t rotl(uint64_t x, int k) { return (x << k) | (x >> (64 - k)); }
+    uint64_t next()
+    {
+        const uint64_t r = rotl(s[1] * 5, 7) * 9, t = s[1] << 17;
+        s[2] ^= s[0];
+        s[3] ^= s[1];
+        s[1] ^= s[2];
+        s[0] ^= s[3];
+        s[2] ^= t;
+        s[3] = rotl(s[3], 45);
+        return r;
+    }
+    double uniform() { return (next() >> 11) * (1.0 / 9007199254740992.0); }
+    double normal()
+    {
+        // Marsaglia polar method
+        double u, v, q;
+        do {
+            u = 2 * uniform() - 1;
+            v = 2 * uniform() - 1;
+            q = u * u + v * v;
+        } while (q >= 1 || q == 0);
+        return u * std::sqrt(-2 * std::log(q) / q);
+    }
+};
+
+
+// A proposal that learns the constrained prior from the live points.
+// propose() fills up to B points (unit cube, row-major) that are uniform
+// within its region and returns how many; 0 or less means "not usable".
+struct Proposal {
+    virtual ~Proposal() {}
+    virtual int train(const double* live, int n, int d) = 0;
+    virtual int propose(const double* live, int n, int d, double* out, int B, uint64_t seed) = 0;
+};
+
+int nested_sample(int nd, lg_batch_loglike fn, void* user, const lg_nested_options* o, lg_nested_result* res,
+                  Proposal* learned, std::string& err);
+
+// Affine-coupling flow proposal trained and run on the GPU (lg_flow.cu).
+Proposal* make_flow_proposal(int device, int d, const lg_flow_options* opts, std::string& err);
+
+}  // namespace lg
