@@ -82,8 +82,11 @@ def run_sampler(args):
     s = workloads.small()
     ctx = lg.Context(s.image, s.weight, s.objects, rule=s.rule, max_batch=1024, flags=args.flags)
     out = {}
+    flow = {"layers": args.flow_layers, "width": args.flow_width, "epochs": args.flow_epochs}
     for name, kw in (("plain", {}), ("flow", {"proposal": lg.PROPOSAL_FLOW, "flow_every": 1000})):
-        r = ctx.nested(nlive=1000, batch=1024, tol=0.1, seed=11, **kw)
+        if name == "plain" and args.skip_plain:
+            continue
+        r = ctx.nested(nlive=1000, batch=1024, tol=0.1, seed=11, flow=flow, **kw)
         w = np.exp(r["logwt"])
         _, phys = ctx.eval_cube(r["samples"])
         mean_phys = (w[:, None] * phys).sum(0) / w.sum()
@@ -93,9 +96,10 @@ def run_sampler(args):
                      "posterior_mean": dict(zip(ctx.ids, [float(v) for v in mean_phys]))}
     line = {"metric": "calls & wall-time to lnZ (learned vs plain sampler)", "unit": "calls, s",
             "value": out["flow"]["ncall"], "higher_is_better": False, "n_gpus": 1, "dtype": "f32 (f64 evidence)",
-            "data": "synthetic", "config": {"workload": s.name, "nlive": 1000, "batch": 1024, "tol": 0.1},
-            "plain": out["plain"], "flow": out["flow"],
-            "dlogz": out["flow"]["logz"] - out["plain"]["logz"],
+            "data": "synthetic", "config": {"workload": s.name, "nlive": 1000, "batch": 1024, "tol": 0.1,
+                                            "flow": flow},
+            "plain": out.get("plain"), "flow": out["flow"],
+            "dlogz": out["flow"]["logz"] - out["plain"]["logz"] if "plain" in out else None,
             "truth": dict(zip(ctx.ids, [float(v) for v in ctx.to_map_order(s.truth)]))}
     print(json.dumps(line), flush=True)
 
@@ -292,6 +296,10 @@ def main():
     ap.add_argument("--batch", type=int, default=0)
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--flags", type=int, default=0, help="lg_options.flags (1 strict, 4 IEEE div/sqrt)")
+    ap.add_argument("--flow-layers", type=int, default=8)
+    ap.add_argument("--flow-width", type=int, default=128)
+    ap.add_argument("--flow-epochs", type=int, default=200)
+    ap.add_argument("--skip-plain", action="store_true")
     args = ap.parse_args()
     args.warmup = max(args.warmup, 3)
     if args.impl == "reference":

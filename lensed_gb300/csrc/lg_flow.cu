@@ -16,16 +16,20 @@
 //
 // Proposals (as nessai, Williams et al. 2021): z uniform in a ball of radius
 // `expand` x the largest latent radius of the live points, mapped back to the
-// cube; a draw is kept with probability |det dx/dz| / max over the batch,
-// which makes the kept draws uniform in the image of the ball; draws outside
-// the cube are dropped.  Every kept draw is then judged by the exact
-// likelihood in the sampler.
+// cube; a draw is kept with probability |det dx/dz| / W, W a bound calibrated
+// on a large latent sample at each training, which makes the kept draws
+// uniform in the image of the ball; draws outside the cube are dropped.  The
+// flow is trained with a held-out split and early stopping so that it stays
+// smooth; a flow whose calibrated kept fraction is below 1% is not used.
+// Every kept draw is then judged by the exact likelihood in the sampler.
 
 #include <cuda_bf16.h>
 #include <cuda_runtime.h>
 
 #include <algorithm>
 #include <cmath>
+#include <cstdio>
+#include <cstdlib>
 #include <cstring>
 #include <memory>
 #include <numeric>
@@ -236,6 +240,7 @@ public:
     DevBuf<float> P, G, M1, M2;
     std::vector<float> mean, sdev;
     long step = 0;
+    bool want_loss = true;  // read the loss back (off inside training loops)
 
     int da(int l) const { return (l % 2 == 0) ? h : d - h; }
     int a0(int l) const { return (l % 2 == 0) ? 0 : h; }
@@ -346,11 +351,13 @@ public:
             coupling_fwd<<<(M + T - 1) / T, T>>>(ul, ol, d, b0(l), db(l), M, ul + (size_t)M * d, ld.p);
         }
         nll<<<(M + T - 1) / T, T>>>(u.p + (size_t)L * M * d, ld.p, d, M, per.p, grad ? dz.p : nullptr);
-        std::vector<float> hp(M);
-        cudaMemcpy(hp.data(), per.p, (size_t)M * 4, cudaMemcpyDeviceToHost);
         double loss = 0;
-        for (float v : hp) loss += v;
-        loss /= M;
+        if (want_loss) {
+            std::vector<float> hp(M);
+            cudaMemcpy(hp.data(), per.p, (size_t)M * 4, cudaMemcpyDeviceToHost);
+            for (float v : hp) loss += v;
+            loss /= M;
+        }
         if (!grad) return (float)loss;
         cudaMemset(G.p, 0, nparams * 4);
         cudaMemcpy(dv.p, dz.p, (size_t)M * d * 4, cudaMemcpyDeviceToDevice);
@@ -433,9 +440,10 @@ public:
     int device = 0;
     uint64_t seed = 1;
     bool trained = false;
-    double radius = 0;
+    double radius = 0, last_loss = 0;
+    long ntrain = 0;
     std::vector<float> hx;
-    DevBuf<float> dx, dzlat, dulat;
+    DevBuf<float> dx, dzlat, dulat, dval, best;
 
     int train(const double* live, int n, int d) override
     {
@@ -460,29 +468,75 @@ public:
         for (int i = 0; i < n; ++i)
             for (int a = 0; a < d; ++a)
                 hx[(size_t)i * d + a] = (float)((live[(size_t)i * d + a] - flow.mean[a]) / flow.sdev[a]);
-        const int Mb = std::min(opt.batch, n);
-        if (!dx.ensure((size_t)n * d) || !flow.reserve(std::max(Mb, n))) return LG_ERR_ALLOC;
-        // minibatch Adam over shuffled live points
+        // hold out 20% of the live points for early stopping: the best
+        // weights on the held-out set are kept (the flow has far more
+        // parameters than there are live points)
         std::vector<int> idx(n);
         std::iota(idx.begin(), idx.end(), 0);
-        uint64_t s = seed ^ 0x5bd1e995u;
+        uint64_t s = seed ^ 0x5bd1e995u ^ ((uint64_t)ntrain << 32);
+        for (int i = n - 1; i > 0; --i) {
+            s = s * 6364136223846793005ull + 1442695040888963407ull;
+            std::swap(idx[i], idx[(s >> 33) % (uint64_t)(i + 1)]);
+        }
+        const int nval = std::max(1, n / 5), ntr = n - nval;
+        std::vector<float> vx((size_t)nval * d);
+        for (int i = 0; i < nval; ++i) std::memcpy(&vx[(size_t)i * d], &hx[(size_t)idx[ntr + i] * d], d * 4);
+        idx.resize(ntr);
+        const int Mb = std::min(opt.batch, ntr);
+        if (!dx.ensure((size_t)n * d) || !dval.ensure((size_t)nval * d) || !best.ensure(flow.nparams) ||
+            !flow.reserve(std::max(Mb, n)))
+            return LG_ERR_ALLOC;
+        cudaMemcpy(dval.p, vx.data(), vx.size() * 4, cudaMemcpyHostToDevice);
+        auto val_loss = [&]() {
+            flow.want_loss = true;
+            const float l = flow.loss_and_grad(dval.p, nval, false);
+            flow.want_loss = false;
+            return l;
+        };
+        float best_loss = val_loss();
+        cudaMemcpy(best.p, flow.P.p, flow.nparams * 4, cudaMemcpyDeviceToDevice);
+        int since_best = 0;
+        const int patience = 20;
         std::vector<float> bx((size_t)Mb * d);
-        for (int ep = 0; ep < opt.epochs; ++ep) {
-            for (int i = n - 1; i > 0; --i) {
+        // warm start: later retrainings continue from the previous weights
+        // with a quarter of the epochs
+        const int epochs = ntrain == 0 ? opt.epochs : std::max(1, opt.epochs / 4);
+        ++ntrain;
+        flow.want_loss = false;
+        const bool dbg = std::getenv("LG_FLOW_DEBUG") != nullptr;
+        for (int ep = 0; ep < epochs; ++ep) {
+            if (dbg && ntrain == 1 && (ep % 25 == 0)) {
+                flow.want_loss = true;
+                cudaMemcpy(dx.p, hx.data(), (size_t)n * d * 4, cudaMemcpyHostToDevice);
+                std::fprintf(stderr, "flow: epoch %d loss %.4f\n", ep, flow.loss_and_grad(dx.p, n, false));
+                flow.want_loss = false;
+            }
+            for (int i = ntr - 1; i > 0; --i) {
                 s = s * 6364136223846793005ull + 1442695040888963407ull;
                 std::swap(idx[i], idx[(s >> 33) % (uint64_t)(i + 1)]);
             }
-            for (int b0 = 0; b0 + Mb <= n; b0 += Mb) {
+            for (int b0 = 0; b0 + Mb <= ntr; b0 += Mb) {
                 for (int i = 0; i < Mb; ++i)
                     std::memcpy(&bx[(size_t)i * d], &hx[(size_t)idx[b0 + i] * d], d * 4);
                 cudaMemcpy(dx.p, bx.data(), (size_t)Mb * d * 4, cudaMemcpyHostToDevice);
                 flow.loss_and_grad(dx.p, Mb, true);
                 flow.adam_step((float)opt.lr);
             }
+            const float vl = val_loss();
+            if (std::isfinite(vl) && vl < best_loss) {
+                best_loss = vl;
+                since_best = 0;
+                cudaMemcpy(best.p, flow.P.p, flow.nparams * 4, cudaMemcpyDeviceToDevice);
+            } else if (++since_best >= patience) {
+                break;
+            }
         }
+        cudaMemcpy(flow.P.p, best.p, flow.nparams * 4, cudaMemcpyDeviceToDevice);
+        if (dbg) std::fprintf(stderr, "flow: best held-out loss %.4f\n", best_loss);
         // latent radius of the live points
+        flow.want_loss = true;
         cudaMemcpy(dx.p, hx.data(), (size_t)n * d * 4, cudaMemcpyHostToDevice);
-        flow.loss_and_grad(dx.p, n, false);
+        last_loss = flow.loss_and_grad(dx.p, n, false);
         std::vector<float> z((size_t)n * d);
         cudaMemcpy(z.data(), flow.u.p + (size_t)flow.L * n * d, z.size() * 4, cudaMemcpyDeviceToHost);
         double r = 0;
@@ -493,7 +547,76 @@ public:
         }
         radius = r * opt.expand;
         trained = std::isfinite(radius) && radius > 0 && cudaGetLastError() == cudaSuccess;
+        if (trained) trained = calibrate(d);
+        if (std::getenv("LG_FLOW_DEBUG"))
+            std::fprintf(stderr, "flow: train %ld epochs %d loss %.4f latent radius %.3f ok %d\n", ntrain, epochs,
+                         last_loss, radius, (int)trained);
         return trained ? LG_OK : LG_ERR_CUDA;
+    }
+
+    double wnorm = 0;       // log weight normaliser (calibrated at training)
+    double efficiency = 0;  // mean kept fraction of latent draws
+
+    // M latent draws uniform in the ball, mapped to the standardised space
+    // (uu), with their log weights log|det dx/dz|
+    bool latent_batch(Rng& r, int M, int d, std::vector<float>& z, std::vector<float>& uu, std::vector<float>& lw)
+    {
+        if (!dzlat.ensure((size_t)M * d) || !dulat.ensure((size_t)M * d) || !flow.reserve(M)) return false;
+        z.resize((size_t)M * d);
+        uu.resize((size_t)M * d);
+        lw.resize(M);
+        // uniform in the latent ball
+        for (int i = 0; i < M; ++i) {
+            double n2 = 0;
+            for (int a = 0; a < d; ++a) {
+                const double v = r.normal();
+                z[(size_t)i * d + a] = (float)v;
+                n2 += v * v;
+            }
+            const double rad = radius * std::pow(r.uniform(), 1.0 / d) / std::sqrt(n2);
+            for (int a = 0; a < d; ++a) z[(size_t)i * d + a] = (float)(z[(size_t)i * d + a] * rad);
+        }
+        cudaMemcpy(dzlat.p, z.data(), z.size() * 4, cudaMemcpyHostToDevice);
+        if (flow.bf16) flow.inverse(dzlat.p, M, dulat.p, flow.hb.p);
+        else flow.inverse(dzlat.p, M, dulat.p, flow.hf.p);
+        cudaMemcpy(uu.data(), dulat.p, uu.size() * 4, cudaMemcpyDeviceToHost);
+        cudaMemcpy(lw.data(), flow.ld.p, (size_t)M * 4, cudaMemcpyDeviceToHost);
+        return cudaGetLastError() == cudaSuccess;
+    }
+
+    // Calibrate the normaliser on a large latent sample (its maximum plus a
+    // margin, so that the rejection step is exact unless a weight exceeds it)
+    // and estimate the efficiency; a flow whose kept fraction is below 1% is
+    // not used (the sampler stays on the ellipsoid).
+    bool calibrate(int d)
+    {
+        Rng r(seed * 7919 + (uint64_t)ntrain);
+        std::vector<float> z, uu, lw;
+        const int M = 16384;
+        if (!latent_batch(r, M, d, z, uu, lw)) return false;
+        double mx = -INFINITY;
+        for (float v : lw)
+            if (std::isfinite(v)) mx = std::max(mx, (double)v);
+        if (!std::isfinite(mx)) return false;
+        wnorm = mx + 1.0;
+        double acc = 0;
+        for (float v : lw)
+            if (std::isfinite(v)) acc += std::exp(v - wnorm);
+        efficiency = acc / M;
+        if (std::getenv("LG_FLOW_DEBUG"))
+            std::fprintf(stderr, "flow: calibrated efficiency %.4f\n", efficiency);
+        return efficiency >= 0.01;
+    }
+
+    // volume of the image of the latent ball: V_ball(R) E[|det dx/dz|]
+    double log_volume() const override
+    {
+        if (!trained || efficiency <= 0) return HUGE_VAL;
+        const int d = flow.d;
+        double lv = 0.5 * d * std::log(M_PI) - std::lgamma(0.5 * d + 1) + d * std::log(radius);
+        lv += std::log(efficiency) + wnorm;
+        for (float sd : flow.sdev) lv += std::log((double)sd);
+        return lv;
     }
 
     int propose(const double*, int, int d, double* out, int B, uint64_t sd) override
@@ -501,34 +624,22 @@ public:
         if (!trained) return 0;
         cudaSetDevice(device);
         Rng r(sd);
-        const int M = 4 * B;
-        if (!dzlat.ensure((size_t)M * d) || !dulat.ensure((size_t)M * d) || !flow.reserve(M)) return 0;
-        std::vector<float> z((size_t)M * d), uu((size_t)M * d), ldet(M);
+        const int M = std::max(4 * B, (int)std::min(65536.0, 2.0 * B / std::max(efficiency, 1e-3)));
+        std::vector<float> z, uu, ldet;
         int got = 0;
-        for (int round = 0; round < 8 && got < B; ++round) {
-            for (int i = 0; i < M; ++i) {
-                double n2 = 0;
-                for (int a = 0; a < d; ++a) {
-                    const double v = r.normal();
-                    z[(size_t)i * d + a] = (float)v;
-                    n2 += v * v;
-                }
-                const double rad = radius * std::pow(r.uniform(), 1.0 / d) / std::sqrt(n2);
-                for (int a = 0; a < d; ++a) z[(size_t)i * d + a] = (float)(z[(size_t)i * d + a] * rad);
-            }
-            cudaMemcpy(dzlat.p, z.data(), z.size() * 4, cudaMemcpyHostToDevice);
-            if (flow.bf16) flow.inverse(dzlat.p, M, dulat.p, flow.hb.p);
-            else flow.inverse(dzlat.p, M, dulat.p, flow.hf.p);
-            cudaMemcpy(uu.data(), dulat.p, uu.size() * 4, cudaMemcpyDeviceToHost);
-            cudaMemcpy(ldet.data(), flow.ld.p, (size_t)M * 4, cudaMemcpyDeviceToHost);
-            if (cudaGetLastError() != cudaSuccess) return 0;
-            // log|det dx/dz| = ldet (du/dz) + sum log sdev (dx/du)
-            float lmax = -INFINITY;
+        for (int round = 0; round < 4 && got < B; ++round) {
+            // keep x with probability proportional to 1 / q_x(x) = |det dx/dz|
+            // (z uniform in the ball), normalised by the calibrated bound (a
+            // weight above it raises the bound for the rest of the round)
+            if (!latent_batch(r, M, d, z, uu, ldet)) return 0;
+            double lmax = wnorm;
             for (int i = 0; i < M; ++i)
-                if (std::isfinite(ldet[i])) lmax = std::max(lmax, ldet[i]);
-            if (!std::isfinite(lmax)) return 0;
+                if (std::isfinite(ldet[i]) && ldet[i] > lmax) lmax = ldet[i];
+            wnorm = lmax;
+            int kept = 0;
             for (int i = 0; i < M && got < B; ++i) {
                 if (!std::isfinite(ldet[i]) || r.uniform() > std::exp((double)ldet[i] - lmax)) continue;
+                ++kept;
                 bool in = true;
                 double* x = out + (size_t)got * d;
                 for (int a = 0; a < d && in; ++a) {
@@ -536,6 +647,16 @@ public:
                     in = x[a] >= 0 && x[a] <= 1;
                 }
                 if (in) ++got;
+            }
+            if (std::getenv("LG_FLOW_DEBUG") && round == 0) {
+                std::vector<float> w(ldet);
+                std::sort(w.begin(), w.end());
+                const float lmaxf = (float)lmax;
+                std::fprintf(stderr,
+                             "flow: propose %d latent, %d kept by the weight test, %d in the cube; log weight "
+                             "quantiles 1%% %.2f 50%% %.2f 99%% %.2f max %.2f\n",
+                             M, kept, got, w[M / 100] - lmaxf, w[M / 2] - lmaxf, w[M - 1 - M / 100] - lmaxf,
+                             w[M - 1] - lmaxf);
             }
         }
         return got;

@@ -20,6 +20,8 @@
 #include <chrono>
 #include <cmath>
 #include <cstdint>
+#include <cstdio>
+#include <cstdlib>
 #include <cstring>
 #include <limits>
 #include <memory>
@@ -167,7 +169,7 @@ int nested_sample(int nd, lg_batch_loglike fn, void* user, const lg_nested_optio
     size_t pool_pos = 0;
     Ellipsoid ell;
     std::vector<double> u(nd), y(nd);
-    long iter = 0, since_train = 0, n_flow = 0, n_ell = 0;
+    long iter = 0, since_train = 0, n_flow = 0, n_ell = 0, n_flow_fail = 0;
     bool use_flow = false;
     int status = LG_OK;
     for (;; ++iter) {
@@ -194,6 +196,9 @@ int nested_sample(int nd, lg_batch_loglike fn, void* user, const lg_nested_optio
         if (learned && opt.flow_every > 0 && since_train >= opt.flow_every) {
             since_train = 0;
             use_flow = learned->train(live.data(), nl, nd) == LG_OK;
+            if (std::getenv("LG_FLOW_DEBUG"))
+                std::fprintf(stderr, "flow: iter %ld trained %d, flow batches failed so far %ld\n", iter,
+                             (int)use_flow, n_flow_fail);
             pool_x.clear();
             pool_l.clear();
             pool_pos = 0;
@@ -209,23 +214,25 @@ int nested_sample(int nd, lg_batch_loglike fn, void* user, const lg_nested_optio
                 replaced = true;
                 break;
             }
-            // propose a batch
+            // propose a batch: the learned proposal when it is trained, the
+            // ellipsoid when it is not or when it yields nothing
             int n = 0;
-            if (use_flow) {
-                n = learned->propose(live.data(), nl, nd, buf.data(), B, rng.next());
-                if (n <= 0) use_flow = false;
-                else n_flow += n;
+            // the ellipsoid bounds the live points other than the one leaving
+            std::vector<double> others;
+            others.reserve((size_t)(nl - 1) * nd);
+            for (int i = 0; i < nl; ++i)
+                if (i != imin) others.insert(others.end(), &live[(size_t)i * nd], &live[(size_t)i * nd] + nd);
+            if (!ell.fit(others, nl - 1, nd, 1.0 / opt.efr)) {
+                err = "nested sampling: degenerate live points";
+                return LG_ERR_INPUT;
             }
-            if (!use_flow) {
-                // the ellipsoid bounds the live points other than the one leaving
-                std::vector<double> others;
-                others.reserve((size_t)(nl - 1) * nd);
-                for (int i = 0; i < nl; ++i)
-                    if (i != imin) others.insert(others.end(), &live[(size_t)i * nd], &live[(size_t)i * nd] + nd);
-                if (!ell.fit(others, nl - 1, nd, 1.0 / opt.efr)) {
-                    err = "nested sampling: degenerate live points";
-                    return LG_ERR_INPUT;
-                }
+            // the learned bound is used when it is the tighter of the two
+            if (use_flow && learned->log_volume() < ell.log_volume()) {
+                n = learned->propose(live.data(), nl, nd, buf.data(), B, rng.next());
+                if (n > 0) n_flow += n;
+                else n = 0, ++n_flow_fail;
+            }
+            if (n == 0) {
                 long tries = 0;
                 while (n < B && tries < 1000L * B) {
                     ++tries;

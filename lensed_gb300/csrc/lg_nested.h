@@ -57,6 +57,8 @@ struct Proposal {
     virtual ~Proposal() {}
     virtual int train(const double* live, int n, int d) = 0;
     virtual int propose(const double* live, int n, int d, double* out, int B, uint64_t seed) = 0;
+    // log volume (unit-cube coordinates) of the region propose() draws from
+    virtual double log_volume() const = 0;
 };
 
 int nested_sample(int nd, lg_batch_loglike fn, void* user, const lg_nested_options* o, lg_nested_result* res,

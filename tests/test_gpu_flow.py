@@ -53,7 +53,7 @@ def banana(x):
     return ll
 
 
-def test_learned_proposal_gains_over_ellipsoid(native):
+def test_learned_proposal_on_a_curved_posterior(native):
     d = 6
     exact = 3 * math.log(2 * math.pi * 0.15 * 0.01)
     common = dict(nlive=500, batch=512, seed=5, tol=0.1)
@@ -62,7 +62,9 @@ def test_learned_proposal_gains_over_ellipsoid(native):
     print(f"banana d={d}: exact lnZ {exact:.3f}; ellipsoid {plain['logz']:.3f}+-{plain['logz_err']:.3f} "
           f"calls {plain['ncall']} ({plain['wall_s']:.1f}s); flow {flow['logz']:.3f}+-{flow['logz_err']:.3f} "
           f"calls {flow['ncall']} ({flow['wall_s']:.1f}s), flow proposals {flow['n_flow_proposals']}")
+    # the learned bound is used where it is tighter than the ellipsoid, and
+    # the evidence stays unbiased (calibrated rejection step)
     assert flow["n_flow_proposals"] > 0
     assert flow["ncall"] < plain["ncall"]
     for r in (plain, flow):
-        assert abs(r["logz"] - exact) < 4 * r["logz_err"] + 0.3
+        assert abs(r["logz"] - exact) < 4 * r["logz_err"] + 0.1
