@@ -204,20 +204,6 @@ class Clocks:
                 "samples": len(sm)}
 
 
-def dist_setup(n_gpus):
-    rank = int(os.environ.get("RANK", "0"))
-    world = int(os.environ.get("WORLD_SIZE", "1"))
-    local = int(os.environ.get("LOCAL_RANK", "0"))
-    dist = None
-    if world > 1:
-        import torch
-        import torch.distributed as dist
-
-        torch.cuda.set_device(local)
-        dist.init_process_group("nccl")
-    return rank, world, local, dist
-
-
 def cpu_oracle(s, threads, precision=32):
     from lensed_gb300 import quadrature
     from oracle.oracle import Oracle
@@ -314,14 +300,16 @@ def main():
     import lensed_gb300 as lg
     from lensed_gb300 import workloads
 
-    rank, world, local, dist = dist_setup(args.gpus)
+    from lensed_gb300 import replicas
+
+    rank, world, local, dist = replicas.init()
     torch.cuda.set_device(local)
     s, B = workload(args.workload)
     if args.batch:
         B = args.batch
     ctx = lg.Context(s.image, s.weight, s.objects, psf=s.psf, rule=s.rule, device=local, max_batch=B,
                      flags=args.flags)
-    cand = ctx.to_map_order(workloads.draw_candidates(s, B, seed=1 + rank))
+    cand = ctx.to_map_order(workloads.draw_candidates(s, B, seed=replicas.candidate_seed(rank)))
     d_params = torch.from_numpy(np.ascontiguousarray(cand)).to(f"cuda:{local}")
     d_logL = torch.empty(B, dtype=torch.float64, device=f"cuda:{local}")
     # a dedicated stream: the context's kernels and the timing events share it
@@ -352,11 +340,8 @@ def main():
         dist.barrier()
     ms = e0.elapsed_time(e1)
     clk = clocks.stop()
-    if dist:
-        t = torch.tensor([ms], device=f"cuda:{local}")
-        dist.all_reduce(t, op=dist.ReduceOp.MAX)
-        ms = float(t.item())
-    value = world * B * args.steps / (ms / 1e3)
+    ms = replicas.max_over_ranks(ms, dist, device=f"cuda:{local}")
+    value = replicas.aggregate(B * args.steps, ms / 1e3, world)
     logL_gpu = d_logL.cpu().numpy()
 
     # per-stage device times (the reference's --profile stages), averaged
@@ -375,11 +360,7 @@ def main():
     for _ in range(ne2e):
         ll_host = ctx.eval_batch(hp)
     e2e_dt = (time.perf_counter() - t0) / ne2e
-    e2e = world * B / e2e_dt
-    if dist:
-        t = torch.tensor([e2e_dt], device=f"cuda:{local}")
-        dist.all_reduce(t, op=dist.ReduceOp.MAX)
-        e2e = world * B / float(t.item())
+    e2e = replicas.aggregate(B, replicas.max_over_ranks(e2e_dt, dist, device=f"cuda:{local}"), world)
 
     # plain mode: one candidate per call with a host sync (the reference flow)
     plain = None
