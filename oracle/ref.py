@@ -16,10 +16,8 @@ import numpy as np
 
 HERE = os.path.dirname(os.path.abspath(__file__))
 OUT = os.path.join(HERE, "_ref")
-if HERE not in sys.path:
-    sys.path.insert(0, HERE)
 
-import build_ref  # noqa: E402
+from oracle import build_ref  # noqa: E402
 
 
 def _ptr(a, t):
