@@ -181,6 +181,39 @@ int lg_eval_cube_batch(lg_ctx* ctx, const double* cube, int B, double* phys, dou
  * estimate (src/nested.c:175-216).  Any output may be NULL. */
 int lg_render(lg_ctx* ctx, const double* params, float* model, float* raw, float* error);
 
+/* The reference's result dumper (src/nested.c:175-257): render one
+ * parameter vector (map order) and return LG_DUMP_LAYERS images of
+ * width x height floats each, in this order, in `layers`
+ * (LG_DUMP_LAYERS * width * height floats):
+ *   IMG  the model (convolved if there is a PSF),
+ *   RES  image - model,
+ *   RAW  the unconvolved model,
+ *   ERR  relative quadrature error, error / RAW,
+ *   WHT  the weight map (0 on masked pixels),
+ *   PVL  per-pixel p-value erfc(sqrt(chi2 / 2)), chi2 = WHT * (IMG - image)^2.
+ * The per-pixel chi^2 is that of the rendered parameters (the reference
+ * reads the per-pixel buffer of its last likelihood evaluation instead). */
+#define LG_DUMP_LAYERS 6
+extern const char* const lg_dump_names[LG_DUMP_LAYERS]; /* "IMG" .. "PVL" */
+int lg_dump(lg_ctx* ctx, const double* params, float* layers);
+
+/* lg_dump followed by lg_write_fits of the six layers under their names:
+ * the counterpart of the dumper's write_output (src/data.c:372-391). */
+int lg_write_output(lg_ctx* ctx, const double* params, const char* path);
+
+/* FITS writer (no CFITSIO): an empty primary HDU (ORIGIN, DATE) and one
+ * 2-D float32 IMAGE extension per layer, EXTNAME = names[i] when names and
+ * names[i] are not NULL (src/data.c:129-165).  Errors go to
+ * lg_last_error(NULL). */
+int lg_write_fits(const char* path, int width, int height, int nlayers, const float* const* layers,
+                  const char* const* names);
+
+/* Same into memory (src/data.c:393-419): *size receives the file size; the
+ * file is copied to buf when buf is not NULL and capacity >= *size
+ * (LG_ERR_INPUT when it is smaller). */
+int lg_write_fits_memory(int width, int height, int nlayers, const float* const* layers, const char* const* names,
+                         void* buf, size_t capacity, size_t* size);
+
 /* Device times (ms) of the four stages of one evaluation of B candidates
  * with device pointers: set_params, render, convolve (0 without a PSF) and
  * the chi^2 finish -- the counterpart of the reference's --profile table

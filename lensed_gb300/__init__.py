@@ -22,7 +22,7 @@ from typing import Optional, Sequence
 import numpy as np
 
 __all__ = ["Context", "Systems", "LensedError", "lib", "plugins", "plugin_params", "quad_rules", "make_weight",
-           "compile_check", "LIB_PATH"]
+           "compile_check", "write_fits", "fits_bytes", "DUMP_LAYERS", "LIB_PATH"]
 
 LIB_PATH = os.path.join(os.path.dirname(os.path.abspath(__file__)), "liblensed_gb300.so")
 
@@ -31,6 +31,7 @@ STATUS = {-1: "input", -2: "compile", -3: "cuda", -4: "alloc", -5: "timeout", -6
 LG_FLAG_STRICT_FP = 1
 LG_FLAG_NO_GRAPH = 2
 LG_FLAG_IEEE_DIV = 4
+DUMP_LAYERS = ("IMG", "RES", "RAW", "ERR", "WHT", "PVL")
 
 
 class LensedError(RuntimeError):
@@ -110,6 +111,11 @@ def lib():
         "lg_eval_batch_device": (C.c_int, [vp, vp, C.c_int, vp, vp]),
         "lg_eval_cube_batch": (C.c_int, [vp, dp, C.c_int, dp, dp]),
         "lg_render": (C.c_int, [vp, dp, fp, fp, fp]),
+        "lg_dump": (C.c_int, [vp, dp, fp]),
+        "lg_write_output": (C.c_int, [vp, dp, C.c_char_p]),
+        "lg_write_fits": (C.c_int, [C.c_char_p, C.c_int, C.c_int, C.c_int, C.POINTER(fp), C.POINTER(C.c_char_p)]),
+        "lg_write_fits_memory": (C.c_int, [C.c_int, C.c_int, C.c_int, C.POINTER(fp), C.POINTER(C.c_char_p), vp,
+                                           C.c_size_t, C.POINTER(C.c_size_t)]),
         "lg_eval_profile": (C.c_int, [vp, vp, C.c_int, vp, fp]),
         "lg_measure_fp32_peak": (C.c_int, [C.c_int, dp]),
         "lg_loglike_images_noalloc": (C.c_int, [vp, vp, vp, C.c_long, C.c_int, vp, vp]),
@@ -286,6 +292,42 @@ def nested_sample_flow(loglike, ndims: int, max_samples: int = 200000, flow: dic
     if rc:
         raise LensedError(rc, lib().lg_last_error(None).decode(errors="replace"))
     return _pack(r, arrays)
+
+
+def _layer_args(layers, names):
+    arrs = [np.ascontiguousarray(a, dtype=np.float32) for a in layers]
+    if not arrs or any(a.ndim != 2 or a.shape != arrs[0].shape for a in arrs):
+        raise ValueError("layers must be 2-D arrays of one shape")
+    ptrs = (C.POINTER(C.c_float) * len(arrs))(*[_p(a, C.c_float) for a in arrs])
+    nm = None
+    if names is not None:
+        if len(names) != len(arrs):
+            raise ValueError("one name per layer")
+        nm = (C.c_char_p * len(arrs))(*[None if n is None else n.encode() for n in names])
+    H, W = arrs[0].shape
+    return arrs, ptrs, nm, W, H
+
+
+def _global_check(rc):
+    if rc != LG_OK:
+        raise LensedError(rc, lib().lg_last_error(None).decode())
+
+
+def write_fits(path: str, layers, names=None) -> None:
+    """Write 2-D float32 layers as IMAGE extensions of a FITS file (after an
+    empty primary HDU), named by EXTNAME when names are given."""
+    arrs, ptrs, nm, W, H = _layer_args(layers, names)
+    _global_check(lib().lg_write_fits(os.fsencode(path), W, H, len(arrs), ptrs, nm))
+
+
+def fits_bytes(layers, names=None) -> bytes:
+    """The FITS file write_fits would write, as bytes."""
+    arrs, ptrs, nm, W, H = _layer_args(layers, names)
+    size = C.c_size_t()
+    _global_check(lib().lg_write_fits_memory(W, H, len(arrs), ptrs, nm, None, 0, C.byref(size)))
+    buf = C.create_string_buffer(size.value)
+    _global_check(lib().lg_write_fits_memory(W, H, len(arrs), ptrs, nm, buf, size.value, C.byref(size)))
+    return buf.raw[: size.value]
 
 
 def make_weight(image, weight_map=None, gain=None, gain_value=1.0, offset=0.0, xweight=None, mask=None):
@@ -493,6 +535,19 @@ class Context:
         self._check(lib().lg_render(self.h, _p(p, C.c_double), _p(m, C.c_float), _p(r, C.c_float),
                                     _p(e, C.c_float)))
         return m, r, e
+
+    def dump(self, params):
+        """The dumper's output layers for one parameter vector (map order):
+        a dict IMG, RES, RAW, ERR, WHT, PVL -> (H, W) float32 array."""
+        p = np.ascontiguousarray(params, dtype=np.float64)
+        out = np.empty((len(DUMP_LAYERS), self.height, self.width), np.float32)
+        self._check(lib().lg_dump(self.h, _p(p, C.c_double), _p(out, C.c_float)))
+        return {n: out[i] for i, n in enumerate(DUMP_LAYERS)}
+
+    def write_output(self, params, path: str) -> None:
+        """Write the dumper's layers for one parameter vector to a FITS file."""
+        p = np.ascontiguousarray(params, dtype=np.float64)
+        self._check(lib().lg_write_output(self.h, _p(p, C.c_double), os.fsencode(path)))
 
     def nested(self, max_samples: int = 200000, flow: dict | None = None, **opts):
         """Nested sampling of this context's posterior (unit-cube means/samples)."""

@@ -13,6 +13,7 @@
 #include <cuda.h>
 #include <cuda_runtime.h>
 
+#include <algorithm>
 #include <cmath>
 #include <cstdio>
 #include <cstring>
@@ -103,6 +104,7 @@ struct lg_ctx {
     double* d_logL = nullptr;
     float* d_model_out = nullptr;
     float* d_err_out = nullptr;
+    float* d_layers = nullptr;  // 6 x N output layers of lg_dump
     double* h_params = nullptr;  // pinned staging
     double* h_logL = nullptr;
     std::map<int, cudaGraphExec_t> graphs;
@@ -175,6 +177,7 @@ struct lg_ctx {
         cudaFree(d_logL);
         cudaFree(d_model_out);
         cudaFree(d_err_out);
+        cudaFree(d_layers);
         cudaFreeHost(h_params);
         cudaFreeHost(h_logL);
         if (mod && drv) drv->moduleUnload(mod);
@@ -558,9 +561,14 @@ int lg_eval_cube_batch(lg_ctx* c, const double* cube, int B, double* phys, doubl
     return LG_OK;
 }
 
-int lg_render(lg_ctx* c, const double* params, float* model, float* raw, float* error)
+namespace {
+
+// Render one parameter vector (map order) on the context's stream: the raw
+// model to d_model_out, its quadrature error to d_err_out and, with a PSF,
+// the convolved model to the first image of d_raw (src/nested.c:175-205).
+// Returns the device pointer of the model (convolved if there is a PSF).
+int render_device(lg_ctx* c, const double* params, const float** d_model)
 {
-    if (!c || !params) return LG_ERR_INPUT;
     int rc;
     if ((rc = c->cuda(cudaSetDevice(c->device), "cudaSetDevice"))) return rc;
     const size_t N = (size_t)c->N, np = c->model.pars.size();
@@ -569,8 +577,6 @@ int lg_render(lg_ctx* c, const double* params, float* model, float* raw, float* 
             (rc = c->cuda(cudaMalloc((void**)&c->d_err_out, N * 4), "render buffer")))
             return rc;
     }
-    // render to d_model_out (value) and d_err_out (error), convolve the value
-    // into the raw buffer's first image when there is a PSF
     float* d_val = c->d_model_out;
     if ((rc = c->cuda(cudaMemcpyAsync(c->d_params, params, np * 8, cudaMemcpyHostToDevice, c->stream), "params")))
         return rc;
@@ -585,16 +591,84 @@ int lg_render(lg_ctx* c, const double* params, float* model, float* raw, float* 
                             c->csmem, c->stream, a_c, "convolve")))
             return rc;
     }
-    if (raw && (rc = c->cuda(cudaMemcpyAsync(raw, d_val, N * 4, cudaMemcpyDeviceToHost, c->stream), "read raw")))
+    *d_model = c->psf ? c->d_raw : d_val;
+    return LG_OK;
+}
+
+// The six output layers of the reference's dumper (src/nested.c:217-254),
+// one pixel per thread: IMG model, RES image - model, RAW unconvolved model,
+// ERR error / raw, WHT weight, PVL erfc(sqrt(chi2 / 2)) with the per-pixel
+// chi2 = weight * (model - image)^2 of the loglike kernel
+// (kernel/lensed.cl:41-53), all in IEEE FP32 except the p-value's double
+// erfc/sqrt, which the reference also evaluates in double.
+__global__ void __launch_bounds__(256)
+    lg_dump_layers(const float* __restrict__ model, const float* __restrict__ raw, const float* __restrict__ err,
+                   const float* __restrict__ image, const float* __restrict__ weight, long N, float* __restrict__ out)
+{
+    for (long k = blockIdx.x * (long)blockDim.x + threadIdx.x; k < N; k += (long)gridDim.x * blockDim.x) {
+        const float m = model[k], v = raw[k], d = image[k], w = weight[k];
+        const float r = __fsub_rn(m, d);
+        const float chi2 = __fmul_rn(__fmul_rn(w, r), r);
+        out[k] = m;
+        out[N + k] = __fsub_rn(d, m);
+        out[2 * N + k] = v;
+        out[3 * N + k] = __fdiv_rn(err[k], v);
+        out[4 * N + k] = w;
+        out[5 * N + k] = (float)erfc(sqrt(0.5 * (double)chi2));
+    }
+}
+
+}  // namespace
+
+int lg_render(lg_ctx* c, const double* params, float* model, float* raw, float* error)
+{
+    if (!c || !params) return LG_ERR_INPUT;
+    int rc;
+    const float* d_model = nullptr;
+    if ((rc = render_device(c, params, &d_model))) return rc;
+    const size_t N = (size_t)c->N;
+    if (raw &&
+        (rc = c->cuda(cudaMemcpyAsync(raw, c->d_model_out, N * 4, cudaMemcpyDeviceToHost, c->stream), "read raw")))
         return rc;
     if (error &&
         (rc = c->cuda(cudaMemcpyAsync(error, c->d_err_out, N * 4, cudaMemcpyDeviceToHost, c->stream), "read error")))
         return rc;
-    if (model && (rc = c->cuda(cudaMemcpyAsync(model, c->psf ? c->d_raw : d_val, N * 4, cudaMemcpyDeviceToHost,
-                                               c->stream),
-                               "read model")))
+    if (model && (rc = c->cuda(cudaMemcpyAsync(model, d_model, N * 4, cudaMemcpyDeviceToHost, c->stream), "read model")))
         return rc;
     return c->cuda(cudaStreamSynchronize(c->stream), "render");
+}
+
+int lg_dump(lg_ctx* c, const double* params, float* layers)
+{
+    if (!c || !params || !layers) return LG_ERR_INPUT;
+    int rc;
+    const float* d_model = nullptr;
+    if ((rc = render_device(c, params, &d_model))) return rc;
+    const long N = c->N;
+    if (!c->d_layers && (rc = c->cuda(cudaMalloc((void**)&c->d_layers, (size_t)N * 6 * 4), "dump buffer"))) return rc;
+    const int blocks = (int)std::min<long>((N + 255) / 256, 4096);
+    lg_dump_layers<<<blocks, 256, 0, c->stream>>>(d_model, c->d_model_out, c->d_err_out, c->d_image, c->d_weight, N,
+                                                  c->d_layers);
+    if ((rc = c->cuda(cudaGetLastError(), "dump layers"))) return rc;
+    if ((rc = c->cuda(cudaMemcpyAsync(layers, c->d_layers, (size_t)N * 6 * 4, cudaMemcpyDeviceToHost, c->stream),
+                      "read layers")))
+        return rc;
+    return c->cuda(cudaStreamSynchronize(c->stream), "dump");
+}
+
+const char* const lg_dump_names[LG_DUMP_LAYERS] = {"IMG", "RES", "RAW", "ERR", "WHT", "PVL"};
+
+int lg_write_output(lg_ctx* c, const double* params, const char* path)
+{
+    if (!c || !params || !path) return LG_ERR_INPUT;
+    std::vector<float> layers((size_t)c->N * LG_DUMP_LAYERS);
+    int rc = lg_dump(c, params, layers.data());
+    if (rc) return rc;
+    const float* ptr[LG_DUMP_LAYERS];
+    for (int i = 0; i < LG_DUMP_LAYERS; ++i) ptr[i] = layers.data() + (size_t)i * c->N;
+    rc = lg_write_fits(path, c->model.width, c->model.height, LG_DUMP_LAYERS, ptr, lg_dump_names);
+    if (rc) c->err = lg_last_error(nullptr);
+    return rc;
 }
 
 // Per-stage device times of one evaluation, the counterpart of the

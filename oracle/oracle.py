@@ -150,6 +150,29 @@ class Oracle:
         return out
 
 
+DUMP_NAMES = ("IMG", "RES", "RAW", "ERR", "WHT", "PVL")
+
+
+def dump_layers(image, weight, model, raw, error):
+    """Oracle restatement of the dumper's output layers (src/nested.c:217-254)
+    from a rendered model: IMG model, RES image - model, RAW unconvolved
+    model, ERR error / RAW, WHT weight, PVL erfc(sqrt(chi2 / 2)) with the
+    per-pixel chi2 = weight * (model - image)^2 of the loglike kernel
+    (kernel/lensed.cl:41-53).  FP32 arithmetic as the reference's; the
+    p-value in double (math.erfc per pixel), rounded to float32."""
+    import math
+
+    f = lambda a: np.ascontiguousarray(a, dtype=np.float32)
+    img, w, m, v, e = f(image), f(weight), f(model), f(raw), f(error)
+    with np.errstate(divide="ignore", invalid="ignore"):
+        r = m - img
+        chi2 = (w * r) * r
+        relerr = e / v
+    pvl = np.array([math.erfc(math.sqrt(0.5 * float(c))) for c in chi2.ravel()], dtype=np.float64)
+    pvl = pvl.astype(np.float32).reshape(m.shape)
+    return {"IMG": m, "RES": img - m, "RAW": v, "ERR": relerr, "WHT": w, "PVL": pvl}
+
+
 def make_weight(image, weight_map=None, gain=None, gain_value=1.0, offset=0.0, xweight=None, mask=None):
     """Oracle restatement of Lensed's weight construction (float32 array)."""
     img = np.ascontiguousarray(image, dtype=np.float32).ravel()
