@@ -176,6 +176,16 @@ int lg_eval_batch_device(lg_ctx* ctx, const double* d_params, int B, double* d_l
  * transform leaves the parameter bounds get logL = -inf and phys NaN. */
 int lg_eval_cube_batch(lg_ctx* ctx, const double* cube, int B, double* phys, double* logL);
 
+/* The unit-cube evaluation on the GPU with device pointers on a caller
+ * stream (NULL = the context's stream), B <= max_batch; returns without
+ * synchronising.  The prior transform of src/nested.c:42-61 runs as a
+ * kernel (one candidate per thread; unif, norm, delta priors; pseudo-prior
+ * parameters at u = 0.5), followed by the likelihood kernels.  d_phys
+ * (B x npars, map order, may be NULL) receives the physical parameters;
+ * points outside the parameter bounds get logL = -inf.  Uses the context's
+ * parameter scratch: calls on one context must be ordered. */
+int lg_eval_cube_batch_device(lg_ctx* ctx, const double* d_cube, int B, double* d_phys, double* d_logL, void* stream);
+
 /* Render one parameter vector (map order) for output: the model (convolved
  * if there is a PSF), the unconvolved model and the quadrature error
  * estimate (src/nested.c:175-216).  Any output may be NULL. */

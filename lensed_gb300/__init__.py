@@ -110,6 +110,7 @@ def lib():
         "lg_eval_batch": (C.c_int, [vp, dp, C.c_int, dp]),
         "lg_eval_batch_device": (C.c_int, [vp, vp, C.c_int, vp, vp]),
         "lg_eval_cube_batch": (C.c_int, [vp, dp, C.c_int, dp, dp]),
+        "lg_eval_cube_batch_device": (C.c_int, [vp, vp, C.c_int, vp, vp, vp]),
         "lg_render": (C.c_int, [vp, dp, fp, fp, fp]),
         "lg_dump": (C.c_int, [vp, dp, fp]),
         "lg_write_output": (C.c_int, [vp, dp, C.c_char_p]),
@@ -526,6 +527,13 @@ class Context:
         self._check(lib().lg_eval_cube_batch(self.h, _p(u, C.c_double), u.shape[0], _p(phys, C.c_double),
                                              _p(out, C.c_double)))
         return out, phys
+
+    def eval_cube_device(self, d_cube: int, B: int, d_phys: int, d_logL: int, stream: int = 0) -> None:
+        """Unit-cube evaluation with device pointers (prior transform on the
+        GPU); d_phys may be 0; asynchronous on the given stream."""
+        self._check(lib().lg_eval_cube_batch_device(self.h, C.c_void_p(d_cube or None), int(B),
+                                                    C.c_void_p(d_phys or None), C.c_void_p(d_logL),
+                                                    C.c_void_p(stream) if stream else None))
 
     def render(self, params):
         """(model, raw, error) images for one parameter vector (map order)."""

@@ -82,7 +82,10 @@ def build(verbose: bool = False, force: bool = False) -> str:
     nvcc = os.path.join(cuda, "bin", "nvcc")
     write_embed()
     inc = ["-I", os.path.join(ROOT, "include"), "-I", BUILD, "-I", os.path.join(PKG, "csrc")]
-    flags = ["-O2", "-std=c++17", ARCH, "-lineinfo", "-Xcompiler", "-fPIC", "-Xcompiler", "-Wall"]
+    # host code: no floating-point contraction, so that it computes the same
+    # bits on x86-64 and on aarch64 (where GCC would otherwise fuse a*b+c)
+    flags = ["-O2", "-std=c++17", ARCH, "-lineinfo", "-Xcompiler", "-fPIC", "-Xcompiler", "-Wall", "-Xcompiler",
+             "-ffp-contract=off"]
     headers = glob.glob(os.path.join(PKG, "csrc", "*.h")) + glob.glob(os.path.join(PKG, "csrc", "*.inc")) + [
         os.path.join(ROOT, "include", "lensed_gb300.h"), os.path.join(BUILD, "lg_embed.inc")]
     objs = []

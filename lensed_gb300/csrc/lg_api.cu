@@ -12,6 +12,7 @@
 
 #include <cuda.h>
 #include <cuda_runtime.h>
+#include <math_constants.h>
 
 #include <algorithm>
 #include <cmath>
@@ -105,6 +106,13 @@ struct lg_ctx {
     float* d_model_out = nullptr;
     float* d_err_out = nullptr;
     float* d_layers = nullptr;  // 6 x N output layers of lg_dump
+    // unit-cube path: priors in map order, cube staging, rejection flags
+    void* d_priors = nullptr;
+    double* d_cube = nullptr;
+    int* d_bad = nullptr;
+    double* h_cube = nullptr;  // pinned
+    int* h_bad = nullptr;      // pinned
+    std::map<int, cudaGraphExec_t> cube_graphs;
     double* h_params = nullptr;  // pinned staging
     double* h_logL = nullptr;
     std::map<int, cudaGraphExec_t> graphs;
@@ -168,6 +176,13 @@ struct lg_ctx {
     {
         for (auto& g : graphs) cudaGraphExecDestroy(g.second);
         graphs.clear();
+        for (auto& g : cube_graphs) cudaGraphExecDestroy(g.second);
+        cube_graphs.clear();
+        cudaFree(d_priors);
+        cudaFree(d_cube);
+        cudaFree(d_bad);
+        cudaFreeHost(h_cube);
+        cudaFreeHost(h_bad);
         cudaFree(d_image);
         cudaFree(d_weight);
         cudaFree(d_models);
@@ -219,6 +234,71 @@ void shape_sizes(const lg::Shape& s, const lg::Model& m, lg_ctx* c)
         c->ctiles = c->ctiles_x * c->ctiles_y;
         c->csmem = th * twp * 4;
     }
+}
+
+// ------------------------------------------------------------ priors --
+// A parameter's prior and bounds in map order, for the unit-cube kernels.
+struct DevPrior {
+    int kind;     // lg::Prior::Kind
+    int bounded;  // reject values outside [lower, upper]
+    double a, b, lower, upper;
+};
+
+// Inverse normal CDF of Abramowitz & Stegun 26.2.23, the transform of the
+// normal prior (src/prior/norm.c:9-16), with every product, sum and quotient
+// rounded separately (no contraction), as the host evaluates it; log is
+// CUDA's double-precision log.
+__device__ double lg_norm_quantile(double u)
+{
+    const double v = u < 0.5 ? u : __dadd_rn(1.0, -u);
+    double t = __dsqrt_rn(__dmul_rn(-2.0, log(v)));
+    const double num = __dadd_rn(__dmul_rn(__dadd_rn(__dmul_rn(0.010328, t), 0.802853), t), 2.515517);
+    const double den = __dadd_rn(
+        __dmul_rn(__dadd_rn(__dmul_rn(__dadd_rn(__dmul_rn(0.001308, t), 0.189269), t), 1.432788), t), 1.0);
+    t = __dadd_rn(t, -__ddiv_rn(num, den));
+    return u < 0.5 ? -t : t;
+}
+
+// Unit cube (B x nd) -> physical parameters (B x np, map order) through the
+// priors: the transform of src/nested.c:42-61, one candidate per thread.
+// Pseudo-prior (derived) parameters, at map positions nd..np-1, take u = 0.5
+// as there.  The reference redraws while a value is out of bounds, which
+// never ends since the draw is a function of u (src/nested.c:54-56); here the
+// candidate is flagged instead (bad[b] = 1) and its logL is set to -inf.
+__global__ void __launch_bounds__(128)
+    lg_prior_transform(const double* __restrict__ cube, int B, int nd, int np, const DevPrior* __restrict__ pri,
+                       double* __restrict__ params, int* __restrict__ bad)
+{
+    const int b = blockIdx.x * blockDim.x + threadIdx.x;
+    if (b >= B) return;
+    int out = 0;
+    for (int i = 0; i < np; ++i) {
+        const DevPrior p = pri[i];
+        const double u = i < nd ? cube[(size_t)b * nd + i] : 0.5;
+        double v;
+        switch (p.kind) {
+        case lg::Prior::DELTA: v = p.a; break;                                              // src/prior/delta.c:50-53
+        case lg::Prior::UNIF: v = __dadd_rn(p.a, __dmul_rn(u, __dadd_rn(p.b, -p.a))); break;  // src/prior/unif.c:68-73
+        case lg::Prior::NORM: v = __dadd_rn(p.a, __dmul_rn(p.b, lg_norm_quantile(u))); break;  // src/prior/norm.c:77-82
+        default: v = CUDART_NAN; out = 1; break;
+        }
+        if (p.bounded && (v < p.lower || v > p.upper)) out = 1;
+        params[(size_t)b * np + i] = v;
+    }
+    bad[b] = out;
+}
+
+// logL = -inf for the candidates the transform rejected; the physical
+// parameters are copied out when phys is not NULL.
+__global__ void __launch_bounds__(128)
+    lg_prior_finish(int B, int np, const int* __restrict__ bad, const double* __restrict__ params,
+                    double* __restrict__ logL, double* __restrict__ phys)
+{
+    const int b = blockIdx.x * blockDim.x + threadIdx.x;
+    if (b >= B) return;
+    if (bad[b]) logL[b] = -CUDART_INF;
+    if (phys)
+        for (int i = 0; i < np; ++i) phys[(size_t)b * np + i] = params[(size_t)b * np + i];
 }
 
 int create_impl(lg_ctx* c, const lg_image_desc* img, const lg_object_desc* objs, int nobjs, const lg_options* opts)
@@ -309,6 +389,24 @@ int create_impl(lg_ctx* c, const lg_image_desc* img, const lg_object_desc* objs,
     if ((rc = c->cuda(cudaMallocHost((void**)&c->h_params, B * np * 8), "pinned params")) ||
         (rc = c->cuda(cudaMallocHost((void**)&c->h_logL, B * 8), "pinned logL")))
         return rc;
+    // unit-cube path (priors are checked when it is called)
+    const size_t nd = (size_t)m.ndims;
+    std::vector<DevPrior> pri(np);
+    for (size_t i = 0; i < np; ++i) {
+        const lg::ParamInfo& par = m.pars[m.pmap[i]];
+        pri[i] = {par.has_prior ? (int)par.prior.kind : 0, par.bounded ? 1 : 0, par.prior.a, par.prior.b, par.lower,
+                  par.upper};
+    }
+    if ((rc = alloc(&c->d_priors, std::max<size_t>(np, 1) * sizeof(DevPrior), "priors")) ||
+        (rc = alloc((void**)&c->d_cube, std::max<size_t>(B * nd, 1) * 8, "cube")) ||
+        (rc = alloc((void**)&c->d_bad, B * 4, "rejection flags")))
+        return rc;
+    if ((rc = c->cuda(cudaMallocHost((void**)&c->h_cube, std::max<size_t>(B * nd, 1) * 8), "pinned cube")) ||
+        (rc = c->cuda(cudaMallocHost((void**)&c->h_bad, B * 4), "pinned flags")))
+        return rc;
+    if (np && (rc = c->cuda(cudaMemcpy(c->d_priors, pri.data(), np * sizeof(DevPrior), cudaMemcpyHostToDevice),
+                            "upload priors")))
+        return rc;
     if ((rc = c->cuda(cudaMemcpy(c->d_image, img->image, N * 4, cudaMemcpyHostToDevice), "upload image")) ||
         (rc = c->cuda(cudaMemcpy(c->d_weight, img->weight, N * 4, cudaMemcpyHostToDevice), "upload weight")))
         return rc;
@@ -343,6 +441,94 @@ int graph_for(lg_ctx* c, int B, cudaGraphExec_t* out)
     if ((rc = c->cuda(e, "graph instantiate"))) return rc;
     c->graphs[B] = ge;
     *out = ge;
+    return LG_OK;
+}
+
+int check_priors(lg_ctx* c)
+{
+    const lg::Model& m = c->model;
+    for (size_t i = 0; i < m.pars.size(); ++i)
+        if (!m.pars[m.pmap[i]].has_prior) return c->fail(LG_ERR_INPUT, "missing prior: " + m.pars[m.pmap[i]].id);
+    return LG_OK;
+}
+
+// Enqueue prior transform .. logL for B unit-cube points (device pointers):
+// the physical parameters land in the context's params buffer (and in
+// d_phys when not NULL), the rejection flags in d_bad.
+int enqueue_cube(lg_ctx* c, int B, const double* d_cube, double* d_phys, double* d_logL, cudaStream_t s)
+{
+    const int np = (int)c->model.pars.size(), nd = c->model.ndims;
+    const int blocks = (B + 127) / 128;
+    int rc;
+    lg_prior_transform<<<blocks, 128, 0, s>>>(d_cube, B, nd, np, static_cast<const DevPrior*>(c->d_priors),
+                                              c->d_params, c->d_bad);
+    if ((rc = c->cuda(cudaGetLastError(), "prior transform"))) return rc;
+    if ((rc = c->enqueue(B, c->d_params, d_logL, s))) return rc;
+    lg_prior_finish<<<blocks, 128, 0, s>>>(B, np, c->d_bad, c->d_params, d_logL, d_phys);
+    return c->cuda(cudaGetLastError(), "prior finish");
+}
+
+// Upload of B cube points, their evaluation and the read-back of logL, the
+// physical parameters and the rejection flags.
+int enqueue_cube_io(lg_ctx* c, int B, cudaStream_t s)
+{
+    const size_t np = c->model.pars.size(), nd = (size_t)c->model.ndims;
+    int rc;
+    if (nd && (rc = c->cuda(cudaMemcpyAsync(c->d_cube, c->h_cube, B * nd * 8, cudaMemcpyHostToDevice, s), "cube upload")))
+        return rc;
+    if ((rc = enqueue_cube(c, B, c->d_cube, nullptr, c->d_logL, s))) return rc;
+    if ((rc = c->cuda(cudaMemcpyAsync(c->h_logL, c->d_logL, B * 8, cudaMemcpyDeviceToHost, s), "logL read")) ||
+        (np && (rc = c->cuda(cudaMemcpyAsync(c->h_params, c->d_params, B * np * 8, cudaMemcpyDeviceToHost, s),
+                             "params read"))) ||
+        (rc = c->cuda(cudaMemcpyAsync(c->h_bad, c->d_bad, B * 4, cudaMemcpyDeviceToHost, s), "flags read")))
+        return rc;
+    return LG_OK;
+}
+
+int cube_graph_for(lg_ctx* c, int B, cudaGraphExec_t* out)
+{
+    auto it = c->cube_graphs.find(B);
+    if (it != c->cube_graphs.end()) {
+        *out = it->second;
+        return LG_OK;
+    }
+    int rc;
+    cudaGraph_t g;
+    if ((rc = c->cuda(cudaStreamBeginCapture(c->stream, cudaStreamCaptureModeThreadLocal), "begin capture")))
+        return rc;
+    int erc = enqueue_cube_io(c, B, c->stream);
+    cudaError_t e = cudaStreamEndCapture(c->stream, &g);
+    if (erc) return erc;
+    if ((rc = c->cuda(e, "end capture"))) return rc;
+    cudaGraphExec_t ge;
+    e = cudaGraphInstantiate(&ge, g, 0);
+    cudaGraphDestroy(g);
+    if ((rc = c->cuda(e, "graph instantiate"))) return rc;
+    c->cube_graphs[B] = ge;
+    *out = ge;
+    return LG_OK;
+}
+
+// Host unit-cube evaluation of B <= max_batch points: logL and the physical
+// parameters (NaN for rejected points when nan_rejected) and flags.
+int cube_eval_chunk(lg_ctx* c, const double* cube, int B, double* phys, double* logL, bool nan_rejected)
+{
+    const size_t np = c->model.pars.size(), nd = (size_t)c->model.ndims;
+    int rc;
+    if (nd) std::memcpy(c->h_cube, cube, (size_t)B * nd * 8);
+    if (c->flags & LG_FLAG_NO_GRAPH) {
+        if ((rc = enqueue_cube_io(c, B, c->stream))) return rc;
+    } else {
+        cudaGraphExec_t ge;
+        if ((rc = cube_graph_for(c, B, &ge))) return rc;
+        if ((rc = c->cuda(cudaGraphLaunch(ge, c->stream), "graph launch"))) return rc;
+    }
+    if ((rc = c->cuda(cudaStreamSynchronize(c->stream), "evaluate"))) return rc;
+    std::memcpy(logL, c->h_logL, (size_t)B * 8);
+    if (phys)
+        for (int b = 0; b < B; ++b)
+            for (size_t i = 0; i < np; ++i)
+                phys[(size_t)b * np + i] = (nan_rejected && c->h_bad[b]) ? NAN : c->h_params[(size_t)b * np + i];
     return LG_OK;
 }
 
@@ -534,31 +720,29 @@ int lg_eval_batch_device(lg_ctx* c, const double* d_params, int B, double* d_log
 int lg_eval_cube_batch(lg_ctx* c, const double* cube, int B, double* phys, double* logL)
 {
     if (!c || !cube || !logL || B < 0) return LG_ERR_INPUT;
-    const lg::Model& m = c->model;
-    const int np = (int)m.pars.size(), nd = m.ndims;
-    for (int i = 0; i < np; ++i)
-        if (!m.pars[m.pmap[i]].has_prior) return c->fail(LG_ERR_INPUT, "missing prior: " + m.pars[m.pmap[i]].id);
-    std::vector<double> p((size_t)B * np);
-    std::vector<char> bad(B, 0);
-    for (int b = 0; b < B; ++b)
-        for (int i = 0; i < np; ++i) {
-            const lg::ParamInfo& par = m.pars[m.pmap[i]];
-            const double u = i < nd ? cube[(size_t)b * nd + i] : 0.5;
-            const double v = par.prior.apply(u);
-            if (par.bounded && (v < par.lower || v > par.upper)) bad[b] = 1;
-            p[(size_t)b * np + i] = v;
-        }
+    int rc;
+    if ((rc = check_priors(c))) return rc;
+    if (B == 0) return LG_OK;
+    if ((rc = c->cuda(cudaSetDevice(c->device), "cudaSetDevice"))) return rc;
+    const size_t np = c->model.pars.size(), nd = (size_t)c->model.ndims;
     for (int b0 = 0; b0 < B; b0 += c->max_batch) {
         const int nb = std::min(c->max_batch, B - b0);
-        int rc = lg_eval_batch(c, p.data() + (size_t)b0 * np, nb, logL + b0);
-        if (rc) return rc;
-    }
-    for (int b = 0; b < B; ++b) {
-        if (bad[b]) logL[b] = -HUGE_VAL;
-        if (phys)
-            for (int i = 0; i < np; ++i) phys[(size_t)b * np + i] = bad[b] ? NAN : p[(size_t)b * np + i];
+        if ((rc = cube_eval_chunk(c, cube + (size_t)b0 * nd, nb, phys ? phys + (size_t)b0 * np : nullptr, logL + b0,
+                                  true)))
+            return rc;
     }
     return LG_OK;
+}
+
+int lg_eval_cube_batch_device(lg_ctx* c, const double* d_cube, int B, double* d_phys, double* d_logL, void* stream)
+{
+    if (!c || (!d_cube && c->model.ndims > 0) || !d_logL || B < 0) return LG_ERR_INPUT;
+    if (B > c->max_batch) return c->fail(LG_ERR_INPUT, "batch larger than max_batch");
+    int rc;
+    if ((rc = check_priors(c))) return rc;
+    if (B == 0) return LG_OK;
+    if ((rc = c->cuda(cudaSetDevice(c->device), "cudaSetDevice"))) return rc;
+    return enqueue_cube(c, B, d_cube, d_phys, d_logL, stream ? (cudaStream_t)stream : c->stream);
 }
 
 namespace {
@@ -756,24 +940,17 @@ void loglike(double cube[], int* ndim, int* npar, double* lnew, void* ctx)
         c->err = "loglike: ndim/npar do not match the context";
         return;
     }
-    bool bad = false;
-    for (int i = 0; i < *npar; ++i) {
-        const lg::ParamInfo& par = m.pars[m.pmap[i]];
-        if (!par.has_prior) {
-            c->err = "missing prior: " + par.id;
-            return;
-        }
-        const double unit = i < *ndim ? cube[i] : 0.5;
-        const double phys = par.prior.apply(unit);
-        if (par.bounded && (phys < par.lower || phys > par.upper)) bad = true;
-        cube[i] = phys;
-    }
-    if (bad) {
+    if (check_priors(c) || c->cuda(cudaSetDevice(c->device), "cudaSetDevice")) return;
+    std::vector<double> p(*npar);
+    double l;
+    if (cube_eval_chunk(c, cube, 1, p.data(), &l, false)) return;
+    // MultiNest records the physical values written back into cube
+    for (int i = 0; i < *npar; ++i) cube[i] = p[i];
+    if (c->h_bad[0]) {
         c->err = "loglike: parameter outside its bounds";
         return;
     }
-    double l;
-    if (lg_eval_batch(c, cube, 1, &l) == LG_OK) *lnew = l;
+    *lnew = l;
 }
 
 }  // extern "C"
