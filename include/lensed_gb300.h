@@ -167,8 +167,10 @@ long lg_masked(const lg_ctx* ctx);
  * set_params, render, convolve, chi^2 and its sum.  B <= max_batch. */
 int lg_eval_batch(lg_ctx* ctx, const double* params, int B, double* logL);
 
-/* Same with device pointers on a caller stream (NULL = the context's
- * stream); returns without synchronising. */
+/* Same with device pointers on a caller stream; returns without
+ * synchronising.  With stream = NULL the work runs on the context's own
+ * (non-blocking) stream, after the work already queued on the legacy
+ * default stream; buffers filled on any other stream must be ready first. */
 int lg_eval_batch_device(lg_ctx* ctx, const double* d_params, int B, double* d_logL, void* stream);
 
 /* Unit-cube points (B x ndims, host) -> physical parameters via the priors
@@ -177,7 +179,7 @@ int lg_eval_batch_device(lg_ctx* ctx, const double* d_params, int B, double* d_l
 int lg_eval_cube_batch(lg_ctx* ctx, const double* cube, int B, double* phys, double* logL);
 
 /* The unit-cube evaluation on the GPU with device pointers on a caller
- * stream (NULL = the context's stream), B <= max_batch; returns without
+ * stream (NULL: as lg_eval_batch_device), B <= max_batch; returns without
  * synchronising.  The prior transform of src/nested.c:42-61 runs as a
  * kernel (one candidate per thread; unif, norm, delta priors; pseudo-prior
  * parameters at u = 0.5), followed by the likelihood kernels.  d_phys
@@ -227,7 +229,8 @@ int lg_write_fits_memory(int width, int height, int nlayers, const float* const*
 /* Device times (ms) of the four stages of one evaluation of B candidates
  * with device pointers: set_params, render, convolve (0 without a PSF) and
  * the chi^2 finish -- the counterpart of the reference's --profile table
- * (src/nested.c:21-40, src/profile.c:36-83). */
+ * (src/nested.c:21-40, src/profile.c:36-83).  Runs on the context's stream
+ * after the work queued on the legacy default stream, and synchronises. */
 int lg_eval_profile(lg_ctx* ctx, const double* d_params, int B, double* d_logL, float* stage_ms);
 
 /* Measured FP32 FMA throughput (TFLOP/s) of a device, for roofline

@@ -493,9 +493,10 @@ class Context:
         return lib().lg_masked(self.h)
 
     def to_map_order(self, params_obj):
-        """Reorder (..., npars) parameters from object order to map order."""
+        """Reorder (..., npars) parameters from object order to map order
+        (C-contiguous, ready for the device entry points)."""
         p = np.asarray(params_obj, dtype=np.float64)
-        return p[..., self.pmap]
+        return np.ascontiguousarray(p[..., self.pmap])
 
     def eval_batch(self, params) -> np.ndarray:
         p = np.ascontiguousarray(np.atleast_2d(params), dtype=np.float64)

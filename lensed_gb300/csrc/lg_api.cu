@@ -444,6 +444,22 @@ int graph_for(lg_ctx* c, int B, cudaGraphExec_t* out)
     return LG_OK;
 }
 
+// The context's stream does not synchronise with the legacy default stream
+// (it is non-blocking, so that graph capture on it stays legal).  Calls that
+// take caller device pointers and run on it first wait for the work already
+// queued on the legacy stream, where frameworks such as PyTorch enqueue the
+// copies that fill those buffers by default.
+int order_after_legacy(lg_ctx* c)
+{
+    cudaEvent_t e;
+    int rc;
+    if ((rc = c->cuda(cudaEventCreateWithFlags(&e, cudaEventDisableTiming), "event"))) return rc;
+    rc = c->cuda(cudaEventRecord(e, cudaStreamLegacy), "event record");
+    if (!rc) rc = c->cuda(cudaStreamWaitEvent(c->stream, e, 0), "stream wait");
+    cudaEventDestroy(e);
+    return rc;
+}
+
 int check_priors(lg_ctx* c)
 {
     const lg::Model& m = c->model;
@@ -714,6 +730,7 @@ int lg_eval_batch_device(lg_ctx* c, const double* d_params, int B, double* d_log
     if (B > c->max_batch) return c->fail(LG_ERR_INPUT, "batch larger than max_batch");
     int rc;
     if ((rc = c->cuda(cudaSetDevice(c->device), "cudaSetDevice"))) return rc;
+    if (!stream && (rc = order_after_legacy(c))) return rc;
     return c->enqueue(B, d_params, d_logL, stream ? (cudaStream_t)stream : c->stream);
 }
 
@@ -742,6 +759,7 @@ int lg_eval_cube_batch_device(lg_ctx* c, const double* d_cube, int B, double* d_
     if ((rc = check_priors(c))) return rc;
     if (B == 0) return LG_OK;
     if ((rc = c->cuda(cudaSetDevice(c->device), "cudaSetDevice"))) return rc;
+    if (!stream && (rc = order_after_legacy(c))) return rc;
     return enqueue_cube(c, B, d_cube, d_phys, d_logL, stream ? (cudaStream_t)stream : c->stream);
 }
 
@@ -863,6 +881,7 @@ int lg_eval_profile(lg_ctx* c, const double* d_params, int B, double* d_logL, fl
     if (B > c->max_batch) return c->fail(LG_ERR_INPUT, "batch larger than max_batch");
     int rc;
     if ((rc = c->cuda(cudaSetDevice(c->device), "cudaSetDevice"))) return rc;
+    if ((rc = order_after_legacy(c))) return rc;
     cudaEvent_t ev[5] = {};
     for (auto& e : ev)
         if ((rc = c->cuda(cudaEventCreate(&e), "event"))) return rc;

@@ -42,6 +42,9 @@ struct Plugin {
     std::vector<ParamDef> pars;
     std::string source;             // CUDA device source of the plugin
     std::vector<std::string> deps;  // plugins whose source must come first
+    // evaluation functions are templates over the vector type (float2 or
+    // lg_pair2), so the paired ray kernels can call them directly
+    bool paired = false;
 };
 
 const Plugin* find_plugin(const std::string& name);

@@ -65,6 +65,40 @@ void emit_compute(std::ostringstream& o, const Model& m)
     o << "    return f;\n}\n\n";
 }
 
+// The same sum for two rays at once (lg_pair2), for the paired ray kernels
+// of the fast mode: plugins with template evaluation functions are called
+// with the pair; any other plugin is called once per ray.
+void emit_compute2(std::ostringstream& o, const Model& m)
+{
+    o << "#define LG_PAIRED 1\n";
+    o << "LG_DEV lg_pair lg_compute2(const lg_model& m, lg_pair2 x)\n{\n"
+      << "    lg_pair2 y = x;\n    lg_pair f = lg_pair_of(0.0f);\n"
+      << "    lg_pair2 a = {lg_pair_of(0.0f), lg_pair_of(0.0f)};\n";
+    int trigger = 0;
+    for (size_t i = 0; i < m.objs.size(); ++i) {
+        const Plugin* p = m.objs[i].plugin;
+        if (p->kind != trigger && p->kind != LG_FOREGROUND) {
+            if (trigger == LG_LENS) o << "    lg_deflect(y, a);\n    a = {lg_pair_of(0.0f), lg_pair_of(0.0f)};\n";
+            trigger = p->kind;
+        }
+        const char* fn = p->kind == LG_LENS ? "lg_deflection_" : (p->kind == LG_SOURCE ? "lg_brightness_" : "lg_foreground_");
+        const char* acc = p->kind == LG_LENS ? "a" : "f";
+        const char* arg = p->kind == LG_FOREGROUND ? "x" : "y";
+        const std::string obj = "&m.o" + std::to_string(i);
+        if (p->paired) {
+            o << "    " << acc << " += " << fn << p->name << "(" << obj << ", " << arg << ");\n";
+        } else if (p->kind == LG_LENS) {
+            o << "    a += lg_pair2_join(" << fn << p->name << "(" << obj << ", lg_lane(y, 0)), " << fn << p->name
+              << "(" << obj << ", lg_lane(y, 1)));\n";
+        } else {
+            o << "    f += lg_pair_of(" << fn << p->name << "(" << obj << ", lg_lane(" << arg << ", 0)), " << fn
+              << p->name << "(" << obj << ", lg_lane(" << arg << ", 1)));\n";
+        }
+    }
+    if (trigger == LG_LENS) o << "    lg_deflect(y, a);\n";
+    o << "    return f;\n}\n\n";
+}
+
 // Generated set_params (src/kernel.c:114-150, :401-656), including the
 // deflection of image-plane (x, y) priors through the lens planes before the
 // object's own plane.
@@ -175,6 +209,7 @@ std::string compose_source(const Model& m, const Shape& s, bool strict, Part par
         o << "#define LG_HAS_PSF 0\n";
     }
     emit_compute(o, m);
+    if (!strict) emit_compute2(o, m);
     o << kernels_source() << "\n";
     return o.str();
 }
@@ -209,6 +244,7 @@ std::string compose_multi_source(const Model& m, const std::vector<std::pair<int
         o << (n ? ", " : "") << "{" << hexf((float)m.rule->weig[n]) << ", " << hexf((float)m.rule->errw[n]) << "}";
     o << "};\n";
     emit_compute(o, m);
+    if (!strict) emit_compute2(o, m);
     o << "#define LG_PSF_SHAPES";
     for (const auto& ps : psf_shapes) o << " LG_PSF_CASE(" << ps.first << ", " << ps.second << ")";
     o << "\n";

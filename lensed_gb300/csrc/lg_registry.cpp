@@ -58,6 +58,7 @@ std::vector<Plugin> builtin_plugins()
         p.kind = kind;
         p.pars = pars;
         p.deps = deps;
+        p.paired = true;
         const char* src = embedded_object(name);
         p.source = src ? src : "";
         v.push_back(p);

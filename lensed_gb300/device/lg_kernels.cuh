@@ -76,6 +76,36 @@ LG_DEV void lg_render_tile(const lg_model* __restrict__ models, float* __restric
         v[j] = 0.0f;
         e[j] = 0.0f;
     }
+#if defined(LG_PAIRED) && LG_RPPT % 2 == 0
+    // the fast mode traces the thread's pixels two at a time with paired
+    // FP32 instructions; each lane computes what the scalar loop computes
+    lg_pair px[LG_RPPT / 2], py[LG_RPPT / 2], pv[LG_RPPT / 2], pe[LG_RPPT / 2];
+#pragma unroll
+    for (int j = 0; j < LG_RPPT / 2; ++j) {
+        px[j] = lg_pair_of(xp[2 * j].x, xp[2 * j + 1].x);
+        py[j] = lg_pair_of(xp[2 * j].y, xp[2 * j + 1].y);
+        pv[j] = lg_pair_of(0.0f);
+        pe[j] = lg_pair_of(0.0f);
+    }
+#pragma unroll 1
+    for (int n = 0; n < LG_Q; ++n) {
+        const float2 q = lg_qq[n];
+        const float2 w = lg_ww[n];
+#pragma unroll
+        for (int j = 0; j < LG_RPPT / 2; ++j) {
+            const lg_pair f = lg_compute2(m, lg_pair2{px[j] + q.x, py[j] + q.y});
+            pv[j] += w.x * f;
+            if (MODE == 2) pe[j] += w.y * f;
+        }
+    }
+#pragma unroll
+    for (int j = 0; j < LG_RPPT / 2; ++j) {
+        v[2 * j] = pv[j].v.x;
+        v[2 * j + 1] = pv[j].v.y;
+        e[2 * j] = pe[j].v.x;
+        e[2 * j + 1] = pe[j].v.y;
+    }
+#else
 #pragma unroll 1
     for (int n = 0; n < LG_Q; ++n) {
         const float2 q = lg_qq[n];
@@ -87,6 +117,7 @@ LG_DEV void lg_render_tile(const lg_model* __restrict__ models, float* __restric
             if (MODE == 2) e[j] += w.y * f;
         }
     }
+#endif
     if (MODE == 1) {
         __shared__ double red[LG_RT / 32];
         double s = 0.0;

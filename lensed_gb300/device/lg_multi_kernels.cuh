@@ -105,6 +105,28 @@ LG_DEV void lg_multi_render_body(const lg_model* __restrict__ models, const lg_s
             xp[j] = make_float2(I.rx + I.sx * (float)(k % I.W), I.ry + I.sy * (float)(k / I.W));
             v[j] = 0.0f;
         }
+#if defined(LG_PAIRED) && LG_RPPT % 2 == 0
+        // paired FP32 ray tracing, as in the single-system render kernel
+        lg_pair px[LG_RPPT / 2], py[LG_RPPT / 2], pv[LG_RPPT / 2];
+#pragma unroll
+        for (int j = 0; j < LG_RPPT / 2; ++j) {
+            px[j] = lg_pair_of(xp[2 * j].x, xp[2 * j + 1].x);
+            py[j] = lg_pair_of(xp[2 * j].y, xp[2 * j + 1].y);
+            pv[j] = lg_pair_of(0.0f);
+        }
+#pragma unroll 1
+        for (int n = 0; n < LG_Q; ++n) {
+            const float2 q = lg_qq[n];
+            const float2 w = lg_ww[n];
+#pragma unroll
+            for (int j = 0; j < LG_RPPT / 2; ++j) pv[j] += w.x * lg_compute2(m, lg_pair2{px[j] + q.x, py[j] + q.y});
+        }
+#pragma unroll
+        for (int j = 0; j < LG_RPPT / 2; ++j) {
+            v[2 * j] = pv[j].v.x;
+            v[2 * j + 1] = pv[j].v.y;
+        }
+#else
 #pragma unroll 1
         for (int n = 0; n < LG_Q; ++n) {
             const float2 q = lg_qq[n];
@@ -112,6 +134,7 @@ LG_DEV void lg_multi_render_body(const lg_model* __restrict__ models, const lg_s
 #pragma unroll
             for (int j = 0; j < LG_RPPT; ++j) v[j] += w.x * lg_compute(m, xp[j] + q);
         }
+#endif
         if (WITH_PSF) {
 #pragma unroll
             for (int j = 0; j < LG_RPPT; ++j) {

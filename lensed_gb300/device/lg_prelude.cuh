@@ -22,6 +22,7 @@
 #define LG_INF __int_as_float(0x7f800000)
 
 #define LG_DEV static __device__ __forceinline__
+#define LG_DEV_MEMBER __device__ __forceinline__
 
 LG_DEV float2 operator+(float2 a, float2 b) { return make_float2(a.x + b.x, a.y + b.y); }
 LG_DEV float2 operator-(float2 a, float2 b) { return make_float2(a.x - b.x, a.y - b.y); }
@@ -100,3 +101,149 @@ LG_DEV void lg_deflect(float2& y, float2 a)
 {
     y -= (dot(a, a) < LG_INF) ? a : make_float2(1E10f, 1E10f);
 }
+
+// ------------------------------------------------------------ ray pairs --
+// The evaluation module of the fast mode traces two rays per thread at once
+// with Blackwell's paired single-precision instructions (add/mul/fma on
+// f32x2): lg_pair holds the value of one scalar for both rays, lg_pair2 a
+// 2-vector for both rays.  Each lane is computed exactly as the scalar code
+// computes it (the same IEEE operations; a product followed by a sum is
+// fused into one fma, as the scalar build contracts it).  The plugins'
+// evaluation functions are templates over the vector type V (float2 or
+// lg_pair2) and are written once for both.
+struct lg_pair {
+    float2 v;  // (ray 0, ray 1)
+};
+// a pending product a * b, fused into an fma by a following + or -
+struct lg_pair_prod {
+    float2 a, b;
+    LG_DEV_MEMBER operator lg_pair() const { return lg_pair{__fmul2_rn(a, b)}; }
+};
+struct lg_pair2 {
+    lg_pair x, y;
+};
+struct lg_pair_mat22 {
+    lg_pair a, b, c, d;
+};
+
+LG_DEV float2 lg_bc(float s) { return make_float2(s, s); }
+LG_DEV lg_pair lg_pair_of(float s) { return lg_pair{lg_bc(s)}; }
+LG_DEV lg_pair lg_pair_of(float a, float b) { return lg_pair{make_float2(a, b)}; }
+LG_DEV lg_pair lg_mat(lg_pair p) { return p; }
+LG_DEV lg_pair lg_mat(lg_pair_prod p) { return p; }
+LG_DEV float2 lg_neg2(float2 a) { return make_float2(-a.x, -a.y); }
+
+// products
+LG_DEV lg_pair_prod operator*(lg_pair a, lg_pair b) { return {a.v, b.v}; }
+LG_DEV lg_pair_prod operator*(float a, lg_pair b) { return {lg_bc(a), b.v}; }
+LG_DEV lg_pair_prod operator*(lg_pair a, float b) { return {a.v, lg_bc(b)}; }
+LG_DEV lg_pair_prod operator*(lg_pair_prod a, lg_pair b) { return {__fmul2_rn(a.a, a.b), b.v}; }
+LG_DEV lg_pair_prod operator*(lg_pair a, lg_pair_prod b) { return {a.v, __fmul2_rn(b.a, b.b)}; }
+LG_DEV lg_pair_prod operator*(lg_pair_prod a, float b) { return {__fmul2_rn(a.a, a.b), lg_bc(b)}; }
+LG_DEV lg_pair_prod operator*(float a, lg_pair_prod b) { return {lg_bc(a), __fmul2_rn(b.a, b.b)}; }
+LG_DEV lg_pair_prod operator*(lg_pair_prod a, lg_pair_prod b) { return {__fmul2_rn(a.a, a.b), __fmul2_rn(b.a, b.b)}; }
+// sums and differences (a product on either side is fused)
+LG_DEV lg_pair operator+(lg_pair a, lg_pair b) { return {__fadd2_rn(a.v, b.v)}; }
+LG_DEV lg_pair operator+(lg_pair a, float b) { return {__fadd2_rn(a.v, lg_bc(b))}; }
+LG_DEV lg_pair operator+(float a, lg_pair b) { return {__fadd2_rn(lg_bc(a), b.v)}; }
+LG_DEV lg_pair operator+(lg_pair_prod p, lg_pair c) { return {__ffma2_rn(p.a, p.b, c.v)}; }
+LG_DEV lg_pair operator+(lg_pair c, lg_pair_prod p) { return {__ffma2_rn(p.a, p.b, c.v)}; }
+LG_DEV lg_pair operator+(lg_pair_prod p, float c) { return {__ffma2_rn(p.a, p.b, lg_bc(c))}; }
+LG_DEV lg_pair operator+(float c, lg_pair_prod p) { return {__ffma2_rn(p.a, p.b, lg_bc(c))}; }
+LG_DEV lg_pair operator+(lg_pair_prod p, lg_pair_prod q) { return {__ffma2_rn(p.a, p.b, __fmul2_rn(q.a, q.b))}; }
+LG_DEV lg_pair operator-(lg_pair a) { return {lg_neg2(a.v)}; }
+LG_DEV lg_pair_prod operator-(lg_pair_prod p) { return {lg_neg2(p.a), p.b}; }
+LG_DEV lg_pair operator-(lg_pair a, lg_pair b) { return {__ffma2_rn(b.v, lg_bc(-1.0f), a.v)}; }
+LG_DEV lg_pair operator-(lg_pair a, float b) { return {__fadd2_rn(a.v, lg_bc(-b))}; }
+LG_DEV lg_pair operator-(float a, lg_pair b) { return {__ffma2_rn(b.v, lg_bc(-1.0f), lg_bc(a))}; }
+LG_DEV lg_pair operator-(lg_pair_prod p, lg_pair c) { return {__ffma2_rn(p.a, p.b, lg_neg2(c.v))}; }
+LG_DEV lg_pair operator-(lg_pair c, lg_pair_prod p) { return {__ffma2_rn(lg_neg2(p.a), p.b, c.v)}; }
+LG_DEV lg_pair operator-(lg_pair_prod p, float c) { return {__ffma2_rn(p.a, p.b, lg_bc(-c))}; }
+LG_DEV lg_pair operator-(float c, lg_pair_prod p) { return {__ffma2_rn(lg_neg2(p.a), p.b, lg_bc(c))}; }
+LG_DEV lg_pair operator-(lg_pair_prod p, lg_pair_prod q) { return {__ffma2_rn(p.a, p.b, lg_neg2(__fmul2_rn(q.a, q.b)))}; }
+// quotients, lane by lane (the module's division)
+LG_DEV lg_pair operator/(lg_pair a, lg_pair b) { return {make_float2(a.v.x / b.v.x, a.v.y / b.v.y)}; }
+LG_DEV lg_pair operator/(lg_pair a, float b) { return {make_float2(a.v.x / b, a.v.y / b)}; }
+LG_DEV lg_pair operator/(float a, lg_pair b) { return {make_float2(a / b.v.x, a / b.v.y)}; }
+LG_DEV lg_pair operator/(lg_pair_prod a, lg_pair b) { return lg_pair(a) / b; }
+LG_DEV lg_pair operator/(lg_pair_prod a, float b) { return lg_pair(a) / b; }
+LG_DEV lg_pair operator/(lg_pair a, lg_pair_prod b) { return a / lg_pair(b); }
+LG_DEV lg_pair operator/(float a, lg_pair_prod b) { return a / lg_pair(b); }
+LG_DEV lg_pair& operator+=(lg_pair& a, lg_pair b) { a = a + b; return a; }
+LG_DEV lg_pair& operator+=(lg_pair& a, lg_pair_prod b) { a = a + b; return a; }
+LG_DEV lg_pair& operator-=(lg_pair& a, lg_pair b) { a = a - b; return a; }
+LG_DEV lg_pair& operator*=(lg_pair& a, lg_pair b) { a = a * b; return a; }
+LG_DEV lg_pair& operator*=(lg_pair& a, float b) { a = a * b; return a; }
+
+// vectors of two rays
+LG_DEV lg_pair2 operator+(lg_pair2 a, lg_pair2 b) { return {a.x + b.x, a.y + b.y}; }
+LG_DEV lg_pair2 operator-(lg_pair2 a, lg_pair2 b) { return {a.x - b.x, a.y - b.y}; }
+LG_DEV lg_pair2 operator+(lg_pair2 a, float2 b) { return {a.x + b.x, a.y + b.y}; }
+LG_DEV lg_pair2 operator-(lg_pair2 a, float2 b) { return {a.x - b.x, a.y - b.y}; }
+LG_DEV lg_pair2 operator-(lg_pair2 a) { return {-a.x, -a.y}; }
+LG_DEV lg_pair2 operator*(float s, lg_pair2 a) { return {s * a.x, s * a.y}; }
+LG_DEV lg_pair2 operator*(lg_pair2 a, float s) { return {a.x * s, a.y * s}; }
+LG_DEV lg_pair2 operator*(lg_pair s, lg_pair2 a) { return {s * a.x, s * a.y}; }
+LG_DEV lg_pair2 operator*(lg_pair2 a, lg_pair s) { return {a.x * s, a.y * s}; }
+LG_DEV lg_pair2 operator*(lg_pair_prod s, lg_pair2 a) { return lg_pair(s) * a; }
+LG_DEV lg_pair2 operator/(lg_pair2 a, float s) { return {a.x / s, a.y / s}; }
+LG_DEV lg_pair2& operator+=(lg_pair2& a, lg_pair2 b) { a = a + b; return a; }
+LG_DEV lg_pair2& operator-=(lg_pair2& a, lg_pair2 b) { a = a - b; return a; }
+LG_DEV lg_pair2& operator-=(lg_pair2& a, float2 b) { a = a - b; return a; }
+LG_DEV lg_pair2& operator*=(lg_pair2& a, float s) { a = s * a; return a; }
+LG_DEV lg_pair2& operator*=(lg_pair2& a, lg_pair s) { a = s * a; return a; }
+LG_DEV lg_pair2& operator*=(lg_pair2& a, lg_pair_prod s) { a = lg_pair(s) * a; return a; }
+LG_DEV lg_pair dot(lg_pair2 a, lg_pair2 b) { return a.x * b.x + a.y * b.y; }
+LG_DEV lg_pair dot(float2 a, lg_pair2 b) { return a.x * b.x + a.y * b.y; }
+LG_DEV lg_pair2 mv22(mat22 m, lg_pair2 v) { return {m.a * v.x + m.b * v.y, m.c * v.x + m.d * v.y}; }
+LG_DEV lg_pair_mat22 make_mat22(lg_pair a, lg_pair b, lg_pair c, lg_pair d) { return {a, b, c, d}; }
+LG_DEV lg_pair2 mv22(lg_pair_mat22 m, lg_pair2 v) { return {m.a * v.x + m.b * v.y, m.c * v.x + m.d * v.y}; }
+LG_DEV lg_pair2 lg_pair2_join(float2 r0, float2 r1) { return {lg_pair_of(r0.x, r1.x), lg_pair_of(r0.y, r1.y)}; }
+LG_DEV float2 lg_lane(lg_pair2 a, int i) { return i ? make_float2(a.x.v.y, a.y.v.y) : make_float2(a.x.v.x, a.y.v.x); }
+
+// elementary functions, lane by lane (the module's single-precision library)
+#define LG_PAIR_FN1(fn) \
+    LG_DEV lg_pair fn(lg_pair a) { return {make_float2(fn(a.v.x), fn(a.v.y))}; } \
+    LG_DEV lg_pair fn(lg_pair_prod a) { return fn(lg_pair(a)); }
+LG_PAIR_FN1(sqrtf)
+LG_PAIR_FN1(rsqrtf)
+LG_PAIR_FN1(expf)
+LG_PAIR_FN1(exp2f)
+LG_PAIR_FN1(logf)
+LG_PAIR_FN1(log2f)
+LG_PAIR_FN1(sinf)
+LG_PAIR_FN1(cosf)
+LG_PAIR_FN1(atanf)
+LG_PAIR_FN1(atanhf)
+LG_PAIR_FN1(fabsf)
+#undef LG_PAIR_FN1
+LG_DEV lg_pair powf(lg_pair a, lg_pair b) { return {make_float2(powf(a.v.x, b.v.x), powf(a.v.y, b.v.y))}; }
+LG_DEV lg_pair powf(lg_pair a, float b) { return {make_float2(powf(a.v.x, b), powf(a.v.y, b))}; }
+LG_DEV lg_pair atan2f(lg_pair y, lg_pair x) { return {make_float2(atan2f(y.v.x, x.v.x), atan2f(y.v.y, x.v.y))}; }
+LG_DEV void sincosf(lg_pair a, lg_pair* s, lg_pair* c)
+{
+    sincosf(a.v.x, &s->v.x, &c->v.x);
+    sincosf(a.v.y, &s->v.y, &c->v.y);
+}
+LG_DEV lg_pair length(lg_pair2 a) { return sqrtf(dot(a, a)); }
+// OpenCL normalize(), lane by lane: a zero vector is returned unchanged
+LG_DEV lg_pair2 normalize(lg_pair2 a)
+{
+    const lg_pair l = length(a);
+    const float2 r0 = lg_lane(a, 0), r1 = lg_lane(a, 1);
+    return lg_pair2_join(l.v.x == 0.0f ? r0 : make_float2(r0.x / l.v.x, r0.y / l.v.x),
+                         l.v.y == 0.0f ? r1 : make_float2(r1.x / l.v.y, r1.y / l.v.y));
+}
+LG_DEV void lg_deflect(lg_pair2& y, lg_pair2 a)
+{
+    const lg_pair d = dot(a, a);
+    const float2 a0 = d.v.x < LG_INF ? lg_lane(a, 0) : make_float2(1E10f, 1E10f);
+    const float2 a1 = d.v.y < LG_INF ? lg_lane(a, 1) : make_float2(1E10f, 1E10f);
+    y -= lg_pair2_join(a0, a1);
+}
+
+// scalar type of a plugin's vector type
+template <class V> struct lg_scalar_of;
+template <> struct lg_scalar_of<float2> { typedef float type; };
+template <> struct lg_scalar_of<lg_pair2> { typedef lg_pair type; };
+#define LG_SCALAR(V) typename lg_scalar_of<V>::type

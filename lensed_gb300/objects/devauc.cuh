@@ -16,7 +16,8 @@ LG_DEV void lg_set_devauc(lg_data_devauc* o, float x, float y, float r, float ma
     o->rs = r;
     o->norm = expf(-0.4f * mag * LG_LOG_10) / LG_PI / r / r / q * LG_DEVAUC_C;
 }
-LG_DEV float lg_brightness_devauc(const lg_data_devauc* __restrict__ o, float2 x)
+template <class V>
+LG_DEV LG_SCALAR(V) lg_brightness_devauc(const lg_data_devauc* __restrict__ o, V x)
 {
     return o->norm * expf(-LG_DEVAUC_B * sqrtf(sqrtf(length(mv22(o->t, x - o->x)) / o->rs)));
 }

@@ -24,18 +24,20 @@ LG_DEV void lg_set_epl(lg_data_epl* o, float x1, float x2, float r, float t, flo
     lg_epl_setup(o, x1, x2, r, t, q, pa);
 }
 // Deflection in the rotated frame for the elliptical coordinates x.
-LG_DEV float2 lg_epl_frame(const lg_data_epl* __restrict__ o, float2 x)
+template <class V>
+LG_DEV V lg_epl_frame(const lg_data_epl* __restrict__ o, V x)
 {
+    typedef LG_SCALAR(V) S;
     const float T = 2 - o->t;
     const float f = o->f;
-    float r = length(x);
-    float phi = atan2f(x.y, x.x);
-    float s, c, s2, c2;
+    S r = length(x);
+    S phi = atan2f(x.y, x.x);
+    S s, c, s2, c2;
     sincosf(phi, &s, &c);
     sincosf(2 * phi, &s2, &c2);
-    mat22 R = make_mat22(c2, -s2, s2, c2);
-    float2 A = make_float2(c, s);
-    float2 a = A;
+    const auto R = make_mat22(c2, -s2, s2, c2);
+    V A = V{c, s};
+    V a = A;
 #pragma unroll
     for (int k = 1; k <= 10; ++k) {
         A = (-f * (2 * k - T) / (2 * k + T)) * mv22(R, A);
@@ -44,7 +46,8 @@ LG_DEV float2 lg_epl_frame(const lg_data_epl* __restrict__ o, float2 x)
     a *= o->n * powf(r, 1 - o->t);
     return mv22(o->w, a);
 }
-LG_DEV float2 lg_deflection_epl(const lg_data_epl* __restrict__ o, float2 x)
+template <class V>
+LG_DEV V lg_deflection_epl(const lg_data_epl* __restrict__ o, V x)
 {
     return lg_epl_frame(o, mv22(o->m, x - o->x));
 }

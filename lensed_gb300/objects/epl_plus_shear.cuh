@@ -11,9 +11,10 @@ LG_DEV void lg_set_epl_plus_shear(lg_data_epl_plus_shear* o, float x1, float x2,
     lg_epl_setup(&o->p, x1, x2, r, t, q, pa);
     o->g = make_mat22(g1, g2, g2, -g1);
 }
-LG_DEV float2 lg_deflection_epl_plus_shear(const lg_data_epl_plus_shear* __restrict__ o, float2 x)
+template <class V>
+LG_DEV V lg_deflection_epl_plus_shear(const lg_data_epl_plus_shear* __restrict__ o, V x)
 {
-    float2 dx = x - o->p.x;
-    float2 y = lg_epl_frame(&o->p, mv22(o->p.m, dx));
+    V dx = x - o->p.x;
+    V y = lg_epl_frame(&o->p, mv22(o->p.m, dx));
     return y + mv22(o->g, dx);
 }

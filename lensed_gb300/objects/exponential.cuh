@@ -14,7 +14,8 @@ LG_DEV void lg_set_exponential(lg_data_exponential* o, float x, float y, float r
     o->rs = rs;
     o->norm = expf(-0.4f * mag * LG_LOG_10) * 0.5f / LG_PI / rs / rs / q;
 }
-LG_DEV float lg_brightness_exponential(const lg_data_exponential* __restrict__ o, float2 x)
+template <class V>
+LG_DEV LG_SCALAR(V) lg_brightness_exponential(const lg_data_exponential* __restrict__ o, V x)
 {
     return o->norm * expf(-length(mv22(o->t, x - o->x)) / o->rs);
 }

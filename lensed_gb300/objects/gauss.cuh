@@ -14,8 +14,9 @@ LG_DEV void lg_set_gauss(lg_data_gauss* o, float x, float y, float sigma, float 
     o->s2 = sigma * sigma;
     o->norm = expf(-0.4f * mag * LG_LOG_10) * 0.5f / LG_PI / o->s2 / q;
 }
-LG_DEV float lg_brightness_gauss(const lg_data_gauss* __restrict__ o, float2 x)
+template <class V>
+LG_DEV LG_SCALAR(V) lg_brightness_gauss(const lg_data_gauss* __restrict__ o, V x)
 {
-    float2 y = mv22(o->t, x - o->x);
+    V y = mv22(o->t, x - o->x);
     return o->norm * expf(-0.5f * dot(y, y) / o->s2);
 }

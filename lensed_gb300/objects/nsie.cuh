@@ -17,11 +17,13 @@ LG_DEV void lg_set_nsie(lg_data_nsie* o, float x, float y, float r, float rc, fl
     o->e = sqrtf(1 - q * q);
     o->d = r * sqrtf(q) / sqrtf(1 - q * q);
 }
-LG_DEV float2 lg_deflection_nsie(const lg_data_nsie* __restrict__ o, float2 x)
+template <class V>
+LG_DEV V lg_deflection_nsie(const lg_data_nsie* __restrict__ o, V x)
 {
+    typedef LG_SCALAR(V) T;
     x -= o->x;
-    float2 y = mv22(o->m, x);
-    float r = sqrtf(o->q2 * y.x * y.x + y.y * y.y);
-    y = o->d * make_float2(atanf(y.x * o->e / (o->rc + r)), atanhf(y.y * o->e / (o->rc * o->q2 + r)));
+    V y = mv22(o->m, x);
+    T r = sqrtf(o->q2 * y.x * y.x + y.y * y.y);
+    y = o->d * V{atanf(y.x * o->e / (o->rc + r)), atanhf(y.y * o->e / (o->rc * o->q2 + r))};
     return mv22(o->w, y);
 }

@@ -10,7 +10,8 @@ LG_DEV void lg_set_nsis(lg_data_nsis* o, float x, float y, float r, float rc)
     o->r = r;
     o->rc = rc;
 }
-LG_DEV float2 lg_deflection_nsis(const lg_data_nsis* __restrict__ o, float2 x)
+template <class V>
+LG_DEV V lg_deflection_nsis(const lg_data_nsis* __restrict__ o, V x)
 {
     x -= o->x;
     return (o->r / (o->rc + length(x))) * x;

@@ -10,7 +10,8 @@ LG_DEV void lg_set_point_mass(lg_data_point_mass* o, float x, float y, float r)
     o->x = make_float2(x, y);
     o->r2 = r * r;
 }
-LG_DEV float2 lg_deflection_point_mass(const lg_data_point_mass* __restrict__ o, float2 x)
+template <class V>
+LG_DEV V lg_deflection_point_mass(const lg_data_point_mass* __restrict__ o, V x)
 {
     x -= o->x;
     return (o->r2 / dot(x, x)) * x;

@@ -25,8 +25,9 @@ LG_DEV void lg_set_sersic(lg_data_sersic* o, float x, float y, float r, float ma
                         : 0.01945f - 0.8902f * n + 10.95f * (n * n) - 19.67f * (n * n * n) + 13.43f * (n * n * n * n);
     lg_sersic_setup(o, x, y, r, mag, n, q, a, b);
 }
-LG_DEV float lg_brightness_sersic(const lg_data_sersic* __restrict__ o, float2 x)
+template <class V>
+LG_DEV LG_SCALAR(V) lg_brightness_sersic(const lg_data_sersic* __restrict__ o, V x)
 {
-    float2 y = mv22(o->t, x - o->x);
+    V y = mv22(o->t, x - o->x);
     return expf(o->log0 - expf(o->log1 + o->m * logf(dot(y, y))));
 }

@@ -7,7 +7,8 @@ LG_DEV void lg_set_sersic_old(lg_data_sersic_old* o, float x, float y, float r, 
 {
     lg_sersic_setup(o, x, y, r, mag, n, q, a, 1.9992f * n - 0.3271f);
 }
-LG_DEV float lg_brightness_sersic_old(const lg_data_sersic_old* __restrict__ o, float2 x)
+template <class V>
+LG_DEV LG_SCALAR(V) lg_brightness_sersic_old(const lg_data_sersic_old* __restrict__ o, V x)
 {
     return lg_brightness_sersic(o, x);
 }

@@ -18,11 +18,13 @@ LG_DEV void lg_set_sie_plus_shear(lg_data_sie_plus_shear* o, float x, float y, f
     o->e = sqrtf(1 - q * q);
     o->d = r * sqrtf(q) / sqrtf(1 - q * q);
 }
-LG_DEV float2 lg_deflection_sie_plus_shear(const lg_data_sie_plus_shear* __restrict__ o, float2 x)
+template <class V>
+LG_DEV V lg_deflection_sie_plus_shear(const lg_data_sie_plus_shear* __restrict__ o, V x)
 {
+    typedef LG_SCALAR(V) T;
     x -= o->x;
-    float2 y = mv22(o->m, x);
-    float r = o->e / sqrtf(o->q2 * y.x * y.x + y.y * y.y);
-    y = o->d * make_float2(atanf(y.x * r), atanhf(y.y * r));
+    V y = mv22(o->m, x);
+    T r = o->e / sqrtf(o->q2 * y.x * y.x + y.y * y.y);
+    y = o->d * V{atanf(y.x * r), atanhf(y.y * r)};
     return mv22(o->w, y) + mv22(o->g, x);
 }

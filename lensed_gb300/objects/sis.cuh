@@ -9,7 +9,8 @@ LG_DEV void lg_set_sis(lg_data_sis* o, float x, float y, float r)
     o->x = make_float2(x, y);
     o->r = r;
 }
-LG_DEV float2 lg_deflection_sis(const lg_data_sis* __restrict__ o, float2 x)
+template <class V>
+LG_DEV V lg_deflection_sis(const lg_data_sis* __restrict__ o, V x)
 {
     return o->r * normalize(x - o->x);
 }

@@ -11,7 +11,8 @@ LG_DEV void lg_set_sis_plus_shear(lg_data_sis_plus_shear* o, float x, float y, f
     o->r = r;
     o->g = make_mat22(g1, g2, g2, -g1);
 }
-LG_DEV float2 lg_deflection_sis_plus_shear(const lg_data_sis_plus_shear* __restrict__ o, float2 x)
+template <class V>
+LG_DEV V lg_deflection_sis_plus_shear(const lg_data_sis_plus_shear* __restrict__ o, V x)
 {
     x -= o->x;
     return o->r * normalize(x) + mv22(o->g, x);

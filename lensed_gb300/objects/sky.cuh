@@ -10,7 +10,8 @@ LG_DEV void lg_set_sky(lg_data_sky* o, float bg, float dx, float dy)
     o->bg = bg;
     o->grad = make_float2(dx, dy);
 }
-LG_DEV float lg_foreground_sky(const lg_data_sky* __restrict__ o, float2 x)
+template <class V>
+LG_DEV LG_SCALAR(V) lg_foreground_sky(const lg_data_sky* __restrict__ o, V x)
 {
     return o->bg + dot(o->grad, x - make_float2(1, 1));
 }

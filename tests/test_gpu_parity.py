@@ -221,6 +221,32 @@ def test_batch_equals_single_and_is_deterministic(native):
     assert np.array_equal(rev[::-1], a)
 
 
+def test_device_entry_points_wait_for_the_legacy_stream(native):
+    """Device buffers that a framework writes with kernels queued on the
+    legacy default stream (PyTorch's default) are touched only after those
+    kernels when the call runs on the context's stream: the profile and the
+    NULL-stream device entry point agree with the host path, and the fill of
+    the logL buffer does not land after the library's results."""
+    torch = pytest.importorskip("torch")
+    s = workloads.config2()
+    B = 1024
+    ctx = lg.Context(s.image, s.weight, s.objects, psf=s.psf, rule=s.rule, max_batch=B)
+    cand = ctx.to_map_order(workloads.draw_candidates(s, B, seed=7))
+    want = ctx.eval_batch(cand)
+    torch.cuda.synchronize()
+    assert cand.flags["C_CONTIGUOUS"]
+    d_params = torch.tensor(cand, dtype=torch.float64, device="cuda")
+    d_logL = torch.full((B,), 7.0, dtype=torch.float64, device="cuda")
+    ctx.profile(d_params.data_ptr(), B, d_logL.data_ptr())
+    assert np.array_equal(d_logL.cpu().numpy(), want)
+    d_params2 = torch.tensor(cand[::-1].copy(), dtype=torch.float64, device="cuda")
+    d_logL2 = torch.full((B,), 7.0, dtype=torch.float64, device="cuda")
+    ctx.eval_batch_device(d_params2.data_ptr(), B, d_logL2.data_ptr())
+    torch.cuda.synchronize()
+    ctx.eval_batch(cand[:1])  # synchronises the context's stream
+    assert np.array_equal(d_logL2.cpu().numpy(), want[::-1])
+
+
 def test_graph_and_direct_launch_agree(native):
     s = workloads.small()
     cand = workloads.draw_candidates(s, 32, seed=4)

@@ -87,6 +87,7 @@ def test_cube_device_entry_point(native):
     d_phys = torch.empty((64, ctx.npars), dtype=torch.float64, device="cuda")
     d_logL = torch.empty(64, dtype=torch.float64, device="cuda")
     s = torch.cuda.Stream()
+    s.wait_stream(torch.cuda.current_stream())  # the inputs were written on the current stream
     ctx.eval_cube_device(d_cube.data_ptr(), 64, d_phys.data_ptr(), d_logL.data_ptr(), s.cuda_stream)
     s.synchronize()
     ll, phys = d_logL.cpu().numpy(), d_phys.cpu().numpy()
