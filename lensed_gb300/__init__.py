@@ -119,6 +119,7 @@ def lib():
                                            C.c_size_t, C.POINTER(C.c_size_t)]),
         "lg_eval_profile": (C.c_int, [vp, vp, C.c_int, vp, fp]),
         "lg_measure_fp32_peak": (C.c_int, [C.c_int, dp]),
+        "lg_probe_pair_math": (C.c_int, [C.c_int, C.c_int, fp, C.c_int, fp]),
         "lg_loglike_images_noalloc": (C.c_int, [vp, vp, vp, C.c_long, C.c_int, vp, vp]),
         "lg_systems_create": (vp, [C.POINTER(_ImageDesc), C.c_int, C.POINTER(_ObjectDesc), C.c_int,
                                    C.POINTER(_Options), ip, ip]),

@@ -201,15 +201,60 @@ LG_DEV lg_pair2 mv22(lg_pair_mat22 m, lg_pair2 v) { return {m.a * v.x + m.b * v.
 LG_DEV lg_pair2 lg_pair2_join(float2 r0, float2 r1) { return {lg_pair_of(r0.x, r1.x), lg_pair_of(r0.y, r1.y)}; }
 LG_DEV float2 lg_lane(lg_pair2 a, int i) { return i ? make_float2(a.x.v.y, a.y.v.y) : make_float2(a.x.v.x, a.y.v.x); }
 
-// elementary functions, lane by lane (the module's single-precision library)
+// SFU approximations (PTX ex2.approx / lg2.approx, subnormals flushed)
+LG_DEV float lg_sfu_ex2(float x)
+{
+    float r;
+    asm("ex2.approx.ftz.f32 %0, %1;" : "=f"(r) : "f"(x));
+    return r;
+}
+LG_DEV float lg_sfu_lg2(float x)
+{
+    float r;
+    asm("lg2.approx.ftz.f32 %0, %1;" : "=f"(r) : "f"(x));
+    return r;
+}
+
+// e^x for two rays: 2^t * 2^c with t = fl(x log2(e)) and c the rest of
+// x log2(e) (the product's rounding error, exact through an fma, plus x
+// times the rounding error of the constant); 2^t from the SFU, 2^c as
+// 1 + c ln 2 (|c| <= 2^-24 |t|).  Within the SFU's few-ulp error of e^x;
+// results below 2^-126 are flushed to zero; for |t| >= 128 (where 2^t is 0
+// or overflows, and for infinite x) and NaN x the result is 2^t itself.
+LG_DEV float lg_exp_pick(float t, float p, float r) { return fabsf(t) < 128.0f ? r : p; }
+LG_DEV lg_pair expf(lg_pair x)
+{
+    const float2 L = lg_bc(0x1.715476p+0f), Llo = lg_bc(0x1.4ae0c0p-26f);
+    const float2 t = __fmul2_rn(x.v, L);
+    const float2 c = __ffma2_rn(x.v, Llo, __ffma2_rn(x.v, L, lg_neg2(t)));
+    const float2 p = make_float2(lg_sfu_ex2(t.x), lg_sfu_ex2(t.y));
+    const float2 r = __ffma2_rn(p, __fmul2_rn(c, lg_bc(0x1.62e430p-1f)), p);
+    return {make_float2(lg_exp_pick(t.x, p.x, r.x), lg_exp_pick(t.y, p.y, r.y))};
+}
+LG_DEV lg_pair expf(lg_pair_prod x) { return expf(lg_pair(x)); }
+
+// ln x for two rays: y ln 2 + (x 2^-y - 1) with y = lg2(x) from the SFU; the
+// second term removes the error of y to first order, leaving an absolute
+// error of about 2^-22 (the SFU's 2^-y).  Outside |y| < 120 (where 2^-y
+// would leave the normal range), and for zero, infinite, negative or NaN x,
+// the result is y ln 2 (subnormal x is flushed: -inf).
+LG_DEV lg_pair logf(lg_pair x)
+{
+    const float2 y = make_float2(lg_sfu_lg2(x.v.x), lg_sfu_lg2(x.v.y));
+    const float2 s = make_float2(lg_sfu_ex2(-y.x), lg_sfu_ex2(-y.y));
+    const float2 u = __fmul2_rn(y, lg_bc(0x1.62e430p-1f));
+    const float2 r = __ffma2_rn(y, lg_bc(0x1.62e430p-1f), __ffma2_rn(x.v, s, lg_bc(-1.0f)));
+    return {make_float2(fabsf(y.x) < 120.0f ? r.x : u.x, fabsf(y.y) < 120.0f ? r.y : u.y)};
+}
+LG_DEV lg_pair logf(lg_pair_prod x) { return logf(lg_pair(x)); }
+
+// other elementary functions, lane by lane (the module's float library)
 #define LG_PAIR_FN1(fn) \
     LG_DEV lg_pair fn(lg_pair a) { return {make_float2(fn(a.v.x), fn(a.v.y))}; } \
     LG_DEV lg_pair fn(lg_pair_prod a) { return fn(lg_pair(a)); }
 LG_PAIR_FN1(sqrtf)
 LG_PAIR_FN1(rsqrtf)
-LG_PAIR_FN1(expf)
 LG_PAIR_FN1(exp2f)
-LG_PAIR_FN1(logf)
 LG_PAIR_FN1(log2f)
 LG_PAIR_FN1(sinf)
 LG_PAIR_FN1(cosf)
