@@ -161,10 +161,30 @@ LG_DEV lg_pair operator-(lg_pair c, lg_pair_prod p) { return {__ffma2_rn(lg_neg2
 LG_DEV lg_pair operator-(lg_pair_prod p, float c) { return {__ffma2_rn(p.a, p.b, lg_bc(-c))}; }
 LG_DEV lg_pair operator-(float c, lg_pair_prod p) { return {__ffma2_rn(lg_neg2(p.a), p.b, lg_bc(c))}; }
 LG_DEV lg_pair operator-(lg_pair_prod p, lg_pair_prod q) { return {__ffma2_rn(p.a, p.b, lg_neg2(__fmul2_rn(q.a, q.b)))}; }
-// quotients, lane by lane (the module's division)
-LG_DEV lg_pair operator/(lg_pair a, lg_pair b) { return {make_float2(a.v.x / b.v.x, a.v.y / b.v.y)}; }
-LG_DEV lg_pair operator/(lg_pair a, float b) { return {make_float2(a.v.x / b, a.v.y / b)}; }
-LG_DEV lg_pair operator/(float a, lg_pair b) { return {make_float2(a / b.v.x, a / b.v.y)}; }
+// quotients: a times the SFU reciprocal of b (PTX rcp.approx, the
+// definition of div.approx: within 2 ulp for 2^-126 <= |b| <= 2^126)
+LG_DEV float lg_sfu_rcp(float x)
+{
+    float r;
+    asm("rcp.approx.ftz.f32 %0, %1;" : "=f"(r) : "f"(x));
+    return r;
+}
+LG_DEV float lg_sfu_sqrt(float x)
+{
+    float r;
+    asm("sqrt.approx.ftz.f32 %0, %1;" : "=f"(r) : "f"(x));
+    return r;
+}
+LG_DEV float lg_sfu_rsqrt(float x)
+{
+    float r;
+    asm("rsqrt.approx.ftz.f32 %0, %1;" : "=f"(r) : "f"(x));
+    return r;
+}
+LG_DEV lg_pair lg_rcp(lg_pair b) { return {make_float2(lg_sfu_rcp(b.v.x), lg_sfu_rcp(b.v.y))}; }
+LG_DEV lg_pair operator/(lg_pair a, lg_pair b) { return {__fmul2_rn(a.v, lg_rcp(b).v)}; }
+LG_DEV lg_pair operator/(lg_pair a, float b) { return {__fmul2_rn(a.v, lg_bc(lg_sfu_rcp(b)))}; }
+LG_DEV lg_pair operator/(float a, lg_pair b) { return {__fmul2_rn(lg_bc(a), lg_rcp(b).v)}; }
 LG_DEV lg_pair operator/(lg_pair_prod a, lg_pair b) { return lg_pair(a) / b; }
 LG_DEV lg_pair operator/(lg_pair_prod a, float b) { return lg_pair(a) / b; }
 LG_DEV lg_pair operator/(lg_pair a, lg_pair_prod b) { return a / lg_pair(b); }
@@ -252,8 +272,12 @@ LG_DEV lg_pair logf(lg_pair_prod x) { return logf(lg_pair(x)); }
 #define LG_PAIR_FN1(fn) \
     LG_DEV lg_pair fn(lg_pair a) { return {make_float2(fn(a.v.x), fn(a.v.y))}; } \
     LG_DEV lg_pair fn(lg_pair_prod a) { return fn(lg_pair(a)); }
-LG_PAIR_FN1(sqrtf)
-LG_PAIR_FN1(rsqrtf)
+// square root and its reciprocal from the SFU (PTX sqrt.approx /
+// rsqrt.approx, within 1 ulp; subnormal inputs flushed)
+LG_DEV lg_pair sqrtf(lg_pair a) { return {make_float2(lg_sfu_sqrt(a.v.x), lg_sfu_sqrt(a.v.y))}; }
+LG_DEV lg_pair sqrtf(lg_pair_prod a) { return sqrtf(lg_pair(a)); }
+LG_DEV lg_pair rsqrtf(lg_pair a) { return {make_float2(lg_sfu_rsqrt(a.v.x), lg_sfu_rsqrt(a.v.y))}; }
+LG_DEV lg_pair rsqrtf(lg_pair_prod a) { return rsqrtf(lg_pair(a)); }
 LG_PAIR_FN1(exp2f)
 LG_PAIR_FN1(log2f)
 LG_PAIR_FN1(sinf)

@@ -1,11 +1,13 @@
-"""Accuracy of the paired-ray exp and log of the fast evaluation modules
-(SFU ex2/lg2 with a first-order correction) against double precision.
+"""Accuracy of the paired-ray exp, log, square root and reciprocal of the
+fast evaluation modules (SFU ex2/lg2 with a first-order correction; SFU
+sqrt and rcp) against double precision.
 
 Bounds, for results in the normal float range:
 * exp: relative error <= 4 ulp (2^-21), the class of CUDA's expf (2 ulp)
   plus the SFU's own approximation error;
 * log: absolute error <= 3e-7 or relative error <= 4 ulp, whichever is
   larger (the correction leaves an absolute error of about 2^-22);
+* sqrt and 1/x: relative error <= 2^-22 (x normal; 1/x for |x| <= 2^126);
 * special values: exp(-inf) = 0, exp(+inf) = exp(overflowing x) = inf,
   exp(NaN) = NaN, results below 2^-126 flushed to 0; log(0) = -inf,
   log(inf) = inf, log(negative) = NaN, log of huge finite x still accurate.
@@ -62,3 +64,18 @@ def test_special_values(native):
     assert np.isneginf(lo[0]) and np.isposinf(lo[1]) and np.isnan(lo[2]) and np.isnan(lo[3])
     assert abs(lo[4] - np.log(3.4e38)) < 1e-5 * np.log(3.4e38)
     assert abs(lo[5] - np.log(2e-38)) < 1e-5 * abs(np.log(2e-38))
+
+
+def test_sqrt_and_reciprocal(native):
+    rng = np.random.default_rng(3)
+    x = np.concatenate([np.exp(rng.uniform(-87, 87, 300000)), rng.uniform(0.25, 4, 100000)]).astype(np.float32)
+    for fn, ref in ((2, np.sqrt), (3, lambda v: 1.0 / v)):
+        got = run(fn, x).astype(np.float64)
+        want = ref(x.astype(np.float64))
+        rel = np.abs(got - want) / want
+        print(f"fn {fn}: max rel error {rel.max():.3g}")
+        assert rel.max() <= 2.0**-22
+    s = run(2, [0.0, np.inf, -1.0, np.nan])
+    assert s[0] == 0 and np.isposinf(s[1]) and np.isnan(s[2]) and np.isnan(s[3])
+    r = run(3, [0.0, np.inf, -2.0])
+    assert np.isposinf(r[0]) and r[1] == 0 and r[2] == -0.5
