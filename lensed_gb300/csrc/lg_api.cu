@@ -155,8 +155,8 @@ struct lg_ctx {
             if ((rc = launch(f_rraw, dim3(rtiles, B), dim3(shape.rt), 0, s, a_r, "render")) || (rc = mark(2)))
                 return rc;
             void* a_c[] = {&d_raw, &d_image, &d_weight, &d_partials};
-            if ((rc = launch(f_cchi2, dim3(ctiles_x, ctiles_y, B), dim3(shape.ctx / shape.cr, shape.cty), csmem, s,
-                             a_c, "convolve")) ||
+            if ((rc = launch(f_cchi2, dim3(ctiles_x, ctiles_y, B), dim3(shape.ctx / shape.cr, shape.conv_block_y()),
+                             csmem, s, a_c, "convolve")) ||
                 (rc = mark(3)))
                 return rc;
             void* a_f[] = {&d_partials, &ctiles, &logL};
@@ -211,10 +211,16 @@ namespace {
 
 // Launch shape for a model (tile sizes chosen for GB300; see the design
 // notes for the measurements behind them).
-lg::Shape choose_shape(const lg::Model& m)
+lg::Shape choose_shape(const lg::Model& m, bool strict)
 {
     lg::Shape s;
-    if (!m.psf.empty() && m.psfw + 8 > 64) s.cr = 8;
+    // fast mode: 32 x 64 convolution tiles, each thread two rows (paired);
+    // the register window of a thread holds 2 (8 + PSF width - 1) floats,
+    // so PSFs wider than 49 pixels keep the single-row kernel
+    if (!m.psf.empty() && !strict && m.psfw <= 49) {
+        s.cty = 64;
+        s.pair_rows = true;
+    }
     return s;
 }
 
@@ -224,15 +230,11 @@ void shape_sizes(const lg::Shape& s, const lg::Model& m, lg_ctx* c)
     const int rtile = s.rt * s.rppt;
     c->rtiles = (int)((N + rtile - 1) / rtile);
     if (!m.psf.empty()) {
-        const int win4 = (s.cr + m.psfw - 1 + 3) / 4 * 4;
-        const int need = s.ctx - s.cr + win4;
-        const int twp = ((need + 27) / 32) * 32 + 4;
-        const int th = s.cty + m.psfh - 1;
-        c->cthreads = (s.ctx / s.cr) * s.cty;
+        // the shared-memory size is read back from the compiled module
+        c->cthreads = (s.ctx / s.cr) * s.conv_block_y();
         c->ctiles_x = (m.width + s.ctx - 1) / s.ctx;
         c->ctiles_y = (m.height + s.cty - 1) / s.cty;
         c->ctiles = c->ctiles_x * c->ctiles_y;
-        c->csmem = th * twp * 4;
     }
 }
 
@@ -319,9 +321,9 @@ int create_impl(lg_ctx* c, const lg_image_desc* img, const lg_object_desc* objs,
 
     // compose and compile the programs (the reference's clBuildProgram,
     // src/lensed.c:706-776)
-    c->shape = choose_shape(m);
-    shape_sizes(c->shape, m, c);
     const bool strict = (c->flags & LG_FLAG_STRICT_FP) != 0;
+    c->shape = choose_shape(m, strict);
+    shape_sizes(c->shape, m, c);
     std::string log;
     std::vector<char> cubin, cubin_set;
     // fast mode: hardware-approximate division and square root per ray
@@ -359,6 +361,16 @@ int create_impl(lg_ctx* c, const lg_image_desc* img, const lg_object_desc* objs,
     unsigned mb = 0;
     if ((rc = c->cuda(cudaMemcpy(&mb, (void*)gp, sizeof mb, cudaMemcpyDeviceToHost), "model size"))) return rc;
     c->model_bytes = mb;
+    if (c->psf) {
+        int csm = 0, cth = 0;
+        if ((rc = c->drvcall(c->drv->moduleGetGlobal(&gp, &gb, c->mod, "lg_conv_smem"), "lg_conv_smem")) ||
+            (rc = c->cuda(cudaMemcpy(&csm, (void*)gp, sizeof csm, cudaMemcpyDeviceToHost), "conv smem")) ||
+            (rc = c->drvcall(c->drv->moduleGetGlobal(&gp, &gb, c->mod, "lg_conv_threads"), "lg_conv_threads")) ||
+            (rc = c->cuda(cudaMemcpy(&cth, (void*)gp, sizeof cth, cudaMemcpyDeviceToHost), "conv threads")))
+            return rc;
+        if (cth != c->cthreads) return c->fail(LG_ERR_COMPILE, "convolution block size mismatch");
+        c->csmem = csm;
+    }
     if (c->psf && c->csmem > 48 * 1024)
         if ((rc = c->drvcall(c->drv->funcSetAttribute(c->f_cchi2, CU_FUNC_ATTRIBUTE_MAX_DYNAMIC_SHARED_SIZE_BYTES,
                                                       c->csmem),
@@ -633,8 +645,8 @@ int lg_compile_check(const lg_image_desc* image, const lg_object_desc* objs, int
     if (!rc) {
         const bool strict = opts && (opts->flags & LG_FLAG_STRICT_FP);
         std::vector<char> cubin;
-        lg::Shape s = choose_shape(m);
-        const bool ieee = strict || (opts->flags & LG_FLAG_IEEE_DIV);
+        lg::Shape s = choose_shape(m, strict);
+        const bool ieee = strict || (opts && (opts->flags & LG_FLAG_IEEE_DIV));
         rc = lg::compile_program(lg::compose_source(m, s, strict, lg::Part::EVAL), !strict, cubin, err, ieee);
         if (!rc) rc = lg::compile_program(lg::compose_source(m, s, strict, lg::Part::SET), false, cubin, err);
     }
@@ -789,7 +801,8 @@ int render_device(lg_ctx* c, const double* params, const float** d_model)
     if ((rc = c->launch(c->f_rdump, dim3(c->rtiles, 1), dim3(c->shape.rt), 0, c->stream, a_r, "render"))) return rc;
     if (c->psf) {
         void* a_c[] = {&d_val, &c->d_raw};
-        if ((rc = c->launch(c->f_cdump, dim3(c->ctiles_x, c->ctiles_y, 1), dim3(c->shape.ctx / c->shape.cr, c->shape.cty),
+        if ((rc = c->launch(c->f_cdump, dim3(c->ctiles_x, c->ctiles_y, 1),
+                            dim3(c->shape.ctx / c->shape.cr, c->shape.conv_block_y()),
                             c->csmem, c->stream, a_c, "convolve")))
             return rc;
     }

@@ -127,6 +127,8 @@ int build_model(const lg_image_desc* img, const lg_object_desc* objs, int nobjs,
 struct Shape {
     int rt = 128, rppt = 2;        // render threads / pixels per thread
     int ctx = 32, cty = 32, cr = 8; // convolution tile and outputs per thread
+    bool pair_rows = false;        // convolution threads own two rows (f32x2)
+    int conv_block_y() const { return pair_rows ? cty / 2 : cty; }
 };
 
 // Compose the NVRTC sources of a model and compile them to cubins for

@@ -140,6 +140,7 @@ int create_systems(lg_systems* S, const lg_image_desc* images, int nsys, const l
 
     // static layout: images, PSFs, raw models and partials by capacity
     const lg::Shape& sh = S->shape;
+    const bool strict_fp = (S->flags & LG_FLAG_STRICT_FP) != 0;
     std::set<std::pair<int, int>> shapes;
     long long img = 0, raw = 0, part = 0;
     int psf_off = 0, csmem = 0;
@@ -152,8 +153,12 @@ int create_systems(lg_systems* S, const lg_image_desc* images, int nsys, const l
         I.pw = m.psfw;
         I.ph = m.psfh;
         I.rtiles = (I.N + sh.rt * sh.rppt - 1) / (sh.rt * sh.rppt);
+        // fast mode, PSF up to 49 wide: paired-row units of 2 * cty rows, as
+        // the single-system context tiles them
+        const bool paired = S->psf && !strict_fp && m.psfw <= 49;
+        const int cty = paired ? 2 * sh.cty : sh.cty;
         I.ctiles_x = (I.W + sh.ctx - 1) / sh.ctx;
-        I.ctiles_y = (I.H + sh.cty - 1) / sh.cty;
+        I.ctiles_y = (I.H + cty - 1) / cty;
         I.ctiles = I.ctiles_x * I.ctiles_y;
         I.psf_off = psf_off;
         double rx = m.pcs[0], ry = m.pcs[1];
@@ -161,9 +166,19 @@ int create_systems(lg_systems* S, const lg_image_desc* images, int nsys, const l
             if (m.psfw % 2 == 0) rx += 0.5;  // src/lensed.c:884-891
             if (m.psfh % 2 == 0) ry += 0.5;
             shapes.insert({m.psfw, m.psfh});
-            const int win4 = (sh.cr + m.psfw - 1 + 3) / 4 * 4;
-            const int twp = ((sh.ctx - sh.cr + win4 + 27) / 32) * 32 + 4;
-            csmem = std::max(csmem, ((sh.cty + m.psfh - 1) * twp + m.psfw * m.psfh) * 4);
+            if (paired) {
+                // layout of lg_multi_conv_unit_pair: row pairs, pair column c at
+                // float 2c + 4 floor(c/8), pitch 16 (mod 32) words
+                const int cwin = (sh.cr + m.psfw - 1 + 1) / 2 * 2;
+                const int cnc = sh.ctx - sh.cr + cwin;
+                const int croww = 2 * (cnc - 1) + 4 * ((cnc - 1) / 8) + 2;
+                const int cp = (croww - 16 + 31) / 32 * 32 + 16;
+                csmem = std::max(csmem, ((sh.cty + m.psfh - 1) * cp + m.psfw * m.psfh) * 4);
+            } else {
+                const int win4 = (sh.cr + m.psfw - 1 + 3) / 4 * 4;
+                const int twp = ((sh.ctx - sh.cr + win4 + 27) / 32) * 32 + 4;
+                csmem = std::max(csmem, ((sh.cty + m.psfh - 1) * twp + m.psfw * m.psfh) * 4);
+            }
             psf_off += m.psfw * m.psfh;
         }
         I.rx = (float)rx;
@@ -181,7 +196,7 @@ int create_systems(lg_systems* S, const lg_image_desc* images, int nsys, const l
     S->csmem = csmem;
 
     // programs
-    const bool strict = (S->flags & LG_FLAG_STRICT_FP) != 0;
+    const bool strict = strict_fp;
     const bool ieee = strict || (S->flags & LG_FLAG_IEEE_DIV);
     std::vector<std::pair<int, int>> shape_list(shapes.begin(), shapes.end());
     std::vector<char> cubin, cubin_set;

@@ -181,6 +181,110 @@ extern "C" __global__ void __launch_bounds__(LG_RT)
 #endif
 #define LG_OX (LG_PSF_W - 1 - LG_PSF_W / 2)
 #define LG_OY (LG_PSF_H - 1 - LG_PSF_H / 2)
+#define LG_CTILES_X ((LG_W + LG_CTX - 1) / LG_CTX)
+#define LG_CTILES_Y ((LG_H + LG_CTY - 1) / LG_CTY)
+#define LG_CTILES (LG_CTILES_X * LG_CTILES_Y)
+
+// chi^2 of a thread's outputs (MODE 1) or their store (MODE 0)
+template <int MODE>
+LG_DEV double lg_conv_out(int b, int gy, int gx0, const float* acc, float* __restrict__ out,
+                          const float* __restrict__ image, const float* __restrict__ weight)
+{
+    double s = 0.0;
+    if (gy < LG_H) {
+#pragma unroll
+        for (int o = 0; o < LG_CR; ++o) {
+            const int gx = gx0 + o;
+            if (gx < LG_W) {
+                const int k = gy * LG_W + gx;
+                if (MODE == 1) {
+                    const float d = acc[o] - image[k];
+                    s += (double)(weight[k] * d * d);
+                } else {
+                    out[(size_t)b * LG_N + k] = acc[o];
+                }
+            }
+        }
+    }
+    return s;
+}
+
+#if defined(LG_PAIRED) && LG_PSF_W <= 49
+// Paired rows (fast mode, PSFs up to 49 pixels wide): a thread computes LG_CR columns of two output
+// rows, y and y + LG_CTY/2, with f32x2 fmas, every lane in the scalar
+// kernel's order.  The halo tile holds each input row together with the row
+// LG_CTY/2 below it as float2 pairs; pair column c of a row sits at float
+// offset 2c + 4 floor(c/8) and the row pitch is 16 (mod 32) words, so the
+// float4 loads of a quarter warp (four column groups of two rows) fall in
+// distinct banks.
+#define LG_CD (LG_CTY / 2)
+#define LG_CWIN ((LG_CR + LG_PSF_W - 1 + 1) / 2 * 2)
+#define LG_CNC (LG_CTX - LG_CR + LG_CWIN)
+#define LG_CCOL(c) (2 * (c) + 4 * ((c) / 8))
+#define LG_CROWW (LG_CCOL(LG_CNC - 1) + 2)
+#define LG_CP ((LG_CROWW - 16 + 31) / 32 * 32 + 16)
+#define LG_CNR (LG_CD + LG_PSF_H - 1)
+#define LG_CTHREADS ((LG_CTX / LG_CR) * LG_CD)
+#define LG_CSMEM (LG_CNR * LG_CP * 4)
+static_assert(LG_CR % 8 == 0 && LG_CTY % 2 == 0, "paired convolution layout");
+
+template <int MODE>
+LG_DEV void lg_conv_tile(const float* __restrict__ raw, float* __restrict__ out, const float* __restrict__ image,
+                         const float* __restrict__ weight, double* __restrict__ partials)
+{
+    extern __shared__ float4 lg_smem4[];
+    float* tile = reinterpret_cast<float*>(lg_smem4);
+    const int b = blockIdx.z;
+    const float* src = raw + (size_t)b * LG_N;
+    const int X0 = blockIdx.x * LG_CTX, Y0 = blockIdx.y * LG_CTY;
+    const int br = Y0 + LG_OY - (LG_PSF_H - 1), bc = X0 + LG_OX - (LG_PSF_W - 1);
+    const int tid = threadIdx.y * blockDim.x + threadIdx.x;
+    for (int i = tid; i < LG_CNR * LG_CNC; i += LG_CTHREADS) {
+        const int r = i / LG_CNC, c = i - r * LG_CNC;
+        int gy0 = br + r, gy1 = br + r + LG_CD, gx = bc + c;
+        gy0 = gy0 < 0 ? 0 : (gy0 > LG_H - 1 ? LG_H - 1 : gy0);
+        gy1 = gy1 < 0 ? 0 : (gy1 > LG_H - 1 ? LG_H - 1 : gy1);
+        gx = gx < 0 ? 0 : (gx > LG_W - 1 ? LG_W - 1 : gx);
+        *reinterpret_cast<float2*>(tile + r * LG_CP + LG_CCOL(c)) = make_float2(src[gy0 * LG_W + gx], src[gy1 * LG_W + gx]);
+    }
+    __syncthreads();
+    const int lx0 = threadIdx.x * LG_CR, ly = threadIdx.y;
+    float2 acc[LG_CR];
+#pragma unroll
+    for (int o = 0; o < LG_CR; ++o) acc[o] = make_float2(0.0f, 0.0f);
+#pragma unroll 1
+    for (int j = 0; j < LG_PSF_H; ++j) {
+        const float* row = tile + (ly + LG_PSF_H - 1 - j) * LG_CP + LG_CCOL(lx0);
+        float2 win[LG_CWIN];
+#pragma unroll
+        for (int t = 0; t < LG_CWIN / 2; ++t) {
+            const float4 q = *reinterpret_cast<const float4*>(row + 4 * t + 4 * (t / 4));
+            win[2 * t] = make_float2(q.x, q.y);
+            win[2 * t + 1] = make_float2(q.z, q.w);
+        }
+        const float* prow = lg_psf + j * LG_PSF_W;
+#pragma unroll
+        for (int i = 0; i < LG_PSF_W; ++i) {
+            const float2 p = make_float2(prow[i], prow[i]);
+#pragma unroll
+            for (int o = 0; o < LG_CR; ++o) acc[o] = __ffma2_rn(p, win[o + LG_PSF_W - 1 - i], acc[o]);
+        }
+    }
+    float a0[LG_CR], a1[LG_CR];
+#pragma unroll
+    for (int o = 0; o < LG_CR; ++o) {
+        a0[o] = acc[o].x;
+        a1[o] = acc[o].y;
+    }
+    double s = lg_conv_out<MODE>(b, Y0 + ly, X0 + lx0, a0, out, image, weight);
+    s += lg_conv_out<MODE>(b, Y0 + ly + LG_CD, X0 + lx0, a1, out, image, weight);
+    if (MODE == 1) {
+        __shared__ double red[LG_CTHREADS / 32];
+        s = lg_block_sum<LG_CTHREADS>(s, red);
+        if (tid == 0) partials[(size_t)b * LG_CTILES + blockIdx.y * LG_CTILES_X + blockIdx.x] = s;
+    }
+}
+#else
 #define LG_WIN4 ((LG_CR + LG_PSF_W - 1 + 3) / 4 * 4)
 #define LG_TW_NEED (LG_CTX - LG_CR + LG_WIN4)
 // row pitch = 4 (mod 32) words: the float4 loads of a quarter warp (two
@@ -188,9 +292,6 @@ extern "C" __global__ void __launch_bounds__(LG_RT)
 #define LG_TWP (((LG_TW_NEED + 27) / 32) * 32 + 4)
 #define LG_TH (LG_CTY + LG_PSF_H - 1)
 #define LG_CTHREADS ((LG_CTX / LG_CR) * LG_CTY)
-#define LG_CTILES_X ((LG_W + LG_CTX - 1) / LG_CTX)
-#define LG_CTILES_Y ((LG_H + LG_CTY - 1) / LG_CTY)
-#define LG_CTILES (LG_CTILES_X * LG_CTILES_Y)
 #define LG_CSMEM (LG_TH * LG_TWP * 4)
 
 template <int MODE>
@@ -236,31 +337,14 @@ LG_DEV void lg_conv_tile(const float* __restrict__ raw, float* __restrict__ out,
             for (int o = 0; o < LG_CR; ++o) acc[o] += p * win[o + LG_PSF_W - 1 - i];
         }
     }
-    const int gy = Y0 + ly;
+    double s = lg_conv_out<MODE>(b, Y0 + ly, X0 + lx0, acc, out, image, weight);
     if (MODE == 1) {
         __shared__ double red[LG_CTHREADS / 32];
-        double s = 0.0;
-        if (gy < LG_H) {
-#pragma unroll
-            for (int o = 0; o < LG_CR; ++o) {
-                const int gx = X0 + lx0 + o;
-                if (gx < LG_W) {
-                    const int k = gy * LG_W + gx;
-                    const float d = acc[o] - image[k];
-                    s += (double)(weight[k] * d * d);
-                }
-            }
-        }
         s = lg_block_sum<LG_CTHREADS>(s, red);
         if (tid == 0) partials[(size_t)b * LG_CTILES + blockIdx.y * LG_CTILES_X + blockIdx.x] = s;
-    } else if (gy < LG_H) {
-#pragma unroll
-        for (int o = 0; o < LG_CR; ++o) {
-            const int gx = X0 + lx0 + o;
-            if (gx < LG_W) out[(size_t)b * LG_N + gy * LG_W + gx] = acc[o];
-        }
     }
 }
+#endif
 
 extern "C" __global__ void __launch_bounds__(LG_CTHREADS)
     lg_conv_chi2(const float* __restrict__ raw, const float* __restrict__ image, const float* __restrict__ weight,

@@ -240,6 +240,85 @@ LG_DEV double lg_multi_conv_unit(const float* __restrict__ src, const float* __r
     return s;
 }
 
+#if defined(LG_PAIRED)
+// The paired-row unit of the fast mode for PSFs up to 49 pixels wide: a
+// 32 x (2 LG_CTY) output tile, each thread LG_CR columns of rows y and
+// y + LG_CTY, in the layout, order and partial-sum grouping of the
+// single-system kernel (so each system's logL is identical to its own
+// context's).
+template <int PW, int PH>
+LG_DEV double lg_multi_conv_unit_pair(const float* __restrict__ src, const float* __restrict__ psf_g, int W, int H,
+                                      int X0, int Y0, const float* __restrict__ image,
+                                      const float* __restrict__ weight, float* smem)
+{
+    constexpr int OX = PW - 1 - PW / 2, OY = PH - 1 - PH / 2;
+    constexpr int CD = LG_CTY;
+    constexpr int CWIN = (LG_CR + PW - 1 + 1) / 2 * 2;
+    constexpr int CNC = LG_CTX - LG_CR + CWIN;
+    constexpr int CROWW = 2 * (CNC - 1) + 4 * ((CNC - 1) / 8) + 2;
+    constexpr int CP = (CROWW - 16 + 31) / 32 * 32 + 16;
+    constexpr int CNR = CD + PH - 1;
+    static_assert(LG_CR % 8 == 0, "paired convolution layout");
+    float* tile = smem;
+    float* psf = smem + CNR * CP;
+    const int tid = threadIdx.y * blockDim.x + threadIdx.x;
+    const int br = Y0 + OY - (PH - 1), bc = X0 + OX - (PW - 1);
+    for (int i = tid; i < CNR * CNC; i += LG_CTHREADS) {
+        const int r = i / CNC, c = i - r * CNC;
+        int gy0 = br + r, gy1 = br + r + CD, gx = bc + c;
+        gy0 = gy0 < 0 ? 0 : (gy0 > H - 1 ? H - 1 : gy0);
+        gy1 = gy1 < 0 ? 0 : (gy1 > H - 1 ? H - 1 : gy1);
+        gx = gx < 0 ? 0 : (gx > W - 1 ? W - 1 : gx);
+        *reinterpret_cast<float2*>(tile + r * CP + 2 * c + 4 * (c / 8)) = make_float2(src[gy0 * W + gx], src[gy1 * W + gx]);
+    }
+    for (int i = tid; i < PW * PH; i += LG_CTHREADS) psf[i] = psf_g[i];
+    __syncthreads();
+    const int lx0 = threadIdx.x * LG_CR, ly = threadIdx.y;
+    float2 acc[LG_CR];
+#pragma unroll
+    for (int o = 0; o < LG_CR; ++o) acc[o] = make_float2(0.0f, 0.0f);
+#pragma unroll 1
+    for (int j = 0; j < PH; ++j) {
+        const float* row = tile + (ly + PH - 1 - j) * CP + 2 * lx0 + 4 * (lx0 / 8);
+        float2 win[CWIN];
+#pragma unroll
+        for (int t = 0; t < CWIN / 2; ++t) {
+            const float4 q = *reinterpret_cast<const float4*>(row + 4 * t + 4 * (t / 4));
+            win[2 * t] = make_float2(q.x, q.y);
+            win[2 * t + 1] = make_float2(q.z, q.w);
+        }
+        const float* prow = psf + j * PW;
+#pragma unroll
+        for (int i = 0; i < PW; ++i) {
+            const float2 p = make_float2(prow[i], prow[i]);
+#pragma unroll
+            for (int o = 0; o < LG_CR; ++o) acc[o] = __ffma2_rn(p, win[o + PW - 1 - i], acc[o]);
+        }
+    }
+    double s0 = 0.0, s1 = 0.0;
+#pragma unroll
+    for (int o = 0; o < LG_CR; ++o) {
+        const int gx = X0 + lx0 + o;
+        if (gx < W) {
+            if (Y0 + ly < H) {
+                const int k = (Y0 + ly) * W + gx;
+                const float d = acc[o].x - image[k];
+                s0 += (double)(weight[k] * d * d);
+            }
+            if (Y0 + ly + CD < H) {
+                const int k = (Y0 + ly + CD) * W + gx;
+                const float d = acc[o].y - image[k];
+                s1 += (double)(weight[k] * d * d);
+            }
+        }
+    }
+    return s0 + s1;
+}
+#define LG_MULTI_PAIRED(w) ((w) <= 49)
+#else
+#define LG_MULTI_PAIRED(w) false
+#endif
+
 extern "C" __global__ void __launch_bounds__(LG_CTHREADS)
     lg_multi_conv_chi2(const float* __restrict__ raw, const lg_sysinfo* __restrict__ info,
                        const lg_sysplan* __restrict__ plan, const long long* __restrict__ hdr,
@@ -264,10 +343,20 @@ extern "C" __global__ void __launch_bounds__(LG_CTHREADS)
         const float* psf = psfs + I.psf_off;
         double acc = 0.0;
         switch (I.pw * 1024 + I.ph) {
+#if defined(LG_PAIRED)
+#define LG_PSF_CASE(w, h)                                                                                        \
+    case (w) * 1024 + (h):                                                                                      \
+        if constexpr (LG_MULTI_PAIRED(w))                                                                        \
+            acc = lg_multi_conv_unit_pair<w, h>(src, psf, I.W, I.H, tx * LG_CTX, ty * 2 * LG_CTY, img, wht, smem); \
+        else                                                                                                     \
+            acc = lg_multi_conv_unit<w, h>(src, psf, I.W, I.H, tx * LG_CTX, ty * LG_CTY, img, wht, smem);        \
+        break;
+#else
 #define LG_PSF_CASE(w, h)                                                                                 \
     case (w) * 1024 + (h):                                                                               \
         acc = lg_multi_conv_unit<w, h>(src, psf, I.W, I.H, tx * LG_CTX, ty * LG_CTY, img, wht, smem);    \
         break;
+#endif
             LG_PSF_SHAPES
 #undef LG_PSF_CASE
         default:
