@@ -233,9 +233,9 @@ int lg_write_fits_memory(int width, int height, int nlayers, const float* const*
  * after the work queued on the legacy default stream, and synchronises. */
 int lg_eval_profile(lg_ctx* ctx, const double* d_params, int B, double* d_logL, float* stage_ms);
 
-/* Diagnostic: the paired-ray exp (fn = 0), log (1), square root (2) or
- * reciprocal (3) of the fast evaluation modules applied to x[0..n) on a
- * device (out[i] = f(x[i])). */
+/* Diagnostic: the paired-ray exp (fn = 0), log (1), square root (2),
+ * reciprocal (3), atan (4) or atanh (5) of the fast evaluation modules
+ * applied to x[0..n) on a device (out[i] = f(x[i])). */
 int lg_probe_pair_math(int device, int fn, const float* x, int n, float* out);
 
 /* Measured FP32 FMA throughput (TFLOP/s) of a device, for roofline

@@ -1,6 +1,6 @@
 // Diagnostic entry point: the paired-ray elementary functions of the device
-// prelude (SFU-based exp, log, square root and reciprocal used by the fast
-// evaluation modules),
+// prelude (exp, log, square root, reciprocal, arctangent and inverse
+// hyperbolic tangent used by the fast evaluation modules),
 // evaluated on a vector of inputs, so their accuracy can be checked against
 // double-precision references on the host.
 
@@ -16,7 +16,12 @@ __global__ void lg_pair_math_kernel(int fn, const float* __restrict__ x, int n, 
     const int i = 2 * (blockIdx.x * blockDim.x + threadIdx.x);
     if (i >= n) return;
     const lg_pair a = lg_pair_of(x[i], i + 1 < n ? x[i + 1] : 1.0f);
-    const lg_pair r = fn == 0 ? expf(a) : fn == 1 ? logf(a) : fn == 2 ? sqrtf(a) : 1.0f / a;
+    const lg_pair r = fn == 0   ? expf(a)
+                      : fn == 1 ? logf(a)
+                      : fn == 2 ? sqrtf(a)
+                      : fn == 3 ? 1.0f / a
+                      : fn == 4 ? atanf(a)
+                                : atanhf(a);
     out[i] = r.v.x;
     if (i + 1 < n) out[i + 1] = r.v.y;
 }
@@ -25,7 +30,7 @@ __global__ void lg_pair_math_kernel(int fn, const float* __restrict__ x, int n, 
 
 extern "C" int lg_probe_pair_math(int device, int fn, const float* x, int n, float* out)
 {
-    if (!x || !out || n < 0 || fn < 0 || fn > 3) return LG_ERR_INPUT;
+    if (!x || !out || n < 0 || fn < 0 || fn > 5) return LG_ERR_INPUT;
     if (n == 0) return LG_OK;
     auto fail = [](cudaError_t e) {
         lg::set_global_error(cudaGetErrorString(e));

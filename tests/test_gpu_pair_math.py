@@ -8,6 +8,9 @@ Bounds, for results in the normal float range:
 * log: absolute error <= 3e-7 or relative error <= 4 ulp, whichever is
   larger (the correction leaves an absolute error of about 2^-22);
 * sqrt and 1/x: relative error <= 2^-22 (x normal; 1/x for |x| <= 2^126);
+* atan: relative error <= 2^-22; atanh: relative error <= 2^-22 for
+  |v| <= 1/2 and absolute error <= 3e-7 above (the deflection angles of
+  the SIE family, added to pixel positions whose own rounding is ~1e-5);
 * special values: exp(-inf) = 0, exp(+inf) = exp(overflowing x) = inf,
   exp(NaN) = NaN, results below 2^-126 flushed to 0; log(0) = -inf,
   log(inf) = inf, log(negative) = NaN, log of huge finite x still accurate.
@@ -79,3 +82,29 @@ def test_sqrt_and_reciprocal(native):
     assert s[0] == 0 and np.isposinf(s[1]) and np.isnan(s[2]) and np.isnan(s[3])
     r = run(3, [0.0, np.inf, -2.0])
     assert np.isposinf(r[0]) and r[1] == 0 and r[2] == -0.5
+
+
+def test_atan_and_atanh(native):
+    rng = np.random.default_rng(4)
+    z = np.concatenate([rng.uniform(-1, 1, 200000), np.exp(rng.uniform(-20, 20, 200000)) * rng.choice([-1, 1], 200000),
+                        [0.0, -0.0, 1.0, -1.0, 1e-30, 1e30]]).astype(np.float32)
+    got = run(4, z).astype(np.float64)
+    want = np.arctan(z.astype(np.float64))
+    nz = want != 0
+    rel = np.abs(got[nz] - want[nz]) / np.abs(want[nz])
+    print(f"atan: max rel error {rel.max():.3g}")
+    assert rel.max() <= 2.0**-22 and np.all(got[~nz] == 0)
+    v = np.concatenate([rng.uniform(-0.999, 0.999, 300000), rng.uniform(-1e-3, 1e-3, 50000),
+                        [0.0, 0.5, -0.5, 0.50001, 0.9999999]]).astype(np.float32)
+    got = run(5, v).astype(np.float64)
+    want = np.arctanh(v.astype(np.float64))
+    small = np.abs(v) <= 0.5
+    nz = small & (want != 0)
+    rel = np.abs(got[nz] - want[nz]) / np.abs(want[nz])
+    absd = np.abs(got[~small] - want[~small])
+    print(f"atanh: max rel error {rel.max():.3g} (|v| <= 1/2), max abs error {absd.max():.3g} above")
+    assert rel.max() <= 2.0**-22 and absd.max() <= 3e-7
+    sp = run(5, [1.0, -1.0, 1.5, np.nan])
+    assert np.isposinf(sp[0]) and np.isneginf(sp[1]) and np.isnan(sp[2]) and np.isnan(sp[3])
+    sa = run(4, [np.inf, -np.inf, np.nan])
+    assert abs(sa[0] - np.pi / 2) < 1e-7 and abs(sa[1] + np.pi / 2) < 1e-7 and np.isnan(sa[2])
