@@ -289,9 +289,10 @@ LG_DEV float2 lg_copysign2(float2 a, float2 b) { return make_float2(copysignf(a.
 LG_DEV float2 lg_abs2(float2 a) { return make_float2(fabsf(a.x), fabsf(a.y)); }
 
 // arctangent for two rays: r = min(|z|, 1/|z|) (SFU reciprocal), atan(r) =
-// r P(r^2) with a degree-9 polynomial in r^2 fitted here to atan on [0, 1]
-// (weighted least squares for relative error, iterated towards minimax;
-// max error 2.4e-9 in exact arithmetic, about 1 ulp evaluated in FP32),
+// r P(r^2) with a degree-9 polynomial in r^2 fitted to atan on [0, 1] by
+// device/fit_polynomials.py (weighted least squares for relative error,
+// iterated towards minimax; max error 2.4e-9 in exact arithmetic, about
+// 1 ulp evaluated in FP32),
 // pi/2 - atan(1/|z|) for |z| > 1, and the sign of z.
 LG_DEV lg_pair atanf(lg_pair z)
 {
@@ -315,8 +316,8 @@ LG_DEV lg_pair atanf(lg_pair z)
 LG_DEV lg_pair atanf(lg_pair_prod z) { return atanf(lg_pair(z)); }
 
 // inverse hyperbolic tangent for two rays: for |v| <= 1/2, v Q(v^2) with a
-// degree-6 polynomial fitted here to atanh on [0, 1/2] (max error 1.3e-9 in
-// exact arithmetic, about 1 ulp in FP32); above, ln((1 + |v|) / (1 - |v|)) / 2
+// degree-6 polynomial fitted to atanh on [0, 1/2] by the same script (max
+// error 1.3e-9 in exact arithmetic, about 1 ulp in FP32); above, ln((1 + |v|) / (1 - |v|)) / 2
 // through the paired log (absolute error about 2e-7, i.e. within 4 ulp
 // there); the sign of v.  |v| = 1 gives inf, |v| > 1 NaN.
 LG_DEV lg_pair atanhf(lg_pair v)
