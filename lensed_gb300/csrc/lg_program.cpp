@@ -264,6 +264,7 @@ int compile_program(const std::string& src, bool fmad, std::vector<char>& cubin,
     std::vector<const char*> opts = {"--gpu-architecture=sm_103a", "-std=c++17", "--generate-line-info",
                                      "--ftz=false", "-diag-suppress=177"};
     opts.push_back(ieee_divsqrt ? "--prec-div=true" : "--prec-div=false");
+    if (ieee_divsqrt) opts.push_back("-DLG_IEEE_DIVSQRT=1");  // paired-ray division and sqrt too
     opts.push_back(ieee_divsqrt ? "--prec-sqrt=true" : "--prec-sqrt=false");
     opts.push_back(fmad ? "--fmad=true" : "--fmad=false");
     if (const char* dump = std::getenv("LG_NVRTC_DUMP")) {

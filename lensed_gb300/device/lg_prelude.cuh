@@ -182,9 +182,16 @@ LG_DEV float lg_sfu_rsqrt(float x)
     return r;
 }
 LG_DEV lg_pair lg_rcp(lg_pair b) { return {make_float2(lg_sfu_rcp(b.v.x), lg_sfu_rcp(b.v.y))}; }
+#ifdef LG_IEEE_DIVSQRT
+// the context asked for IEEE division and square root: lane by lane
+LG_DEV lg_pair operator/(lg_pair a, lg_pair b) { return {make_float2(a.v.x / b.v.x, a.v.y / b.v.y)}; }
+LG_DEV lg_pair operator/(lg_pair a, float b) { return {make_float2(a.v.x / b, a.v.y / b)}; }
+LG_DEV lg_pair operator/(float a, lg_pair b) { return {make_float2(a / b.v.x, a / b.v.y)}; }
+#else
 LG_DEV lg_pair operator/(lg_pair a, lg_pair b) { return {__fmul2_rn(a.v, lg_rcp(b).v)}; }
 LG_DEV lg_pair operator/(lg_pair a, float b) { return {__fmul2_rn(a.v, lg_bc(lg_sfu_rcp(b)))}; }
 LG_DEV lg_pair operator/(float a, lg_pair b) { return {__fmul2_rn(lg_bc(a), lg_rcp(b).v)}; }
+#endif
 LG_DEV lg_pair operator/(lg_pair_prod a, lg_pair b) { return lg_pair(a) / b; }
 LG_DEV lg_pair operator/(lg_pair_prod a, float b) { return lg_pair(a) / b; }
 LG_DEV lg_pair operator/(lg_pair a, lg_pair_prod b) { return a / lg_pair(b); }
@@ -274,7 +281,11 @@ LG_DEV lg_pair logf(lg_pair_prod x) { return logf(lg_pair(x)); }
     LG_DEV lg_pair fn(lg_pair_prod a) { return fn(lg_pair(a)); }
 // square root and its reciprocal from the SFU (PTX sqrt.approx /
 // rsqrt.approx, within 1 ulp; subnormal inputs flushed)
+#ifdef LG_IEEE_DIVSQRT
+LG_DEV lg_pair sqrtf(lg_pair a) { return {make_float2(sqrtf(a.v.x), sqrtf(a.v.y))}; }
+#else
 LG_DEV lg_pair sqrtf(lg_pair a) { return {make_float2(lg_sfu_sqrt(a.v.x), lg_sfu_sqrt(a.v.y))}; }
+#endif
 LG_DEV lg_pair sqrtf(lg_pair_prod a) { return sqrtf(lg_pair(a)); }
 LG_DEV lg_pair rsqrtf(lg_pair a) { return {make_float2(lg_sfu_rsqrt(a.v.x), lg_sfu_rsqrt(a.v.y))}; }
 LG_DEV lg_pair rsqrtf(lg_pair_prod a) { return rsqrtf(lg_pair(a)); }
