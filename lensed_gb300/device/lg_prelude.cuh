@@ -350,8 +350,16 @@ LG_DEV lg_pair atanhf(lg_pair v)
 }
 LG_DEV lg_pair atanhf(lg_pair_prod v) { return atanhf(lg_pair(v)); }
 
+// a^b for two rays and a >= 0 (the plugins' radial power laws): exp(b ln a)
+// through the paired exp and log (a few ulp; b = 0 gives 1, as powf);
+// negative a falls back to the library per lane
+LG_DEV lg_pair powf(lg_pair a, float b)
+{
+    const lg_pair r = expf(b * logf(a));
+    return {make_float2(b == 0.0f ? 1.0f : (a.v.x < 0.0f ? powf(a.v.x, b) : r.v.x),
+                        b == 0.0f ? 1.0f : (a.v.y < 0.0f ? powf(a.v.y, b) : r.v.y))};
+}
 LG_DEV lg_pair powf(lg_pair a, lg_pair b) { return {make_float2(powf(a.v.x, b.v.x), powf(a.v.y, b.v.y))}; }
-LG_DEV lg_pair powf(lg_pair a, float b) { return {make_float2(powf(a.v.x, b), powf(a.v.y, b))}; }
 LG_DEV lg_pair atan2f(lg_pair y, lg_pair x) { return {make_float2(atan2f(y.v.x, x.v.x), atan2f(y.v.y, x.v.y))}; }
 LG_DEV void sincosf(lg_pair a, lg_pair* s, lg_pair* c)
 {
@@ -373,6 +381,25 @@ LG_DEV void lg_deflect(lg_pair2& y, lg_pair2 a)
     const float2 a0 = d.v.x < LG_INF ? lg_lane(a, 0) : make_float2(1E10f, 1E10f);
     const float2 a1 = d.v.y < LG_INF ? lg_lane(a, 1) : make_float2(1E10f, 1E10f);
     y -= lg_pair2_join(a0, a1);
+}
+
+// Polar angles of a plugin's frame for two rays: r = |x|, (c, s) = (cos,
+// sin) of phi = atan2(x.y, x.x) and (c2, s2) of 2 phi, from the coordinates:
+// c = x/r, s = y/r, c2 = c^2 - s^2, s2 = 2 s c (the values of the
+// reference's atan2 and sincos to within rounding), phi = 0 at the origin.
+// The one-ray version, which follows the reference's calls, sits with the
+// plugin that uses it (after the strict mode's function mapping).
+LG_DEV void lg_polar(lg_pair2 x, lg_pair* r, lg_pair* c, lg_pair* s, lg_pair* c2, lg_pair* s2)
+{
+    *r = length(x);
+    const lg_pair ir = 1.0f / *r;
+    lg_pair cc = x.x * ir, ss = x.y * ir;
+    if (!(r->v.x > 0.0f)) { cc.v.x = 1.0f; ss.v.x = 0.0f; }
+    if (!(r->v.y > 0.0f)) { cc.v.y = 1.0f; ss.v.y = 0.0f; }
+    *c = cc;
+    *s = ss;
+    *c2 = cc * cc - ss * ss;
+    *s2 = 2.0f * ss * cc;
 }
 
 // scalar type of a plugin's vector type

@@ -24,17 +24,23 @@ LG_DEV void lg_set_epl(lg_data_epl* o, float x1, float x2, float r, float t, flo
     lg_epl_setup(o, x1, x2, r, t, q, pa);
 }
 // Deflection in the rotated frame for the elliptical coordinates x.
+// r = |x|, sincos of phi = atan2(x.y, x.x) and of 2 phi, as
+// objects/epl.cl computes them (the two-ray version is in the prelude)
+LG_DEV void lg_polar(float2 x, float* r, float* c, float* s, float* c2, float* s2)
+{
+    *r = length(x);
+    const float phi = atan2f(x.y, x.x);
+    sincosf(phi, s, c);
+    sincosf(2 * phi, s2, c2);
+}
 template <class V>
 LG_DEV V lg_epl_frame(const lg_data_epl* __restrict__ o, V x)
 {
     typedef LG_SCALAR(V) S;
     const float T = 2 - o->t;
     const float f = o->f;
-    S r = length(x);
-    S phi = atan2f(x.y, x.x);
-    S s, c, s2, c2;
-    sincosf(phi, &s, &c);
-    sincosf(2 * phi, &s2, &c2);
+    S r, c, s, c2, s2;
+    lg_polar(x, &r, &c, &s, &c2, &s2);  // atan2, sincos(phi), sincos(2 phi)
     const auto R = make_mat22(c2, -s2, s2, c2);
     V A = V{c, s};
     V a = A;
