@@ -130,14 +130,17 @@ def test_reference_images_on_gpu(native, golden):
         ctx.close()
 
 
-@pytest.mark.parametrize("psf_size", [7, 8, 15])
-def test_psf_convolution_matches_oracle(native, psf_size):
+@pytest.mark.parametrize("psf_size", [7, 8, 15, 49, 51])
+@pytest.mark.parametrize("flags", [0, lg.LG_FLAG_STRICT_FP])
+def test_psf_convolution_matches_oracle(native, psf_size, flags):
+    """Paired-row convolution (fast mode, PSF width <= 49) and the single-row
+    kernel (strict mode, wider PSFs), on images smaller than the PSF too."""
     plugins, params = PLUGIN_CASES[4]
-    W, H = 45, 52
+    W, H = (45, 52) if psf_size < 40 else (40, 70)
     psf = workloads.psf_gauss_wings(psf_size, 2.0)
     if psf_size == 8:
         psf = psf[:, :7].copy()  # even height, odd width: one-axis half-pixel shift
-    ctx = make_ctx(plugins, W, H, psf=psf, rule="sub2")
+    ctx = make_ctx(plugins, W, H, psf=psf, rule="sub2", flags=flags)
     model, raw, _ = ctx.render(ctx.to_map_order(params))
     o = Oracle(plugins, W, H, quadrature.rule("sub2"), psf=psf, precision=32)
     v, _, c = o.render(params)

@@ -41,3 +41,28 @@ def test_systems_reject_bad_counts(native):
     S = lg.Systems([(s.image, s.weight, s.psf, None) for s in syst], syst[0].objects, capacity=[2, 2])
     with pytest.raises(lg.LensedError):
         S.eval([np.zeros((3, S.npars)), np.zeros((1, S.npars))])
+
+
+def test_systems_with_paired_and_single_row_units(native):
+    """PSFs on both sides of the paired-row limit (49 pixels) in one batch:
+    each system still equals its own context, in fast and strict mode."""
+    base = _systems(3)
+    widths = [15, 51, 25]
+    syst = []
+    for s, w in zip(base, widths):
+        psf = workloads.psf_gauss_wings(w, 2.0)
+        syst.append((s, psf))
+    objs = base[0].objects
+    for flags in (0, lg.LG_FLAG_STRICT_FP):
+        S = lg.Systems([(s.image, s.weight, psf, None) for s, psf in syst], objs, capacity=[3] * 3, rule="g3k7",
+                       flags=flags)
+        params = []
+        for s, psf in syst:
+            ctx = lg.Context(s.image, s.weight, s.objects, psf=psf, rule="g3k7", max_batch=3, flags=flags)
+            params.append(ctx.to_map_order(workloads.draw_candidates(s, 3, seed=5)))
+            ctx.close()
+        got = S.eval(params)
+        for (s, psf), p, g in zip(syst, params, got):
+            ctx = lg.Context(s.image, s.weight, s.objects, psf=psf, rule="g3k7", max_batch=3, flags=flags)
+            assert np.array_equal(g, ctx.eval_batch(p)), (s.name, flags)
+            ctx.close()
