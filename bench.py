@@ -45,6 +45,13 @@ UNIT = "evals/s"
 # (add/sub/mul/div/sqrt = 1, each libm-class call = 1), counted from the
 # plugin formulas; plus per-ray overheads of compute() and the quadrature
 # loop.  Used for the algorithmic FLOPs of the render kernel.
+# DRAM bytes (read + write) of one launch of the dominant kernel, measured
+# with ncu on the GB300 for the default workload (the kernel's time under ncu
+# matched the bench's CUDA events): the render writes the raw models
+# (268 MB algorithmic; about 60 MB are still in L2 when it ends) and the
+# convolution reads them once (268 MB) -- no re-reads.
+MEASURED_TRAFFIC = {("config2", 1024, "render"): 208.45e6, ("config2", 1024, "convolve"): 269.2e6}
+
 RAY_FLOPS = {
     "sis": 12, "sis_plus_shear": 20, "nsis": 10, "sie": 26, "sie_plus_shear": 34, "nsie": 30,
     "point_mass": 9, "epl": 172, "epl_plus_shear": 180, "sersic": 17, "sersic_old": 17, "exponential": 15,
@@ -391,7 +398,9 @@ def main():
             "bound": "fp32", "achieved": ach, "peak": peak, "unit": "TFLOP/s", "frac": ach / peak,
             "peak_source": "measured FP32 FMA probe (lg_measure_fp32_peak) on this GPU" if peak_fp32 else
                            "nominal 152 SM x 128 lanes x 2 flop x 2070 MHz",
-            "nominal_peak": nominal, "traffic": None,
+            "nominal_peak": nominal, "traffic": MEASURED_TRAFFIC.get((args.workload, B, dom)),
+            "traffic_source": "ncu dram__bytes_read.sum + dram__bytes_write.sum, one launch of this workload"
+                              if (args.workload, B, dom) in MEASURED_TRAFFIC else None,
             "algorithmic_flops_per_launch": render_flops if dom == "render" else conv_flops,
             "stage_ms": {"set_params": float(stage[0]), "render": float(stage[1]), "convolve": float(stage[2]),
                          "finish": float(stage[3])},
