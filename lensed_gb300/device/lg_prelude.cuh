@@ -331,22 +331,31 @@ LG_DEV lg_pair atanf(lg_pair_prod z) { return atanf(lg_pair(z)); }
 // error 1.3e-9 in exact arithmetic, about 1 ulp in FP32); above, ln((1 + |v|) / (1 - |v|)) / 2
 // through the paired log (absolute error about 2e-7, i.e. within 4 ulp
 // there); the sign of v.  |v| = 1 gives inf, |v| > 1 NaN.
+// The two branches are taken only when a lane of the thread needs them:
+// neighbouring rays mostly fall on the same side of 1/2, so whole warps skip
+// the branch they do not need.
 LG_DEV lg_pair atanhf(lg_pair v)
 {
     const float2 a = lg_abs2(v.v);
-    const float2 s = __fmul2_rn(a, a);
-    float2 p = lg_bc(0x1.6dad62p-3f);
-    p = __ffma2_rn(p, s, lg_bc(0x1.986234p-5f));
-    p = __ffma2_rn(p, s, lg_bc(0x1.e6379cp-4f));
-    p = __ffma2_rn(p, s, lg_bc(0x1.2323c0p-3f));
-    p = __ffma2_rn(p, s, lg_bc(0x1.99a96cp-3f));
-    p = __ffma2_rn(p, s, lg_bc(0x1.555534p-2f));
-    p = __ffma2_rn(__fmul2_rn(p, s), a, a);  // a + a s Q'(s)
-    const float2 num = __fadd2_rn(lg_bc(1.0f), a);
-    const float2 den = __ffma2_rn(a, lg_bc(-1.0f), lg_bc(1.0f));
-    const lg_pair l = logf(lg_pair{__fmul2_rn(num, make_float2(lg_sfu_rcp(den.x), lg_sfu_rcp(den.y)))});
-    const float2 h = __fmul2_rn(l.v, lg_bc(0.5f));
-    return {lg_copysign2(make_float2(a.x <= 0.5f ? p.x : h.x, a.y <= 0.5f ? p.y : h.y), v.v)};
+    const bool small0 = a.x <= 0.5f, small1 = a.y <= 0.5f;
+    float2 p = a, h = a;
+    if (small0 || small1) {
+        const float2 s = __fmul2_rn(a, a);
+        p = lg_bc(0x1.6dad62p-3f);
+        p = __ffma2_rn(p, s, lg_bc(0x1.986234p-5f));
+        p = __ffma2_rn(p, s, lg_bc(0x1.e6379cp-4f));
+        p = __ffma2_rn(p, s, lg_bc(0x1.2323c0p-3f));
+        p = __ffma2_rn(p, s, lg_bc(0x1.99a96cp-3f));
+        p = __ffma2_rn(p, s, lg_bc(0x1.555534p-2f));
+        p = __ffma2_rn(__fmul2_rn(p, s), a, a);  // a + a s Q'(s)
+    }
+    if (!(small0 && small1)) {
+        const float2 num = __fadd2_rn(lg_bc(1.0f), a);
+        const float2 den = __ffma2_rn(a, lg_bc(-1.0f), lg_bc(1.0f));
+        const lg_pair l = logf(lg_pair{__fmul2_rn(num, make_float2(lg_sfu_rcp(den.x), lg_sfu_rcp(den.y)))});
+        h = __fmul2_rn(l.v, lg_bc(0.5f));
+    }
+    return {lg_copysign2(make_float2(small0 ? p.x : h.x, small1 ? p.y : h.y), v.v)};
 }
 LG_DEV lg_pair atanhf(lg_pair_prod v) { return atanhf(lg_pair(v)); }
 
