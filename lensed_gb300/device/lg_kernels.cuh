@@ -55,9 +55,17 @@ LG_DEV double lg_block_sum(double v, double* red)
 
 // ---------------------------------------------------------------- render --
 // kernel/lensed.cl:9-39.  Block (tile, candidate); each thread integrates
-// LG_RPPT pixels (strided by LG_RT so loads and stores coalesce) over the
-// quadrature rule.  MODE 0 stores the raw model, MODE 1 reduces the chi^2
-// directly (no PSF), MODE 2 stores value and error for one candidate.
+// LG_RPPT pixels over the quadrature rule: strided by LG_RT in the scalar
+// kernel (so that loads and stores coalesce), adjacent in the paired kernel
+// (a thread's two rays are neighbours, so they mostly take the same
+// branches; stores are float2).  MODE 0 stores the raw model, MODE 1 reduces
+// the chi^2 directly (no PSF), MODE 2 stores value and error for one
+// candidate.
+#if defined(LG_PAIRED) && LG_RPPT % 2 == 0
+#define LG_PIX(t, j) (LG_RPPT * (t) + (j))
+#else
+#define LG_PIX(t, j) ((t) + (j) * LG_RT)
+#endif
 template <int MODE>
 LG_DEV void lg_render_tile(const lg_model* __restrict__ models, float* __restrict__ out, float* __restrict__ err,
                            const float* __restrict__ image, const float* __restrict__ weight,
@@ -65,12 +73,12 @@ LG_DEV void lg_render_tile(const lg_model* __restrict__ models, float* __restric
 {
     const int b = blockIdx.y;
     const lg_model m = models[b];
-    const int base = blockIdx.x * LG_RTILE + threadIdx.x;
+    const int base = blockIdx.x * LG_RTILE;
     float2 xp[LG_RPPT];
     float v[LG_RPPT], e[LG_RPPT];
 #pragma unroll
     for (int j = 0; j < LG_RPPT; ++j) {
-        int k = base + j * LG_RT;
+        int k = base + LG_PIX(threadIdx.x, j);
         k = k < LG_N ? k : LG_N - 1;
         xp[j] = make_float2(LG_RX + LG_SX * (float)(k % LG_W), LG_RY + LG_SY * (float)(k / LG_W));
         v[j] = 0.0f;
@@ -123,7 +131,7 @@ LG_DEV void lg_render_tile(const lg_model* __restrict__ models, float* __restric
         double s = 0.0;
 #pragma unroll
         for (int j = 0; j < LG_RPPT; ++j) {
-            const int k = base + j * LG_RT;
+            const int k = base + LG_PIX(threadIdx.x, j);
             if (k < LG_N) {
                 const float d = v[j] - image[k];
                 s += (double)(weight[k] * d * d);
@@ -132,14 +140,27 @@ LG_DEV void lg_render_tile(const lg_model* __restrict__ models, float* __restric
         s = lg_block_sum<LG_RT>(s, red);
         if (threadIdx.x == 0) partials[(size_t)b * gridDim.x + blockIdx.x] = s;
     } else {
+#if defined(LG_PAIRED) && LG_RPPT % 2 == 0 && LG_N % 2 == 0
+        // adjacent pixel pairs: one 8-byte store per pair (N even, so the
+        // pair's address is 8-byte aligned)
+#pragma unroll
+        for (int j = 0; j < LG_RPPT; j += 2) {
+            const int k = base + LG_PIX(threadIdx.x, j);
+            if (k < LG_N) {
+                *reinterpret_cast<float2*>(out + (size_t)b * LG_N + k) = make_float2(v[j], v[j + 1]);
+                if (MODE == 2) *reinterpret_cast<float2*>(err + (size_t)b * LG_N + k) = make_float2(e[j], e[j + 1]);
+            }
+        }
+#else
 #pragma unroll
         for (int j = 0; j < LG_RPPT; ++j) {
-            const int k = base + j * LG_RT;
+            const int k = base + LG_PIX(threadIdx.x, j);
             if (k < LG_N) {
                 out[(size_t)b * LG_N + k] = v[j];
                 if (MODE == 2) err[(size_t)b * LG_N + k] = e[j];
             }
         }
+#endif
     }
 }
 

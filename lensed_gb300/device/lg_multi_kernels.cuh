@@ -79,6 +79,13 @@ LG_DEV double lg_block_sum(double v, double* red)
 
 // ------------------------------------------------------------- render --
 // WITH_PSF: store raw models; else reduce the chi^2 of each tile directly.
+// Pixels of a thread as in the single-system kernel: adjacent in the paired
+// kernel, strided by LG_RT otherwise.
+#if defined(LG_PAIRED) && LG_RPPT % 2 == 0
+#define LG_MPIX(t, j) (LG_RPPT * (t) + (j))
+#else
+#define LG_MPIX(t, j) ((t) + (j) * LG_RT)
+#endif
 template <bool WITH_PSF>
 LG_DEV void lg_multi_render_body(const lg_model* __restrict__ models, const lg_sysinfo* __restrict__ info,
                                  const lg_sysplan* __restrict__ plan, const long long* __restrict__ hdr,
@@ -95,12 +102,12 @@ LG_DEV void lg_multi_render_body(const lg_model* __restrict__ models, const lg_s
         const long long local = u - P.r_unit0;
         const int b = (int)(local / I.rtiles), t = (int)(local - (long long)b * I.rtiles);
         const lg_model m = models[P.cand0 + b];
-        const int base = t * LG_RTILE + threadIdx.x;
+        const int base = t * LG_RTILE;
         float2 xp[LG_RPPT];
         float v[LG_RPPT];
 #pragma unroll
         for (int j = 0; j < LG_RPPT; ++j) {
-            int k = base + j * LG_RT;
+            int k = base + LG_MPIX(threadIdx.x, j);
             k = k < I.N ? k : I.N - 1;
             xp[j] = make_float2(I.rx + I.sx * (float)(k % I.W), I.ry + I.sy * (float)(k / I.W));
             v[j] = 0.0f;
@@ -138,14 +145,14 @@ LG_DEV void lg_multi_render_body(const lg_model* __restrict__ models, const lg_s
         if (WITH_PSF) {
 #pragma unroll
             for (int j = 0; j < LG_RPPT; ++j) {
-                const int k = base + j * LG_RT;
+                const int k = base + LG_MPIX(threadIdx.x, j);
                 if (k < I.N) raw[P.raw0 + (long long)b * I.N + k] = v[j];
             }
         } else {
             double acc = 0.0;
 #pragma unroll
             for (int j = 0; j < LG_RPPT; ++j) {
-                const int k = base + j * LG_RT;
+                const int k = base + LG_MPIX(threadIdx.x, j);
                 if (k < I.N) {
                     const float d = v[j] - images[I.img_off + k];
                     acc += (double)(weights[I.img_off + k] * d * d);
