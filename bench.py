@@ -98,6 +98,7 @@ def run_sampler(args):
         _, phys = ctx.eval_cube(r["samples"])
         mean_phys = (w[:, None] * phys).sum(0) / w.sum()
         out[name] = {"logz": r["logz"], "logz_err": r["logz_err"], "ncall": r["ncall"], "wall_s": r["wall_s"],
+                     "eval_s": r["eval_s"], "train_s": r["train_s"], "propose_s": r["propose_s"],
                      "niter": r["niter"], "flow_proposals": r["n_flow_proposals"],
                      "ellipsoid_proposals": r["n_ellipsoid_proposals"],
                      "posterior_mean": dict(zip(ctx.ids, [float(v) for v in mean_phys]))}
@@ -118,8 +119,10 @@ def run_systems(args):
     from lensed_gb300 import workloads
 
     syst, per = workload("systems")
+    t_create = time.perf_counter()
     S = lg.Systems([(s.image, s.weight, s.psf, None) for s in syst], syst[0].objects, capacity=[per] * len(syst),
-                   rule="g3k7", flags=args.flags)
+                   rule="g3k7", flags=args.flags | (0 if args.no_autotune else lg.LG_FLAG_AUTOTUNE))
+    t_create = time.perf_counter() - t_create
     params = []
     for s in syst:
         ctx = lg.Context(s.image, s.weight, s.objects, psf=s.psf, rule=s.rule, max_batch=1)
@@ -139,7 +142,9 @@ def run_systems(args):
             "vs_baseline": None, "dtype": "f32 (f64 chi^2 reduction)", "data": "synthetic",
             "config": {"workload": f"{len(syst)} systems, sizes " + ",".join(str(s.width) for s in syst)
                        + f" (mean {pix:.0f} px), epl_plus_shear+sersic+sky, odd PSFs 15-31, rule g3k7",
-                       "batch": total, "per_system": per},
+                       "batch": total, "per_system": per, "launch_shape": S.launch_shape,
+                       "autotune": (S.tune_report.splitlines() or ["off"])[0]
+                                   + f" (creation {t_create:.1f} s)"},
             "gpu_launches": 4 * args.steps,
             "e2e": {"value": total / dt, "unit": UNIT,
                     "h2d_bytes_per_step": int(sum(p.nbytes for p in params)), "d2h_bytes_per_step": 8 * total}}
@@ -293,6 +298,8 @@ def main():
     ap.add_argument("--flow-width", type=int, default=128)
     ap.add_argument("--flow-epochs", type=int, default=200)
     ap.add_argument("--skip-plain", action="store_true")
+    ap.add_argument("--no-autotune", action="store_true",
+                    help="keep the default launch shape instead of timing the tuner's candidates at creation")
     args = ap.parse_args()
     args.warmup = max(args.warmup, 3)
     if args.impl == "reference":
@@ -314,8 +321,10 @@ def main():
     s, B = workload(args.workload)
     if args.batch:
         B = args.batch
+    t_create = time.perf_counter()
     ctx = lg.Context(s.image, s.weight, s.objects, psf=s.psf, rule=s.rule, device=local, max_batch=B,
-                     flags=args.flags)
+                     flags=args.flags | (0 if args.no_autotune else lg.LG_FLAG_AUTOTUNE))
+    t_create = time.perf_counter() - t_create
     cand = ctx.to_map_order(workloads.draw_candidates(s, B, seed=replicas.candidate_seed(rank)))
     d_params = torch.from_numpy(np.ascontiguousarray(cand)).to(f"cuda:{local}")
     d_logL = torch.empty(B, dtype=torch.float64, device=f"cuda:{local}")
@@ -407,10 +416,13 @@ def main():
             "convolve_tflops": (conv_flops / (stage[2] * 1e-3) / 1e12) if stage[2] > 0 else None,
             "rays_per_s": B * N * Q / (stage[1] * 1e-3)}
 
+    config = describe(s, B)
+    config["launch_shape"] = ctx.launch_shape
+    config["autotune"] = (ctx.tune_report.splitlines() or ["off"])[0] + f" (context creation {t_create:.1f} s)"
     line = {"metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
             "warmup": args.warmup, "ms_per_step": ms / args.steps, "higher_is_better": True, "scaling": "weak",
             "vs_baseline": None, "dtype": "f32 (f64 chi^2 reduction)", "data": "synthetic",
-            "config": describe(s, B), "gpu_launches": 4 * args.steps,
+            "config": config, "gpu_launches": 4 * args.steps,
             "e2e": {"value": e2e, "unit": UNIT, "h2d_bytes_per_step": int(hp.nbytes), "d2h_bytes_per_step": 8 * B},
             "plain_evals_per_s": plain, "roofline": roof}
     if clk:

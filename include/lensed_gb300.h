@@ -62,6 +62,7 @@ extern "C" {
 #define LG_FLAG_STRICT_FP 1 /* no FMA contraction in the composed program */
 #define LG_FLAG_NO_GRAPH 2  /* launch kernels directly instead of graph replay */
 #define LG_FLAG_IEEE_DIV 4  /* fast mode with IEEE division and square root per ray */
+#define LG_FLAG_AUTOTUNE 8  /* choose the launch shape by timing candidates at creation */
 
 typedef struct lg_ctx lg_ctx;
 
@@ -233,6 +234,37 @@ int lg_write_fits_memory(int width, int height, int nlayers, const float* const*
  * after the work queued on the legacy default stream, and synchronises. */
 int lg_eval_profile(lg_ctx* ctx, const double* d_params, int B, double* d_logL, float* stage_ms);
 
+/* Launch shape of the evaluation kernels, as 7 ints: render threads per
+ * block, pixels per thread group, quadrature split (threads of a group that
+ * share its pixels, each taking every split-th quadrature point; 1 in strict
+ * mode), convolution tile width, tile height, outputs per thread, paired
+ * rows (0/1).  The counterpart of the reference's work-group sizing
+ * (src/lensed.c:866-1047), which queries the device for the render
+ * work-group size and halves the convolution tile until it fits local
+ * memory.  With LG_FLAG_AUTOTUNE, lg_create compiles candidate shapes in
+ * parallel, times them on max_batch candidates drawn from the priors and
+ * keeps the fastest render and convolution; the choice is cached per
+ * program, device, batch and flags in the process, and in the text file
+ * named by the environment variable LG_TUNE_CACHE when it is set.  Results
+ * are the same for every shape up to the order of FP64 partial sums, and,
+ * with a quadrature split above 1, of the FP32 quadrature sum. */
+int lg_launch_shape(const lg_ctx* ctx, int shape[7]);
+/* Recompile the evaluation module for a given shape (LG_ERR_INPUT for an
+ * invalid one, LG_ERR_UNSUPPORTED when the convolution tile does not fit
+ * the device's shared memory). */
+int lg_set_launch_shape(lg_ctx* ctx, const int shape[7]);
+/* The autotuner's candidates and their render and convolution times ("" if
+ * the context was not tuned). */
+const char* lg_tune_report(const lg_ctx* ctx);
+/* Without a GPU: the candidate shapes the autotuner would time for a model
+ * (up to max_shapes x 7 ints written; returns the count), and a compile
+ * check of the model's evaluation module for one shape (like
+ * lg_compile_check). */
+int lg_tune_candidates(const lg_image_desc* image, const lg_object_desc* objs, int nobjs, const lg_options* opts,
+                       int* shapes, int max_shapes);
+int lg_compile_check_shape(const lg_image_desc* image, const lg_object_desc* objs, int nobjs, const lg_options* opts,
+                           const int shape[7], char* log, size_t log_size);
+
 /* Diagnostic: the paired-ray exp (fn = 0), log (1), square root (2),
  * reciprocal (3), atan (4) or atanh (5) of the fast evaluation modules
  * applied to x[0..n) on a device (out[i] = f(x[i])). */
@@ -279,6 +311,14 @@ int lg_systems_npars(const lg_systems* S);
  * (npars doubles each, map order); logL receives sum(counts) values in the
  * same order.  Each system's values equal those of its own lg_ctx. */
 int lg_systems_eval(lg_systems* S, const double* params, const int* counts, double* logL);
+/* Launch shape of the multi-system kernels (the 7 ints of lg_launch_shape;
+ * the tile height counts thread rows, a paired-row unit covering two of
+ * them per thread, and the paired flag is 0: paired rows are chosen per
+ * system).  LG_FLAG_AUTOTUNE at creation times render and convolution
+ * candidates with every system at capacity. */
+int lg_systems_launch_shape(const lg_systems* S, int shape[7]);
+int lg_systems_set_launch_shape(lg_systems* S, const int shape[7]);
+const char* lg_systems_tune_report(const lg_systems* S);
 
 /* ------------------------------------------------------- nested sampling */
 /* The sampler that replaces MultiNest's role (src/lensed.c:1236-1288):
@@ -309,6 +349,9 @@ typedef struct {
     double* samples;       /* max_samples x ndims, or NULL: dead + final live points */
     double* sample_logwt;  /* max_samples, or NULL: log posterior weights */
     long max_samples;
+    /* wall time (s) spent in the likelihood callback, in training the
+     * learned proposal and in drawing proposals (ellipsoid or flow) */
+    double eval_s, train_s, propose_s;
 } lg_nested_result;
 
 /* Learned proposal: affine coupling layers with MLP conditioners, trained by

@@ -31,6 +31,8 @@ STATUS = {-1: "input", -2: "compile", -3: "cuda", -4: "alloc", -5: "timeout", -6
 LG_FLAG_STRICT_FP = 1
 LG_FLAG_NO_GRAPH = 2
 LG_FLAG_IEEE_DIV = 4
+LG_FLAG_AUTOTUNE = 8
+SHAPE_FIELDS = ("rt", "rppt", "qs", "ctx", "cty", "cr", "pair_rows")
 DUMP_LAYERS = ("IMG", "RES", "RAW", "ERR", "WHT", "PVL")
 
 
@@ -61,7 +63,8 @@ class NestedResult(C.Structure):
                 ("n_flow_proposals", C.c_long), ("n_ellipsoid_proposals", C.c_long), ("wall_s", C.c_double),
                 ("mean", C.POINTER(C.c_double)), ("std", C.POINTER(C.c_double)),
                 ("samples", C.POINTER(C.c_double)), ("sample_logwt", C.POINTER(C.c_double)),
-                ("max_samples", C.c_long)]
+                ("max_samples", C.c_long), ("eval_s", C.c_double), ("train_s", C.c_double),
+                ("propose_s", C.c_double)]
 
 
 class FlowOptions(C.Structure):
@@ -118,6 +121,16 @@ def lib():
         "lg_write_fits_memory": (C.c_int, [C.c_int, C.c_int, C.c_int, C.POINTER(fp), C.POINTER(C.c_char_p), vp,
                                            C.c_size_t, C.POINTER(C.c_size_t)]),
         "lg_eval_profile": (C.c_int, [vp, vp, C.c_int, vp, fp]),
+        "lg_launch_shape": (C.c_int, [vp, ip]),
+        "lg_set_launch_shape": (C.c_int, [vp, ip]),
+        "lg_tune_report": (C.c_char_p, [vp]),
+        "lg_tune_candidates": (C.c_int, [C.POINTER(_ImageDesc), C.POINTER(_ObjectDesc), C.c_int,
+                                         C.POINTER(_Options), ip, C.c_int]),
+        "lg_compile_check_shape": (C.c_int, [C.POINTER(_ImageDesc), C.POINTER(_ObjectDesc), C.c_int,
+                                             C.POINTER(_Options), ip, C.c_char_p, C.c_size_t]),
+        "lg_systems_launch_shape": (C.c_int, [vp, ip]),
+        "lg_systems_set_launch_shape": (C.c_int, [vp, ip]),
+        "lg_systems_tune_report": (C.c_char_p, [vp]),
         "lg_measure_fp32_peak": (C.c_int, [C.c_int, dp]),
         "lg_probe_pair_math": (C.c_int, [C.c_int, C.c_int, fp, C.c_int, fp]),
         "lg_loglike_images_noalloc": (C.c_int, [vp, vp, vp, C.c_long, C.c_int, vp, vp]),
@@ -237,6 +250,7 @@ def _pack(r, arrays):
     n = min(r.nsamples, r.max_samples)
     return {"logz": r.logz, "logz_err": r.logz_err, "information": r.information, "max_logl": r.max_logl,
             "ncall": r.ncall, "niter": r.niter, "nsamples": r.nsamples, "wall_s": r.wall_s,
+            "eval_s": r.eval_s, "train_s": r.train_s, "propose_s": r.propose_s,
             "n_flow_proposals": r.n_flow_proposals, "n_ellipsoid_proposals": r.n_ellipsoid_proposals,
             "mean": arrays["mean"], "std": arrays["std"], "samples": arrays["samples"][:n],
             "logwt": arrays["logwt"][:n]}
@@ -401,6 +415,32 @@ def compile_check(width, height, objects, psf=None, rule="g3k7", pcs=None, flags
     return buf.value.decode(errors="replace")
 
 
+def tune_candidates(width, height, objects, psf=None, rule="g3k7", pcs=None, flags=0):
+    """The launch shapes the autotuner times for a model (list of dicts)."""
+    psf_a = _f32(psf)
+    arr, keep = _objects(objects)
+    d = _image_desc(width, height, None, None, psf_a, pcs)
+    buf = (C.c_int * (7 * 64))()
+    n = lib().lg_tune_candidates(C.byref(d), arr, len(objects), C.byref(_options(rule, 0, 0, flags)), buf, 64)
+    if n < 0:
+        raise LensedError(n, lib().lg_last_error(None).decode(errors="replace"))
+    return [dict(zip(SHAPE_FIELDS, list(buf[7 * i: 7 * i + 7]))) for i in range(min(n, 64))]
+
+
+def compile_check_shape(width, height, objects, shape: dict, psf=None, rule="g3k7", pcs=None, flags=0):
+    """compile_check of the evaluation module for one launch shape."""
+    psf_a = _f32(psf)
+    arr, keep = _objects(objects)
+    d = _image_desc(width, height, None, None, psf_a, pcs)
+    v = (C.c_int * 7)(*[int(shape[k]) for k in SHAPE_FIELDS])
+    buf = C.create_string_buffer(1 << 16)
+    rc = lib().lg_compile_check_shape(C.byref(d), arr, len(objects), C.byref(_options(rule, 0, 0, flags)), v, buf,
+                                      len(buf))
+    if rc:
+        raise LensedError(rc, buf.value.decode(errors="replace"))
+    return buf.value.decode(errors="replace")
+
+
 class Systems:
     """A batch of lens systems sharing the objects (wraps lg_systems_*).
 
@@ -436,6 +476,27 @@ class Systems:
 
     def __del__(self):
         self.close()
+
+    @property
+    def launch_shape(self) -> dict:
+        """Launch shape of the multi-system kernels (see lg_systems_launch_shape)."""
+        v = (C.c_int * 7)()
+        lib().lg_systems_launch_shape(self.h, v)
+        return dict(zip(SHAPE_FIELDS, list(v)))
+
+    def set_launch_shape(self, **shape) -> None:
+        """Recompile the kernels for a launch shape (fields of SHAPE_FIELDS;
+        missing ones keep their current value)."""
+        cur = self.launch_shape
+        cur.update(shape)
+        v = (C.c_int * 7)(*[int(cur[k]) for k in SHAPE_FIELDS])
+        rc = lib().lg_systems_set_launch_shape(self.h, v)
+        if rc:
+            raise LensedError(rc, lib().lg_systems_last_error(self.h).decode(errors="replace"))
+
+    @property
+    def tune_report(self) -> str:
+        return lib().lg_systems_tune_report(self.h).decode()
 
     def eval(self, params_list):
         """params_list: per system a (count, npars) array in map order."""
@@ -492,6 +553,26 @@ class Context:
     @property
     def masked(self) -> int:
         return lib().lg_masked(self.h)
+
+    @property
+    def launch_shape(self) -> dict:
+        """Launch shape of the evaluation kernels (see lg_launch_shape)."""
+        v = (C.c_int * 7)()
+        self._check(lib().lg_launch_shape(self.h, v))
+        return dict(zip(SHAPE_FIELDS, list(v)))
+
+    def set_launch_shape(self, **shape) -> None:
+        """Recompile the evaluation kernels for a launch shape (fields of
+        SHAPE_FIELDS; missing ones keep their current value)."""
+        cur = self.launch_shape
+        cur.update(shape)
+        v = (C.c_int * 7)(*[int(cur[k]) for k in SHAPE_FIELDS])
+        self._check(lib().lg_set_launch_shape(self.h, v))
+
+    @property
+    def tune_report(self) -> str:
+        """The autotuner's candidates and timings ("" if not tuned)."""
+        return lib().lg_tune_report(self.h).decode()
 
     def to_map_order(self, params_obj):
         """Reorder (..., npars) parameters from object order to map order

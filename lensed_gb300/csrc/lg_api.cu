@@ -20,6 +20,7 @@
 #include <cstring>
 #include <map>
 #include <mutex>
+#include <sstream>
 #include <string>
 #include <vector>
 
@@ -94,6 +95,8 @@ struct lg_ctx {
     CUfunction f_cchi2 = nullptr, f_cdump = nullptr, f_finish = nullptr;
     size_t model_bytes = 0;
     int rtiles = 0, ctiles = 0, ctiles_x = 0, ctiles_y = 0, cthreads = 0, csmem = 0;
+
+    std::string tune_report;  // candidates and timings of the autotuner
 
     cudaStream_t stream = nullptr;
     float* d_image = nullptr;
@@ -227,7 +230,7 @@ lg::Shape choose_shape(const lg::Model& m, bool strict)
 void shape_sizes(const lg::Shape& s, const lg::Model& m, lg_ctx* c)
 {
     const long N = (long)m.width * m.height;
-    const int rtile = s.rt * s.rppt;
+    const int rtile = s.rtile();
     c->rtiles = (int)((N + rtile - 1) / rtile);
     if (!m.psf.empty()) {
         // the shared-memory size is read back from the compiled module
@@ -303,6 +306,226 @@ __global__ void __launch_bounds__(128)
         for (int i = 0; i < np; ++i) phys[(size_t)b * np + i] = params[(size_t)b * np + i];
 }
 
+bool ctx_strict(const lg_ctx* c) { return (c->flags & LG_FLAG_STRICT_FP) != 0; }
+// fast mode: hardware-approximate division and square root per ray
+// (<= 2 ulp, as the reference's -cl-fast-relaxed-math build allows) unless
+// LG_FLAG_IEEE_DIV; strict mode and set_params stay IEEE
+bool ctx_ieee(const lg_ctx* c) { return ctx_strict(c) || (c->flags & LG_FLAG_IEEE_DIV); }
+
+int compile_eval(lg_ctx* c, const lg::Shape& s, std::vector<char>& cubin)
+{
+    std::string log;
+    const bool strict = ctx_strict(c);
+    int rc = lg::compile_program(lg::compose_source(c->model, s, strict, lg::Part::EVAL), !strict, cubin, log,
+                                 ctx_ieee(c));
+    return rc ? c->fail(rc, log) : LG_OK;
+}
+
+// Make the evaluation module compiled for shape s the context's: its
+// kernels, the convolution's shared memory and a partial-sum buffer for
+// max_batch candidates.  The previous module and the graphs captured with
+// it are released first.
+int load_eval(lg_ctx* c, const lg::Shape& s, const std::vector<char>& cubin)
+{
+    int rc;
+    if (c->stream && (rc = c->cuda(cudaStreamSynchronize(c->stream), "synchronize"))) return rc;
+    for (auto& g : c->graphs) cudaGraphExecDestroy(g.second);
+    c->graphs.clear();
+    for (auto& g : c->cube_graphs) cudaGraphExecDestroy(g.second);
+    c->cube_graphs.clear();
+    if (c->mod) c->drv->moduleUnload(c->mod);
+    c->mod = nullptr;
+    cudaFree(c->d_partials);
+    c->d_partials = nullptr;
+    c->shape = s;
+    shape_sizes(s, c->model, c);
+    if ((rc = c->drvcall(c->drv->moduleLoadData(&c->mod, cubin.data()), "cuModuleLoadData"))) return rc;
+    struct {
+        CUfunction* f;
+        const char* n;
+        bool need;
+    } fns[] = {{&c->f_rraw, "lg_render_raw", true},  {&c->f_rchi2, "lg_render_chi2", true},
+               {&c->f_rdump, "lg_render_dump", true}, {&c->f_finish, "lg_finish", true},
+               {&c->f_cchi2, "lg_conv_chi2", c->psf}, {&c->f_cdump, "lg_conv_dump", c->psf}};
+    for (auto& f : fns)
+        if (f.need && (rc = c->drvcall(c->drv->moduleGetFunction(f.f, c->mod, f.n), f.n))) return rc;
+    CUdeviceptr gp;
+    size_t gb;
+    if (c->psf) {
+        int csm = 0, cth = 0;
+        if ((rc = c->drvcall(c->drv->moduleGetGlobal(&gp, &gb, c->mod, "lg_conv_smem"), "lg_conv_smem")) ||
+            (rc = c->cuda(cudaMemcpy(&csm, (void*)gp, sizeof csm, cudaMemcpyDeviceToHost), "conv smem")) ||
+            (rc = c->drvcall(c->drv->moduleGetGlobal(&gp, &gb, c->mod, "lg_conv_threads"), "lg_conv_threads")) ||
+            (rc = c->cuda(cudaMemcpy(&cth, (void*)gp, sizeof cth, cudaMemcpyDeviceToHost), "conv threads")))
+            return rc;
+        if (cth != c->cthreads) return c->fail(LG_ERR_COMPILE, "convolution block size mismatch");
+        int optin = 0;
+        cudaDeviceGetAttribute(&optin, cudaDevAttrMaxSharedMemoryPerBlockOptin, c->device);
+        if (csm > optin)
+            return c->fail(LG_ERR_UNSUPPORTED, "convolution tile needs " + std::to_string(csm) +
+                                                   " bytes of shared memory, above the device's " +
+                                                   std::to_string(optin));
+        c->csmem = csm;
+        if (c->csmem > 48 * 1024)
+            if ((rc = c->drvcall(c->drv->funcSetAttribute(c->f_cchi2, CU_FUNC_ATTRIBUTE_MAX_DYNAMIC_SHARED_SIZE_BYTES,
+                                                          c->csmem),
+                                 "convolve smem")) ||
+                (rc = c->drvcall(c->drv->funcSetAttribute(c->f_cdump, CU_FUNC_ATTRIBUTE_MAX_DYNAMIC_SHARED_SIZE_BYTES,
+                                                          c->csmem),
+                                 "convolve smem")))
+                return rc;
+    }
+    const size_t ntiles = (size_t)(c->psf ? c->ctiles : c->rtiles);
+    if (cudaMalloc((void**)&c->d_partials, (size_t)c->max_batch * ntiles * 8) != cudaSuccess)
+        return c->fail(LG_ERR_ALLOC, "cudaMalloc partials");
+    return LG_OK;
+}
+
+// Candidate parameter vectors for timing: B draws from the priors (map
+// order; derived parameters at u = 0.5), from a fixed seed.
+void prior_draws(const lg::Model& m, int B, double* out)
+{
+    uint64_t st = 0x243f6a8885a308d3ull;
+    auto unif = [&]() {
+        st += 0x9e3779b97f4a7c15ull;
+        uint64_t z = st;
+        z = (z ^ (z >> 30)) * 0xbf58476d1ce4e5b9ull;
+        z = (z ^ (z >> 27)) * 0x94d049bb133111ebull;
+        z ^= z >> 31;
+        return ((z >> 11) + 0.5) * (1.0 / 9007199254740992.0);
+    };
+    const size_t np = m.pars.size();
+    for (int b = 0; b < B; ++b)
+        for (size_t i = 0; i < np; ++i) {
+            const lg::ParamInfo& p = m.pars[m.pmap[i]];
+            out[(size_t)b * np + i] = p.prior.apply((int)i < m.ndims ? unif() : 0.5);
+        }
+}
+
+// Render and convolution times (ms, best of several runs) of the loaded
+// module on the candidates in d_params.
+int time_stages(lg_ctx* c, int B, double* render_ms, double* conv_ms)
+{
+    cudaEvent_t ev[5] = {};
+    int rc = LG_OK;
+    for (auto& e : ev)
+        if (!rc) rc = c->cuda(cudaEventCreate(&e), "event");
+    double best[2] = {1e30, 1e30}, total = 0;
+    for (int rep = 0; !rc && rep < 40; ++rep) {
+        rc = c->enqueue(B, c->d_params, c->d_logL, c->stream, ev);
+        if (!rc) rc = c->cuda(cudaStreamSynchronize(c->stream), "tune run");
+        float t[3] = {0, 0, 0};
+        for (int i = 0; i < 3 && !rc; ++i) rc = c->cuda(cudaEventElapsedTime(&t[i], ev[i + 1], ev[i + 2]), "elapsed");
+        if (rc || rep == 0) continue;  // the first run warms up
+        best[0] = std::min(best[0], (double)t[0]);
+        best[1] = std::min(best[1], (double)t[1]);
+        total += t[0] + t[1];
+        if (rep >= 3 && total > 30.0) break;
+    }
+    for (auto& e : ev)
+        if (e) cudaEventDestroy(e);
+    *render_ms = best[0];
+    *conv_ms = best[1];
+    return rc;
+}
+
+// LG_FLAG_AUTOTUNE: compile the candidate shapes in parallel, time each on
+// max_batch candidates drawn from the priors, keep the fastest render and
+// the fastest convolution (a cached choice for the same program, device,
+// batch and flags is reused without timing).
+int autotune(lg_ctx* c)
+{
+    const lg::Model& m = c->model;
+    const bool strict = ctx_strict(c);
+    const lg::Shape base = choose_shape(m, strict);
+    const std::string key = lg::tune_key(lg::compose_source(m, base, strict, lg::Part::EVAL), c->device,
+                                         c->max_batch, c->flags & (LG_FLAG_STRICT_FP | LG_FLAG_IEEE_DIV));
+    std::ostringstream rep;
+    int rc;
+    lg::Shape chosen;
+    if (lg::tune_cache_get(key, chosen) && lg::check_shape(chosen, strict, c->psf, m.psfw).empty()) {
+        std::vector<char> cubin;
+        if ((rc = compile_eval(c, chosen, cubin)) || (rc = load_eval(c, chosen, cubin))) return rc;
+        c->tune_report = "cached " + key + ": " + chosen.str() + "\n";
+        return LG_OK;
+    }
+    for (size_t i = 0; i < m.pars.size(); ++i)
+        if (!m.pars[i].has_prior) {
+            std::vector<char> cubin;
+            if ((rc = compile_eval(c, base, cubin)) || (rc = load_eval(c, base, cubin))) return rc;
+            c->tune_report = "not tuned (no prior for " + m.pars[i].id + " to draw candidates from): " +
+                             base.str() + "\n";
+            return LG_OK;
+        }
+    const int B = c->max_batch;
+    const size_t np = m.pars.size();
+    prior_draws(m, B, c->h_params);
+    if ((rc = c->cuda(cudaMemcpy(c->d_params, c->h_params, (size_t)B * np * 8, cudaMemcpyHostToDevice), "params")))
+        return rc;
+    // render candidates with the base convolution, convolution candidates
+    // with the base render
+    std::vector<lg::Shape> cand;
+    std::vector<int> is_render;
+    for (const lg::Shape& s : lg::render_candidates(base, strict))
+        if (lg::check_shape(s, strict, c->psf, m.psfw).empty()) cand.push_back(s), is_render.push_back(1);
+    if (c->psf)
+        for (const lg::Shape& s : lg::conv_candidates(base)) {
+            if (!lg::check_shape(s, strict, c->psf, m.psfw).empty()) continue;
+            bool dup = false;
+            for (const lg::Shape& t : cand) dup = dup || t == s;
+            if (!dup) cand.push_back(s), is_render.push_back(0);
+        }
+    std::vector<std::string> srcs;
+    for (const lg::Shape& s : cand) srcs.push_back(lg::compose_source(m, s, strict, lg::Part::EVAL));
+    std::vector<std::vector<char>> cubins;
+    std::vector<int> rcs;
+    std::vector<std::string> logs;
+    lg::compile_parallel(srcs, !strict, ctx_ieee(c), cubins, rcs, logs);
+    double best_r = 1e30, best_c = 1e30;
+    lg::Shape br = base, bc = base;
+    for (size_t i = 0; i < cand.size(); ++i) {
+        double r_ms = 0, c_ms = 0;
+        if (rcs[i]) {
+            rep << "  " << cand[i].str() << ": compile failed\n";
+            continue;
+        }
+        if ((rc = load_eval(c, cand[i], cubins[i]))) {
+            if (rc != LG_ERR_UNSUPPORTED) return rc;
+            rep << "  " << cand[i].str() << ": " << c->err << "\n";
+            c->err.clear();
+            continue;
+        }
+        if ((rc = time_stages(c, B, &r_ms, &c_ms))) return rc;
+        char line[256];
+        std::snprintf(line, sizeof line, "  %s: render %.4f ms, convolve %.4f ms\n", cand[i].str().c_str(), r_ms,
+                      c_ms);
+        rep << line;
+        // the base shape is a render candidate; its convolution time also
+        // stands for the base convolution
+        const bool base_conv = cand[i].ctx == base.ctx && cand[i].cty == base.cty && cand[i].cr == base.cr;
+        if (is_render[i] && r_ms < best_r) best_r = r_ms, br = cand[i];
+        if ((!is_render[i] || base_conv) && c->psf && c_ms < best_c) best_c = c_ms, bc = cand[i];
+    }
+    chosen = br;
+    if (c->psf) {
+        chosen.ctx = bc.ctx;
+        chosen.cty = bc.cty;
+        chosen.cr = bc.cr;
+    }
+    const std::vector<char>* cb = nullptr;
+    for (size_t i = 0; i < cand.size(); ++i)
+        if (!rcs[i] && cand[i] == chosen) cb = &cubins[i];
+    std::vector<char> own;
+    if (!cb) {
+        if ((rc = compile_eval(c, chosen, own))) return rc;
+        cb = &own;
+    }
+    if ((rc = load_eval(c, chosen, *cb))) return rc;
+    lg::tune_cache_put(key, chosen);
+    c->tune_report = "tuned " + key + " on " + std::to_string(B) + " candidates: " + chosen.str() + "\n" + rep.str();
+    return LG_OK;
+}
+
 int create_impl(lg_ctx* c, const lg_image_desc* img, const lg_object_desc* objs, int nobjs, const lg_options* opts)
 {
     int rc = lg::build_model(img, objs, nobjs, opts, c->model, c->err);
@@ -320,18 +543,12 @@ int create_impl(lg_ctx* c, const lg_image_desc* img, const lg_object_desc* objs,
         if (img->weight[k] == 0) c->masked++;
 
     // compose and compile the programs (the reference's clBuildProgram,
-    // src/lensed.c:706-776)
+    // src/lensed.c:706-776): the set_params module here, the evaluation
+    // module (whose launch shape may be tuned) once the buffers exist
     const bool strict = (c->flags & LG_FLAG_STRICT_FP) != 0;
     c->shape = choose_shape(m, strict);
-    shape_sizes(c->shape, m, c);
     std::string log;
-    std::vector<char> cubin, cubin_set;
-    // fast mode: hardware-approximate division and square root per ray
-    // (<= 2 ulp, as the reference's -cl-fast-relaxed-math build allows)
-    // unless LG_FLAG_IEEE_DIV; strict mode and set_params stay IEEE
-    const bool ieee = strict || (c->flags & LG_FLAG_IEEE_DIV);
-    rc = lg::compile_program(lg::compose_source(m, c->shape, strict, lg::Part::EVAL), !strict, cubin, log, ieee);
-    if (rc) return c->fail(rc, log);
+    std::vector<char> cubin_set;
     rc = lg::compile_program(lg::compose_source(m, c->shape, strict, lg::Part::SET), false, cubin_set, log);
     if (rc) return c->fail(rc, log);
 
@@ -339,21 +556,10 @@ int create_impl(lg_ctx* c, const lg_image_desc* img, const lg_object_desc* objs,
     if ((rc = c->cuda(cudaFree(nullptr), "CUDA context"))) return rc;
     c->drv = driver();
     if (!c->drv) return c->fail(LG_ERR_CUDA, "CUDA driver entry points unavailable");
-    if ((rc = c->drvcall(c->drv->moduleLoadData(&c->mod, cubin.data()), "cuModuleLoadData")) ||
-        (rc = c->drvcall(c->drv->moduleLoadData(&c->mod_set, cubin_set.data()), "cuModuleLoadData")))
-        return rc;
+    if ((rc = c->drvcall(c->drv->moduleLoadData(&c->mod_set, cubin_set.data()), "cuModuleLoadData"))) return rc;
     if ((rc = c->drvcall(c->drv->moduleGetFunction(&c->f_setp, c->mod_set, "lg_set_params_kernel"),
                          "lg_set_params_kernel")))
         return rc;
-    struct {
-        CUfunction* f;
-        const char* n;
-        bool need;
-    } fns[] = {{&c->f_rraw, "lg_render_raw", true},  {&c->f_rchi2, "lg_render_chi2", true},
-               {&c->f_rdump, "lg_render_dump", true}, {&c->f_finish, "lg_finish", true},
-               {&c->f_cchi2, "lg_conv_chi2", c->psf}, {&c->f_cdump, "lg_conv_dump", c->psf}};
-    for (auto& f : fns)
-        if (f.need && (rc = c->drvcall(c->drv->moduleGetFunction(f.f, c->mod, f.n), f.n))) return rc;
     CUdeviceptr gp;
     size_t gb;
     if ((rc = c->drvcall(c->drv->moduleGetGlobal(&gp, &gb, c->mod_set, "lg_model_bytes"), "lg_model_bytes")))
@@ -361,28 +567,9 @@ int create_impl(lg_ctx* c, const lg_image_desc* img, const lg_object_desc* objs,
     unsigned mb = 0;
     if ((rc = c->cuda(cudaMemcpy(&mb, (void*)gp, sizeof mb, cudaMemcpyDeviceToHost), "model size"))) return rc;
     c->model_bytes = mb;
-    if (c->psf) {
-        int csm = 0, cth = 0;
-        if ((rc = c->drvcall(c->drv->moduleGetGlobal(&gp, &gb, c->mod, "lg_conv_smem"), "lg_conv_smem")) ||
-            (rc = c->cuda(cudaMemcpy(&csm, (void*)gp, sizeof csm, cudaMemcpyDeviceToHost), "conv smem")) ||
-            (rc = c->drvcall(c->drv->moduleGetGlobal(&gp, &gb, c->mod, "lg_conv_threads"), "lg_conv_threads")) ||
-            (rc = c->cuda(cudaMemcpy(&cth, (void*)gp, sizeof cth, cudaMemcpyDeviceToHost), "conv threads")))
-            return rc;
-        if (cth != c->cthreads) return c->fail(LG_ERR_COMPILE, "convolution block size mismatch");
-        c->csmem = csm;
-    }
-    if (c->psf && c->csmem > 48 * 1024)
-        if ((rc = c->drvcall(c->drv->funcSetAttribute(c->f_cchi2, CU_FUNC_ATTRIBUTE_MAX_DYNAMIC_SHARED_SIZE_BYTES,
-                                                      c->csmem),
-                             "convolve smem")) ||
-            (rc = c->drvcall(c->drv->funcSetAttribute(c->f_cdump, CU_FUNC_ATTRIBUTE_MAX_DYNAMIC_SHARED_SIZE_BYTES,
-                                                      c->csmem),
-                             "convolve smem")))
-            return rc;
 
     if ((rc = c->cuda(cudaStreamCreateWithFlags(&c->stream, cudaStreamNonBlocking), "stream"))) return rc;
     const size_t B = (size_t)c->max_batch, N = (size_t)c->N, np = m.pars.size();
-    const size_t ntiles = (size_t)(c->psf ? c->ctiles : c->rtiles);
     auto alloc = [&](void** p, size_t bytes, const char* what) {
         cudaError_t e = cudaMalloc(p, bytes);
         if (e != cudaSuccess) {
@@ -393,7 +580,6 @@ int create_impl(lg_ctx* c, const lg_image_desc* img, const lg_object_desc* objs,
     };
     if ((rc = alloc((void**)&c->d_image, N * 4, "image")) || (rc = alloc((void**)&c->d_weight, N * 4, "weight")) ||
         (rc = alloc(&c->d_models, B * c->model_bytes, "models")) ||
-        (rc = alloc((void**)&c->d_partials, B * ntiles * 8, "partials")) ||
         (rc = alloc((void**)&c->d_params, B * np * 8, "params")) ||
         (rc = alloc((void**)&c->d_logL, B * 8, "logL")))
         return rc;
@@ -422,7 +608,10 @@ int create_impl(lg_ctx* c, const lg_image_desc* img, const lg_object_desc* objs,
     if ((rc = c->cuda(cudaMemcpy(c->d_image, img->image, N * 4, cudaMemcpyHostToDevice), "upload image")) ||
         (rc = c->cuda(cudaMemcpy(c->d_weight, img->weight, N * 4, cudaMemcpyHostToDevice), "upload weight")))
         return rc;
-    return LG_OK;
+    if (c->flags & LG_FLAG_AUTOTUNE) return autotune(c);
+    std::vector<char> cubin;
+    if ((rc = compile_eval(c, c->shape, cubin))) return rc;
+    return load_eval(c, c->shape, cubin);
 }
 
 // Graph of upload + evaluation + read-back for B candidates, built on first
@@ -656,6 +845,64 @@ int lg_compile_check(const lg_image_desc* image, const lg_object_desc* objs, int
     return rc;
 }
 
+int lg_tune_candidates(const lg_image_desc* image, const lg_object_desc* objs, int nobjs, const lg_options* opts,
+                       int* shapes, int max_shapes)
+{
+    lg::Model m;
+    std::string err;
+    int rc = lg::build_model(image, objs, nobjs, opts, m, err);
+    if (rc) {
+        g_create_error = err;
+        return rc;
+    }
+    const bool strict = opts && (opts->flags & LG_FLAG_STRICT_FP);
+    const lg::Shape base = choose_shape(m, strict);
+    std::vector<lg::Shape> cand;
+    for (const lg::Shape& s : lg::render_candidates(base, strict))
+        if (lg::check_shape(s, strict, !m.psf.empty(), m.psfw).empty()) cand.push_back(s);
+    if (!m.psf.empty())
+        for (const lg::Shape& s : lg::conv_candidates(base)) {
+            bool dup = false;
+            for (const lg::Shape& t : cand) dup = dup || t == s;
+            if (!dup && lg::check_shape(s, strict, true, m.psfw).empty()) cand.push_back(s);
+        }
+    for (int i = 0; i < (int)cand.size() && i < max_shapes && shapes; ++i) {
+        const lg::Shape& s = cand[i];
+        const int v[7] = {s.rt, s.rppt, s.qs, s.ctx, s.cty, s.cr, s.pair_rows ? 1 : 0};
+        std::memcpy(shapes + 7 * i, v, sizeof v);
+    }
+    return (int)cand.size();
+}
+
+int lg_compile_check_shape(const lg_image_desc* image, const lg_object_desc* objs, int nobjs, const lg_options* opts,
+                           const int shape[7], char* log, size_t log_size)
+{
+    lg::Model m;
+    std::string err;
+    int rc = shape ? lg::build_model(image, objs, nobjs, opts, m, err) : LG_ERR_INPUT;
+    if (!rc) {
+        const bool strict = opts && (opts->flags & LG_FLAG_STRICT_FP);
+        lg::Shape s;
+        s.rt = shape[0];
+        s.rppt = shape[1];
+        s.qs = shape[2];
+        s.ctx = shape[3];
+        s.cty = shape[4];
+        s.cr = shape[5];
+        s.pair_rows = shape[6] != 0;
+        err = lg::check_shape(s, strict, !m.psf.empty(), m.psfw);
+        if (!err.empty()) {
+            rc = LG_ERR_INPUT;
+        } else {
+            std::vector<char> cubin;
+            const bool ieee = strict || (opts && (opts->flags & LG_FLAG_IEEE_DIV));
+            rc = lg::compile_program(lg::compose_source(m, s, strict, lg::Part::EVAL), !strict, cubin, err, ieee);
+        }
+    }
+    if (log && log_size) std::snprintf(log, log_size, "%s", err.c_str());
+    return rc;
+}
+
 lg_ctx* lg_create(const lg_image_desc* image, const lg_object_desc* objs, int nobjs, const lg_options* opts,
                   int* status)
 {
@@ -885,6 +1132,46 @@ int lg_write_output(lg_ctx* c, const double* params, const char* path)
     if (rc) c->err = lg_last_error(nullptr);
     return rc;
 }
+
+int lg_launch_shape(const lg_ctx* c, int shape[7])
+{
+    if (!c || !shape) return LG_ERR_INPUT;
+    const lg::Shape& s = c->shape;
+    const int v[7] = {s.rt, s.rppt, s.qs, s.ctx, s.cty, s.cr, s.pair_rows ? 1 : 0};
+    std::memcpy(shape, v, sizeof v);
+    return LG_OK;
+}
+
+int lg_set_launch_shape(lg_ctx* c, const int shape[7])
+{
+    if (!c || !shape) return LG_ERR_INPUT;
+    lg::Shape s;
+    s.rt = shape[0];
+    s.rppt = shape[1];
+    s.qs = shape[2];
+    s.ctx = shape[3];
+    s.cty = shape[4];
+    s.cr = shape[5];
+    s.pair_rows = shape[6] != 0;
+    const std::string why = lg::check_shape(s, ctx_strict(c), c->psf, c->model.psfw);
+    if (!why.empty()) return c->fail(LG_ERR_INPUT, "launch shape: " + why);
+    int rc;
+    if ((rc = c->cuda(cudaSetDevice(c->device), "cudaSetDevice"))) return rc;
+    std::vector<char> cubin;
+    const lg::Shape old = c->shape;
+    if ((rc = compile_eval(c, s, cubin))) return rc;
+    rc = load_eval(c, s, cubin);
+    if (rc == LG_ERR_UNSUPPORTED) {
+        // keep the context usable with its previous shape
+        const std::string msg = c->err;
+        std::vector<char> prev;
+        if (!compile_eval(c, old, prev) && !load_eval(c, old, prev)) c->err = msg;
+        else rc = LG_ERR_CUDA;
+    }
+    return rc;
+}
+
+const char* lg_tune_report(const lg_ctx* c) { return c ? c->tune_report.c_str() : ""; }
 
 // Per-stage device times of one evaluation, the counterpart of the
 // reference's --profile event table (src/nested.c:21-40, src/profile.c).

@@ -125,10 +125,18 @@ int build_model(const lg_image_desc* img, const lg_object_desc* objs, int nobjs,
 
 // Launch-shape parameters baked into the program.
 struct Shape {
-    int rt = 128, rppt = 2;        // render threads / pixels per thread
+    int rt = 128, rppt = 2;        // render threads / pixels per thread group
+    int qs = 1;                    // threads per group splitting the quadrature points
     int ctx = 32, cty = 32, cr = 8; // convolution tile and outputs per thread
     bool pair_rows = false;        // convolution threads own two rows (f32x2)
     int conv_block_y() const { return pair_rows ? cty / 2 : cty; }
+    int rtile() const { return rt / qs * rppt; }  // pixels per render block
+    bool operator==(const Shape& o) const
+    {
+        return rt == o.rt && rppt == o.rppt && qs == o.qs && ctx == o.ctx && cty == o.cty && cr == o.cr &&
+               pair_rows == o.pair_rows;
+    }
+    std::string str() const;
 };
 
 // Compose the NVRTC sources of a model and compile them to cubins for
@@ -143,5 +151,22 @@ std::string compose_multi_source(const Model& m, const std::vector<std::pair<int
                                  const Shape& s, bool strict);
 int compile_program(const std::string& src, bool fmad, std::vector<char>& cubin, std::string& log,
                     bool ieee_divsqrt = true);
+
+// ---------------------------------------------------------------- autotuner
+// Candidate launch shapes around a base shape (lg_tune.cpp): render shapes
+// vary threads, pixels per group and (fast mode) the quadrature split;
+// convolution shapes vary the tile and outputs per thread.
+std::vector<Shape> render_candidates(const Shape& base, bool strict);
+std::vector<Shape> conv_candidates(const Shape& base, bool multi = false);
+// "" when the shape is valid for the program, else the reason.
+std::string check_shape(const Shape& s, bool strict, bool psf, int psfw);
+// Compile several programs at once (NVRTC is thread-safe).
+void compile_parallel(const std::vector<std::string>& srcs, bool fmad, bool ieee,
+                      std::vector<std::vector<char>>& cubins, std::vector<int>& rcs, std::vector<std::string>& logs);
+std::string device_signature(int device);
+std::string tune_key(const std::string& program, int device, int batch, int flags);
+bool tune_cache_get(const std::string& key, Shape& s);
+void tune_cache_put(const std::string& key, const Shape& s);
+void tune_cache_clear();
 
 }  // namespace lg

@@ -139,8 +139,13 @@ int nested_sample(int nd, lg_batch_loglike fn, void* user, const lg_nested_optio
     std::vector<double> live((size_t)nl * nd), llive(nl);
     std::vector<double> buf((size_t)B * nd), lbuf(B);
     long ncall = 0;
+    using clock = std::chrono::steady_clock;
+    double t_eval = 0, t_train = 0, t_prop = 0;
+    auto since = [](clock::time_point t) { return std::chrono::duration<double>(clock::now() - t).count(); };
     auto evaluate = [&](const double* x, int n, double* l) {
+        const auto te = clock::now();
         int rc = fn(user, x, n, l);
+        t_eval += since(te);
         ncall += n;
         return rc;
     };
@@ -195,7 +200,9 @@ int nested_sample(int nd, lg_batch_loglike fn, void* user, const lg_nested_optio
         // learned proposal: (re)train every flow_every replacements
         if (learned && opt.flow_every > 0 && since_train >= opt.flow_every) {
             since_train = 0;
+            const auto tt = clock::now();
             use_flow = learned->train(live.data(), nl, nd) == LG_OK;
+            t_train += since(tt);
             if (std::getenv("LG_FLOW_DEBUG"))
                 std::fprintf(stderr, "flow: iter %ld trained %d, flow batches failed so far %ld\n", iter,
                              (int)use_flow, n_flow_fail);
@@ -217,6 +224,7 @@ int nested_sample(int nd, lg_batch_loglike fn, void* user, const lg_nested_optio
             // propose a batch: the learned proposal when it is trained, the
             // ellipsoid when it is not or when it yields nothing
             int n = 0;
+            const auto tp = clock::now();
             // the ellipsoid bounds the live points other than the one leaving
             std::vector<double> others;
             others.reserve((size_t)(nl - 1) * nd);
@@ -248,6 +256,7 @@ int nested_sample(int nd, lg_batch_loglike fn, void* user, const lg_nested_optio
                     return LG_ERR_INPUT;
                 }
             }
+            t_prop += since(tp);
             if (int rc = evaluate(buf.data(), n, lbuf.data())) {
                 err = "likelihood callback failed";
                 return rc;
@@ -300,6 +309,9 @@ int nested_sample(int nd, lg_batch_loglike fn, void* user, const lg_nested_optio
     res->n_flow_proposals = n_flow;
     res->n_ellipsoid_proposals = n_ell;
     res->wall_s = std::chrono::duration<double>(std::chrono::steady_clock::now() - t0).count();
+    res->eval_s = t_eval;
+    res->train_s = t_train;
+    res->propose_s = t_prop;
     if (res->mean && res->std)
         for (int a = 0; a < nd; ++a) {
             res->mean[a] = mean[a] / wsum;

@@ -9,6 +9,7 @@
 
 #include <nvrtc.h>
 
+#include <atomic>
 #include <cmath>
 #include <cstdio>
 #include <cstdlib>
@@ -156,7 +157,7 @@ std::string compose_source(const Model& m, const Shape& s, bool strict, Part par
     for (const auto& ob : m.objs) o << " " << ob.id << "=" << ob.plugin->name;
     o << "\n// image " << m.width << "x" << m.height << ", rule " << m.rule->name << " (" << m.rule->size
       << " points), PSF " << m.psfw << "x" << m.psfh << (strict ? ", strict FP" : "") << "\n\n";
-    o << "#define LG_RT " << s.rt << "\n#define LG_RPPT " << s.rppt << "\n";
+    o << "#define LG_RT " << s.rt << "\n#define LG_RPPT " << s.rppt << "\n#define LG_QS " << s.qs << "\n";
     o << "#define LG_CTX " << s.ctx << "\n#define LG_CTY " << s.cty << "\n#define LG_CR " << s.cr << "\n\n";
     o << prelude_source() << "\n";
     if (set || strict) o << crmath_source() << "\n";
@@ -222,7 +223,7 @@ std::string compose_multi_source(const Model& m, const std::vector<std::pair<int
     for (const auto& ob : m.objs) o << " " << ob.id << "=" << ob.plugin->name;
     o << "\n// rule " << m.rule->name << " (" << m.rule->size << " points)" << (strict ? ", strict FP" : "")
       << "\n\n";
-    o << "#define LG_RT " << s.rt << "\n#define LG_RPPT " << s.rppt << "\n";
+    o << "#define LG_RT " << s.rt << "\n#define LG_RPPT " << s.rppt << "\n#define LG_QS " << s.qs << "\n";
     o << "#define LG_CTX " << s.ctx << "\n#define LG_CTY " << s.cty << "\n#define LG_CR " << s.cr << "\n\n";
     o << prelude_source() << "\n";
     if (strict) o << crmath_source() << "\n";
@@ -268,7 +269,7 @@ int compile_program(const std::string& src, bool fmad, std::vector<char>& cubin,
     opts.push_back(ieee_divsqrt ? "--prec-sqrt=true" : "--prec-sqrt=false");
     opts.push_back(fmad ? "--fmad=true" : "--fmad=false");
     if (const char* dump = std::getenv("LG_NVRTC_DUMP")) {
-        static int seq = 0;
+        static std::atomic<int> seq{0};
         std::string path = std::string(dump) + "." + std::to_string(seq++) + ".cu";
         if (FILE* f = std::fopen(path.c_str(), "w")) {
             std::fputs(src.c_str(), f);

@@ -5,8 +5,8 @@
 //   LG_RX, LG_RY, LG_SX, LG_SY pixel coordinate system (after the even-PSF shift)
 //   LG_HAS_PSF, LG_PSF_W, LG_PSF_H, lg_psf[] (normalised PSF, constant)
 //   LG_NPARS, lg_model, lg_compute()
-// and the launch-shape parameters LG_RT, LG_RPPT (render) and LG_CTX, LG_CTY,
-// LG_CR (convolution).
+// and the launch-shape parameters LG_RT, LG_RPPT, LG_QS (render) and LG_CTX,
+// LG_CTY, LG_CR (convolution).
 //
 // Data layout in HBM, per context:
 //   models   lg_model[B]              object data of each candidate
@@ -25,8 +25,17 @@
 #ifndef LG_RPPT
 #define LG_RPPT 2
 #endif
-#define LG_RTILE (LG_RT * LG_RPPT)
+// quadrature split: LG_QS adjacent threads share a thread's pixels, each
+// taking every LG_QS-th quadrature point (fast mode only: the split changes
+// the order of the quadrature sum)
+#ifndef LG_QS
+#define LG_QS 1
+#endif
+#define LG_RG (LG_RT / LG_QS)
+#define LG_RTILE (LG_RG * LG_RPPT)
 #define LG_RTILES ((LG_N + LG_RTILE - 1) / LG_RTILE)
+static_assert(LG_QS == 1 || LG_QS == 2 || LG_QS == 4, "quadrature split of 1, 2 or 4 threads");
+static_assert(LG_RT % 32 == 0, "render block of whole warps");
 
 // ------------------------------------------------------------ reductions --
 LG_DEV double lg_warp_sum(double v)
@@ -54,18 +63,29 @@ LG_DEV double lg_block_sum(double v, double* red)
 }
 
 // ---------------------------------------------------------------- render --
-// kernel/lensed.cl:9-39.  Block (tile, candidate); each thread integrates
-// LG_RPPT pixels over the quadrature rule: strided by LG_RT in the scalar
-// kernel (so that loads and stores coalesce), adjacent in the paired kernel
-// (a thread's two rays are neighbours, so they mostly take the same
-// branches; stores are float2).  MODE 0 stores the raw model, MODE 1 reduces
-// the chi^2 directly (no PSF), MODE 2 stores value and error for one
+// kernel/lensed.cl:9-39.  Block (tile, candidate); each group of LG_QS
+// threads integrates LG_RPPT pixels over the quadrature rule: strided by the
+// group count in the scalar kernel (so that loads and stores coalesce),
+// adjacent in the paired kernel (a thread's two rays are neighbours, so they
+// mostly take the same branches; stores are float2).  With LG_QS > 1 the
+// threads of a group take quadrature points n = sub, sub + LG_QS, ... and
+// their sums are combined by a butterfly of shuffles (every lane ends with
+// the same, order-independent result).  MODE 0 stores the raw model, MODE 1
+// reduces the chi^2 directly (no PSF), MODE 2 stores value and error for one
 // candidate.
 #if defined(LG_PAIRED) && LG_RPPT % 2 == 0
 #define LG_PIX(t, j) (LG_RPPT * (t) + (j))
 #else
-#define LG_PIX(t, j) ((t) + (j) * LG_RT)
+#define LG_PIX(t, j) ((t) + (j) * LG_RG)
 #endif
+
+// sum of v over the LG_QS lanes of a quadrature group
+LG_DEV float lg_qs_sum(float v)
+{
+#pragma unroll
+    for (int o = 1; o < LG_QS; o <<= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
+    return v;
+}
 template <int MODE>
 LG_DEV void lg_render_tile(const lg_model* __restrict__ models, float* __restrict__ out, float* __restrict__ err,
                            const float* __restrict__ image, const float* __restrict__ weight,
@@ -74,11 +94,12 @@ LG_DEV void lg_render_tile(const lg_model* __restrict__ models, float* __restric
     const int b = blockIdx.y;
     const lg_model m = models[b];
     const int base = blockIdx.x * LG_RTILE;
+    const int grp = threadIdx.x / LG_QS, sub = threadIdx.x % LG_QS;
     float2 xp[LG_RPPT];
     float v[LG_RPPT], e[LG_RPPT];
 #pragma unroll
     for (int j = 0; j < LG_RPPT; ++j) {
-        int k = base + LG_PIX(threadIdx.x, j);
+        int k = base + LG_PIX(grp, j);
         k = k < LG_N ? k : LG_N - 1;
         xp[j] = make_float2(LG_RX + LG_SX * (float)(k % LG_W), LG_RY + LG_SY * (float)(k / LG_W));
         v[j] = 0.0f;
@@ -96,7 +117,7 @@ LG_DEV void lg_render_tile(const lg_model* __restrict__ models, float* __restric
         pe[j] = lg_pair_of(0.0f);
     }
 #pragma unroll 1
-    for (int n = 0; n < LG_Q; ++n) {
+    for (int n = sub; n < LG_Q; n += LG_QS) {
         const float2 q = lg_qq[n];
         const float2 w = lg_ww[n];
 #pragma unroll
@@ -115,7 +136,7 @@ LG_DEV void lg_render_tile(const lg_model* __restrict__ models, float* __restric
     }
 #else
 #pragma unroll 1
-    for (int n = 0; n < LG_Q; ++n) {
+    for (int n = sub; n < LG_Q; n += LG_QS) {
         const float2 q = lg_qq[n];
         const float2 w = lg_ww[n];
 #pragma unroll
@@ -126,13 +147,20 @@ LG_DEV void lg_render_tile(const lg_model* __restrict__ models, float* __restric
         }
     }
 #endif
+    if (LG_QS > 1) {
+#pragma unroll
+        for (int j = 0; j < LG_RPPT; ++j) {
+            v[j] = lg_qs_sum(v[j]);
+            if (MODE == 2) e[j] = lg_qs_sum(e[j]);
+        }
+    }
     if (MODE == 1) {
         __shared__ double red[LG_RT / 32];
         double s = 0.0;
 #pragma unroll
         for (int j = 0; j < LG_RPPT; ++j) {
-            const int k = base + LG_PIX(threadIdx.x, j);
-            if (k < LG_N) {
+            const int k = base + LG_PIX(grp, j);
+            if (sub == 0 && k < LG_N) {
                 const float d = v[j] - image[k];
                 s += (double)(weight[k] * d * d);
             }
@@ -145,8 +173,8 @@ LG_DEV void lg_render_tile(const lg_model* __restrict__ models, float* __restric
         // pair's address is 8-byte aligned)
 #pragma unroll
         for (int j = 0; j < LG_RPPT; j += 2) {
-            const int k = base + LG_PIX(threadIdx.x, j);
-            if (k < LG_N) {
+            const int k = base + LG_PIX(grp, j);
+            if (sub == 0 && k < LG_N) {
                 *reinterpret_cast<float2*>(out + (size_t)b * LG_N + k) = make_float2(v[j], v[j + 1]);
                 if (MODE == 2) *reinterpret_cast<float2*>(err + (size_t)b * LG_N + k) = make_float2(e[j], e[j + 1]);
             }
@@ -154,8 +182,8 @@ LG_DEV void lg_render_tile(const lg_model* __restrict__ models, float* __restric
 #else
 #pragma unroll
         for (int j = 0; j < LG_RPPT; ++j) {
-            const int k = base + LG_PIX(threadIdx.x, j);
-            if (k < LG_N) {
+            const int k = base + LG_PIX(grp, j);
+            if (sub == 0 && k < LG_N) {
                 out[(size_t)b * LG_N + k] = v[j];
                 if (MODE == 2) err[(size_t)b * LG_N + k] = e[j];
             }

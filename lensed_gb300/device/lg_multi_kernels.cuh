@@ -17,7 +17,14 @@
 #ifndef LG_RPPT
 #define LG_RPPT 2
 #endif
-#define LG_RTILE (LG_RT * LG_RPPT)
+// quadrature split (fast mode only), as in the single-system render kernel
+#ifndef LG_QS
+#define LG_QS 1
+#endif
+#define LG_RG (LG_RT / LG_QS)
+#define LG_RTILE (LG_RG * LG_RPPT)
+static_assert(LG_QS == 1 || LG_QS == 2 || LG_QS == 4, "quadrature split of 1, 2 or 4 threads");
+static_assert(LG_RT % 32 == 0, "render block of whole warps");
 #ifndef LG_CTX
 #define LG_CTX 32
 #endif
@@ -79,13 +86,22 @@ LG_DEV double lg_block_sum(double v, double* red)
 
 // ------------------------------------------------------------- render --
 // WITH_PSF: store raw models; else reduce the chi^2 of each tile directly.
-// Pixels of a thread as in the single-system kernel: adjacent in the paired
-// kernel, strided by LG_RT otherwise.
+// Pixels of a thread group as in the single-system kernel: adjacent in the
+// paired kernel, strided by the group count otherwise; LG_QS threads of a
+// group split the quadrature points and combine their sums by shuffles.
 #if defined(LG_PAIRED) && LG_RPPT % 2 == 0
 #define LG_MPIX(t, j) (LG_RPPT * (t) + (j))
 #else
-#define LG_MPIX(t, j) ((t) + (j) * LG_RT)
+#define LG_MPIX(t, j) ((t) + (j) * LG_RG)
 #endif
+
+LG_DEV float lg_qs_sum(float v)
+{
+#pragma unroll
+    for (int o = 1; o < LG_QS; o <<= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
+    return v;
+}
+
 template <bool WITH_PSF>
 LG_DEV void lg_multi_render_body(const lg_model* __restrict__ models, const lg_sysinfo* __restrict__ info,
                                  const lg_sysplan* __restrict__ plan, const long long* __restrict__ hdr,
@@ -95,6 +111,7 @@ LG_DEV void lg_multi_render_body(const lg_model* __restrict__ models, const lg_s
     __shared__ double red[LG_RT / 32];
     const long long U = hdr[0];
     const int nsys = (int)hdr[3];
+    const int grp = threadIdx.x / LG_QS, sub = threadIdx.x % LG_QS;
     for (long long u = blockIdx.x; u < U; u += gridDim.x) {
         const int s = lg_find_system(plan, nsys, u, false);
         const lg_sysinfo I = info[s];
@@ -107,7 +124,7 @@ LG_DEV void lg_multi_render_body(const lg_model* __restrict__ models, const lg_s
         float v[LG_RPPT];
 #pragma unroll
         for (int j = 0; j < LG_RPPT; ++j) {
-            int k = base + LG_MPIX(threadIdx.x, j);
+            int k = base + LG_MPIX(grp, j);
             k = k < I.N ? k : I.N - 1;
             xp[j] = make_float2(I.rx + I.sx * (float)(k % I.W), I.ry + I.sy * (float)(k / I.W));
             v[j] = 0.0f;
@@ -122,7 +139,7 @@ LG_DEV void lg_multi_render_body(const lg_model* __restrict__ models, const lg_s
             pv[j] = lg_pair_of(0.0f);
         }
 #pragma unroll 1
-        for (int n = 0; n < LG_Q; ++n) {
+        for (int n = sub; n < LG_Q; n += LG_QS) {
             const float2 q = lg_qq[n];
             const float2 w = lg_ww[n];
 #pragma unroll
@@ -135,25 +152,29 @@ LG_DEV void lg_multi_render_body(const lg_model* __restrict__ models, const lg_s
         }
 #else
 #pragma unroll 1
-        for (int n = 0; n < LG_Q; ++n) {
+        for (int n = sub; n < LG_Q; n += LG_QS) {
             const float2 q = lg_qq[n];
             const float2 w = lg_ww[n];
 #pragma unroll
             for (int j = 0; j < LG_RPPT; ++j) v[j] += w.x * lg_compute(m, xp[j] + q);
         }
 #endif
+        if (LG_QS > 1) {
+#pragma unroll
+            for (int j = 0; j < LG_RPPT; ++j) v[j] = lg_qs_sum(v[j]);
+        }
         if (WITH_PSF) {
 #pragma unroll
             for (int j = 0; j < LG_RPPT; ++j) {
-                const int k = base + LG_MPIX(threadIdx.x, j);
-                if (k < I.N) raw[P.raw0 + (long long)b * I.N + k] = v[j];
+                const int k = base + LG_MPIX(grp, j);
+                if (sub == 0 && k < I.N) raw[P.raw0 + (long long)b * I.N + k] = v[j];
             }
         } else {
             double acc = 0.0;
 #pragma unroll
             for (int j = 0; j < LG_RPPT; ++j) {
-                const int k = base + LG_MPIX(threadIdx.x, j);
-                if (k < I.N) {
+                const int k = base + LG_MPIX(grp, j);
+                if (sub == 0 && k < I.N) {
                     const float d = v[j] - images[I.img_off + k];
                     acc += (double)(weights[I.img_off + k] * d * d);
                 }
