@@ -364,6 +364,10 @@ typedef struct {
     int batch;      /* training batch (default 256) */
     double lr;      /* Adam learning rate (default 1e-3) */
     double expand;  /* latent radius enlargement over the live points (default 1.1) */
+    int patience;   /* epochs without held-out improvement before a retraining stops (default 10) */
+    int lag;        /* replacements after a retraining starts at which the new flow takes over
+                       (default 500): the retraining runs on its own stream meanwhile, and the
+                       sampler waits for it there if it has not finished */
 } lg_flow_options;
 
 typedef int (*lg_batch_loglike)(void* user, const double* cube, int B, double* logL);
@@ -378,6 +382,13 @@ int lg_nested_sample(int ndims, lg_batch_loglike fn, void* user, const lg_nested
 long lg_flow_nparams(int d, int layers, int width, int hidden);
 int lg_flow_loss_grad(int device, int d, int layers, int width, int hidden, int bf16, const float* params,
                       const float* x, int n, float* loss, float* grad);
+/* One retraining of the learned proposal on n points (n x d, row-major),
+ * as the sampler does it on its live points: history receives the held-out
+ * loss before training and after each epoch (NaN past the last epoch run);
+ * returns the epochs run (negative: error); *efficiency = calibrated kept
+ * fraction of latent draws. */
+int lg_flow_fit(int device, int d, const lg_flow_options* opts, const double* pts, int n, float* history,
+                int max_history, double* efficiency);
 /* lg_nested_sample with the learned proposal on the given CUDA device. */
 int lg_nested_sample_flow(int ndims, lg_batch_loglike fn, void* user, const lg_nested_options* opts,
                           const lg_flow_options* flow, int device, lg_nested_result* result);

@@ -69,7 +69,8 @@ class NestedResult(C.Structure):
 
 class FlowOptions(C.Structure):
     _fields_ = [("layers", C.c_int), ("width", C.c_int), ("hidden", C.c_int), ("epochs", C.c_int),
-                ("batch", C.c_int), ("lr", C.c_double), ("expand", C.c_double)]
+                ("batch", C.c_int), ("lr", C.c_double), ("expand", C.c_double), ("patience", C.c_int),
+                ("lag", C.c_int)]
 
 
 BATCH_LOGLIKE = C.CFUNCTYPE(C.c_int, C.c_void_p, C.POINTER(C.c_double), C.c_int, C.POINTER(C.c_double))
@@ -149,6 +150,7 @@ def lib():
         "lg_nested_run": (C.c_int, [vp, C.POINTER(NestedOptions), C.POINTER(FlowOptions),
                                     C.POINTER(NestedResult)]),
         "lg_flow_nparams": (C.c_long, [C.c_int, C.c_int, C.c_int, C.c_int]),
+        "lg_flow_fit": (C.c_int, [C.c_int, C.c_int, C.POINTER(FlowOptions), dp, C.c_int, fp, C.c_int, dp]),
         "lg_flow_loss_grad": (C.c_int, [C.c_int, C.c_int, C.c_int, C.c_int, C.c_int, C.c_int, fp, fp, C.c_int,
                                         fp, fp]),
         "loglike": (None, [dp, ip, ip, dp, vp]),
@@ -254,6 +256,21 @@ def _pack(r, arrays):
             "n_flow_proposals": r.n_flow_proposals, "n_ellipsoid_proposals": r.n_ellipsoid_proposals,
             "mean": arrays["mean"], "std": arrays["std"], "samples": arrays["samples"][:n],
             "logwt": arrays["logwt"][:n]}
+
+
+def flow_fit(points, device: int = 0, **flow):
+    """One retraining of the learned proposal on points (n, d), as the
+    sampler retrains on its live points: returns (held-out loss before
+    training and after each epoch, calibrated kept fraction)."""
+    x = np.ascontiguousarray(points, dtype=np.float64)
+    hist = np.full(256, np.nan, np.float32)
+    eff = C.c_double()
+    fo = _flow_opts(**flow)
+    rc = lib().lg_flow_fit(device, x.shape[1], C.byref(fo), _p(x, C.c_double), x.shape[0], _p(hist, C.c_float),
+                           hist.size, C.byref(eff))
+    if rc < 0:
+        raise LensedError(rc, lib().lg_last_error(None).decode(errors="replace"))
+    return hist[: rc + 1], eff.value
 
 
 def nested_sample(loglike, ndims: int, max_samples: int = 200000, **opts):

@@ -10,9 +10,28 @@
 // with s = c * tanh(s_raw / c) (c = LG_FLOW_CLAMP) and (s_raw, t) from an MLP
 // conditioner (width W, `hidden` ReLU layers, zero-initialised output layer so
 // training starts from the identity).  log p(x) = log N(z; 0, I) + sum s
-// - sum log s_std.  Weights and gradients are FP32; hidden activations are
-// stored in BF16 for the backward pass (the BF16 variant can be switched off
-// to check gradients against the CPU restatement).
+// - sum log s_std.  Weights, gradients and optimiser state are FP32; hidden
+// activations are rounded to BF16 as they are produced (the next layer and
+// the backward pass use the rounded values; the BF16 variant can be switched
+// off to check gradients against the CPU restatement).
+//
+// Kernels (all the flow's work for one step is one launch):
+//   lg_flow_step   a block takes FR rows of a minibatch through every
+//                  coupling layer and back: forward, loss, backward, and the
+//                  block's partial weight gradients (its rows' sums) into
+//                  its own slice of a partial-gradient buffer;
+//   lg_flow_adam   sums the blocks' slices in a fixed order (deterministic)
+//                  and takes an Adam step;
+//   lg_flow_check  held-out loss in a fixed order; keeps the best weights
+//                  and stops training after `patience` epochs without
+//                  improvement -- on the device, so a whole retraining is
+//                  issued without a host synchronisation (later launches of
+//                  a stopped training return at once);
+//   lg_flow_inverse  latent points back to the cube through every layer;
+//   lg_flow_latent / _accept / _compact  proposals: uniform draws in the
+//                  latent ball (counter-based RNG, Box-Muller), the
+//                  rejection test against the calibrated weight bound, the
+//                  unit-cube test and an order-preserving compaction.
 //
 // Proposals (as nessai, Williams et al. 2021): z uniform in a ball of radius
 // `expand` x the largest latent radius of the live points, mapped back to the
@@ -40,174 +59,701 @@
 #include "lg_nested.h"
 
 #define LG_FLOW_CLAMP 5.0f
+#define LG_FLOW_HISTORY 256
 
 namespace lg {
 namespace {
 
-constexpr int TS = 32;  // GEMM tile
+constexpr int FT = 256;        // threads per block of the fused kernels
+constexpr int FR = 8;          // minibatch rows per training block
+constexpr int FRI = 32;        // rows per inverse block
+constexpr int MAX_W = 128;     // conditioner width limit (shared-memory tiles)
+constexpr int MAX_D = 64;      // dimension limit
+constexpr int MAX_DENSE = 64;  // coupling layers x dense layers limit
 
 __device__ __forceinline__ float to_f(float v) { return v; }
 __device__ __forceinline__ float to_f(__nv_bfloat16 v) { return __bfloat162float(v); }
 __device__ __forceinline__ void from_f(float& d, float v) { d = v; }
 __device__ __forceinline__ void from_f(__nv_bfloat16& d, float v) { d = __float2bfloat16_rn(v); }
 
-// C = act(op(A) op(B) + bias) [* (mask > 0)] [+ C]
-// op(A)(m, k) = ta ? A[k * lda + m] : A[m * lda + k]; op(B)(k, n) likewise.
-// 16 x 16 threads, 2 x 2 outputs each, 32 x 32 tiles staged in shared memory.
-template <typename TA, typename TB, typename TC, typename TM>
-__global__ void __launch_bounds__(256) gemm(const TA* __restrict__ A, int lda, int ta, const TB* __restrict__ B,
-                                            int ldb, int tb, TC* __restrict__ C, int ldc, int M, int N, int K,
-                                            const float* __restrict__ bias, int relu, const TM* __restrict__ mask,
-                                            int accumulate)
+// Shape of a flow, passed by value to the kernels.
+struct FlowDims {
+    int d, h, L, W, NH;
+    __host__ __device__ int da(int l) const { return (l % 2 == 0) ? h : d - h; }
+    __host__ __device__ int a0(int l) const { return (l % 2 == 0) ? 0 : h; }
+    __host__ __device__ int db(int l) const { return d - da(l); }
+    __host__ __device__ int b0(int l) const { return (l % 2 == 0) ? h : 0; }
+    __host__ __device__ int kin(int l, int k) const { return k == 0 ? da(l) : W; }
+    __host__ __device__ int kout(int l, int k) const { return k == NH ? 2 * db(l) : W; }
+    __host__ __device__ int dbmax() const { return d - h; }
+};
+
+// Parameter offsets of every dense layer: weights [kin][kout] row-major, then
+// the bias [kout], layer by layer (the layout of the CPU restatement).
+__device__ void fill_offsets(const FlowDims& f, int* offs)
 {
-    __shared__ float As[TS][TS + 1], Bs[TS][TS + 1];
-    const int tx = threadIdx.x, ty = threadIdx.y, tid = ty * 16 + tx;
-    const int row0 = blockIdx.y * TS, col0 = blockIdx.x * TS;
-    float acc[2][2] = {{0, 0}, {0, 0}};
-    for (int k0 = 0; k0 < K; k0 += TS) {
-        for (int e = tid; e < TS * TS; e += 256) {
-            const int i = e / TS, j = e % TS;
-            const int m = row0 + i, k = k0 + j;
-            As[i][j] = (m < M && k < K) ? to_f(ta ? A[(size_t)k * lda + m] : A[(size_t)m * lda + k]) : 0.0f;
-            const int kb = k0 + i, n = col0 + j;
-            Bs[i][j] = (kb < K && n < N) ? to_f(tb ? B[(size_t)n * ldb + kb] : B[(size_t)kb * ldb + n]) : 0.0f;
+    if (threadIdx.x == 0) {
+        int n = 0;
+        for (int l = 0; l < f.L; ++l)
+            for (int k = 0; k <= f.NH; ++k) {
+                offs[2 * (l * (f.NH + 1) + k)] = n;
+                n += f.kin(l, k) * f.kout(l, k);
+                offs[2 * (l * (f.NH + 1) + k) + 1] = n;
+                n += f.kout(l, k);
+            }
+    }
+    __syncthreads();
+}
+
+// Asynchronous 4-byte global -> shared copies (no registers held while in
+// flight, so a thread's whole share of a weight matrix is requested at once).
+__device__ __forceinline__ void cp_async4(float* dst, const float* src)
+{
+    const unsigned d = (unsigned)__cvta_generic_to_shared(dst);
+    asm volatile("cp.async.ca.shared.global [%0], [%1], 4;\n" ::"r"(d), "l"(src) : "memory");
+}
+__device__ __forceinline__ void cp_async_wait_all() { asm volatile("cp.async.wait_all;\n" ::: "memory"); }
+
+// Stage a K x N row-major weight matrix into shared memory: Ws[k][n] (pitch
+// N) or, transposed, Ws[n][k] (pitch K + 1, conflict-free both ways).
+__device__ void stage_weights(float* Ws, const float* __restrict__ Wg, int K, int N, bool transpose)
+{
+    const int pk = K + 1;
+    for (int e = threadIdx.x; e < K * N; e += FT) {
+        const int k = e / N, n = e - k * N;
+        cp_async4(transpose ? Ws + n * pk + k : Ws + e, Wg + e);
+    }
+    cp_async_wait_all();
+    __syncthreads();
+}
+
+// Y[r][n] = act(sum_k X[r][k] W[k][n] + b[n]) for R rows (X, Y in shared
+// memory, W staged into Ws).  Micro-tile per thread: CPT adjacent columns
+// (LANES column slots) x R / (FT / LANES) rows, all compile-time so that the
+// accumulators stay in registers; the k loop runs in order with FP32
+// accumulation (rows read four k at a time when their pitch allows), then
+// the bias and the ReLU.  With Hs, the result is also rounded to TH (stored
+// there and written back to Y as the rounded value).
+template <int R, int LANES, int CPT, typename TH>
+__device__ void dense_fwd_tile(const float* X, int ldx, int K, const float* Ws, const float* __restrict__ bg, int N,
+                               bool relu, float* Y, int ldy, TH* Hs)
+{
+    constexpr int GROUPS = FT / LANES, RPT = R / GROUPS;
+    static_assert(R % GROUPS == 0, "rows per block must split over the thread groups");
+    const int lane = threadIdx.x % LANES, g = threadIdx.x / LANES;
+    const float* x0 = X + g * RPT * ldx;
+    const bool vec = (ldx % 4) == 0;
+    for (int c = lane * CPT; c < N; c += LANES * CPT) {
+        float acc[RPT][CPT];
+#pragma unroll
+        for (int i = 0; i < RPT; ++i)
+#pragma unroll
+            for (int j = 0; j < CPT; ++j) acc[i][j] = 0.0f;
+        int k = 0;
+        if (vec)
+            for (; k + 3 < K; k += 4) {
+                float w[4][CPT];
+#pragma unroll
+                for (int q = 0; q < 4; ++q) {
+                    if (CPT == 2) {
+                        const float2 t = *reinterpret_cast<const float2*>(Ws + (k + q) * N + c);
+                        w[q][0] = t.x;
+                        w[q][CPT - 1] = t.y;
+                    } else {
+                        w[q][0] = Ws[(k + q) * N + c];
+                    }
+                }
+#pragma unroll
+                for (int i = 0; i < RPT; ++i) {
+                    const float4 xv = *reinterpret_cast<const float4*>(x0 + i * ldx + k);
+#pragma unroll
+                    for (int j = 0; j < CPT; ++j) {
+                        float a = acc[i][j];
+                        a += xv.x * w[0][j];
+                        a += xv.y * w[1][j];
+                        a += xv.z * w[2][j];
+                        a += xv.w * w[3][j];
+                        acc[i][j] = a;
+                    }
+                }
+            }
+        for (; k < K; ++k) {
+#pragma unroll
+            for (int j = 0; j < CPT; ++j) {
+                const float w = Ws[k * N + c + j];
+#pragma unroll
+                for (int i = 0; i < RPT; ++i) acc[i][j] += x0[i * ldx + k] * w;
+            }
+        }
+#pragma unroll
+        for (int j = 0; j < CPT; ++j) {
+            const float b = __ldg(bg + c + j);
+#pragma unroll
+            for (int i = 0; i < RPT; ++i) {
+                const int r = g * RPT + i;
+                float v = acc[i][j] + b;
+                if (relu) v = v > 0.0f ? v : 0.0f;
+                if (Hs) {
+                    from_f(Hs[r * N + c + j], v);
+                    v = to_f(Hs[r * N + c + j]);
+                }
+                Y[r * ldy + c + j] = v;
+            }
+        }
+    }
+}
+
+template <int R, typename TH>
+__device__ void dense_fwd(const float* X, int ldx, int K, const float* __restrict__ Wg, const float* __restrict__ bg,
+                          int N, bool relu, float* Y, int ldy, TH* Hs, float* Ws)
+{
+    stage_weights(Ws, Wg, K, N, false);
+    if (N >= 128 && N % 2 == 0)
+        dense_fwd_tile<R, 64, 2, TH>(X, ldx, K, Ws, bg, N, relu, Y, ldy, Hs);
+    else if (N >= 64 && N % 2 == 0)
+        dense_fwd_tile<R, 32, 2, TH>(X, ldx, K, Ws, bg, N, relu, Y, ldy, Hs);
+    else
+        dense_fwd_tile<R, 32, 1, TH>(X, ldx, K, Ws, bg, N, relu, Y, ldy, Hs);
+    __syncthreads();
+}
+
+// dX[r][k] = sum_n dY[r][n] W[k][n] from the transposed weights WT[n][k]
+// (pitch K + 1), masked by X > 0 when mask_relu; thread column k, R /
+// (FT / LANES) rows per thread (compile-time).
+template <int R, int LANES, typename TX>
+__device__ void dense_dx(const TX* X, int ldx, int K, const float* dY, int ldy, int N, const float* WT, float* dX,
+                         int lddx, bool mask_relu)
+{
+    constexpr int GROUPS = FT / LANES, RPT = R / GROUPS;
+    static_assert(R % GROUPS == 0, "rows per block must split over the thread groups");
+    const int pk = K + 1, g = threadIdx.x / LANES;
+    const float* y0 = dY + g * RPT * ldy;
+    for (int k = threadIdx.x % LANES; k < K; k += LANES) {
+        float acc[RPT];
+#pragma unroll
+        for (int i = 0; i < RPT; ++i) acc[i] = 0.0f;
+        for (int n = 0; n < N; ++n) {
+            const float w = WT[n * pk + k];
+#pragma unroll
+            for (int i = 0; i < RPT; ++i) acc[i] += y0[i * ldy + n] * w;
+        }
+#pragma unroll
+        for (int i = 0; i < RPT; ++i) {
+            const int r = g * RPT + i;
+            float v = acc[i];
+            if (mask_relu && !(to_f(X[r * ldx + k]) > 0.0f)) v = 0.0f;
+            dX[r * lddx + k] = v;
+        }
+    }
+}
+
+// Backward of a dense layer for R rows: partial weight and bias gradients
+// of this block's rows (written to gW, gb: the block's slice), and
+// dX[r][k] = sum_n dY[r][n] W[k][n], masked by X > 0 when mask_relu (the
+// input was a ReLU output).  X is read as TH (stored activations) or float.
+template <int R, typename TX>
+__device__ void dense_bwd(const TX* X, int ldx, int K, const float* dY, int ldy, int N, const float* __restrict__ Wg,
+                          float* __restrict__ gW, float* __restrict__ gb, float* dX, int lddx, bool mask_relu,
+                          float* WT)
+{
+    // W transposed, WT[n][k] (requested now, waited for before dX)
+    const int pk = K + 1;
+    if (dX)
+        for (int e = threadIdx.x; e < K * N; e += FT) {
+            const int k = e / N, n = e - k * N;
+            cp_async4(WT + n * pk + k, Wg + e);
+        }
+    // weight gradient: thread column n, all R rows of dY in registers
+    int lanes = 32;
+    while (lanes < N && lanes < FT) lanes <<= 1;
+    int groups = FT / lanes;
+    for (int n = threadIdx.x % lanes; n < N; n += lanes) {
+        float dy[R];
+#pragma unroll
+        for (int r = 0; r < R; ++r) dy[r] = dY[r * ldy + n];
+        for (int k = threadIdx.x / lanes; k < K; k += groups) {
+            float acc = 0.0f;
+#pragma unroll
+            for (int r = 0; r < R; ++r) acc += to_f(X[r * ldx + k]) * dy[r];
+            gW[(size_t)k * N + n] = acc;
+        }
+        if (threadIdx.x / lanes == 0) {
+            float acc = 0.0f;
+#pragma unroll
+            for (int r = 0; r < R; ++r) acc += dy[r];
+            gb[n] = acc;
+        }
+    }
+    cp_async_wait_all();
+    __syncthreads();
+    // input gradient: thread column k, rows split over the groups
+    if (dX) {
+        if (K >= 64)
+            dense_dx<R, 64>(X, ldx, K, dY, ldy, N, WT, dX, lddx, mask_relu);
+        else
+            dense_dx<R, 32>(X, ldx, K, dY, ldy, N, WT, dX, lddx, mask_relu);
+    }
+    __syncthreads();
+}
+
+// Shared-memory layout of lg_flow_step for R rows (floats unless noted).
+struct StepSmem {
+    int us, os, ld, xa, a, b, da, db, wt, dv, du, hs, offs, total;
+    __host__ __device__ StepSmem(const FlowDims& f, int R, int hbytes)
+    {
+        int o = 0;
+        auto take = [&](int n) {
+            const int at = o;
+            o += (n + 3) / 4 * 4;
+            return at;
+        };
+        us = take((f.L + 1) * R * f.d);
+        os = take(f.L * R * 2 * f.dbmax());
+        ld = take(R);
+        // work rows: hidden activations (W wide), conditioner outputs and
+        // their gradients (2 dbmax wide)
+        const int wr = f.W > 2 * f.dbmax() ? f.W : 2 * f.dbmax();
+        xa = take(R * f.dbmax());
+        a = take(R * wr);
+        b = take(R * wr);
+        da = take(R * wr);
+        db = take(R * wr);
+        wt = take(f.W * (f.W + 1) > 2 * f.dbmax() * (f.W + 1) ? f.W * (f.W + 1) : 2 * f.dbmax() * (f.W + 1));
+        dv = take(R * f.d);
+        du = take(R * f.d);
+        offs = take(2 * (f.L * (f.NH + 1)));
+        hs = o;  // TH activations: L x NH x R x W
+        total = o * 4 + ((f.L * f.NH * R * f.W * hbytes + 15) / 16) * 16;
+    }
+};
+
+// One training step (or a forward evaluation, grad = 0) of the flow on rows
+// idx[row0 + r] (or row0 + r when idx is NULL) of X (n x d, standardised),
+// R rows per block, M rows in the minibatch.  Writes per-row losses
+// 0.5 |z|^2 - logdet (loss), optionally |z|^2 (znorm2), and with grad the
+// block's partial gradient slice gpart[blockIdx.x][nparams].
+template <int R, typename TH>
+__global__ void __launch_bounds__(FT)
+    lg_flow_step(FlowDims f, const float* __restrict__ P, const float* __restrict__ X,
+                 const int* __restrict__ idx, int row0, int M, int grad, float* __restrict__ loss,
+                 float* __restrict__ znorm2, float* __restrict__ gpart, long nparams, const int* __restrict__ stop)
+{
+    if (stop && *stop) return;
+    extern __shared__ float4 smem4[];
+    float* sm = reinterpret_cast<float*>(smem4);
+    const StepSmem L(f, R, (int)sizeof(TH));
+    float* Us = sm + L.us;
+    float* Os = sm + L.os;
+    float* ld = sm + L.ld;
+    float* xa = sm + L.xa;
+    float* A = sm + L.a;
+    float* B = sm + L.b;
+    float* dA = sm + L.da;
+    float* dB = sm + L.db;
+    float* WT = sm + L.wt;
+    float* dv = sm + L.dv;
+    float* du = sm + L.du;
+    int* offs = reinterpret_cast<int*>(sm + L.offs);
+    TH* Hs = reinterpret_cast<TH*>(sm + L.hs);
+    const int d = f.d, W = f.W, NH = f.NH, nd = NH + 1, dbm = f.dbmax();
+    fill_offsets(f, offs);
+    const int base = blockIdx.x * R;
+    // rows beyond M are zero inputs; their loss and gradient are dropped
+    for (int e = threadIdx.x; e < R * d; e += FT) {
+        const int r = e / d, j = e - r * d;
+        const int m = base + r;
+        Us[e] = m < M ? X[(size_t)(idx ? idx[row0 + m] : row0 + m) * d + j] : 0.0f;
+    }
+    if (threadIdx.x < R) ld[threadIdx.x] = 0.0f;
+    __syncthreads();
+    // ---- forward
+    for (int l = 0; l < f.L; ++l) {
+        const int da = f.da(l), db = f.db(l), a0 = f.a0(l), b0 = f.b0(l);
+        const float* u = Us + l * R * d;
+        for (int e = threadIdx.x; e < R * da; e += FT) {
+            const int r = e / da, j = e - r * da;
+            xa[r * dbm + j] = u[r * d + a0 + j];
         }
         __syncthreads();
-#pragma unroll 8
-        for (int kk = 0; kk < TS; ++kk) {
-            const float a0 = As[ty * 2][kk], a1 = As[ty * 2 + 1][kk];
-            const float b0 = Bs[kk][tx * 2], b1 = Bs[kk][tx * 2 + 1];
-            acc[0][0] += a0 * b0;
-            acc[0][1] += a0 * b1;
-            acc[1][0] += a1 * b0;
-            acc[1][1] += a1 * b1;
+        const int* of = offs + 2 * l * nd;
+        TH* hl = Hs + (size_t)l * NH * R * W;
+        dense_fwd<R, TH>(xa, dbm, da, P + of[0], P + of[1], W, true, A, W, hl, WT);
+        for (int k = 1; k < NH; ++k) {
+            dense_fwd<R, TH>(A, W, W, P + of[2 * k], P + of[2 * k + 1], W, true, B, W, hl + (size_t)k * R * W, WT);
+            float* t = A;
+            A = B;
+            B = t;
+        }
+        float* o = Os + l * R * 2 * dbm;
+        dense_fwd<R, TH>(A, W, W, P + of[2 * NH], P + of[2 * NH + 1], 2 * db, false, o, 2 * dbm, (TH*)nullptr, WT);
+        // coupling: v = u, v_B = u_B exp(s) + t; logdet += sum s
+        float* v = Us + (l + 1) * R * d;
+        for (int e = threadIdx.x; e < R * d; e += FT) v[e] = u[e];
+        __syncthreads();
+        if (threadIdx.x < R) {
+            const int r = threadIdx.x;
+            float acc = 0.0f;
+            for (int j = 0; j < db; ++j) {
+                const float s = LG_FLOW_CLAMP * tanhf(o[r * 2 * dbm + j] / LG_FLOW_CLAMP);
+                v[r * d + b0 + j] = u[r * d + b0 + j] * expf(s) + o[r * 2 * dbm + db + j];
+                acc += s;
+            }
+            ld[r] += acc;
         }
         __syncthreads();
     }
-    for (int i = 0; i < 2; ++i)
-        for (int j = 0; j < 2; ++j) {
-            const int m = row0 + ty * 2 + i, n = col0 + tx * 2 + j;
-            if (m >= M || n >= N) continue;
-            float v = acc[i][j] + (bias ? bias[n] : 0.0f);
-            if (relu) v = v > 0 ? v : 0;
-            if (mask && !(to_f(mask[(size_t)m * N + n]) > 0)) v = 0;
-            TC* c = &C[(size_t)m * ldc + n];
-            if (accumulate) v += to_f(*c);
-            from_f(*c, v);
+    // ---- loss: 0.5 |z|^2 - logdet per row
+    const float* z = Us + f.L * R * d;
+    if (threadIdx.x < R) {
+        const int r = threadIdx.x;
+        float q = 0.0f;
+        for (int j = 0; j < d; ++j) q += z[r * d + j] * z[r * d + j];
+        if (base + r < M) {
+            loss[base + r] = 0.5f * q - ld[r];
+            if (znorm2) znorm2[base + r] = q;
         }
-}
-
-// column sums: out[n] (+)= sum_m X[m][n]
-__global__ void colsum(const float* __restrict__ X, int M, int N, float* __restrict__ out, int accumulate)
-{
-    const int n = blockIdx.x * blockDim.x + threadIdx.x;
-    if (n >= N) return;
-    float s = 0;
-    for (int m = 0; m < M; ++m) s += X[(size_t)m * N + n];
-    out[n] = accumulate ? out[n] + s : s;
-}
-
-// gather the conditioning half: in[m][j] = u[m][a0 + j]
-__global__ void gather_half(const float* __restrict__ u, int d, int a0, int da, int M, float* __restrict__ in)
-{
-    const int e = blockIdx.x * blockDim.x + threadIdx.x;
-    if (e >= M * da) return;
-    const int m = e / da, j = e % da;
-    in[e] = u[(size_t)m * d + a0 + j];
-}
-
-// forward coupling: v = u with v_B = u_B exp(s) + t; logdet += sum s
-__global__ void coupling_fwd(const float* __restrict__ u, const float* __restrict__ o, int d, int b0, int db,
-                             int M, float* __restrict__ v, float* __restrict__ logdet)
-{
-    const int m = blockIdx.x * blockDim.x + threadIdx.x;
-    if (m >= M) return;
-    float ld = 0;
-    for (int j = 0; j < d; ++j) v[(size_t)m * d + j] = u[(size_t)m * d + j];
-    for (int j = 0; j < db; ++j) {
-        const float sr = o[(size_t)m * 2 * db + j], t = o[(size_t)m * 2 * db + db + j];
-        const float s = LG_FLOW_CLAMP * tanhf(sr / LG_FLOW_CLAMP);
-        v[(size_t)m * d + b0 + j] = u[(size_t)m * d + b0 + j] * expf(s) + t;
-        ld += s;
     }
-    logdet[m] += ld;
-}
-
-// inverse coupling: u_B = (v_B - t) exp(-s); logdet -= sum s
-__global__ void coupling_inv(const float* __restrict__ v, const float* __restrict__ o, int d, int b0, int db, int M,
-                             float* __restrict__ u, float* __restrict__ logdet)
-{
-    const int m = blockIdx.x * blockDim.x + threadIdx.x;
-    if (m >= M) return;
-    float ld = 0;
-    for (int j = 0; j < d; ++j) u[(size_t)m * d + j] = v[(size_t)m * d + j];
-    for (int j = 0; j < db; ++j) {
-        const float sr = o[(size_t)m * 2 * db + j], t = o[(size_t)m * 2 * db + db + j];
-        const float s = LG_FLOW_CLAMP * tanhf(sr / LG_FLOW_CLAMP);
-        u[(size_t)m * d + b0 + j] = (v[(size_t)m * d + b0 + j] - t) * expf(-s);
-        ld -= s;
-    }
-    logdet[m] += ld;
-}
-
-// backward of a coupling layer.  dv: gradient w.r.t. the layer output;
-// writes do (gradient w.r.t. the conditioner output) and du (w.r.t. the
-// input, conditioning half still missing the conditioner's contribution).
-// dlogdet is the gradient of the loss w.r.t. every s (the loss is
-// -mean(logdet), so -1/M).
-__global__ void coupling_bwd(const float* __restrict__ u, const float* __restrict__ o, const float* __restrict__ dv,
-                             int d, int b0, int db, int M, float dlogdet, float* __restrict__ dout,
-                             float* __restrict__ du)
-{
-    const int m = blockIdx.x * blockDim.x + threadIdx.x;
-    if (m >= M) return;
-    for (int j = 0; j < d; ++j) du[(size_t)m * d + j] = dv[(size_t)m * d + j];
-    for (int j = 0; j < db; ++j) {
-        const float sr = o[(size_t)m * 2 * db + j];
-        const float th = tanhf(sr / LG_FLOW_CLAMP);
-        const float s = LG_FLOW_CLAMP * th, es = expf(s);
-        const float g = dv[(size_t)m * d + b0 + j];
-        const float ub = u[(size_t)m * d + b0 + j];
-        const float ds = g * ub * es + dlogdet;
-        dout[(size_t)m * 2 * db + j] = ds * (1.0f - th * th);
-        dout[(size_t)m * 2 * db + db + j] = g;
-        du[(size_t)m * d + b0 + j] = g * es;
+    if (!grad) return;
+    // ---- backward: dz = z / M, dlogdet = -1 / M (mean loss); rows beyond M
+    // carry no gradient
+    for (int e = threadIdx.x; e < R * d; e += FT) dv[e] = (base + e / d < M) ? z[e] / M : 0.0f;
+    __syncthreads();
+    float* gp = gpart + (size_t)blockIdx.x * nparams;
+    for (int l = f.L - 1; l >= 0; --l) {
+        const int da = f.da(l), db = f.db(l), a0 = f.a0(l), b0 = f.b0(l);
+        const float* u = Us + l * R * d;
+        const float* o = Os + l * R * 2 * dbm;
+        // coupling backward: dO = (ds (1 - th^2), g), du = dv with du_B = g e^s
+        float* dO = dB;  // R x 2db, pitch 2 dbm
+        for (int e = threadIdx.x; e < R * d; e += FT) du[e] = dv[e];
+        __syncthreads();
+        for (int e = threadIdx.x; e < R * db; e += FT) {
+            const int r = e / db, j = e - r * db;
+            const float th = tanhf(o[r * 2 * dbm + j] / LG_FLOW_CLAMP);
+            const float s = LG_FLOW_CLAMP * th, es = expf(s);
+            const float g = dv[r * d + b0 + j];
+            const float dlog = base + r < M ? -1.0f / M : 0.0f;
+            const float ds = g * u[r * d + b0 + j] * es + dlog;
+            dO[r * 2 * dbm + j] = ds * (1.0f - th * th);
+            dO[r * 2 * dbm + db + j] = g;
+            du[r * d + b0 + j] = g * es;
+        }
+        __syncthreads();
+        const int* of = offs + 2 * l * nd;
+        const TH* hl = Hs + (size_t)l * NH * R * W;
+        // output dense: input the last hidden activation
+        dense_bwd<R, TH>(hl + (size_t)(NH - 1) * R * W, W, W, dO, 2 * dbm, 2 * db, P + of[2 * NH], gp + of[2 * NH],
+                         gp + of[2 * NH + 1], dA, W, true, WT);
+        for (int k = NH - 1; k >= 1; --k) {
+            dense_bwd<R, TH>(hl + (size_t)(k - 1) * R * W, W, W, dA, W, W, P + of[2 * k], gp + of[2 * k],
+                             gp + of[2 * k + 1], dB, W, true, WT);
+            float* t = dA;
+            dA = dB;
+            dB = t;
+        }
+        // first dense: input the conditioning half of u
+        for (int e = threadIdx.x; e < R * da; e += FT) {
+            const int r = e / da, j = e - r * da;
+            xa[r * dbm + j] = u[r * d + a0 + j];
+        }
+        __syncthreads();
+        dense_bwd<R, float>(xa, dbm, da, dA, W, W, P + of[0], gp + of[0], gp + of[1], dB, dbm, false, WT);
+        for (int e = threadIdx.x; e < R * da; e += FT) {
+            const int r = e / da, j = e - r * da;
+            du[r * d + a0 + j] += dB[r * dbm + j];
+        }
+        __syncthreads();
+        for (int e = threadIdx.x; e < R * d; e += FT) dv[e] = du[e];
+        __syncthreads();
     }
 }
 
-// scatter-add the conditioner's input gradient into du's conditioning half
-__global__ void add_half(float* __restrict__ du, int d, int a0, int da, int M, const float* __restrict__ din)
+// Gradient = sum of the blocks' slices in block order; then (adam) an Adam
+// step with bias corrections c1, c2 of this step.
+__global__ void __launch_bounds__(256)
+    lg_flow_adam(float* __restrict__ P, const float* __restrict__ gpart, int nparts, long n, float* __restrict__ G,
+                 float* __restrict__ m1, float* __restrict__ m2, int adam, float lr, float b1, float b2, float c1,
+                 float c2, const int* __restrict__ stop)
 {
-    const int e = blockIdx.x * blockDim.x + threadIdx.x;
-    if (e >= M * da) return;
-    const int m = e / da, j = e % da;
-    du[(size_t)m * d + a0 + j] += din[e];
-}
-
-// loss terms: per sample 0.5|z|^2 - logdet; dz = z / M
-__global__ void nll(const float* __restrict__ z, const float* __restrict__ logdet, int d, int M,
-                    float* __restrict__ per, float* __restrict__ dz)
-{
-    const int m = blockIdx.x * blockDim.x + threadIdx.x;
-    if (m >= M) return;
-    float q = 0;
-    for (int j = 0; j < d; ++j) {
-        const float v = z[(size_t)m * d + j];
-        q += v * v;
-        if (dz) dz[(size_t)m * d + j] = v / M;
-    }
-    per[m] = 0.5f * q - logdet[m];
-}
-
-__global__ void adam(float* __restrict__ p, const float* __restrict__ g, float* __restrict__ m1,
-                     float* __restrict__ m2, long n, float lr, float b1, float b2, float c1, float c2)
-{
+    if (stop && *stop) return;
     const long i = (long)blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= n) return;
-    const float gi = g[i];
-    m1[i] = b1 * m1[i] + (1 - b1) * gi;
-    m2[i] = b2 * m2[i] + (1 - b2) * gi * gi;
-    p[i] -= lr * (m1[i] / c1) / (sqrtf(m2[i] / c2) + 1e-8f);
+    float g = 0.0f;
+    for (int c = 0; c < nparts; ++c) g += gpart[(size_t)c * n + i];
+    if (G) G[i] = g;
+    if (!adam) return;
+    const float a = b1 * m1[i] + (1 - b1) * g, b = b2 * m2[i] + (1 - b2) * g * g;
+    m1[i] = a;
+    m2[i] = b;
+    P[i] -= lr * (a / c1) / (sqrtf(b / c2) + 1e-8f);
+}
+
+// Early stopping on the device.  state: [0] best held-out loss, [1] epochs
+// since the best (as float), [2] last held-out loss, [3] training epochs
+// completed (counted when epoch = 1), [4] 1 if the last check improved,
+// [8 + e] the held-out loss after epoch e; stop: set once `patience` epochs
+// pass without improvement.  The held-out loss is the mean of the per-row
+// losses (lane j sums rows j, j + 32, ... in order, then a fixed tree).
+__global__ void __launch_bounds__(32)
+    lg_flow_check(const float* __restrict__ loss, int n, float* __restrict__ state, int patience, int* stop,
+                  int epoch)
+{
+    if (*stop) return;
+    double s = 0.0;
+    for (int i = threadIdx.x; i < n; i += 32) s += loss[i];
+    for (int o = 16; o > 0; o >>= 1) s += __shfl_down_sync(0xffffffffu, s, o);
+    if (threadIdx.x == 0) {
+        const float v = (float)(s / n);
+        state[2] = v;
+        state[3] += (float)epoch;
+        const int e = (int)state[3];
+        if (e < LG_FLOW_HISTORY) state[8 + e] = v;
+        const bool improved = isfinite(v) && v < state[0];
+        state[4] = improved ? 1.0f : 0.0f;
+        if (improved) {
+            state[0] = v;
+            state[1] = 0.0f;
+        } else {
+            state[1] += 1.0f;
+            if (state[1] >= (float)patience) *stop = 1;
+        }
+    }
+}
+
+// best = P after a check that improved (state[4]); skipped once stopped.
+__global__ void __launch_bounds__(256)
+    lg_flow_keep(const float* __restrict__ state, const int* __restrict__ stop, const float* __restrict__ P,
+                 float* __restrict__ best, long n)
+{
+    if (state[4] == 0.0f) return;
+    const long i = (long)blockIdx.x * blockDim.x + threadIdx.x;
+    if (i < n) best[i] = P[i];
+    (void)stop;
+}
+
+// Shared-memory layout of lg_flow_inverse for R rows (floats unless noted).
+struct InvSmem {
+    int cur, xa, a, b, o, ld, offs, ws, hb, total;
+    __host__ __device__ InvSmem(const FlowDims& f, int R, int hbytes)
+    {
+        int q = 0;
+        auto take = [&](int n) {
+            const int at = q;
+            q += (n + 3) / 4 * 4;
+            return at;
+        };
+        const int wr = f.W > 2 * f.dbmax() ? f.W : 2 * f.dbmax();
+        cur = take(R * f.d);
+        xa = take(R * f.dbmax());
+        a = take(R * wr);
+        b = take(R * wr);
+        o = take(R * 2 * f.dbmax());
+        ld = take(R);
+        offs = take(2 * (f.L * (f.NH + 1)));
+        ws = take(f.W * (f.W > 2 * f.dbmax() ? f.W : 2 * f.dbmax()));
+        hb = q;
+        total = q * 4 + ((R * f.W * hbytes + 15) / 16) * 16;
+    }
+};
+
+// Inverse flow of M latent points (R rows per block): z -> u (standardised
+// cube coordinates), ldet = log |det du/dz| = -sum s.
+template <int R, typename TH>
+__global__ void __launch_bounds__(FT)
+    lg_flow_inverse(FlowDims f, const float* __restrict__ P, const float* __restrict__ Z, int M,
+                    float* __restrict__ Uout, float* __restrict__ ldet)
+{
+    extern __shared__ float4 smem4[];
+    float* sm = reinterpret_cast<float*>(smem4);
+    const InvSmem L(f, R, (int)sizeof(TH));
+    const int d = f.d, W = f.W, NH = f.NH, nd = NH + 1, dbm = f.dbmax();
+    float* cur = sm + L.cur;
+    float* xa = sm + L.xa;
+    float* A = sm + L.a;
+    float* B = sm + L.b;
+    float* o = sm + L.o;
+    float* ld = sm + L.ld;
+    int* offs = reinterpret_cast<int*>(sm + L.offs);
+    float* Ws = sm + L.ws;
+    TH* hbuf = reinterpret_cast<TH*>(sm + L.hb);  // rounding buffer of a hidden layer
+    fill_offsets(f, offs);
+    const int base = blockIdx.x * R;
+    for (int e = threadIdx.x; e < R * d; e += FT) cur[e] = base + e / d < M ? Z[(size_t)base * d + e] : 0.0f;
+    if (threadIdx.x < R) ld[threadIdx.x] = 0.0f;
+    __syncthreads();
+    for (int l = f.L - 1; l >= 0; --l) {
+        const int da = f.da(l), db = f.db(l), a0 = f.a0(l), b0 = f.b0(l);
+        for (int e = threadIdx.x; e < R * da; e += FT) {
+            const int r = e / da, j = e - r * da;
+            xa[r * dbm + j] = cur[r * d + a0 + j];
+        }
+        __syncthreads();
+        const int* of = offs + 2 * l * nd;
+        dense_fwd<R, TH>(xa, dbm, da, P + of[0], P + of[1], W, true, A, W, hbuf, Ws);
+        for (int k = 1; k < NH; ++k) {
+            dense_fwd<R, TH>(A, W, W, P + of[2 * k], P + of[2 * k + 1], W, true, B, W, hbuf, Ws);
+            float* t = A;
+            A = B;
+            B = t;
+        }
+        dense_fwd<R, TH>(A, W, W, P + of[2 * NH], P + of[2 * NH + 1], 2 * db, false, o, 2 * dbm, (TH*)nullptr, Ws);
+        // u_B = (v_B - t) exp(-s); logdet -= sum s
+        for (int r = threadIdx.x; r < R; r += FT) {
+            float acc = 0.0f;
+            for (int j = 0; j < db; ++j) {
+                const float s = LG_FLOW_CLAMP * tanhf(o[r * 2 * dbm + j] / LG_FLOW_CLAMP);
+                cur[r * d + b0 + j] = (cur[r * d + b0 + j] - o[r * 2 * dbm + db + j]) * expf(-s);
+                acc -= s;
+            }
+            ld[r] += acc;
+        }
+        __syncthreads();
+    }
+    for (int e = threadIdx.x; e < R * d; e += FT)
+        if (base + e / d < M) Uout[(size_t)base * d + e] = cur[e];
+    for (int r = threadIdx.x; r < R; r += FT)
+        if (base + r < M) ldet[base + r] = ld[r];
+}
+
+// Counter-based uniforms in (0, 1): splitmix64 finaliser of (key, counter).
+__device__ __forceinline__ double lg_u01(unsigned long long key, unsigned long long ctr)
+{
+    unsigned long long z = key + 0x9E3779B97F4A7C15ull * (ctr + 1);
+    z = (z ^ (z >> 30)) * 0xBF58476D1CE4E5B9ull;
+    z = (z ^ (z >> 27)) * 0x94D049BB133111EBull;
+    z ^= z >> 31;
+    return ((double)(z >> 11) + 0.5) * (1.0 / 9007199254740992.0);
+}
+
+// M points uniform in the d-ball of radius rad = expand sqrt(rad2[0]): normal
+// direction (Box-Muller pairs, regenerated from the counter for the second
+// pass instead of being held) scaled by rad u^(1/d).
+__device__ __forceinline__ float2 lg_normal_pair(unsigned long long key, unsigned long long c)
+{
+    const float u1 = (float)lg_u01(key, c), u2 = (float)lg_u01(key, c + 1);
+    const float r = sqrtf(-2.0f * logf(u1));
+    float sn, cs;
+    sincospif(2.0f * u2, &sn, &cs);
+    return make_float2(r * cs, r * sn);
+}
+
+__global__ void __launch_bounds__(256)
+    lg_flow_latent(unsigned long long key, int M, int d, const double* __restrict__ rad2, double expand,
+                   float* __restrict__ Z)
+{
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= M) return;
+    const double rad = expand * sqrt(rad2[0]);
+    const unsigned long long c0 = (unsigned long long)i * (MAX_D + 2);
+    float n2 = 0.0f;
+    for (int a = 0; a < d; a += 2) {
+        const float2 v = lg_normal_pair(key, c0 + a);
+        n2 += v.x * v.x + (a + 1 < d ? v.y * v.y : 0.0f);
+    }
+    const float scale = (float)(rad * pow(lg_u01(key, c0 + MAX_D), 1.0 / d)) * rsqrtf(n2);
+    for (int a = 0; a < d; a += 2) {
+        const float2 v = lg_normal_pair(key, c0 + a);
+        Z[(size_t)i * d + a] = v.x * scale;
+        if (a + 1 < d) Z[(size_t)i * d + a + 1] = v.y * scale;
+    }
+}
+
+// Maximum of the finite log weights and of a floor (the calibrated bound),
+// in one block: out[0].
+__global__ void __launch_bounds__(1024) lg_flow_max(const float* __restrict__ v, int n, double floor_,
+                                                     double* __restrict__ out)
+{
+    __shared__ double red[32];
+    double m = -INFINITY;
+    for (int i = threadIdx.x; i < n; i += blockDim.x)
+        if (isfinite(v[i])) m = fmax(m, (double)v[i]);
+    for (int o = 16; o > 0; o >>= 1) m = fmax(m, __shfl_xor_sync(0xffffffffu, m, o));
+    if ((threadIdx.x & 31) == 0) red[threadIdx.x >> 5] = m;
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        double r = floor_;
+        for (int w = 0; w < (int)(blockDim.x >> 5); ++w) r = fmax(r, red[w]);
+        out[0] = r;
+    }
+}
+
+// Calibration sums: out[1] = sum exp(v - out[0]) over finite v (one block,
+// fixed order per thread then a fixed tree).
+__global__ void __launch_bounds__(1024) lg_flow_expsum(const float* __restrict__ v, int n, double* __restrict__ out)
+{
+    __shared__ double red[1024];
+    const double m = out[0];
+    double s = 0.0;
+    for (int i = threadIdx.x; i < n; i += blockDim.x)
+        if (isfinite(v[i])) s += exp((double)v[i] - m);
+    red[threadIdx.x] = s;
+    __syncthreads();
+    for (int o = blockDim.x / 2; o > 0; o >>= 1) {
+        if ((int)threadIdx.x < o) red[threadIdx.x] += red[threadIdx.x + o];
+        __syncthreads();
+    }
+    if (threadIdx.x == 0) out[1] = red[0];
+}
+
+// Rejection and cube tests of M proposals: keep draw i with probability
+// exp(ldet_i - lmax) (lmax = bound[0]), then x = mean + sdev u must lie in the
+// unit cube.  flag[i] = 2 kept and inside, 1 kept outside, 0 rejected.
+__global__ void __launch_bounds__(256)
+    lg_flow_accept(unsigned long long key, int M, int d, const float* __restrict__ U, const float* __restrict__ ldet,
+                   const double* __restrict__ bound, const float* __restrict__ mean, const float* __restrict__ sdev,
+                   double* __restrict__ X, int* __restrict__ flag)
+{
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= M) return;
+    const float l = ldet[i];
+    int f = 0;
+    if (isfinite(l) && !(lg_u01(key, (unsigned long long)i) > exp((double)l - bound[0]))) {
+        f = 2;
+        for (int a = 0; a < d; ++a) {
+            const double x = (double)mean[a] + (double)sdev[a] * (double)U[(size_t)i * d + a];
+            X[(size_t)i * d + a] = x;
+            if (!(x >= 0.0 && x <= 1.0)) f = 1;
+        }
+    }
+    flag[i] = f;
+}
+
+// Order-preserving compaction (one block): the first `room` draws with
+// flag 2 go to out in draw order; cnt[0] = how many were written, cnt[1] =
+// how many passed the weight test.
+__global__ void __launch_bounds__(1024)
+    lg_flow_compact(const int* __restrict__ flag, int M, const double* __restrict__ X, int d, int room,
+                    double* __restrict__ out, int* __restrict__ cnt)
+{
+    __shared__ int part[1024], kept[1024];
+    const int T = blockDim.x, t = threadIdx.x;
+    const int per = (M + T - 1) / T, lo = t * per, hi = min(M, lo + per);
+    int c = 0, k = 0;
+    for (int i = lo; i < hi; ++i) {
+        c += flag[i] == 2;
+        k += flag[i] > 0;
+    }
+    part[t] = c;
+    kept[t] = k;
+    __syncthreads();
+    if (t == 0) {
+        int s = 0, ks = 0;
+        for (int j = 0; j < T; ++j) {
+            const int v = part[j];
+            part[j] = s;
+            s += v;
+            ks += kept[j];
+        }
+        cnt[0] = min(s, room);
+        cnt[1] = ks;
+    }
+    __syncthreads();
+    int pos = part[t];
+    for (int i = lo; i < hi && pos < room; ++i)
+        if (flag[i] == 2) {
+            for (int a = 0; a < d; ++a) out[(size_t)pos * d + a] = X[(size_t)i * d + a];
+            ++pos;
+        }
 }
 
 template <typename T>
@@ -221,7 +767,24 @@ struct DevBuf {
         cudaFree(p);
         p = nullptr;
         n = 0;
-        if (cudaMalloc(&p, count * sizeof(T)) != cudaSuccess) return false;
+        if (cudaMalloc(&p, std::max<size_t>(count, 1) * sizeof(T)) != cudaSuccess) return false;
+        n = count;
+        return true;
+    }
+};
+
+template <typename T>
+struct HostBuf {
+    T* p = nullptr;
+    size_t n = 0;
+    ~HostBuf() { cudaFreeHost(p); }
+    bool ensure(size_t count)
+    {
+        if (count <= n) return true;
+        cudaFreeHost(p);
+        p = nullptr;
+        n = 0;
+        if (cudaMallocHost((void**)&p, std::max<size_t>(count, 1) * sizeof(T)) != cudaSuccess) return false;
         n = count;
         return true;
     }
@@ -232,43 +795,61 @@ struct DevBuf {
 // The flow: parameters, optimiser state and work buffers on one device.
 class Flow {
 public:
-    int d = 0, L = 8, W = 128, NH = 2, h = 0;
+    FlowDims f{};
     bool bf16 = true;
-    std::vector<size_t> off;  // per layer, per dense layer: weight offset, bias offset
-    std::vector<int> din, dout;
     size_t nparams = 0;
-    DevBuf<float> P, G, M1, M2;
+    DevBuf<float> P, G, M1, M2, gpart, loss, znorm;
     std::vector<float> mean, sdev;
     long step = 0;
-    bool want_loss = true;  // read the loss back (off inside training loops)
+    cudaStream_t stream = nullptr;
+    std::string err;
 
-    int da(int l) const { return (l % 2 == 0) ? h : d - h; }
-    int a0(int l) const { return (l % 2 == 0) ? 0 : h; }
-    int db(int l) const { return d - da(l); }
-    int b0(int l) const { return (l % 2 == 0) ? h : 0; }
-    int ndense() const { return NH + 1; }
-    size_t woff(int l, int k) const { return off[(size_t)(l * ndense() + k) * 2]; }
-    size_t boff(int l, int k) const { return off[(size_t)(l * ndense() + k) * 2 + 1]; }
-    int kin(int l, int k) const { return k == 0 ? da(l) : W; }
-    int kout(int l, int k) const { return k == ndense() - 1 ? 2 * db(l) : W; }
+    ~Flow()
+    {
+        if (stream) cudaStreamDestroy(stream);
+    }
+
+    static size_t count_params(const FlowDims& f)
+    {
+        size_t n = 0;
+        for (int l = 0; l < f.L; ++l)
+            for (int k = 0; k <= f.NH; ++k) n += (size_t)f.kin(l, k) * f.kout(l, k) + f.kout(l, k);
+        return n;
+    }
+
+    int step_smem() const { return StepSmem(f, FR, bf16 ? 2 : 4).total; }
+    int inverse_smem() const { return InvSmem(f, FRI, bf16 ? 2 : 4).total; }
 
     bool init(int dim, int layers, int width, int hidden, uint64_t seed)
     {
-        d = dim;
-        L = layers;
-        W = width;
-        NH = hidden;
-        h = d / 2;
-        if (d < 2) return false;
-        off.clear();
-        nparams = 0;
-        for (int l = 0; l < L; ++l)
-            for (int k = 0; k < ndense(); ++k) {
-                off.push_back(nparams);
-                nparams += (size_t)kin(l, k) * kout(l, k);
-                off.push_back(nparams);
-                nparams += kout(l, k);
-            }
+        f.d = dim;
+        f.h = dim / 2;
+        f.L = layers;
+        f.W = width;
+        f.NH = hidden;
+        if (dim < 2 || dim > MAX_D || width < 1 || width > MAX_W || hidden < 1 || layers < 1 ||
+            layers * (hidden + 1) > MAX_DENSE) {
+            err = "flow: dimension 2-64, width 1-128, at least one layer and hidden layer, layers x (hidden + 1) <= 64";
+            return false;
+        }
+        int optin = 0, dev = 0;
+        cudaGetDevice(&dev);
+        cudaDeviceGetAttribute(&optin, cudaDevAttrMaxSharedMemoryPerBlockOptin, dev);
+        if (step_smem() > optin || inverse_smem() > optin) {
+            err = "flow: layers x hidden x width too large for the training block's shared memory";
+            return false;
+        }
+        if (!stream && cudaStreamCreateWithFlags(&stream, cudaStreamNonBlocking) != cudaSuccess) return false;
+        const int sm_step = step_smem(), sm_inv = inverse_smem();
+        if (bf16) {
+            cudaFuncSetAttribute(lg_flow_step<FR, __nv_bfloat16>, cudaFuncAttributeMaxDynamicSharedMemorySize, sm_step);
+            cudaFuncSetAttribute(lg_flow_inverse<FRI, __nv_bfloat16>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                 sm_inv);
+        } else {
+            cudaFuncSetAttribute(lg_flow_step<FR, float>, cudaFuncAttributeMaxDynamicSharedMemorySize, sm_step);
+            cudaFuncSetAttribute(lg_flow_inverse<FRI, float>, cudaFuncAttributeMaxDynamicSharedMemorySize, sm_inv);
+        }
+        nparams = count_params(f);
         if (!P.ensure(nparams) || !G.ensure(nparams) || !M1.ensure(nparams) || !M2.ensure(nparams)) return false;
         // He-uniform hidden weights, zero output layer and biases: the flow
         // starts as the identity map
@@ -278,10 +859,15 @@ public:
             s = s * 6364136223846793005ull + 1442695040888963407ull;
             return ((s >> 11) * (1.0 / 9007199254740992.0)) * 2 - 1;
         };
-        for (int l = 0; l < L; ++l)
-            for (int k = 0; k + 1 < ndense(); ++k) {
-                const double lim = std::sqrt(6.0 / kin(l, k));
-                for (size_t i = 0; i < (size_t)kin(l, k) * kout(l, k); ++i) host[woff(l, k) + i] = (float)(lim * unif());
+        size_t o = 0;
+        for (int l = 0; l < f.L; ++l)
+            for (int k = 0; k <= f.NH; ++k) {
+                const size_t nw = (size_t)f.kin(l, k) * f.kout(l, k);
+                if (k < f.NH) {
+                    const double lim = std::sqrt(6.0 / f.kin(l, k));
+                    for (size_t i = 0; i < nw; ++i) host[o + i] = (float)(lim * unif());
+                }
+                o += nw + f.kout(l, k);
             }
         cudaMemcpy(P.p, host.data(), nparams * 4, cudaMemcpyHostToDevice);
         cudaMemset(M1.p, 0, nparams * 4);
@@ -290,374 +876,316 @@ public:
         return cudaGetLastError() == cudaSuccess;
     }
 
-    // work buffers for a batch of M samples
-    DevBuf<float> u, in, o, ld, per, dz, du, dv, dob, din_b, tmp;
-    DevBuf<__nv_bfloat16> hb;
-    DevBuf<float> hf;
-
-    bool reserve(int M)
+    // Work buffers for passes over up to n rows and gradient passes over up
+    // to mb rows (reserved before a retraining is enqueued, so that no
+    // buffer is reallocated under enqueued kernels).
+    bool reserve(int n, int mb)
     {
-        const size_t hs = (size_t)L * NH * M * W;
-        return u.ensure((size_t)(L + 1) * M * d) && in.ensure((size_t)L * M * std::max(h, d - h) + 1) &&
-               o.ensure((size_t)L * M * 2 * std::max(h, d - h) + 1) && ld.ensure(M) && per.ensure(M) &&
-               dz.ensure((size_t)M * d) && du.ensure((size_t)M * d) && dv.ensure((size_t)M * d) &&
-               dob.ensure((size_t)M * 2 * std::max(h, d - h) + 1) && din_b.ensure((size_t)M * std::max(W, d) + 1) &&
-               tmp.ensure((size_t)M * std::max(W, d) + 1) &&
-               (bf16 ? hb.ensure(hs) : hf.ensure(hs));
+        return loss.ensure(n) && znorm.ensure(n) && gpart.ensure((size_t)((mb + FR - 1) / FR) * nparams);
     }
 
-    template <typename TA, typename TB, typename TC, typename TM>
-    static void mm(const TA* A, int lda, int ta, const TB* B, int ldb, int tb, TC* C, int ldc, int M, int N, int K,
-                   const float* bias, int relu, const TM* mask, int acc)
+    // Enqueue one forward (+ backward) pass over rows [row0, row0 + M) of
+    // the index list (or of X when idx is NULL): per-row losses in loss,
+    // |z|^2 in znorm (when asked), partial gradients in gpart.
+    bool pass(const float* X, const int* idx, int row0, int M, bool grad, bool want_z, const int* stop)
     {
-        dim3 g((N + TS - 1) / TS, (M + TS - 1) / TS);
-        gemm<TA, TB, TC, TM><<<g, dim3(16, 16)>>>(A, lda, ta, B, ldb, tb, C, ldc, M, N, K, bias, relu, mask, acc);
+        const int blocks = (M + FR - 1) / FR;
+        if (!loss.ensure(M) || (want_z && !znorm.ensure(M)) || (grad && !gpart.ensure((size_t)blocks * nparams)))
+            return false;
+        const int sm = step_smem();
+        if (bf16)
+            lg_flow_step<FR, __nv_bfloat16><<<blocks, FT, sm, stream>>>(f, P.p, X, idx, row0, M, grad, loss.p,
+                                                                        want_z ? znorm.p : nullptr, gpart.p,
+                                                                        (long)nparams, stop);
+        else
+            lg_flow_step<FR, float><<<blocks, FT, sm, stream>>>(f, P.p, X, idx, row0, M, grad, loss.p,
+                                                                want_z ? znorm.p : nullptr, gpart.p, (long)nparams,
+                                                                stop);
+        return cudaGetLastError() == cudaSuccess;
     }
 
-    template <typename TH>
-    TH* hid(TH* base, int l, int k, int M) const
+    // Sum of the partial gradients into G and (adam) an Adam step.
+    bool update(int M, bool adam, float lr, const int* stop)
     {
-        return base + ((size_t)l * NH + k) * M * W;
-    }
-
-    // conditioner of layer l on in (M x da) -> o (M x 2db), hidden
-    // activations stored for the backward pass
-    template <typename TH>
-    void conditioner(int l, const float* x, int M, float* out, TH* hbase)
-    {
-        const float* p = P.p;
-        // first hidden layer from the float input
-        mm<float, float, TH, float>(x, da(l), 0, p + woff(l, 0), W, 0, hid(hbase, l, 0, M), W, M, W, da(l),
-                                    p + boff(l, 0), 1, nullptr, 0);
-        for (int k = 1; k < NH; ++k)
-            mm<TH, float, TH, float>(hid(hbase, l, k - 1, M), W, 0, p + woff(l, k), W, 0, hid(hbase, l, k, M), W, M,
-                                     W, W, p + boff(l, k), 1, nullptr, 0);
-        mm<TH, float, float, float>(hid(hbase, l, NH - 1, M), W, 0, p + woff(l, NH), 2 * db(l), 0, out, 2 * db(l),
-                                    M, 2 * db(l), W, p + boff(l, NH), 0, nullptr, 0);
-    }
-
-    template <typename TH>
-    float forward_backward(const float* x, int M, bool grad, TH* hbase)
-    {
-        const int T = 128;
-        cudaMemcpy(u.p, x, (size_t)M * d * 4, cudaMemcpyDeviceToDevice);
-        cudaMemset(ld.p, 0, (size_t)M * 4);
-        for (int l = 0; l < L; ++l) {
-            float* ul = u.p + (size_t)l * M * d;
-            float* il = in.p + (size_t)l * M * std::max(h, d - h);
-            float* ol = o.p + (size_t)l * M * 2 * std::max(h, d - h);
-            gather_half<<<(M * da(l) + T - 1) / T, T>>>(ul, d, a0(l), da(l), M, il);
-            conditioner(l, il, M, ol, hbase);
-            coupling_fwd<<<(M + T - 1) / T, T>>>(ul, ol, d, b0(l), db(l), M, ul + (size_t)M * d, ld.p);
+        const int blocks = (M + FR - 1) / FR;
+        float c1 = 1, c2 = 1;
+        if (adam) {
+            ++step;
+            c1 = 1 - std::pow(0.9f, (float)step);
+            c2 = 1 - std::pow(0.999f, (float)step);
         }
-        nll<<<(M + T - 1) / T, T>>>(u.p + (size_t)L * M * d, ld.p, d, M, per.p, grad ? dz.p : nullptr);
-        double loss = 0;
-        if (want_loss) {
-            std::vector<float> hp(M);
-            cudaMemcpy(hp.data(), per.p, (size_t)M * 4, cudaMemcpyDeviceToHost);
-            for (float v : hp) loss += v;
-            loss /= M;
-        }
-        if (!grad) return (float)loss;
-        cudaMemset(G.p, 0, nparams * 4);
-        cudaMemcpy(dv.p, dz.p, (size_t)M * d * 4, cudaMemcpyDeviceToDevice);
-        for (int l = L - 1; l >= 0; --l) {
-            float* ul = u.p + (size_t)l * M * d;
-            float* il = in.p + (size_t)l * M * std::max(h, d - h);
-            float* ol = o.p + (size_t)l * M * 2 * std::max(h, d - h);
-            coupling_bwd<<<(M + T - 1) / T, T>>>(ul, ol, dv.p, d, b0(l), db(l), M, -1.0f / M, dob.p, du.p);
-            float* g = G.p;
-            const float* p = P.p;
-            // output dense layer
-            TH* hl = hid(hbase, l, NH - 1, M);
-            mm<TH, float, float, float>(hl, W, 1, dob.p, 2 * db(l), 0, g + woff(l, NH), 2 * db(l), W, 2 * db(l), M,
-                                        nullptr, 0, nullptr, 0);
-            colsum<<<(2 * db(l) + T - 1) / T, T>>>(dob.p, M, 2 * db(l), g + boff(l, NH), 0);
-            // gradient w.r.t. the last hidden activation, masked by ReLU
-            // (kept in din_b as float)
-            mm<float, float, float, TH>(dob.p, 2 * db(l), 0, p + woff(l, NH), 2 * db(l), 1, din_b.p, W, M, W,
-                                        2 * db(l), nullptr, 0, hl, 0);
-            for (int k = NH - 1; k >= 1; --k) {
-                TH* hprev = hid(hbase, l, k - 1, M);
-                mm<TH, float, float, float>(hprev, W, 1, din_b.p, W, 0, g + woff(l, k), W, W, W, M, nullptr, 0,
-                                            nullptr, 0);
-                colsum<<<(W + T - 1) / T, T>>>(din_b.p, M, W, g + boff(l, k), 0);
-                mm<float, float, float, TH>(din_b.p, W, 0, p + woff(l, k), W, 1, tmp.p, W, M, W, W, nullptr, 0,
-                                            hprev, 0);
-                std::swap(din_b.p, tmp.p);
-            }
-            // first dense layer
-            mm<float, float, float, float>(il, da(l), 1, din_b.p, W, 0, g + woff(l, 0), W, da(l), W, M, nullptr, 0,
-                                           nullptr, 0);
-            colsum<<<(W + T - 1) / T, T>>>(din_b.p, M, W, g + boff(l, 0), 0);
-            // gradient w.r.t. the conditioning input, added to du
-            mm<float, float, float, float>(din_b.p, W, 0, p + woff(l, 0), W, 1, tmp.p, da(l), M, da(l), W, nullptr,
-                                           0, nullptr, 0);
-            add_half<<<(M * da(l) + T - 1) / T, T>>>(du.p, d, a0(l), da(l), M, tmp.p);
-            std::swap(dv.p, du.p);
-        }
-        return (float)loss;
+        lg_flow_adam<<<(unsigned)((nparams + 255) / 256), 256, 0, stream>>>(
+            P.p, gpart.p, blocks, (long)nparams, adam ? nullptr : G.p, M1.p, M2.p, adam ? 1 : 0, lr, 0.9f, 0.999f,
+            c1, c2, stop);
+        return cudaGetLastError() == cudaSuccess;
     }
 
-    float loss_and_grad(const float* x, int M, bool grad)
+    // Inverse map of M latent points (device) through the weights W ->
+    // standardised u (device), log|det du/dz| per point (device).
+    bool inverse(const float* W, const float* z, int M, float* uout, float* ldet, cudaStream_t st)
     {
-        return bf16 ? forward_backward<__nv_bfloat16>(x, M, grad, hb.p) : forward_backward<float>(x, M, grad, hf.p);
-    }
-
-    void adam_step(float lr)
-    {
-        ++step;
-        const float b1 = 0.9f, b2 = 0.999f;
-        const float c1 = 1 - std::pow(b1, (float)step), c2 = 1 - std::pow(b2, (float)step);
-        adam<<<(unsigned)((nparams + 255) / 256), 256>>>(P.p, G.p, M1.p, M2.p, (long)nparams, lr, b1, b2, c1, c2);
-    }
-
-    // inverse map of M latent points (device) -> standardised u (device),
-    // log|det du/dz| per point (device)
-    template <typename TH>
-    void inverse(const float* z, int M, float* uout, TH* hbase)
-    {
-        const int T = 128;
-        float* cur = u.p;
-        cudaMemcpy(cur, z, (size_t)M * d * 4, cudaMemcpyDeviceToDevice);
-        cudaMemset(ld.p, 0, (size_t)M * 4);
-        for (int l = L - 1; l >= 0; --l) {
-            float* nxt = (l % 2 == 0) ? dv.p : du.p;
-            if (l == 0) nxt = uout;
-            gather_half<<<(M * da(l) + T - 1) / T, T>>>(cur, d, a0(l), da(l), M, in.p);
-            conditioner(l, in.p, M, o.p, hbase);
-            coupling_inv<<<(M + T - 1) / T, T>>>(cur, o.p, d, b0(l), db(l), M, nxt, ld.p);
-            cur = nxt;
-        }
+        const int blocks = (M + FRI - 1) / FRI, sm = inverse_smem();
+        if (bf16)
+            lg_flow_inverse<FRI, __nv_bfloat16><<<blocks, FT, sm, st>>>(f, W, z, M, uout, ldet);
+        else
+            lg_flow_inverse<FRI, float><<<blocks, FT, sm, st>>>(f, W, z, M, uout, ldet);
+        return cudaGetLastError() == cudaSuccess;
     }
 };
 
-// The proposal used by the sampler.
+// The proposal used by the sampler.  Retraining runs on the flow's own
+// stream while the sampler goes on with the current proposal: train()
+// enqueues the whole retraining -- epochs with device-side early stopping,
+// the best weights copied into the idle one of two proposal slots, the
+// latent radius of the live points and the calibration of the weight bound
+// -- and returns; the new slot takes over when advance() reaches `lag`
+// replacements (waiting for the retraining then if it is still running) or
+// at the next train(), whichever comes first.  Proposals run on a second
+// stream from the active slot.
 class FlowProposal : public Proposal {
 public:
     Flow flow;
     lg_flow_options opt;
     int device = 0;
     uint64_t seed = 1;
-    bool trained = false;
-    double radius = 0, last_loss = 0;
     long ntrain = 0;
-    std::vector<float> hx;
-    DevBuf<float> dx, dzlat, dulat, dval, best;
+    cudaStream_t ps = nullptr;  // proposals
+    cudaEvent_t done = nullptr;
+    bool pending = false;
+    int act = -1, pslot = 0;  // active slot (-1: none) and the slot being trained
+    // per slot: weights, standardisation, latent radius^2 and calibration
+    DevBuf<float> Puse[2], dmean[2], dsdev[2];
+    DevBuf<double> dres[2];  // [0] max |z|^2 of the live points, [1] max log weight, [2] sum exp(w - max)
+    std::vector<float> hmean[2], hsdev[2];
+    double radius[2] = {0, 0}, wnorm[2] = {0, 0}, efficiency[2] = {0, 0};
+    bool usable[2] = {false, false};
+    // training inputs and results
+    DevBuf<float> dx, best, state;
+    DevBuf<int> didx, dstop;
+    HostBuf<float> hx, hstate, hinit;
+    HostBuf<int> hidx;
+    HostBuf<double> hres;
+    int steps_per_epoch = 0;
+    long step0 = 0;
+    // calibration and proposal work buffers (separate: they run on
+    // different streams)
+    DevBuf<float> cz, cu, cld, dz, du, dld;
+    DevBuf<int> dflag, dcnt;
+    DevBuf<double> dX, dout, dbound;
+    HostBuf<double> hbound, hout;
+    HostBuf<int> hcnt;
+
+    ~FlowProposal()
+    {
+        if (flow.stream) cudaStreamSynchronize(flow.stream);
+        if (ps) cudaStreamSynchronize(ps);
+        if (ps) cudaStreamDestroy(ps);
+        if (done) cudaEventDestroy(done);
+    }
+
+    static int fail_cuda()
+    {
+        cudaGetLastError();
+        return LG_ERR_CUDA;
+    }
 
     int train(const double* live, int n, int d) override
     {
         cudaSetDevice(device);
-        if (flow.d != d) {
+        if (pending) finish();
+        if (flow.f.d != d) {
             flow.bf16 = true;
-            if (!flow.init(d, opt.layers, opt.width, opt.hidden, seed)) return LG_ERR_CUDA;
+            if (!flow.init(d, opt.layers, opt.width, opt.hidden, seed)) return LG_ERR_INPUT;
         }
+        if (!ps && cudaStreamCreateWithFlags(&ps, cudaStreamNonBlocking) != cudaSuccess) return fail_cuda();
+        if (!done && cudaEventCreateWithFlags(&done, cudaEventDisableTiming) != cudaSuccess) return fail_cuda();
+        cudaStream_t s = flow.stream;
+        pslot = act < 0 ? 0 : 1 - act;
         // standardise by the live set
-        flow.mean.assign(d, 0);
-        flow.sdev.assign(d, 0);
+        std::vector<float>& mean = hmean[pslot];
+        std::vector<float>& sdev = hsdev[pslot];
+        mean.assign(d, 0);
+        sdev.assign(d, 0);
         for (int i = 0; i < n; ++i)
-            for (int a = 0; a < d; ++a) flow.mean[a] += (float)live[(size_t)i * d + a];
-        for (auto& m : flow.mean) m /= n;
+            for (int a = 0; a < d; ++a) mean[a] += (float)live[(size_t)i * d + a];
+        for (auto& m : mean) m /= n;
         for (int i = 0; i < n; ++i)
             for (int a = 0; a < d; ++a) {
-                const double v = live[(size_t)i * d + a] - flow.mean[a];
-                flow.sdev[a] += (float)(v * v);
+                const double v = live[(size_t)i * d + a] - mean[a];
+                sdev[a] += (float)(v * v);
             }
-        for (auto& s : flow.sdev) s = std::sqrt(std::max(s / n, 1e-24f));
-        hx.resize((size_t)n * d);
-        for (int i = 0; i < n; ++i)
-            for (int a = 0; a < d; ++a)
-                hx[(size_t)i * d + a] = (float)((live[(size_t)i * d + a] - flow.mean[a]) / flow.sdev[a]);
+        for (auto& sd : sdev) sd = std::sqrt(std::max(sd / n, 1e-24f));
         // hold out 20% of the live points for early stopping: the best
         // weights on the held-out set are kept (the flow has far more
         // parameters than there are live points)
-        std::vector<int> idx(n);
-        std::iota(idx.begin(), idx.end(), 0);
-        uint64_t s = seed ^ 0x5bd1e995u ^ ((uint64_t)ntrain << 32);
-        for (int i = n - 1; i > 0; --i) {
-            s = s * 6364136223846793005ull + 1442695040888963407ull;
-            std::swap(idx[i], idx[(s >> 33) % (uint64_t)(i + 1)]);
-        }
         const int nval = std::max(1, n / 5), ntr = n - nval;
-        std::vector<float> vx((size_t)nval * d);
-        for (int i = 0; i < nval; ++i) std::memcpy(&vx[(size_t)i * d], &hx[(size_t)idx[ntr + i] * d], d * 4);
-        idx.resize(ntr);
-        const int Mb = std::min(opt.batch, ntr);
-        if (!dx.ensure((size_t)n * d) || !dval.ensure((size_t)nval * d) || !best.ensure(flow.nparams) ||
-            !flow.reserve(std::max(Mb, n)))
-            return LG_ERR_ALLOC;
-        cudaMemcpy(dval.p, vx.data(), vx.size() * 4, cudaMemcpyHostToDevice);
-        auto val_loss = [&]() {
-            flow.want_loss = true;
-            const float l = flow.loss_and_grad(dval.p, nval, false);
-            flow.want_loss = false;
-            return l;
-        };
-        float best_loss = val_loss();
-        cudaMemcpy(best.p, flow.P.p, flow.nparams * 4, cudaMemcpyDeviceToDevice);
-        int since_best = 0;
-        const int patience = 20;
-        std::vector<float> bx((size_t)Mb * d);
         // warm start: later retrainings continue from the previous weights
         // with a quarter of the epochs
         const int epochs = ntrain == 0 ? opt.epochs : std::max(1, opt.epochs / 4);
-        ++ntrain;
-        flow.want_loss = false;
-        const bool dbg = std::getenv("LG_FLOW_DEBUG") != nullptr;
+        const int Mb = std::min(opt.batch, ntr);
+        steps_per_epoch = ntr / Mb;
+        const size_t nidx = (size_t)nval + (size_t)epochs * ntr, nst = 8 + LG_FLOW_HISTORY;
+        if (!hx.ensure((size_t)n * d + 2 * (size_t)d) || !hidx.ensure(nidx) || !dx.ensure((size_t)n * d) ||
+            !didx.ensure(nidx) || !best.ensure(flow.nparams) || !state.ensure(nst) || !dstop.ensure(1) ||
+            !hstate.ensure(nst) || !hinit.ensure(nst) || !hres.ensure(3) || !Puse[pslot].ensure(flow.nparams) ||
+            !dmean[pslot].ensure(d) || !dsdev[pslot].ensure(d) || !dres[pslot].ensure(3) || !flow.reserve(n, Mb) ||
+            !cz.ensure((size_t)16384 * d) || !cu.ensure((size_t)16384 * d) || !cld.ensure(16384))
+            return LG_ERR_ALLOC;
+        // rows: the standardised live set (then mean and sdev); index list:
+        // the held-out rows, then one shuffle of the training rows per epoch
+        for (int i = 0; i < n; ++i)
+            for (int a = 0; a < d; ++a)
+                hx.p[(size_t)i * d + a] = (float)((live[(size_t)i * d + a] - mean[a]) / sdev[a]);
+        std::memcpy(hx.p + (size_t)n * d, mean.data(), d * 4);
+        std::memcpy(hx.p + (size_t)n * d + d, sdev.data(), d * 4);
+        std::vector<int> idx(n);
+        std::iota(idx.begin(), idx.end(), 0);
+        uint64_t st = seed ^ 0x5bd1e995u ^ ((uint64_t)ntrain << 32);
+        auto next = [&]() {
+            st = st * 6364136223846793005ull + 1442695040888963407ull;
+            return st >> 33;
+        };
+        for (int i = n - 1; i > 0; --i) std::swap(idx[i], idx[next() % (uint64_t)(i + 1)]);
+        std::memcpy(hidx.p, idx.data() + ntr, (size_t)nval * sizeof(int));
+        idx.resize(ntr);
         for (int ep = 0; ep < epochs; ++ep) {
-            if (dbg && ntrain == 1 && (ep % 25 == 0)) {
-                flow.want_loss = true;
-                cudaMemcpy(dx.p, hx.data(), (size_t)n * d * 4, cudaMemcpyHostToDevice);
-                std::fprintf(stderr, "flow: epoch %d loss %.4f\n", ep, flow.loss_and_grad(dx.p, n, false));
-                flow.want_loss = false;
-            }
-            for (int i = ntr - 1; i > 0; --i) {
-                s = s * 6364136223846793005ull + 1442695040888963407ull;
-                std::swap(idx[i], idx[(s >> 33) % (uint64_t)(i + 1)]);
-            }
-            for (int b0 = 0; b0 + Mb <= ntr; b0 += Mb) {
-                for (int i = 0; i < Mb; ++i)
-                    std::memcpy(&bx[(size_t)i * d], &hx[(size_t)idx[b0 + i] * d], d * 4);
-                cudaMemcpy(dx.p, bx.data(), (size_t)Mb * d * 4, cudaMemcpyHostToDevice);
-                flow.loss_and_grad(dx.p, Mb, true);
-                flow.adam_step((float)opt.lr);
-            }
-            const float vl = val_loss();
-            if (std::isfinite(vl) && vl < best_loss) {
-                best_loss = vl;
-                since_best = 0;
-                cudaMemcpy(best.p, flow.P.p, flow.nparams * 4, cudaMemcpyDeviceToDevice);
-            } else if (++since_best >= patience) {
-                break;
-            }
+            for (int i = ntr - 1; i > 0; --i) std::swap(idx[i], idx[next() % (uint64_t)(i + 1)]);
+            std::memcpy(hidx.p + nval + (size_t)ep * ntr, idx.data(), (size_t)ntr * sizeof(int));
         }
-        cudaMemcpy(flow.P.p, best.p, flow.nparams * 4, cudaMemcpyDeviceToDevice);
-        if (dbg) std::fprintf(stderr, "flow: best held-out loss %.4f\n", best_loss);
-        // latent radius of the live points
-        flow.want_loss = true;
-        cudaMemcpy(dx.p, hx.data(), (size_t)n * d * 4, cudaMemcpyHostToDevice);
-        last_loss = flow.loss_and_grad(dx.p, n, false);
-        std::vector<float> z((size_t)n * d);
-        cudaMemcpy(z.data(), flow.u.p + (size_t)flow.L * n * d, z.size() * 4, cudaMemcpyDeviceToHost);
-        double r = 0;
-        for (int i = 0; i < n; ++i) {
-            double q = 0;
-            for (int a = 0; a < d; ++a) q += (double)z[(size_t)i * d + a] * z[(size_t)i * d + a];
-            r = std::max(r, std::sqrt(q));
+        std::fill(hinit.p, hinit.p + nst, NAN);
+        hinit.p[0] = INFINITY;
+        hinit.p[1] = hinit.p[2] = hinit.p[3] = hinit.p[4] = 0.0f;
+        const uint64_t cal_key = seed * 7919 + (uint64_t)ntrain;
+        ++ntrain;
+        step0 = flow.step;
+        if (cudaMemcpyAsync(dx.p, hx.p, (size_t)n * d * 4, cudaMemcpyHostToDevice, s) ||
+            cudaMemcpyAsync(dmean[pslot].p, hx.p + (size_t)n * d, d * 4, cudaMemcpyHostToDevice, s) ||
+            cudaMemcpyAsync(dsdev[pslot].p, hx.p + (size_t)n * d + d, d * 4, cudaMemcpyHostToDevice, s) ||
+            cudaMemcpyAsync(didx.p, hidx.p, nidx * sizeof(int), cudaMemcpyHostToDevice, s) ||
+            cudaMemcpyAsync(state.p, hinit.p, nst * sizeof(float), cudaMemcpyHostToDevice, s) ||
+            cudaMemsetAsync(dstop.p, 0, sizeof(int), s))
+            return fail_cuda();
+        // the whole retraining is enqueued at once: the held-out check stops
+        // it on the device, keeping the best weights
+        const int patience = std::max(1, opt.patience);
+        const unsigned kb = (unsigned)((flow.nparams + 255) / 256);
+        bool ok = flow.pass(dx.p, didx.p, 0, nval, false, false, dstop.p);
+        lg_flow_check<<<1, 32, 0, s>>>(flow.loss.p, nval, state.p, patience, dstop.p, 0);
+        lg_flow_keep<<<kb, 256, 0, s>>>(state.p, dstop.p, flow.P.p, best.p, (long)flow.nparams);
+        for (int ep = 0; ok && ep < epochs; ++ep) {
+            const int row0 = nval + ep * ntr;
+            for (int b = 0; ok && b < steps_per_epoch; ++b)
+                ok = flow.pass(dx.p, didx.p, row0 + b * Mb, Mb, true, false, dstop.p) &&
+                     flow.update(Mb, true, (float)opt.lr, dstop.p);
+            ok = ok && flow.pass(dx.p, didx.p, 0, nval, false, false, dstop.p);
+            lg_flow_check<<<1, 32, 0, s>>>(flow.loss.p, nval, state.p, patience, dstop.p, 1);
+            lg_flow_keep<<<kb, 256, 0, s>>>(state.p, dstop.p, flow.P.p, best.p, (long)flow.nparams);
         }
-        radius = r * opt.expand;
-        trained = std::isfinite(radius) && radius > 0 && cudaGetLastError() == cudaSuccess;
-        if (trained) trained = calibrate(d);
-        if (std::getenv("LG_FLOW_DEBUG"))
-            std::fprintf(stderr, "flow: train %ld epochs %d loss %.4f latent radius %.3f ok %d\n", ntrain, epochs,
-                         last_loss, radius, (int)trained);
-        return trained ? LG_OK : LG_ERR_CUDA;
+        // best weights: the training state and the proposal slot
+        if (!ok || cudaMemcpyAsync(flow.P.p, best.p, flow.nparams * 4, cudaMemcpyDeviceToDevice, s) ||
+            cudaMemcpyAsync(Puse[pslot].p, best.p, flow.nparams * 4, cudaMemcpyDeviceToDevice, s))
+            return fail_cuda();
+        // latent radius of the live points: max |z|^2 over all of them
+        if (!flow.pass(dx.p, nullptr, 0, n, false, true, nullptr)) return fail_cuda();
+        double* r = dres[pslot].p;
+        lg_flow_max<<<1, 1024, 0, s>>>(flow.znorm.p, n, -INFINITY, r);
+        // calibration of the weight bound on 16384 latent draws: their
+        // maximum log weight and sum of exp(weight - maximum)
+        const int Mc = 16384;
+        lg_flow_latent<<<(Mc + 255) / 256, 256, 0, s>>>(cal_key, Mc, d, r, opt.expand, cz.p);
+        if (!flow.inverse(Puse[pslot].p, cz.p, Mc, cu.p, cld.p, s)) return fail_cuda();
+        lg_flow_max<<<1, 1024, 0, s>>>(cld.p, Mc, -INFINITY, r + 1);
+        lg_flow_expsum<<<1, 1024, 0, s>>>(cld.p, Mc, r + 1);
+        if (cudaMemcpyAsync(hres.p, r, 3 * sizeof(double), cudaMemcpyDeviceToHost, s) ||
+            cudaMemcpyAsync(hstate.p, state.p, nst * sizeof(float), cudaMemcpyDeviceToHost, s) ||
+            cudaEventRecord(done, s))
+            return fail_cuda();
+        pending = true;
+        return LG_OK;
     }
 
-    double wnorm = 0;       // log weight normaliser (calibrated at training)
-    double efficiency = 0;  // mean kept fraction of latent draws
-
-    // M latent draws uniform in the ball, mapped to the standardised space
-    // (uu), with their log weights log|det dx/dz|
-    bool latent_batch(Rng& r, int M, int d, std::vector<float>& z, std::vector<float>& uu, std::vector<float>& lw)
+    // Wait for the pending retraining and make its slot the active one (or
+    // leave no flow active when it is unusable: a kept fraction below 1%).
+    void finish()
     {
-        if (!dzlat.ensure((size_t)M * d) || !dulat.ensure((size_t)M * d) || !flow.reserve(M)) return false;
-        z.resize((size_t)M * d);
-        uu.resize((size_t)M * d);
-        lw.resize(M);
-        // uniform in the latent ball
-        for (int i = 0; i < M; ++i) {
-            double n2 = 0;
-            for (int a = 0; a < d; ++a) {
-                const double v = r.normal();
-                z[(size_t)i * d + a] = (float)v;
-                n2 += v * v;
-            }
-            const double rad = radius * std::pow(r.uniform(), 1.0 / d) / std::sqrt(n2);
-            for (int a = 0; a < d; ++a) z[(size_t)i * d + a] = (float)(z[(size_t)i * d + a] * rad);
+        pending = false;
+        if (cudaEventSynchronize(done) != cudaSuccess) {
+            fail_cuda();
+            act = -1;
+            return;
         }
-        cudaMemcpy(dzlat.p, z.data(), z.size() * 4, cudaMemcpyHostToDevice);
-        if (flow.bf16) flow.inverse(dzlat.p, M, dulat.p, flow.hb.p);
-        else flow.inverse(dzlat.p, M, dulat.p, flow.hf.p);
-        cudaMemcpy(uu.data(), dulat.p, uu.size() * 4, cudaMemcpyDeviceToHost);
-        cudaMemcpy(lw.data(), flow.ld.p, (size_t)M * 4, cudaMemcpyDeviceToHost);
-        return cudaGetLastError() == cudaSuccess;
+        const int k = pslot, d = flow.f.d;
+        // Adam steps the device actually took (those after the stop returned
+        // at once): the bias corrections of the next retraining continue
+        // from there
+        flow.step = step0 + (long)hstate.p[3] * steps_per_epoch;
+        radius[k] = std::sqrt(hres.p[0]) * opt.expand;
+        const double mx = hres.p[1];
+        wnorm[k] = mx + 1.0;
+        efficiency[k] = hres.p[2] * std::exp(-1.0) / 16384;  // mean exp(w - wnorm)
+        usable[k] = std::isfinite(radius[k]) && radius[k] > 0 && std::isfinite(mx) && efficiency[k] >= 0.01;
+        act = usable[k] ? k : -1;
+        if (std::getenv("LG_FLOW_DEBUG"))
+            std::fprintf(stderr,
+                         "flow: train %ld epochs %d, held-out loss %.4f, latent radius %.3f, calibrated efficiency "
+                         "%.4f, usable %d (d %d)\n",
+                         ntrain, (int)hstate.p[3], hstate.p[0], radius[k], efficiency[k], (int)usable[k], d);
     }
 
-    // Calibrate the normaliser on a large latent sample (its maximum plus a
-    // margin, so that the rejection step is exact unless a weight exceeds it)
-    // and estimate the efficiency; a flow whose kept fraction is below 1% is
-    // not used (the sampler stays on the ellipsoid).
-    bool calibrate(int d)
+    void advance(long since_train) override
     {
-        Rng r(seed * 7919 + (uint64_t)ntrain);
-        std::vector<float> z, uu, lw;
-        const int M = 16384;
-        if (!latent_batch(r, M, d, z, uu, lw)) return false;
-        double mx = -INFINITY;
-        for (float v : lw)
-            if (std::isfinite(v)) mx = std::max(mx, (double)v);
-        if (!std::isfinite(mx)) return false;
-        wnorm = mx + 1.0;
-        double acc = 0;
-        for (float v : lw)
-            if (std::isfinite(v)) acc += std::exp(v - wnorm);
-        efficiency = acc / M;
-        if (std::getenv("LG_FLOW_DEBUG"))
-            std::fprintf(stderr, "flow: calibrated efficiency %.4f\n", efficiency);
-        return efficiency >= 0.01;
+        if (pending && since_train >= opt.lag) finish();
     }
 
     // volume of the image of the latent ball: V_ball(R) E[|det dx/dz|]
     double log_volume() const override
     {
-        if (!trained || efficiency <= 0) return HUGE_VAL;
-        const int d = flow.d;
-        double lv = 0.5 * d * std::log(M_PI) - std::lgamma(0.5 * d + 1) + d * std::log(radius);
-        lv += std::log(efficiency) + wnorm;
-        for (float sd : flow.sdev) lv += std::log((double)sd);
+        if (act < 0) return HUGE_VAL;
+        const int d = flow.f.d;
+        double lv = 0.5 * d * std::log(M_PI) - std::lgamma(0.5 * d + 1) + d * std::log(radius[act]);
+        lv += std::log(efficiency[act]) + wnorm[act];
+        for (float sd : hsdev[act]) lv += std::log((double)sd);
         return lv;
     }
 
     int propose(const double*, int, int d, double* out, int B, uint64_t sd) override
     {
-        if (!trained) return 0;
+        if (act < 0) return 0;
         cudaSetDevice(device);
+        const int k = act;
+        const int M = std::max(4 * B, (int)std::min(65536.0, 2.0 * B / std::max(efficiency[k], 1e-3)));
+        if (!dz.ensure((size_t)M * d) || !du.ensure((size_t)M * d) || !dld.ensure(M) || !dX.ensure((size_t)M * d) ||
+            !dflag.ensure(M) || !dout.ensure((size_t)B * d) || !dcnt.ensure(2) || !dbound.ensure(1) ||
+            !hbound.ensure(1) || !hcnt.ensure(2) || !hout.ensure((size_t)B * d))
+            return 0;
         Rng r(sd);
-        const int M = std::max(4 * B, (int)std::min(65536.0, 2.0 * B / std::max(efficiency, 1e-3)));
-        std::vector<float> z, uu, ldet;
         int got = 0;
         for (int round = 0; round < 4 && got < B; ++round) {
             // keep x with probability proportional to 1 / q_x(x) = |det dx/dz|
             // (z uniform in the ball), normalised by the calibrated bound (a
             // weight above it raises the bound for the rest of the round)
-            if (!latent_batch(r, M, d, z, uu, ldet)) return 0;
-            double lmax = wnorm;
-            for (int i = 0; i < M; ++i)
-                if (std::isfinite(ldet[i]) && ldet[i] > lmax) lmax = ldet[i];
-            wnorm = lmax;
-            int kept = 0;
-            for (int i = 0; i < M && got < B; ++i) {
-                if (!std::isfinite(ldet[i]) || r.uniform() > std::exp((double)ldet[i] - lmax)) continue;
-                ++kept;
-                bool in = true;
-                double* x = out + (size_t)got * d;
-                for (int a = 0; a < d && in; ++a) {
-                    x[a] = flow.mean[a] + (double)flow.sdev[a] * uu[(size_t)i * d + a];
-                    in = x[a] >= 0 && x[a] <= 1;
-                }
-                if (in) ++got;
-            }
-            if (std::getenv("LG_FLOW_DEBUG") && round == 0) {
-                std::vector<float> w(ldet);
-                std::sort(w.begin(), w.end());
-                const float lmaxf = (float)lmax;
-                std::fprintf(stderr,
-                             "flow: propose %d latent, %d kept by the weight test, %d in the cube; log weight "
-                             "quantiles 1%% %.2f 50%% %.2f 99%% %.2f max %.2f\n",
-                             M, kept, got, w[M / 100] - lmaxf, w[M / 2] - lmaxf, w[M - 1 - M / 100] - lmaxf,
-                             w[M - 1] - lmaxf);
-            }
+            const uint64_t k_lat = r.next(), k_acc = r.next();
+            lg_flow_latent<<<(M + 255) / 256, 256, 0, ps>>>(k_lat, M, d, dres[k].p, opt.expand, dz.p);
+            if (!flow.inverse(Puse[k].p, dz.p, M, du.p, dld.p, ps)) return fail_cuda(), 0;
+            lg_flow_max<<<1, 1024, 0, ps>>>(dld.p, M, wnorm[k], dbound.p);
+            lg_flow_accept<<<(M + 255) / 256, 256, 0, ps>>>(k_acc, M, d, du.p, dld.p, dbound.p, dmean[k].p,
+                                                             dsdev[k].p, dX.p, dflag.p);
+            lg_flow_compact<<<1, 1024, 0, ps>>>(dflag.p, M, dX.p, d, B - got, dout.p + (size_t)got * d, dcnt.p);
+            if (cudaMemcpyAsync(hcnt.p, dcnt.p, 2 * sizeof(int), cudaMemcpyDeviceToHost, ps) ||
+                cudaMemcpyAsync(hbound.p, dbound.p, sizeof(double), cudaMemcpyDeviceToHost, ps) ||
+                cudaStreamSynchronize(ps))
+                return fail_cuda(), 0;
+            wnorm[k] = hbound.p[0];
+            if (std::getenv("LG_FLOW_DEBUG") && round == 0)
+                std::fprintf(stderr, "flow: propose %d latent, %d kept by the weight test, %d in the cube\n", M,
+                             hcnt.p[1], hcnt.p[0]);
+            got += hcnt.p[0];
+        }
+        if (got > 0) {
+            if (cudaMemcpyAsync(hout.p, dout.p, (size_t)got * d * sizeof(double), cudaMemcpyDeviceToHost, ps) ||
+                cudaStreamSynchronize(ps))
+                return fail_cuda(), 0;
+            std::memcpy(out, hout.p, (size_t)got * d * sizeof(double));
         }
         return got;
     }
@@ -690,40 +1218,67 @@ lg_flow_options lg_flow_defaults(void)
     o.batch = 256;
     o.lr = 1e-3;
     o.expand = 1.1;
+    o.patience = 10;
+    o.lag = 500;
     return o;
 }
 
-// Loss and gradient of the flow on n points (standardised space, host
-// arrays), for gradient checks against the CPU restatement: params in/out
-// (lg_flow_nparams values), grad out.  bf16 = 0 keeps activations in FP32.
 long lg_flow_nparams(int d, int layers, int width, int hidden)
 {
-    lg::Flow f;
-    f.d = d;
-    f.L = layers;
-    f.W = width;
-    f.NH = hidden;
-    f.h = d / 2;
-    long n = 0;
-    for (int l = 0; l < f.L; ++l)
-        for (int k = 0; k < f.ndense(); ++k) n += (long)f.kin(l, k) * f.kout(l, k) + f.kout(l, k);
-    return n;
+    lg::FlowDims f{d, d / 2, layers, width, hidden};
+    return (long)lg::Flow::count_params(f);
 }
 
+// Train a flow proposal on n points (row-major n x d, any scale: they are
+// standardised as the sampler's live points are) exactly as the sampler
+// retrains it, for tests: history[0..] receives the held-out loss before
+// training and after each epoch (up to max_history values, NaN past the
+// epochs that ran); returns the number of epochs run (negative on error);
+// *efficiency the calibrated kept fraction of latent draws.
+int lg_flow_fit(int device, int d, const lg_flow_options* opts, const double* pts, int n, float* history,
+                int max_history, double* efficiency)
+{
+    if (!pts || n < 10 || d < 2) return LG_ERR_INPUT;
+    std::string err;
+    std::unique_ptr<lg::FlowProposal> p(static_cast<lg::FlowProposal*>(lg::make_flow_proposal(device, d, opts, err)));
+    if (!p) return LG_ERR_ALLOC;
+    const int rc = p->train(pts, n, d);
+    if (rc) return rc;
+    p->finish();
+    for (int i = 0; i < max_history && history; ++i) history[i] = i < LG_FLOW_HISTORY ? p->hstate.p[8 + i] : NAN;
+    if (efficiency) *efficiency = p->efficiency[p->pslot];
+    return (int)p->hstate.p[3];
+}
+
+// Loss and gradient of the flow on n points (standardised space, host
+// arrays), for gradient checks against the CPU restatement: params in,
+// loss (mean over the points) and grad out.  bf16 = 0 keeps activations in
+// FP32.  Runs the training kernels themselves (one step, no update).
 int lg_flow_loss_grad(int device, int d, int layers, int width, int hidden, int bf16, const float* params,
                       const float* x, int n, float* loss, float* grad)
 {
+    if (!params || !x || !loss || !grad || n <= 0) return LG_ERR_INPUT;
     if (cudaSetDevice(device) != cudaSuccess) return LG_ERR_CUDA;
     lg::Flow f;
     f.bf16 = bf16 != 0;
-    if (!f.init(d, layers, width, hidden, 1) || !f.reserve(n)) return LG_ERR_ALLOC;
+    if (!f.init(d, layers, width, hidden, 1)) {
+        lg::set_global_error(f.err.c_str());
+        return f.err.empty() ? LG_ERR_ALLOC : LG_ERR_INPUT;
+    }
     cudaMemcpy(f.P.p, params, f.nparams * 4, cudaMemcpyHostToDevice);
     lg::DevBuf<float> dx;
     if (!dx.ensure((size_t)n * d)) return LG_ERR_ALLOC;
     cudaMemcpy(dx.p, x, (size_t)n * d * 4, cudaMemcpyHostToDevice);
-    *loss = f.loss_and_grad(dx.p, n, true);
-    cudaMemcpy(grad, f.G.p, f.nparams * 4, cudaMemcpyDeviceToHost);
-    return cudaDeviceSynchronize() == cudaSuccess ? LG_OK : LG_ERR_CUDA;
+    if (!f.pass(dx.p, nullptr, 0, n, true, false, nullptr) || !f.update(n, false, 0.0f, nullptr)) return LG_ERR_CUDA;
+    std::vector<float> per(n);
+    if (cudaMemcpyAsync(per.data(), f.loss.p, (size_t)n * 4, cudaMemcpyDeviceToHost, f.stream) ||
+        cudaMemcpyAsync(grad, f.G.p, f.nparams * 4, cudaMemcpyDeviceToHost, f.stream) ||
+        cudaStreamSynchronize(f.stream))
+        return LG_ERR_CUDA;
+    double s = 0;
+    for (float v : per) s += v;
+    *loss = (float)(s / n);
+    return LG_OK;
 }
 
 }  // extern "C"

@@ -210,6 +210,7 @@ int nested_sample(int nd, lg_batch_loglike fn, void* user, const lg_nested_optio
             pool_l.clear();
             pool_pos = 0;
         }
+        if (learned && use_flow) learned->advance(since_train);
         // replacement: next pool point above the threshold, else a new batch
         bool replaced = false;
         for (int attempt = 0; attempt < 100000 && !replaced; ++attempt) {

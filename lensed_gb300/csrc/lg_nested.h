@@ -57,6 +57,10 @@ struct Proposal {
     virtual ~Proposal() {}
     virtual int train(const double* live, int n, int d) = 0;
     virtual int propose(const double* live, int n, int d, double* out, int B, uint64_t seed) = 0;
+    // called before every replacement with the replacements made since the
+    // last train(): a proposal that trains in the background switches to
+    // its new state at a fixed count, so that runs are reproducible
+    virtual void advance(long since_train) { (void)since_train; }
     // log volume (unit-cube coordinates) of the region propose() draws from
     virtual double log_volume() const = 0;
 };
