@@ -382,6 +382,13 @@ int lg_nested_sample(int ndims, lg_batch_loglike fn, void* user, const lg_nested
 long lg_flow_nparams(int d, int layers, int width, int hidden);
 int lg_flow_loss_grad(int device, int d, int layers, int width, int hidden, int bf16, const float* params,
                       const float* x, int n, float* loss, float* grad);
+/* Inverse flow of M latent points (M x d) with the given parameters: tc = 1
+ * the tensor-core kernel of the proposals (BF16 weights and activations,
+ * FP32 accumulation; width a multiple of 32), tc = 0 the FP32-weight kernel
+ * (bf16 = 1: BF16 hidden activations).  u: M x d standardised points,
+ * ldet: log |det du/dz|.  For checks against the CPU restatement. */
+int lg_flow_inverse_check(int device, int d, int layers, int width, int hidden, int bf16, int tc,
+                          const float* params, const float* z, int M, float* u, float* ldet);
 /* One retraining of the learned proposal on n points (n x d, row-major),
  * as the sampler does it on its live points: history receives the held-out
  * loss before training and after each epoch (NaN past the last epoch run);

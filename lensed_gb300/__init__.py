@@ -150,6 +150,7 @@ def lib():
         "lg_nested_run": (C.c_int, [vp, C.POINTER(NestedOptions), C.POINTER(FlowOptions),
                                     C.POINTER(NestedResult)]),
         "lg_flow_nparams": (C.c_long, [C.c_int, C.c_int, C.c_int, C.c_int]),
+        "lg_flow_inverse_check": (C.c_int, [C.c_int] * 7 + [fp, fp, C.c_int, fp, fp]),
         "lg_flow_fit": (C.c_int, [C.c_int, C.c_int, C.POINTER(FlowOptions), dp, C.c_int, fp, C.c_int, dp]),
         "lg_flow_loss_grad": (C.c_int, [C.c_int, C.c_int, C.c_int, C.c_int, C.c_int, C.c_int, fp, fp, C.c_int,
                                         fp, fp]),

@@ -615,6 +615,349 @@ __global__ void __launch_bounds__(FT)
         if (base + r < M) ldet[base + r] = ld[r];
 }
 
+// ------------------------------------------------ tensor-core inverse --
+// The proposal's inverse flow on the 5th-generation tensor cores: a block
+// takes 128 latent points (the MMA's M) through every coupling layer.  Each
+// dense layer is one chain of tcgen05.mma (kind::f16: BF16 operands, FP32
+// accumulators in tensor memory) issued by one thread: activations (A,
+// 128 x K) and weights (B, N x K) in shared memory, both K-major without
+// swizzle in 8 x 16-byte core matrices.  A layer's weights, packed once per
+// retraining into that layout (lg_flow_pack), arrive by one bulk TMA copy
+// into one of two buffers, the next layer's copy in flight while this one
+// computes.  Epilogues read the accumulators back with tcgen05.ld (thread =
+// row), add the bias, apply the ReLU and store BF16 activations as the next
+// layer's A; the coupling (exp, tanh) runs in FP32 per row.  The map differs
+// from the FP32-weight flow by the BF16 rounding of weights and of the
+// conditioner's input; the log-determinant is that of the map applied, so
+// the calibrated rejection step stays exact for it.
+
+__device__ __forceinline__ uint32_t lg_saddr(const void* p) { return (uint32_t)__cvta_generic_to_shared(p); }
+
+// Shared-memory matrix descriptor: K-major, no swizzle; lbo = bytes between
+// core matrices along K, sbo = bytes between 8-row groups.
+__device__ __forceinline__ uint64_t lg_umma_desc(uint32_t addr, uint32_t lbo, uint32_t sbo)
+{
+    return (uint64_t)((addr & 0x3FFFF) >> 4) | ((uint64_t)((lbo >> 4) & 0x3FFF) << 16) |
+           ((uint64_t)((sbo >> 4) & 0x3FFF) << 32) | ((uint64_t)1 << 46);
+}
+
+// Instruction descriptor: BF16 A and B (K-major), FP32 D, M x N.
+__device__ __forceinline__ uint32_t lg_umma_idesc(int M, int N)
+{
+    return (1u << 4) | (1u << 7) | (1u << 10) | ((uint32_t)(N >> 3) << 17) | ((uint32_t)(M >> 4) << 24);
+}
+
+__device__ __forceinline__ void lg_mma(uint32_t tmem, uint64_t a, uint64_t b, uint32_t idesc, uint32_t acc)
+{
+    asm volatile("{\n.reg .pred p;\nsetp.ne.b32 p, %4, 0;\ntcgen05.mma.cta_group::1.kind::f16 [%0], %1, %2, %3, p;\n}" ::"r"(
+                     tmem),
+                 "l"(a), "l"(b), "r"(idesc), "r"(acc));
+}
+
+__device__ __forceinline__ void lg_mma_commit(void* mbar)
+{
+    asm volatile("tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];" ::"r"(lg_saddr(mbar))
+                 : "memory");
+}
+
+// Bounded wait on an mbarrier phase (one thread); false when it ran out.
+__device__ __forceinline__ bool lg_mbar_wait(void* mbar, uint32_t parity)
+{
+    uint32_t done = 0;
+    for (long it = 0; it < (1L << 20) && !done; ++it)
+        asm volatile("{\n.reg .pred p;\nmbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\nselp.u32 %0, 1, 0, p;\n}"
+                     : "=r"(done)
+                     : "r"(lg_saddr(mbar)), "r"(parity)
+                     : "memory");
+    return done != 0;
+}
+
+// 16 FP32 accumulator columns of this thread's tensor-memory lane.
+__device__ __forceinline__ void lg_tmem_ld16(uint32_t taddr, float* v)
+{
+    uint32_t r[16];
+    asm volatile("tcgen05.ld.sync.aligned.32x32b.x16.b32 {%0,%1,%2,%3,%4,%5,%6,%7,%8,%9,%10,%11,%12,%13,%14,%15}, [%16];"
+                 : "=r"(r[0]), "=r"(r[1]), "=r"(r[2]), "=r"(r[3]), "=r"(r[4]), "=r"(r[5]), "=r"(r[6]), "=r"(r[7]),
+                   "=r"(r[8]), "=r"(r[9]), "=r"(r[10]), "=r"(r[11]), "=r"(r[12]), "=r"(r[13]), "=r"(r[14]), "=r"(r[15])
+                 : "r"(taddr));
+    asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory");
+#pragma unroll
+    for (int j = 0; j < 16; ++j) v[j] = __uint_as_float(r[j]);
+}
+
+// Sizes of the packed weights of one coupling layer (BF16 elements): the
+// input dense (W x Kp0), the hidden denses (W x W each) and the output dense
+// (Np x W), every block N x K in core-matrix order; Kp0 = dbmax rounded up
+// to 16, Np = 2 dbmax rounded up to 16.
+struct TcDims {
+    int kp0, np, s0, sh, so, sl;
+    __host__ __device__ explicit TcDims(const FlowDims& f)
+    {
+        kp0 = (f.dbmax() + 15) / 16 * 16;
+        np = (2 * f.dbmax() + 15) / 16 * 16;
+        s0 = f.W * kp0;
+        sh = f.W * f.W;
+        so = np * f.W;
+        sl = s0 + (f.NH - 1) * sh + so;
+    }
+};
+
+// Element offset of (row n, column k) in an N x K block of core matrices.
+__host__ __device__ __forceinline__ int lg_core_off(int n, int k, int K)
+{
+    return (n / 8) * (K / 8) * 64 + (k / 8) * 64 + (n % 8) * 8 + (k % 8);
+}
+
+// Pack FP32 weights P (library layout, W[k][n] per dense) into BF16 B
+// operands: element (n, k) of each dense = W[k][n], zero in the padding.
+__global__ void __launch_bounds__(256)
+    lg_flow_pack(FlowDims f, const float* __restrict__ P, __nv_bfloat16* __restrict__ out)
+{
+    const TcDims t(f);
+    const long total = (long)f.L * t.sl;
+    for (long e = (long)blockIdx.x * blockDim.x + threadIdx.x; e < total; e += (long)gridDim.x * blockDim.x) {
+        const int l = (int)(e / t.sl);
+        int o = (int)(e - (long)l * t.sl);
+        int dn, K, N, Kp;
+        if (o < t.s0) {
+            dn = 0, K = f.da(l), N = f.W, Kp = t.kp0;
+        } else if (o < t.s0 + (f.NH - 1) * t.sh) {
+            o -= t.s0;
+            dn = 1 + o / t.sh;
+            o -= (dn - 1) * t.sh;
+            K = f.W, N = f.W, Kp = f.W;
+        } else {
+            o -= t.s0 + (f.NH - 1) * t.sh;
+            dn = f.NH, K = f.W, N = 2 * f.db(l), Kp = f.W;
+        }
+        // invert lg_core_off
+        const int g = o / ((Kp / 8) * 64), rem = o - g * (Kp / 8) * 64;
+        const int j = rem / 64, rem2 = rem - j * 64;
+        const int n = g * 8 + rem2 / 8, k = j * 8 + rem2 % 8;
+        // weight offset of dense (l, dn) in the library layout
+        long w = 0;
+        for (int ll = 0; ll < l; ++ll)
+            for (int kk = 0; kk <= f.NH; ++kk) w += (long)f.kin(ll, kk) * f.kout(ll, kk) + f.kout(ll, kk);
+        for (int kk = 0; kk < dn; ++kk) w += (long)f.kin(l, kk) * f.kout(l, kk) + f.kout(l, kk);
+        const float v = (k < K && n < N) ? P[w + (long)k * N + n] : 0.0f;
+        out[e] = __float2bfloat16_rn(v);
+    }
+}
+
+// Shared-memory layout of lg_flow_inverse_tc (bytes).
+struct TcSmem {
+    int wbuf, a0, a1, a2, cur, obuf, ld, bar, total;
+    __host__ __device__ explicit TcSmem(const FlowDims& f)
+    {
+        const TcDims t(f);
+        int q = 0;
+        auto take = [&](int bytes) {
+            const int at = q;
+            q += (bytes + 127) / 128 * 128;
+            return at;
+        };
+        wbuf = take(2 * 2 * t.sl);
+        a0 = take(128 * t.kp0 * 2);
+        a1 = take(128 * f.W * 2);
+        a2 = take(128 * f.W * 2);
+        cur = take(128 * f.d * 4);
+        obuf = take(128 * t.np * 4);
+        ld = take(128 * 4);
+        bar = take(64);
+        total = q;
+    }
+};
+
+__global__ void __launch_bounds__(256, 1)
+    lg_flow_inverse_tc(FlowDims f, const float* __restrict__ P, const __nv_bfloat16* __restrict__ packed,
+                       const float* __restrict__ Z, int M, float* __restrict__ Uout, float* __restrict__ ldet,
+                       int* __restrict__ err)
+{
+    extern __shared__ __align__(1024) unsigned char smem[];
+    const TcDims td(f);
+    const TcSmem L(f);
+    const int t = threadIdx.x, w = t / 32, lane = t % 32;
+    const int d = f.d, W = f.W, NH = f.NH;
+    unsigned char* wb = smem + L.wbuf;
+    __nv_bfloat16* A0 = reinterpret_cast<__nv_bfloat16*>(smem + L.a0);
+    __nv_bfloat16* A1 = reinterpret_cast<__nv_bfloat16*>(smem + L.a1);
+    __nv_bfloat16* A2 = reinterpret_cast<__nv_bfloat16*>(smem + L.a2);
+    float* cur = reinterpret_cast<float*>(smem + L.cur);
+    float* ob = reinterpret_cast<float*>(smem + L.obuf);
+    float* ld = reinterpret_cast<float*>(smem + L.ld);
+    uint64_t* bars = reinterpret_cast<uint64_t*>(smem + L.bar);  // [0] MMA, [1], [2] weight buffers
+    uint32_t* misc = reinterpret_cast<uint32_t*>(smem + L.bar + 32);  // [0] TMEM base, [1] abort flag
+    const uint32_t lbytes = 2u * td.sl;
+    uint32_t tcols = 32;
+    while (tcols < 2u * W) tcols <<= 1;
+
+    if (w == 0) {
+        asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;" ::"r"(lg_saddr(misc)),
+                     "r"(tcols));
+        asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;");
+    }
+    if (t == 0) {
+        for (int i = 0; i < 3; ++i)
+            asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" ::"r"(lg_saddr(bars + i)), "r"(1));
+        asm volatile("fence.mbarrier_init.release.cluster;");
+        misc[1] = 0;
+    }
+    // latent rows
+    const int base = blockIdx.x * 128;
+    for (int e = t; e < 128 * d; e += 256) cur[e] = base + e / d < M ? Z[(size_t)base * d + e] : 0.0f;
+    if (t < 128) ld[t] = 0.0f;
+    asm volatile("tcgen05.fence::before_thread_sync;");
+    __syncthreads();
+    asm volatile("tcgen05.fence::after_thread_sync;");
+    const uint32_t tmem = misc[0];
+    // weights of the first two layers (the inverse runs from layer L-1 down)
+    auto issue_weights = [&](int l, int b) {
+        void* bar = bars + 1 + b;
+        asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(lg_saddr(bar)), "r"(lbytes)
+                     : "memory");
+        asm volatile("cp.async.bulk.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1], %2, [%3];" ::"r"(
+                         lg_saddr(wb + (size_t)b * lbytes)),
+                     "l"(packed + (size_t)l * td.sl), "r"(lbytes), "r"(lg_saddr(bar))
+                     : "memory");
+    };
+    // weight copies issued to and waited for per buffer (thread 0's view;
+    // every thread keeps the same counts)
+    int issued[2] = {1, f.L > 1 ? 1 : 0}, waited[2] = {0, 0};
+    if (t == 0) {
+        issue_weights(f.L - 1, 0);
+        if (f.L > 1) issue_weights(f.L - 2, 1);
+    }
+    uint32_t mma_phase = 0;
+    bool ok = true;
+    // one MMA chain: D (tmem column col) = A (128 x K) . B (N x K)^T
+    auto gemm = [&](uint32_t col, const void* A, const void* B, int K, int N) {
+        if (t == 0) {
+            asm volatile("tcgen05.fence::after_thread_sync;");
+            const uint32_t sb = (uint32_t)(K / 8) * 128, idesc = lg_umma_idesc(128, N);
+            for (int ks = 0; ks < K / 16; ++ks)
+                lg_mma(tmem + col, lg_umma_desc(lg_saddr(A) + ks * 256, 128, sb),
+                       lg_umma_desc(lg_saddr(B) + ks * 256, 128, sb), idesc, ks > 0);
+            lg_mma_commit(bars);
+            if (!lg_mbar_wait(bars, mma_phase)) misc[1] = 1;
+        }
+        mma_phase ^= 1u;
+        __syncthreads();
+        asm volatile("tcgen05.fence::after_thread_sync;");
+        return misc[1] == 0;
+    };
+    // epilogue of a hidden dense: tmem columns [col, col + W) + bias, ReLU,
+    // BF16 into Aout (128 x W core matrices); warp w reads lanes of w % 4,
+    // warps 0-3 the first half of the columns, 4-7 the second
+    auto hidden_epilogue = [&](uint32_t col, const float* __restrict__ bias, __nv_bfloat16* Aout) {
+        const int m = 32 * (w % 4) + lane, half = w / 4;
+        const uint32_t taddr = tmem + ((uint32_t)(32 * (w % 4)) << 16) + col;
+        for (int n0 = half * (W / 2); n0 < (half + 1) * (W / 2); n0 += 16) {
+            float v[16];
+            lg_tmem_ld16(taddr + n0, v);
+            __align__(16) __nv_bfloat16 h[16];
+#pragma unroll
+            for (int j = 0; j < 16; ++j) {
+                const float x = v[j] + __ldg(bias + n0 + j);
+                h[j] = __float2bfloat16_rn(x > 0.0f ? x : 0.0f);
+            }
+            uint4* dst = reinterpret_cast<uint4*>(Aout + lg_core_off(m, n0, W));
+            dst[0] = reinterpret_cast<const uint4*>(h)[0];
+            dst[8] = reinterpret_cast<const uint4*>(h)[1];  // next core matrix along K: +64 elements
+        }
+        asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
+        asm volatile("tcgen05.fence::before_thread_sync;");
+        __syncthreads();
+    };
+    for (int i = 0, l = f.L - 1; l >= 0 && ok; ++i, --l) {
+        const int b = i % 2;
+        const int da = f.da(l), db = f.db(l), a0 = f.a0(l), b0 = f.b0(l);
+        // parameter offsets of this layer's biases (library layout)
+        long woff = 0;
+        for (int ll = 0; ll < l; ++ll)
+            for (int kk = 0; kk <= NH; ++kk) woff += (long)f.kin(ll, kk) * f.kout(ll, kk) + f.kout(ll, kk);
+        // the conditioning half as BF16 A0 (zero padding to kp0)
+        for (int e = t; e < 128 * td.kp0; e += 256) {
+            const int m = e / td.kp0, k = e - m * td.kp0;
+            A0[lg_core_off(m, k, td.kp0)] = __float2bfloat16_rn(k < da ? cur[m * d + a0 + k] : 0.0f);
+        }
+        asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
+        if (t == 0 && !lg_mbar_wait(bars + 1 + b, (uint32_t)waited[b] & 1u)) misc[1] = 1;
+        __syncthreads();
+        if (!misc[1]) ++waited[b];
+        if (misc[1]) {
+            ok = false;
+            break;
+        }
+        const unsigned char* Wl = wb + (size_t)b * lbytes;
+        // input dense
+        long bo = woff + (long)f.kin(l, 0) * f.kout(l, 0);
+        if (!(ok = gemm(0, A0, Wl, td.kp0, W))) break;
+        hidden_epilogue(0, P + bo, A1);
+        long wo = bo + f.kout(l, 0);
+        // hidden denses
+        __nv_bfloat16* Ain = A1;
+        uint32_t col = 0;
+        for (int k = 1; k < NH && ok; ++k) {
+            col = (uint32_t)(k % 2) * W;
+            __nv_bfloat16* Aout = (Ain == A1) ? A2 : A1;
+            ok = gemm(col, Ain, Wl + 2 * (td.s0 + (size_t)(k - 1) * td.sh), W, W);
+            if (!ok) break;
+            bo = wo + (long)f.kin(l, k) * f.kout(l, k);
+            hidden_epilogue(col, P + bo, Aout);
+            wo = bo + f.kout(l, k);
+            Ain = Aout;
+        }
+        if (!ok) break;
+        // output dense into the other accumulator
+        const uint32_t ocol = (uint32_t)(NH % 2) * W;
+        if (!(ok = gemm(ocol, Ain, Wl + 2 * (td.s0 + (size_t)(NH - 1) * td.sh), W, td.np))) break;
+        const float* obias = P + wo + (long)f.kin(l, NH) * f.kout(l, NH);
+        // this layer's weights are consumed: prefetch layer l - 2
+        if (l - 2 >= 0) {
+            if (t == 0) issue_weights(l - 2, b);
+            ++issued[b];
+        }
+        // output accumulators -> obuf (rows 0..127), then the coupling
+        if (w < 4) {
+            const uint32_t taddr = tmem + ((uint32_t)(32 * w) << 16) + ocol;
+            const int m = 32 * w + lane;
+            for (int n0 = 0; n0 < td.np; n0 += 16) {
+                float v[16];
+                lg_tmem_ld16(taddr + n0, v);
+#pragma unroll
+                for (int j = 0; j < 16; ++j) ob[m * td.np + n0 + j] = v[j];
+            }
+        }
+        asm volatile("tcgen05.fence::before_thread_sync;");
+        __syncthreads();
+        if (t < 128) {
+            float acc = 0.0f;
+            for (int j = 0; j < db; ++j) {
+                const float sr = ob[t * td.np + j] + __ldg(obias + j);
+                const float tt = ob[t * td.np + db + j] + __ldg(obias + db + j);
+                const float s = LG_FLOW_CLAMP * tanhf(sr / LG_FLOW_CLAMP);
+                cur[t * d + b0 + j] = (cur[t * d + b0 + j] - tt) * expf(-s);
+                acc -= s;
+            }
+            ld[t] += acc;
+        }
+        __syncthreads();
+    }
+    if (ok) {
+        for (int e = t; e < 128 * d; e += 256)
+            if (base + e / d < M) Uout[(size_t)base * d + e] = cur[e];
+        if (t < 128 && base + t < M) ldet[base + t] = ld[t];
+    } else if (t == 0) {
+        atomicExch(err, 1);
+        // weight copies still in flight land before the block exits
+        for (int b = 0; b < 2; ++b)
+            for (; waited[b] < issued[b]; ++waited[b]) lg_mbar_wait(bars + 1 + b, (uint32_t)waited[b] & 1u);
+    }
+    asm volatile("tcgen05.fence::before_thread_sync;");
+    __syncthreads();
+    if (w == 0) asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" ::"r"(tmem), "r"(tcols));
+}
+
 // Counter-based uniforms in (0, 1): splitmix64 finaliser of (key, counter).
 __device__ __forceinline__ double lg_u01(unsigned long long key, unsigned long long ctr)
 {
@@ -797,6 +1140,7 @@ class Flow {
 public:
     FlowDims f{};
     bool bf16 = true;
+    bool tc = false;  // proposals' inverse on the tensor cores (BF16 activations, width % 32 == 0)
     size_t nparams = 0;
     DevBuf<float> P, G, M1, M2, gpart, loss, znorm;
     std::vector<float> mean, sdev;
@@ -839,6 +1183,11 @@ public:
             err = "flow: layers x hidden x width too large for the training block's shared memory";
             return false;
         }
+        int cc = 0;
+        cudaDeviceGetAttribute(&cc, cudaDevAttrComputeCapabilityMajor, dev);
+        tc = bf16 && cc >= 10 && width % 32 == 0 && width <= 256 && TcDims(f).np <= width &&
+             TcSmem(f).total <= optin && !std::getenv("LG_FLOW_NO_TC");
+        if (tc) cudaFuncSetAttribute(lg_flow_inverse_tc, cudaFuncAttributeMaxDynamicSharedMemorySize, TcSmem(f).total);
         if (!stream && cudaStreamCreateWithFlags(&stream, cudaStreamNonBlocking) != cudaSuccess) return false;
         const int sm_step = step_smem(), sm_inv = inverse_smem();
         if (bf16) {
@@ -920,10 +1269,26 @@ public:
         return cudaGetLastError() == cudaSuccess;
     }
 
-    // Inverse map of M latent points (device) through the weights W ->
-    // standardised u (device), log|det du/dz| per point (device).
-    bool inverse(const float* W, const float* z, int M, float* uout, float* ldet, cudaStream_t st)
+    size_t packed_size() const { return (size_t)f.L * TcDims(f).sl; }
+
+    // BF16 tensor-core operands of the weights W (for the tc inverse).
+    bool pack(const float* W, __nv_bfloat16* out, cudaStream_t st)
     {
+        lg_flow_pack<<<(unsigned)std::min<size_t>((packed_size() + 255) / 256, 4096), 256, 0, st>>>(f, W, out);
+        return cudaGetLastError() == cudaSuccess;
+    }
+
+    // Inverse map of M latent points (device) through the weights W (and
+    // their packed copy when the tensor-core path is on) -> standardised u
+    // (device), log|det du/dz| per point (device); err is set by the
+    // tensor-core kernel if one of its bounded waits ran out.
+    bool inverse(const float* W, const __nv_bfloat16* packed, const float* z, int M, float* uout, float* ldet,
+                 cudaStream_t st, int* err)
+    {
+        if (tc && packed) {
+            lg_flow_inverse_tc<<<(M + 127) / 128, 256, TcSmem(f).total, st>>>(f, W, packed, z, M, uout, ldet, err);
+            return cudaGetLastError() == cudaSuccess;
+        }
         const int blocks = (M + FRI - 1) / FRI, sm = inverse_smem();
         if (bf16)
             lg_flow_inverse<FRI, __nv_bfloat16><<<blocks, FT, sm, st>>>(f, W, z, M, uout, ldet);
@@ -955,6 +1320,8 @@ public:
     int act = -1, pslot = 0;  // active slot (-1: none) and the slot being trained
     // per slot: weights, standardisation, latent radius^2 and calibration
     DevBuf<float> Puse[2], dmean[2], dsdev[2];
+    DevBuf<__nv_bfloat16> dpack[2];  // tensor-core operands of Puse
+    DevBuf<int> dtcerr;              // set by the tensor-core inverse on a timeout
     DevBuf<double> dres[2];  // [0] max |z|^2 of the live points, [1] max log weight, [2] sum exp(w - max)
     std::vector<float> hmean[2], hsdev[2];
     double radius[2] = {0, 0}, wnorm[2] = {0, 0}, efficiency[2] = {0, 0};
@@ -1027,9 +1394,10 @@ public:
         const size_t nidx = (size_t)nval + (size_t)epochs * ntr, nst = 8 + LG_FLOW_HISTORY;
         if (!hx.ensure((size_t)n * d + 2 * (size_t)d) || !hidx.ensure(nidx) || !dx.ensure((size_t)n * d) ||
             !didx.ensure(nidx) || !best.ensure(flow.nparams) || !state.ensure(nst) || !dstop.ensure(1) ||
-            !hstate.ensure(nst) || !hinit.ensure(nst) || !hres.ensure(3) || !Puse[pslot].ensure(flow.nparams) ||
+            !hstate.ensure(nst) || !hinit.ensure(nst) || !hres.ensure(4) || !Puse[pslot].ensure(flow.nparams) ||
             !dmean[pslot].ensure(d) || !dsdev[pslot].ensure(d) || !dres[pslot].ensure(3) || !flow.reserve(n, Mb) ||
-            !cz.ensure((size_t)16384 * d) || !cu.ensure((size_t)16384 * d) || !cld.ensure(16384))
+            !cz.ensure((size_t)16384 * d) || !cu.ensure((size_t)16384 * d) || !cld.ensure(16384) ||
+            !dtcerr.ensure(2) || (flow.tc && !dpack[pslot].ensure(flow.packed_size())))
             return LG_ERR_ALLOC;
         // rows: the standardised live set (then mean and sdev); index list:
         // the held-out rows, then one shuffle of the training rows per epoch
@@ -1063,7 +1431,7 @@ public:
             cudaMemcpyAsync(dsdev[pslot].p, hx.p + (size_t)n * d + d, d * 4, cudaMemcpyHostToDevice, s) ||
             cudaMemcpyAsync(didx.p, hidx.p, nidx * sizeof(int), cudaMemcpyHostToDevice, s) ||
             cudaMemcpyAsync(state.p, hinit.p, nst * sizeof(float), cudaMemcpyHostToDevice, s) ||
-            cudaMemsetAsync(dstop.p, 0, sizeof(int), s))
+            cudaMemsetAsync(dstop.p, 0, sizeof(int), s) || cudaMemsetAsync(dtcerr.p, 0, 2 * sizeof(int), s))
             return fail_cuda();
         // the whole retraining is enqueued at once: the held-out check stops
         // it on the device, keeping the best weights
@@ -1083,7 +1451,8 @@ public:
         }
         // best weights: the training state and the proposal slot
         if (!ok || cudaMemcpyAsync(flow.P.p, best.p, flow.nparams * 4, cudaMemcpyDeviceToDevice, s) ||
-            cudaMemcpyAsync(Puse[pslot].p, best.p, flow.nparams * 4, cudaMemcpyDeviceToDevice, s))
+            cudaMemcpyAsync(Puse[pslot].p, best.p, flow.nparams * 4, cudaMemcpyDeviceToDevice, s) ||
+            (flow.tc && !flow.pack(Puse[pslot].p, dpack[pslot].p, s)))
             return fail_cuda();
         // latent radius of the live points: max |z|^2 over all of them
         if (!flow.pass(dx.p, nullptr, 0, n, false, true, nullptr)) return fail_cuda();
@@ -1093,10 +1462,11 @@ public:
         // maximum log weight and sum of exp(weight - maximum)
         const int Mc = 16384;
         lg_flow_latent<<<(Mc + 255) / 256, 256, 0, s>>>(cal_key, Mc, d, r, opt.expand, cz.p);
-        if (!flow.inverse(Puse[pslot].p, cz.p, Mc, cu.p, cld.p, s)) return fail_cuda();
+        if (!flow.inverse(Puse[pslot].p, dpack[pslot].p, cz.p, Mc, cu.p, cld.p, s, dtcerr.p)) return fail_cuda();
         lg_flow_max<<<1, 1024, 0, s>>>(cld.p, Mc, -INFINITY, r + 1);
         lg_flow_expsum<<<1, 1024, 0, s>>>(cld.p, Mc, r + 1);
         if (cudaMemcpyAsync(hres.p, r, 3 * sizeof(double), cudaMemcpyDeviceToHost, s) ||
+            cudaMemcpyAsync(hres.p + 3, dtcerr.p, sizeof(int), cudaMemcpyDeviceToHost, s) ||
             cudaMemcpyAsync(hstate.p, state.p, nst * sizeof(float), cudaMemcpyDeviceToHost, s) ||
             cudaEventRecord(done, s))
             return fail_cuda();
@@ -1123,7 +1493,11 @@ public:
         const double mx = hres.p[1];
         wnorm[k] = mx + 1.0;
         efficiency[k] = hres.p[2] * std::exp(-1.0) / 16384;  // mean exp(w - wnorm)
-        usable[k] = std::isfinite(radius[k]) && radius[k] > 0 && std::isfinite(mx) && efficiency[k] >= 0.01;
+        int tcerr = 0;
+        std::memcpy(&tcerr, hres.p + 3, sizeof tcerr);
+        usable[k] = std::isfinite(radius[k]) && radius[k] > 0 && std::isfinite(mx) && efficiency[k] >= 0.01 &&
+                    tcerr == 0;
+        if (tcerr) std::fprintf(stderr, "lensed_gb300: flow inverse: a bounded wait ran out; flow not used\n");
         act = usable[k] ? k : -1;
         if (std::getenv("LG_FLOW_DEBUG"))
             std::fprintf(stderr,
@@ -1156,7 +1530,7 @@ public:
         const int M = std::max(4 * B, (int)std::min(65536.0, 2.0 * B / std::max(efficiency[k], 1e-3)));
         if (!dz.ensure((size_t)M * d) || !du.ensure((size_t)M * d) || !dld.ensure(M) || !dX.ensure((size_t)M * d) ||
             !dflag.ensure(M) || !dout.ensure((size_t)B * d) || !dcnt.ensure(2) || !dbound.ensure(1) ||
-            !hbound.ensure(1) || !hcnt.ensure(2) || !hout.ensure((size_t)B * d))
+            !hbound.ensure(1) || !hcnt.ensure(3) || !hout.ensure((size_t)B * d))
             return 0;
         Rng r(sd);
         int got = 0;
@@ -1166,15 +1540,21 @@ public:
             // weight above it raises the bound for the rest of the round)
             const uint64_t k_lat = r.next(), k_acc = r.next();
             lg_flow_latent<<<(M + 255) / 256, 256, 0, ps>>>(k_lat, M, d, dres[k].p, opt.expand, dz.p);
-            if (!flow.inverse(Puse[k].p, dz.p, M, du.p, dld.p, ps)) return fail_cuda(), 0;
+            if (!flow.inverse(Puse[k].p, dpack[k].p, dz.p, M, du.p, dld.p, ps, dtcerr.p + 1)) return fail_cuda(), 0;
             lg_flow_max<<<1, 1024, 0, ps>>>(dld.p, M, wnorm[k], dbound.p);
             lg_flow_accept<<<(M + 255) / 256, 256, 0, ps>>>(k_acc, M, d, du.p, dld.p, dbound.p, dmean[k].p,
                                                              dsdev[k].p, dX.p, dflag.p);
             lg_flow_compact<<<1, 1024, 0, ps>>>(dflag.p, M, dX.p, d, B - got, dout.p + (size_t)got * d, dcnt.p);
             if (cudaMemcpyAsync(hcnt.p, dcnt.p, 2 * sizeof(int), cudaMemcpyDeviceToHost, ps) ||
+                cudaMemcpyAsync(hcnt.p + 2, dtcerr.p + 1, sizeof(int), cudaMemcpyDeviceToHost, ps) ||
                 cudaMemcpyAsync(hbound.p, dbound.p, sizeof(double), cudaMemcpyDeviceToHost, ps) ||
                 cudaStreamSynchronize(ps))
                 return fail_cuda(), 0;
+            if (hcnt.p[2]) {
+                std::fprintf(stderr, "lensed_gb300: flow inverse: a bounded wait ran out; flow dropped\n");
+                act = -1;
+                return 0;
+            }
             wnorm[k] = hbound.p[0];
             if (std::getenv("LG_FLOW_DEBUG") && round == 0)
                 std::fprintf(stderr, "flow: propose %d latent, %d kept by the weight test, %d in the cube\n", M,
@@ -1248,6 +1628,46 @@ int lg_flow_fit(int device, int d, const lg_flow_options* opts, const double* pt
     for (int i = 0; i < max_history && history; ++i) history[i] = i < LG_FLOW_HISTORY ? p->hstate.p[8 + i] : NAN;
     if (efficiency) *efficiency = p->efficiency[p->pslot];
     return (int)p->hstate.p[3];
+}
+
+// Inverse of a flow with the given parameters on M latent points (host
+// arrays), for checks against the CPU restatement: tc = 1 runs the
+// tensor-core kernel (BF16 weights and conditioner input), tc = 0 the FP32
+// one; bf16 selects BF16 hidden activations for the latter.
+int lg_flow_inverse_check(int device, int d, int layers, int width, int hidden, int bf16, int tc,
+                          const float* params, const float* z, int M, float* u, float* ldet)
+{
+    if (!params || !z || !u || !ldet || M <= 0) return LG_ERR_INPUT;
+    if (cudaSetDevice(device) != cudaSuccess) return LG_ERR_CUDA;
+    lg::Flow f;
+    f.bf16 = bf16 != 0 || tc != 0;
+    if (!f.init(d, layers, width, hidden, 1)) {
+        lg::set_global_error(f.err.c_str());
+        return f.err.empty() ? LG_ERR_ALLOC : LG_ERR_INPUT;
+    }
+    if (tc && !f.tc) {
+        lg::set_global_error("flow inverse check: the tensor-core path needs width % 32 == 0 (<= 256) on sm_100+");
+        return LG_ERR_UNSUPPORTED;
+    }
+    f.tc = tc != 0;
+    lg::DevBuf<float> dz, du, dl;
+    lg::DevBuf<__nv_bfloat16> pk;
+    lg::DevBuf<int> e;
+    if (!dz.ensure((size_t)M * d) || !du.ensure((size_t)M * d) || !dl.ensure(M) || !e.ensure(1) ||
+        (f.tc && !pk.ensure(f.packed_size())))
+        return LG_ERR_ALLOC;
+    cudaMemcpy(f.P.p, params, f.nparams * 4, cudaMemcpyHostToDevice);
+    cudaMemcpy(dz.p, z, (size_t)M * d * 4, cudaMemcpyHostToDevice);
+    cudaMemset(e.p, 0, sizeof(int));
+    if ((f.tc && !f.pack(f.P.p, pk.p, f.stream)) ||
+        !f.inverse(f.P.p, f.tc ? pk.p : nullptr, dz.p, M, du.p, dl.p, f.stream, e.p))
+        return LG_ERR_CUDA;
+    int herr = 0;
+    if (cudaMemcpyAsync(u, du.p, (size_t)M * d * 4, cudaMemcpyDeviceToHost, f.stream) ||
+        cudaMemcpyAsync(ldet, dl.p, (size_t)M * 4, cudaMemcpyDeviceToHost, f.stream) ||
+        cudaMemcpyAsync(&herr, e.p, sizeof(int), cudaMemcpyDeviceToHost, f.stream) || cudaStreamSynchronize(f.stream))
+        return LG_ERR_CUDA;
+    return herr ? LG_ERR_TIMEOUT : LG_OK;
 }
 
 // Loss and gradient of the flow on n points (standardised space, host

@@ -79,3 +79,41 @@ def loss_grad(params, x, d, layers, width, hidden):
         du[:, a0:a0 + da] += dcur
         dv = du
     return loss, grad
+
+
+def bf16(a):
+    """Round float64 values to bfloat16 (through float32, round to nearest
+    even), returned as float64."""
+    f = np.asarray(a, np.float64).astype(np.float32)
+    bits = f.view(np.uint32).astype(np.uint64)
+    bits = (bits + 0x7FFF + ((bits >> 16) & 1)) & 0xFFFF0000
+    return bits.astype(np.uint32).view(np.float32).astype(np.float64)
+
+
+def inverse(params, z, d, layers, width, hidden, mode="fp32"):
+    """Inverse flow z -> u and log|det du/dz| in float64, with the rounding
+    points of the library's kernels: mode "fp32" none, "bf16" hidden
+    activations rounded to bfloat16 (FP32-weight kernel), "tc" also the
+    weights and the conditioner input (tensor-core kernel)."""
+    L, n = layout(d, layers, width, hidden)
+    p = np.asarray(params, np.float64)
+    cur = np.array(z, np.float64)
+    ld = np.zeros(cur.shape[0])
+    for (da, db, a0, b0, dense) in reversed(L):
+        x = cur[:, a0:a0 + da]
+        if mode == "tc":
+            x = bf16(x)
+        for k, (w0, kin, kout, b) in enumerate(dense):
+            W = p[w0:w0 + kin * kout].reshape(kin, kout)
+            if mode == "tc":
+                W = bf16(W)
+            x = x @ W + p[b:b + kout]
+            if k < len(dense) - 1:
+                x = np.maximum(x, 0)
+                if mode in ("bf16", "tc"):
+                    x = bf16(x)
+        sr, t = x[:, :db], x[:, db:]
+        s = CLAMP * np.tanh(sr / CLAMP)
+        cur[:, b0:b0 + db] = (cur[:, b0:b0 + db] - t) * np.exp(-s)
+        ld -= s.sum(1)
+    return cur, ld

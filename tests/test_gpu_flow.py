@@ -85,3 +85,40 @@ def test_retraining_lowers_the_held_out_loss(native):
           f"kept fraction {eff:.4f}")
     assert np.nanmin(hist[1:]) < hist[0] - 1.0
     assert len(hist) - 1 <= 40
+
+
+def _inverse_case(tc, bf16, d=13, layers=8, width=128, hidden=2, M=1000):
+    import ctypes as C
+
+    rng = np.random.Generator(np.random.PCG64(7))
+    npar = lg.lib().lg_flow_nparams(d, layers, width, hidden)
+    params = (rng.normal(size=npar) * 0.08).astype(np.float32)
+    z = rng.normal(size=(M, d)).astype(np.float32)
+    u = np.zeros((M, d), np.float32)
+    ld = np.zeros(M, np.float32)
+    P = lambda a: a.ctypes.data_as(C.POINTER(C.c_float))
+    rc = lg.lib().lg_flow_inverse_check(0, d, layers, width, hidden, bf16, tc, P(params), P(z), M, P(u), P(ld))
+    assert rc == 0, lg.lib().lg_last_error(None)
+    mode = "tc" if tc else ("bf16" if bf16 else "fp32")
+    want_u, want_ld = flow_oracle.inverse(params.astype(np.float64), z.astype(np.float64), d, layers, width,
+                                          hidden, mode)
+    du = np.abs(u - want_u) / (1 + np.abs(want_u))
+    dl = np.abs(ld - want_ld) / (1 + np.abs(want_ld))
+    print(f"inverse {mode}: u error max {du.max():.3g} median {np.median(du):.3g}; "
+          f"logdet error max {dl.max():.3g} median {np.median(dl):.3g}")
+    return du, dl
+
+
+def test_inverse_fp32_kernel(native):
+    du, dl = _inverse_case(tc=0, bf16=0)
+    assert du.max() <= 1e-4 and dl.max() <= 1e-4
+
+
+def test_inverse_tensor_core_kernel(native):
+    """The proposals' inverse on tcgen05 (BF16 operands in shared memory,
+    FP32 accumulators in tensor memory) against the same map in float64 with
+    the same BF16 rounding points: agreement to FP32 accumulation order,
+    except where an FP32 difference flips a BF16 rounding downstream."""
+    du, dl = _inverse_case(tc=1, bf16=1)
+    assert np.median(du) <= 1e-5 and np.median(dl) <= 1e-5
+    assert du.max() <= 2e-2 and dl.max() <= 2e-2
