@@ -112,6 +112,36 @@ def run_sampler(args):
     print(json.dumps(line), flush=True)
 
 
+def run_flow_inverse(args):
+    """The learned proposal's inverse flow (d = 13, 8 coupling layers, width
+    128) on M latent points with random weights, through the tcgen05 kernel
+    and the FP32 kernel (lg_flow_inverse_check: host copies included in the
+    wall times; kernel times come from ncu)."""
+    import ctypes as C
+
+    import lensed_gb300 as lg
+
+    d, layers, width, hidden = 13, 8, 128, 2
+    M = args.batch or 65536
+    rng = np.random.Generator(np.random.PCG64(7))
+    npar = lg.lib().lg_flow_nparams(d, layers, width, hidden)
+    params = (rng.normal(size=npar) * 0.08).astype(np.float32)
+    z = rng.normal(size=(M, d)).astype(np.float32)
+    P = lambda a: a.ctypes.data_as(C.POINTER(C.c_float))
+    out = {}
+    for tc in (1, 0):
+        u = np.zeros((M, d), np.float32)
+        ld = np.zeros(M, np.float32)
+        t0 = time.perf_counter()
+        rc = lg.lib().lg_flow_inverse_check(0, d, layers, width, hidden, 1, tc, P(params), P(z), M, P(u), P(ld))
+        out["tc" if tc else "fp32"] = {"rc": rc, "wall_s": time.perf_counter() - t0, "u": u, "ld": ld}
+    line = {"metric": "learned-proposal inverse flow", "M": M, "flow": [d, layers, width, hidden],
+            "wall_s": {k: v["wall_s"] for k, v in out.items()}, "rc": {k: v["rc"] for k, v in out.items()},
+            "max_abs_diff_u": float(np.abs(out["tc"]["u"] - out["fp32"]["u"]).max()),
+            "max_abs_diff_logdet": float(np.abs(out["tc"]["ld"] - out["fp32"]["ld"]).max())}
+    print(json.dumps(line), flush=True)
+
+
 def run_systems(args):
     """16 systems of uneven sizes, 256 candidates each, one batch per step
     through lg_systems_eval (host buffers in and out: value = e2e)."""
@@ -308,6 +338,8 @@ def main():
         return run_systems(args)
     if args.workload == "sampler":
         return run_sampler(args)
+    if args.workload == "flow-inverse":
+        return run_flow_inverse(args)
 
     import torch
 
