@@ -22,6 +22,8 @@ the correctly rounded values); its tolerances:
   * the FP32 paths' distance to the FP64 oracle is reported, not bounded
     tighter than the FP32 budget.
 """
+import os
+
 import numpy as np
 import pytest
 
@@ -183,6 +185,31 @@ def test_loglike_config2_full_size(native):
     assert np.all(d32 <= logl_tol(w32))
     assert np.abs(got - w32).max() < 0.5 * np.abs(w32 - w64).max()
     assert ctx.masked == int((ctx._weight == 0).sum())
+
+
+def test_loglike_large_workload_full_size(native):
+    """The large configuration at full size: 1024^2 at 0.02"/px, EPL+shear +
+    NSIE satellite + point mass, two Sersic sources and a Gaussian clump,
+    sky, 41x41 PSF, 49-point g3k7 rule.  Two candidates against the FP32
+    oracle (tolerance as everywhere) with the error against the all-FP64
+    oracle stated for each, in fast and strict mode."""
+    s = workloads.large()
+    cand = workloads.draw_candidates(s, 2, seed=3)
+    threads = max(16, os.cpu_count() or 1)
+    o32 = Oracle(s.plugins, s.width, s.height, quadrature.rule(s.rule), psf=s.psf, image=s.image, weight=s.weight,
+                 precision=32, threads=threads)
+    o64 = Oracle(s.plugins, s.width, s.height, quadrature.rule(s.rule), psf=s.psf, image=s.image, weight=s.weight,
+                 precision=64, threads=threads)
+    w32, w64 = o32.loglike(cand), o64.loglike(cand)
+    for flags, name in ((0, "large fast"), (lg.LG_FLAG_STRICT_FP, "large strict")):
+        ctx = lg.Context(s.image, s.weight, s.objects, psf=s.psf, rule=s.rule, max_batch=2, flags=flags)
+        got = ctx.eval_batch(ctx.to_map_order(cand))
+        d32 = _report(name, got, w32, w64)
+        print(f"{name}: relative error vs the FP64 oracle {np.array2string(np.abs(got - w64) / np.abs(w64), precision=2)}")
+        assert np.all(d32 <= logl_tol(w32))
+        if flags:
+            assert d32.max() <= 1e-6 * np.abs(w32).max()
+        ctx.close()
 
 
 def test_loglike_config2_fast_ieee_division(native):
