@@ -410,14 +410,22 @@ def main():
     e2e_dt = (time.perf_counter() - t0) / ne2e
     e2e = replicas.aggregate(B, replicas.max_over_ranks(e2e_dt, dist, device=f"cuda:{local}"), world)
 
-    # plain mode: one candidate per call with a host sync (the reference flow)
-    plain = None
+    # plain mode: one candidate per call with a host sync (the reference
+    # flow, e.g. MultiNest's callback), on a context created for it
+    # (max_batch = 1; its launch shape tuned for one candidate)
+    plain, plain_shape = None, None
     if rank == 0:
-        n1 = 200
+        ctx1 = lg.Context(s.image, s.weight, s.objects, psf=s.psf, rule=s.rule, device=local, max_batch=1,
+                          flags=args.flags | (0 if args.no_autotune else lg.LG_FLAG_AUTOTUNE))
+        plain_shape = ctx1.launch_shape
+        for i in range(20):
+            ctx1.eval_batch(hp[i % B: i % B + 1])
+        n1 = 400
         t0 = time.perf_counter()
         for i in range(n1):
-            ctx.eval_batch(hp[i % B: i % B + 1])
+            ctx1.eval_batch(hp[i % B: i % B + 1])
         plain = n1 / (time.perf_counter() - t0)
+        ctx1.close()
 
     # roofline of the dominant kernel
     N, Q = s.width * s.height, len(lg.quad_rules()[s.rule][1])
@@ -456,7 +464,7 @@ def main():
             "vs_baseline": None, "dtype": "f32 (f64 chi^2 reduction)", "data": "synthetic",
             "config": config, "gpu_launches": 4 * args.steps,
             "e2e": {"value": e2e, "unit": UNIT, "h2d_bytes_per_step": int(hp.nbytes), "d2h_bytes_per_step": 8 * B},
-            "plain_evals_per_s": plain, "roofline": roof}
+            "plain_evals_per_s": plain, "plain_launch_shape": plain_shape, "roofline": roof}
     if clk:
         line["clocks"] = clk
     if rank == 0 and world == 1 and not args.no_cpu_baseline:

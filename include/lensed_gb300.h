@@ -338,6 +338,10 @@ typedef struct {
     long maxiter;   /* 0: unlimited */
     int proposal;   /* LG_PROPOSAL_* */
     int flow_every; /* retrain the flow every this many replacements */
+    const int* wrap; /* ndims flags or NULL: periodic parameters (the prior keyword "wrap", passed to
+                        MultiNest by the reference, src/lensed.c:1254-1275); a proposal outside [0, 1]
+                        on such a dimension is wrapped into it instead of rejected.  lg_nested_run takes
+                        them from the context's priors when NULL */
 } lg_nested_options;
 
 typedef struct {

@@ -54,7 +54,8 @@ class _ObjectDesc(C.Structure):
 
 class NestedOptions(C.Structure):
     _fields_ = [("nlive", C.c_int), ("tol", C.c_double), ("efr", C.c_double), ("batch", C.c_int),
-                ("seed", C.c_int), ("maxiter", C.c_long), ("proposal", C.c_int), ("flow_every", C.c_int)]
+                ("seed", C.c_int), ("maxiter", C.c_long), ("proposal", C.c_int), ("flow_every", C.c_int),
+                ("wrap", C.POINTER(C.c_int))]
 
 
 class NestedResult(C.Structure):
@@ -226,6 +227,11 @@ def _nested_opts(**kw):
     for k, v in kw.items():
         if not hasattr(o, k):
             raise TypeError(f"unknown nested option {k}")
+        if k == "wrap":
+            # periodic dimensions: a sequence of flags, kept alive with the options
+            arr = (C.c_int * len(v))(*[int(bool(x)) for x in v])
+            o._wrap_keep = arr
+            v = C.cast(arr, C.POINTER(C.c_int))
         setattr(o, k, v)
     return o
 

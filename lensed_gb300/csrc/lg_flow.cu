@@ -1039,12 +1039,13 @@ __global__ void __launch_bounds__(1024) lg_flow_expsum(const float* __restrict__
 }
 
 // Rejection and cube tests of M proposals: keep draw i with probability
-// exp(ldet_i - lmax) (lmax = bound[0]), then x = mean + sdev u must lie in the
-// unit cube.  flag[i] = 2 kept and inside, 1 kept outside, 0 rejected.
+// exp(ldet_i - lmax) (lmax = bound[0]), then x = mean + sdev u, wrapped into
+// [0, 1) on periodic dimensions, must lie in the unit cube.  flag[i] = 2
+// kept and inside, 1 kept outside, 0 rejected.
 __global__ void __launch_bounds__(256)
     lg_flow_accept(unsigned long long key, int M, int d, const float* __restrict__ U, const float* __restrict__ ldet,
                    const double* __restrict__ bound, const float* __restrict__ mean, const float* __restrict__ sdev,
-                   double* __restrict__ X, int* __restrict__ flag)
+                   const int* __restrict__ wrap, double* __restrict__ X, int* __restrict__ flag)
 {
     const int i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= M) return;
@@ -1053,7 +1054,8 @@ __global__ void __launch_bounds__(256)
     if (isfinite(l) && !(lg_u01(key, (unsigned long long)i) > exp((double)l - bound[0]))) {
         f = 2;
         for (int a = 0; a < d; ++a) {
-            const double x = (double)mean[a] + (double)sdev[a] * (double)U[(size_t)i * d + a];
+            double x = (double)mean[a] + (double)sdev[a] * (double)U[(size_t)i * d + a];
+            if (wrap[a]) x -= floor(x);  // periodic dimension
             X[(size_t)i * d + a] = x;
             if (!(x >= 0.0 && x <= 1.0)) f = 1;
         }
@@ -1322,6 +1324,8 @@ public:
     DevBuf<float> Puse[2], dmean[2], dsdev[2];
     DevBuf<__nv_bfloat16> dpack[2];  // tensor-core operands of Puse
     DevBuf<int> dtcerr;              // set by the tensor-core inverse on a timeout
+    DevBuf<int> dwrap;               // periodic dimensions
+    std::vector<int> wrap;
     DevBuf<double> dres[2];  // [0] max |z|^2 of the live points, [1] max log weight, [2] sum exp(w - max)
     std::vector<float> hmean[2], hsdev[2];
     double radius[2] = {0, 0}, wnorm[2] = {0, 0}, efficiency[2] = {0, 0};
@@ -1506,6 +1510,14 @@ public:
                          ntrain, (int)hstate.p[3], hstate.p[0], radius[k], efficiency[k], (int)usable[k], d);
     }
 
+    void set_wrap(const int* w, int d) override
+    {
+        wrap.assign(d, 0);
+        if (w)
+            for (int a = 0; a < d; ++a) wrap[a] = w[a] != 0;
+        if (dwrap.ensure(d)) cudaMemcpy(dwrap.p, wrap.data(), d * sizeof(int), cudaMemcpyHostToDevice);
+    }
+
     void advance(long since_train) override
     {
         if (pending && since_train >= opt.lag) finish();
@@ -1542,8 +1554,9 @@ public:
             lg_flow_latent<<<(M + 255) / 256, 256, 0, ps>>>(k_lat, M, d, dres[k].p, opt.expand, dz.p);
             if (!flow.inverse(Puse[k].p, dpack[k].p, dz.p, M, du.p, dld.p, ps, dtcerr.p + 1)) return fail_cuda(), 0;
             lg_flow_max<<<1, 1024, 0, ps>>>(dld.p, M, wnorm[k], dbound.p);
+            if ((int)wrap.size() != d) set_wrap(nullptr, d);
             lg_flow_accept<<<(M + 255) / 256, 256, 0, ps>>>(k_acc, M, d, du.p, dld.p, dbound.p, dmean[k].p,
-                                                             dsdev[k].p, dX.p, dflag.p);
+                                                             dsdev[k].p, dwrap.p, dX.p, dflag.p);
             lg_flow_compact<<<1, 1024, 0, ps>>>(dflag.p, M, dX.p, d, B - got, dout.p + (size_t)got * d, dcnt.p);
             if (cudaMemcpyAsync(hcnt.p, dcnt.p, 2 * sizeof(int), cudaMemcpyDeviceToHost, ps) ||
                 cudaMemcpyAsync(hcnt.p + 2, dtcerr.p + 1, sizeof(int), cudaMemcpyDeviceToHost, ps) ||

@@ -135,6 +135,7 @@ int nested_sample(int nd, lg_batch_loglike fn, void* user, const lg_nested_optio
         return LG_ERR_INPUT;
     }
     const int nl = opt.nlive, B = opt.batch;
+    if (learned) learned->set_wrap(opt.wrap, nd);
     Rng rng((uint64_t)(opt.seed < 0 ? std::chrono::steady_clock::now().time_since_epoch().count() : opt.seed));
     std::vector<double> live((size_t)nl * nd), llive(nl);
     std::vector<double> buf((size_t)B * nd), lbuf(B);
@@ -248,7 +249,10 @@ int nested_sample(int nd, lg_batch_loglike fn, void* user, const lg_nested_optio
                     double* x = &buf[(size_t)n * nd];
                     ell.sample(rng, x, u);
                     bool in = true;
-                    for (int a = 0; a < nd && in; ++a) in = x[a] >= 0 && x[a] <= 1;
+                    for (int a = 0; a < nd && in; ++a) {
+                        if (opt.wrap && opt.wrap[a]) x[a] -= std::floor(x[a]);
+                        in = x[a] >= 0 && x[a] <= 1;
+                    }
                     if (in) ++n;
                 }
                 n_ell += n;
@@ -342,6 +346,7 @@ lg_nested_options lg_nested_defaults(void)
     o.maxiter = 0;
     o.proposal = LG_PROPOSAL_ELLIPSOID;
     o.flow_every = 1000;
+    o.wrap = nullptr;
     return o;
 }
 
@@ -384,6 +389,12 @@ extern "C" int lg_nested_run(lg_ctx* ctx, const lg_nested_options* opts, const l
     lg_nested_options o = opts ? *opts : lg_nested_defaults();
     CtxUser u{ctx, lg::ctx_max_batch(ctx)};
     if (o.batch > u.max_batch) o.batch = u.max_batch;
+    // periodic parameters from the priors' "wrap" keyword (src/lensed.c:1254-1259)
+    std::vector<int> wrap(std::max(lg_ndims(ctx), 0), 0);
+    if (!o.wrap) {
+        for (int i = 0; i < (int)wrap.size(); ++i) lg_param(ctx, i, nullptr, &wrap[i], nullptr, nullptr);
+        o.wrap = wrap.data();
+    }
     std::string err;
     std::unique_ptr<lg::Proposal> prop;
     if (o.proposal == LG_PROPOSAL_FLOW) {

@@ -61,6 +61,8 @@ struct Proposal {
     // last train(): a proposal that trains in the background switches to
     // its new state at a fixed count, so that runs are reproducible
     virtual void advance(long since_train) { (void)since_train; }
+    // periodic dimensions: proposals are wrapped into [0, 1) there
+    virtual void set_wrap(const int* wrap, int d) { (void)wrap, (void)d; }
     // log volume (unit-cube coordinates) of the region propose() draws from
     virtual double log_volume() const = 0;
 };

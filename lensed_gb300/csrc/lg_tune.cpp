@@ -73,11 +73,12 @@ std::vector<Shape> conv_candidates(const Shape& base, bool multi)
     // row halves, so their height is even and their outputs a multiple of 8.
     // The multi-system kernels count thread rows (a paired unit covers two
     // of them per thread) and need outputs in multiples of 8.
-    static const int paired[][3] = {{32, 64, 8}, {32, 32, 8}, {64, 64, 8}, {64, 32, 8}, {32, 64, 16}};
-    static const int single[][3] = {{32, 32, 8}, {32, 16, 8}, {64, 32, 8}, {32, 32, 16}, {32, 64, 8}};
-    static const int units[][3] = {{32, 32, 8}, {32, 16, 8}, {64, 32, 8}, {64, 16, 8}, {32, 32, 16}};
+    // (the smallest tiles keep small batches spread over the SMs)
+    static const int paired[][3] = {{32, 64, 8}, {32, 32, 8}, {64, 64, 8}, {64, 32, 8}, {32, 64, 16}, {32, 16, 8}};
+    static const int single[][3] = {{32, 32, 8}, {32, 16, 8}, {64, 32, 8}, {32, 32, 16}, {32, 64, 8}, {32, 8, 8}};
+    static const int units[][3] = {{32, 32, 8}, {32, 16, 8}, {64, 32, 8}, {64, 16, 8}, {32, 32, 16}, {32, 8, 8}};
     std::vector<Shape> out;
-    const int n = 5;
+    const int n = 6;
     for (int i = 0; i < n; ++i) {
         const int* c = multi ? units[i] : base.pair_rows ? paired[i] : single[i];
         Shape s = base;

@@ -122,3 +122,20 @@ def test_inverse_tensor_core_kernel(native):
     du, dl = _inverse_case(tc=1, bf16=1)
     assert np.median(du) <= 1e-5 and np.median(dl) <= 1e-5
     assert du.max() <= 2e-2 and dl.max() <= 2e-2
+
+
+def test_learned_proposal_with_a_wrapped_dimension(native):
+    """The flow's proposals wrap periodic dimensions into the cube as the
+    ellipsoid's do (Gaussian centred on the boundary 0 = 1 of dimension 0)."""
+    sigma = 0.05
+
+    def f(x):
+        d0 = x[:, 0] - np.round(x[:, 0])
+        return -0.5 * (d0 / sigma) ** 2 - 0.5 * np.sum(((x[:, 1:] - 0.5) / sigma) ** 2, axis=1)
+
+    exact = 2.0 * math.log(2 * math.pi * sigma ** 2)
+    r = lg.nested_sample_flow(f, 4, nlive=400, batch=512, seed=3, tol=0.1, flow_every=400, wrap=[1, 0, 0, 0],
+                              flow=dict(layers=4, width=64, epochs=60, lag=200))
+    print(f"wrapped Gaussian d=4: exact {exact:.3f}, flow {r['logz']:.3f}+-{r['logz_err']:.3f}, "
+          f"calls {r['ncall']}, flow proposals {r['n_flow_proposals']}")
+    assert abs(r["logz"] - exact) < 4 * r["logz_err"] + 0.1

@@ -45,3 +45,24 @@ def test_callback_errors_propagate(native):
         raise RuntimeError("boom")
     with pytest.raises(RuntimeError):
         lg.nested_sample(bad, 2, nlive=20, batch=8)
+
+
+def test_wrapped_dimension(native):
+    """A periodic parameter (the prior keyword "wrap"): the likelihood in
+    dimension 0 is a Gaussian centred on the boundary 0 = 1 of a periodic
+    coordinate; with wrap on, proposals leaving the cube there re-enter on
+    the other side, and the evidence is the full Gaussian integral."""
+    sigma = 0.05
+
+    def f(x):
+        d0 = x[:, 0] - np.round(x[:, 0])  # periodic distance to 0 = 1
+        return -0.5 * (d0 / sigma) ** 2 - 0.5 * np.sum(((x[:, 1:] - 0.5) / sigma) ** 2, axis=1)
+
+    exact = 1.5 * math.log(2 * math.pi * sigma ** 2)
+    r = lg.nested_sample(f, 3, nlive=300, batch=256, seed=11, tol=0.05, wrap=[1, 0, 0])
+    assert abs(r["logz"] - exact) < 4 * r["logz_err"] + 0.05, (r["logz"], exact)
+    w = np.exp(r["logwt"])
+    x0 = r["samples"][:, 0]
+    # posterior mass on both sides of the boundary, none in the middle
+    assert w[x0 < 0.2].sum() > 0.3 and w[x0 > 0.8].sum() > 0.3
+    assert w[(x0 > 0.3) & (x0 < 0.7)].sum() < 1e-3
