@@ -342,6 +342,10 @@ typedef struct {
                         MultiNest by the reference, src/lensed.c:1254-1275); a proposal outside [0, 1]
                         on such a dimension is wrapped into it instead of rejected.  lg_nested_run takes
                         them from the context's priors when NULL */
+    const char* checkpoint; /* state file or NULL: the counterpart of MultiNest's resume files
+                               (option resume, src/input/options.c:217-221) */
+    int checkpoint_every;   /* write the state every this many iterations (0: only when stopping) */
+    int resume;             /* continue from the state file when it exists and matches */
 } lg_nested_options;
 
 typedef struct {

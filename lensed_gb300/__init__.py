@@ -55,7 +55,8 @@ class _ObjectDesc(C.Structure):
 class NestedOptions(C.Structure):
     _fields_ = [("nlive", C.c_int), ("tol", C.c_double), ("efr", C.c_double), ("batch", C.c_int),
                 ("seed", C.c_int), ("maxiter", C.c_long), ("proposal", C.c_int), ("flow_every", C.c_int),
-                ("wrap", C.POINTER(C.c_int))]
+                ("wrap", C.POINTER(C.c_int)), ("checkpoint", C.c_char_p), ("checkpoint_every", C.c_int),
+                ("resume", C.c_int)]
 
 
 class NestedResult(C.Structure):
@@ -227,6 +228,8 @@ def _nested_opts(**kw):
     for k, v in kw.items():
         if not hasattr(o, k):
             raise TypeError(f"unknown nested option {k}")
+        if k == "checkpoint" and isinstance(v, str):
+            v = os.fsencode(v)
         if k == "wrap":
             # periodic dimensions: a sequence of flags, kept alive with the options
             arr = (C.c_int * len(v))(*[int(bool(x)) for x in v])

@@ -124,6 +124,87 @@ double logaddexp(double a, double b)
 
 }  // namespace
 
+// The sampler's state between two iterations: written to the checkpoint
+// file and read back to resume.  A resumed run with the ellipsoidal proposal
+// continues exactly as the uninterrupted run would (same draws, same
+// result); the learned proposal is not part of the state and is retrained
+// at its next scheduled retraining.
+struct SamplerState {
+    int nd = 0, nl = 0, batch = 0;
+    long iter = 0, ncall = 0, since_train = 0, n_flow = 0, n_ell = 0, n_flow_fail = 0;
+    double logz = -HUGE_VAL, H = 0, logx = 0;
+    uint64_t rng[4] = {0, 0, 0, 0};
+    std::vector<double> live, llive, dead_x, dead_l, dead_lw, pool_x, pool_l;
+    uint64_t pool_pos = 0;
+};
+
+namespace {
+
+const char kStateMagic[8] = {'L', 'G', 'N', 'S', 'T', 'A', 'T', '1'};
+
+template <class T>
+bool put(FILE* f, const T& v)
+{
+    return std::fwrite(&v, sizeof v, 1, f) == 1;
+}
+template <class T>
+bool get(FILE* f, T& v)
+{
+    return std::fread(&v, sizeof v, 1, f) == 1;
+}
+bool put_vec(FILE* f, const std::vector<double>& v)
+{
+    const uint64_t n = v.size();
+    return put(f, n) && (n == 0 || std::fwrite(v.data(), sizeof(double), n, f) == n);
+}
+bool get_vec(FILE* f, std::vector<double>& v)
+{
+    uint64_t n = 0;
+    if (!get(f, n) || n > (uint64_t)1 << 34) return false;
+    v.resize(n);
+    return n == 0 || std::fread(v.data(), sizeof(double), n, f) == n;
+}
+
+// Write the state to path (through a temporary file renamed over it, so an
+// interrupted write leaves the previous state intact).
+bool save_state(const char* path, const SamplerState& s)
+{
+    const std::string tmp = std::string(path) + ".tmp";
+    FILE* f = std::fopen(tmp.c_str(), "wb");
+    if (!f) return false;
+    bool ok = std::fwrite(kStateMagic, 1, 8, f) == 8 && put(f, s.nd) && put(f, s.nl) && put(f, s.batch) &&
+              put(f, s.iter) && put(f, s.ncall) && put(f, s.since_train) && put(f, s.n_flow) && put(f, s.n_ell) &&
+              put(f, s.n_flow_fail) && put(f, s.logz) && put(f, s.H) && put(f, s.logx);
+    for (int i = 0; i < 4 && ok; ++i) ok = put(f, s.rng[i]);
+    ok = ok && put_vec(f, s.live) && put_vec(f, s.llive) && put_vec(f, s.dead_x) && put_vec(f, s.dead_l) &&
+         put_vec(f, s.dead_lw) && put_vec(f, s.pool_x) && put_vec(f, s.pool_l) && put(f, s.pool_pos);
+    ok = (std::fclose(f) == 0) && ok;
+    return ok && std::rename(tmp.c_str(), path) == 0;
+}
+
+// Read a state written by save_state; false if absent, unreadable or for
+// another dimension, live-point count or batch size.
+bool load_state(const char* path, int nd, int nl, int batch, SamplerState& s)
+{
+    FILE* f = std::fopen(path, "rb");
+    if (!f) return false;
+    char magic[8];
+    bool ok = std::fread(magic, 1, 8, f) == 8 && std::memcmp(magic, kStateMagic, 8) == 0 && get(f, s.nd) &&
+              get(f, s.nl) && get(f, s.batch) && s.nd == nd && s.nl == nl && s.batch == batch && get(f, s.iter) &&
+              get(f, s.ncall) && get(f, s.since_train) && get(f, s.n_flow) && get(f, s.n_ell) &&
+              get(f, s.n_flow_fail) && get(f, s.logz) && get(f, s.H) && get(f, s.logx);
+    for (int i = 0; i < 4 && ok; ++i) ok = get(f, s.rng[i]);
+    ok = ok && get_vec(f, s.live) && get_vec(f, s.llive) && get_vec(f, s.dead_x) && get_vec(f, s.dead_l) &&
+         get_vec(f, s.dead_lw) && get_vec(f, s.pool_x) && get_vec(f, s.pool_l) && get(f, s.pool_pos);
+    std::fclose(f);
+    ok = ok && s.live.size() == (size_t)nl * nd && s.llive.size() == (size_t)nl &&
+         s.dead_x.size() == s.dead_l.size() * nd && s.dead_lw.size() == s.dead_l.size() &&
+         s.pool_x.size() == s.pool_l.size() * nd && s.pool_pos <= s.pool_l.size();
+    return ok;
+}
+
+}  // namespace
+
 int nested_sample(int nd, lg_batch_loglike fn, void* user, const lg_nested_options* o, lg_nested_result* res,
                   Proposal* learned, std::string& err)
 {
@@ -150,8 +231,10 @@ int nested_sample(int nd, lg_batch_loglike fn, void* user, const lg_nested_optio
         ncall += n;
         return rc;
     };
+    SamplerState st;
+    const bool resumed = opt.checkpoint && opt.resume && load_state(opt.checkpoint, nd, nl, B, st);
     // initial live points: uniform in the cube
-    for (int i0 = 0; i0 < nl; i0 += B) {
+    for (int i0 = 0; !resumed && i0 < nl; i0 += B) {
         const int n = std::min(B, nl - i0);
         for (size_t k = 0; k < (size_t)n * nd; ++k) buf[k] = rng.uniform();
         if (int rc = evaluate(buf.data(), n, lbuf.data())) {
@@ -178,8 +261,66 @@ int nested_sample(int nd, lg_batch_loglike fn, void* user, const lg_nested_optio
     long iter = 0, since_train = 0, n_flow = 0, n_ell = 0, n_flow_fail = 0;
     bool use_flow = false;
     int status = LG_OK;
+    if (resumed) {
+        live = st.live;
+        llive = st.llive;
+        dead_x = st.dead_x;
+        dead_l = st.dead_l;
+        dead_lw = st.dead_lw;
+        pool_x = st.pool_x;
+        pool_l = st.pool_l;
+        pool_pos = (size_t)st.pool_pos;
+        logz = st.logz;
+        H = st.H;
+        logx = st.logx;
+        iter = st.iter;
+        ncall = st.ncall;
+        since_train = st.since_train;
+        n_flow = st.n_flow;
+        n_ell = st.n_ell;
+        n_flow_fail = st.n_flow_fail;
+        for (int i = 0; i < 4; ++i) rng.s[i] = st.rng[i];
+    }
+    // the state between iterations, for the checkpoint file
+    auto checkpoint = [&]() {
+        if (!opt.checkpoint) return true;
+        SamplerState c;
+        c.nd = nd;
+        c.nl = nl;
+        c.batch = B;
+        c.iter = iter;
+        c.ncall = ncall;
+        c.since_train = since_train;
+        c.n_flow = n_flow;
+        c.n_ell = n_ell;
+        c.n_flow_fail = n_flow_fail;
+        c.logz = logz;
+        c.H = H;
+        c.logx = logx;
+        for (int i = 0; i < 4; ++i) c.rng[i] = rng.s[i];
+        c.live = live;
+        c.llive = llive;
+        c.dead_x = dead_x;
+        c.dead_l = dead_l;
+        c.dead_lw = dead_lw;
+        c.pool_x = pool_x;
+        c.pool_l = pool_l;
+        c.pool_pos = pool_pos;
+        return save_state(opt.checkpoint, c);
+    };
     for (;; ++iter) {
-        if (opt.maxiter > 0 && iter >= opt.maxiter) break;
+        if (opt.checkpoint && opt.checkpoint_every > 0 && iter > 0 && iter % opt.checkpoint_every == 0 &&
+            !checkpoint()) {
+            err = std::string("nested sampling: cannot write the checkpoint ") + opt.checkpoint;
+            return LG_ERR_INPUT;
+        }
+        if (opt.maxiter > 0 && iter >= opt.maxiter) {
+            if (!checkpoint()) {
+                err = std::string("nested sampling: cannot write the checkpoint ") + opt.checkpoint;
+                return LG_ERR_INPUT;
+            }
+            break;
+        }
         int imin = 0;
         double lmax = -HUGE_VAL;
         for (int i = 0; i < nl; ++i) {
@@ -187,7 +328,13 @@ int nested_sample(int nd, lg_batch_loglike fn, void* user, const lg_nested_optio
             lmax = std::max(lmax, llive[i]);
         }
         // termination: the live points can still add at most X * Lmax
-        if (iter > 0 && logaddexp(logz, logx + lmax) - logz < opt.tol) break;
+        if (iter > 0 && logaddexp(logz, logx + lmax) - logz < opt.tol) {
+            if (!checkpoint()) {
+                err = std::string("nested sampling: cannot write the checkpoint ") + opt.checkpoint;
+                return LG_ERR_INPUT;
+            }
+            break;
+        }
         const double lmin = llive[imin];
         const double lw = logx + lw_step + lmin;
         const double lznew = logaddexp(logz, lw);
@@ -347,6 +494,9 @@ lg_nested_options lg_nested_defaults(void)
     o.proposal = LG_PROPOSAL_ELLIPSOID;
     o.flow_every = 1000;
     o.wrap = nullptr;
+    o.checkpoint = nullptr;
+    o.checkpoint_every = 0;
+    o.resume = 0;
     return o;
 }
 

@@ -1,6 +1,7 @@
 """The nested sampler on analytic likelihoods (CPU): evidence and moments
 against closed forms, determinism, and the batched proposal pool."""
 import math
+import os
 
 import numpy as np
 import pytest
@@ -66,3 +67,26 @@ def test_wrapped_dimension(native):
     # posterior mass on both sides of the boundary, none in the middle
     assert w[x0 < 0.2].sum() > 0.3 and w[x0 > 0.8].sum() > 0.3
     assert w[(x0 > 0.3) & (x0 < 0.7)].sum() < 1e-3
+
+
+def test_checkpoint_and_resume_continue_exactly(native, tmp_path):
+    """A run stopped after 400 iterations (checkpoints every 150) and resumed
+    from its state file ends with the same evidence, calls and samples as the
+    uninterrupted run: the state holds the live and dead points, the
+    evidence accumulators, the RNG and the pool of evaluated proposals."""
+    f = gaussian(np.array([0.3, 0.6, 0.45]), 0.07)
+    common = dict(nlive=200, batch=64, seed=5, tol=0.05)
+    full = lg.nested_sample(f, 3, **common)
+    path = str(tmp_path / "state.bin")
+    part = lg.nested_sample(f, 3, maxiter=400, checkpoint=path, checkpoint_every=150, **common)
+    assert part["niter"] == 400 and os.path.exists(path)
+    rest = lg.nested_sample(f, 3, checkpoint=path, resume=1, **common)
+    assert rest["logz"] == full["logz"] and rest["ncall"] == full["ncall"] and rest["niter"] == full["niter"]
+    assert np.array_equal(rest["samples"], full["samples"])
+    # a finished state resumes to the same result at once
+    again = lg.nested_sample(f, 3, checkpoint=path, resume=1, **common)
+    assert again["logz"] == full["logz"] and again["ncall"] == full["ncall"]
+    # a state for another problem size is ignored (a fresh run)
+    other = lg.nested_sample(gaussian(np.full(2, 0.5), 0.1), 2, checkpoint=path, resume=1, nlive=100, batch=64,
+                             seed=5)
+    assert other["niter"] > 0
