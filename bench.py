@@ -462,7 +462,7 @@ def main():
     line = {"metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
             "warmup": args.warmup, "ms_per_step": ms / args.steps, "higher_is_better": True, "scaling": "weak",
             "vs_baseline": None, "dtype": "f32 (f64 chi^2 reduction)", "data": "synthetic",
-            "config": config, "gpu_launches": 4 * args.steps,
+            "config": config, "gpu_launches": 3 * args.steps,
             "e2e": {"value": e2e, "unit": UNIT, "h2d_bytes_per_step": int(hp.nbytes), "d2h_bytes_per_step": 8 * B},
             "plain_evals_per_s": plain, "plain_launch_shape": plain_shape, "roofline": roof}
     if clk:

@@ -227,9 +227,10 @@ int lg_write_fits(const char* path, int width, int height, int nlayers, const fl
 int lg_write_fits_memory(int width, int height, int nlayers, const float* const* layers, const char* const* names,
                          void* buf, size_t capacity, size_t* size);
 
-/* Device times (ms) of the four stages of one evaluation of B candidates
- * with device pointers: set_params, render, convolve (0 without a PSF) and
- * the chi^2 finish -- the counterpart of the reference's --profile table
+/* Device times (ms) of the stages of one evaluation of B candidates with
+ * device pointers: set_params, render, convolve + chi^2 (0 without a PSF)
+ * and a fourth entry that is 0 (the chi^2 sum ends the last stage) -- the
+ * counterpart of the reference's --profile table
  * (src/nested.c:21-40, src/profile.c:36-83).  Runs on the context's stream
  * after the work queued on the legacy default stream, and synchronises. */
 int lg_eval_profile(lg_ctx* ctx, const double* d_params, int B, double* d_logL, float* stage_ms);

@@ -2,10 +2,11 @@
 //
 // One context = one lens system resident on one GPU (image, weight, PSF,
 // quadrature and the composed program), with scratch sized for max_batch
-// candidates.  An evaluation of B candidates is four launches on the
-// context's stream -- set_params, render, convolve+chi^2 (PSF only), finish
-// -- captured once per B into a CUDA graph together with the parameter
-// upload and the logL read-back, then replayed.  This replaces, per
+// candidates.  An evaluation of B candidates is three launches on the
+// context's stream -- set_params, render, convolve+chi^2 (PSF only; the
+// block finishing a candidate's last tile writes its logL) -- captured once
+// per B into a CUDA graph together with the parameter upload and the logL
+// read-back, then replayed.  This replaces, per
 // candidate, the reference's map/unmap of the parameter buffer, four OpenCL
 // enqueues, a blocking read of N floats and a host double loop
 // (src/nested.c:63-115).
@@ -92,7 +93,9 @@ struct lg_ctx {
     CUmodule mod = nullptr;      // evaluation module
     CUmodule mod_set = nullptr;  // set_params module
     CUfunction f_setp = nullptr, f_rraw = nullptr, f_rchi2 = nullptr, f_rdump = nullptr;
-    CUfunction f_cchi2 = nullptr, f_cdump = nullptr, f_finish = nullptr;
+    CUfunction f_setp_split = nullptr;  // small batches: one warp per object
+    int nobj = 0;
+    CUfunction f_cchi2 = nullptr, f_cdump = nullptr;
     size_t model_bytes = 0;
     int rtiles = 0, ctiles = 0, ctiles_x = 0, ctiles_y = 0, cthreads = 0, csmem = 0;
 
@@ -104,6 +107,7 @@ struct lg_ctx {
     void* d_models = nullptr;
     float* d_raw = nullptr;
     double* d_partials = nullptr;
+    unsigned* d_counters = nullptr;  // tiles done per candidate (zero between launches)
     double* d_params = nullptr;
     double* d_logL = nullptr;
     float* d_model_out = nullptr;
@@ -142,36 +146,39 @@ struct lg_ctx {
         return drvcall(drv->launchKernel(f, g.x, g.y, g.z, b.x, b.y, b.z, smem, (CUstream)s, args, nullptr), what);
     }
 
-    // Enqueue set_params .. finish for B candidates; params and logL are
-    // device pointers.  With ev != NULL, ev[0..4] are recorded before
-    // set_params, render, convolve and finish and after finish.
+    // Enqueue set_params, render and (with a PSF) convolve for B
+    // candidates; params and logL are device pointers (the last stage ends
+    // with logL, the block finishing a candidate's last tile summing its
+    // partials).  With ev != NULL, ev[0..4] are recorded before set_params,
+    // render, convolve and after the last stage (twice: no separate finish).
     int enqueue(int B, const double* params, double* logL, cudaStream_t s, cudaEvent_t* ev = nullptr)
     {
         int rc;
         auto mark = [&](int i) { return ev ? cuda(cudaEventRecord(ev[i], s), "event") : LG_OK; };
         void* a_setp[] = {&params, &B, &d_models};
-        if ((rc = mark(0)) || (rc = launch(f_setp, dim3((B + 127) / 128), dim3(128), 0, s, a_setp, "set_params")) ||
+        // a handful of candidates: the objects of a candidate side by side
+        // (one warp each); else one thread per candidate
+        const bool split = B <= 32 && nobj > 1 && nobj <= 32;
+        if ((rc = mark(0)) ||
+            (rc = split ? launch(f_setp_split, dim3(B), dim3(32 * nobj), 0, s, a_setp, "set_params")
+                        : launch(f_setp, dim3((B + 127) / 128), dim3(128), 0, s, a_setp, "set_params")) ||
             (rc = mark(1)))
             return rc;
         if (psf) {
             void* a_r[] = {&d_models, &d_raw};
             if ((rc = launch(f_rraw, dim3(rtiles, B), dim3(shape.rt), 0, s, a_r, "render")) || (rc = mark(2)))
                 return rc;
-            void* a_c[] = {&d_raw, &d_image, &d_weight, &d_partials};
+            void* a_c[] = {&d_raw, &d_image, &d_weight, &d_partials, &d_counters, &logL};
             if ((rc = launch(f_cchi2, dim3(ctiles_x, ctiles_y, B), dim3(shape.ctx / shape.cr, shape.conv_block_y()),
                              csmem, s, a_c, "convolve")) ||
                 (rc = mark(3)))
                 return rc;
-            void* a_f[] = {&d_partials, &ctiles, &logL};
-            if ((rc = launch(f_finish, dim3(B), dim3(256), 0, s, a_f, "finish"))) return rc;
             return mark(4);
         }
-        void* a_r[] = {&d_models, &d_image, &d_weight, &d_partials};
+        void* a_r[] = {&d_models, &d_image, &d_weight, &d_partials, &d_counters, &logL};
         if ((rc = launch(f_rchi2, dim3(rtiles, B), dim3(shape.rt), 0, s, a_r, "render")) || (rc = mark(2)) ||
             (rc = mark(3)))
             return rc;
-        void* a_f[] = {&d_partials, &rtiles, &logL};
-        if ((rc = launch(f_finish, dim3(B), dim3(256), 0, s, a_f, "finish"))) return rc;
         return mark(4);
     }
 
@@ -191,6 +198,7 @@ struct lg_ctx {
         cudaFree(d_models);
         cudaFree(d_raw);
         cudaFree(d_partials);
+        cudaFree(d_counters);
         cudaFree(d_params);
         cudaFree(d_logL);
         cudaFree(d_model_out);
@@ -337,6 +345,8 @@ int load_eval(lg_ctx* c, const lg::Shape& s, const std::vector<char>& cubin)
     c->mod = nullptr;
     cudaFree(c->d_partials);
     c->d_partials = nullptr;
+    cudaFree(c->d_counters);
+    c->d_counters = nullptr;
     c->shape = s;
     shape_sizes(s, c->model, c);
     if ((rc = c->drvcall(c->drv->moduleLoadData(&c->mod, cubin.data()), "cuModuleLoadData"))) return rc;
@@ -345,7 +355,7 @@ int load_eval(lg_ctx* c, const lg::Shape& s, const std::vector<char>& cubin)
         const char* n;
         bool need;
     } fns[] = {{&c->f_rraw, "lg_render_raw", true},  {&c->f_rchi2, "lg_render_chi2", true},
-               {&c->f_rdump, "lg_render_dump", true}, {&c->f_finish, "lg_finish", true},
+               {&c->f_rdump, "lg_render_dump", true},
                {&c->f_cchi2, "lg_conv_chi2", c->psf}, {&c->f_cdump, "lg_conv_dump", c->psf}};
     for (auto& f : fns)
         if (f.need && (rc = c->drvcall(c->drv->moduleGetFunction(f.f, c->mod, f.n), f.n))) return rc;
@@ -376,8 +386,11 @@ int load_eval(lg_ctx* c, const lg::Shape& s, const std::vector<char>& cubin)
                 return rc;
     }
     const size_t ntiles = (size_t)(c->psf ? c->ctiles : c->rtiles);
-    if (cudaMalloc((void**)&c->d_partials, (size_t)c->max_batch * ntiles * 8) != cudaSuccess)
+    if (cudaMalloc((void**)&c->d_partials, (size_t)c->max_batch * ntiles * 8) != cudaSuccess ||
+        cudaMalloc((void**)&c->d_counters, (size_t)c->max_batch * sizeof(unsigned)) != cudaSuccess)
         return c->fail(LG_ERR_ALLOC, "cudaMalloc partials");
+    if ((rc = c->cuda(cudaMemset(c->d_counters, 0, (size_t)c->max_batch * sizeof(unsigned)), "clear counters")))
+        return rc;
     return LG_OK;
 }
 
@@ -502,7 +515,8 @@ int autotune(lg_ctx* c)
         rep << line;
         // the base shape is a render candidate; its convolution time also
         // stands for the base convolution
-        const bool base_conv = cand[i].ctx == base.ctx && cand[i].cty == base.cty && cand[i].cr == base.cr;
+        const bool base_conv = cand[i].ctx == base.ctx && cand[i].cty == base.cty && cand[i].cr == base.cr &&
+                               cand[i].pair_rows == base.pair_rows;
         if (is_render[i] && r_ms < best_r) best_r = r_ms, br = cand[i];
         if ((!is_render[i] || base_conv) && c->psf && c_ms < best_c) best_c = c_ms, bc = cand[i];
     }
@@ -511,6 +525,7 @@ int autotune(lg_ctx* c)
         chosen.ctx = bc.ctx;
         chosen.cty = bc.cty;
         chosen.cr = bc.cr;
+        chosen.pair_rows = bc.pair_rows;
     }
     const std::vector<char>* cb = nullptr;
     for (size_t i = 0; i < cand.size(); ++i)
@@ -558,7 +573,9 @@ int create_impl(lg_ctx* c, const lg_image_desc* img, const lg_object_desc* objs,
     if (!c->drv) return c->fail(LG_ERR_CUDA, "CUDA driver entry points unavailable");
     if ((rc = c->drvcall(c->drv->moduleLoadData(&c->mod_set, cubin_set.data()), "cuModuleLoadData"))) return rc;
     if ((rc = c->drvcall(c->drv->moduleGetFunction(&c->f_setp, c->mod_set, "lg_set_params_kernel"),
-                         "lg_set_params_kernel")))
+                         "lg_set_params_kernel")) ||
+        (rc = c->drvcall(c->drv->moduleGetFunction(&c->f_setp_split, c->mod_set, "lg_set_params_split"),
+                         "lg_set_params_split")))
         return rc;
     CUdeviceptr gp;
     size_t gb;
@@ -567,6 +584,9 @@ int create_impl(lg_ctx* c, const lg_image_desc* img, const lg_object_desc* objs,
     unsigned mb = 0;
     if ((rc = c->cuda(cudaMemcpy(&mb, (void*)gp, sizeof mb, cudaMemcpyDeviceToHost), "model size"))) return rc;
     c->model_bytes = mb;
+    if ((rc = c->drvcall(c->drv->moduleGetGlobal(&gp, &gb, c->mod_set, "lg_model_objects"), "lg_model_objects")) ||
+        (rc = c->cuda(cudaMemcpy(&c->nobj, (void*)gp, sizeof c->nobj, cudaMemcpyDeviceToHost), "object count")))
+        return rc;
 
     if ((rc = c->cuda(cudaStreamCreateWithFlags(&c->stream, cudaStreamNonBlocking), "stream"))) return rc;
     const size_t B = (size_t)c->max_batch, N = (size_t)c->N, np = m.pars.size();
@@ -1043,7 +1063,10 @@ int render_device(lg_ctx* c, const double* params, const float** d_model)
         return rc;
     int one = 1;
     void* a_setp[] = {&c->d_params, &one, &c->d_models};
-    if ((rc = c->launch(c->f_setp, dim3(1), dim3(128), 0, c->stream, a_setp, "set_params"))) return rc;
+    if ((rc = c->nobj > 1 && c->nobj <= 32
+                  ? c->launch(c->f_setp_split, dim3(1), dim3(32 * c->nobj), 0, c->stream, a_setp, "set_params")
+                  : c->launch(c->f_setp, dim3(1), dim3(128), 0, c->stream, a_setp, "set_params")))
+        return rc;
     void* a_r[] = {&c->d_models, &d_val, &c->d_err_out};
     if ((rc = c->launch(c->f_rdump, dim3(c->rtiles, 1), dim3(c->shape.rt), 0, c->stream, a_r, "render"))) return rc;
     if (c->psf) {

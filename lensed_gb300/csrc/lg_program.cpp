@@ -145,6 +145,54 @@ void emit_set_params(std::ostringstream& o, const Model& m)
         o << ");\n";
     }
     o << "}\n\n";
+    // the same, one object at a time (for the kernel that gives every object
+    // its own warp): objects with image-plane priors read the lenses of
+    // earlier planes, so they run in a second phase
+    o << "#define LG_NOBJ " << m.objs.size() << "\n";
+    o << "__constant__ int lg_obj_phase[LG_NOBJ] = {";
+    for (size_t i = 0; i < m.objs.size(); ++i) o << (i ? ", " : "") << (m.objs[i].ipp ? 1 : 0);
+    o << "};\n";
+    o << "LG_DEV void lg_set_object(lg_model& m, const float* p, int which)\n{\n"
+      << "    float2 x = make_float2(0.0f, 0.0f);\n    float2 a = make_float2(0.0f, 0.0f);\n"
+      << "    (void)x;\n    (void)a;\n    switch (which) {\n";
+    trigger = 0;
+    plane = 0;
+    for (size_t i = 0; i < m.objs.size(); ++i) {
+        const ObjectInfo& ob = m.objs[i];
+        const Plugin* pl = ob.plugin;
+        if (pl->kind != trigger && pl->kind != LG_FOREGROUND) {
+            if (trigger == LG_LENS && pl->kind == LG_SOURCE) plane = i;
+            trigger = pl->kind;
+        }
+        const int np = (int)pl->pars.size();
+        o << "    case " << i << ": {\n";
+        if (ob.ipp) {
+            int xp = -1;
+            for (int j = 0; j < np; ++j)
+                if (m.pars[ob.par0 + j].prior.ipp && pl->pars[j].type == LG_POSITION_X) xp = j;
+            o << "        x = make_float2(p[" << ob.par0 + xp << "], p[" << ob.par0 + xp + 1 << "]);\n";
+            int trigger2 = 0;
+            for (size_t k = 0; k < plane; ++k) {
+                const Plugin* q = m.objs[k].plugin;
+                if (q->kind != trigger2 && q->kind != LG_FOREGROUND) {
+                    if (trigger2 == LG_LENS) o << "        lg_deflect(x, a);\n        a = make_float2(0.0f, 0.0f);\n";
+                    trigger2 = q->kind;
+                }
+                if (q->kind == LG_LENS) o << "        a += lg_deflection_" << q->name << "(&m.o" << k << ", x);\n";
+            }
+            if (trigger2 == LG_LENS) o << "        lg_deflect(x, a);\n";
+        }
+        o << "        lg_set_" << pl->name << "(&m.o" << i;
+        for (int j = 0; j < np; ++j) {
+            const ParamInfo& pi = m.pars[ob.par0 + j];
+            if (ob.ipp && pi.prior.ipp)
+                o << ", " << (pl->pars[j].type == LG_POSITION_X ? "x.x" : (pl->pars[j].type == LG_POSITION_Y ? "x.y" : "0"));
+            else
+                o << ", p[" << ob.par0 + j << "]";
+        }
+        o << ");\n        break;\n    }\n";
+    }
+    o << "    default: break;\n    }\n}\n\n";
 }
 
 }  // namespace
@@ -158,8 +206,10 @@ std::string compose_source(const Model& m, const Shape& s, bool strict, Part par
     o << "\n// image " << m.width << "x" << m.height << ", rule " << m.rule->name << " (" << m.rule->size
       << " points), PSF " << m.psfw << "x" << m.psfh << (strict ? ", strict FP" : "") << "\n\n";
     o << "#define LG_RT " << s.rt << "\n#define LG_RPPT " << s.rppt << "\n#define LG_QS " << s.qs << "\n";
-    o << "#define LG_CTX " << s.ctx << "\n#define LG_CTY " << s.cty << "\n#define LG_CR " << s.cr << "\n\n";
-    o << prelude_source() << "\n";
+    o << "#define LG_CTX " << s.ctx << "\n#define LG_CTY " << s.cty << "\n#define LG_CR " << s.cr << "\n";
+    // fast mode with a PSF up to 49 wide pairs rows unless the shape says not
+    if (!strict && !s.pair_rows && m.psfw <= 49) o << "#define LG_CONV_SINGLE 1\n";
+    o << "\n" << prelude_source() << "\n";
     if (set || strict) o << crmath_source() << "\n";
     std::set<std::string> done;
     for (const auto& ob : m.objs) emit_plugin(o, ob.plugin, done);

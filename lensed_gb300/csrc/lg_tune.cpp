@@ -87,6 +87,19 @@ std::vector<Shape> conv_candidates(const Shape& base, bool multi)
         s.cr = c[2];
         out.push_back(s);
     }
+    if (!multi && base.pair_rows) {
+        // single-row tiles of four outputs per thread: the most threads for a
+        // batch of one or a few candidates (same per-pixel arithmetic)
+        static const int small[][3] = {{32, 16, 4}, {16, 16, 4}};
+        for (const auto& c : small) {
+            Shape s = base;
+            s.ctx = c[0];
+            s.cty = c[1];
+            s.cr = c[2];
+            s.pair_rows = false;
+            out.push_back(s);
+        }
+    }
     return out;
 }
 

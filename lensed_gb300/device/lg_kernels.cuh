@@ -12,12 +12,14 @@
 //   models   lg_model[B]              object data of each candidate
 //   raw      float[B][N]              unconvolved model (PSF path only)
 //   partials double[B][ntiles]        per-tile chi^2 partial sums
+//   counters unsigned[B]              tiles done per candidate (zero between launches)
 //   logL     double[B]
 //   image, weight float[N]            resident for the context's lifetime
 //
 // The chi^2 of a pixel is w*(m-d)^2 in FP32 as in kernel/lensed.cl:41-55;
 // sums are FP64 (per thread, then a fixed-order block tree, then a
-// fixed-order sum over tiles), so results are deterministic run to run.
+// fixed-order sum over tiles by the block that finishes a candidate's last
+// tile), so results are deterministic run to run.
 
 #ifndef LG_RT
 #define LG_RT 128
@@ -62,6 +64,39 @@ LG_DEV double lg_block_sum(double v, double* red)
     return s;
 }
 
+// A tile's chi^2 partial sum (valid in thread 0) is written; the block that
+// completes a candidate's last tile (counted with an atomic per candidate)
+// then sums that candidate's partials in tile order -- the same order
+// whichever block comes last, so results stay deterministic -- writes
+// logL = -chi2/2 (src/nested.c:106-115) and resets the counter for the next
+// launch.
+template <int NT>
+LG_DEV void lg_tile_done(double s, double* __restrict__ partials, int ntiles, int tile, int b,
+                         unsigned* __restrict__ counters, double* __restrict__ logL, double* red)
+{
+    __shared__ int last;
+    const int tid = threadIdx.y * blockDim.x + threadIdx.x;
+    if (tid == 0) {
+        partials[(size_t)b * ntiles + tile] = s;
+        __threadfence();
+        last = atomicAdd(counters + b, 1u) == (unsigned)(ntiles - 1);
+    }
+    __syncthreads();
+    if (!last || tid >= 32) return;
+    // one warp, lane l summing tiles l, l + 32, ... in order, then a fixed
+    // shuffle tree: the grouping does not depend on the launch shape (the
+    // multi-system finish sums the same way)
+    __threadfence();
+    double acc = 0.0;
+    for (int t = tid; t < ntiles; t += 32) acc += __ldcg(partials + (size_t)b * ntiles + t);
+    acc = lg_warp_sum(acc);
+    if (tid == 0) {
+        logL[b] = -0.5 * acc;
+        counters[b] = 0u;
+    }
+    (void)red;
+}
+
 // ---------------------------------------------------------------- render --
 // kernel/lensed.cl:9-39.  Block (tile, candidate); each group of LG_QS
 // threads integrates LG_RPPT pixels over the quadrature rule: strided by the
@@ -89,7 +124,8 @@ LG_DEV float lg_qs_sum(float v)
 template <int MODE>
 LG_DEV void lg_render_tile(const lg_model* __restrict__ models, float* __restrict__ out, float* __restrict__ err,
                            const float* __restrict__ image, const float* __restrict__ weight,
-                           double* __restrict__ partials)
+                           double* __restrict__ partials, unsigned* __restrict__ counters,
+                           double* __restrict__ logL)
 {
     const int b = blockIdx.y;
     const lg_model m = models[b];
@@ -166,7 +202,7 @@ LG_DEV void lg_render_tile(const lg_model* __restrict__ models, float* __restric
             }
         }
         s = lg_block_sum<LG_RT>(s, red);
-        if (threadIdx.x == 0) partials[(size_t)b * gridDim.x + blockIdx.x] = s;
+        lg_tile_done<LG_RT>(s, partials, gridDim.x, blockIdx.x, b, counters, logL, red);
     } else {
 #if defined(LG_PAIRED) && LG_RPPT % 2 == 0 && LG_N % 2 == 0
         // adjacent pixel pairs: one 8-byte store per pair (N even, so the
@@ -195,20 +231,21 @@ LG_DEV void lg_render_tile(const lg_model* __restrict__ models, float* __restric
 extern "C" __global__ void __launch_bounds__(LG_RT) lg_render_raw(const lg_model* __restrict__ models,
                                                                   float* __restrict__ raw)
 {
-    lg_render_tile<0>(models, raw, nullptr, nullptr, nullptr, nullptr);
+    lg_render_tile<0>(models, raw, nullptr, nullptr, nullptr, nullptr, nullptr, nullptr);
 }
 
 extern "C" __global__ void __launch_bounds__(LG_RT)
     lg_render_chi2(const lg_model* __restrict__ models, const float* __restrict__ image,
-                   const float* __restrict__ weight, double* __restrict__ partials)
+                   const float* __restrict__ weight, double* __restrict__ partials, unsigned* __restrict__ counters,
+                   double* __restrict__ logL)
 {
-    lg_render_tile<1>(models, nullptr, nullptr, image, weight, partials);
+    lg_render_tile<1>(models, nullptr, nullptr, image, weight, partials, counters, logL);
 }
 
 extern "C" __global__ void __launch_bounds__(LG_RT)
     lg_render_dump(const lg_model* __restrict__ models, float* __restrict__ value, float* __restrict__ error)
 {
-    lg_render_tile<2>(models, value, error, nullptr, nullptr, nullptr);
+    lg_render_tile<2>(models, value, error, nullptr, nullptr, nullptr, nullptr, nullptr);
 }
 
 // -------------------------------------------------------------- convolve --
@@ -258,8 +295,9 @@ LG_DEV double lg_conv_out(int b, int gy, int gx0, const float* acc, float* __res
     return s;
 }
 
-#if defined(LG_PAIRED) && LG_PSF_W <= 49
-// Paired rows (fast mode, PSFs up to 49 pixels wide): a thread computes LG_CR columns of two output
+#if defined(LG_PAIRED) && LG_PSF_W <= 49 && !defined(LG_CONV_SINGLE)
+// Paired rows (fast mode, PSFs up to 49 pixels wide, unless the launch shape
+// asks for single rows -- small tiles for small batches): a thread computes LG_CR columns of two output
 // rows, y and y + LG_CTY/2, with f32x2 fmas, every lane in the scalar
 // kernel's order.  The halo tile holds each input row together with the row
 // LG_CTY/2 below it as float2 pairs; pair column c of a row sits at float
@@ -279,7 +317,8 @@ static_assert(LG_CR % 8 == 0 && LG_CTY % 2 == 0, "paired convolution layout");
 
 template <int MODE>
 LG_DEV void lg_conv_tile(const float* __restrict__ raw, float* __restrict__ out, const float* __restrict__ image,
-                         const float* __restrict__ weight, double* __restrict__ partials)
+                         const float* __restrict__ weight, double* __restrict__ partials,
+                         unsigned* __restrict__ counters, double* __restrict__ logL)
 {
     extern __shared__ float4 lg_smem4[];
     float* tile = reinterpret_cast<float*>(lg_smem4);
@@ -330,7 +369,8 @@ LG_DEV void lg_conv_tile(const float* __restrict__ raw, float* __restrict__ out,
     if (MODE == 1) {
         __shared__ double red[LG_CTHREADS / 32];
         s = lg_block_sum<LG_CTHREADS>(s, red);
-        if (tid == 0) partials[(size_t)b * LG_CTILES + blockIdx.y * LG_CTILES_X + blockIdx.x] = s;
+        lg_tile_done<LG_CTHREADS>(s, partials, LG_CTILES, blockIdx.y * LG_CTILES_X + blockIdx.x, b, counters, logL,
+                                  red);
     }
 }
 #else
@@ -345,7 +385,8 @@ LG_DEV void lg_conv_tile(const float* __restrict__ raw, float* __restrict__ out,
 
 template <int MODE>
 LG_DEV void lg_conv_tile(const float* __restrict__ raw, float* __restrict__ out, const float* __restrict__ image,
-                         const float* __restrict__ weight, double* __restrict__ partials)
+                         const float* __restrict__ weight, double* __restrict__ partials,
+                         unsigned* __restrict__ counters, double* __restrict__ logL)
 {
     extern __shared__ float4 lg_smem4[];
     float* tile = reinterpret_cast<float*>(lg_smem4);
@@ -390,38 +431,25 @@ LG_DEV void lg_conv_tile(const float* __restrict__ raw, float* __restrict__ out,
     if (MODE == 1) {
         __shared__ double red[LG_CTHREADS / 32];
         s = lg_block_sum<LG_CTHREADS>(s, red);
-        if (tid == 0) partials[(size_t)b * LG_CTILES + blockIdx.y * LG_CTILES_X + blockIdx.x] = s;
+        lg_tile_done<LG_CTHREADS>(s, partials, LG_CTILES, blockIdx.y * LG_CTILES_X + blockIdx.x, b, counters, logL,
+                                  red);
     }
 }
 #endif
 
 extern "C" __global__ void __launch_bounds__(LG_CTHREADS)
     lg_conv_chi2(const float* __restrict__ raw, const float* __restrict__ image, const float* __restrict__ weight,
-                 double* __restrict__ partials)
+                 double* __restrict__ partials, unsigned* __restrict__ counters, double* __restrict__ logL)
 {
-    lg_conv_tile<1>(raw, nullptr, image, weight, partials);
+    lg_conv_tile<1>(raw, nullptr, image, weight, partials, counters, logL);
 }
 
 extern "C" __global__ void __launch_bounds__(LG_CTHREADS) lg_conv_dump(const float* __restrict__ raw,
                                                                        float* __restrict__ out)
 {
-    lg_conv_tile<0>(raw, out, nullptr, nullptr, nullptr);
+    lg_conv_tile<0>(raw, out, nullptr, nullptr, nullptr, nullptr, nullptr);
 }
 #endif
-
-// ---------------------------------------------------------------- finish --
-// logL[b] = -chi2/2 (src/nested.c:106-115) from the per-tile partials, in
-// a fixed order.
-extern "C" __global__ void __launch_bounds__(256)
-    lg_finish(const double* __restrict__ partials, int ntiles, double* __restrict__ logL)
-{
-    __shared__ double red[8];
-    const int b = blockIdx.x;
-    double s = 0.0;
-    for (int t = threadIdx.x; t < ntiles; t += 256) s += partials[(size_t)b * ntiles + t];
-    s = lg_block_sum<256>(s, red);
-    if (threadIdx.x == 0) logL[b] = -0.5 * s;
-}
 
 // Sizes the host reads back after loading the module.
 extern "C" __device__ const unsigned lg_model_bytes_eval = sizeof(lg_model);

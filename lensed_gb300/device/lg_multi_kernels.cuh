@@ -396,22 +396,25 @@ extern "C" __global__ void __launch_bounds__(LG_CTHREADS)
 }
 
 // ------------------------------------------------------------- finish --
-// logL of every candidate from its partials, in a fixed order.
+// logL of every candidate from its partials, one warp per candidate: lane l
+// sums tiles l, l + 32, ... in order, then a fixed shuffle tree -- the
+// grouping of the single-system kernels, so each system's logL is identical
+// to its own context's.
 extern "C" __global__ void __launch_bounds__(256)
     lg_multi_finish(const double* __restrict__ partials, const lg_sysinfo* __restrict__ info,
                     const lg_sysplan* __restrict__ plan, const long long* __restrict__ hdr, int with_psf,
                     double* __restrict__ logL)
 {
-    __shared__ double red[8];
     const int C = (int)hdr[2], nsys = (int)hdr[3];
-    for (int c = blockIdx.x; c < C; c += gridDim.x) {
+    const int warp = threadIdx.x / 32, lane = threadIdx.x % 32;
+    for (int c = blockIdx.x * 8 + warp; c < C; c += gridDim.x * 8) {
         int s = 0;
         while (s + 1 < nsys && plan[s + 1].cand0 <= c) ++s;
         const int n = with_psf ? info[s].ctiles : info[s].rtiles;
         const double* p = partials + plan[s].part0 + (long long)(c - plan[s].cand0) * n;
         double acc = 0.0;
-        for (int t = threadIdx.x; t < n; t += 256) acc += p[t];
-        acc = lg_block_sum<256>(acc, red);
-        if (threadIdx.x == 0) logL[c] = -0.5 * acc;
+        for (int t = lane; t < n; t += 32) acc += p[t];
+        acc = lg_warp_sum(acc);
+        if (lane == 0) logL[c] = -0.5 * acc;
     }
 }

@@ -26,7 +26,9 @@ def test_fast_mode_candidates_with_psf_compile(native):
     render = {(s["rt"], s["rppt"], s["qs"]) for s in shapes}
     conv = {(s["ctx"], s["cty"], s["cr"]) for s in shapes}
     assert (128, 2, 1) in render and any(q > 1 for _, _, q in render)  # quadrature split candidates
-    assert len(conv) >= 4 and all(s["pair_rows"] == 1 for s in shapes)
+    assert len(conv) >= 4 and sum(s["pair_rows"] == 1 for s in shapes) >= 7
+    # single-row tiles of four outputs per thread for small batches
+    assert any(s["pair_rows"] == 0 and s["cr"] == 4 for s in shapes)
     _compile_all(shapes, psf=psf, rule="sub5")
 
 
