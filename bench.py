@@ -90,7 +90,10 @@ def run_sampler(args):
     ctx = lg.Context(s.image, s.weight, s.objects, rule=s.rule, max_batch=1024, flags=args.flags)
     out = {}
     flow = {"layers": args.flow_layers, "width": args.flow_width, "epochs": args.flow_epochs}
-    for name, kw in (("plain", {}), ("flow", {"proposal": lg.PROPOSAL_FLOW, "flow_every": 1000})):
+    arms = [("plain", {}), ("flow", {"proposal": lg.PROPOSAL_FLOW, "flow_every": 1000})]
+    if args.max_ellipsoids > 1:
+        arms.append(("plain_multi", {"max_ellipsoids": args.max_ellipsoids}))
+    for name, kw in arms:
         if name == "plain" and args.skip_plain:
             continue
         r = ctx.nested(nlive=1000, batch=1024, tol=0.1, seed=11, flow=flow, **kw)
@@ -106,7 +109,7 @@ def run_sampler(args):
             "value": out["flow"]["ncall"], "higher_is_better": False, "n_gpus": 1, "dtype": "f32 (f64 evidence)",
             "data": "synthetic", "config": {"workload": s.name, "nlive": 1000, "batch": 1024, "tol": 0.1,
                                             "flow": flow},
-            "plain": out.get("plain"), "flow": out["flow"],
+            "plain": out.get("plain"), "flow": out["flow"], "plain_multi_ellipsoid": out.get("plain_multi"),
             "dlogz": out["flow"]["logz"] - out["plain"]["logz"] if "plain" in out else None,
             "truth": dict(zip(ctx.ids, [float(v) for v in ctx.to_map_order(s.truth)]))}
     print(json.dumps(line), flush=True)
@@ -328,6 +331,8 @@ def main():
     ap.add_argument("--flow-width", type=int, default=128)
     ap.add_argument("--flow-epochs", type=int, default=200)
     ap.add_argument("--skip-plain", action="store_true")
+    ap.add_argument("--max-ellipsoids", type=int, default=8,
+                    help="sampler workload: also run the plain sampler with this many bounding ellipsoids (1: skip)")
     ap.add_argument("--no-autotune", action="store_true",
                     help="keep the default launch shape instead of timing the tuner's candidates at creation")
     args = ap.parse_args()

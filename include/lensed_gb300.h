@@ -347,6 +347,9 @@ typedef struct {
                                (option resume, src/input/options.c:217-221) */
     int checkpoint_every;   /* write the state every this many iterations (0: only when stopping) */
     int resume;             /* continue from the state file when it exists and matches */
+    int max_ellipsoids;     /* 1: one bounding ellipsoid (default); more: the multi-ellipsoidal
+                               decomposition of MultiNest's multi-modal mode (option mmodal,
+                               src/input/options.c), up to this many ellipsoids */
 } lg_nested_options;
 
 typedef struct {

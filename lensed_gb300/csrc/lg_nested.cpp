@@ -103,12 +103,174 @@ struct Ellipsoid {
             x[a] = mu[a] + rad * s;
         }
     }
-    // log volume of the ellipsoid (for diagnostics)
+    // log volume of the ellipsoid
     double log_volume() const
     {
         double lv = 0.5 * d * std::log(M_PI) - std::lgamma(0.5 * d + 1) + 0.5 * d * std::log(scale);
         for (int a = 0; a < d; ++a) lv += std::log(L[(size_t)a * d + a]);
         return lv;
+    }
+    bool contains(const double* x, std::vector<double>& y) const { return mahalanobis(x, y) <= scale; }
+    // grow (never shrink) to a log volume of at least lv_min
+    void enlarge_to(double lv_min)
+    {
+        const double lv = log_volume();
+        if (lv < lv_min) scale *= std::exp(2.0 * (lv_min - lv) / d);
+    }
+};
+
+// Several ellipsoids bounding the live points (the multi-ellipsoidal
+// decomposition of Feroz & Hobson 2008, MultiNest's multi-modal mode): a set
+// of points is split in two by 2-means (started from the extreme points
+// along its principal axis) while the two enlarged ellipsoids of the halves
+// have less than half the volume of the set's; each ellipsoid's volume is
+// then at least its share of the live points times the expected prior
+// volume X of the constrained region.  Draws are uniform in the union: an
+// ellipsoid picked with probability proportional to its volume, a uniform
+// point in it, kept with probability 1 / (number of ellipsoids holding it).
+struct Bound {
+    int d = 0;
+    std::vector<Ellipsoid> ell;
+    std::vector<double> logv;
+    std::vector<double> cum;  // cumulative volume fractions
+    double logv_sum = -HUGE_VAL;
+
+    static double lae(double a, double b)
+    {
+        if (a == -HUGE_VAL) return b;
+        if (b == -HUGE_VAL) return a;
+        const double m = std::max(a, b);
+        return m + std::log(std::exp(a - m) + std::exp(b - m));
+    }
+
+    // 2-means split of the points idx; false if a half is too small
+    static bool two_means(const std::vector<double>& pts, const std::vector<int>& idx, int d, std::vector<int>& a,
+                          std::vector<int>& b)
+    {
+        const size_t n = idx.size();
+        std::vector<double> m(d, 0.0), C((size_t)d * d, 0.0), v(d, 1.0 / std::sqrt((double)d)), w(d);
+        for (int i : idx)
+            for (int k = 0; k < d; ++k) m[k] += pts[(size_t)i * d + k];
+        for (auto& x : m) x /= (double)n;
+        for (int i : idx)
+            for (int k = 0; k < d; ++k)
+                for (int l = 0; l < d; ++l)
+                    C[(size_t)k * d + l] += (pts[(size_t)i * d + k] - m[k]) * (pts[(size_t)i * d + l] - m[l]);
+        for (int it = 0; it < 30; ++it) {  // principal axis by power iteration
+            double nrm = 0;
+            for (int k = 0; k < d; ++k) {
+                w[k] = 0;
+                for (int l = 0; l < d; ++l) w[k] += C[(size_t)k * d + l] * v[l];
+                nrm += w[k] * w[k];
+            }
+            nrm = std::sqrt(nrm);
+            if (!(nrm > 0)) break;
+            for (int k = 0; k < d; ++k) v[k] = w[k] / nrm;
+        }
+        int lo = idx[0], hi = idx[0];
+        double plo = HUGE_VAL, phi = -HUGE_VAL;
+        for (int i : idx) {
+            double p = 0;
+            for (int k = 0; k < d; ++k) p += (pts[(size_t)i * d + k] - m[k]) * v[k];
+            if (p < plo) plo = p, lo = i;
+            if (p > phi) phi = p, hi = i;
+        }
+        std::vector<double> c0(pts.begin() + (size_t)lo * d, pts.begin() + (size_t)lo * d + d);
+        std::vector<double> c1(pts.begin() + (size_t)hi * d, pts.begin() + (size_t)hi * d + d);
+        std::vector<char> side(n, 0);
+        for (int it = 0; it < 50; ++it) {
+            bool changed = false;
+            std::vector<double> s0(d, 0.0), s1(d, 0.0);
+            size_t n0 = 0, n1 = 0;
+            for (size_t j = 0; j < n; ++j) {
+                const double* x = &pts[(size_t)idx[j] * d];
+                double d0 = 0, d1 = 0;
+                for (int k = 0; k < d; ++k) {
+                    d0 += (x[k] - c0[k]) * (x[k] - c0[k]);
+                    d1 += (x[k] - c1[k]) * (x[k] - c1[k]);
+                }
+                const char sd = d1 < d0;
+                changed = changed || sd != side[j];
+                side[j] = sd;
+                for (int k = 0; k < d; ++k) (sd ? s1 : s0)[k] += x[k];
+                (sd ? n1 : n0)++;
+            }
+            if (n0 == 0 || n1 == 0) return false;
+            for (int k = 0; k < d; ++k) c0[k] = s0[k] / (double)n0, c1[k] = s1[k] / (double)n1;
+            if (!changed && it > 0) break;
+        }
+        a.clear();
+        b.clear();
+        for (size_t j = 0; j < n; ++j) (side[j] ? b : a).push_back(idx[j]);
+        return a.size() > (size_t)d + 1 && b.size() > (size_t)d + 1;
+    }
+
+    static bool fit_subset(const std::vector<double>& pts, const std::vector<int>& idx, int d, double enlarge,
+                           Ellipsoid& e)
+    {
+        std::vector<double> sub(idx.size() * (size_t)d);
+        for (size_t j = 0; j < idx.size(); ++j)
+            std::memcpy(&sub[j * d], &pts[(size_t)idx[j] * d], d * sizeof(double));
+        return e.fit(sub, (int)idx.size(), d, enlarge);
+    }
+
+    void decompose(const std::vector<double>& pts, const std::vector<int>& idx, int dim, double enlarge,
+                   int depth, std::vector<std::vector<int>>& members, Ellipsoid e)
+    {
+        std::vector<int> a, b;
+        Ellipsoid ea, eb;
+        if (depth > 0 && idx.size() >= 2 * ((size_t)dim + 2) && two_means(pts, idx, dim, a, b) &&
+            fit_subset(pts, a, dim, enlarge, ea) && fit_subset(pts, b, dim, enlarge, eb) &&
+            lae(ea.log_volume(), eb.log_volume()) < std::log(0.5) + e.log_volume()) {
+            decompose(pts, a, dim, enlarge, depth - 1, members, ea);
+            decompose(pts, b, dim, enlarge, depth - 1, members, eb);
+            return;
+        }
+        ell.push_back(e);
+        members.push_back(idx);
+    }
+
+    // Fit to n points; logx = ln of the expected prior volume of the
+    // constrained region; at most 2^depth ellipsoids.
+    bool fit(const std::vector<double>& pts, int n, int dim, double enlarge, double logx, int depth)
+    {
+        d = dim;
+        ell.clear();
+        std::vector<int> idx(n);
+        for (int i = 0; i < n; ++i) idx[i] = i;
+        Ellipsoid e;
+        if (!fit_subset(pts, idx, dim, enlarge, e)) return false;
+        std::vector<std::vector<int>> members;
+        decompose(pts, idx, dim, enlarge, depth, members, e);
+        return finish(logx, members, n);
+    }
+
+    bool finish(double logx, const std::vector<std::vector<int>>& members, int n)
+    {
+        logv.clear();
+        cum.clear();
+        logv_sum = -HUGE_VAL;
+        for (size_t k = 0; k < ell.size(); ++k) {
+            if (!members.empty()) ell[k].enlarge_to(logx + std::log((double)members[k].size() / n));
+            logv.push_back(ell[k].log_volume());
+            logv_sum = lae(logv_sum, logv.back());
+        }
+        double c = 0;
+        for (double lv : logv) cum.push_back(c += std::exp(lv - logv_sum));
+        return std::isfinite(logv_sum);
+    }
+
+    // one uniform draw in the union; false if the draw was rejected for
+    // lying in several ellipsoids
+    bool sample(Rng& r, double* x, std::vector<double>& u, std::vector<double>& y) const
+    {
+        const double t = r.uniform() * cum.back();
+        size_t k = 0;
+        while (k + 1 < cum.size() && cum[k] < t) ++k;
+        ell[k].sample(r, x, u);
+        int inside = 0;
+        for (const Ellipsoid& e : ell) inside += e.contains(x, y);
+        return inside <= 1 || r.uniform() * inside < 1.0;
     }
 };
 
@@ -136,11 +298,14 @@ struct SamplerState {
     uint64_t rng[4] = {0, 0, 0, 0};
     std::vector<double> live, llive, dead_x, dead_l, dead_lw, pool_x, pool_l;
     uint64_t pool_pos = 0;
+    // multi-ellipsoid bound: [count, iteration of the fit, then per
+    // ellipsoid scale, centre (d), Cholesky factor (d x d)]
+    std::vector<double> bound;
 };
 
 namespace {
 
-const char kStateMagic[8] = {'L', 'G', 'N', 'S', 'T', 'A', 'T', '1'};
+const char kStateMagic[8] = {'L', 'G', 'N', 'S', 'T', 'A', 'T', '2'};
 
 template <class T>
 bool put(FILE* f, const T& v)
@@ -177,7 +342,8 @@ bool save_state(const char* path, const SamplerState& s)
               put(f, s.n_flow_fail) && put(f, s.logz) && put(f, s.H) && put(f, s.logx);
     for (int i = 0; i < 4 && ok; ++i) ok = put(f, s.rng[i]);
     ok = ok && put_vec(f, s.live) && put_vec(f, s.llive) && put_vec(f, s.dead_x) && put_vec(f, s.dead_l) &&
-         put_vec(f, s.dead_lw) && put_vec(f, s.pool_x) && put_vec(f, s.pool_l) && put(f, s.pool_pos);
+         put_vec(f, s.dead_lw) && put_vec(f, s.pool_x) && put_vec(f, s.pool_l) && put(f, s.pool_pos) &&
+         put_vec(f, s.bound);
     ok = (std::fclose(f) == 0) && ok;
     return ok && std::rename(tmp.c_str(), path) == 0;
 }
@@ -195,7 +361,8 @@ bool load_state(const char* path, int nd, int nl, int batch, SamplerState& s)
               get(f, s.n_flow_fail) && get(f, s.logz) && get(f, s.H) && get(f, s.logx);
     for (int i = 0; i < 4 && ok; ++i) ok = get(f, s.rng[i]);
     ok = ok && get_vec(f, s.live) && get_vec(f, s.llive) && get_vec(f, s.dead_x) && get_vec(f, s.dead_l) &&
-         get_vec(f, s.dead_lw) && get_vec(f, s.pool_x) && get_vec(f, s.pool_l) && get(f, s.pool_pos);
+         get_vec(f, s.dead_lw) && get_vec(f, s.pool_x) && get_vec(f, s.pool_l) && get(f, s.pool_pos) &&
+         get_vec(f, s.bound);
     std::fclose(f);
     ok = ok && s.live.size() == (size_t)nl * nd && s.llive.size() == (size_t)nl &&
          s.dead_x.size() == s.dead_l.size() * nd && s.dead_lw.size() == s.dead_l.size() &&
@@ -257,6 +424,14 @@ int nested_sample(int nd, lg_batch_loglike fn, void* user, const lg_nested_optio
     std::vector<double> pool_l;
     size_t pool_pos = 0;
     Ellipsoid ell;
+    // multi-ellipsoid mode: the decomposition is refitted every nlive / 10
+    // iterations (and kept in the checkpoint, so that resumed runs repeat it)
+    const bool multi = opt.max_ellipsoids > 1;
+    int depth = 0;
+    while ((2 << depth) <= opt.max_ellipsoids && depth < 10) ++depth;
+    Bound bound;
+    long bound_iter = -1;
+    const long refit_every = std::max(1, nl / 10);
     std::vector<double> u(nd), y(nd);
     long iter = 0, since_train = 0, n_flow = 0, n_ell = 0, n_flow_fail = 0;
     bool use_flow = false;
@@ -280,6 +455,23 @@ int nested_sample(int nd, lg_batch_loglike fn, void* user, const lg_nested_optio
         n_ell = st.n_ell;
         n_flow_fail = st.n_flow_fail;
         for (int i = 0; i < 4; ++i) rng.s[i] = st.rng[i];
+        if (multi && st.bound.size() >= 2) {
+            const int ne = (int)st.bound[0];
+            bound_iter = (long)st.bound[1];
+            size_t o = 2;
+            bound.d = nd;
+            for (int k = 0; k < ne && o + 1 + nd + (size_t)nd * nd <= st.bound.size(); ++k) {
+                Ellipsoid e;
+                e.d = nd;
+                e.scale = st.bound[o++];
+                e.mu.assign(st.bound.begin() + o, st.bound.begin() + o + nd);
+                o += nd;
+                e.L.assign(st.bound.begin() + o, st.bound.begin() + o + (size_t)nd * nd);
+                o += (size_t)nd * nd;
+                bound.ell.push_back(e);
+            }
+            if (!bound.finish(0, {}, 1)) bound.ell.clear(), bound_iter = -1;
+        }
     }
     // the state between iterations, for the checkpoint file
     auto checkpoint = [&]() {
@@ -306,6 +498,14 @@ int nested_sample(int nd, lg_batch_loglike fn, void* user, const lg_nested_optio
         c.pool_x = pool_x;
         c.pool_l = pool_l;
         c.pool_pos = pool_pos;
+        if (multi && !bound.ell.empty()) {
+            c.bound = {(double)bound.ell.size(), (double)bound_iter};
+            for (const Ellipsoid& e : bound.ell) {
+                c.bound.push_back(e.scale);
+                c.bound.insert(c.bound.end(), e.mu.begin(), e.mu.end());
+                c.bound.insert(c.bound.end(), e.L.begin(), e.L.end());
+            }
+        }
         return save_state(opt.checkpoint, c);
     };
     for (;; ++iter) {
@@ -379,12 +579,25 @@ int nested_sample(int nd, lg_batch_loglike fn, void* user, const lg_nested_optio
             others.reserve((size_t)(nl - 1) * nd);
             for (int i = 0; i < nl; ++i)
                 if (i != imin) others.insert(others.end(), &live[(size_t)i * nd], &live[(size_t)i * nd] + nd);
-            if (!ell.fit(others, nl - 1, nd, 1.0 / opt.efr)) {
-                err = "nested sampling: degenerate live points";
-                return LG_ERR_INPUT;
+            double bound_logv;
+            if (multi) {
+                if (bound.ell.empty() || iter - bound_iter >= refit_every) {
+                    if (!bound.fit(others, nl - 1, nd, 1.0 / opt.efr, logx, depth)) {
+                        err = "nested sampling: degenerate live points";
+                        return LG_ERR_INPUT;
+                    }
+                    bound_iter = iter;
+                }
+                bound_logv = bound.logv_sum;
+            } else {
+                if (!ell.fit(others, nl - 1, nd, 1.0 / opt.efr)) {
+                    err = "nested sampling: degenerate live points";
+                    return LG_ERR_INPUT;
+                }
+                bound_logv = ell.log_volume();
             }
             // the learned bound is used when it is the tighter of the two
-            if (use_flow && learned->log_volume() < ell.log_volume()) {
+            if (use_flow && learned->log_volume() < bound_logv) {
                 n = learned->propose(live.data(), nl, nd, buf.data(), B, rng.next());
                 if (n > 0) n_flow += n;
                 else n = 0, ++n_flow_fail;
@@ -394,7 +607,11 @@ int nested_sample(int nd, lg_batch_loglike fn, void* user, const lg_nested_optio
                 while (n < B && tries < 1000L * B) {
                     ++tries;
                     double* x = &buf[(size_t)n * nd];
-                    ell.sample(rng, x, u);
+                    if (multi) {
+                        if (!bound.sample(rng, x, u, y)) continue;
+                    } else {
+                        ell.sample(rng, x, u);
+                    }
                     bool in = true;
                     for (int a = 0; a < nd && in; ++a) {
                         if (opt.wrap && opt.wrap[a]) x[a] -= std::floor(x[a]);
@@ -497,6 +714,7 @@ lg_nested_options lg_nested_defaults(void)
     o.checkpoint = nullptr;
     o.checkpoint_every = 0;
     o.resume = 0;
+    o.max_ellipsoids = 1;
     return o;
 }
 

@@ -90,3 +90,38 @@ def test_checkpoint_and_resume_continue_exactly(native, tmp_path):
     other = lg.nested_sample(gaussian(np.full(2, 0.5), 0.1), 2, checkpoint=path, resume=1, nlive=100, batch=64,
                              seed=5)
     assert other["niter"] > 0
+
+
+def test_multi_ellipsoid_bound_on_two_modes(native):
+    """Two well separated modes (d = 4): the multi-ellipsoidal bound (MultiNest's
+    multi-modal mode) finds the evidence with far fewer likelihood calls than
+    one ellipsoid spanning both modes and the empty space between them."""
+    d, sigma = 4, 0.03
+
+    def f(x):
+        a = -0.5 * np.sum(((x - 0.3) / sigma) ** 2, axis=1)
+        b = -0.5 * np.sum(((x - 0.7) / sigma) ** 2, axis=1)
+        return np.logaddexp(a, b) + math.log(0.5)
+
+    exact = 0.5 * d * math.log(2 * math.pi * sigma ** 2)
+    common = dict(nlive=400, batch=256, seed=2, tol=0.1)
+    one = lg.nested_sample(f, d, **common)
+    many = lg.nested_sample(f, d, max_ellipsoids=8, **common)
+    print(f"two modes d={d}: exact {exact:.3f}; one ellipsoid {one['logz']:.3f}+-{one['logz_err']:.3f} "
+          f"({one['ncall']} calls); up to 8 {many['logz']:.3f}+-{many['logz_err']:.3f} ({many['ncall']} calls)")
+    for r in (one, many):
+        assert abs(r["logz"] - exact) < 4 * r["logz_err"] + 0.1
+    assert many["ncall"] < 0.5 * one["ncall"]
+    # both modes carry about half of the posterior
+    w = np.exp(many["logwt"])
+    assert 0.35 < w[many["samples"][:, 0] < 0.5].sum() < 0.65
+
+
+def test_multi_ellipsoid_resume_is_exact(native, tmp_path):
+    f = gaussian(np.array([0.3, 0.6, 0.45]), 0.07)
+    common = dict(nlive=200, batch=64, seed=5, tol=0.05, max_ellipsoids=4)
+    full = lg.nested_sample(f, 3, **common)
+    path = str(tmp_path / "state.bin")
+    lg.nested_sample(f, 3, maxiter=333, checkpoint=path, **common)
+    rest = lg.nested_sample(f, 3, checkpoint=path, resume=1, **common)
+    assert rest["logz"] == full["logz"] and rest["ncall"] == full["ncall"]
