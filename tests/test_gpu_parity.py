@@ -150,6 +150,45 @@ def test_psf_convolution_matches_oracle(native, psf_size, flags):
     assert_image_close(model, c, "convolved")
 
 
+@pytest.mark.parametrize("W,H,psf_size", [(5, 3, 7), (45, 52, 101), (20, 17, 1), (24, 30, 71), (33, 1, 9)])
+@pytest.mark.parametrize("flags", [0, lg.LG_FLAG_STRICT_FP])
+def test_convolution_edge_sizes(native, W, H, psf_size, flags):
+    """Images smaller than one tile, the largest PSF (101 x 101), a 1 x 1
+    PSF, PSFs larger than the image in both directions and a one-row image:
+    the clamp-to-edge convolution equals the oracle's, and the logL too."""
+    plugins, params = PLUGIN_CASES[4]
+    params = list(params)
+    params[0], params[1] = (W + 1) / 2, (H + 1) / 2
+    psf = workloads.psf_gauss_wings(psf_size, 2.0) if psf_size > 1 else np.ones((1, 1), np.float32)
+    rng = np.random.Generator(np.random.PCG64(psf_size))
+    image = rng.normal(10.0, 1.0, (H, W)).astype(np.float32)
+    weight = rng.uniform(0.5, 1.5, (H, W)).astype(np.float32)
+    ctx = make_ctx(plugins, W, H, psf=psf, rule="sub2", flags=flags, image=image, weight=weight)
+    p = ctx.to_map_order(params)
+    model, raw, _ = ctx.render(p)
+    o = Oracle(plugins, W, H, quadrature.rule("sub2"), psf=psf, image=image, weight=weight, precision=32)
+    v, _, c = o.render(params)
+    assert_image_close(raw, v, "raw")
+    assert_image_close(model, c, "convolved")
+    got = ctx.eval_batch(p[None, :])
+    want = o.loglike(np.asarray(params)[None, :])
+    assert np.all(np.abs(got - want) <= logl_tol(want)), (got, want)
+
+
+def test_fully_masked_image_and_oversized_psf(native):
+    """All weights zero: chi^2 = 0, logL = 0 for every candidate; a PSF above
+    the 101 x 101 limit is refused with a status, not a crash."""
+    plugins, params = PLUGIN_CASES[4]
+    W, H = 40, 30
+    ctx = make_ctx(plugins, W, H, psf=workloads.psf_gauss_wings(9, 2.0), rule="sub2",
+                   weight=np.zeros((H, W), np.float32))
+    assert ctx.masked == W * H
+    got = ctx.eval_batch(np.tile(ctx.to_map_order(params), (5, 1)))
+    assert np.all(got == 0.0)
+    with pytest.raises(lg.LensedError):
+        make_ctx(plugins, W, H, psf=workloads.psf_gauss_wings(103, 2.0), rule="sub2")
+
+
 def _loglike_case(system, B, seed=0):
     ctx = lg.Context(system.image, system.weight, system.objects, psf=system.psf, rule=system.rule,
                      max_batch=max(B, 8))
