@@ -100,17 +100,26 @@ def run_sampler(args):
         w = np.exp(r["logwt"])
         _, phys = ctx.eval_cube(r["samples"])
         mean_phys = (w[:, None] * phys).sum(0) / w.sum()
+        std_phys = np.sqrt(np.maximum((w[:, None] * (phys - mean_phys) ** 2).sum(0) / w.sum(), 0.0))
         out[name] = {"logz": r["logz"], "logz_err": r["logz_err"], "ncall": r["ncall"], "wall_s": r["wall_s"],
                      "eval_s": r["eval_s"], "train_s": r["train_s"], "propose_s": r["propose_s"],
                      "niter": r["niter"], "flow_proposals": r["n_flow_proposals"],
                      "ellipsoid_proposals": r["n_ellipsoid_proposals"],
-                     "posterior_mean": dict(zip(ctx.ids, [float(v) for v in mean_phys]))}
+                     "posterior_mean": dict(zip(ctx.ids, [float(v) for v in mean_phys])),
+                     "posterior_std": dict(zip(ctx.ids, [float(v) for v in std_phys]))}
     line = {"metric": "calls & wall-time to lnZ (learned vs plain sampler)", "unit": "calls, s",
             "value": out["flow"]["ncall"], "higher_is_better": False, "n_gpus": 1, "dtype": "f32 (f64 evidence)",
             "data": "synthetic", "config": {"workload": s.name, "nlive": 1000, "batch": 1024, "tol": 0.1,
                                             "flow": flow},
             "plain": out.get("plain"), "flow": out["flow"], "plain_multi_ellipsoid": out.get("plain_multi"),
             "dlogz": out["flow"]["logz"] - out["plain"]["logz"] if "plain" in out else None,
+            # largest difference of the learned and plain posterior means, in
+            # posterior standard deviations (free parameters)
+            "max_mean_shift_in_std": max(
+                abs(out["flow"]["posterior_mean"][k] - out["plain"]["posterior_mean"][k])
+                / out["plain"]["posterior_std"][k]
+                for k in out["plain"]["posterior_std"] if out["plain"]["posterior_std"][k] > 0) if "plain" in out
+            else None,
             "truth": dict(zip(ctx.ids, [float(v) for v in ctx.to_map_order(s.truth)]))}
     print(json.dumps(line), flush=True)
 

@@ -29,6 +29,9 @@
 
 namespace lg {
 
+// batches up to this size go through mapped host memory in the host API
+constexpr int kZeroCopyBatch = 64;
+
 namespace {
 std::mutex g_drv_mu;
 Driver g_drv;
@@ -122,6 +125,15 @@ struct lg_ctx {
     std::map<int, cudaGraphExec_t> cube_graphs;
     double* h_params = nullptr;  // pinned staging
     double* h_logL = nullptr;
+    // host API, small batches: parameters and logL in mapped pinned memory
+    // that the kernels read and write directly (no copy nodes in the graph)
+    double* z_params = nullptr;  // host address
+    double* z_logL = nullptr;
+    double* zd_params = nullptr;  // device addresses of the same memory
+    double* zd_logL = nullptr;
+    double *z_cube = nullptr, *z_phys = nullptr, *zd_cube = nullptr, *zd_phys = nullptr;  // unit-cube path
+    int *z_bad = nullptr, *zd_bad = nullptr;
+    int last_bad = 0;  // rejection flag of the first point of the last unit-cube call
     std::map<int, cudaGraphExec_t> graphs;
 
     int fail(int code, const std::string& msg)
@@ -206,6 +218,11 @@ struct lg_ctx {
         cudaFree(d_layers);
         cudaFreeHost(h_params);
         cudaFreeHost(h_logL);
+        cudaFreeHost(z_params);
+        cudaFreeHost(z_logL);
+        cudaFreeHost(z_cube);
+        cudaFreeHost(z_phys);
+        cudaFreeHost(z_bad);
         if (mod && drv) drv->moduleUnload(mod);
         if (mod_set && drv) drv->moduleUnload(mod_set);
         mod_set = nullptr;
@@ -607,6 +624,24 @@ int create_impl(lg_ctx* c, const lg_image_desc* img, const lg_object_desc* objs,
     if ((rc = c->cuda(cudaMallocHost((void**)&c->h_params, B * np * 8), "pinned params")) ||
         (rc = c->cuda(cudaMallocHost((void**)&c->h_logL, B * 8), "pinned logL")))
         return rc;
+    {
+        const size_t zb = std::min<size_t>(B, lg::kZeroCopyBatch);
+        if ((rc = c->cuda(cudaHostAlloc((void**)&c->z_params, std::max<size_t>(zb * np, 1) * 8, cudaHostAllocMapped),
+                          "mapped params")) ||
+            (rc = c->cuda(cudaHostAlloc((void**)&c->z_logL, zb * 8, cudaHostAllocMapped), "mapped logL")) ||
+            (rc = c->cuda(cudaHostGetDevicePointer((void**)&c->zd_params, c->z_params, 0), "mapped params")) ||
+            (rc = c->cuda(cudaHostGetDevicePointer((void**)&c->zd_logL, c->z_logL, 0), "mapped logL")))
+            return rc;
+        const size_t nd = std::max<size_t>((size_t)m.ndims, 1);
+        if ((rc = c->cuda(cudaHostAlloc((void**)&c->z_cube, zb * nd * 8, cudaHostAllocMapped), "mapped cube")) ||
+            (rc = c->cuda(cudaHostAlloc((void**)&c->z_phys, std::max<size_t>(zb * np, 1) * 8, cudaHostAllocMapped),
+                          "mapped phys")) ||
+            (rc = c->cuda(cudaHostAlloc((void**)&c->z_bad, zb * 4, cudaHostAllocMapped), "mapped flags")) ||
+            (rc = c->cuda(cudaHostGetDevicePointer((void**)&c->zd_cube, c->z_cube, 0), "mapped cube")) ||
+            (rc = c->cuda(cudaHostGetDevicePointer((void**)&c->zd_phys, c->z_phys, 0), "mapped phys")) ||
+            (rc = c->cuda(cudaHostGetDevicePointer((void**)&c->zd_bad, c->z_bad, 0), "mapped flags")))
+            return rc;
+    }
     // unit-cube path (priors are checked when it is called)
     const size_t nd = (size_t)m.ndims;
     std::vector<DevPrior> pri(np);
@@ -648,11 +683,19 @@ int graph_for(lg_ctx* c, int B, cudaGraphExec_t* out)
     cudaGraph_t g;
     if ((rc = c->cuda(cudaStreamBeginCapture(c->stream, cudaStreamCaptureModeThreadLocal), "begin capture")))
         return rc;
-    int erc = c->cuda(cudaMemcpyAsync(c->d_params, c->h_params, B * np * 8, cudaMemcpyHostToDevice, c->stream),
+    int erc = LG_OK;
+    if (B <= lg::kZeroCopyBatch) {
+        // small batches: the kernels read the parameters from and write logL
+        // to mapped host memory directly
+        erc = c->enqueue(B, c->zd_params, c->zd_logL, c->stream);
+    } else {
+        erc = c->cuda(cudaMemcpyAsync(c->d_params, c->h_params, B * np * 8, cudaMemcpyHostToDevice, c->stream),
                       "params upload");
-    if (!erc) erc = c->enqueue(B, c->d_params, c->d_logL, c->stream);
-    if (!erc)
-        erc = c->cuda(cudaMemcpyAsync(c->h_logL, c->d_logL, B * 8, cudaMemcpyDeviceToHost, c->stream), "logL read");
+        if (!erc) erc = c->enqueue(B, c->d_params, c->d_logL, c->stream);
+        if (!erc)
+            erc = c->cuda(cudaMemcpyAsync(c->h_logL, c->d_logL, B * 8, cudaMemcpyDeviceToHost, c->stream),
+                          "logL read");
+    }
     cudaError_t e = cudaStreamEndCapture(c->stream, &g);
     if (erc) return erc;
     if ((rc = c->cuda(e, "end capture"))) return rc;
@@ -691,17 +734,20 @@ int check_priors(lg_ctx* c)
 
 // Enqueue prior transform .. logL for B unit-cube points (device pointers):
 // the physical parameters land in the context's params buffer (and in
-// d_phys when not NULL), the rejection flags in d_bad.
-int enqueue_cube(lg_ctx* c, int B, const double* d_cube, double* d_phys, double* d_logL, cudaStream_t s)
+// d_phys when not NULL), the rejection flags in bad (the context's d_bad
+// when NULL).
+int enqueue_cube(lg_ctx* c, int B, const double* d_cube, double* d_phys, double* d_logL, cudaStream_t s,
+                 int* bad = nullptr)
 {
     const int np = (int)c->model.pars.size(), nd = c->model.ndims;
     const int blocks = (B + 127) / 128;
+    if (!bad) bad = c->d_bad;
     int rc;
     lg_prior_transform<<<blocks, 128, 0, s>>>(d_cube, B, nd, np, static_cast<const DevPrior*>(c->d_priors),
-                                              c->d_params, c->d_bad);
+                                              c->d_params, bad);
     if ((rc = c->cuda(cudaGetLastError(), "prior transform"))) return rc;
     if ((rc = c->enqueue(B, c->d_params, d_logL, s))) return rc;
-    lg_prior_finish<<<blocks, 128, 0, s>>>(B, np, c->d_bad, c->d_params, d_logL, d_phys);
+    lg_prior_finish<<<blocks, 128, 0, s>>>(B, np, bad, c->d_params, d_logL, d_phys);
     return c->cuda(cudaGetLastError(), "prior finish");
 }
 
@@ -733,7 +779,10 @@ int cube_graph_for(lg_ctx* c, int B, cudaGraphExec_t* out)
     cudaGraph_t g;
     if ((rc = c->cuda(cudaStreamBeginCapture(c->stream, cudaStreamCaptureModeThreadLocal), "begin capture")))
         return rc;
-    int erc = enqueue_cube_io(c, B, c->stream);
+    // small batches read the cube from and write logL, the physical values
+    // and the flags to mapped host memory directly
+    int erc = B <= lg::kZeroCopyBatch ? enqueue_cube(c, B, c->zd_cube, c->zd_phys, c->zd_logL, c->stream, c->zd_bad)
+                                      : enqueue_cube_io(c, B, c->stream);
     cudaError_t e = cudaStreamEndCapture(c->stream, &g);
     if (erc) return erc;
     if ((rc = c->cuda(e, "end capture"))) return rc;
@@ -752,7 +801,8 @@ int cube_eval_chunk(lg_ctx* c, const double* cube, int B, double* phys, double* 
 {
     const size_t np = c->model.pars.size(), nd = (size_t)c->model.ndims;
     int rc;
-    if (nd) std::memcpy(c->h_cube, cube, (size_t)B * nd * 8);
+    const bool zero_copy = !(c->flags & LG_FLAG_NO_GRAPH) && B <= lg::kZeroCopyBatch;
+    if (nd) std::memcpy(zero_copy ? c->z_cube : c->h_cube, cube, (size_t)B * nd * 8);
     if (c->flags & LG_FLAG_NO_GRAPH) {
         if ((rc = enqueue_cube_io(c, B, c->stream))) return rc;
     } else {
@@ -761,11 +811,15 @@ int cube_eval_chunk(lg_ctx* c, const double* cube, int B, double* phys, double* 
         if ((rc = c->cuda(cudaGraphLaunch(ge, c->stream), "graph launch"))) return rc;
     }
     if ((rc = c->cuda(cudaStreamSynchronize(c->stream), "evaluate"))) return rc;
-    std::memcpy(logL, c->h_logL, (size_t)B * 8);
+    const double* hl = zero_copy ? c->z_logL : c->h_logL;
+    const double* hp = zero_copy ? c->z_phys : c->h_params;
+    const int* hb = zero_copy ? c->z_bad : c->h_bad;
+    std::memcpy(logL, hl, (size_t)B * 8);
     if (phys)
         for (int b = 0; b < B; ++b)
             for (size_t i = 0; i < np; ++i)
-                phys[(size_t)b * np + i] = (nan_rejected && c->h_bad[b]) ? NAN : c->h_params[(size_t)b * np + i];
+                phys[(size_t)b * np + i] = (nan_rejected && hb[b]) ? NAN : hp[(size_t)b * np + i];
+    c->last_bad = hb[0];
     return LG_OK;
 }
 
@@ -993,9 +1047,14 @@ int lg_eval_batch(lg_ctx* c, const double* params, int B, double* logL)
                           "logL read")))
             return rc;
     } else {
+        const bool zero_copy = B <= lg::kZeroCopyBatch;
+        if (zero_copy) std::memcpy(c->z_params, params, (size_t)B * np * 8);
         cudaGraphExec_t ge;
         if ((rc = graph_for(c, B, &ge))) return rc;
         if ((rc = c->cuda(cudaGraphLaunch(ge, c->stream), "graph launch"))) return rc;
+        if ((rc = c->cuda(cudaStreamSynchronize(c->stream), "evaluate"))) return rc;
+        std::memcpy(logL, zero_copy ? c->z_logL : c->h_logL, (size_t)B * 8);
+        return LG_OK;
     }
     if ((rc = c->cuda(cudaStreamSynchronize(c->stream), "evaluate"))) return rc;
     std::memcpy(logL, c->h_logL, (size_t)B * 8);
@@ -1288,7 +1347,7 @@ void loglike(double cube[], int* ndim, int* npar, double* lnew, void* ctx)
     if (cube_eval_chunk(c, cube, 1, p.data(), &l, false)) return;
     // MultiNest records the physical values written back into cube
     for (int i = 0; i < *npar; ++i) cube[i] = p[i];
-    if (c->h_bad[0]) {
+    if (c->last_bad) {
         c->err = "loglike: parameter outside its bounds";
         return;
     }
