@@ -89,6 +89,7 @@ def run_sampler(args):
     s = workloads.small()
     ctx = lg.Context(s.image, s.weight, s.objects, rule=s.rule, max_batch=1024, flags=args.flags)
     out = {}
+    seeds = [11 + 7 * k for k in range(max(1, args.sampler_seeds))]
     flow = {"layers": args.flow_layers, "width": args.flow_width, "epochs": args.flow_epochs}
     arms = [("plain", {}), ("flow", {"proposal": lg.PROPOSAL_FLOW, "flow_every": 1000})]
     if args.max_ellipsoids > 1:
@@ -96,7 +97,8 @@ def run_sampler(args):
     for name, kw in arms:
         if name == "plain" and args.skip_plain:
             continue
-        r = ctx.nested(nlive=1000, batch=1024, tol=0.1, seed=11, flow=flow, **kw)
+        runs = [ctx.nested(nlive=1000, batch=1024, tol=0.1, seed=sd, flow=flow, **kw) for sd in seeds]
+        r = runs[0]
         w = np.exp(r["logwt"])
         _, phys = ctx.eval_cube(r["samples"])
         mean_phys = (w[:, None] * phys).sum(0) / w.sum()
@@ -106,9 +108,15 @@ def run_sampler(args):
                      "niter": r["niter"], "flow_proposals": r["n_flow_proposals"],
                      "ellipsoid_proposals": r["n_ellipsoid_proposals"],
                      "posterior_mean": dict(zip(ctx.ids, [float(v) for v in mean_phys])),
-                     "posterior_std": dict(zip(ctx.ids, [float(v) for v in std_phys]))}
+                     "posterior_std": dict(zip(ctx.ids, [float(v) for v in std_phys])),
+                     # every seed: ln Z, calls, wall time
+                     "seeds": {str(sd): {"logz": x["logz"], "ncall": x["ncall"], "wall_s": x["wall_s"],
+                                         "flow_proposals": x["n_flow_proposals"]} for sd, x in zip(seeds, runs)},
+                     "mean_ncall": float(np.mean([x["ncall"] for x in runs])),
+                     "mean_wall_s": float(np.mean([x["wall_s"] for x in runs])),
+                     "mean_logz": float(np.mean([x["logz"] for x in runs]))}
     line = {"metric": "calls & wall-time to lnZ (learned vs plain sampler)", "unit": "calls, s",
-            "value": out["flow"]["ncall"], "higher_is_better": False, "n_gpus": 1, "dtype": "f32 (f64 evidence)",
+            "value": out["flow"]["mean_ncall"], "higher_is_better": False, "n_gpus": 1, "dtype": "f32 (f64 evidence)",
             "data": "synthetic", "config": {"workload": s.name, "nlive": 1000, "batch": 1024, "tol": 0.1,
                                             "flow": flow},
             "plain": out.get("plain"), "flow": out["flow"], "plain_multi_ellipsoid": out.get("plain_multi"),
@@ -126,9 +134,9 @@ def run_sampler(args):
 
 def run_flow_inverse(args):
     """The learned proposal's inverse flow (d = 13, 8 coupling layers, width
-    128) on M latent points with random weights, through the tcgen05 kernel
-    and the FP32 kernel (lg_flow_inverse_check: host copies included in the
-    wall times; kernel times come from ncu)."""
+    128) on M latent points with random weights: device time per launch of
+    the tcgen05 kernel and of the FP32 kernel (CUDA events, 20 launches after
+    warm-up), and their largest differences on the same points."""
     import ctypes as C
 
     import lensed_gb300 as lg
@@ -144,11 +152,17 @@ def run_flow_inverse(args):
     for tc in (1, 0):
         u = np.zeros((M, d), np.float32)
         ld = np.zeros(M, np.float32)
-        t0 = time.perf_counter()
         rc = lg.lib().lg_flow_inverse_check(0, d, layers, width, hidden, 1, tc, P(params), P(z), M, P(u), P(ld))
-        out["tc" if tc else "fp32"] = {"rc": rc, "wall_s": time.perf_counter() - t0, "u": u, "ld": ld}
+        ms = np.zeros(1, np.float32)
+        rct = lg.lib().lg_flow_inverse_time(0, d, layers, width, hidden, tc, P(params), P(z), M, 20, P(ms))
+        out["tc" if tc else "fp32"] = {"rc": rc, "rc_time": rct, "ms": float(ms[0]), "u": u, "ld": ld}
+    # dense FLOPs per point: 8 layers x 2 x (6.5 x 128 + 128 x 128 + 128 x 13)
+    flop = 2.0 * sum(a * b for a, b in [(d // 2 + d % 2, width), (width, width), (width, 2 * (d // 2 + d % 2))]) * layers
     line = {"metric": "learned-proposal inverse flow", "M": M, "flow": [d, layers, width, hidden],
-            "wall_s": {k: v["wall_s"] for k, v in out.items()}, "rc": {k: v["rc"] for k, v in out.items()},
+            "ms_per_launch": {k: v["ms"] for k, v in out.items()},
+            "latent_points_per_s": {k: M / (v["ms"] * 1e-3) for k, v in out.items() if v["ms"] > 0},
+            "tflops": {k: M * flop / (v["ms"] * 1e-3) / 1e12 for k, v in out.items() if v["ms"] > 0},
+            "rc": {k: [v["rc"], v["rc_time"]] for k, v in out.items()},
             "max_abs_diff_u": float(np.abs(out["tc"]["u"] - out["fp32"]["u"]).max()),
             "max_abs_diff_logdet": float(np.abs(out["tc"]["ld"] - out["fp32"]["ld"]).max())}
     print(json.dumps(line), flush=True)
@@ -340,6 +354,7 @@ def main():
     ap.add_argument("--flow-width", type=int, default=128)
     ap.add_argument("--flow-epochs", type=int, default=200)
     ap.add_argument("--skip-plain", action="store_true")
+    ap.add_argument("--sampler-seeds", type=int, default=3, help="sampler workload: runs (seeds) per sampler")
     ap.add_argument("--max-ellipsoids", type=int, default=8,
                     help="sampler workload: also run the plain sampler with this many bounding ellipsoids (1: skip)")
     ap.add_argument("--no-autotune", action="store_true",

@@ -375,11 +375,16 @@ typedef struct {
     int epochs;     /* training epochs per retraining (default 200) */
     int batch;      /* training batch (default 256) */
     double lr;      /* Adam learning rate (default 1e-3) */
-    double expand;  /* latent radius enlargement over the live points (default 1.1) */
-    int patience;   /* epochs without held-out improvement before a retraining stops (default 10) */
+    double expand;  /* volume enlargement of the latent ball through the farthest live point
+                       (default 1.25, as the plain sampler's 1 / efr) */
+    int patience;   /* epochs without held-out improvement before a retraining stops (default 6) */
     int lag;        /* replacements after a retraining starts at which the new flow takes over
-                       (default 500): the retraining runs on its own stream meanwhile, and the
+                       (default 800): the retraining runs on its own stream meanwhile, and the
                        sampler waits for it there if it has not finished */
+    double draw_cost; /* cost of one latent draw of the flow in likelihood calls (default 0.005, a
+                         128^2 image with a 9-point rule): the flow is used when its volume times
+                         1 + draw_cost x latent draws per proposal is below the ellipsoids' volume;
+                         0 for expensive likelihoods.  A fixed number, so that runs repeat */
 } lg_flow_options;
 
 typedef int (*lg_batch_loglike)(void* user, const double* cube, int B, double* logL);
@@ -401,6 +406,12 @@ int lg_flow_loss_grad(int device, int d, int layers, int width, int hidden, int 
  * ldet: log |det du/dz|.  For checks against the CPU restatement. */
 int lg_flow_inverse_check(int device, int d, int layers, int width, int hidden, int bf16, int tc,
                           const float* params, const float* z, int M, float* u, float* ldet);
+
+/* Device time of the inverse flow (lg_flow_inverse_check's arguments; z
+   uploaded once): reps launches after two warm-up launches, timed with CUDA
+   events on the launching stream; *ms = milliseconds per launch. */
+int lg_flow_inverse_time(int device, int d, int layers, int width, int hidden, int tc, const float* params,
+                         const float* z, int M, int reps, float* ms);
 /* One retraining of the learned proposal on n points (n x d, row-major),
  * as the sampler does it on its live points: history receives the held-out
  * loss before training and after each epoch (NaN past the last epoch run);
@@ -408,6 +419,13 @@ int lg_flow_inverse_check(int device, int d, int layers, int width, int hidden, 
  * fraction of latent draws. */
 int lg_flow_fit(int device, int d, const lg_flow_options* opts, const double* pts, int n, float* history,
                 int max_history, double* efficiency);
+/* The sampler's GPU draws uniform in a union of nell ellipsoids (and the
+ * unit cube; periodic dimensions, wrap[a] != 0, wrapped): packed holds per
+ * ellipsoid its centre (d), lower Cholesky factor of the covariance (d x d,
+ * row-major) and scale (the ellipsoid is (x - mu)^T C^-1 (x - mu) <= scale),
+ * logv their log volumes.  Returns the number of points written (<= B). */
+int lg_ellipsoid_draw_check(int device, int d, int nell, const double* packed, const double* logv, const int* wrap,
+                            double* out, int B, unsigned long long seed);
 /* lg_nested_sample with the learned proposal on the given CUDA device. */
 int lg_nested_sample_flow(int ndims, lg_batch_loglike fn, void* user, const lg_nested_options* opts,
                           const lg_flow_options* flow, int device, lg_nested_result* result);

@@ -33,13 +33,13 @@
 //                  rejection test against the calibrated weight bound, the
 //                  unit-cube test and an order-preserving compaction.
 //
-// Proposals (as nessai, Williams et al. 2021): z uniform in a ball of radius
-// `expand` x the largest latent radius of the live points, mapped back to the
-// cube; a draw is kept with probability |det dx/dz| / W, W a bound calibrated
+// Proposals (as nessai, Williams et al. 2021): z uniform in the ball through
+// the farthest live point in latent space, its volume enlarged by `expand`
+// (as the plain sampler enlarges its ellipsoid), mapped back to the cube; a draw is kept with probability |det dx/dz| / W, W a bound calibrated
 // on a large latent sample at each training, which makes the kept draws
 // uniform in the image of the ball; draws outside the cube are dropped.  The
 // flow is trained with a held-out split and early stopping so that it stays
-// smooth; a flow whose calibrated kept fraction is below 1% is not used.
+// smooth; a flow whose calibrated kept fraction is below 0.2% is not used.
 // Every kept draw is then judged by the exact likelihood in the sampler.
 
 #include <cuda_bf16.h>
@@ -70,6 +70,9 @@ constexpr int FRI = 32;        // rows per inverse block
 constexpr int MAX_W = 128;     // conditioner width limit (shared-memory tiles)
 constexpr int MAX_D = 64;      // dimension limit
 constexpr int MAX_DENSE = 64;  // coupling layers x dense layers limit
+// smallest calibrated kept fraction of latent draws for which a flow is used
+// (its draws cost little on the tensor cores; below, the ellipsoid is used)
+constexpr double kMinKept = 0.002;
 
 __device__ __forceinline__ float to_f(float v) { return v; }
 __device__ __forceinline__ float to_f(__nv_bfloat16 v) { return __bfloat162float(v); }
@@ -744,9 +747,13 @@ __global__ void __launch_bounds__(256)
     }
 }
 
-// Shared-memory layout of lg_flow_inverse_tc (bytes).
+// Shared-memory layout of lg_flow_inverse_tc (bytes): one layer's weights,
+// the conditioner input and one hidden activation tile (each epilogue
+// overwrites the tile its MMA chain has finished reading), so that two
+// blocks fit on an SM and one block's epilogues overlap the other's MMAs
+// and weight copies.
 struct TcSmem {
-    int wbuf, a0, a1, a2, cur, obuf, ld, bar, total;
+    int wbuf, a0, a1, cur, obuf, ld, bar, total;
     __host__ __device__ explicit TcSmem(const FlowDims& f)
     {
         const TcDims t(f);
@@ -756,10 +763,9 @@ struct TcSmem {
             q += (bytes + 127) / 128 * 128;
             return at;
         };
-        wbuf = take(2 * 2 * t.sl);
+        wbuf = take(2 * t.sl);
         a0 = take(128 * t.kp0 * 2);
         a1 = take(128 * f.W * 2);
-        a2 = take(128 * f.W * 2);
         cur = take(128 * f.d * 4);
         obuf = take(128 * t.np * 4);
         ld = take(128 * 4);
@@ -768,7 +774,7 @@ struct TcSmem {
     }
 };
 
-__global__ void __launch_bounds__(256, 1)
+__global__ void __launch_bounds__(256, 2)
     lg_flow_inverse_tc(FlowDims f, const float* __restrict__ P, const __nv_bfloat16* __restrict__ packed,
                        const float* __restrict__ Z, int M, float* __restrict__ Uout, float* __restrict__ ldet,
                        int* __restrict__ err)
@@ -781,15 +787,15 @@ __global__ void __launch_bounds__(256, 1)
     unsigned char* wb = smem + L.wbuf;
     __nv_bfloat16* A0 = reinterpret_cast<__nv_bfloat16*>(smem + L.a0);
     __nv_bfloat16* A1 = reinterpret_cast<__nv_bfloat16*>(smem + L.a1);
-    __nv_bfloat16* A2 = reinterpret_cast<__nv_bfloat16*>(smem + L.a2);
     float* cur = reinterpret_cast<float*>(smem + L.cur);
     float* ob = reinterpret_cast<float*>(smem + L.obuf);
     float* ld = reinterpret_cast<float*>(smem + L.ld);
-    uint64_t* bars = reinterpret_cast<uint64_t*>(smem + L.bar);  // [0] MMA, [1], [2] weight buffers
+    uint64_t* bars = reinterpret_cast<uint64_t*>(smem + L.bar);  // [0] MMA, [1] weights
     uint32_t* misc = reinterpret_cast<uint32_t*>(smem + L.bar + 32);  // [0] TMEM base, [1] abort flag
     const uint32_t lbytes = 2u * td.sl;
+    // one accumulator of max(W, np) columns
     uint32_t tcols = 32;
-    while (tcols < 2u * W) tcols <<= 1;
+    while (tcols < (uint32_t)max(W, td.np)) tcols <<= 1;
 
     if (w == 0) {
         asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;" ::"r"(lg_saddr(misc)),
@@ -797,7 +803,7 @@ __global__ void __launch_bounds__(256, 1)
         asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;");
     }
     if (t == 0) {
-        for (int i = 0; i < 3; ++i)
+        for (int i = 0; i < 2; ++i)
             asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" ::"r"(lg_saddr(bars + i)), "r"(1));
         asm volatile("fence.mbarrier_init.release.cluster;");
         misc[1] = 0;
@@ -810,32 +816,28 @@ __global__ void __launch_bounds__(256, 1)
     __syncthreads();
     asm volatile("tcgen05.fence::after_thread_sync;");
     const uint32_t tmem = misc[0];
-    // weights of the first two layers (the inverse runs from layer L-1 down)
-    auto issue_weights = [&](int l, int b) {
-        void* bar = bars + 1 + b;
+    auto issue_weights = [&](int l) {
+        void* bar = bars + 1;
         asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(lg_saddr(bar)), "r"(lbytes)
                      : "memory");
         asm volatile("cp.async.bulk.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1], %2, [%3];" ::"r"(
-                         lg_saddr(wb + (size_t)b * lbytes)),
+                         lg_saddr(wb)),
                      "l"(packed + (size_t)l * td.sl), "r"(lbytes), "r"(lg_saddr(bar))
                      : "memory");
     };
-    // weight copies issued to and waited for per buffer (thread 0's view;
-    // every thread keeps the same counts)
-    int issued[2] = {1, f.L > 1 ? 1 : 0}, waited[2] = {0, 0};
-    if (t == 0) {
-        issue_weights(f.L - 1, 0);
-        if (f.L > 1) issue_weights(f.L - 2, 1);
-    }
+    // weight copies issued and waited for (thread 0's view; every thread
+    // keeps the same counts); the inverse runs from layer L-1 down
+    int issued = 1, waited = 0;
+    if (t == 0) issue_weights(f.L - 1);
     uint32_t mma_phase = 0;
     bool ok = true;
-    // one MMA chain: D (tmem column col) = A (128 x K) . B (N x K)^T
-    auto gemm = [&](uint32_t col, const void* A, const void* B, int K, int N) {
+    // one MMA chain: D (tmem) = A (128 x K) . B (N x K)^T
+    auto gemm = [&](const void* A, const void* B, int K, int N) {
         if (t == 0) {
             asm volatile("tcgen05.fence::after_thread_sync;");
             const uint32_t sb = (uint32_t)(K / 8) * 128, idesc = lg_umma_idesc(128, N);
             for (int ks = 0; ks < K / 16; ++ks)
-                lg_mma(tmem + col, lg_umma_desc(lg_saddr(A) + ks * 256, 128, sb),
+                lg_mma(tmem, lg_umma_desc(lg_saddr(A) + ks * 256, 128, sb),
                        lg_umma_desc(lg_saddr(B) + ks * 256, 128, sb), idesc, ks > 0);
             lg_mma_commit(bars);
             if (!lg_mbar_wait(bars, mma_phase)) misc[1] = 1;
@@ -845,12 +847,13 @@ __global__ void __launch_bounds__(256, 1)
         asm volatile("tcgen05.fence::after_thread_sync;");
         return misc[1] == 0;
     };
-    // epilogue of a hidden dense: tmem columns [col, col + W) + bias, ReLU,
-    // BF16 into Aout (128 x W core matrices); warp w reads lanes of w % 4,
-    // warps 0-3 the first half of the columns, 4-7 the second
-    auto hidden_epilogue = [&](uint32_t col, const float* __restrict__ bias, __nv_bfloat16* Aout) {
+    // epilogue of a hidden dense: tmem columns [0, W) + bias, ReLU, BF16
+    // into A1 (128 x W core matrices; the chain that read A1 has completed);
+    // warp w reads lanes of w % 4, warps 0-3 the first half of the columns,
+    // 4-7 the second
+    auto hidden_epilogue = [&](const float* __restrict__ bias) {
         const int m = 32 * (w % 4) + lane, half = w / 4;
-        const uint32_t taddr = tmem + ((uint32_t)(32 * (w % 4)) << 16) + col;
+        const uint32_t taddr = tmem + ((uint32_t)(32 * (w % 4)) << 16);
         for (int n0 = half * (W / 2); n0 < (half + 1) * (W / 2); n0 += 16) {
             float v[16];
             lg_tmem_ld16(taddr + n0, v);
@@ -860,7 +863,7 @@ __global__ void __launch_bounds__(256, 1)
                 const float x = v[j] + __ldg(bias + n0 + j);
                 h[j] = __float2bfloat16_rn(x > 0.0f ? x : 0.0f);
             }
-            uint4* dst = reinterpret_cast<uint4*>(Aout + lg_core_off(m, n0, W));
+            uint4* dst = reinterpret_cast<uint4*>(A1 + lg_core_off(m, n0, W));
             dst[0] = reinterpret_cast<const uint4*>(h)[0];
             dst[8] = reinterpret_cast<const uint4*>(h)[1];  // next core matrix along K: +64 elements
         }
@@ -868,8 +871,7 @@ __global__ void __launch_bounds__(256, 1)
         asm volatile("tcgen05.fence::before_thread_sync;");
         __syncthreads();
     };
-    for (int i = 0, l = f.L - 1; l >= 0 && ok; ++i, --l) {
-        const int b = i % 2;
+    for (int l = f.L - 1; l >= 0 && ok; --l) {
         const int da = f.da(l), db = f.db(l), a0 = f.a0(l), b0 = f.b0(l);
         // parameter offsets of this layer's biases (library layout)
         long woff = 0;
@@ -881,45 +883,39 @@ __global__ void __launch_bounds__(256, 1)
             A0[lg_core_off(m, k, td.kp0)] = __float2bfloat16_rn(k < da ? cur[m * d + a0 + k] : 0.0f);
         }
         asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
-        if (t == 0 && !lg_mbar_wait(bars + 1 + b, (uint32_t)waited[b] & 1u)) misc[1] = 1;
+        if (t == 0 && !lg_mbar_wait(bars + 1, (uint32_t)waited & 1u)) misc[1] = 1;
         __syncthreads();
-        if (!misc[1]) ++waited[b];
+        if (!misc[1]) ++waited;
         if (misc[1]) {
             ok = false;
             break;
         }
-        const unsigned char* Wl = wb + (size_t)b * lbytes;
         // input dense
         long bo = woff + (long)f.kin(l, 0) * f.kout(l, 0);
-        if (!(ok = gemm(0, A0, Wl, td.kp0, W))) break;
-        hidden_epilogue(0, P + bo, A1);
+        if (!(ok = gemm(A0, wb, td.kp0, W))) break;
+        hidden_epilogue(P + bo);
         long wo = bo + f.kout(l, 0);
-        // hidden denses
-        __nv_bfloat16* Ain = A1;
-        uint32_t col = 0;
+        // hidden denses, in place in A1
         for (int k = 1; k < NH && ok; ++k) {
-            col = (uint32_t)(k % 2) * W;
-            __nv_bfloat16* Aout = (Ain == A1) ? A2 : A1;
-            ok = gemm(col, Ain, Wl + 2 * (td.s0 + (size_t)(k - 1) * td.sh), W, W);
+            ok = gemm(A1, wb + 2 * (td.s0 + (size_t)(k - 1) * td.sh), W, W);
             if (!ok) break;
             bo = wo + (long)f.kin(l, k) * f.kout(l, k);
-            hidden_epilogue(col, P + bo, Aout);
+            hidden_epilogue(P + bo);
             wo = bo + f.kout(l, k);
-            Ain = Aout;
         }
         if (!ok) break;
-        // output dense into the other accumulator
-        const uint32_t ocol = (uint32_t)(NH % 2) * W;
-        if (!(ok = gemm(ocol, Ain, Wl + 2 * (td.s0 + (size_t)(NH - 1) * td.sh), W, td.np))) break;
+        // output dense
+        if (!(ok = gemm(A1, wb + 2 * (td.s0 + (size_t)(NH - 1) * td.sh), W, td.np))) break;
         const float* obias = P + wo + (long)f.kin(l, NH) * f.kout(l, NH);
-        // this layer's weights are consumed: prefetch layer l - 2
-        if (l - 2 >= 0) {
-            if (t == 0) issue_weights(l - 2, b);
-            ++issued[b];
+        // this layer's weights are consumed: the next layer's copy runs
+        // under the output epilogue and the coupling
+        if (l - 1 >= 0) {
+            if (t == 0) issue_weights(l - 1);
+            ++issued;
         }
         // output accumulators -> obuf (rows 0..127), then the coupling
         if (w < 4) {
-            const uint32_t taddr = tmem + ((uint32_t)(32 * w) << 16) + ocol;
+            const uint32_t taddr = tmem + ((uint32_t)(32 * w) << 16);
             const int m = 32 * w + lane;
             for (int n0 = 0; n0 < td.np; n0 += 16) {
                 float v[16];
@@ -949,9 +945,8 @@ __global__ void __launch_bounds__(256, 1)
         if (t < 128 && base + t < M) ldet[base + t] = ld[t];
     } else if (t == 0) {
         atomicExch(err, 1);
-        // weight copies still in flight land before the block exits
-        for (int b = 0; b < 2; ++b)
-            for (; waited[b] < issued[b]; ++waited[b]) lg_mbar_wait(bars + 1 + b, (uint32_t)waited[b] & 1u);
+        // a weight copy still in flight lands before the block exits
+        for (; waited < issued; ++waited) lg_mbar_wait(bars + 1, (uint32_t)waited & 1u);
     }
     asm volatile("tcgen05.fence::before_thread_sync;");
     __syncthreads();
@@ -968,7 +963,7 @@ __device__ __forceinline__ double lg_u01(unsigned long long key, unsigned long l
     return ((double)(z >> 11) + 0.5) * (1.0 / 9007199254740992.0);
 }
 
-// M points uniform in the d-ball of radius rad = expand sqrt(rad2[0]): normal
+// M points uniform in the d-ball of radius rad = scale sqrt(rad2[0]): normal
 // direction (Box-Muller pairs, regenerated from the counter for the second
 // pass instead of being held) scaled by rad u^(1/d).
 __device__ __forceinline__ float2 lg_normal_pair(unsigned long long key, unsigned long long c)
@@ -981,12 +976,12 @@ __device__ __forceinline__ float2 lg_normal_pair(unsigned long long key, unsigne
 }
 
 __global__ void __launch_bounds__(256)
-    lg_flow_latent(unsigned long long key, int M, int d, const double* __restrict__ rad2, double expand,
+    lg_flow_latent(unsigned long long key, int M, int d, const double* __restrict__ rad2, double rscale,
                    float* __restrict__ Z)
 {
     const int i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= M) return;
-    const double rad = expand * sqrt(rad2[0]);
+    const double rad = rscale * sqrt(rad2[0]);
     const unsigned long long c0 = (unsigned long long)i * (MAX_D + 2);
     float n2 = 0.0f;
     for (int a = 0; a < d; a += 2) {
@@ -1343,8 +1338,26 @@ public:
     DevBuf<float> cz, cu, cld, dz, du, dld;
     DevBuf<int> dflag, dcnt;
     DevBuf<double> dX, dout, dbound;
-    HostBuf<double> hbound, hout;
-    HostBuf<int> hcnt;
+    // Proposals come from a pool of kept draws of the active flow, refilled
+    // by one batch of latent draws at a time on the proposal stream; the
+    // next refill is enqueued as soon as the pool holds less than two
+    // batches, so that it runs under the likelihood calls of the next
+    // two.  Kept draws do not depend on the likelihood threshold, only on
+    // the flow and the weight bound, so they stay valid until the flow is
+    // replaced (gen counts the weights a slot has held).
+    HostBuf<double> hout;  // refill: kept draws
+    HostBuf<double> hbound;
+    HostBuf<int> hcnt;     // refill: [0] kept and in the cube, [1] kept, [2] inverse timeout
+    std::vector<double> pool;
+    size_t pool_pos = 0;
+    int pool_slot = -1;
+    long gen[2] = {0, 0}, pool_gen = -1;
+    bool inflight = false;
+    int refill_slot = -1;
+    long refill_gen = -1;
+    int refill_room = 0, refill_M = 0;
+    double kept_frac[2] = {0, 0};  // kept draws in the cube per latent draw
+    cudaEvent_t refill_done = nullptr;
 
     ~FlowProposal()
     {
@@ -1352,7 +1365,12 @@ public:
         if (ps) cudaStreamSynchronize(ps);
         if (ps) cudaStreamDestroy(ps);
         if (done) cudaEventDestroy(done);
+        if (refill_done) cudaEventDestroy(refill_done);
     }
+
+    // latent radius factor: the ball through the farthest live point,
+    // its volume enlarged by opt.expand
+    double rexp(int d) const { return std::pow(std::max(opt.expand, 1.0), 1.0 / d); }
 
     static int fail_cuda()
     {
@@ -1370,8 +1388,12 @@ public:
         }
         if (!ps && cudaStreamCreateWithFlags(&ps, cudaStreamNonBlocking) != cudaSuccess) return fail_cuda();
         if (!done && cudaEventCreateWithFlags(&done, cudaEventDisableTiming) != cudaSuccess) return fail_cuda();
+        if (!refill_done && cudaEventCreateWithFlags(&refill_done, cudaEventDisableTiming) != cudaSuccess)
+            return fail_cuda();
         cudaStream_t s = flow.stream;
         pslot = act < 0 ? 0 : 1 - act;
+        // a refill still reading this slot's weights runs first
+        if (inflight && cudaStreamWaitEvent(s, refill_done, 0) != cudaSuccess) return fail_cuda();
         // standardise by the live set
         std::vector<float>& mean = hmean[pslot];
         std::vector<float>& sdev = hsdev[pslot];
@@ -1465,7 +1487,7 @@ public:
         // calibration of the weight bound on 16384 latent draws: their
         // maximum log weight and sum of exp(weight - maximum)
         const int Mc = 16384;
-        lg_flow_latent<<<(Mc + 255) / 256, 256, 0, s>>>(cal_key, Mc, d, r, opt.expand, cz.p);
+        lg_flow_latent<<<(Mc + 255) / 256, 256, 0, s>>>(cal_key, Mc, d, r, rexp(d), cz.p);
         if (!flow.inverse(Puse[pslot].p, dpack[pslot].p, cz.p, Mc, cu.p, cld.p, s, dtcerr.p)) return fail_cuda();
         lg_flow_max<<<1, 1024, 0, s>>>(cld.p, Mc, -INFINITY, r + 1);
         lg_flow_expsum<<<1, 1024, 0, s>>>(cld.p, Mc, r + 1);
@@ -1479,7 +1501,7 @@ public:
     }
 
     // Wait for the pending retraining and make its slot the active one (or
-    // leave no flow active when it is unusable: a kept fraction below 1%).
+    // leave no flow active when it is unusable: a kept fraction below 0.2%).
     void finish()
     {
         pending = false;
@@ -1493,16 +1515,18 @@ public:
         // at once): the bias corrections of the next retraining continue
         // from there
         flow.step = step0 + (long)hstate.p[3] * steps_per_epoch;
-        radius[k] = std::sqrt(hres.p[0]) * opt.expand;
+        radius[k] = std::sqrt(hres.p[0]) * rexp(d);
         const double mx = hres.p[1];
         wnorm[k] = mx + 1.0;
         efficiency[k] = hres.p[2] * std::exp(-1.0) / 16384;  // mean exp(w - wnorm)
         int tcerr = 0;
         std::memcpy(&tcerr, hres.p + 3, sizeof tcerr);
-        usable[k] = std::isfinite(radius[k]) && radius[k] > 0 && std::isfinite(mx) && efficiency[k] >= 0.01 &&
+        usable[k] = std::isfinite(radius[k]) && radius[k] > 0 && std::isfinite(mx) && efficiency[k] >= kMinKept &&
                     tcerr == 0;
         if (tcerr) std::fprintf(stderr, "lensed_gb300: flow inverse: a bounded wait ran out; flow not used\n");
         act = usable[k] ? k : -1;
+        ++gen[k];
+        kept_frac[k] = efficiency[k];
         if (std::getenv("LG_FLOW_DEBUG"))
             std::fprintf(stderr,
                          "flow: train %ld epochs %d, held-out loss %.4f, latent radius %.3f, calibrated efficiency "
@@ -1523,6 +1547,13 @@ public:
         if (pending && since_train >= opt.lag) finish();
     }
 
+    // cost factor of a proposal: 1 + draw_cost x latent draws per point kept
+    // by the weight test
+    double log_cost() const override
+    {
+        return act < 0 ? 0.0 : std::log1p(std::max(opt.draw_cost, 0.0) / std::max(efficiency[act], kMinKept));
+    }
+
     // volume of the image of the latent ball: V_ball(R) E[|det dx/dz|]
     double log_volume() const override
     {
@@ -1534,52 +1565,101 @@ public:
         return lv;
     }
 
+    // Enqueue one refill of the pool from slot k: latent draws enough for
+    // about four batches of kept draws (at most 2^20), the inverse flow, the
+    // weight test against the bound (a weight above it raises the bound),
+    // the cube test and an order-preserving compaction, and the copies of
+    // the counts, the bound and the kept draws back to the host.
+    bool enqueue_refill(int k, int d, int B, uint64_t key)
+    {
+        const double kf = std::max(kept_frac[k], kMinKept);
+        const int M = (int)std::max(4.0 * B, std::min((double)(1 << 20), 4.0 * B / kf));
+        const int room = 8 * B;
+        if (!dz.ensure((size_t)M * d) || !du.ensure((size_t)M * d) || !dld.ensure(M) || !dX.ensure((size_t)M * d) ||
+            !dflag.ensure(M) || !dout.ensure((size_t)room * d) || !dcnt.ensure(2) || !dbound.ensure(1) ||
+            !hbound.ensure(1) || !hcnt.ensure(3) || !hout.ensure((size_t)room * d))
+            return false;
+        if ((int)wrap.size() != d) set_wrap(nullptr, d);
+        Rng r(key);
+        const uint64_t k_lat = r.next(), k_acc = r.next();
+        // keep x with probability proportional to 1 / q_x(x) = |det dx/dz|
+        // (z uniform in the ball), normalised by the calibrated bound
+        lg_flow_latent<<<(M + 255) / 256, 256, 0, ps>>>(k_lat, M, d, dres[k].p, rexp(d), dz.p);
+        if (!flow.inverse(Puse[k].p, dpack[k].p, dz.p, M, du.p, dld.p, ps, dtcerr.p + 1)) return false;
+        lg_flow_max<<<1, 1024, 0, ps>>>(dld.p, M, wnorm[k], dbound.p);
+        lg_flow_accept<<<(M + 255) / 256, 256, 0, ps>>>(k_acc, M, d, du.p, dld.p, dbound.p, dmean[k].p, dsdev[k].p,
+                                                         dwrap.p, dX.p, dflag.p);
+        lg_flow_compact<<<1, 1024, 0, ps>>>(dflag.p, M, dX.p, d, room, dout.p, dcnt.p);
+        if (cudaMemcpyAsync(hcnt.p, dcnt.p, 2 * sizeof(int), cudaMemcpyDeviceToHost, ps) ||
+            cudaMemcpyAsync(hcnt.p + 2, dtcerr.p + 1, sizeof(int), cudaMemcpyDeviceToHost, ps) ||
+            cudaMemcpyAsync(hbound.p, dbound.p, sizeof(double), cudaMemcpyDeviceToHost, ps) ||
+            cudaMemcpyAsync(hout.p, dout.p, (size_t)room * d * sizeof(double), cudaMemcpyDeviceToHost, ps) ||
+            cudaEventRecord(refill_done, ps))
+            return false;
+        inflight = true;
+        refill_slot = k;
+        refill_gen = gen[k];
+        refill_room = room;
+        refill_M = M;
+        return true;
+    }
+
+    // Wait for the refill in flight and append its draws to the pool when
+    // they come from the active flow; false on a CUDA error or an inverse
+    // timeout (the flow is then dropped).
+    bool merge(int d)
+    {
+        inflight = false;
+        if (cudaEventSynchronize(refill_done) != cudaSuccess) return false;
+        if (hcnt.p[2]) {
+            std::fprintf(stderr, "lensed_gb300: flow inverse: a bounded wait ran out; flow dropped\n");
+            act = -1;
+            return false;
+        }
+        const int k = refill_slot;
+        if (k != act || refill_gen != gen[k]) return true;
+        wnorm[k] = hbound.p[0];
+        const int n = std::min(hcnt.p[0], refill_room);
+        kept_frac[k] = 0.5 * kept_frac[k] + 0.5 * (double)hcnt.p[0] / refill_M;
+        if (std::getenv("LG_FLOW_DEBUG"))
+            std::fprintf(stderr, "flow: refill %d latent, %d kept by the weight test, %d in the cube\n", refill_M,
+                         hcnt.p[1], hcnt.p[0]);
+        pool.erase(pool.begin(), pool.begin() + (long)pool_pos * d);
+        pool_pos = 0;
+        pool.insert(pool.end(), hout.p, hout.p + (size_t)n * d);
+        return true;
+    }
+
     int propose(const double*, int, int d, double* out, int B, uint64_t sd) override
     {
         if (act < 0) return 0;
         cudaSetDevice(device);
         const int k = act;
-        const int M = std::max(4 * B, (int)std::min(65536.0, 2.0 * B / std::max(efficiency[k], 1e-3)));
-        if (!dz.ensure((size_t)M * d) || !du.ensure((size_t)M * d) || !dld.ensure(M) || !dX.ensure((size_t)M * d) ||
-            !dflag.ensure(M) || !dout.ensure((size_t)B * d) || !dcnt.ensure(2) || !dbound.ensure(1) ||
-            !hbound.ensure(1) || !hcnt.ensure(3) || !hout.ensure((size_t)B * d))
-            return 0;
+        if (pool_slot != k || pool_gen != gen[k]) {  // a new flow: its own pool
+            pool.clear();
+            pool_pos = 0;
+            pool_slot = k;
+            pool_gen = gen[k];
+        }
         Rng r(sd);
-        int got = 0;
-        for (int round = 0; round < 4 && got < B; ++round) {
-            // keep x with probability proportional to 1 / q_x(x) = |det dx/dz|
-            // (z uniform in the ball), normalised by the calibrated bound (a
-            // weight above it raises the bound for the rest of the round)
-            const uint64_t k_lat = r.next(), k_acc = r.next();
-            lg_flow_latent<<<(M + 255) / 256, 256, 0, ps>>>(k_lat, M, d, dres[k].p, opt.expand, dz.p);
-            if (!flow.inverse(Puse[k].p, dpack[k].p, dz.p, M, du.p, dld.p, ps, dtcerr.p + 1)) return fail_cuda(), 0;
-            lg_flow_max<<<1, 1024, 0, ps>>>(dld.p, M, wnorm[k], dbound.p);
-            if ((int)wrap.size() != d) set_wrap(nullptr, d);
-            lg_flow_accept<<<(M + 255) / 256, 256, 0, ps>>>(k_acc, M, d, du.p, dld.p, dbound.p, dmean[k].p,
-                                                             dsdev[k].p, dwrap.p, dX.p, dflag.p);
-            lg_flow_compact<<<1, 1024, 0, ps>>>(dflag.p, M, dX.p, d, B - got, dout.p + (size_t)got * d, dcnt.p);
-            if (cudaMemcpyAsync(hcnt.p, dcnt.p, 2 * sizeof(int), cudaMemcpyDeviceToHost, ps) ||
-                cudaMemcpyAsync(hcnt.p + 2, dtcerr.p + 1, sizeof(int), cudaMemcpyDeviceToHost, ps) ||
-                cudaMemcpyAsync(hbound.p, dbound.p, sizeof(double), cudaMemcpyDeviceToHost, ps) ||
-                cudaStreamSynchronize(ps))
-                return fail_cuda(), 0;
-            if (hcnt.p[2]) {
-                std::fprintf(stderr, "lensed_gb300: flow inverse: a bounded wait ran out; flow dropped\n");
-                act = -1;
-                return 0;
+        int got = 0, refills = 0;
+        for (;;) {
+            const size_t avail = pool.size() / d - pool_pos;
+            const int take = (int)std::min<size_t>(avail, (size_t)(B - got));
+            std::memcpy(out + (size_t)got * d, pool.data() + pool_pos * d, (size_t)take * d * sizeof(double));
+            pool_pos += take;
+            got += take;
+            if (got == B) break;
+            if (!inflight) {
+                if (refills++ == 8) break;
+                if (!enqueue_refill(k, d, B, r.next())) return fail_cuda(), 0;
             }
-            wnorm[k] = hbound.p[0];
-            if (std::getenv("LG_FLOW_DEBUG") && round == 0)
-                std::fprintf(stderr, "flow: propose %d latent, %d kept by the weight test, %d in the cube\n", M,
-                             hcnt.p[1], hcnt.p[0]);
-            got += hcnt.p[0];
+            if (!merge(d)) return act < 0 ? 0 : (fail_cuda(), 0);
         }
-        if (got > 0) {
-            if (cudaMemcpyAsync(hout.p, dout.p, (size_t)got * d * sizeof(double), cudaMemcpyDeviceToHost, ps) ||
-                cudaStreamSynchronize(ps))
-                return fail_cuda(), 0;
-            std::memcpy(out, hout.p, (size_t)got * d * sizeof(double));
-        }
+        // the next refill runs under the likelihood calls of this batch
+        // and the next
+        if (!inflight && pool.size() / d - pool_pos < 2 * (size_t)B && !enqueue_refill(k, d, B, r.next()))
+            return fail_cuda(), 0;
         return got;
     }
 };
@@ -1610,9 +1690,10 @@ lg_flow_options lg_flow_defaults(void)
     o.epochs = 200;
     o.batch = 256;
     o.lr = 1e-3;
-    o.expand = 1.1;
-    o.patience = 10;
-    o.lag = 500;
+    o.expand = 1.25;
+    o.patience = 6;
+    o.lag = 800;
+    o.draw_cost = 0.005;
     return o;
 }
 
@@ -1680,6 +1761,52 @@ int lg_flow_inverse_check(int device, int d, int layers, int width, int hidden, 
         cudaMemcpyAsync(ldet, dl.p, (size_t)M * 4, cudaMemcpyDeviceToHost, f.stream) ||
         cudaMemcpyAsync(&herr, e.p, sizeof(int), cudaMemcpyDeviceToHost, f.stream) || cudaStreamSynchronize(f.stream))
         return LG_ERR_CUDA;
+    return herr ? LG_ERR_TIMEOUT : LG_OK;
+}
+
+// Device time of the inverse flow on M latent points (uploaded once): reps
+// launches after two warm-up launches, CUDA events on the launching stream;
+// *ms = milliseconds per launch.
+int lg_flow_inverse_time(int device, int d, int layers, int width, int hidden, int tc, const float* params,
+                         const float* z, int M, int reps, float* ms)
+{
+    if (!params || !z || !ms || M <= 0 || reps <= 0) return LG_ERR_INPUT;
+    if (cudaSetDevice(device) != cudaSuccess) return LG_ERR_CUDA;
+    lg::Flow f;
+    f.bf16 = true;
+    if (!f.init(d, layers, width, hidden, 1)) {
+        lg::set_global_error(f.err.c_str());
+        return f.err.empty() ? LG_ERR_ALLOC : LG_ERR_INPUT;
+    }
+    if (tc && !f.tc) {
+        lg::set_global_error("flow inverse timing: the tensor-core path needs width % 32 == 0 (<= 256) on sm_100+");
+        return LG_ERR_UNSUPPORTED;
+    }
+    f.tc = tc != 0;
+    lg::DevBuf<float> dz, du, dl;
+    lg::DevBuf<__nv_bfloat16> pk;
+    lg::DevBuf<int> e;
+    if (!dz.ensure((size_t)M * d) || !du.ensure((size_t)M * d) || !dl.ensure(M) || !e.ensure(1) ||
+        (f.tc && !pk.ensure(f.packed_size())))
+        return LG_ERR_ALLOC;
+    cudaEvent_t e0 = nullptr, e1 = nullptr;
+    if (cudaMemcpy(f.P.p, params, f.nparams * 4, cudaMemcpyHostToDevice) ||
+        cudaMemcpy(dz.p, z, (size_t)M * d * 4, cudaMemcpyHostToDevice) || cudaMemset(e.p, 0, sizeof(int)) ||
+        (f.tc && !f.pack(f.P.p, pk.p, f.stream)) || cudaEventCreate(&e0) || cudaEventCreate(&e1))
+        return LG_ERR_CUDA;
+    bool ok = true;
+    for (int i = 0; i < 2 && ok; ++i) ok = f.inverse(f.P.p, f.tc ? pk.p : nullptr, dz.p, M, du.p, dl.p, f.stream, e.p);
+    ok = ok && cudaEventRecord(e0, f.stream) == cudaSuccess;
+    for (int i = 0; i < reps && ok; ++i) ok = f.inverse(f.P.p, f.tc ? pk.p : nullptr, dz.p, M, du.p, dl.p, f.stream, e.p);
+    int herr = 0;
+    float t = 0;
+    ok = ok && cudaEventRecord(e1, f.stream) == cudaSuccess &&
+         cudaMemcpyAsync(&herr, e.p, sizeof(int), cudaMemcpyDeviceToHost, f.stream) == cudaSuccess &&
+         cudaStreamSynchronize(f.stream) == cudaSuccess && cudaEventElapsedTime(&t, e0, e1) == cudaSuccess;
+    cudaEventDestroy(e0);
+    cudaEventDestroy(e1);
+    if (!ok) return LG_ERR_CUDA;
+    *ms = t / reps;
     return herr ? LG_ERR_TIMEOUT : LG_OK;
 }
 

@@ -373,7 +373,7 @@ bool load_state(const char* path, int nd, int nl, int batch, SamplerState& s)
 }  // namespace
 
 int nested_sample(int nd, lg_batch_loglike fn, void* user, const lg_nested_options* o, lg_nested_result* res,
-                  Proposal* learned, std::string& err)
+                  Proposal* learned, std::string& err, EllipsoidDrawer* drawer)
 {
     const auto t0 = std::chrono::steady_clock::now();
     lg_nested_options opt = lg_nested_defaults();
@@ -596,11 +596,38 @@ int nested_sample(int nd, lg_batch_loglike fn, void* user, const lg_nested_optio
                 }
                 bound_logv = ell.log_volume();
             }
-            // the learned bound is used when it is the tighter of the two
-            if (use_flow && learned->log_volume() < bound_logv) {
+            // the learned bound is used when it is the tighter of the two,
+            // its volume weighted by the cost of drawing from it (fixed by
+            // the options, so that runs repeat)
+            if (use_flow && learned->log_volume() + learned->log_cost() < bound_logv) {
                 n = learned->propose(live.data(), nl, nd, buf.data(), B, rng.next());
                 if (n > 0) n_flow += n;
                 else n = 0, ++n_flow_fail;
+            }
+            if (n == 0 && drawer) {
+                // the ellipsoids' draws on the GPU
+                std::vector<double> packed, logv;
+                auto pack = [&](const Ellipsoid& e) {
+                    packed.insert(packed.end(), e.mu.begin(), e.mu.end());
+                    packed.insert(packed.end(), e.L.begin(), e.L.end());
+                    packed.push_back(e.scale);
+                    logv.push_back(e.log_volume());
+                };
+                if (multi)
+                    for (const Ellipsoid& e : bound.ell) pack(e);
+                else
+                    pack(ell);
+                n = drawer->draw(nd, (int)logv.size(), packed.data(), logv.data(), opt.wrap, buf.data(), B,
+                                 rng.next());
+                if (n < 0) {
+                    err = "nested sampling: GPU ellipsoid draws failed";
+                    return LG_ERR_CUDA;
+                }
+                n_ell += n;
+                if (n == 0) {
+                    err = "nested sampling: ellipsoid left the unit cube";
+                    return LG_ERR_INPUT;
+                }
             }
             if (n == 0) {
                 long tries = 0;
@@ -772,7 +799,8 @@ extern "C" int lg_nested_run(lg_ctx* ctx, const lg_nested_options* opts, const l
             return LG_ERR_ALLOC;
         }
     }
-    int rc = lg::nested_sample(lg_ndims(ctx), ctx_loglike, &u, &o, result, prop.get(), err);
+    std::unique_ptr<lg::EllipsoidDrawer> drawer(lg::make_gpu_ellipsoid_drawer(lg::ctx_device(ctx), err));
+    int rc = lg::nested_sample(lg_ndims(ctx), ctx_loglike, &u, &o, result, prop.get(), err, drawer.get());
     if (rc) lg::set_global_error(err.c_str());
     return rc;
 }
@@ -788,7 +816,8 @@ extern "C" int lg_nested_sample_flow(int ndims, lg_batch_loglike fn, void* user,
     }
     lg_nested_options o = opts ? *opts : lg_nested_defaults();
     o.proposal = LG_PROPOSAL_FLOW;
-    int rc = lg::nested_sample(ndims, fn, user, &o, result, prop.get(), err);
+    std::unique_ptr<lg::EllipsoidDrawer> drawer(lg::make_gpu_ellipsoid_drawer(device, err));
+    int rc = lg::nested_sample(ndims, fn, user, &o, result, prop.get(), err, drawer.get());
     if (rc) lg::set_global_error(err.c_str());
     return rc;
 }

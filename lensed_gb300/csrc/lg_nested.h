@@ -65,10 +65,24 @@ struct Proposal {
     virtual void set_wrap(const int* wrap, int d) { (void)wrap, (void)d; }
     // log volume (unit-cube coordinates) of the region propose() draws from
     virtual double log_volume() const = 0;
+    // log of the cost of one of its proposals in likelihood calls (>= 0:
+    // the call itself plus drawing it); the sampler weighs volumes by it
+    virtual double log_cost() const { return 0.0; }
 };
 
+// Uniform draws in a union of ellipsoids (and the unit cube, periodic
+// dimensions wrapped) on the GPU (lg_propose.cu).  packed: per ellipsoid its
+// centre (d), lower Cholesky factor (d x d) and scale; logv: log volumes.
+// Returns the number of points written to out (up to B), negative on error.
+struct EllipsoidDrawer {
+    virtual ~EllipsoidDrawer() {}
+    virtual int draw(int d, int nell, const double* packed, const double* logv, const int* wrap, double* out,
+                     int B, uint64_t seed) = 0;
+};
+EllipsoidDrawer* make_gpu_ellipsoid_drawer(int device, std::string& err);
+
 int nested_sample(int nd, lg_batch_loglike fn, void* user, const lg_nested_options* o, lg_nested_result* res,
-                  Proposal* learned, std::string& err);
+                  Proposal* learned, std::string& err, EllipsoidDrawer* drawer = nullptr);
 
 // Affine-coupling flow proposal trained and run on the GPU (lg_flow.cu).
 Proposal* make_flow_proposal(int device, int d, const lg_flow_options* opts, std::string& err);

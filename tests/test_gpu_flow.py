@@ -139,3 +139,54 @@ def test_learned_proposal_with_a_wrapped_dimension(native):
     print(f"wrapped Gaussian d=4: exact {exact:.3f}, flow {r['logz']:.3f}+-{r['logz_err']:.3f}, "
           f"calls {r['ncall']}, flow proposals {r['n_flow_proposals']}")
     assert abs(r["logz"] - exact) < 4 * r["logz_err"] + 0.1
+
+
+def _draw(ells, B, wrap=None, seed=1):
+    """GPU draws in a union of spheres/ellipsoids given as (mu, cov, scale)."""
+    import ctypes as C
+
+    d = len(ells[0][0])
+    packed, logv = [], []
+    for mu, cov, scale in ells:
+        L = np.linalg.cholesky(np.asarray(cov, np.float64))
+        packed += list(mu) + list(L.ravel()) + [scale]
+        logv.append(0.5 * d * math.log(math.pi) - math.lgamma(0.5 * d + 1) + 0.5 * d * math.log(scale)
+                    + np.log(np.diag(L)).sum())
+    packed = np.array(packed, np.float64)
+    logv = np.array(logv, np.float64)
+    w = None if wrap is None else np.array(wrap, np.int32)
+    out = np.zeros((B, d))
+    n = lg.lib().lg_ellipsoid_draw_check(0, d, len(ells), packed.ctypes.data_as(C.POINTER(C.c_double)),
+                                         logv.ctypes.data_as(C.POINTER(C.c_double)),
+                                         None if w is None else w.ctypes.data_as(C.POINTER(C.c_int)),
+                                         out.ctypes.data_as(C.POINTER(C.c_double)), B, seed)
+    assert n == B, n
+    return out
+
+
+def test_gpu_ellipsoid_draws_are_uniform(native):
+    """The sampler's GPU proposals: uniform in one ball (radial CDF r^d,
+    centred), uniform in the union of two overlapping balls (the overlap
+    holds its volume share, not twice it), periodic wrapping."""
+    d, B = 3, 200000
+    x = _draw([([0.5] * d, np.eye(d) * 0.09, 1.0)], B)  # radius 0.3
+    r = np.linalg.norm(x - 0.5, axis=1) / 0.3
+    assert r.max() <= 1 + 1e-9
+    assert np.abs(np.mean(r ** d) - 0.5) < 0.005 and np.abs(x.mean(0) - 0.5).max() < 0.003
+    # two balls of radius 0.2, centres 0.2 apart along x: overlap volume share
+    c1, c2 = np.array([0.4, 0.5, 0.5]), np.array([0.6, 0.5, 0.5])
+    x = _draw([(c1, np.eye(d) * 0.04, 1.0), (c2, np.eye(d) * 0.04, 1.0)], B, seed=3)
+    in1 = np.linalg.norm(x - c1, axis=1) <= 0.2 + 1e-12
+    in2 = np.linalg.norm(x - c2, axis=1) <= 0.2 + 1e-12
+    assert np.all(in1 | in2)
+    R, dd = 0.2, 0.2
+    lens = math.pi * (4 * R + dd) * (2 * R - dd) ** 2 / 12  # lens-shaped overlap of two balls
+    ball = 4 / 3 * math.pi * R ** 3
+    share = lens / (2 * ball - lens)
+    assert abs(np.mean(in1 & in2) - share) < 0.006, (np.mean(in1 & in2), share)
+    # a ball of radius 0.1 across the boundary x0 = 0 of a periodic
+    # dimension: the cap below 0 (height 0.05, 5/32 of the ball) re-enters
+    # near x0 = 1
+    x = _draw([([0.05, 0.5, 0.5], np.eye(d) * 0.01, 1.0)], 100000, wrap=[1, 0, 0], seed=5)
+    assert np.all((x >= 0) & (x <= 1))
+    assert abs(np.mean(x[:, 0] > 0.5) - 5 / 32) < 0.006, np.mean(x[:, 0] > 0.5)
