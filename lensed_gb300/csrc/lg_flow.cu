@@ -46,6 +46,7 @@
 #include <cuda_runtime.h>
 
 #include <algorithm>
+#include <chrono>
 #include <cmath>
 #include <cstdio>
 #include <cstdlib>
@@ -1038,9 +1039,10 @@ __global__ void __launch_bounds__(1024) lg_flow_expsum(const float* __restrict__
 // [0, 1) on periodic dimensions, must lie in the unit cube.  flag[i] = 2
 // kept and inside, 1 kept outside, 0 rejected.
 __global__ void __launch_bounds__(256)
-    lg_flow_accept(unsigned long long key, int M, int d, const float* __restrict__ U, const float* __restrict__ ldet,
-                   const double* __restrict__ bound, const float* __restrict__ mean, const float* __restrict__ sdev,
-                   const int* __restrict__ wrap, double* __restrict__ X, int* __restrict__ flag)
+    lg_flow_accept(unsigned long long key, int M, int d, const float* __restrict__ Z, const float* __restrict__ U,
+                   const float* __restrict__ ldet, const double* __restrict__ bound, const float* __restrict__ mean,
+                   const float* __restrict__ sdev, const int* __restrict__ wrap, double* __restrict__ X,
+                   int* __restrict__ flag)
 {
     const int i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= M) return;
@@ -1048,19 +1050,22 @@ __global__ void __launch_bounds__(256)
     int f = 0;
     if (isfinite(l) && !(lg_u01(key, (unsigned long long)i) > exp((double)l - bound[0]))) {
         f = 2;
+        double z2 = 0.0;
         for (int a = 0; a < d; ++a) {
             double x = (double)mean[a] + (double)sdev[a] * (double)U[(size_t)i * d + a];
             if (wrap[a]) x -= floor(x);  // periodic dimension
-            X[(size_t)i * d + a] = x;
+            X[(size_t)i * (d + 1) + a] = x;
             if (!(x >= 0.0 && x <= 1.0)) f = 1;
+            z2 += (double)Z[(size_t)i * d + a] * Z[(size_t)i * d + a];
         }
+        X[(size_t)i * (d + 1) + d] = z2;  // latent radius^2, for later radius updates
     }
     flag[i] = f;
 }
 
 // Order-preserving compaction (one block): the first `room` draws with
-// flag 2 go to out in draw order; cnt[0] = how many were written, cnt[1] =
-// how many passed the weight test.
+// flag 2 (rows of d values) go to out in draw order; cnt[0] = how many were
+// written, cnt[1] = how many passed the weight test.
 __global__ void __launch_bounds__(1024)
     lg_flow_compact(const int* __restrict__ flag, int M, const double* __restrict__ X, int d, int room,
                     double* __restrict__ out, int* __restrict__ cnt)
@@ -1185,7 +1190,12 @@ public:
         tc = bf16 && cc >= 10 && width % 32 == 0 && width <= 256 && TcDims(f).np <= width &&
              TcSmem(f).total <= optin && !std::getenv("LG_FLOW_NO_TC");
         if (tc) cudaFuncSetAttribute(lg_flow_inverse_tc, cudaFuncAttributeMaxDynamicSharedMemorySize, TcSmem(f).total);
-        if (!stream && cudaStreamCreateWithFlags(&stream, cudaStreamNonBlocking) != cudaSuccess) return false;
+        // the highest stream priority: training launches are small and
+        // run beside the likelihood's large grids, whose blocks they then
+        // pass in the queue as SMs free up
+        int lo = 0, hi = 0;
+        cudaDeviceGetStreamPriorityRange(&lo, &hi);
+        if (!stream && cudaStreamCreateWithPriority(&stream, cudaStreamNonBlocking, hi) != cudaSuccess) return false;
         const int sm_step = step_smem(), sm_inv = inverse_smem();
         if (bf16) {
             cudaFuncSetAttribute(lg_flow_step<FR, __nv_bfloat16>, cudaFuncAttributeMaxDynamicSharedMemorySize, sm_step);
@@ -1312,7 +1322,7 @@ public:
     uint64_t seed = 1;
     long ntrain = 0;
     cudaStream_t ps = nullptr;  // proposals
-    cudaEvent_t done = nullptr;
+    cudaEvent_t done = nullptr, started = nullptr;  // a retraining's end and start on its stream
     bool pending = false;
     int act = -1, pslot = 0;  // active slot (-1: none) and the slot being trained
     // per slot: weights, standardisation, latent radius^2 and calibration
@@ -1358,6 +1368,22 @@ public:
     int refill_room = 0, refill_M = 0;
     double kept_frac[2] = {0, 0};  // kept draws in the cube per latent draw
     cudaEvent_t refill_done = nullptr;
+    // Between trainings the latent ball follows the live points: every
+    // refresh() runs the live points through the active flow (largest
+    // latent radius) and recalibrates the weight bound for that ball on the
+    // proposal stream; the result is applied at the next refresh(), a fixed
+    // number of replacements later, so that runs repeat.  A smaller ball
+    // keeps the pooled draws inside it (each carries its latent radius), a
+    // larger one drops the pool.
+    double r2live[2] = {0, 0};  // largest |z|^2 of the live points per slot
+    HostBuf<float> hlive;
+    HostBuf<double> htrack;
+    DevBuf<float> dlive, dtl, dtz, tz, tu, tld;
+    DevBuf<double> dtrack;  // [0] max |z|^2 of the live points, [1] max log weight, [2] sum exp(w - max)
+    bool track_pending = false;
+    int track_slot = -1;
+    long track_gen = -1, ntrack = 0;
+    cudaEvent_t track_done = nullptr;
 
     ~FlowProposal()
     {
@@ -1365,7 +1391,9 @@ public:
         if (ps) cudaStreamSynchronize(ps);
         if (ps) cudaStreamDestroy(ps);
         if (done) cudaEventDestroy(done);
+        if (started) cudaEventDestroy(started);
         if (refill_done) cudaEventDestroy(refill_done);
+        if (track_done) cudaEventDestroy(track_done);
     }
 
     // latent radius factor: the ball through the farthest live point,
@@ -1387,13 +1415,16 @@ public:
             if (!flow.init(d, opt.layers, opt.width, opt.hidden, seed)) return LG_ERR_INPUT;
         }
         if (!ps && cudaStreamCreateWithFlags(&ps, cudaStreamNonBlocking) != cudaSuccess) return fail_cuda();
-        if (!done && cudaEventCreateWithFlags(&done, cudaEventDisableTiming) != cudaSuccess) return fail_cuda();
+        if (!done && cudaEventCreate(&done) != cudaSuccess) return fail_cuda();
+        if (!started && cudaEventCreate(&started) != cudaSuccess) return fail_cuda();
         if (!refill_done && cudaEventCreateWithFlags(&refill_done, cudaEventDisableTiming) != cudaSuccess)
             return fail_cuda();
         cudaStream_t s = flow.stream;
         pslot = act < 0 ? 0 : 1 - act;
-        // a refill still reading this slot's weights runs first
+        // a refill or a radius update still reading this slot's weights
+        // runs first
         if (inflight && cudaStreamWaitEvent(s, refill_done, 0) != cudaSuccess) return fail_cuda();
+        if (track_pending && cudaStreamWaitEvent(s, track_done, 0) != cudaSuccess) return fail_cuda();
         // standardise by the live set
         std::vector<float>& mean = hmean[pslot];
         std::vector<float>& sdev = hsdev[pslot];
@@ -1413,8 +1444,9 @@ public:
         // parameters than there are live points)
         const int nval = std::max(1, n / 5), ntr = n - nval;
         // warm start: later retrainings continue from the previous weights
-        // with a quarter of the epochs
-        const int epochs = ntrain == 0 ? opt.epochs : std::max(1, opt.epochs / 4);
+        // with an eighth of the epochs (early stopping ends most of them
+        // after 6 to 11)
+        const int epochs = ntrain == 0 ? opt.epochs : std::max(1, opt.epochs / 8);
         const int Mb = std::min(opt.batch, ntr);
         steps_per_epoch = ntr / Mb;
         const size_t nidx = (size_t)nval + (size_t)epochs * ntr, nst = 8 + LG_FLOW_HISTORY;
@@ -1457,7 +1489,8 @@ public:
             cudaMemcpyAsync(dsdev[pslot].p, hx.p + (size_t)n * d + d, d * 4, cudaMemcpyHostToDevice, s) ||
             cudaMemcpyAsync(didx.p, hidx.p, nidx * sizeof(int), cudaMemcpyHostToDevice, s) ||
             cudaMemcpyAsync(state.p, hinit.p, nst * sizeof(float), cudaMemcpyHostToDevice, s) ||
-            cudaMemsetAsync(dstop.p, 0, sizeof(int), s) || cudaMemsetAsync(dtcerr.p, 0, 2 * sizeof(int), s))
+            cudaMemsetAsync(dstop.p, 0, sizeof(int), s) || cudaMemsetAsync(dtcerr.p, 0, 2 * sizeof(int), s) ||
+            cudaEventRecord(started, s))
             return fail_cuda();
         // the whole retraining is enqueued at once: the held-out check stops
         // it on the device, keeping the best weights
@@ -1505,16 +1538,21 @@ public:
     void finish()
     {
         pending = false;
+        const auto tw = std::chrono::steady_clock::now();
         if (cudaEventSynchronize(done) != cudaSuccess) {
             fail_cuda();
             act = -1;
             return;
         }
+        const double waited_ms = std::chrono::duration<double, std::milli>(std::chrono::steady_clock::now() - tw).count();
+        float train_ms = 0;
+        cudaEventElapsedTime(&train_ms, started, done);
         const int k = pslot, d = flow.f.d;
         // Adam steps the device actually took (those after the stop returned
         // at once): the bias corrections of the next retraining continue
         // from there
         flow.step = step0 + (long)hstate.p[3] * steps_per_epoch;
+        r2live[k] = hres.p[0];
         radius[k] = std::sqrt(hres.p[0]) * rexp(d);
         const double mx = hres.p[1];
         wnorm[k] = mx + 1.0;
@@ -1530,8 +1568,9 @@ public:
         if (std::getenv("LG_FLOW_DEBUG"))
             std::fprintf(stderr,
                          "flow: train %ld epochs %d, held-out loss %.4f, latent radius %.3f, calibrated efficiency "
-                         "%.4f, usable %d (d %d)\n",
-                         ntrain, (int)hstate.p[3], hstate.p[0], radius[k], efficiency[k], (int)usable[k], d);
+                         "%.4f, usable %d (d %d), on the GPU %.2f ms, waited %.2f ms\n",
+                         ntrain, (int)hstate.p[3], hstate.p[0], radius[k], efficiency[k], (int)usable[k], d, train_ms,
+                         waited_ms);
     }
 
     void set_wrap(const int* w, int d) override
@@ -1574,10 +1613,10 @@ public:
     {
         const double kf = std::max(kept_frac[k], kMinKept);
         const int M = (int)std::max(4.0 * B, std::min((double)(1 << 20), 4.0 * B / kf));
-        const int room = 8 * B;
-        if (!dz.ensure((size_t)M * d) || !du.ensure((size_t)M * d) || !dld.ensure(M) || !dX.ensure((size_t)M * d) ||
-            !dflag.ensure(M) || !dout.ensure((size_t)room * d) || !dcnt.ensure(2) || !dbound.ensure(1) ||
-            !hbound.ensure(1) || !hcnt.ensure(3) || !hout.ensure((size_t)room * d))
+        const int room = 8 * B, w = d + 1;  // rows: the point, then its latent radius^2
+        if (!dz.ensure((size_t)M * d) || !du.ensure((size_t)M * d) || !dld.ensure(M) || !dX.ensure((size_t)M * w) ||
+            !dflag.ensure(M) || !dout.ensure((size_t)room * w) || !dcnt.ensure(2) || !dbound.ensure(1) ||
+            !hbound.ensure(1) || !hcnt.ensure(3) || !hout.ensure((size_t)room * w))
             return false;
         if ((int)wrap.size() != d) set_wrap(nullptr, d);
         Rng r(key);
@@ -1587,13 +1626,13 @@ public:
         lg_flow_latent<<<(M + 255) / 256, 256, 0, ps>>>(k_lat, M, d, dres[k].p, rexp(d), dz.p);
         if (!flow.inverse(Puse[k].p, dpack[k].p, dz.p, M, du.p, dld.p, ps, dtcerr.p + 1)) return false;
         lg_flow_max<<<1, 1024, 0, ps>>>(dld.p, M, wnorm[k], dbound.p);
-        lg_flow_accept<<<(M + 255) / 256, 256, 0, ps>>>(k_acc, M, d, du.p, dld.p, dbound.p, dmean[k].p, dsdev[k].p,
-                                                         dwrap.p, dX.p, dflag.p);
-        lg_flow_compact<<<1, 1024, 0, ps>>>(dflag.p, M, dX.p, d, room, dout.p, dcnt.p);
+        lg_flow_accept<<<(M + 255) / 256, 256, 0, ps>>>(k_acc, M, d, dz.p, du.p, dld.p, dbound.p, dmean[k].p,
+                                                         dsdev[k].p, dwrap.p, dX.p, dflag.p);
+        lg_flow_compact<<<1, 1024, 0, ps>>>(dflag.p, M, dX.p, w, room, dout.p, dcnt.p);
         if (cudaMemcpyAsync(hcnt.p, dcnt.p, 2 * sizeof(int), cudaMemcpyDeviceToHost, ps) ||
             cudaMemcpyAsync(hcnt.p + 2, dtcerr.p + 1, sizeof(int), cudaMemcpyDeviceToHost, ps) ||
             cudaMemcpyAsync(hbound.p, dbound.p, sizeof(double), cudaMemcpyDeviceToHost, ps) ||
-            cudaMemcpyAsync(hout.p, dout.p, (size_t)room * d * sizeof(double), cudaMemcpyDeviceToHost, ps) ||
+            cudaMemcpyAsync(hout.p, dout.p, (size_t)room * w * sizeof(double), cudaMemcpyDeviceToHost, ps) ||
             cudaEventRecord(refill_done, ps))
             return false;
         inflight = true;
@@ -1624,10 +1663,99 @@ public:
         if (std::getenv("LG_FLOW_DEBUG"))
             std::fprintf(stderr, "flow: refill %d latent, %d kept by the weight test, %d in the cube\n", refill_M,
                          hcnt.p[1], hcnt.p[0]);
-        pool.erase(pool.begin(), pool.begin() + (long)pool_pos * d);
+        pool.erase(pool.begin(), pool.begin() + (long)pool_pos * (d + 1));
         pool_pos = 0;
-        pool.insert(pool.end(), hout.p, hout.p + (size_t)n * d);
+        // draws of a ball larger than the current one are kept when they
+        // fall inside it
+        const double b2 = ball2(k, d);
+        for (int i = 0; i < n; ++i) {
+            const double* row = hout.p + (size_t)i * (d + 1);
+            if (row[d] <= b2) pool.insert(pool.end(), row, row + d + 1);
+        }
         return true;
+    }
+
+    // squared latent radius of slot k's ball (a relative margin of 1e-5
+    // for the FP32 rounding of the draws)
+    double ball2(int k, int d) const { return r2live[k] * rexp(d) * rexp(d) * (1.0 + 1e-5); }
+
+    void refresh(const double* live, int n, int d) override
+    {
+        if (act < 0 || !ps || n < 1) return;
+        cudaSetDevice(device);
+        if (track_pending) apply_track(d);
+        if (act < 0) return;
+        const int k = act, Mc = 16384;
+        if (!track_done && cudaEventCreateWithFlags(&track_done, cudaEventDisableTiming) != cudaSuccess) return;
+        if (!hlive.ensure((size_t)n * d) || !dlive.ensure((size_t)n * d) || !dtl.ensure(n) || !dtz.ensure(n) ||
+            !dtrack.ensure(3) || !htrack.ensure(3) || !tz.ensure((size_t)Mc * d) || !tu.ensure((size_t)Mc * d) ||
+            !tld.ensure(Mc))
+            return;
+        for (int i = 0; i < n; ++i)
+            for (int a = 0; a < d; ++a)
+                hlive.p[(size_t)i * d + a] = (float)((live[(size_t)i * d + a] - hmean[k][a]) / hsdev[k][a]);
+        if (cudaMemcpyAsync(dlive.p, hlive.p, (size_t)n * d * sizeof(float), cudaMemcpyHostToDevice, ps)) return;
+        // the live points' latent radii through the active weights
+        const int blocks = (n + FR - 1) / FR, sm = flow.step_smem();
+        if (flow.bf16)
+            lg_flow_step<FR, __nv_bfloat16><<<blocks, FT, sm, ps>>>(flow.f, Puse[k].p, dlive.p, nullptr, 0, n, 0,
+                                                                    dtl.p, dtz.p, nullptr, (long)flow.nparams,
+                                                                    nullptr);
+        else
+            lg_flow_step<FR, float><<<blocks, FT, sm, ps>>>(flow.f, Puse[k].p, dlive.p, nullptr, 0, n, 0, dtl.p,
+                                                            dtz.p, nullptr, (long)flow.nparams, nullptr);
+        lg_flow_max<<<1, 1024, 0, ps>>>(dtz.p, n, -INFINITY, dtrack.p);
+        // the weight bound of that ball, calibrated as at training
+        const uint64_t key = seed * 0x9E3779B97F4A7C15ull + 0xD1B54A32D192ED03ull * (uint64_t)(++ntrack);
+        lg_flow_latent<<<(Mc + 255) / 256, 256, 0, ps>>>(key, Mc, d, dtrack.p, rexp(d), tz.p);
+        if (!flow.inverse(Puse[k].p, dpack[k].p, tz.p, Mc, tu.p, tld.p, ps, dtcerr.p + 1)) return;
+        lg_flow_max<<<1, 1024, 0, ps>>>(tld.p, Mc, -INFINITY, dtrack.p + 1);
+        lg_flow_expsum<<<1, 1024, 0, ps>>>(tld.p, Mc, dtrack.p + 1);
+        if (cudaMemcpyAsync(htrack.p, dtrack.p, 3 * sizeof(double), cudaMemcpyDeviceToHost, ps) ||
+            cudaEventRecord(track_done, ps))
+            return;
+        track_pending = true;
+        track_slot = k;
+        track_gen = gen[k];
+    }
+
+    // Take the radius update enqueued at the previous refresh(): the ball,
+    // the weight bound and the kept fraction of the active slot.
+    void apply_track(int d)
+    {
+        track_pending = false;
+        if (cudaEventSynchronize(track_done) != cudaSuccess) return;
+        const int k = track_slot;
+        if (k != act || track_gen != gen[k]) return;
+        const double r2 = htrack.p[0], mx = htrack.p[1], eff = htrack.p[2] * std::exp(-1.0) / 16384;
+        if (!(std::isfinite(r2) && r2 > 0 && std::isfinite(mx) && eff >= kMinKept)) return;
+        if (r2 > r2live[k]) {  // a larger ball: the pooled draws no longer cover it
+            ++gen[k];
+            pool.clear();
+            pool_pos = 0;
+            pool_gen = gen[k];
+        }
+        r2live[k] = r2;
+        radius[k] = std::sqrt(r2) * rexp(d);
+        wnorm[k] = mx + 1.0;
+        efficiency[k] = eff;
+        kept_frac[k] = eff;
+        cudaMemcpyAsync(dres[k].p, dtrack.p, sizeof(double), cudaMemcpyDeviceToDevice, ps);
+        // pooled draws outside the smaller ball are dropped
+        const double b2 = ball2(k, d);
+        size_t o = 0;
+        for (size_t i = pool_pos; i < pool.size() / (d + 1); ++i) {
+            const double* row = &pool[i * (d + 1)];
+            if (row[d] <= b2) {
+                std::memmove(&pool[o * (d + 1)], row, (d + 1) * sizeof(double));
+                ++o;
+            }
+        }
+        pool.resize(o * (d + 1));
+        pool_pos = 0;
+        if (std::getenv("LG_FLOW_DEBUG"))
+            std::fprintf(stderr, "flow: radius update: latent radius %.3f, efficiency %.4f, pool %zu\n", radius[k],
+                         eff, o);
     }
 
     int propose(const double*, int, int d, double* out, int B, uint64_t sd) override
@@ -1643,10 +1771,12 @@ public:
         }
         Rng r(sd);
         int got = 0, refills = 0;
+        const size_t w = (size_t)d + 1;
         for (;;) {
-            const size_t avail = pool.size() / d - pool_pos;
+            const size_t avail = pool.size() / w - pool_pos;
             const int take = (int)std::min<size_t>(avail, (size_t)(B - got));
-            std::memcpy(out + (size_t)got * d, pool.data() + pool_pos * d, (size_t)take * d * sizeof(double));
+            for (int i = 0; i < take; ++i)
+                std::memcpy(out + (size_t)(got + i) * d, pool.data() + (pool_pos + i) * w, d * sizeof(double));
             pool_pos += take;
             got += take;
             if (got == B) break;
@@ -1658,7 +1788,7 @@ public:
         }
         // the next refill runs under the likelihood calls of this batch
         // and the next
-        if (!inflight && pool.size() / d - pool_pos < 2 * (size_t)B && !enqueue_refill(k, d, B, r.next()))
+        if (!inflight && pool.size() / w - pool_pos < 2 * (size_t)B && !enqueue_refill(k, d, B, r.next()))
             return fail_cuda(), 0;
         return got;
     }

@@ -38,6 +38,7 @@ namespace lg {
 struct Ellipsoid {
     int d = 0;
     std::vector<double> mu, L;  // L lower triangular, row-major d x d
+    std::vector<double> Li;     // L^-1 (lower triangular): Mahalanobis distances as mat-vecs
     double scale = 1;           // (x-mu)^T C^-1 (x-mu) <= scale defines the boundary
 
     bool fit(const std::vector<double>& pts, int n, int dim, double enlarge_volume)
@@ -47,14 +48,28 @@ struct Ellipsoid {
         for (int i = 0; i < n; ++i)
             for (int k = 0; k < d; ++k) mu[k] += pts[(size_t)i * d + k];
         for (auto& m : mu) m /= n;
-        std::vector<double> C((size_t)d * d, 0);
+        // centred coordinates, one row per dimension, so that each
+        // covariance entry is a dot product over the points (four partial
+        // sums in a fixed order)
+        std::vector<double> xt((size_t)d * n);
         for (int i = 0; i < n; ++i)
-            for (int a = 0; a < d; ++a) {
-                const double xa = pts[(size_t)i * d + a] - mu[a];
-                for (int b = 0; b <= a; ++b) C[(size_t)a * d + b] += xa * (pts[(size_t)i * d + b] - mu[b]);
-            }
+            for (int k = 0; k < d; ++k) xt[(size_t)k * n + i] = pts[(size_t)i * d + k] - mu[k];
+        std::vector<double> C((size_t)d * d, 0);
         for (int a = 0; a < d; ++a)
-            for (int b = 0; b <= a; ++b) C[(size_t)a * d + b] /= n;
+            for (int b = 0; b <= a; ++b) {
+                const double* xa = &xt[(size_t)a * n];
+                const double* xb = &xt[(size_t)b * n];
+                double s0 = 0, s1 = 0, s2 = 0, s3 = 0;
+                int i = 0;
+                for (; i + 4 <= n; i += 4) {
+                    s0 += xa[i] * xb[i];
+                    s1 += xa[i + 1] * xb[i + 1];
+                    s2 += xa[i + 2] * xb[i + 2];
+                    s3 += xa[i + 3] * xb[i + 3];
+                }
+                for (; i < n; ++i) s0 += xa[i] * xb[i];
+                C[(size_t)a * d + b] = ((s0 + s1) + (s2 + s3)) / n;
+            }
         // Cholesky with a small diagonal floor for degenerate point sets
         L.assign((size_t)d * d, 0);
         for (int a = 0; a < d; ++a) {
@@ -69,24 +84,43 @@ struct Ellipsoid {
                 }
             }
         }
+        invert();
         double kmax = 0;
-        std::vector<double> y(d);
+        std::vector<double> x(d);
         for (int i = 0; i < n; ++i) {
-            kmax = std::max(kmax, mahalanobis(&pts[(size_t)i * d], y));
+            for (int k = 0; k < d; ++k) x[k] = xt[(size_t)k * n + i];
+            kmax = std::max(kmax, centred_norm2(x.data()));
         }
         scale = kmax * std::pow(enlarge_volume, 2.0 / d);
         return std::isfinite(scale) && scale > 0;
     }
-    double mahalanobis(const double* x, std::vector<double>& y) const
+    // Li = L^-1 by forward substitution on the unit vectors
+    void invert()
+    {
+        Li.assign((size_t)d * d, 0);
+        for (int c = 0; c < d; ++c)
+            for (int a = c; a < d; ++a) {
+                double s = a == c ? 1.0 : 0.0;
+                for (int k = c; k < a; ++k) s -= L[(size_t)a * d + k] * Li[(size_t)k * d + c];
+                Li[(size_t)a * d + c] = s / L[(size_t)a * d + a];
+            }
+    }
+    // |L^-1 x|^2 of a centred point: rows independent of each other
+    double centred_norm2(const double* x) const
     {
         double m = 0;
         for (int a = 0; a < d; ++a) {
-            double s = x[a] - mu[a];
-            for (int k = 0; k < a; ++k) s -= L[(size_t)a * d + k] * y[k];
-            y[a] = s / L[(size_t)a * d + a];
-            m += y[a] * y[a];
+            const double* r = &Li[(size_t)a * d];
+            double s = 0;
+            for (int k = 0; k <= a; ++k) s += r[k] * x[k];
+            m += s * s;
         }
         return m;
+    }
+    double mahalanobis(const double* x, std::vector<double>& y) const
+    {
+        for (int a = 0; a < d; ++a) y[a] = x[a] - mu[a];
+        return centred_norm2(y.data());
     }
     // uniform draw inside the ellipsoid
     void sample(Rng& r, double* x, std::vector<double>& u) const
@@ -467,6 +501,7 @@ int nested_sample(int nd, lg_batch_loglike fn, void* user, const lg_nested_optio
                 e.mu.assign(st.bound.begin() + o, st.bound.begin() + o + nd);
                 o += nd;
                 e.L.assign(st.bound.begin() + o, st.bound.begin() + o + (size_t)nd * nd);
+                e.invert();
                 o += (size_t)nd * nd;
                 bound.ell.push_back(e);
             }
@@ -508,6 +543,17 @@ int nested_sample(int nd, lg_batch_loglike fn, void* user, const lg_nested_optio
         }
         return save_state(opt.checkpoint, c);
     };
+    // live points ordered by logL in a binary min-heap (ties by index, the
+    // point a scan for the first minimum would pick), and the largest logL:
+    // O(log nlive) per iteration instead of a scan of the live set
+    std::vector<std::pair<double, int>> order(nl);
+    double lmax = -HUGE_VAL;
+    for (int i = 0; i < nl; ++i) {
+        order[i] = {llive[i], i};
+        lmax = std::max(lmax, llive[i]);
+    }
+    const auto later = [](const std::pair<double, int>& a, const std::pair<double, int>& b) { return a > b; };
+    std::make_heap(order.begin(), order.end(), later);
     for (;; ++iter) {
         if (opt.checkpoint && opt.checkpoint_every > 0 && iter > 0 && iter % opt.checkpoint_every == 0 &&
             !checkpoint()) {
@@ -521,12 +567,7 @@ int nested_sample(int nd, lg_batch_loglike fn, void* user, const lg_nested_optio
             }
             break;
         }
-        int imin = 0;
-        double lmax = -HUGE_VAL;
-        for (int i = 0; i < nl; ++i) {
-            if (llive[i] < llive[imin]) imin = i;
-            lmax = std::max(lmax, llive[i]);
-        }
+        const int imin = order.front().second;
         // termination: the live points can still add at most X * Lmax
         if (iter > 0 && logaddexp(logz, logx + lmax) - logz < opt.tol) {
             if (!checkpoint()) {
@@ -558,7 +599,14 @@ int nested_sample(int nd, lg_batch_loglike fn, void* user, const lg_nested_optio
             pool_l.clear();
             pool_pos = 0;
         }
-        if (learned && use_flow) learned->advance(since_train);
+        if (learned && use_flow) {
+            learned->advance(since_train);
+            if (since_train > 0 && since_train % refit_every == 0) {
+                const auto tt = clock::now();
+                learned->refresh(live.data(), nl, nd);
+                t_train += since(tt);
+            }
+        }
         // replacement: next pool point above the threshold, else a new batch
         bool replaced = false;
         for (int attempt = 0; attempt < 100000 && !replaced; ++attempt) {
@@ -566,6 +614,10 @@ int nested_sample(int nd, lg_batch_loglike fn, void* user, const lg_nested_optio
             if (pool_pos < pool_l.size()) {
                 std::memcpy(&live[(size_t)imin * nd], &pool_x[pool_pos * nd], nd * sizeof(double));
                 llive[imin] = pool_l[pool_pos];
+                std::pop_heap(order.begin(), order.end(), later);
+                order.back() = {llive[imin], imin};
+                std::push_heap(order.begin(), order.end(), later);
+                lmax = std::max(lmax, llive[imin]);
                 ++pool_pos;
                 replaced = true;
                 break;
@@ -685,11 +737,11 @@ int nested_sample(int nd, lg_batch_loglike fn, void* user, const lg_nested_optio
     // posterior moments in the cube
     const size_t ns = dead_l.size();
     std::vector<double> mean(nd, 0), m2(nd, 0);
-    double wsum = 0, lmax = -HUGE_VAL;
+    double wsum = 0, lbest = -HUGE_VAL;
     for (size_t i = 0; i < ns; ++i) {
         const double w = std::exp(dead_lw[i] - logz);
         wsum += w;
-        lmax = std::max(lmax, dead_l[i]);
+        lbest = std::max(lbest, dead_l[i]);
         for (int a = 0; a < nd; ++a) {
             mean[a] += w * dead_x[i * nd + a];
             m2[a] += w * dead_x[i * nd + a] * dead_x[i * nd + a];
@@ -698,7 +750,7 @@ int nested_sample(int nd, lg_batch_loglike fn, void* user, const lg_nested_optio
     res->logz = logz;
     res->logz_err = std::sqrt(std::max(H, 0.0) / nl);
     res->information = H;
-    res->max_logl = lmax;
+    res->max_logl = lbest;
     res->ncall = ncall;
     res->niter = iter;
     res->nsamples = (long)ns;

@@ -61,6 +61,9 @@ struct Proposal {
     // last train(): a proposal that trains in the background switches to
     // its new state at a fixed count, so that runs are reproducible
     virtual void advance(long since_train) { (void)since_train; }
+    // called every nlive / 10 replacements with the live points: a learned
+    // bound can follow the shrinking constrained region between trainings
+    virtual void refresh(const double* live, int n, int d) { (void)live, (void)n, (void)d; }
     // periodic dimensions: proposals are wrapped into [0, 1) there
     virtual void set_wrap(const int* wrap, int d) { (void)wrap, (void)d; }
     // log volume (unit-cube coordinates) of the region propose() draws from
