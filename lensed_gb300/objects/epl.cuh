@@ -7,6 +7,7 @@ struct lg_data_epl {
     mat22 m;   // rotate, make elliptical, scale by 1/r
     mat22 w;   // rotate back
     float t, f, n;
+    float c[10];  // the recursion's factors -f (2k - T) / (2k + T), k = 1..10, T = 2 - t
 };
 LG_DEV void lg_epl_setup(lg_data_epl* o, float x1, float x2, float r, float t, float q, float pa)
 {
@@ -18,6 +19,11 @@ LG_DEV void lg_epl_setup(lg_data_epl* o, float x1, float x2, float r, float t, f
     o->t = t;
     o->f = (1 - q) / (1 + q);
     o->n = 2 * r * sqrtf(q) / (1 + q);
+    // the same expression the reference evaluates per ray (objects/epl.cl),
+    // once per candidate
+    const float T = 2 - o->t;
+    const float f = o->f;
+    for (int k = 1; k <= 10; ++k) o->c[k - 1] = -f * (2 * k - T) / (2 * k + T);
 }
 LG_DEV void lg_set_epl(lg_data_epl* o, float x1, float x2, float r, float t, float q, float pa)
 {
@@ -37,8 +43,6 @@ template <class V>
 LG_DEV V lg_epl_frame(const lg_data_epl* __restrict__ o, V x)
 {
     typedef LG_SCALAR(V) S;
-    const float T = 2 - o->t;
-    const float f = o->f;
     S r, c, s, c2, s2;
     lg_polar(x, &r, &c, &s, &c2, &s2);  // atan2, sincos(phi), sincos(2 phi)
     const auto R = make_mat22(c2, -s2, s2, c2);
@@ -46,7 +50,7 @@ LG_DEV V lg_epl_frame(const lg_data_epl* __restrict__ o, V x)
     V a = A;
 #pragma unroll
     for (int k = 1; k <= 10; ++k) {
-        A = (-f * (2 * k - T) / (2 * k + T)) * mv22(R, A);
+        A = o->c[k - 1] * mv22(R, A);
         a += A;
     }
     a *= o->n * powf(r, 1 - o->t);
