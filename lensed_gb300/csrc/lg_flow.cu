@@ -28,10 +28,12 @@
 //                  issued without a host synchronisation (later launches of
 //                  a stopped training return at once);
 //   lg_flow_inverse  latent points back to the cube through every layer;
-//   lg_flow_latent / _accept / _compact  proposals: uniform draws in the
-//                  latent ball (counter-based RNG, Box-Muller), the
-//                  rejection test against the calibrated weight bound, the
-//                  unit-cube test and an order-preserving compaction.
+//   lg_flow_latent / _max_part / _accept / _scan / _scatter  proposals:
+//                  uniform draws in the latent ball (counter-based RNG,
+//                  Box-Muller), the weight bound, the rejection test
+//                  against it, the unit-cube test and an order-preserving
+//                  compaction, all in FP32 (GB300's FP64 rate is a small
+//                  fraction of its FP32 rate).
 //
 // Proposals (as nessai, Williams et al. 2021): z uniform in the ball through
 // the farthest live point in latent space, its volume enlarged by `expand`
@@ -954,14 +956,17 @@ __global__ void __launch_bounds__(256, 2)
     if (w == 0) asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" ::"r"(tmem), "r"(tcols));
 }
 
-// Counter-based uniforms in (0, 1): splitmix64 finaliser of (key, counter).
-__device__ __forceinline__ double lg_u01(unsigned long long key, unsigned long long ctr)
+// Counter-based uniforms in (0, 1): splitmix64 finaliser of (key, counter),
+// the top 23 bits as an odd multiple of 2^-24 (exact in FP32).  The
+// proposal kernels stay in FP32: GB300 runs FP64 at a small fraction of
+// the FP32 rate.
+__device__ __forceinline__ float lg_u01(unsigned long long key, unsigned long long ctr)
 {
     unsigned long long z = key + 0x9E3779B97F4A7C15ull * (ctr + 1);
     z = (z ^ (z >> 30)) * 0xBF58476D1CE4E5B9ull;
     z = (z ^ (z >> 27)) * 0x94D049BB133111EBull;
     z ^= z >> 31;
-    return ((double)(z >> 11) + 0.5) * (1.0 / 9007199254740992.0);
+    return (float)((((unsigned)(z >> 41)) << 1) | 1u) * 0x1p-24f;
 }
 
 // M points uniform in the d-ball of radius rad = scale sqrt(rad2[0]): normal
@@ -969,7 +974,7 @@ __device__ __forceinline__ double lg_u01(unsigned long long key, unsigned long l
 // pass instead of being held) scaled by rad u^(1/d).
 __device__ __forceinline__ float2 lg_normal_pair(unsigned long long key, unsigned long long c)
 {
-    const float u1 = (float)lg_u01(key, c), u2 = (float)lg_u01(key, c + 1);
+    const float u1 = lg_u01(key, c), u2 = lg_u01(key, c + 1);
     const float r = sqrtf(-2.0f * logf(u1));
     float sn, cs;
     sincospif(2.0f * u2, &sn, &cs);
@@ -977,19 +982,19 @@ __device__ __forceinline__ float2 lg_normal_pair(unsigned long long key, unsigne
 }
 
 __global__ void __launch_bounds__(256)
-    lg_flow_latent(unsigned long long key, int M, int d, const double* __restrict__ rad2, double rscale,
+    lg_flow_latent(unsigned long long key, int M, int d, const double* __restrict__ rad2, float rscale,
                    float* __restrict__ Z)
 {
     const int i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= M) return;
-    const double rad = rscale * sqrt(rad2[0]);
+    const float rad = rscale * sqrtf((float)rad2[0]);
     const unsigned long long c0 = (unsigned long long)i * (MAX_D + 2);
     float n2 = 0.0f;
     for (int a = 0; a < d; a += 2) {
         const float2 v = lg_normal_pair(key, c0 + a);
         n2 += v.x * v.x + (a + 1 < d ? v.y * v.y : 0.0f);
     }
-    const float scale = (float)(rad * pow(lg_u01(key, c0 + MAX_D), 1.0 / d)) * rsqrtf(n2);
+    const float scale = rad * exp2f(log2f(lg_u01(key, c0 + MAX_D)) / d) * rsqrtf(n2);
     for (int a = 0; a < d; a += 2) {
         const float2 v = lg_normal_pair(key, c0 + a);
         Z[(size_t)i * d + a] = v.x * scale;
@@ -997,34 +1002,54 @@ __global__ void __launch_bounds__(256)
     }
 }
 
+// FP32 maximum of a block's share of v (finite values only), by warp
+// shuffles and one warp; -inf when there are none.
+__device__ __forceinline__ float lg_block_max(const float* __restrict__ v, int lo, int hi, int step)
+{
+    __shared__ float red[32];
+    float m = -INFINITY;
+    for (int i = lo; i < hi; i += step)
+        if (isfinite(v[i])) m = fmaxf(m, v[i]);
+    for (int o = 16; o > 0; o >>= 1) m = fmaxf(m, __shfl_xor_sync(0xffffffffu, m, o));
+    if ((threadIdx.x & 31) == 0) red[threadIdx.x >> 5] = m;
+    __syncthreads();
+    m = -INFINITY;
+    if (threadIdx.x < 32) {
+        m = threadIdx.x < (blockDim.x >> 5) ? red[threadIdx.x] : -INFINITY;
+        for (int o = 16; o > 0; o >>= 1) m = fmaxf(m, __shfl_xor_sync(0xffffffffu, m, o));
+    }
+    return m;  // valid in thread 0
+}
+
 // Maximum of the finite log weights and of a floor (the calibrated bound),
 // in one block: out[0].
 __global__ void __launch_bounds__(1024) lg_flow_max(const float* __restrict__ v, int n, double floor_,
                                                      double* __restrict__ out)
 {
-    __shared__ double red[32];
-    double m = -INFINITY;
-    for (int i = threadIdx.x; i < n; i += blockDim.x)
-        if (isfinite(v[i])) m = fmax(m, (double)v[i]);
-    for (int o = 16; o > 0; o >>= 1) m = fmax(m, __shfl_xor_sync(0xffffffffu, m, o));
-    if ((threadIdx.x & 31) == 0) red[threadIdx.x >> 5] = m;
-    __syncthreads();
-    if (threadIdx.x == 0) {
-        double r = floor_;
-        for (int w = 0; w < (int)(blockDim.x >> 5); ++w) r = fmax(r, red[w]);
-        out[0] = r;
-    }
+    const float m = lg_block_max(v, threadIdx.x, n, blockDim.x);
+    if (threadIdx.x == 0) out[0] = fmax(floor_, (double)m);
 }
 
-// Calibration sums: out[1] = sum exp(v - out[0]) over finite v (one block,
-// fixed order per thread then a fixed tree).
+// The same over many blocks: part[b] = block b's maximum of its contiguous
+// share, then lg_flow_max over the parts (the maximum does not depend on
+// the grouping).
+__global__ void __launch_bounds__(256) lg_flow_max_part(const float* __restrict__ v, int n, int per,
+                                                         float* __restrict__ part)
+{
+    const int lo = blockIdx.x * per, hi = min(n, lo + per);
+    const float m = lg_block_max(v, lo + threadIdx.x, hi, blockDim.x);
+    if (threadIdx.x == 0) part[blockIdx.x] = m;
+}
+
+// Calibration sums: out[1] = sum exp(v - out[0]) over finite v (one block:
+// FP32 terms summed per thread in a fixed order, then an FP64 tree).
 __global__ void __launch_bounds__(1024) lg_flow_expsum(const float* __restrict__ v, int n, double* __restrict__ out)
 {
     __shared__ double red[1024];
-    const double m = out[0];
-    double s = 0.0;
+    const float m = (float)out[0];
+    float s = 0.0f;
     for (int i = threadIdx.x; i < n; i += blockDim.x)
-        if (isfinite(v[i])) s += exp((double)v[i] - m);
+        if (isfinite(v[i])) s += expf(v[i] - m);
     red[threadIdx.x] = s;
     __syncthreads();
     for (int o = blockDim.x / 2; o > 0; o >>= 1) {
@@ -1036,47 +1061,55 @@ __global__ void __launch_bounds__(1024) lg_flow_expsum(const float* __restrict__
 
 // Rejection and cube tests of M proposals: keep draw i with probability
 // exp(ldet_i - lmax) (lmax = bound[0]), then x = mean + sdev u, wrapped into
-// [0, 1) on periodic dimensions, must lie in the unit cube.  flag[i] = 2
-// kept and inside, 1 kept outside, 0 rejected.
+// [0, 1) on periodic dimensions, must lie in the unit cube (FP32; the row
+// stores it in FP64 with |z|^2 last).  flag[i] = 2 kept and inside, 1 kept
+// outside, 0 rejected; bcnt[2 b], bcnt[2 b + 1] = block b's counts of
+// flag 2 and of flag > 0 (blocks of 256).
 __global__ void __launch_bounds__(256)
     lg_flow_accept(unsigned long long key, int M, int d, const float* __restrict__ Z, const float* __restrict__ U,
                    const float* __restrict__ ldet, const double* __restrict__ bound, const float* __restrict__ mean,
                    const float* __restrict__ sdev, const int* __restrict__ wrap, double* __restrict__ X,
-                   int* __restrict__ flag)
+                   int* __restrict__ flag, int* __restrict__ bcnt)
 {
     const int i = blockIdx.x * blockDim.x + threadIdx.x;
-    if (i >= M) return;
-    const float l = ldet[i];
     int f = 0;
-    if (isfinite(l) && !(lg_u01(key, (unsigned long long)i) > exp((double)l - bound[0]))) {
-        f = 2;
-        double z2 = 0.0;
-        for (int a = 0; a < d; ++a) {
-            double x = (double)mean[a] + (double)sdev[a] * (double)U[(size_t)i * d + a];
-            if (wrap[a]) x -= floor(x);  // periodic dimension
-            X[(size_t)i * (d + 1) + a] = x;
-            if (!(x >= 0.0 && x <= 1.0)) f = 1;
-            z2 += (double)Z[(size_t)i * d + a] * Z[(size_t)i * d + a];
+    if (i < M) {
+        const float l = ldet[i];
+        if (isfinite(l) && !(lg_u01(key, (unsigned long long)i) > expf(l - (float)bound[0]))) {
+            f = 2;
+            float z2 = 0.0f;
+            for (int a = 0; a < d; ++a) {
+                float x = fmaf(sdev[a], U[(size_t)i * d + a], mean[a]);
+                if (wrap[a]) x -= floorf(x);  // periodic dimension
+                X[(size_t)i * (d + 1) + a] = x;
+                if (!(x >= 0.0f && x <= 1.0f)) f = 1;
+                const float zz = Z[(size_t)i * d + a];
+                z2 = fmaf(zz, zz, z2);
+            }
+            X[(size_t)i * (d + 1) + d] = z2;  // latent radius^2, for later radius updates
         }
-        X[(size_t)i * (d + 1) + d] = z2;  // latent radius^2, for later radius updates
+        flag[i] = f;
     }
-    flag[i] = f;
+    const int n2 = __syncthreads_count(f == 2), nk = __syncthreads_count(f > 0);
+    if (threadIdx.x == 0) {
+        bcnt[2 * blockIdx.x] = n2;
+        bcnt[2 * blockIdx.x + 1] = nk;
+    }
 }
 
-// Order-preserving compaction (one block): the first `room` draws with
-// flag 2 (rows of d values) go to out in draw order; cnt[0] = how many were
-// written, cnt[1] = how many passed the weight test.
+// Exclusive offsets of the blocks' kept-and-inside counts (one block, in
+// block order): boff[b]; cnt[0] = min(total, room), cnt[1] = draws that
+// passed the weight test.
 __global__ void __launch_bounds__(1024)
-    lg_flow_compact(const int* __restrict__ flag, int M, const double* __restrict__ X, int d, int room,
-                    double* __restrict__ out, int* __restrict__ cnt)
+    lg_flow_scan(const int* __restrict__ bcnt, int nb, int room, int* __restrict__ boff, int* __restrict__ cnt)
 {
     __shared__ int part[1024], kept[1024];
     const int T = blockDim.x, t = threadIdx.x;
-    const int per = (M + T - 1) / T, lo = t * per, hi = min(M, lo + per);
+    const int per = (nb + T - 1) / T, lo = t * per, hi = min(nb, lo + per);
     int c = 0, k = 0;
-    for (int i = lo; i < hi; ++i) {
-        c += flag[i] == 2;
-        k += flag[i] > 0;
+    for (int b = lo; b < hi; ++b) {
+        c += bcnt[2 * b];
+        k += bcnt[2 * b + 1];
     }
     part[t] = c;
     kept[t] = k;
@@ -1094,11 +1127,30 @@ __global__ void __launch_bounds__(1024)
     }
     __syncthreads();
     int pos = part[t];
-    for (int i = lo; i < hi && pos < room; ++i)
-        if (flag[i] == 2) {
-            for (int a = 0; a < d; ++a) out[(size_t)pos * d + a] = X[(size_t)i * d + a];
-            ++pos;
-        }
+    for (int b = lo; b < hi; ++b) {
+        boff[b] = pos;
+        pos += bcnt[2 * b];
+    }
+}
+
+// Scatter of the kept-and-inside rows (w values each) to out in draw
+// order: one block per accept block, ranks within the block by warp
+// ballots; rows past `room` are dropped.
+__global__ void __launch_bounds__(256)
+    lg_flow_scatter(const int* __restrict__ flag, int M, const double* __restrict__ X, int w, int room,
+                    const int* __restrict__ boff, double* __restrict__ out)
+{
+    __shared__ int wsum[8];
+    const int i = blockIdx.x * blockDim.x + threadIdx.x, lane = threadIdx.x & 31, wp = threadIdx.x >> 5;
+    const bool keep = i < M && flag[i] == 2;
+    const unsigned bal = __ballot_sync(0xffffffffu, keep);
+    if (lane == 0) wsum[wp] = __popc(bal);
+    __syncthreads();
+    int base = boff[blockIdx.x];
+    for (int j = 0; j < wp; ++j) base += wsum[j];
+    const int pos = base + __popc(bal & ((1u << lane) - 1u));
+    if (keep && pos < room)
+        for (int a = 0; a < w; ++a) out[(size_t)pos * w + a] = X[(size_t)i * w + a];
 }
 
 template <typename T>
@@ -1345,8 +1397,8 @@ public:
     long step0 = 0;
     // calibration and proposal work buffers (separate: they run on
     // different streams)
-    DevBuf<float> cz, cu, cld, dz, du, dld;
-    DevBuf<int> dflag, dcnt;
+    DevBuf<float> cz, cu, cld, dz, du, dld, dpart;
+    DevBuf<int> dflag, dcnt, dbcnt, dboff;
     DevBuf<double> dX, dout, dbound;
     // Proposals come from a pool of kept draws of the active flow, refilled
     // by one batch of latent draws at a time on the proposal stream; the
@@ -1607,16 +1659,19 @@ public:
     // Enqueue one refill of the pool from slot k: latent draws enough for
     // about four batches of kept draws (at most 2^20), the inverse flow, the
     // weight test against the bound (a weight above it raises the bound),
-    // the cube test and an order-preserving compaction, and the copies of
-    // the counts, the bound and the kept draws back to the host.
+    // the cube test and an order-preserving compaction (block counts, one
+    // scan, a scatter), and the copies of the counts, the bound and the
+    // kept draws back to the host.
     bool enqueue_refill(int k, int d, int B, uint64_t key)
     {
         const double kf = std::max(kept_frac[k], kMinKept);
         const int M = (int)std::max(4.0 * B, std::min((double)(1 << 20), 4.0 * B / kf));
         const int room = 8 * B, w = d + 1;  // rows: the point, then its latent radius^2
+        const int nb = (M + 255) / 256, per = 4096, np = (M + per - 1) / per;
         if (!dz.ensure((size_t)M * d) || !du.ensure((size_t)M * d) || !dld.ensure(M) || !dX.ensure((size_t)M * w) ||
             !dflag.ensure(M) || !dout.ensure((size_t)room * w) || !dcnt.ensure(2) || !dbound.ensure(1) ||
-            !hbound.ensure(1) || !hcnt.ensure(3) || !hout.ensure((size_t)room * w))
+            !hbound.ensure(1) || !hcnt.ensure(3) || !hout.ensure((size_t)room * w) || !dbcnt.ensure(2 * (size_t)nb) ||
+            !dboff.ensure(nb) || !dpart.ensure(np))
             return false;
         if ((int)wrap.size() != d) set_wrap(nullptr, d);
         Rng r(key);
@@ -1625,10 +1680,12 @@ public:
         // (z uniform in the ball), normalised by the calibrated bound
         lg_flow_latent<<<(M + 255) / 256, 256, 0, ps>>>(k_lat, M, d, dres[k].p, rexp(d), dz.p);
         if (!flow.inverse(Puse[k].p, dpack[k].p, dz.p, M, du.p, dld.p, ps, dtcerr.p + 1)) return false;
-        lg_flow_max<<<1, 1024, 0, ps>>>(dld.p, M, wnorm[k], dbound.p);
-        lg_flow_accept<<<(M + 255) / 256, 256, 0, ps>>>(k_acc, M, d, dz.p, du.p, dld.p, dbound.p, dmean[k].p,
-                                                         dsdev[k].p, dwrap.p, dX.p, dflag.p);
-        lg_flow_compact<<<1, 1024, 0, ps>>>(dflag.p, M, dX.p, w, room, dout.p, dcnt.p);
+        lg_flow_max_part<<<np, 256, 0, ps>>>(dld.p, M, per, dpart.p);
+        lg_flow_max<<<1, 256, 0, ps>>>(dpart.p, np, wnorm[k], dbound.p);
+        lg_flow_accept<<<nb, 256, 0, ps>>>(k_acc, M, d, dz.p, du.p, dld.p, dbound.p, dmean[k].p, dsdev[k].p, dwrap.p,
+                                           dX.p, dflag.p, dbcnt.p);
+        lg_flow_scan<<<1, 1024, 0, ps>>>(dbcnt.p, nb, room, dboff.p, dcnt.p);
+        lg_flow_scatter<<<nb, 256, 0, ps>>>(dflag.p, M, dX.p, w, room, dboff.p, dout.p);
         if (cudaMemcpyAsync(hcnt.p, dcnt.p, 2 * sizeof(int), cudaMemcpyDeviceToHost, ps) ||
             cudaMemcpyAsync(hcnt.p + 2, dtcerr.p + 1, sizeof(int), cudaMemcpyDeviceToHost, ps) ||
             cudaMemcpyAsync(hbound.p, dbound.p, sizeof(double), cudaMemcpyDeviceToHost, ps) ||

@@ -27,78 +27,90 @@ namespace {
 
 constexpr int kMaxDim = 64;
 
-// uniform in (0, 1) from (key, counter): splitmix64 finaliser
-__device__ __forceinline__ double lg_prop_u01(unsigned long long key, unsigned long long ctr)
+// uniform in (0, 1) from (key, counter): splitmix64 finaliser, the top 23
+// bits as an odd multiple of 2^-24 (exact in FP32)
+__device__ __forceinline__ float lg_prop_u01(unsigned long long key, unsigned long long ctr)
 {
     unsigned long long z = key + 0x9E3779B97F4A7C15ull * (ctr + 1);
     z = (z ^ (z >> 30)) * 0xBF58476D1CE4E5B9ull;
     z = (z ^ (z >> 27)) * 0x94D049BB133111EBull;
     z ^= z >> 31;
-    return ((double)(z >> 11) + 0.5) * (1.0 / 9007199254740992.0);
+    return (float)((((unsigned)(z >> 41)) << 1) | 1u) * 0x1p-24f;
 }
 
-// M candidates: ellipsoid k chosen by volume (cum: cumulative volume
-// fractions), a uniform point in it, the multiple-cover rejection, wrapping
-// and the cube test.  E holds per ellipsoid its centre (d), lower Cholesky
-// factor (d x d, row-major) and scale (the bound is (x-mu)^T C^-1 (x-mu) <=
-// scale).  flag[i] = 1 when draw i is kept.
+// Per ellipsoid in the FP32 table F (stride 2 d^2 + 2): its lower Cholesky
+// factor L and L^-1 (d x d each, row-major), sqrt(scale) and scale (the
+// bound is |L^-1 (x - mu)|^2 <= scale).  Centres stay in FP64 (mu, d per
+// ellipsoid); dmu[k][j] = mu_k - mu_j in FP32.
+struct EllTable {
+    int d, nell;
+    const double* mu;
+    const float* F;
+    const float* dmu;
+    const float* cum;  // cumulative volume fractions
+    __device__ int stride() const { return 2 * d * d + 2; }
+};
+
+// M candidates: ellipsoid k chosen by volume, a uniform point in it
+// (offset from its centre in FP32, the centre added in FP64), the
+// multiple-cover rejection, wrapping and the cube test.  GB300 runs FP64
+// at a small fraction of the FP32 rate, so only the final additions and
+// the cube test are FP64.  flag[i] = 1 when draw i is kept.
 __global__ void __launch_bounds__(128)
-    lg_ell_draw(unsigned long long key, int M, int d, int nell, const double* __restrict__ E,
-                const double* __restrict__ cum, const int* __restrict__ wrap, double* __restrict__ X,
+    lg_ell_draw(unsigned long long key, int M, EllTable T, const int* __restrict__ wrap, double* __restrict__ X,
                 int* __restrict__ flag)
 {
     const int i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= M) return;
-    const size_t stride = (size_t)d + (size_t)d * d + 1;
+    const int d = T.d, nell = T.nell;
     const unsigned long long c0 = (unsigned long long)i * (kMaxDim + 4);
-    const double t = lg_prop_u01(key, c0) * cum[nell - 1];
+    const float t = lg_prop_u01(key, c0) * T.cum[nell - 1];
     int k = 0;
-    while (k + 1 < nell && cum[k] < t) ++k;
-    const double* mu = E + k * stride;
-    const double* L = mu + d;
-    const double scale = L[(size_t)d * d];
-    double z[kMaxDim], x[kMaxDim];
-    double n2 = 0.0;
+    while (k + 1 < nell && T.cum[k] < t) ++k;
+    const float* Fk = T.F + (size_t)k * T.stride();
+    float z[kMaxDim], off[kMaxDim];
+    float n2 = 0.0f;
     for (int a = 0; a < d; a += 2) {
-        const double u1 = lg_prop_u01(key, c0 + 1 + a), u2 = lg_prop_u01(key, c0 + 2 + a);
-        const double r = sqrt(-2.0 * log(u1));
-        double s, c;
-        sincospi(2.0 * u2, &s, &c);
-        z[a] = r * c;
+        const float u1 = lg_prop_u01(key, c0 + 1 + a), u2 = lg_prop_u01(key, c0 + 2 + a);
+        const float r = sqrtf(-2.0f * logf(u1));
+        float sn, cs;
+        sincospif(2.0f * u2, &sn, &cs);
+        z[a] = r * cs;
         n2 += z[a] * z[a];
         if (a + 1 < d) {
-            z[a + 1] = r * s;
+            z[a + 1] = r * sn;
             n2 += z[a + 1] * z[a + 1];
         }
     }
-    const double rad = sqrt(scale) * pow(lg_prop_u01(key, c0 + kMaxDim + 1), 1.0 / d) / sqrt(n2);
+    const float rad = Fk[2 * d * d] * exp2f(log2f(lg_prop_u01(key, c0 + kMaxDim + 1)) / d) * rsqrtf(n2);
     for (int a = 0; a < d; ++a) {
-        double s = 0.0;
-        for (int b = 0; b <= a; ++b) s += L[(size_t)a * d + b] * z[b];
-        x[a] = mu[a] + rad * s;
+        float s = 0.0f;
+        for (int b = 0; b <= a; ++b) s += Fk[a * d + b] * z[b];
+        off[a] = rad * s;
     }
     int keep = 1;
     if (nell > 1) {
         // uniform in the union: keep with probability 1 / (ellipsoids holding x)
         int inside = 0;
         for (int j = 0; j < nell; ++j) {
-            const double* mj = E + j * stride;
-            const double* Lj = mj + d;
-            double m = 0.0;
-            for (int a = 0; a < d; ++a) {  // forward substitution L y = x - mu
-                double s = x[a] - mj[a];
-                for (int b = 0; b < a; ++b) s -= Lj[(size_t)a * d + b] * z[b];
-                z[a] = s / Lj[(size_t)a * d + a];
-                m += z[a] * z[a];
+            const float* Fj = T.F + (size_t)j * T.stride();
+            const float* dm = T.dmu + ((size_t)k * nell + j) * d;
+            float m = 0.0f;
+            for (int a = 0; a < d; ++a) {  // L_j^-1 (x - mu_j), x - mu_j = off + mu_k - mu_j
+                float s = 0.0f;
+                for (int b = 0; b <= a; ++b) s += Fj[d * d + a * d + b] * (off[b] + dm[b]);
+                m += s * s;
             }
-            inside += m <= Lj[(size_t)d * d];
+            inside += m <= Fj[2 * d * d + 1];
         }
-        if (inside > 1 && lg_prop_u01(key, c0 + kMaxDim + 2) * inside >= 1.0) keep = 0;
+        if (inside > 1 && lg_prop_u01(key, c0 + kMaxDim + 2) * inside >= 1.0f) keep = 0;
     }
+    const double* mu = T.mu + (size_t)k * d;
     for (int a = 0; a < d; ++a) {
-        if (wrap && wrap[a]) x[a] -= floor(x[a]);
-        if (!(x[a] >= 0.0 && x[a] <= 1.0)) keep = 0;
-        X[(size_t)i * d + a] = x[a];
+        double x = mu[a] + (double)off[a];
+        if (wrap && wrap[a]) x -= floor(x);
+        if (!(x >= 0.0 && x <= 1.0)) keep = 0;
+        X[(size_t)i * d + a] = x;
     }
     flag[i] = keep;
 }
@@ -159,8 +171,9 @@ class GpuEllipsoidDrawer : public EllipsoidDrawer {
 public:
     int device = 0;
     cudaStream_t s = nullptr;
-    Buf<double> dE, dcum, dX, dout, hE, hout;
-    Buf<int> dwrap, dflag, dcnt, hcnt;
+    Buf<double> dmu, dX, dout, hmu, hout;
+    Buf<float> dF, hF;
+    Buf<int> dflag, dcnt, hcnt;
     double accept = 0.5;  // running estimate of the kept fraction
 
     ~GpuEllipsoidDrawer()
@@ -177,32 +190,60 @@ public:
         if (d < 1 || d > kMaxDim || nell < 1 || B < 1) return -1;
         cudaSetDevice(device);
         if (!s && cudaStreamCreateWithFlags(&s, cudaStreamNonBlocking) != cudaSuccess) return -1;
-        const size_t stride = (size_t)d + (size_t)d * d + 1;
-        if (!hE.ensure(nell * stride + nell + d, true) || !dE.ensure(nell * stride) || !dcum.ensure(nell) ||
-            !dwrap.ensure(d) || !dcnt.ensure(2) || !hcnt.ensure(2, true) || !dout.ensure((size_t)B * d) ||
-            !hout.ensure((size_t)B * d, true))
+        const size_t stride = (size_t)d + (size_t)d * d + 1;  // packed: mu, L, scale per ellipsoid
+        const size_t fs = 2 * (size_t)d * d + 2, nf = nell * fs + (size_t)nell * nell * d + nell;
+        if (!hmu.ensure((size_t)nell * d, true) || !dmu.ensure((size_t)nell * d) || !hF.ensure(nf + d, true) ||
+            !dF.ensure(nf + d) || !dcnt.ensure(2) || !hcnt.ensure(2, true) ||
+            !dout.ensure((size_t)B * d) || !hout.ensure((size_t)B * d, true))
             return -1;
-        // ellipsoids, cumulative volume fractions and wrap flags: one upload
-        std::memcpy(hE.p, packed, nell * stride * sizeof(double));
+        // FP32 table: L, L^-1, sqrt(scale), scale per ellipsoid; centre
+        // differences; cumulative volume fractions; then the wrap flags
+        float* F = hF.p;
+        float* dm = F + nell * fs;
+        float* cum = dm + (size_t)nell * nell * d;
+        std::vector<double> Li((size_t)d * d);
+        for (int k = 0; k < nell; ++k) {
+            const double* e = packed + k * stride;
+            const double* L = e + d;
+            std::memcpy(hmu.p + (size_t)k * d, e, d * sizeof(double));
+            // L^-1 by forward substitution on the unit vectors
+            std::fill(Li.begin(), Li.end(), 0.0);
+            for (int c = 0; c < d; ++c)
+                for (int a = c; a < d; ++a) {
+                    double v = a == c ? 1.0 : 0.0;
+                    for (int b = c; b < a; ++b) v -= L[(size_t)a * d + b] * Li[(size_t)b * d + c];
+                    Li[(size_t)a * d + c] = v / L[(size_t)a * d + a];
+                }
+            float* Fk = F + k * fs;
+            for (size_t q = 0; q < (size_t)d * d; ++q) {
+                Fk[q] = (float)L[q];
+                Fk[(size_t)d * d + q] = (float)Li[q];
+            }
+            Fk[2 * d * d] = (float)std::sqrt(e[stride - 1]);
+            Fk[2 * d * d + 1] = (float)e[stride - 1];
+        }
+        for (int k = 0; k < nell; ++k)
+            for (int j = 0; j < nell; ++j)
+                for (int a = 0; a < d; ++a)
+                    dm[((size_t)k * nell + j) * d + a] = (float)(packed[k * stride + a] - packed[j * stride + a]);
         double mx = -HUGE_VAL;
         for (int k = 0; k < nell; ++k) mx = std::max(mx, logv[k]);
         double c = 0;
-        for (int k = 0; k < nell; ++k) hE.p[nell * stride + k] = c += std::exp(logv[k] - mx);
-        double* hw = hE.p + nell * stride + nell;
-        for (int a = 0; a < d; ++a) hw[a] = wrap && wrap[a] ? 1.0 : 0.0;
-        std::vector<int> iw(d);
-        for (int a = 0; a < d; ++a) iw[a] = hw[a] != 0.0;
-        if (cudaMemcpyAsync(dE.p, hE.p, nell * stride * sizeof(double), cudaMemcpyHostToDevice, s) ||
-            cudaMemcpyAsync(dcum.p, hE.p + nell * stride, nell * sizeof(double), cudaMemcpyHostToDevice, s) ||
-            cudaMemcpyAsync(dwrap.p, iw.data(), d * sizeof(int), cudaMemcpyHostToDevice, s))
+        for (int k = 0; k < nell; ++k) cum[k] = (float)(c += std::exp(logv[k] - mx));
+        int* hw = reinterpret_cast<int*>(hF.p + nf);
+        for (int a = 0; a < d; ++a) hw[a] = wrap && wrap[a] ? 1 : 0;
+        if (cudaMemcpyAsync(dmu.p, hmu.p, (size_t)nell * d * sizeof(double), cudaMemcpyHostToDevice, s) ||
+            cudaMemcpyAsync(dF.p, hF.p, (nf + d) * sizeof(float), cudaMemcpyHostToDevice, s))
             return -1;
+        EllTable T{d, nell, dmu.p, dF.p, dF.p + nell * fs, dF.p + nell * fs + (size_t)nell * nell * d};
+        const int* dw = reinterpret_cast<const int*>(dF.p + nf);
         int got = 0;
         for (int round = 0; round < 16 && got < B; ++round) {
             const int need = B - got;
             const int M = (int)std::min<double>(1 << 20, std::max(2.0 * need, 1.3 * need / std::max(accept, 1e-4)));
             if (!dX.ensure((size_t)M * d) || !dflag.ensure(M)) return -1;
-            lg_ell_draw<<<(M + 127) / 128, 128, 0, s>>>(seed + 0x632BE59BD9B4E019ull * (uint64_t)round, M, d, nell,
-                                                         dE.p, dcum.p, dwrap.p, dX.p, dflag.p);
+            lg_ell_draw<<<(M + 127) / 128, 128, 0, s>>>(seed + 0x632BE59BD9B4E019ull * (uint64_t)round, M, T, dw, dX.p,
+                                                         dflag.p);
             lg_ell_compact<<<1, 1024, 0, s>>>(dflag.p, M, dX.p, d, need, dout.p + (size_t)got * d, dcnt.p);
             // the counts and the room for this round's points in one wait
             if (cudaMemcpyAsync(hcnt.p, dcnt.p, 2 * sizeof(int), cudaMemcpyDeviceToHost, s) ||
