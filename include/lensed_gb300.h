@@ -377,7 +377,7 @@ typedef struct {
     double lr;      /* Adam learning rate (default 1e-3) */
     double expand;  /* volume enlargement of the latent ball through the farthest live point
                        (default 1.25, as the plain sampler's 1 / efr) */
-    int patience;   /* epochs without held-out improvement before a retraining stops (default 6) */
+    int patience;   /* epochs without held-out improvement before a retraining stops (default 4) */
     int lag;        /* replacements after a retraining starts at which the new flow takes over
                        (default 800): the retraining runs on its own stream meanwhile, and the
                        sampler waits for it there if it has not finished */

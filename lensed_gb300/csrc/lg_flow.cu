@@ -1878,7 +1878,7 @@ lg_flow_options lg_flow_defaults(void)
     o.batch = 256;
     o.lr = 1e-3;
     o.expand = 1.25;
-    o.patience = 6;
+    o.patience = 4;
     o.lag = 800;
     o.draw_cost = 0.005;
     return o;
