@@ -372,7 +372,8 @@ typedef struct {
     int layers;     /* coupling layers (default 8) */
     int width;      /* hidden units (default 128) */
     int hidden;     /* hidden layers per conditioner (default 2) */
-    int epochs;     /* training epochs per retraining (default 200) */
+    int epochs;     /* epochs of the first training (default 200); later retrainings start from the
+                       previous weights with an eighth of them */
     int batch;      /* training batch (default 256) */
     double lr;      /* Adam learning rate (default 1e-3) */
     double expand;  /* volume enlargement of the latent ball through the farthest live point
