@@ -16,7 +16,7 @@
 // off to check gradients against the CPU restatement).
 //
 // Kernels (all the flow's work for one step is one launch):
-//   lg_flow_step   a block takes FR rows of a minibatch through every
+//   lg_flow_step   a block takes FR (FP32: FR32) rows of a minibatch through every
 //                  coupling layer and back: forward, loss, backward, and the
 //                  block's partial weight gradients (its rows' sums) into
 //                  its own slice of a partial-gradient buffer;
@@ -68,7 +68,8 @@ namespace lg {
 namespace {
 
 constexpr int FT = 256;        // threads per block of the fused kernels
-constexpr int FR = 8;          // minibatch rows per training block
+constexpr int FR = 16;         // minibatch rows per training block (BF16 activations)
+constexpr int FR32 = 8;        // the same with FP32 activations (twice the shared memory per row)
 constexpr int FRI = 32;        // rows per inverse block
 constexpr int MAX_W = 128;     // conditioner width limit (shared-memory tiles)
 constexpr int MAX_D = 64;      // dimension limit
@@ -1215,7 +1216,8 @@ public:
         return n;
     }
 
-    int step_smem() const { return StepSmem(f, FR, bf16 ? 2 : 4).total; }
+    int rows() const { return bf16 ? FR : FR32; }  // minibatch rows per training block
+    int step_smem() const { return StepSmem(f, rows(), bf16 ? 2 : 4).total; }
     int inverse_smem() const { return InvSmem(f, FRI, bf16 ? 2 : 4).total; }
 
     bool init(int dim, int layers, int width, int hidden, uint64_t seed)
@@ -1254,7 +1256,7 @@ public:
             cudaFuncSetAttribute(lg_flow_inverse<FRI, __nv_bfloat16>, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                  sm_inv);
         } else {
-            cudaFuncSetAttribute(lg_flow_step<FR, float>, cudaFuncAttributeMaxDynamicSharedMemorySize, sm_step);
+            cudaFuncSetAttribute(lg_flow_step<FR32, float>, cudaFuncAttributeMaxDynamicSharedMemorySize, sm_step);
             cudaFuncSetAttribute(lg_flow_inverse<FRI, float>, cudaFuncAttributeMaxDynamicSharedMemorySize, sm_inv);
         }
         nparams = count_params(f);
@@ -1289,7 +1291,7 @@ public:
     // buffer is reallocated under enqueued kernels).
     bool reserve(int n, int mb)
     {
-        return loss.ensure(n) && znorm.ensure(n) && gpart.ensure((size_t)((mb + FR - 1) / FR) * nparams);
+        return loss.ensure(n) && znorm.ensure(n) && gpart.ensure((size_t)((mb + rows() - 1) / rows()) * nparams);
     }
 
     // Enqueue one forward (+ backward) pass over rows [row0, row0 + M) of
@@ -1297,7 +1299,7 @@ public:
     // |z|^2 in znorm (when asked), partial gradients in gpart.
     bool pass(const float* X, const int* idx, int row0, int M, bool grad, bool want_z, const int* stop)
     {
-        const int blocks = (M + FR - 1) / FR;
+        const int blocks = (M + rows() - 1) / rows();
         if (!loss.ensure(M) || (want_z && !znorm.ensure(M)) || (grad && !gpart.ensure((size_t)blocks * nparams)))
             return false;
         const int sm = step_smem();
@@ -1306,7 +1308,7 @@ public:
                                                                         want_z ? znorm.p : nullptr, gpart.p,
                                                                         (long)nparams, stop);
         else
-            lg_flow_step<FR, float><<<blocks, FT, sm, stream>>>(f, P.p, X, idx, row0, M, grad, loss.p,
+            lg_flow_step<FR32, float><<<blocks, FT, sm, stream>>>(f, P.p, X, idx, row0, M, grad, loss.p,
                                                                 want_z ? znorm.p : nullptr, gpart.p, (long)nparams,
                                                                 stop);
         return cudaGetLastError() == cudaSuccess;
@@ -1315,7 +1317,7 @@ public:
     // Sum of the partial gradients into G and (adam) an Adam step.
     bool update(int M, bool adam, float lr, const int* stop)
     {
-        const int blocks = (M + FR - 1) / FR;
+        const int blocks = (M + rows() - 1) / rows();
         float c1 = 1, c2 = 1;
         if (adam) {
             ++step;
@@ -1753,13 +1755,13 @@ public:
                 hlive.p[(size_t)i * d + a] = (float)((live[(size_t)i * d + a] - hmean[k][a]) / hsdev[k][a]);
         if (cudaMemcpyAsync(dlive.p, hlive.p, (size_t)n * d * sizeof(float), cudaMemcpyHostToDevice, ps)) return;
         // the live points' latent radii through the active weights
-        const int blocks = (n + FR - 1) / FR, sm = flow.step_smem();
+        const int blocks = (n + flow.rows() - 1) / flow.rows(), sm = flow.step_smem();
         if (flow.bf16)
             lg_flow_step<FR, __nv_bfloat16><<<blocks, FT, sm, ps>>>(flow.f, Puse[k].p, dlive.p, nullptr, 0, n, 0,
                                                                     dtl.p, dtz.p, nullptr, (long)flow.nparams,
                                                                     nullptr);
         else
-            lg_flow_step<FR, float><<<blocks, FT, sm, ps>>>(flow.f, Puse[k].p, dlive.p, nullptr, 0, n, 0, dtl.p,
+            lg_flow_step<FR32, float><<<blocks, FT, sm, ps>>>(flow.f, Puse[k].p, dlive.p, nullptr, 0, n, 0, dtl.p,
                                                             dtz.p, nullptr, (long)flow.nparams, nullptr);
         lg_flow_max<<<1, 1024, 0, ps>>>(dtz.p, n, -INFINITY, dtrack.p);
         // the weight bound of that ball, calibrated as at training
