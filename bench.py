@@ -114,13 +114,22 @@ def run_sampler(args):
                                          "flow_proposals": x["n_flow_proposals"]} for sd, x in zip(seeds, runs)},
                      "mean_ncall": float(np.mean([x["ncall"] for x in runs])),
                      "mean_wall_s": float(np.mean([x["wall_s"] for x in runs])),
-                     "mean_logz": float(np.mean([x["logz"] for x in runs]))}
+                     "mean_logz": float(np.mean([x["logz"] for x in runs])),
+                     # standard error of the mean ln Z from the seeds' spread
+                     "mean_logz_se": float(np.std([x["logz"] for x in runs], ddof=1) / np.sqrt(len(runs)))
+                     if len(runs) > 1 else float(r["logz_err"])}
     line = {"metric": "calls & wall-time to lnZ (learned vs plain sampler)", "unit": "calls, s",
             "value": out["flow"]["mean_ncall"], "higher_is_better": False, "n_gpus": 1, "dtype": "f32 (f64 evidence)",
             "data": "synthetic", "config": {"workload": s.name, "nlive": 1000, "batch": 1024, "tol": 0.1,
                                             "flow": flow},
             "plain": out.get("plain"), "flow": out["flow"], "plain_multi_ellipsoid": out.get("plain_multi"),
-            "dlogz": out["flow"]["logz"] - out["plain"]["logz"] if "plain" in out else None,
+            # mean ln Z of the learned runs minus that of the plain runs, and
+            # its standard error (a single run's ln Z scatters by about its
+            # quoted error, 0.23 here, so single-seed differences say little)
+            "dlogz": out["flow"]["mean_logz"] - out["plain"]["mean_logz"] if "plain" in out else None,
+            "dlogz_se": float(np.hypot(out["flow"]["mean_logz_se"], out["plain"]["mean_logz_se"]))
+            if "plain" in out else None,
+            "seeds": seeds,
             # largest difference of the learned and plain posterior means, in
             # posterior standard deviations (free parameters)
             "max_mean_shift_in_std": max(
