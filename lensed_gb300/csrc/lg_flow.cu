@@ -1543,7 +1543,10 @@ public:
             cudaMemcpyAsync(dsdev[pslot].p, hx.p + (size_t)n * d + d, d * 4, cudaMemcpyHostToDevice, s) ||
             cudaMemcpyAsync(didx.p, hidx.p, nidx * sizeof(int), cudaMemcpyHostToDevice, s) ||
             cudaMemcpyAsync(state.p, hinit.p, nst * sizeof(float), cudaMemcpyHostToDevice, s) ||
-            cudaMemsetAsync(dstop.p, 0, sizeof(int), s) || cudaMemsetAsync(dtcerr.p, 0, 2 * sizeof(int), s) ||
+            cudaMemsetAsync(dstop.p, 0, sizeof(int), s) ||
+            // timeout flags: [0] this stream's calibration, [1] the proposal
+            // stream's inverses (cleared there when a flow takes over)
+            cudaMemsetAsync(dtcerr.p, 0, (ntrain == 1 ? 2 : 1) * sizeof(int), s) ||
             cudaEventRecord(started, s))
             return fail_cuda();
         // the whole retraining is enqueued at once: the held-out check stops
@@ -1619,6 +1622,9 @@ public:
         act = usable[k] ? k : -1;
         ++gen[k];
         kept_frac[k] = efficiency[k];
+        // the proposal stream's timeout flag starts clear for the new flow
+        // (after the work already queued there)
+        if (ps) cudaMemsetAsync(dtcerr.p + 1, 0, sizeof(int), ps);
         if (std::getenv("LG_FLOW_DEBUG"))
             std::fprintf(stderr,
                          "flow: train %ld epochs %d, held-out loss %.4f, latent radius %.3f, calibrated efficiency "
