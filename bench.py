@@ -363,7 +363,8 @@ def main():
     ap.add_argument("--flow-width", type=int, default=128)
     ap.add_argument("--flow-epochs", type=int, default=200)
     ap.add_argument("--skip-plain", action="store_true")
-    ap.add_argument("--sampler-seeds", type=int, default=3, help="sampler workload: runs (seeds) per sampler")
+    ap.add_argument("--sampler-seeds", type=int, default=8,
+                    help="sampler workload: runs (seeds) per sampler (one run's ln Z scatters by about 0.2)")
     ap.add_argument("--max-ellipsoids", type=int, default=8,
                     help="sampler workload: also run the plain sampler with this many bounding ellipsoids (1: skip)")
     ap.add_argument("--no-autotune", action="store_true",
@@ -456,13 +457,25 @@ def main():
         ctx1 = lg.Context(s.image, s.weight, s.objects, psf=s.psf, rule=s.rule, device=local, max_batch=1,
                           flags=args.flags | (0 if args.no_autotune else lg.LG_FLAG_AUTOTUNE))
         plain_shape = ctx1.launch_shape
+        # through the C ABI as a C caller makes it (lg_eval_batch, B = 1),
+        # the argument pointers prepared once
+        import ctypes as C
+
+        rows = [np.ascontiguousarray(hp[i:i + 1]) for i in range(min(B, 64))]
+        ptrs = [r.ctypes.data_as(C.POINTER(C.c_double)) for r in rows]
+        one = np.zeros(1)
+        pone = one.ctypes.data_as(C.POINTER(C.c_double))
+        call = lg.lib().lg_eval_batch
         for i in range(20):
-            ctx1.eval_batch(hp[i % B: i % B + 1])
-        n1 = 400
+            if call(ctx1.h, ptrs[i % len(ptrs)], 1, pone):
+                raise SystemExit("plain evaluation failed")
+        n1 = 1000
         t0 = time.perf_counter()
         for i in range(n1):
-            ctx1.eval_batch(hp[i % B: i % B + 1])
+            call(ctx1.h, ptrs[i % len(ptrs)], 1, pone)
         plain = n1 / (time.perf_counter() - t0)
+        if not np.isfinite(one[0]):
+            raise SystemExit("non-finite plain logL")
         ctx1.close()
 
     # roofline of the dominant kernel
