@@ -329,6 +329,8 @@ struct SamplerState {
     int nd = 0, nl = 0, batch = 0;
     long iter = 0, ncall = 0, since_train = 0, n_flow = 0, n_ell = 0, n_flow_fail = 0;
     double logz = -HUGE_VAL, H = 0, logx = 0;
+    double plat_level = HUGE_VAL;  // logL of the plateau being removed
+    long plat_j = 0;               // its points removed so far
     uint64_t rng[4] = {0, 0, 0, 0};
     std::vector<double> live, llive, dead_x, dead_l, dead_lw, pool_x, pool_l;
     uint64_t pool_pos = 0;
@@ -339,7 +341,7 @@ struct SamplerState {
 
 namespace {
 
-const char kStateMagic[8] = {'L', 'G', 'N', 'S', 'T', 'A', 'T', '2'};
+const char kStateMagic[8] = {'L', 'G', 'N', 'S', 'T', 'A', 'T', '3'};
 
 template <class T>
 bool put(FILE* f, const T& v)
@@ -373,7 +375,8 @@ bool save_state(const char* path, const SamplerState& s)
     if (!f) return false;
     bool ok = std::fwrite(kStateMagic, 1, 8, f) == 8 && put(f, s.nd) && put(f, s.nl) && put(f, s.batch) &&
               put(f, s.iter) && put(f, s.ncall) && put(f, s.since_train) && put(f, s.n_flow) && put(f, s.n_ell) &&
-              put(f, s.n_flow_fail) && put(f, s.logz) && put(f, s.H) && put(f, s.logx);
+              put(f, s.n_flow_fail) && put(f, s.logz) && put(f, s.H) && put(f, s.logx) && put(f, s.plat_level) &&
+              put(f, s.plat_j);
     for (int i = 0; i < 4 && ok; ++i) ok = put(f, s.rng[i]);
     ok = ok && put_vec(f, s.live) && put_vec(f, s.llive) && put_vec(f, s.dead_x) && put_vec(f, s.dead_l) &&
          put_vec(f, s.dead_lw) && put_vec(f, s.pool_x) && put_vec(f, s.pool_l) && put(f, s.pool_pos) &&
@@ -392,7 +395,8 @@ bool load_state(const char* path, int nd, int nl, int batch, SamplerState& s)
     bool ok = std::fread(magic, 1, 8, f) == 8 && std::memcmp(magic, kStateMagic, 8) == 0 && get(f, s.nd) &&
               get(f, s.nl) && get(f, s.batch) && s.nd == nd && s.nl == nl && s.batch == batch && get(f, s.iter) &&
               get(f, s.ncall) && get(f, s.since_train) && get(f, s.n_flow) && get(f, s.n_ell) &&
-              get(f, s.n_flow_fail) && get(f, s.logz) && get(f, s.H) && get(f, s.logx);
+              get(f, s.n_flow_fail) && get(f, s.logz) && get(f, s.H) && get(f, s.logx) && get(f, s.plat_level) &&
+              get(f, s.plat_j);
     for (int i = 0; i < 4 && ok; ++i) ok = get(f, s.rng[i]);
     ok = ok && get_vec(f, s.live) && get_vec(f, s.llive) && get_vec(f, s.dead_x) && get_vec(f, s.dead_l) &&
          get_vec(f, s.dead_lw) && get_vec(f, s.pool_x) && get_vec(f, s.pool_l) && get(f, s.pool_pos) &&
@@ -434,25 +438,46 @@ int nested_sample(int nd, lg_batch_loglike fn, void* user, const lg_nested_optio
     };
     SamplerState st;
     const bool resumed = opt.checkpoint && opt.resume && load_state(opt.checkpoint, nd, nl, B, st);
-    // initial live points: uniform in the cube
-    for (int i0 = 0; !resumed && i0 < nl; i0 += B) {
-        const int n = std::min(B, nl - i0);
+    // initial live points: uniform in the cube where logL > -inf.  Draws
+    // with logL = -inf (or NaN: outside the priors' bounds, say) are
+    // dropped and counted, and the run starts from the prior volume
+    // fraction they leave, ln X0 = ln((nlive - 1) / (draws - 1)) (the
+    // unbiased estimate for draws made until nlive were kept); without such
+    // draws X0 = 1 and the draws are those of a plain start.
+    int have = 0;
+    long ndraw = 0;
+    bool dropped = false;
+    const long max_draws = std::max<long>(100000000L, 1000L * nl);
+    while (!resumed && have < nl) {
+        if (ndraw >= max_draws) {
+            err = "nested sampling: logL is -inf almost everywhere in the prior";
+            return LG_ERR_INPUT;
+        }
+        const int n = dropped ? B : std::min(B, nl - have);
         for (size_t k = 0; k < (size_t)n * nd; ++k) buf[k] = rng.uniform();
         if (int rc = evaluate(buf.data(), n, lbuf.data())) {
             err = "likelihood callback failed";
             return rc;
         }
-        for (int i = 0; i < n; ++i) {
-            std::memcpy(&live[(size_t)(i0 + i) * nd], &buf[(size_t)i * nd], nd * sizeof(double));
-            llive[i0 + i] = std::isnan(lbuf[i]) ? -HUGE_VAL : lbuf[i];
+        for (int i = 0; i < n && have < nl; ++i) {
+            ++ndraw;
+            if (!(lbuf[i] > -HUGE_VAL)) {
+                dropped = true;
+                continue;
+            }
+            std::memcpy(&live[(size_t)have * nd], &buf[(size_t)i * nd], nd * sizeof(double));
+            llive[have++] = lbuf[i];
         }
     }
     // dead points
     std::vector<double> dead_x;
     std::vector<double> dead_l, dead_lw;
-    double logz = -HUGE_VAL, H = 0, logx = 0;
+    double logz = -HUGE_VAL, H = 0;
+    double logx = !resumed && ndraw > nl ? std::log((double)(nl - 1) / (double)(ndraw - 1)) : 0.0;
     const double dlogx = 1.0 / nl;
     const double lw_step = std::log1p(-std::exp(-dlogx));  // log(1 - e^{-1/nl})
+    double plat_level = HUGE_VAL;  // the lowest logL while tied points leave
+    long plat_j = 0;               // tied points removed so far
     // pool of evaluated proposals, used in draw order
     std::vector<double> pool_x;
     std::vector<double> pool_l;
@@ -482,6 +507,8 @@ int nested_sample(int nd, lg_batch_loglike fn, void* user, const lg_nested_optio
         logz = st.logz;
         H = st.H;
         logx = st.logx;
+        plat_level = st.plat_level;
+        plat_j = st.plat_j;
         iter = st.iter;
         ncall = st.ncall;
         since_train = st.since_train;
@@ -524,6 +551,8 @@ int nested_sample(int nd, lg_batch_loglike fn, void* user, const lg_nested_optio
         c.logz = logz;
         c.H = H;
         c.logx = logx;
+        c.plat_level = plat_level;
+        c.plat_j = plat_j;
         for (int i = 0; i < 4; ++i) c.rng[i] = rng.s[i];
         c.live = live;
         c.llive = llive;
@@ -577,12 +606,25 @@ int nested_sample(int nd, lg_batch_loglike fn, void* user, const lg_nested_optio
             break;
         }
         const double lmin = llive[imin];
-        const double lw = logx + lw_step + lmin;
+        // live points tied at the lowest logL (a plateau, e.g. -inf where
+        // the priors' bounds reject a draw): the j-th of them to leave
+        // shrinks ln X by 1 / (nlive - j), as if the j before it had not
+        // been replaced, so that the plateau's share of the volume is
+        // estimated by its share of the live points (Fowlie, Handley & Su
+        // 2021); a lone lowest point shrinks it by the usual 1 / nlive
+        if (lmin == plat_level) {
+            ++plat_j;
+        } else {
+            plat_level = lmin;
+            plat_j = 0;
+        }
+        const double step = plat_j == 0 ? dlogx : 1.0 / (double)std::max<long>(nl - plat_j, 1);
+        const double lw = logx + (plat_j == 0 ? lw_step : std::log1p(-std::exp(-step))) + lmin;
         const double lznew = logaddexp(logz, lw);
         H = (lmin == -HUGE_VAL ? 0 : std::exp(lw - lznew) * lmin) +
             (logz == -HUGE_VAL ? 0 : std::exp(logz - lznew) * (H + logz)) - lznew;
         logz = lznew;
-        logx -= dlogx;
+        logx -= step;
         dead_x.insert(dead_x.end(), &live[(size_t)imin * nd], &live[(size_t)imin * nd] + nd);
         dead_l.push_back(lmin);
         dead_lw.push_back(lw);

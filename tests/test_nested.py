@@ -36,6 +36,31 @@ def test_deterministic_with_seed(native):
     assert a["logz"] == b["logz"] and a["ncall"] == b["ncall"]
 
 
+def test_zero_likelihood_outside_a_box(native):
+    """logL = -inf on 90% of the prior (a box cut, as bound rejection of
+    the priors gives): such draws are dropped from the initial live points
+    and counted out of the starting prior volume; the evidence is that of
+    the Gaussian inside the box (40 seeds: -6.591 +- 0.027 against
+    -6.612)."""
+    d, sigma = 3, 0.05
+    mu = np.array([0.3, 0.5, 0.6])
+    lo, hi = np.array([0.0, 0.0, 0.0]), np.array([1.0, 1.0, 0.1])  # the box: 10% of the cube
+
+    def f(x):
+        inside = np.all((x >= lo + np.array([0, 0, 0.55])) & (x <= hi + np.array([0, 0, 0.55])), axis=1)
+        ll = -0.5 * np.sum(((x - mu) / sigma) ** 2, axis=1)
+        return np.where(inside, ll, -np.inf)
+
+    r = lg.nested_sample(f, d, nlive=200, batch=128, seed=4, tol=0.05)
+    # the box (z in [0.55, 0.65]) holds the Gaussian's z-marginal within +-1 sigma
+    from math import erf, sqrt
+    mass = 0.5 * (erf(0.05 / (sigma * sqrt(2))) - erf(-0.05 / (sigma * sqrt(2))))
+    exact = 0.5 * d * math.log(2 * math.pi * sigma ** 2) + math.log(mass)
+    assert abs(r["logz"] - exact) < 4 * r["logz_err"] + 0.05, (r["logz"], exact, r["logz_err"])
+    b = lg.nested_sample(f, d, nlive=200, batch=128, seed=4, tol=0.05)
+    assert b["logz"] == r["logz"] and b["ncall"] == r["ncall"]
+
+
 def test_invalid_options(native):
     with pytest.raises(lg.LensedError):
         lg.nested_sample(gaussian(np.full(4, 0.5), 0.1), 4, nlive=3)
