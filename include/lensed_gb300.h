@@ -257,6 +257,13 @@ int lg_set_launch_shape(lg_ctx* ctx, const int shape[7]);
 /* The autotuner's candidates and their render and convolution times ("" if
  * the context was not tuned). */
 const char* lg_tune_report(const lg_ctx* ctx);
+/* 1 when batches of up to 4 candidates through the host entry points
+ * (lg_eval_batch, lg_eval_cube_batch, loglike) take their object data and
+ * prior transform from the host (the set module's arithmetic, checked
+ * against it byte for byte on sample candidates at lg_create), 0 when they
+ * use the set_params kernel (models with registered plugins, or a check
+ * that did not match). */
+int lg_host_set_active(const lg_ctx* ctx);
 /* Without a GPU: the candidate shapes the autotuner would time for a model
  * (up to max_shapes x 7 ints written; returns the count), and a compile
  * check of the model's evaluation module for one shape (like

@@ -127,6 +127,7 @@ def lib():
         "lg_launch_shape": (C.c_int, [vp, ip]),
         "lg_set_launch_shape": (C.c_int, [vp, ip]),
         "lg_tune_report": (C.c_char_p, [vp]),
+        "lg_host_set_active": (C.c_int, [vp]),
         "lg_tune_candidates": (C.c_int, [C.POINTER(_ImageDesc), C.POINTER(_ObjectDesc), C.c_int,
                                          C.POINTER(_Options), ip, C.c_int]),
         "lg_compile_check_shape": (C.c_int, [C.POINTER(_ImageDesc), C.POINTER(_ObjectDesc), C.c_int,
@@ -602,6 +603,11 @@ class Context:
     def tune_report(self) -> str:
         """The autotuner's candidates and timings ("" if not tuned)."""
         return lib().lg_tune_report(self.h).decode()
+
+    @property
+    def host_set(self) -> bool:
+        """Batches of up to 4 candidates take their object data from the host."""
+        return bool(lib().lg_host_set_active(self.h))
 
     def to_map_order(self, params_obj):
         """Reorder (..., npars) parameters from object order to map order

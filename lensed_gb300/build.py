@@ -87,7 +87,7 @@ def build(verbose: bool = False, force: bool = False) -> str:
     flags = ["-O2", "-std=c++17", ARCH, "-lineinfo", "-Xcompiler", "-fPIC", "-Xcompiler", "-Wall", "-Xcompiler",
              "-ffp-contract=off"]
     headers = glob.glob(os.path.join(PKG, "csrc", "*.h")) + glob.glob(os.path.join(PKG, "csrc", "*.inc")) + \
-        glob.glob(os.path.join(PKG, "device", "*.cuh")) + [
+        glob.glob(os.path.join(PKG, "device", "*.cuh")) + glob.glob(os.path.join(PKG, "objects", "*.cuh")) + [
         os.path.join(ROOT, "include", "lensed_gb300.h"), os.path.join(BUILD, "lg_embed.inc")]
     objs = []
     jobs = []

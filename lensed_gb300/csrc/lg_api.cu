@@ -31,6 +31,9 @@ namespace lg {
 
 // batches up to this size go through mapped host memory in the host API
 constexpr int kZeroCopyBatch = 64;
+// batches up to this size through the host API take their object data from
+// the host (lg_host_set.cpp) when the context's check passed
+constexpr int kHostSet = 4;
 
 namespace {
 std::mutex g_drv_mu;
@@ -135,6 +138,12 @@ struct lg_ctx {
     int *z_bad = nullptr, *zd_bad = nullptr;
     int last_bad = 0;  // rejection flag of the first point of the last unit-cube call
     std::map<int, cudaGraphExec_t> graphs;
+    // batches of up to kHostSet through the host API: object data computed
+    // on the host and copied in by the replayed graph (no set_params launch)
+    lg::HostSetLayout hset;
+    bool host_set = false;
+    unsigned char* z_models = nullptr;  // pinned, kHostSet x model_bytes
+    std::map<int, cudaGraphExec_t> hgraphs;
 
     int fail(int code, const std::string& msg)
     {
@@ -163,19 +172,24 @@ struct lg_ctx {
     // with logL, the block finishing a candidate's last tile summing its
     // partials).  With ev != NULL, ev[0..4] are recorded before set_params,
     // render, convolve and after the last stage (twice: no separate finish).
-    int enqueue(int B, const double* params, double* logL, cudaStream_t s, cudaEvent_t* ev = nullptr)
+    // set_params for B candidates into d_models: a handful of candidates
+    // get the objects of a candidate side by side (one warp each); else one
+    // thread per candidate
+    int launch_set(int B, const double* params, cudaStream_t s)
+    {
+        void* a_setp[] = {&params, &B, &d_models};
+        const bool split = B <= 32 && nobj > 1 && nobj <= 32;
+        return split ? launch(f_setp_split, dim3(B), dim3(32 * nobj), 0, s, a_setp, "set_params")
+                     : launch(f_setp, dim3((B + 127) / 128), dim3(128), 0, s, a_setp, "set_params");
+    }
+
+    // set = false: the object data are already in d_models
+    int enqueue(int B, const double* params, double* logL, cudaStream_t s, cudaEvent_t* ev = nullptr,
+                bool set = true)
     {
         int rc;
         auto mark = [&](int i) { return ev ? cuda(cudaEventRecord(ev[i], s), "event") : LG_OK; };
-        void* a_setp[] = {&params, &B, &d_models};
-        // a handful of candidates: the objects of a candidate side by side
-        // (one warp each); else one thread per candidate
-        const bool split = B <= 32 && nobj > 1 && nobj <= 32;
-        if ((rc = mark(0)) ||
-            (rc = split ? launch(f_setp_split, dim3(B), dim3(32 * nobj), 0, s, a_setp, "set_params")
-                        : launch(f_setp, dim3((B + 127) / 128), dim3(128), 0, s, a_setp, "set_params")) ||
-            (rc = mark(1)))
-            return rc;
+        if ((rc = mark(0)) || (set && (rc = launch_set(B, params, s))) || (rc = mark(1))) return rc;
         if (psf) {
             void* a_r[] = {&d_models, &d_raw};
             if ((rc = launch(f_rraw, dim3(rtiles, B), dim3(shape.rt), 0, s, a_r, "render")) || (rc = mark(2)))
@@ -200,6 +214,10 @@ struct lg_ctx {
         graphs.clear();
         for (auto& g : cube_graphs) cudaGraphExecDestroy(g.second);
         cube_graphs.clear();
+        for (auto& g : hgraphs) cudaGraphExecDestroy(g.second);
+        hgraphs.clear();
+        cudaFreeHost(z_models);
+        z_models = nullptr;
         cudaFree(d_priors);
         cudaFree(d_cube);
         cudaFree(d_bad);
@@ -669,6 +687,102 @@ int create_impl(lg_ctx* c, const lg_image_desc* img, const lg_object_desc* objs,
     return load_eval(c, c->shape, cubin);
 }
 
+// Host set_params for small batches: the layout of the device's lg_model
+// and, on sample candidates (prior draws, else points inside the bounds),
+// object data identical byte for byte to the set module's; otherwise the
+// context keeps the device path.
+int init_host_set(lg_ctx* c)
+{
+    const lg::Model& m = c->model;
+    c->hset = lg::host_set_layout(m);
+    if (!c->hset.ok || c->hset.bytes != c->model_bytes) return LG_OK;
+    const int K = std::min(lg::kHostSet, c->max_batch);
+    const size_t np = m.pars.size(), mb = c->model_bytes;
+    std::vector<double> P(K * np);
+    for (int k = 0; k < K; ++k)
+        for (size_t i = 0; i < np; ++i) {
+            const lg::ParamInfo& par = m.pars[m.pmap[i]];
+            const double u = 0.2 + 0.6 * std::fmod(0.37 * (double)i + (k + 0.5) / K, 1.0);
+            // without a prior or finite bounds, a value typical of the
+            // parameter's kind
+            double v = 0.5 + 0.5 * u;
+            switch (par.type) {
+            case LG_POSITION_X:
+            case LG_POSITION_Y: v = 10.0 + 20.0 * u; break;
+            case LG_RADIUS: v = 1.0 + 4.0 * u; break;
+            case LG_MAGNITUDE: v = -3.0 + 2.0 * u; break;
+            case LG_AXIS_RATIO: v = 0.5 + 0.4 * u; break;
+            case LG_POS_ANGLE: v = 180.0 * u; break;
+            default: break;
+            }
+            if (par.has_prior)
+                v = par.prior.apply(u);
+            else if (par.bounded && !(v >= par.lower && v <= par.upper) && std::isfinite(par.lower) &&
+                     std::isfinite(par.upper))
+                v = par.lower + u * (par.upper - par.lower);
+            P[k * np + i] = v;
+        }
+    std::vector<unsigned char> host(K * mb), dev(K * mb);
+    for (int k = 0; k < K; ++k) lg::host_set_params(m, c->hset, &P[k * np], &host[k * mb]);
+    int rc;
+    if ((rc = c->cuda(cudaMemcpyAsync(c->d_params, P.data(), K * np * 8, cudaMemcpyHostToDevice, c->stream),
+                      "params upload")) ||
+        (rc = c->launch_set(K, c->d_params, c->stream)) ||
+        (rc = c->cuda(cudaMemcpyAsync(dev.data(), c->d_models, K * mb, cudaMemcpyDeviceToHost, c->stream),
+                      "object data")) ||
+        (rc = c->cuda(cudaStreamSynchronize(c->stream), "set_params check")))
+        return rc;
+    if (std::memcmp(host.data(), dev.data(), K * mb) != 0) return LG_OK;
+    if ((rc = c->cuda(cudaHostAlloc((void**)&c->z_models, lg::kHostSet * mb, cudaHostAllocDefault), "pinned models")))
+        return rc;
+    c->host_set = true;
+    return LG_OK;
+}
+
+// Graph of B candidates whose object data the host has put in z_models:
+// their upload, render, convolution + chi^2, logL into mapped memory.
+int host_graph_for(lg_ctx* c, int B, cudaGraphExec_t* out)
+{
+    auto it = c->hgraphs.find(B);
+    if (it != c->hgraphs.end()) {
+        *out = it->second;
+        return LG_OK;
+    }
+    int rc;
+    cudaGraph_t g;
+    if ((rc = c->cuda(cudaStreamBeginCapture(c->stream, cudaStreamCaptureModeThreadLocal), "begin capture")))
+        return rc;
+    int erc = c->cuda(cudaMemcpyAsync(c->d_models, c->z_models, (size_t)B * c->model_bytes, cudaMemcpyHostToDevice,
+                                      c->stream),
+                      "object data upload");
+    if (!erc) erc = c->enqueue(B, nullptr, c->zd_logL, c->stream, nullptr, false);
+    cudaError_t e = cudaStreamEndCapture(c->stream, &g);
+    if (erc) return erc;
+    if ((rc = c->cuda(e, "end capture"))) return rc;
+    cudaGraphExec_t ge;
+    e = cudaGraphInstantiate(&ge, g, 0);
+    cudaGraphDestroy(g);
+    if ((rc = c->cuda(e, "graph instantiate"))) return rc;
+    c->hgraphs[B] = ge;
+    *out = ge;
+    return LG_OK;
+}
+
+// logL of B <= kHostSet candidates (physical parameters, map order) with
+// the object data from the host.
+int host_set_eval(lg_ctx* c, const double* params, int B, double* logL)
+{
+    const size_t np = c->model.pars.size(), mb = c->model_bytes;
+    for (int b = 0; b < B; ++b) lg::host_set_params(c->model, c->hset, params + (size_t)b * np, c->z_models + b * mb);
+    cudaGraphExec_t ge;
+    int rc;
+    if ((rc = host_graph_for(c, B, &ge)) || (rc = c->cuda(cudaGraphLaunch(ge, c->stream), "graph launch")) ||
+        (rc = c->cuda(cudaStreamSynchronize(c->stream), "evaluate")))
+        return rc;
+    std::memcpy(logL, c->z_logL, (size_t)B * 8);
+    return LG_OK;
+}
+
 // Graph of upload + evaluation + read-back for B candidates, built on first
 // use and replayed afterwards.
 int graph_for(lg_ctx* c, int B, cudaGraphExec_t* out)
@@ -801,6 +915,36 @@ int cube_eval_chunk(lg_ctx* c, const double* cube, int B, double* phys, double* 
 {
     const size_t np = c->model.pars.size(), nd = (size_t)c->model.ndims;
     int rc;
+    if (c->host_set && B <= lg::kHostSet && !(c->flags & LG_FLAG_NO_GRAPH)) {
+        // the prior transform on the host too (the arithmetic of
+        // lg_prior_transform: src/nested.c:42-61)
+        const lg::Model& m = c->model;
+        double* P = c->h_params;
+        int bad[lg::kHostSet];
+        for (int b = 0; b < B; ++b) {
+            bad[b] = 0;
+            for (size_t i = 0; i < np; ++i) {
+                const lg::ParamInfo& par = m.pars[m.pmap[i]];
+                const double u = i < nd ? cube[(size_t)b * nd + i] : 0.5;
+                double v = NAN;
+                if (par.has_prior && par.prior.kind != lg::Prior::NONE)
+                    v = par.prior.apply(u);
+                else
+                    bad[b] = 1;
+                if (par.bounded && (v < par.lower || v > par.upper)) bad[b] = 1;
+                P[(size_t)b * np + i] = v;
+            }
+        }
+        if ((rc = host_set_eval(c, P, B, logL))) return rc;
+        for (int b = 0; b < B; ++b) {
+            if (bad[b]) logL[b] = -HUGE_VAL;
+            if (phys)
+                for (size_t i = 0; i < np; ++i)
+                    phys[(size_t)b * np + i] = (nan_rejected && bad[b]) ? NAN : P[(size_t)b * np + i];
+        }
+        c->last_bad = bad[0];
+        return LG_OK;
+    }
     const bool zero_copy = !(c->flags & LG_FLAG_NO_GRAPH) && B <= lg::kZeroCopyBatch;
     if (nd) std::memcpy(zero_copy ? c->z_cube : c->h_cube, cube, (size_t)B * nd * 8);
     if (c->flags & LG_FLAG_NO_GRAPH) {
@@ -986,6 +1130,7 @@ lg_ctx* lg_create(const lg_image_desc* image, const lg_object_desc* objs, int no
         return nullptr;
     }
     int rc = create_impl(c, image, objs, nobjs, opts);
+    if (!rc) rc = init_host_set(c);
     if (status) *status = rc;
     if (rc) {
         g_create_error = c->err;
@@ -1047,6 +1192,7 @@ int lg_eval_batch(lg_ctx* c, const double* params, int B, double* logL)
                           "logL read")))
             return rc;
     } else {
+        if (c->host_set && B <= lg::kHostSet) return host_set_eval(c, params, B, logL);
         const bool zero_copy = B <= lg::kZeroCopyBatch;
         if (zero_copy) std::memcpy(c->z_params, params, (size_t)B * np * 8);
         cudaGraphExec_t ge;
@@ -1254,6 +1400,8 @@ int lg_set_launch_shape(lg_ctx* c, const int shape[7])
 }
 
 const char* lg_tune_report(const lg_ctx* c) { return c ? c->tune_report.c_str() : ""; }
+
+int lg_host_set_active(const lg_ctx* c) { return c && c->host_set ? 1 : 0; }
 
 // Per-stage device times of one evaluation, the counterpart of the
 // reference's --profile event table (src/nested.c:21-40, src/profile.c).

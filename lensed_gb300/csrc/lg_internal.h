@@ -45,6 +45,7 @@ struct Plugin {
     // evaluation functions are templates over the vector type (float2 or
     // lg_pair2), so the paired ray kernels can call them directly
     bool paired = false;
+    bool builtin = false;  // one of the library's own plugins (host set_params exists for it)
 };
 
 const Plugin* find_plugin(const std::string& name);
@@ -122,6 +123,22 @@ struct Model {
 // normalisation); no device work.
 int build_model(const lg_image_desc* img, const lg_object_desc* objs, int nobjs, const lg_options* opts,
                 Model& m, std::string& err);
+
+// set_params on the host for small batches (lg_host_set.cpp): the built-in
+// plugins' set functions compiled for the host with the same IEEE
+// single-precision arithmetic (no contraction) and the same FP64-evaluated
+// elementary functions as the set module, laid out as the device's
+// lg_model.  ok is false when a plugin has no host code.
+struct HostSetLayout {
+    bool ok = false;
+    size_t bytes = 0;            // sizeof(lg_model)
+    std::vector<size_t> offset;  // per object
+    std::vector<int> index;      // per object: entry of the host plugin table
+};
+HostSetLayout host_set_layout(const Model& m);
+// Object data of one candidate (params: np doubles in map order) into out
+// (L.bytes, zero padding).
+void host_set_params(const Model& m, const HostSetLayout& L, const double* params, unsigned char* out);
 
 // Launch-shape parameters baked into the program.
 struct Shape {

@@ -59,6 +59,7 @@ std::vector<Plugin> builtin_plugins()
         p.pars = pars;
         p.deps = deps;
         p.paired = true;
+        p.builtin = true;
         const char* src = embedded_object(name);
         p.source = src ? src : "";
         v.push_back(p);

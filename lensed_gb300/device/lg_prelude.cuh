@@ -21,8 +21,14 @@
 
 #define LG_INF __int_as_float(0x7f800000)
 
+#ifdef LG_HOST_SET
+// the scalar part below, compiled for the host (small batches' set_params)
+#define LG_DEV static inline
+#define LG_DEV_MEMBER inline
+#else
 #define LG_DEV static __device__ __forceinline__
 #define LG_DEV_MEMBER __device__ __forceinline__
+#endif
 
 LG_DEV float2 operator+(float2 a, float2 b) { return make_float2(a.x + b.x, a.y + b.y); }
 LG_DEV float2 operator-(float2 a, float2 b) { return make_float2(a.x - b.x, a.y - b.y); }
@@ -102,6 +108,7 @@ LG_DEV void lg_deflect(float2& y, float2 a)
     y -= (dot(a, a) < LG_INF) ? a : make_float2(1E10f, 1E10f);
 }
 
+#ifndef LG_HOST_SET
 // ------------------------------------------------------------ ray pairs --
 // The evaluation module of the fast mode traces two rays per thread at once
 // with Blackwell's paired single-precision instructions (add/mul/fma on
@@ -411,8 +418,12 @@ LG_DEV void lg_polar(lg_pair2 x, lg_pair* r, lg_pair* c, lg_pair* s, lg_pair* c2
     *s2 = 2.0f * ss * cc;
 }
 
+#endif  // LG_HOST_SET
+
 // scalar type of a plugin's vector type
 template <class V> struct lg_scalar_of;
 template <> struct lg_scalar_of<float2> { typedef float type; };
+#ifndef LG_HOST_SET
 template <> struct lg_scalar_of<lg_pair2> { typedef lg_pair type; };
+#endif
 #define LG_SCALAR(V) typename lg_scalar_of<V>::type

@@ -14,6 +14,7 @@ extern "C" __global__ void lg_set_params_kernel(const double* __restrict__ param
     float p[LG_NPARS];
     lg_load_params(params + (size_t)b * LG_NPARS, p);
     lg_model m;
+    memset(&m, 0, sizeof m);  // padding included: object data compare byte for byte
     lg_set_params(m, p);
     models[b] = m;
 }
@@ -31,13 +32,14 @@ extern "C" __global__ void lg_set_params_split(const double* __restrict__ params
     const int b = blockIdx.x;
     if (b >= B) return;
     const int w = threadIdx.x / 32, lane = threadIdx.x % 32;
+    static_assert(sizeof(lg_model) % 4 == 0, "object data are 32-bit words");
+    for (int i = threadIdx.x; i < (int)(sizeof(lg_model) / 4); i += blockDim.x) reinterpret_cast<unsigned*>(&m)[i] = 0;
     if (threadIdx.x == 0) lg_load_params(params + (size_t)b * LG_NPARS, p);
     __syncthreads();
     if (lane == 0 && w < LG_NOBJ && lg_obj_phase[w] == 0) lg_set_object(m, p, w);
     __syncthreads();
     if (lane == 0 && w < LG_NOBJ && lg_obj_phase[w] == 1) lg_set_object(m, p, w);
     __syncthreads();
-    static_assert(sizeof(lg_model) % 4 == 0, "object data are 32-bit words");
     const unsigned* src = reinterpret_cast<const unsigned*>(&m);
     unsigned* dst = reinterpret_cast<unsigned*>(models + b);
     for (int i = threadIdx.x; i < (int)(sizeof(lg_model) / 4); i += blockDim.x) dst[i] = src[i];

@@ -338,6 +338,50 @@ def test_image_plane_prior_parity(native):
     assert_image_close(raw, o.render(params)[0], "ipp")
 
 
+def test_host_set_params_match_the_set_module(native):
+    """Batches of up to 4 candidates through the host API take their object
+    data (and, from the unit cube, the prior transform) from the host: the
+    logL of one candidate at a time equals the batched (set_params kernel)
+    logL bit for bit, in fast and strict mode and with image-plane priors
+    (deflected through the lens on the host)."""
+    s = workloads.config2()
+    for flags in (0, lg.LG_FLAG_STRICT_FP):
+        ctx = lg.Context(s.image, s.weight, s.objects, psf=s.psf, rule=s.rule, max_batch=16, flags=flags)
+        assert ctx.host_set
+        cand = ctx.to_map_order(workloads.draw_candidates(s, 16, seed=21))
+        batch = ctx.eval_batch(cand)
+        for B in (1, 2, 3, 4):
+            part = np.concatenate([ctx.eval_batch(cand[i:i + B]) for i in range(0, 16 - 16 % B, B)])
+            assert np.array_equal(part, batch[:len(part)]), (flags, B)
+        cube = np.random.Generator(np.random.PCG64(5)).random((8, ctx.ndims))
+        ll8, ph8 = ctx.eval_cube(cube)
+        for b in range(8):
+            l1, p1 = ctx.loglike(cube[b])
+            assert l1 == ll8[b] and np.array_equal(p1, ph8[b])
+        ctx.close()
+    W = H = 48
+    priors = [{"x": "unif 20 28", "y": "unif 20 28", "r": "unif 5 12", "q": "unif 0.5 0.95", "pa": "unif 0 180"},
+              {"x": "image unif 10 20", "y": "image unif 25 35", "r": "unif 1 3", "mag": "unif -3 0",
+               "n": "unif 1 4", "q": "unif 0.5 1", "pa": "unif 0 180"}]
+    ctx = make_ctx(["sie", "sersic"], W, H, psf=None, rule="sub3", priors=priors, max_batch=8)
+    assert ctx.host_set
+    cube = np.random.Generator(np.random.PCG64(6)).random((8, ctx.ndims))
+    ll8, ph8 = ctx.eval_cube(cube)
+    single = np.array([ctx.eval_cube(cube[b:b + 1])[0][0] for b in range(8)])
+    assert np.array_equal(single, ll8)
+    ctx.close()
+    # every built-in plugin: one candidate at a time against a batch of 8
+    rng = np.random.Generator(np.random.PCG64(7))
+    for plugins, params in PLUGIN_CASES:
+        ctx = make_ctx(plugins, 41, 37, rule="sub3", image=np.full((37, 41), 3.0, np.float32), max_batch=8)
+        assert ctx.host_set, plugins
+        P = np.tile(ctx.to_map_order(np.array(params)), (8, 1)) * (1 + 0.02 * rng.standard_normal((8, len(params))))
+        batch = ctx.eval_batch(P)
+        single = np.array([ctx.eval_batch(P[b:b + 1])[0] for b in range(8)])
+        assert np.array_equal(single, batch), plugins
+        ctx.close()
+
+
 def test_cube_transform_and_reference_callback(native):
     s = workloads.small()
     ctx = lg.Context(s.image, s.weight, s.objects, rule=s.rule, max_batch=16)
