@@ -52,7 +52,7 @@ std::vector<Shape> render_candidates(const Shape& base, bool strict)
 {
     // (threads, pixels per group, quadrature split)
     static const int fast[][3] = {{128, 2, 1}, {256, 2, 1}, {64, 2, 1}, {128, 4, 1}, {128, 2, 2}, {256, 2, 2},
-                                  {128, 2, 4}};
+                                  {128, 2, 4}, {128, 2, 8}};
     static const int scalar[][3] = {{128, 2, 1}, {256, 2, 1}, {64, 2, 1}, {128, 1, 1}, {128, 4, 1}};
     std::vector<Shape> out;
     const int n = strict ? (int)(sizeof scalar / sizeof scalar[0]) : (int)(sizeof fast / sizeof fast[0]);
@@ -107,7 +107,7 @@ std::string check_shape(const Shape& s, bool strict, bool psf, int psfw)
 {
     if (s.rt < 32 || s.rt > 1024 || s.rt % 32) return "render threads must be a multiple of 32 in [32, 1024]";
     if (s.rppt < 1 || s.rppt > 8) return "pixels per thread group must be in [1, 8]";
-    if (s.qs != 1 && s.qs != 2 && s.qs != 4) return "quadrature split must be 1, 2 or 4";
+    if (s.qs != 1 && s.qs != 2 && s.qs != 4 && s.qs != 8) return "quadrature split must be 1, 2, 4 or 8";
     if (strict && s.qs != 1) return "strict mode keeps the quadrature sum in order (split 1)";
     if (!psf) return "";
     if (s.cr != 4 && s.cr != 8 && s.cr != 16) return "convolution outputs per thread must be 4, 8 or 16";

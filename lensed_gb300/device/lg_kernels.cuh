@@ -36,7 +36,7 @@
 #define LG_RG (LG_RT / LG_QS)
 #define LG_RTILE (LG_RG * LG_RPPT)
 #define LG_RTILES ((LG_N + LG_RTILE - 1) / LG_RTILE)
-static_assert(LG_QS == 1 || LG_QS == 2 || LG_QS == 4, "quadrature split of 1, 2 or 4 threads");
+static_assert(LG_QS == 1 || LG_QS == 2 || LG_QS == 4 || LG_QS == 8, "quadrature split of 1, 2, 4 or 8 threads");
 static_assert(LG_RT % 32 == 0, "render block of whole warps");
 
 // ------------------------------------------------------------ reductions --

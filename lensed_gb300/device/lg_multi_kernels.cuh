@@ -23,7 +23,7 @@
 #endif
 #define LG_RG (LG_RT / LG_QS)
 #define LG_RTILE (LG_RG * LG_RPPT)
-static_assert(LG_QS == 1 || LG_QS == 2 || LG_QS == 4, "quadrature split of 1, 2 or 4 threads");
+static_assert(LG_QS == 1 || LG_QS == 2 || LG_QS == 4 || LG_QS == 8, "quadrature split of 1, 2, 4 or 8 threads");
 static_assert(LG_RT % 32 == 0, "render block of whole warps");
 #ifndef LG_CTX
 #define LG_CTX 32

@@ -173,7 +173,7 @@ def test_no_psf_and_missing_priors(native):
         np.allclose(ctx2.eval_batch(ctx2.to_map_order(cand)), got, rtol=1e-5)
 
 
-MULTI_RENDER = [(128, 2, 1), (256, 2, 1), (64, 2, 1), (128, 4, 1), (128, 2, 2), (256, 2, 2), (128, 2, 4)]
+MULTI_RENDER = [(128, 2, 1), (256, 2, 1), (64, 2, 1), (128, 4, 1), (128, 2, 2), (256, 2, 2), (128, 2, 4), (128, 2, 8)]
 MULTI_CONV = [(32, 32, 8), (32, 16, 8), (64, 32, 8), (64, 16, 8), (32, 32, 16), (32, 8, 8)]
 
 

@@ -48,7 +48,7 @@ def test_no_psf_candidates_are_render_only(native):
 
 @pytest.mark.parametrize("bad,flags,psfw", [
     (dict(qs=2), lg.LG_FLAG_STRICT_FP, 11),    # strict mode keeps the quadrature sum in order
-    (dict(qs=3), 0, 11),                        # split of 1, 2 or 4 threads
+    (dict(qs=3), 0, 11),                        # split of 1, 2, 4 or 8 threads
     (dict(rt=100), 0, 11),                      # whole warps
     (dict(rppt=0), 0, 11),
     (dict(cr=8, ctx=36), 0, 11),                # tile width a multiple of cr
