@@ -363,7 +363,7 @@ def main():
     ap.add_argument("--flow-width", type=int, default=128)
     ap.add_argument("--flow-epochs", type=int, default=200)
     ap.add_argument("--skip-plain", action="store_true")
-    ap.add_argument("--sampler-seeds", type=int, default=8,
+    ap.add_argument("--sampler-seeds", type=int, default=16,
                     help="sampler workload: runs (seeds) per sampler (one run's ln Z scatters by about 0.2)")
     ap.add_argument("--max-ellipsoids", type=int, default=8,
                     help="sampler workload: also run the plain sampler with this many bounding ellipsoids (1: skip)")
