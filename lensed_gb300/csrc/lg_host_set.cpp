@@ -41,13 +41,6 @@
 namespace lg {
 namespace hostset {
 
-static inline float __int_as_float(int i)
-{
-    float f;
-    std::memcpy(&f, &i, sizeof f);
-    return f;
-}
-
 #define LG_HOST_SET 1
 #include "../device/lg_prelude.cuh"
 #include "../device/lg_crmath_on.cuh"

@@ -57,7 +57,7 @@ struct EllTable {
 // at a small fraction of the FP32 rate, so only the final additions and
 // the cube test are FP64.  flag[i] = 1 when draw i is kept.
 __global__ void __launch_bounds__(128)
-    lg_ell_draw(unsigned long long key, int M, EllTable T, const int* __restrict__ wrap, double* __restrict__ X,
+    lg_ell_draw(unsigned long long key, int M, EllTable T, const float* __restrict__ wrap, double* __restrict__ X,
                 int* __restrict__ flag)
 {
     const int i = blockIdx.x * blockDim.x + threadIdx.x;
@@ -108,7 +108,7 @@ __global__ void __launch_bounds__(128)
     const double* mu = T.mu + (size_t)k * d;
     for (int a = 0; a < d; ++a) {
         double x = mu[a] + (double)off[a];
-        if (wrap && wrap[a]) x -= floor(x);
+        if (wrap && wrap[a] != 0.0f) x -= floor(x);
         if (!(x >= 0.0 && x <= 1.0)) keep = 0;
         X[(size_t)i * d + a] = x;
     }
@@ -230,13 +230,13 @@ public:
         for (int k = 0; k < nell; ++k) mx = std::max(mx, logv[k]);
         double c = 0;
         for (int k = 0; k < nell; ++k) cum[k] = (float)(c += std::exp(logv[k] - mx));
-        int* hw = reinterpret_cast<int*>(hF.p + nf);
-        for (int a = 0; a < d; ++a) hw[a] = wrap && wrap[a] ? 1 : 0;
+        float* hw = hF.p + nf;  // wrap flags as 0 / 1
+        for (int a = 0; a < d; ++a) hw[a] = wrap && wrap[a] ? 1.0f : 0.0f;
         if (cudaMemcpyAsync(dmu.p, hmu.p, (size_t)nell * d * sizeof(double), cudaMemcpyHostToDevice, s) ||
             cudaMemcpyAsync(dF.p, hF.p, (nf + d) * sizeof(float), cudaMemcpyHostToDevice, s))
             return -1;
         EllTable T{d, nell, dmu.p, dF.p, dF.p + nell * fs, dF.p + nell * fs + (size_t)nell * nell * d};
-        const int* dw = reinterpret_cast<const int*>(dF.p + nf);
+        const float* dw = dF.p + nf;
         int got = 0;
         for (int round = 0; round < 16 && got < B; ++round) {
             const int need = B - got;

@@ -19,7 +19,11 @@
 #define LG_LOG_PI 1.14472988584940017414f
 #define LG_LOG_2PI 1.83787706640934548356f
 
+#ifdef LG_HOST_SET
+#define LG_INF HUGE_VALF
+#else
 #define LG_INF __int_as_float(0x7f800000)
+#endif
 
 #ifdef LG_HOST_SET
 // the scalar part below, compiled for the host (small batches' set_params)
