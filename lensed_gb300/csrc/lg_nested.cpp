@@ -597,8 +597,10 @@ int nested_sample(int nd, lg_batch_loglike fn, void* user, const lg_nested_optio
             break;
         }
         const int imin = order.front().second;
-        // termination: the live points can still add at most X * Lmax
-        if (iter > 0 && logaddexp(logz, logx + lmax) - logz < opt.tol) {
+        // termination: the live points can still add at most X * Lmax; or
+        // they all share one logL (a plateau at the top: nothing above it
+        // to draw, and the rest of the evidence is exactly X * L)
+        if ((iter > 0 && logaddexp(logz, logx + lmax) - logz < opt.tol) || llive[imin] == lmax) {
             if (!checkpoint()) {
                 err = std::string("nested sampling: cannot write the checkpoint ") + opt.checkpoint;
                 return LG_ERR_INPUT;
