@@ -357,6 +357,12 @@ typedef struct {
     int max_ellipsoids;     /* 1: one bounding ellipsoid (default); more: the multi-ellipsoidal
                                decomposition of MultiNest's multi-modal mode (option mmodal,
                                src/input/options.c), up to this many ellipsoids */
+    int ceff;               /* constant efficiency mode (the reference's ceff option, which then
+                               passes efr = acc, src/lensed.c:1247-1248): efr is the target fraction
+                               of ellipsoid proposals accepted, and the bound's volume adapts to it,
+                               below the live points' enclosing volume if need be.  Faster; as in
+                               MultiNest the evidence can come out biased.  0 (default): efr is the
+                               fixed volume enlargement 1 / efr */
 } lg_nested_options;
 
 typedef struct {

@@ -56,7 +56,7 @@ class NestedOptions(C.Structure):
     _fields_ = [("nlive", C.c_int), ("tol", C.c_double), ("efr", C.c_double), ("batch", C.c_int),
                 ("seed", C.c_int), ("maxiter", C.c_long), ("proposal", C.c_int), ("flow_every", C.c_int),
                 ("wrap", C.POINTER(C.c_int)), ("checkpoint", C.c_char_p), ("checkpoint_every", C.c_int),
-                ("resume", C.c_int), ("max_ellipsoids", C.c_int)]
+                ("resume", C.c_int), ("max_ellipsoids", C.c_int), ("ceff", C.c_int)]
 
 
 class NestedResult(C.Structure):

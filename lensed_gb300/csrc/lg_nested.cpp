@@ -331,6 +331,9 @@ struct SamplerState {
     double logz = -HUGE_VAL, H = 0, logx = 0;
     double plat_level = HUGE_VAL;  // logL of the plateau being removed
     long plat_j = 0;               // its points removed so far
+    double log_enl = 0;            // constant efficiency mode: log volume enlargement
+    uint64_t pool_used = 0;        // replacements taken from the pool
+    int pool_ell = 0;              // the pool came from the ellipsoidal bound
     uint64_t rng[4] = {0, 0, 0, 0};
     std::vector<double> live, llive, dead_x, dead_l, dead_lw, pool_x, pool_l;
     uint64_t pool_pos = 0;
@@ -376,7 +379,7 @@ bool save_state(const char* path, const SamplerState& s)
     bool ok = std::fwrite(kStateMagic, 1, 8, f) == 8 && put(f, s.nd) && put(f, s.nl) && put(f, s.batch) &&
               put(f, s.iter) && put(f, s.ncall) && put(f, s.since_train) && put(f, s.n_flow) && put(f, s.n_ell) &&
               put(f, s.n_flow_fail) && put(f, s.logz) && put(f, s.H) && put(f, s.logx) && put(f, s.plat_level) &&
-              put(f, s.plat_j);
+              put(f, s.plat_j) && put(f, s.log_enl) && put(f, s.pool_used) && put(f, s.pool_ell);
     for (int i = 0; i < 4 && ok; ++i) ok = put(f, s.rng[i]);
     ok = ok && put_vec(f, s.live) && put_vec(f, s.llive) && put_vec(f, s.dead_x) && put_vec(f, s.dead_l) &&
          put_vec(f, s.dead_lw) && put_vec(f, s.pool_x) && put_vec(f, s.pool_l) && put(f, s.pool_pos) &&
@@ -396,7 +399,7 @@ bool load_state(const char* path, int nd, int nl, int batch, SamplerState& s)
               get(f, s.nl) && get(f, s.batch) && s.nd == nd && s.nl == nl && s.batch == batch && get(f, s.iter) &&
               get(f, s.ncall) && get(f, s.since_train) && get(f, s.n_flow) && get(f, s.n_ell) &&
               get(f, s.n_flow_fail) && get(f, s.logz) && get(f, s.H) && get(f, s.logx) && get(f, s.plat_level) &&
-              get(f, s.plat_j);
+              get(f, s.plat_j) && get(f, s.log_enl) && get(f, s.pool_used) && get(f, s.pool_ell);
     for (int i = 0; i < 4 && ok; ++i) ok = get(f, s.rng[i]);
     ok = ok && get_vec(f, s.live) && get_vec(f, s.llive) && get_vec(f, s.dead_x) && get_vec(f, s.dead_l) &&
          get_vec(f, s.dead_lw) && get_vec(f, s.pool_x) && get_vec(f, s.pool_l) && get(f, s.pool_pos) &&
@@ -416,7 +419,7 @@ int nested_sample(int nd, lg_batch_loglike fn, void* user, const lg_nested_optio
     const auto t0 = std::chrono::steady_clock::now();
     lg_nested_options opt = lg_nested_defaults();
     if (o) opt = *o;
-    if (nd <= 0 || !fn || !res || opt.nlive < nd + 1 || opt.batch <= 0) {
+    if (nd <= 0 || !fn || !res || opt.nlive < nd + 1 || opt.batch <= 0 || !(opt.efr > 0)) {
         err = "nested sampling: invalid arguments (nlive must exceed the dimension)";
         return LG_ERR_INPUT;
     }
@@ -478,6 +481,11 @@ int nested_sample(int nd, lg_batch_loglike fn, void* user, const lg_nested_optio
     const double lw_step = std::log1p(-std::exp(-dlogx));  // log(1 - e^{-1/nl})
     double plat_level = HUGE_VAL;  // the lowest logL while tied points leave
     long plat_j = 0;               // tied points removed so far
+    // constant efficiency mode: the bound's log volume enlargement, moved
+    // after each fully used ellipsoid batch towards the target acceptance
+    double log_enl = std::log(1.25);
+    uint64_t pool_used = 0;
+    int pool_ell = 0;
     // pool of evaluated proposals, used in draw order
     std::vector<double> pool_x;
     std::vector<double> pool_l;
@@ -509,6 +517,9 @@ int nested_sample(int nd, lg_batch_loglike fn, void* user, const lg_nested_optio
         logx = st.logx;
         plat_level = st.plat_level;
         plat_j = st.plat_j;
+        log_enl = st.log_enl;
+        pool_used = st.pool_used;
+        pool_ell = st.pool_ell;
         iter = st.iter;
         ncall = st.ncall;
         since_train = st.since_train;
@@ -553,6 +564,9 @@ int nested_sample(int nd, lg_batch_loglike fn, void* user, const lg_nested_optio
         c.logx = logx;
         c.plat_level = plat_level;
         c.plat_j = plat_j;
+        c.log_enl = log_enl;
+        c.pool_used = pool_used;
+        c.pool_ell = pool_ell;
         for (int i = 0; i < 4; ++i) c.rng[i] = rng.s[i];
         c.live = live;
         c.llive = llive;
@@ -663,8 +677,16 @@ int nested_sample(int nd, lg_batch_loglike fn, void* user, const lg_nested_optio
                 std::push_heap(order.begin(), order.end(), later);
                 lmax = std::max(lmax, llive[imin]);
                 ++pool_pos;
+                ++pool_used;
                 replaced = true;
                 break;
+            }
+            // constant efficiency mode: the batch just used up accepted a
+            // fraction acc of its proposals; move the enlargement halfway
+            // (in log) towards the target efr, within [0.1, 10]
+            if (opt.ceff && pool_ell && !pool_l.empty()) {
+                const double acc = std::max((double)pool_used, 0.5) / (double)pool_l.size();
+                log_enl = std::min(std::log(10.0), std::max(std::log(0.1), log_enl + 0.5 * std::log(acc / opt.efr)));
             }
             // propose a batch: the learned proposal when it is trained, the
             // ellipsoid when it is not or when it yields nothing
@@ -678,7 +700,9 @@ int nested_sample(int nd, lg_batch_loglike fn, void* user, const lg_nested_optio
             double bound_logv;
             if (multi) {
                 if (bound.ell.empty() || iter - bound_iter >= refit_every) {
-                    if (!bound.fit(others, nl - 1, nd, 1.0 / opt.efr, logx, depth)) {
+                    // (constant efficiency mode lifts the floor of X on the volume)
+                    if (!bound.fit(others, nl - 1, nd, opt.ceff ? std::exp(log_enl) : 1.0 / opt.efr,
+                                   opt.ceff ? -HUGE_VAL : logx, depth)) {
                         err = "nested sampling: degenerate live points";
                         return LG_ERR_INPUT;
                     }
@@ -686,7 +710,7 @@ int nested_sample(int nd, lg_batch_loglike fn, void* user, const lg_nested_optio
                 }
                 bound_logv = bound.logv_sum;
             } else {
-                if (!ell.fit(others, nl - 1, nd, 1.0 / opt.efr)) {
+                if (!ell.fit(others, nl - 1, nd, opt.ceff ? std::exp(log_enl) : 1.0 / opt.efr)) {
                     err = "nested sampling: degenerate live points";
                     return LG_ERR_INPUT;
                 }
@@ -700,6 +724,7 @@ int nested_sample(int nd, lg_batch_loglike fn, void* user, const lg_nested_optio
                 if (n > 0) n_flow += n;
                 else n = 0, ++n_flow_fail;
             }
+            const int from_ell = n == 0;
             if (n == 0 && drawer) {
                 // the ellipsoids' draws on the GPU
                 std::vector<double> packed, logv;
@@ -755,6 +780,8 @@ int nested_sample(int nd, lg_batch_loglike fn, void* user, const lg_nested_optio
             }
             pool_x.assign(buf.begin(), buf.begin() + (size_t)n * nd);
             pool_l.assign(lbuf.begin(), lbuf.begin() + n);
+            pool_used = 0;
+            pool_ell = from_ell;
             for (auto& v : pool_l)
                 if (std::isnan(v)) v = -HUGE_VAL;
             pool_pos = 0;
@@ -838,6 +865,7 @@ lg_nested_options lg_nested_defaults(void)
     o.checkpoint_every = 0;
     o.resume = 0;
     o.max_ellipsoids = 1;
+    o.ceff = 0;
     return o;
 }
 

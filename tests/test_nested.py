@@ -140,6 +140,24 @@ def test_plateaus_of_a_stepped_likelihood(native, tmp_path):
     assert rest["logz"] == full["logz"] and rest["ncall"] == full["ncall"] and rest["niter"] == full["niter"]
 
 
+def test_constant_efficiency_mode(native, tmp_path):
+    """ceff = 1 (the reference's ceff option): the bound's volume follows
+    the target acceptance efr -- about 1 / efr likelihood calls per
+    replacement -- and a resumed run continues exactly (the enlargement is
+    in the state)."""
+    d, sigma = 5, 0.05
+    f = gaussian(np.full(d, 0.45), sigma)
+    exact = 0.5 * d * math.log(2 * math.pi * sigma ** 2)
+    common = dict(nlive=300, batch=256, seed=2, tol=0.05, ceff=1, efr=0.3)
+    r = lg.nested_sample(f, d, **common)
+    assert 2.5 < r["ncall"] / r["niter"] < 4.5, r["ncall"] / r["niter"]
+    assert abs(r["logz"] - exact) < 4 * r["logz_err"] + 0.1, (r["logz"], exact)
+    path = str(tmp_path / "state.bin")
+    lg.nested_sample(f, d, maxiter=1500, checkpoint=path, **common)
+    rest = lg.nested_sample(f, d, checkpoint=path, resume=1, **common)
+    assert rest["logz"] == r["logz"] and rest["ncall"] == r["ncall"]
+
+
 def test_multi_ellipsoid_bound_on_two_modes(native):
     """Two well separated modes (d = 4): the multi-ellipsoidal bound (MultiNest's
     multi-modal mode) finds the evidence with far fewer likelihood calls than
