@@ -452,7 +452,7 @@ def main():
     # plain mode: one candidate per call with a host sync (the reference
     # flow, e.g. MultiNest's callback), on a context created for it
     # (max_batch = 1; its launch shape tuned for one candidate)
-    plain, plain_shape = None, None
+    plain, plain_shape, plain_loglike = None, None, None
     if rank == 0:
         ctx1 = lg.Context(s.image, s.weight, s.objects, psf=s.psf, rule=s.rule, device=local, max_batch=1,
                           flags=args.flags | (0 if args.no_autotune else lg.LG_FLAG_AUTOTUNE))
@@ -476,6 +476,24 @@ def main():
         plain = n1 / (time.perf_counter() - t0)
         if not np.isfinite(one[0]):
             raise SystemExit("non-finite plain logL")
+        # the reference-signature callback loglike(cube, ndim, npar, lnew,
+        # ctx) (src/nested.h:3): unit cube in, physical values written back
+        cb = lg.lib().loglike
+        cb.restype = None
+        cb.argtypes = [C.POINTER(C.c_double), C.POINTER(C.c_int), C.POINTER(C.c_int), C.POINTER(C.c_double),
+                       C.c_void_p]
+        nd, npar, lnew = C.c_int(ctx1.ndims), C.c_int(ctx1.npars), C.c_double()
+        cubes = np.random.Generator(np.random.PCG64(3)).random((64, ctx1.npars))
+        work = np.empty(ctx1.npars)
+        pw = work.ctypes.data_as(C.POINTER(C.c_double))
+        for i in range(20):
+            work[:] = cubes[i % 64]
+            cb(pw, C.byref(nd), C.byref(npar), C.byref(lnew), ctx1.h)
+        t0 = time.perf_counter()
+        for i in range(n1):
+            work[:] = cubes[i % 64]
+            cb(pw, C.byref(nd), C.byref(npar), C.byref(lnew), ctx1.h)
+        plain_loglike = n1 / (time.perf_counter() - t0)
         ctx1.close()
 
     # roofline of the dominant kernel
@@ -515,7 +533,8 @@ def main():
             "vs_baseline": None, "dtype": "f32 (f64 chi^2 reduction)", "data": "synthetic",
             "config": config, "gpu_launches": 3 * args.steps,
             "e2e": {"value": e2e, "unit": UNIT, "h2d_bytes_per_step": int(hp.nbytes), "d2h_bytes_per_step": 8 * B},
-            "plain_evals_per_s": plain, "plain_launch_shape": plain_shape, "roofline": roof}
+            "plain_evals_per_s": plain, "plain_loglike_callback_per_s": plain_loglike,
+            "plain_launch_shape": plain_shape, "roofline": roof}
     if clk:
         line["clocks"] = clk
     if rank == 0 and world == 1 and not args.no_cpu_baseline:
