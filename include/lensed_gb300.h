@@ -295,8 +295,12 @@ int lg_measure_fp32_peak(int device, double* tflops);
  * allocations are not allowed).  It allocates nothing: its scratch is a
  * static device array of LG_NOALLOC_MAX_PARTIALS doubles shared by all calls,
  * so calls that overlap on the GPU race and must be serialised by the caller.
- * The first call on a device looks up the array's device address; make that
- * first call before any stream capture.  B is limited to 65535; larger B, null
+ * The first call in a CUDA context (per device, and again after
+ * cudaDeviceReset) looks up the array's device address; with CUDA's lazy
+ * module loading that first call also loads the library's kernels and places
+ * the array, a one-time allocation made by the driver.  A caller that may
+ * not allocate at all makes one call at its own set-up time, before any
+ * stream capture; later calls allocate nothing.  B is limited to 65535; larger B, null
  * pointers or non-positive sizes return LG_ERR_INPUT (message in
  * lg_last_error(NULL)). */
 int lg_loglike_images_noalloc(const float* d_image, const float* d_weight, const float* d_models, long n_pixels,
@@ -353,7 +357,10 @@ typedef struct {
     const char* checkpoint; /* state file or NULL: the counterpart of MultiNest's resume files
                                (option resume, src/input/options.c:217-221) */
     int checkpoint_every;   /* write the state every this many iterations (0: only when stopping) */
-    int resume;             /* continue from the state file when it exists and matches */
+    int resume;             /* continue from the state file when it exists; an existing file that is
+                               not a state of this run (another format version, truncated, another
+                               dimension, nlive or batch) is an error (LG_ERR_INPUT), not a fresh
+                               start */
     int max_ellipsoids;     /* 1: one bounding ellipsoid (default); more: the multi-ellipsoidal
                                decomposition of MultiNest's multi-modal mode (option mmodal,
                                src/input/options.c), up to this many ellipsoids */

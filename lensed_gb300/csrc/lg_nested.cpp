@@ -344,7 +344,9 @@ struct SamplerState {
 
 namespace {
 
-const char kStateMagic[8] = {'L', 'G', 'N', 'S', 'T', 'A', 'T', '3'};
+// format version in the last byte: bumped whenever the layout changes, so a
+// state of another layout is refused instead of being read misaligned
+const char kStateMagic[8] = {'L', 'G', 'N', 'S', 'T', 'A', 'T', '4'};
 
 template <class T>
 bool put(FILE* f, const T& v)
@@ -388,15 +390,27 @@ bool save_state(const char* path, const SamplerState& s)
     return ok && std::rename(tmp.c_str(), path) == 0;
 }
 
-// Read a state written by save_state; false if absent, unreadable or for
-// another dimension, live-point count or batch size.
-bool load_state(const char* path, int nd, int nl, int batch, SamplerState& s)
+enum class Load { ABSENT, OK, BAD };
+
+// Read a state written by save_state.  ABSENT if there is no file; BAD (with
+// the reason in why) if the file is not a state of this run: another format
+// version, truncated, or for another dimension, live-point count or batch.
+Load load_state(const char* path, int nd, int nl, int batch, SamplerState& s, std::string& why)
 {
     FILE* f = std::fopen(path, "rb");
-    if (!f) return false;
+    if (!f) return Load::ABSENT;
     char magic[8];
-    bool ok = std::fread(magic, 1, 8, f) == 8 && std::memcmp(magic, kStateMagic, 8) == 0 && get(f, s.nd) &&
-              get(f, s.nl) && get(f, s.batch) && s.nd == nd && s.nl == nl && s.batch == batch && get(f, s.iter) &&
+    if (std::fread(magic, 1, 8, f) != 8 || std::memcmp(magic, kStateMagic, 8) != 0) {
+        std::fclose(f);
+        why = "not a sampler state of this format version";
+        return Load::BAD;
+    }
+    if (!get(f, s.nd) || !get(f, s.nl) || !get(f, s.batch) || s.nd != nd || s.nl != nl || s.batch != batch) {
+        std::fclose(f);
+        why = "a state for another dimension, live-point count or batch size";
+        return Load::BAD;
+    }
+    bool ok = get(f, s.iter) &&
               get(f, s.ncall) && get(f, s.since_train) && get(f, s.n_flow) && get(f, s.n_ell) &&
               get(f, s.n_flow_fail) && get(f, s.logz) && get(f, s.H) && get(f, s.logx) && get(f, s.plat_level) &&
               get(f, s.plat_j) && get(f, s.log_enl) && get(f, s.pool_used) && get(f, s.pool_ell);
@@ -408,7 +422,8 @@ bool load_state(const char* path, int nd, int nl, int batch, SamplerState& s)
     ok = ok && s.live.size() == (size_t)nl * nd && s.llive.size() == (size_t)nl &&
          s.dead_x.size() == s.dead_l.size() * nd && s.dead_lw.size() == s.dead_l.size() &&
          s.pool_x.size() == s.pool_l.size() * nd && s.pool_pos <= s.pool_l.size();
-    return ok;
+    if (!ok) why = "truncated or inconsistent state";
+    return ok ? Load::OK : Load::BAD;
 }
 
 }  // namespace
@@ -440,7 +455,16 @@ int nested_sample(int nd, lg_batch_loglike fn, void* user, const lg_nested_optio
         return rc;
     };
     SamplerState st;
-    const bool resumed = opt.checkpoint && opt.resume && load_state(opt.checkpoint, nd, nl, B, st);
+    bool resumed = false;
+    if (opt.checkpoint && opt.resume) {
+        std::string why;
+        const Load ld = load_state(opt.checkpoint, nd, nl, B, st, why);
+        if (ld == Load::BAD) {
+            err = std::string("nested sampling: cannot resume from ") + opt.checkpoint + ": " + why;
+            return LG_ERR_INPUT;
+        }
+        resumed = ld == Load::OK;
+    }
     // initial live points: uniform in the cube where logL > -inf.  Draws
     // with logL = -inf (or NaN: outside the priors' bounds, say) are
     // dropped and counted, and the run starts from the prior volume

@@ -17,7 +17,15 @@
 // streams, or two host threads) race on it and must be serialised by the
 // caller.  Nothing in it needs clearing: every partial a call reads was
 // written earlier in the same call.
+//
+// Set-up: the first call in a CUDA context (per device, and again after
+// cudaDeviceReset) looks up the array's device address.  With CUDA's lazy
+// module loading that lookup is also what loads this file's kernels and
+// places the array on the device -- a one-time allocation made by the
+// driver.  A caller that may not allocate at all makes one call at its own
+// set-up time, before any stream capture; later calls allocate nothing.
 
+#include <cuda.h>
 #include <cuda_runtime.h>
 
 #include <cstdio>
@@ -38,14 +46,57 @@ constexpr int kMaxDevices = 64;
 constexpr long kPixelsPerTile = 2048;
 
 std::mutex g_mu;
-double* g_scratch[kMaxDevices] = {};
 
-// Device address of the scratch array on the current device, looked up once
-// per device (the array's name in host code is only a host-side stand-in).
+// The scratch address, valid in the CUDA context it was looked up in.
+// Contexts are told apart by their driver-assigned unique id (never reused
+// within a process), so a context re-created after cudaDeviceReset gets a
+// fresh lookup instead of a stale address.
+struct Scratch {
+    unsigned long long ctx_id = 0;
+    double* ptr = nullptr;
+};
+Scratch g_scratch[kMaxDevices];
+
+typedef CUresult (*CtxGetCurrentFn)(CUcontext*);
+typedef CUresult (*CtxGetIdFn)(CUcontext, unsigned long long*);
+
+template <class F>
+bool resolve(const char* name, F& f)
+{
+    void* p = nullptr;
+    cudaDriverEntryPointQueryResult q;
+    if (cudaGetDriverEntryPointByVersion(name, &p, 12000, cudaEnableDefault, &q) != cudaSuccess ||
+        q != cudaDriverEntryPointSuccess || !p)
+        return false;
+    f = reinterpret_cast<F>(p);
+    return true;
+}
+
+// Unique id of the current context; 0 if the driver cannot say (the address
+// is then looked up on every call).
+unsigned long long current_context_id()
+{
+    static CtxGetCurrentFn get_current = nullptr;
+    static CtxGetIdFn get_id = nullptr;
+    static bool resolved = false;
+    if (!resolved) {
+        resolved = true;
+        if (!resolve("cuCtxGetCurrent", get_current) || !resolve("cuCtxGetId", get_id)) get_current = nullptr;
+    }
+    CUcontext c = nullptr;
+    unsigned long long id = 0;
+    if (!get_current || get_current(&c) != CUDA_SUCCESS || !c || get_id(c, &id) != CUDA_SUCCESS) return 0;
+    return id;
+}
+
+// Device address of the scratch array in the current context of `device`
+// (the array's name in host code is only a host-side stand-in).
 int scratch_for(int device, double** out)
 {
     std::lock_guard<std::mutex> lk(g_mu);
-    if (!g_scratch[device]) {
+    Scratch& sc = g_scratch[device];
+    const unsigned long long id = current_context_id();
+    if (!sc.ptr || id == 0 || sc.ctx_id != id) {
         void* p = nullptr;
         cudaError_t e = cudaGetSymbolAddress(&p, lg_noalloc_scratch);
         if (e != cudaSuccess) {
@@ -55,9 +106,11 @@ int scratch_for(int device, double** out)
             lg::set_global_error(msg);
             return LG_ERR_CUDA;
         }
-        g_scratch[device] = static_cast<double*>(p);
+        sc.ptr = static_cast<double*>(p);
+        // cudaGetSymbolAddress made the context current if it was not
+        sc.ctx_id = id ? id : current_context_id();
     }
-    *out = g_scratch[device];
+    *out = sc.ptr;
     return LG_OK;
 }
 

@@ -240,13 +240,35 @@ def _box(truth, spans):
     return t - s, t + s
 
 
+# Parameter names of the built-in plugins in their declaration order
+# (objects/<name>.cl `params` blocks).  Kept in Python so that building a
+# workload never loads the native library: the CPU reference arm of the
+# bench must run without it.  tests/test_cabi.py checks this table against
+# the library's plugin registry.
+PLUGIN_PARAM_NAMES = {
+    "sis": ("x", "y", "r"),
+    "sis_plus_shear": ("x", "y", "r", "g1", "g2"),
+    "nsis": ("x", "y", "r", "rc"),
+    "sie": ("x", "y", "r", "q", "pa"),
+    "sie_plus_shear": ("x", "y", "r", "q", "pa", "g1", "g2"),
+    "nsie": ("x", "y", "r", "rc", "q", "pa"),
+    "point_mass": ("x", "y", "r"),
+    "epl": ("x", "y", "r", "t", "q", "pa"),
+    "epl_plus_shear": ("x", "y", "r", "t", "q", "pa", "g1", "g2"),
+    "sersic": ("x", "y", "r", "mag", "n", "q", "pa"),
+    "sersic_old": ("x", "y", "r", "mag", "n", "q", "pa"),
+    "exponential": ("x", "y", "rs", "mag", "q", "pa"),
+    "devauc": ("x", "y", "r", "mag", "q", "pa"),
+    "gauss": ("x", "y", "sigma", "mag", "q", "pa"),
+    "sky": ("bg", "dx", "dy"),
+}
+
+
 def _priors_from_box(plugins, lower, upper, fixed):
     """Per-object dicts of prior strings: 'unif lo hi' or a fixed value."""
     out, k = [], 0
-    from . import plugin_params  # noqa: F401 (names only; no device work)
-
     for pl in plugins:
-        names = [p[0] for p in plugin_params(pl)]
+        names = PLUGIN_PARAM_NAMES[pl]
         d = {}
         for n in names:
             if k in fixed:

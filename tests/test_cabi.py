@@ -50,6 +50,29 @@ def test_plugin_registry_matches_reference_parameter_blocks(native):
     assert epl["q"][1] == 5 and epl["pa"][1] == 6 and epl["x"][1] == 1
 
 
+def test_workload_name_table_matches_registry(native):
+    from lensed_gb300.workloads import PLUGIN_PARAM_NAMES
+
+    assert set(PLUGIN_PARAM_NAMES) == set(PLUGINS)
+    for name, names in PLUGIN_PARAM_NAMES.items():
+        assert [p[0] for p in lg.plugin_params(name)] == list(names), name
+
+
+def test_building_workloads_does_not_load_the_library():
+    """The CPU reference arm of the bench builds its workload with no native
+    code of the package mapped into the process."""
+    import subprocess
+    import sys
+
+    code = ("import sys; sys.path.insert(0, '.'); import lensed_gb300 as lg; from lensed_gb300 import workloads; "
+            "workloads.config2(); workloads.small(); workloads.large(); workloads.systems(); "
+            "maps = open('/proc/self/maps').read(); print('liblensed_gb300' in maps, lg._lib is None)")
+    root = os.path.dirname(os.path.dirname(__file__))
+    out = subprocess.run([sys.executable, "-c", code], cwd=root, capture_output=True, text=True, timeout=600)
+    assert out.returncode == 0, out.stderr
+    assert out.stdout.split() == ["False", "True"], out.stdout
+
+
 def test_library_rules_equal_python_rules(native):
     rules = lg.quad_rules()
     for name, (a, w, e) in rules.items():

@@ -111,10 +111,18 @@ def test_checkpoint_and_resume_continue_exactly(native, tmp_path):
     # a finished state resumes to the same result at once
     again = lg.nested_sample(f, 3, checkpoint=path, resume=1, **common)
     assert again["logz"] == full["logz"] and again["ncall"] == full["ncall"]
-    # a state for another problem size is ignored (a fresh run)
-    other = lg.nested_sample(gaussian(np.full(2, 0.5), 0.1), 2, checkpoint=path, resume=1, nlive=100, batch=64,
-                             seed=5)
-    assert other["niter"] > 0
+    # a state for another problem size, or a file of another format, is an
+    # error rather than a silent fresh start
+    with pytest.raises(lg.LensedError, match="another dimension"):
+        lg.nested_sample(gaussian(np.full(2, 0.5), 0.1), 2, checkpoint=path, resume=1, nlive=100, batch=64, seed=5)
+    with open(path, "r+b") as fh:
+        fh.seek(7)
+        fh.write(b"3")  # the previous format version
+    with pytest.raises(lg.LensedError, match="format version"):
+        lg.nested_sample(f, 3, checkpoint=path, resume=1, **common)
+    # no file at all: a fresh run
+    fresh = lg.nested_sample(f, 3, checkpoint=str(tmp_path / "none.bin"), resume=1, **common)
+    assert fresh["logz"] == full["logz"]
 
 
 def test_plateaus_of_a_stepped_likelihood(native, tmp_path):

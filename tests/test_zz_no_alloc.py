@@ -6,7 +6,9 @@ allowed): it reduces model images the caller already holds, with its scratch
 in a static device array.  Its logL must agree with the context's own
 evaluation of the same parameters (whose model images come from lg_render)
 to within the strict-mode logL tolerance, on two calls in a row (the second
-call reuses the scratch left by the first).
+call reuses the scratch left by the first).  The first call in a process may
+load the library's kernels and place the static array (CUDA's lazy module
+loading); the second must leave the device's free memory unchanged.
 """
 import ctypes as C
 
@@ -34,15 +36,22 @@ def test_noalloc_loglike_matches_eval_batch_twice(native):
     d_img, d_w = _dev(s.image, torch), _dev(s.weight, torch)
     d_models = _dev(models, torch)
     N = s.width * s.height
+    # every output buffer exists before the first call
+    outs = [torch.full((B,), np.nan, dtype=torch.float64, device="cuda") for _ in range(2)]
+    torch.cuda.synchronize()
+    free = []
     for call in range(2):
-        d_logL = torch.full((B,), np.nan, dtype=torch.float64, device="cuda")
+        free.append(torch.cuda.mem_get_info()[0])
         rc = lg.lib().lg_loglike_images_noalloc(C.c_void_p(d_img.data_ptr()), C.c_void_p(d_w.data_ptr()),
                                                 C.c_void_p(d_models.data_ptr()), N, B,
-                                                C.c_void_p(d_logL.data_ptr()), None)
+                                                C.c_void_p(outs[call].data_ptr()), None)
         assert rc == 0, lg.lib().lg_last_error(None)
         torch.cuda.synchronize()
-        got = d_logL.cpu().numpy()
+        free.append(torch.cuda.mem_get_info()[0])
+        got = outs[call].cpu().numpy()
         assert np.all(np.abs(got - want) <= 1e-6), (call, got - want)
+    # the second call allocated nothing on the device
+    assert free[3] == free[2], free
 
 
 def test_noalloc_rejects_oversize_and_null(native):
