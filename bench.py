@@ -8,10 +8,17 @@ Gaussian-plus-wings PSF, 25-point (5x5) pixel quadrature, 10% random mask,
 the whole batch (set_params -> render -> convolve + chi^2 -> logL).
 
 Arms
-  default            the CUDA path.  ``value``: device-resident parameters,
-                     CUDA-event timing of K steps on the launching stream.
-                     ``e2e``: the public C-ABI call ``lg_eval_batch`` with host
-                     parameters and host logL (H2D + D2H inside the timing).
+  default            the CUDA path in the default (exact) floating-point
+                     mode, whose logL equals the FP32 oracle's (elementary
+                     functions correctly rounded, no contraction).  ``value``:
+                     device-resident parameters, CUDA-event timing of K steps
+                     on the launching stream.  ``e2e``: the public C-ABI call
+                     ``lg_eval_batch`` with host parameters and host logL
+                     (H2D + D2H inside the timing).  ``parity``: the first
+                     --parity-n timed candidates against the FP32 oracle on
+                     the host.  ``fast_mode``: the same batch timed with
+                     LG_FLAG_FAST_MATH (hardware-approximate functions, FMA
+                     contraction) and its parity.
   --impl reference   the reference algorithm on the host CPU: the
                      reference's own sources compiled here if that build is
                      present (oracle/_ref), else the C++ restatement (oracle),
@@ -290,6 +297,28 @@ def cpu_oracle(s, threads, precision=32):
                   weight=s.weight, precision=precision, threads=threads, math="libm")
 
 
+def Oracle_for(s, threads):
+    """The FP32 oracle of a workload (correctly rounded elementary
+    functions: the reference's semantics the parity bound is stated for)."""
+    from lensed_gb300 import quadrature
+    from oracle.oracle import Oracle
+
+    return Oracle(s.plugins, s.width, s.height, quadrature.rule(s.rule), psf=s.psf, image=s.image,
+                  weight=s.weight, precision=32, threads=threads)
+
+
+def parity_block(got, want, mode):
+    d = np.abs(np.asarray(got) - np.asarray(want))
+    return {"mode": mode, "n": int(d.size), "max_abs_dlogL": float(d.max()), "median_abs_dlogL": float(np.median(d)),
+            "bound": 1e-3, "within_bound": bool(d.max() <= 1e-3),
+            "abs_logL_range": [float(np.abs(want).min()), float(np.abs(want).max())],
+            "oracle": "FP32 restatement, elementary functions evaluated in double and rounded once"}
+
+
+def mode_name(flags):
+    return "strict" if flags & 1 else ("fast" if flags & 16 else "exact")
+
+
 def ref_impl(s):
     """The reference's own code built for the host (oracle/_ref) if present
     for this workload, else the C++ restatement."""
@@ -357,8 +386,13 @@ def main():
     ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
     ap.add_argument("--workload", default="config2")
     ap.add_argument("--batch", type=int, default=0)
-    ap.add_argument("--no-cpu-baseline", action="store_true")
-    ap.add_argument("--flags", type=int, default=0, help="lg_options.flags (1 strict, 4 IEEE div/sqrt)")
+    ap.add_argument("--no-cpu-baseline", action="store_true",
+                    help="skip the CPU baseline and the oracle parity check of the timed results")
+    ap.add_argument("--flags", type=int, default=0,
+                    help="lg_options.flags: 0 exact (default), 1 strict, 16 fast, 16|4 fast with IEEE div/sqrt")
+    ap.add_argument("--no-fast", action="store_true", help="do not time the fast mode beside the exact one")
+    ap.add_argument("--parity-n", type=int, default=128,
+                    help="timed candidates checked against the FP32 oracle (CPU) for the parity block")
     ap.add_argument("--flow-layers", type=int, default=8)
     ap.add_argument("--flow-width", type=int, default=128)
     ap.add_argument("--flow-epochs", type=int, default=200)
@@ -392,51 +426,68 @@ def main():
     s, B = workload(args.workload)
     if args.batch:
         B = args.batch
-    t_create = time.perf_counter()
-    ctx = lg.Context(s.image, s.weight, s.objects, psf=s.psf, rule=s.rule, device=local, max_batch=B,
-                     flags=args.flags | (0 if args.no_autotune else lg.LG_FLAG_AUTOTUNE))
-    t_create = time.perf_counter() - t_create
-    cand = ctx.to_map_order(workloads.draw_candidates(s, B, seed=replicas.candidate_seed(rank)))
-    d_params = torch.from_numpy(np.ascontiguousarray(cand)).to(f"cuda:{local}")
-    d_logL = torch.empty(B, dtype=torch.float64, device=f"cuda:{local}")
     # a dedicated stream: the context's kernels and the timing events share it
     stream = torch.cuda.Stream(device=f"cuda:{local}")
-    sh = stream.cuda_stream
+    cand_obj = workloads.draw_candidates(s, B, seed=replicas.candidate_seed(rank))
 
-    def step():
-        ctx.eval_batch_device(d_params.data_ptr(), B, d_logL.data_ptr(), sh)
+    def timed(flags, clocks=None):
+        """Create a context in the given floating-point mode and time K steps
+        of the device-resident batch evaluation (CUDA events on the launching
+        stream, barrier and max over ranks)."""
+        t_create = time.perf_counter()
+        ctx = lg.Context(s.image, s.weight, s.objects, psf=s.psf, rule=s.rule, device=local, max_batch=B,
+                         flags=flags | (0 if args.no_autotune else lg.LG_FLAG_AUTOTUNE))
+        t_create = time.perf_counter() - t_create
+        cand = ctx.to_map_order(cand_obj)
+        d_params = torch.from_numpy(np.ascontiguousarray(cand)).to(f"cuda:{local}")
+        d_logL = torch.empty(B, dtype=torch.float64, device=f"cuda:{local}")
+        sh = stream.cuda_stream
 
-    for _ in range(args.warmup):
-        step()
-    torch.cuda.synchronize()
-    if not np.all(np.isfinite(d_logL.cpu().numpy())):
-        raise SystemExit("non-finite logL in warm-up")
-    clocks = Clocks(local)
-    clocks.start()
-    time.sleep(0.3)
-    if dist:
-        dist.barrier()
-    torch.cuda.synchronize()
-    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
-    e0.record(stream)
-    for _ in range(args.steps):
-        step()
-    e1.record(stream)
-    torch.cuda.synchronize()
-    if dist:
-        dist.barrier()
-    ms = e0.elapsed_time(e1)
-    clk = clocks.stop()
-    ms = replicas.max_over_ranks(ms, dist, device=f"cuda:{local}")
-    value = replicas.aggregate(B * args.steps, ms / 1e3, world)
-    logL_gpu = d_logL.cpu().numpy()
+        def step():
+            ctx.eval_batch_device(d_params.data_ptr(), B, d_logL.data_ptr(), sh)
 
-    # per-stage device times (the reference's --profile stages), averaged
-    stage = np.zeros(4)
-    nprof = 5
-    for _ in range(nprof):
-        stage += ctx.profile(d_params.data_ptr(), B, d_logL.data_ptr())
-    stage /= nprof
+        for _ in range(args.warmup):
+            step()
+        torch.cuda.synchronize()
+        if not np.all(np.isfinite(d_logL.cpu().numpy())):
+            raise SystemExit("non-finite logL in warm-up")
+        if clocks:
+            clocks.start()
+            time.sleep(0.3)
+        if dist:
+            dist.barrier()
+        torch.cuda.synchronize()
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e0.record(stream)
+        for _ in range(args.steps):
+            step()
+        e1.record(stream)
+        torch.cuda.synchronize()
+        if dist:
+            dist.barrier()
+        ms = e0.elapsed_time(e1)
+        clk = clocks.stop() if clocks else None
+        ms = replicas.max_over_ranks(ms, dist, device=f"cuda:{local}")
+        value = replicas.aggregate(B * args.steps, ms / 1e3, world)
+        logL = d_logL.cpu().numpy()
+        # per-stage device times (the reference's --profile stages), averaged
+        stage = np.zeros(4)
+        nprof = 5
+        for _ in range(nprof):
+            stage += ctx.profile(d_params.data_ptr(), B, d_logL.data_ptr())
+        stage /= nprof
+        return {"ctx": ctx, "cand": cand, "value": value, "ms": ms, "clocks": clk, "logL": logL, "stage": stage,
+                "t_create": t_create}
+
+    # the headline: the default (exact) mode unless --flags asks otherwise
+    head = timed(args.flags, Clocks(local))
+    ctx, cand, value, ms, clk, logL_gpu, stage, t_create = (head[k] for k in (
+        "ctx", "cand", "value", "ms", "clocks", "logL", "stage", "t_create"))
+    # the fast mode beside it (hardware-approximate functions, FMA contraction)
+    fast = None
+    if args.flags == 0 and not args.no_fast:
+        fast = timed(lg.LG_FLAG_FAST_MATH)
+        fast["ctx"].close()
 
     # end to end through the public C ABI with host buffers
     hp = np.ascontiguousarray(cand)
@@ -496,7 +547,7 @@ def main():
         plain_loglike = n1 / (time.perf_counter() - t0)
         ctx1.close()
 
-    # roofline of the dominant kernel
+    # roofline of the dominant kernel (headline mode)
     N, Q = s.width * s.height, len(lg.quad_rules()[s.rule][1])
     render_flops = B * N * Q * ray_flops(s.plugins)
     conv_flops = 2.0 * B * N * (s.psf.size if s.psf is not None else 0)
@@ -526,6 +577,7 @@ def main():
             "rays_per_s": B * N * Q / (stage[1] * 1e-3)}
 
     config = describe(s, B)
+    config["fp_mode"] = mode_name(args.flags)
     config["launch_shape"] = ctx.launch_shape
     config["autotune"] = (ctx.tune_report.splitlines() or ["off"])[0] + f" (context creation {t_create:.1f} s)"
     line = {"metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
@@ -535,6 +587,12 @@ def main():
             "e2e": {"value": e2e, "unit": UNIT, "h2d_bytes_per_step": int(hp.nbytes), "d2h_bytes_per_step": 8 * B},
             "plain_evals_per_s": plain, "plain_loglike_callback_per_s": plain_loglike,
             "plain_launch_shape": plain_shape, "roofline": roof}
+    if fast is not None:
+        fst = fast["stage"]
+        line["fast_mode"] = {"value": fast["value"], "unit": UNIT, "ms_per_step": fast["ms"] / args.steps,
+                             "flags": "LG_FLAG_FAST_MATH",
+                             "stage_ms": {"set_params": float(fst[0]), "render": float(fst[1]),
+                                          "convolve": float(fst[2]), "finish": float(fst[3])}}
     if clk:
         line["clocks"] = clk
     if rank == 0 and world == 1 and not args.no_cpu_baseline:
@@ -543,6 +601,15 @@ def main():
         v, n, dt = cpu_rate(s, workloads.draw_candidates(s, 8, seed=1), threads, kind=kind, ref=R)
         line["cpu_baseline"] = {"value": v, "unit": UNIT, "cores": threads, "kind": kind,
                                 "sample": f"{n} candidates of the same workload, one at a time, {dt:.1f} s"}
+        # parity of the timed results: the first n of the timed candidates
+        # against the FP32 oracle (the checker; the reference's semantics
+        # with correctly rounded elementary functions)
+        npar = min(B, args.parity_n)
+        o32 = Oracle_for(s, threads)
+        want = o32.loglike(cand_obj[:npar])
+        line["parity"] = parity_block(logL_gpu[:npar], want, mode_name(args.flags))
+        if fast is not None:
+            line["fast_mode"]["parity"] = parity_block(fast["logL"][:npar], want, "fast")
     if rank == 0:
         print(json.dumps(line), flush=True)
     if dist:

@@ -58,11 +58,29 @@ extern "C" {
 #define LG_AXIS_RATIO 5
 #define LG_POS_ANGLE 6
 
-/* context flags */
-#define LG_FLAG_STRICT_FP 1 /* no FMA contraction in the composed program */
-#define LG_FLAG_NO_GRAPH 2  /* launch kernels directly instead of graph replay */
-#define LG_FLAG_IEEE_DIV 4  /* fast mode with IEEE division and square root per ray */
-#define LG_FLAG_AUTOTUNE 8  /* choose the launch shape by timing candidates at creation */
+/* context flags.  The floating-point mode of the per-ray arithmetic:
+ *   default (exact)    IEEE single precision in the reference's operation
+ *                      order, no FMA contraction, every elementary function
+ *                      correctly rounded (its value in double, rounded once):
+ *                      model images and logL identical to the oracle's and to
+ *                      the strict mode's.  Rays are traced in pairs with
+ *                      f32x2 instructions; exp, log, atan and atanh are
+ *                      computed in single-precision double-word arithmetic,
+ *                      the others in double.
+ *   LG_FLAG_STRICT_FP  the same results one ray at a time with every
+ *                      elementary function evaluated in double (the
+ *                      definition the default mode reproduces; slow on
+ *                      GB300's FP64 pipe)
+ *   LG_FLAG_FAST_MATH  ray pairs with FMA contraction and hardware-
+ *                      approximate functions (a few ulp each; what the
+ *                      reference's -cl-fast-relaxed-math build allows):
+ *                      about twice the default's throughput, logL within
+ *                      about 1e-3 + 2e-6 |logL| of the oracle's */
+#define LG_FLAG_STRICT_FP 1  /* strict mode (above) */
+#define LG_FLAG_NO_GRAPH 2   /* launch kernels directly instead of graph replay */
+#define LG_FLAG_IEEE_DIV 4   /* fast mode with IEEE division and square root per ray */
+#define LG_FLAG_AUTOTUNE 8   /* choose the launch shape by timing candidates at creation */
+#define LG_FLAG_FAST_MATH 16 /* fast mode (above) */
 
 typedef struct lg_ctx lg_ctx;
 
@@ -171,7 +189,10 @@ int lg_eval_batch(lg_ctx* ctx, const double* params, int B, double* logL);
 /* Same with device pointers on a caller stream; returns without
  * synchronising.  With stream = NULL the work runs on the context's own
  * (non-blocking) stream, after the work already queued on the legacy
- * default stream; buffers filled on any other stream must be ready first. */
+ * default stream; buffers filled on any other stream must be ready first.
+ * Calls on one context run in call order whatever streams they are made on
+ * (they share the context's scratch): a call on a caller stream first waits
+ * for the context's earlier calls, and later calls wait for it. */
 int lg_eval_batch_device(lg_ctx* ctx, const double* d_params, int B, double* d_logL, void* stream);
 
 /* Unit-cube points (B x ndims, host) -> physical parameters via the priors
@@ -185,8 +206,8 @@ int lg_eval_cube_batch(lg_ctx* ctx, const double* cube, int B, double* phys, dou
  * kernel (one candidate per thread; unif, norm, delta priors; pseudo-prior
  * parameters at u = 0.5), followed by the likelihood kernels.  d_phys
  * (B x npars, map order, may be NULL) receives the physical parameters;
- * points outside the parameter bounds get logL = -inf.  Uses the context's
- * parameter scratch: calls on one context must be ordered. */
+ * points outside the parameter bounds get logL = -inf.  Calls on one
+ * context are ordered as for lg_eval_batch_device. */
 int lg_eval_cube_batch_device(lg_ctx* ctx, const double* d_cube, int B, double* d_phys, double* d_logL, void* stream);
 
 /* Render one parameter vector (map order) for output: the model (convolved
@@ -274,9 +295,19 @@ int lg_compile_check_shape(const lg_image_desc* image, const lg_object_desc* obj
                            const int shape[7], char* log, size_t log_size);
 
 /* Diagnostic: the paired-ray exp (fn = 0), log (1), square root (2),
- * reciprocal (3), atan (4) or atanh (5) of the fast evaluation modules
- * applied to x[0..n) on a device (out[i] = f(x[i])). */
+ * reciprocal (3), atan (4) or atanh (5) of the fast evaluation modules, or
+ * the correctly rounded exp (6), log (7), atan (8) or atanh (9) of the exact
+ * modules, applied to x[0..n) on a device (out[i] = f(x[i])). */
 int lg_probe_pair_math(int device, int fn, const float* x, int n, float* out);
+
+/* Diagnostic: compares the exact modules' correctly rounded exp (fn = 0),
+ * log (1), atan (2) or atanh (3), on ray pairs, with the function evaluated
+ * in double and rounded once, for every float whose bit pattern lies in
+ * [lo, hi) (hi <= 2^32), on a device.  *mismatches receives the number of
+ * inputs whose results differ (NaN matches NaN); the first nfirst of their
+ * bit patterns go to first. */
+int lg_probe_crf_sweep(int device, int fn, unsigned long long lo, unsigned long long hi,
+                       unsigned long long* mismatches, unsigned* first, int nfirst);
 
 /* Measured FP32 FMA throughput (TFLOP/s) of a device, for roofline
  * denominators. */
@@ -406,6 +437,11 @@ typedef struct {
                          128^2 image with a 9-point rule): the flow is used when its volume times
                          1 + draw_cost x latent draws per proposal is below the ellipsoids' volume;
                          0 for expensive likelihoods.  A fixed number, so that runs repeat */
+    int wait_tries;   /* polls of each bounded wait of the tensor-core inverse before it gives up
+                         (0: the default 2^20; negative: none -- every wait gives up at once, which
+                         exercises the timeout path: the kernel flags the error, lets its own copies
+                         and tensor-core work in flight complete, frees its tensor memory and
+                         returns, and the sampler drops that flow) */
 } lg_flow_options;
 
 typedef int (*lg_batch_loglike)(void* user, const double* cube, int B, double* logL);
@@ -436,8 +472,9 @@ int lg_flow_inverse_time(int device, int d, int layers, int width, int hidden, i
 /* One retraining of the learned proposal on n points (n x d, row-major),
  * as the sampler does it on its live points: history receives the held-out
  * loss before training and after each epoch (NaN past the last epoch run);
- * returns the epochs run (negative: error); *efficiency = calibrated kept
- * fraction of latent draws. */
+ * returns the epochs run (negative: error; LG_ERR_TIMEOUT when a bounded
+ * wait of the calibration's tensor-core inverse ran out, see wait_tries);
+ * *efficiency = calibrated kept fraction of latent draws. */
 int lg_flow_fit(int device, int d, const lg_flow_options* opts, const double* pts, int n, float* history,
                 int max_history, double* efficiency);
 /* The sampler's GPU draws uniform in a union of nell ellipsoids (and the

@@ -32,6 +32,7 @@ LG_FLAG_STRICT_FP = 1
 LG_FLAG_NO_GRAPH = 2
 LG_FLAG_IEEE_DIV = 4
 LG_FLAG_AUTOTUNE = 8
+LG_FLAG_FAST_MATH = 16
 SHAPE_FIELDS = ("rt", "rppt", "qs", "ctx", "cty", "cr", "pair_rows")
 DUMP_LAYERS = ("IMG", "RES", "RAW", "ERR", "WHT", "PVL")
 
@@ -72,7 +73,7 @@ class NestedResult(C.Structure):
 class FlowOptions(C.Structure):
     _fields_ = [("layers", C.c_int), ("width", C.c_int), ("hidden", C.c_int), ("epochs", C.c_int),
                 ("batch", C.c_int), ("lr", C.c_double), ("expand", C.c_double), ("patience", C.c_int),
-                ("lag", C.c_int), ("draw_cost", C.c_double)]
+                ("lag", C.c_int), ("draw_cost", C.c_double), ("wait_tries", C.c_int)]
 
 
 BATCH_LOGLIKE = C.CFUNCTYPE(C.c_int, C.c_void_p, C.POINTER(C.c_double), C.c_int, C.POINTER(C.c_double))
@@ -137,6 +138,8 @@ def lib():
         "lg_systems_tune_report": (C.c_char_p, [vp]),
         "lg_measure_fp32_peak": (C.c_int, [C.c_int, dp]),
         "lg_probe_pair_math": (C.c_int, [C.c_int, C.c_int, fp, C.c_int, fp]),
+        "lg_probe_crf_sweep": (C.c_int, [C.c_int, C.c_int, C.c_ulonglong, C.c_ulonglong,
+                                         C.POINTER(C.c_ulonglong), C.POINTER(C.c_uint), C.c_int]),
         "lg_loglike_images_noalloc": (C.c_int, [vp, vp, vp, C.c_long, C.c_int, vp, vp]),
         "lg_systems_create": (vp, [C.POINTER(_ImageDesc), C.c_int, C.POINTER(_ObjectDesc), C.c_int,
                                    C.POINTER(_Options), ip, ip]),

@@ -44,6 +44,13 @@ def write_embed() -> str:
     setk = open(os.path.join(PKG, "device", "lg_set_kernel.cuh")).read()
     crmath = open(os.path.join(PKG, "device", "lg_crmath_on.cuh")).read()
     multi = open(os.path.join(PKG, "device", "lg_multi_kernels.cuh")).read()
+    # the correctly rounded functions with their tables inlined (NVRTC has no
+    # include path to this tree)
+    inc = '#ifndef LG_CRF_TABLES_INLINE\n#include "lg_crf_tables.cuh"\n#endif\n'
+    crf = open(os.path.join(PKG, "device", "lg_crfloat.cuh")).read()
+    assert inc in crf
+    crf = crf.replace(inc, open(os.path.join(PKG, "device", "lg_crf_tables.cuh")).read())
+    exact = open(os.path.join(PKG, "device", "lg_exact_pair.cuh")).read()
     objs = sorted(glob.glob(os.path.join(PKG, "objects", "*.cuh")))
     lines = ["// generated by lensed_gb300/build.py: device sources for NVRTC", ""]
     lines.append(f"static const char LG_EMBED_PRELUDE[] = {_raw(prelude)};")
@@ -51,6 +58,8 @@ def write_embed() -> str:
     lines.append(f"static const char LG_EMBED_SET_KERNEL[] = {_raw(setk)};")
     lines.append(f"static const char LG_EMBED_CRMATH[] = {_raw(crmath)};")
     lines.append(f"static const char LG_EMBED_MULTI[] = {_raw(multi)};")
+    lines.append(f"static const char LG_EMBED_CRF[] = {_raw(crf)};")
+    lines.append(f"static const char LG_EMBED_EXACT_PAIR[] = {_raw(exact)};")
     lines.append("struct lg_embedded_object { const char* name; const char* text; };")
     lines.append("static const lg_embedded_object LG_EMBED_OBJECTS[] = {")
     for p in objs:

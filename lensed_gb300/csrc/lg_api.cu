@@ -108,6 +108,8 @@ struct lg_ctx {
     std::string tune_report;  // candidates and timings of the autotuner
 
     cudaStream_t stream = nullptr;
+    // joins calls made on caller streams into the context's order
+    cudaEvent_t ev_join = nullptr;
     float* d_image = nullptr;
     float* d_weight = nullptr;
     void* d_models = nullptr;
@@ -244,6 +246,8 @@ struct lg_ctx {
         if (mod && drv) drv->moduleUnload(mod);
         if (mod_set && drv) drv->moduleUnload(mod_set);
         mod_set = nullptr;
+        if (ev_join) cudaEventDestroy(ev_join);
+        ev_join = nullptr;
         if (stream) cudaStreamDestroy(stream);
         mod = nullptr;
         stream = nullptr;
@@ -257,13 +261,13 @@ namespace {
 
 // Launch shape for a model (tile sizes chosen for GB300; see the design
 // notes for the measurements behind them).
-lg::Shape choose_shape(const lg::Model& m, bool strict)
+lg::Shape choose_shape(const lg::Model& m, lg::Fp mode)
 {
     lg::Shape s;
-    // fast mode: 32 x 64 convolution tiles, each thread two rows (paired);
-    // the register window of a thread holds 2 (8 + PSF width - 1) floats,
-    // so PSFs wider than 49 pixels keep the single-row kernel
-    if (!m.psf.empty() && !strict && m.psfw <= 49) {
+    // fast and exact modes: 32 x 64 convolution tiles, each thread two rows
+    // (paired); the register window of a thread holds 2 (8 + PSF width - 1)
+    // floats, so PSFs wider than 49 pixels keep the single-row kernel
+    if (!m.psf.empty() && mode != lg::Fp::STRICT && m.psfw <= 49) {
         s.cty = 64;
         s.pair_rows = true;
     }
@@ -349,18 +353,18 @@ __global__ void __launch_bounds__(128)
         for (int i = 0; i < np; ++i) phys[(size_t)b * np + i] = params[(size_t)b * np + i];
 }
 
-bool ctx_strict(const lg_ctx* c) { return (c->flags & LG_FLAG_STRICT_FP) != 0; }
+lg::Fp ctx_mode(const lg_ctx* c) { return lg::fp_mode(c->flags); }
 // fast mode: hardware-approximate division and square root per ray
 // (<= 2 ulp, as the reference's -cl-fast-relaxed-math build allows) unless
-// LG_FLAG_IEEE_DIV; strict mode and set_params stay IEEE
-bool ctx_ieee(const lg_ctx* c) { return ctx_strict(c) || (c->flags & LG_FLAG_IEEE_DIV); }
+// LG_FLAG_IEEE_DIV; the exact and strict modes and set_params stay IEEE
+bool ctx_ieee(const lg_ctx* c) { return lg::fp_ieee(c->flags); }
 
 int compile_eval(lg_ctx* c, const lg::Shape& s, std::vector<char>& cubin)
 {
     std::string log;
-    const bool strict = ctx_strict(c);
-    int rc = lg::compile_program(lg::compose_source(c->model, s, strict, lg::Part::EVAL), !strict, cubin, log,
-                                 ctx_ieee(c));
+    const lg::Fp mode = ctx_mode(c);
+    int rc = lg::compile_program(lg::compose_source(c->model, s, mode, lg::Part::EVAL), lg::fp_fmad(mode), cubin,
+                                 log, ctx_ieee(c));
     return rc ? c->fail(rc, log) : LG_OK;
 }
 
@@ -484,14 +488,14 @@ int time_stages(lg_ctx* c, int B, double* render_ms, double* conv_ms)
 int autotune(lg_ctx* c)
 {
     const lg::Model& m = c->model;
-    const bool strict = ctx_strict(c);
-    const lg::Shape base = choose_shape(m, strict);
-    const std::string key = lg::tune_key(lg::compose_source(m, base, strict, lg::Part::EVAL), c->device,
-                                         c->max_batch, c->flags & (LG_FLAG_STRICT_FP | LG_FLAG_IEEE_DIV));
+    const lg::Fp mode = ctx_mode(c);
+    const lg::Shape base = choose_shape(m, mode);
+    const std::string key = lg::tune_key(lg::compose_source(m, base, mode, lg::Part::EVAL), c->device,
+                                         c->max_batch, c->flags & (LG_FLAG_STRICT_FP | LG_FLAG_IEEE_DIV | LG_FLAG_FAST_MATH));
     std::ostringstream rep;
     int rc;
     lg::Shape chosen;
-    if (lg::tune_cache_get(key, chosen) && lg::check_shape(chosen, strict, c->psf, m.psfw).empty()) {
+    if (lg::tune_cache_get(key, chosen) && lg::check_shape(chosen, mode, c->psf, m.psfw).empty()) {
         std::vector<char> cubin;
         if ((rc = compile_eval(c, chosen, cubin)) || (rc = load_eval(c, chosen, cubin))) return rc;
         c->tune_report = "cached " + key + ": " + chosen.str() + "\n";
@@ -514,21 +518,21 @@ int autotune(lg_ctx* c)
     // with the base render
     std::vector<lg::Shape> cand;
     std::vector<int> is_render;
-    for (const lg::Shape& s : lg::render_candidates(base, strict))
-        if (lg::check_shape(s, strict, c->psf, m.psfw).empty()) cand.push_back(s), is_render.push_back(1);
+    for (const lg::Shape& s : lg::render_candidates(base, mode))
+        if (lg::check_shape(s, mode, c->psf, m.psfw).empty()) cand.push_back(s), is_render.push_back(1);
     if (c->psf)
         for (const lg::Shape& s : lg::conv_candidates(base)) {
-            if (!lg::check_shape(s, strict, c->psf, m.psfw).empty()) continue;
+            if (!lg::check_shape(s, mode, c->psf, m.psfw).empty()) continue;
             bool dup = false;
             for (const lg::Shape& t : cand) dup = dup || t == s;
             if (!dup) cand.push_back(s), is_render.push_back(0);
         }
     std::vector<std::string> srcs;
-    for (const lg::Shape& s : cand) srcs.push_back(lg::compose_source(m, s, strict, lg::Part::EVAL));
+    for (const lg::Shape& s : cand) srcs.push_back(lg::compose_source(m, s, mode, lg::Part::EVAL));
     std::vector<std::vector<char>> cubins;
     std::vector<int> rcs;
     std::vector<std::string> logs;
-    lg::compile_parallel(srcs, !strict, ctx_ieee(c), cubins, rcs, logs);
+    lg::compile_parallel(srcs, lg::fp_fmad(mode), ctx_ieee(c), cubins, rcs, logs);
     double best_r = 1e30, best_c = 1e30;
     lg::Shape br = base, bc = base;
     for (size_t i = 0; i < cand.size(); ++i) {
@@ -595,11 +599,11 @@ int create_impl(lg_ctx* c, const lg_image_desc* img, const lg_object_desc* objs,
     // compose and compile the programs (the reference's clBuildProgram,
     // src/lensed.c:706-776): the set_params module here, the evaluation
     // module (whose launch shape may be tuned) once the buffers exist
-    const bool strict = (c->flags & LG_FLAG_STRICT_FP) != 0;
-    c->shape = choose_shape(m, strict);
+    const lg::Fp mode = lg::fp_mode(c->flags);
+    c->shape = choose_shape(m, mode);
     std::string log;
     std::vector<char> cubin_set;
-    rc = lg::compile_program(lg::compose_source(m, c->shape, strict, lg::Part::SET), false, cubin_set, log);
+    rc = lg::compile_program(lg::compose_source(m, c->shape, mode, lg::Part::SET), false, cubin_set, log);
     if (rc) return c->fail(rc, log);
 
     if ((rc = c->cuda(cudaSetDevice(c->device), "cudaSetDevice"))) return rc;
@@ -623,7 +627,9 @@ int create_impl(lg_ctx* c, const lg_image_desc* img, const lg_object_desc* objs,
         (rc = c->cuda(cudaMemcpy(&c->nobj, (void*)gp, sizeof c->nobj, cudaMemcpyDeviceToHost), "object count")))
         return rc;
 
-    if ((rc = c->cuda(cudaStreamCreateWithFlags(&c->stream, cudaStreamNonBlocking), "stream"))) return rc;
+    if ((rc = c->cuda(cudaStreamCreateWithFlags(&c->stream, cudaStreamNonBlocking), "stream")) ||
+        (rc = c->cuda(cudaEventCreateWithFlags(&c->ev_join, cudaEventDisableTiming), "event")))
+        return rc;
     const size_t B = (size_t)c->max_batch, N = (size_t)c->N, np = m.pars.size();
     auto alloc = [&](void** p, size_t bytes, const char* what) {
         cudaError_t e = cudaMalloc(p, bytes);
@@ -838,6 +844,26 @@ int order_after_legacy(lg_ctx* c)
     return rc;
 }
 
+// Calls on one context share its scratch (parameters, object data, raw
+// models, partial sums, tile counters), so they run in order whatever
+// stream they are made on: a call on a caller stream s first waits for the
+// work queued on the context's stream, and the context's stream then waits
+// for the call (the context's stream is the join point of every call).
+int join_before(lg_ctx* c, cudaStream_t s)
+{
+    int rc;
+    if (s == c->stream) return LG_OK;
+    if ((rc = c->cuda(cudaEventRecord(c->ev_join, c->stream), "event record"))) return rc;
+    return c->cuda(cudaStreamWaitEvent(s, c->ev_join, 0), "stream wait");
+}
+int join_after(lg_ctx* c, cudaStream_t s)
+{
+    int rc;
+    if (s == c->stream) return LG_OK;
+    if ((rc = c->cuda(cudaEventRecord(c->ev_join, s), "event record"))) return rc;
+    return c->cuda(cudaStreamWaitEvent(c->stream, c->ev_join, 0), "stream wait");
+}
+
 int check_priors(lg_ctx* c)
 {
     const lg::Model& m = c->model;
@@ -1050,12 +1076,13 @@ int lg_compile_check(const lg_image_desc* image, const lg_object_desc* objs, int
     std::string err;
     int rc = lg::build_model(image, objs, nobjs, opts, m, err);
     if (!rc) {
-        const bool strict = opts && (opts->flags & LG_FLAG_STRICT_FP);
+        const int flags = opts ? opts->flags : 0;
+        const lg::Fp mode = lg::fp_mode(flags);
         std::vector<char> cubin;
-        lg::Shape s = choose_shape(m, strict);
-        const bool ieee = strict || (opts && (opts->flags & LG_FLAG_IEEE_DIV));
-        rc = lg::compile_program(lg::compose_source(m, s, strict, lg::Part::EVAL), !strict, cubin, err, ieee);
-        if (!rc) rc = lg::compile_program(lg::compose_source(m, s, strict, lg::Part::SET), false, cubin, err);
+        lg::Shape s = choose_shape(m, mode);
+        rc = lg::compile_program(lg::compose_source(m, s, mode, lg::Part::EVAL), lg::fp_fmad(mode), cubin, err,
+                                 lg::fp_ieee(flags));
+        if (!rc) rc = lg::compile_program(lg::compose_source(m, s, mode, lg::Part::SET), false, cubin, err);
     }
     if (log && log_size) {
         std::snprintf(log, log_size, "%s", err.c_str());
@@ -1073,16 +1100,16 @@ int lg_tune_candidates(const lg_image_desc* image, const lg_object_desc* objs, i
         g_create_error = err;
         return rc;
     }
-    const bool strict = opts && (opts->flags & LG_FLAG_STRICT_FP);
-    const lg::Shape base = choose_shape(m, strict);
+    const lg::Fp mode = lg::fp_mode(opts ? opts->flags : 0);
+    const lg::Shape base = choose_shape(m, mode);
     std::vector<lg::Shape> cand;
-    for (const lg::Shape& s : lg::render_candidates(base, strict))
-        if (lg::check_shape(s, strict, !m.psf.empty(), m.psfw).empty()) cand.push_back(s);
+    for (const lg::Shape& s : lg::render_candidates(base, mode))
+        if (lg::check_shape(s, mode, !m.psf.empty(), m.psfw).empty()) cand.push_back(s);
     if (!m.psf.empty())
         for (const lg::Shape& s : lg::conv_candidates(base)) {
             bool dup = false;
             for (const lg::Shape& t : cand) dup = dup || t == s;
-            if (!dup && lg::check_shape(s, strict, true, m.psfw).empty()) cand.push_back(s);
+            if (!dup && lg::check_shape(s, mode, true, m.psfw).empty()) cand.push_back(s);
         }
     for (int i = 0; i < (int)cand.size() && i < max_shapes && shapes; ++i) {
         const lg::Shape& s = cand[i];
@@ -1099,7 +1126,8 @@ int lg_compile_check_shape(const lg_image_desc* image, const lg_object_desc* obj
     std::string err;
     int rc = shape ? lg::build_model(image, objs, nobjs, opts, m, err) : LG_ERR_INPUT;
     if (!rc) {
-        const bool strict = opts && (opts->flags & LG_FLAG_STRICT_FP);
+        const int flags = opts ? opts->flags : 0;
+        const lg::Fp mode = lg::fp_mode(flags);
         lg::Shape s;
         s.rt = shape[0];
         s.rppt = shape[1];
@@ -1108,13 +1136,13 @@ int lg_compile_check_shape(const lg_image_desc* image, const lg_object_desc* obj
         s.cty = shape[4];
         s.cr = shape[5];
         s.pair_rows = shape[6] != 0;
-        err = lg::check_shape(s, strict, !m.psf.empty(), m.psfw);
+        err = lg::check_shape(s, mode, !m.psf.empty(), m.psfw);
         if (!err.empty()) {
             rc = LG_ERR_INPUT;
         } else {
             std::vector<char> cubin;
-            const bool ieee = strict || (opts && (opts->flags & LG_FLAG_IEEE_DIV));
-            rc = lg::compile_program(lg::compose_source(m, s, strict, lg::Part::EVAL), !strict, cubin, err, ieee);
+            rc = lg::compile_program(lg::compose_source(m, s, mode, lg::Part::EVAL), lg::fp_fmad(mode), cubin, err,
+                                     lg::fp_ieee(flags));
         }
     }
     if (log && log_size) std::snprintf(log, log_size, "%s", err.c_str());
@@ -1215,7 +1243,9 @@ int lg_eval_batch_device(lg_ctx* c, const double* d_params, int B, double* d_log
     int rc;
     if ((rc = c->cuda(cudaSetDevice(c->device), "cudaSetDevice"))) return rc;
     if (!stream && (rc = order_after_legacy(c))) return rc;
-    return c->enqueue(B, d_params, d_logL, stream ? (cudaStream_t)stream : c->stream);
+    const cudaStream_t s = stream ? (cudaStream_t)stream : c->stream;
+    if ((rc = join_before(c, s)) || (rc = c->enqueue(B, d_params, d_logL, s))) return rc;
+    return join_after(c, s);
 }
 
 int lg_eval_cube_batch(lg_ctx* c, const double* cube, int B, double* phys, double* logL)
@@ -1244,7 +1274,9 @@ int lg_eval_cube_batch_device(lg_ctx* c, const double* d_cube, int B, double* d_
     if (B == 0) return LG_OK;
     if ((rc = c->cuda(cudaSetDevice(c->device), "cudaSetDevice"))) return rc;
     if (!stream && (rc = order_after_legacy(c))) return rc;
-    return enqueue_cube(c, B, d_cube, d_phys, d_logL, stream ? (cudaStream_t)stream : c->stream);
+    const cudaStream_t s = stream ? (cudaStream_t)stream : c->stream;
+    if ((rc = join_before(c, s)) || (rc = enqueue_cube(c, B, d_cube, d_phys, d_logL, s))) return rc;
+    return join_after(c, s);
 }
 
 namespace {
@@ -1381,7 +1413,7 @@ int lg_set_launch_shape(lg_ctx* c, const int shape[7])
     s.cty = shape[4];
     s.cr = shape[5];
     s.pair_rows = shape[6] != 0;
-    const std::string why = lg::check_shape(s, ctx_strict(c), c->psf, c->model.psfw);
+    const std::string why = lg::check_shape(s, ctx_mode(c), c->psf, c->model.psfw);
     if (!why.empty()) return c->fail(LG_ERR_INPUT, "launch shape: " + why);
     int rc;
     if ((rc = c->cuda(cudaSetDevice(c->device), "cudaSetDevice"))) return rc;

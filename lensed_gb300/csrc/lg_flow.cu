@@ -667,11 +667,15 @@ __device__ __forceinline__ void lg_mma_commit(void* mbar)
                  : "memory");
 }
 
-// Bounded wait on an mbarrier phase (one thread); false when it ran out.
-__device__ __forceinline__ bool lg_mbar_wait(void* mbar, uint32_t parity)
+// Polls of an mbarrier phase before a bounded wait gives up.
+constexpr long kMbarTries = 1L << 20;
+
+// Bounded wait on an mbarrier phase (one thread): at most `tries` polls
+// (none for tries <= 0); false when it ran out.
+__device__ __forceinline__ bool lg_mbar_wait(void* mbar, uint32_t parity, long tries = kMbarTries)
 {
     uint32_t done = 0;
-    for (long it = 0; it < (1L << 20) && !done; ++it)
+    for (long it = 0; it < tries && !done; ++it)
         asm volatile("{\n.reg .pred p;\nmbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\nselp.u32 %0, 1, 0, p;\n}"
                      : "=r"(done)
                      : "r"(lg_saddr(mbar)), "r"(parity)
@@ -781,7 +785,7 @@ struct TcSmem {
 __global__ void __launch_bounds__(256, 2)
     lg_flow_inverse_tc(FlowDims f, const float* __restrict__ P, const __nv_bfloat16* __restrict__ packed,
                        const float* __restrict__ Z, int M, float* __restrict__ Uout, float* __restrict__ ldet,
-                       int* __restrict__ err)
+                       int* __restrict__ err, long tries)
 {
     extern __shared__ __align__(1024) unsigned char smem[];
     const TcDims td(f);
@@ -835,6 +839,10 @@ __global__ void __launch_bounds__(256, 2)
     if (t == 0) issue_weights(f.L - 1);
     uint32_t mma_phase = 0;
     bool ok = true;
+    // a chain whose completion wait ran out (thread 0): drained before the
+    // tensor memory is freed
+    bool mma_pending = false;
+    uint32_t pending_parity = 0;
     // one MMA chain: D (tmem) = A (128 x K) . B (N x K)^T
     auto gemm = [&](const void* A, const void* B, int K, int N) {
         if (t == 0) {
@@ -844,7 +852,11 @@ __global__ void __launch_bounds__(256, 2)
                 lg_mma(tmem, lg_umma_desc(lg_saddr(A) + ks * 256, 128, sb),
                        lg_umma_desc(lg_saddr(B) + ks * 256, 128, sb), idesc, ks > 0);
             lg_mma_commit(bars);
-            if (!lg_mbar_wait(bars, mma_phase)) misc[1] = 1;
+            if (!lg_mbar_wait(bars, mma_phase, tries)) {
+                misc[1] = 1;
+                mma_pending = true;
+                pending_parity = mma_phase;
+            }
         }
         mma_phase ^= 1u;
         __syncthreads();
@@ -887,7 +899,7 @@ __global__ void __launch_bounds__(256, 2)
             A0[lg_core_off(m, k, td.kp0)] = __float2bfloat16_rn(k < da ? cur[m * d + a0 + k] : 0.0f);
         }
         asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
-        if (t == 0 && !lg_mbar_wait(bars + 1, (uint32_t)waited & 1u)) misc[1] = 1;
+        if (t == 0 && !lg_mbar_wait(bars + 1, (uint32_t)waited & 1u, tries)) misc[1] = 1;
         __syncthreads();
         if (!misc[1]) ++waited;
         if (misc[1]) {
@@ -949,7 +961,10 @@ __global__ void __launch_bounds__(256, 2)
         if (t < 128 && base + t < M) ldet[base + t] = ld[t];
     } else if (t == 0) {
         atomicExch(err, 1);
-        // a weight copy still in flight lands before the block exits
+        // what is still in flight completes before the tensor memory is
+        // freed and the block exits: the MMA chain whose wait gave up, and
+        // the weight copies issued (waits with the full budget)
+        if (mma_pending) lg_mbar_wait(bars, pending_parity);
         for (; waited < issued; ++waited) lg_mbar_wait(bars + 1, (uint32_t)waited & 1u);
     }
     asm volatile("tcgen05.fence::before_thread_sync;");
@@ -1332,6 +1347,9 @@ public:
 
     size_t packed_size() const { return (size_t)f.L * TcDims(f).sl; }
 
+    // polls per bounded wait of the tensor-core inverse
+    long wait_tries = kMbarTries;
+
     // BF16 tensor-core operands of the weights W (for the tc inverse).
     bool pack(const float* W, __nv_bfloat16* out, cudaStream_t st)
     {
@@ -1347,7 +1365,8 @@ public:
                  cudaStream_t st, int* err)
     {
         if (tc && packed) {
-            lg_flow_inverse_tc<<<(M + 127) / 128, 256, TcSmem(f).total, st>>>(f, W, packed, z, M, uout, ldet, err);
+            lg_flow_inverse_tc<<<(M + 127) / 128, 256, TcSmem(f).total, st>>>(f, W, packed, z, M, uout, ldet, err,
+                                                                              wait_tries);
             return cudaGetLastError() == cudaSuccess;
         }
         const int blocks = (M + FRI - 1) / FRI, sm = inverse_smem();
@@ -1467,6 +1486,7 @@ public:
         if (flow.f.d != d) {
             flow.bf16 = true;
             if (!flow.init(d, opt.layers, opt.width, opt.hidden, seed)) return LG_ERR_INPUT;
+            flow.wait_tries = opt.wait_tries == 0 ? kMbarTries : (opt.wait_tries < 0 ? 0 : opt.wait_tries);
         }
         if (!ps && cudaStreamCreateWithFlags(&ps, cudaStreamNonBlocking) != cudaSuccess) return fail_cuda();
         if (!done && cudaEventCreate(&done) != cudaSuccess) return fail_cuda();
@@ -1889,6 +1909,7 @@ lg_flow_options lg_flow_defaults(void)
     o.patience = 4;
     o.lag = 800;
     o.draw_cost = 0.005;
+    o.wait_tries = 0;
     return o;
 }
 
@@ -1902,8 +1923,10 @@ long lg_flow_nparams(int d, int layers, int width, int hidden)
 // standardised as the sampler's live points are) exactly as the sampler
 // retrains it, for tests: history[0..] receives the held-out loss before
 // training and after each epoch (up to max_history values, NaN past the
-// epochs that ran); returns the number of epochs run (negative on error);
-// *efficiency the calibrated kept fraction of latent draws.
+// epochs that ran); returns the number of epochs run (negative on error;
+// LG_ERR_TIMEOUT when a bounded wait of the calibration's tensor-core
+// inverse ran out); *efficiency the calibrated kept fraction of latent
+// draws.
 int lg_flow_fit(int device, int d, const lg_flow_options* opts, const double* pts, int n, float* history,
                 int max_history, double* efficiency)
 {
@@ -1916,6 +1939,12 @@ int lg_flow_fit(int device, int d, const lg_flow_options* opts, const double* pt
     p->finish();
     for (int i = 0; i < max_history && history; ++i) history[i] = i < LG_FLOW_HISTORY ? p->hstate.p[8 + i] : NAN;
     if (efficiency) *efficiency = p->efficiency[p->pslot];
+    int tcerr = 0;
+    std::memcpy(&tcerr, p->hres.p + 3, sizeof tcerr);
+    if (tcerr) {
+        lg::set_global_error("flow fit: a bounded wait of the tensor-core inverse ran out (calibration)");
+        return LG_ERR_TIMEOUT;
+    }
     return (int)p->hstate.p[3];
 }
 

@@ -59,6 +59,8 @@ const char* kernels_source();
 const char* set_kernel_source();
 const char* crmath_source();
 const char* multi_kernels_source();
+const char* crf_source();         // correctly rounded exp/log/atan/atanh in FP32 arithmetic
+const char* exact_pair_source();  // their ray-pair overloads for the exact modules
 
 // ------------------------------------------------------------------- priors
 // Lensed's prior plugins (src/prior.c:47-51): delta (pseudo), unif, norm.
@@ -156,16 +158,33 @@ struct Shape {
     std::string str() const;
 };
 
+// Floating-point mode of the evaluation module.
+//   EXACT   (default) rays traced in pairs with f32x2 instructions, no
+//           contraction, IEEE division and square root, elementary functions
+//           correctly rounded (lg_crfloat.cuh, or in double): every image is
+//           bit-identical to the strict module's and the oracle's
+//   STRICT  (LG_FLAG_STRICT_FP) one ray at a time, every elementary
+//           function evaluated in double and rounded once: the definition
+//           the exact mode reproduces
+//   FAST    (LG_FLAG_FAST_MATH) ray pairs with FMA contraction and the
+//           SFU-based functions of the prelude (a few ulp)
+enum class Fp { FAST, EXACT, STRICT };
+Fp fp_mode(int flags);
+inline bool fp_fmad(Fp m) { return m == Fp::FAST; }
+// IEEE division and square root per ray (the fast mode only with
+// LG_FLAG_IEEE_DIV)
+bool fp_ieee(int flags);
+
 // Compose the NVRTC sources of a model and compile them to cubins for
 // sm_103a.  The set_params module always uses the double-evaluated
-// elementary functions and no FMA contraction; the evaluation module uses
-// them only in strict mode.
+// elementary functions and no FMA contraction; the evaluation module per
+// its floating-point mode.
 enum class Part { SET, EVAL };
-std::string compose_source(const Model& m, const Shape& s, bool strict, Part part);
+std::string compose_source(const Model& m, const Shape& s, Fp mode, Part part);
 // Evaluation module for a batch of systems sharing m's objects and rule; the
 // PSF shapes (w, h) present in the batch get their own convolution code.
 std::string compose_multi_source(const Model& m, const std::vector<std::pair<int, int>>& psf_shapes,
-                                 const Shape& s, bool strict);
+                                 const Shape& s, Fp mode);
 int compile_program(const std::string& src, bool fmad, std::vector<char>& cubin, std::string& log,
                     bool ieee_divsqrt = true);
 
@@ -173,10 +192,10 @@ int compile_program(const std::string& src, bool fmad, std::vector<char>& cubin,
 // Candidate launch shapes around a base shape (lg_tune.cpp): render shapes
 // vary threads, pixels per group and (fast mode) the quadrature split;
 // convolution shapes vary the tile and outputs per thread.
-std::vector<Shape> render_candidates(const Shape& base, bool strict);
+std::vector<Shape> render_candidates(const Shape& base, Fp mode);
 std::vector<Shape> conv_candidates(const Shape& base, bool multi = false);
 // "" when the shape is valid for the program, else the reason.
-std::string check_shape(const Shape& s, bool strict, bool psf, int psfw);
+std::string check_shape(const Shape& s, Fp mode, bool psf, int psfw);
 // Compile several programs at once (NVRTC is thread-safe).
 void compile_parallel(const std::vector<std::string>& srcs, bool fmad, bool ieee,
                       std::vector<std::vector<char>>& cubins, std::vector<int>& rcs, std::vector<std::string>& logs);

@@ -1,15 +1,57 @@
-// Diagnostic entry point: the paired-ray elementary functions of the device
-// prelude (exp, log, square root, reciprocal, arctangent and inverse
-// hyperbolic tangent used by the fast evaluation modules),
-// evaluated on a vector of inputs, so their accuracy can be checked against
-// double-precision references on the host.
+// Diagnostic entry points: the paired-ray elementary functions of the
+// device prelude (exp, log, square root, reciprocal, arctangent and inverse
+// hyperbolic tangent used by the fast evaluation modules) and the correctly
+// rounded functions of the exact modules (lg_crfloat.cuh), evaluated on a
+// vector of inputs, so their accuracy can be checked against
+// double-precision references on the host; and a sweep that compares the
+// correctly rounded functions with the double evaluation on the device over
+// a range of float bit patterns.
 
 #include <cuda_runtime.h>
 
 #include "lg_internal.h"
 #include "../device/lg_prelude.cuh"
+#include "../device/lg_crfloat.cuh"
 
 namespace {
+
+// correctly rounded function fn (0 exp, 1 log, 2 atan, 3 atanh) of a pair
+__device__ float2 crf_pair(int fn, float2 a)
+{
+    return fn == 0 ? lg_crf_exp(a) : fn == 1 ? lg_crf_log(a) : fn == 2 ? lg_crf_atan(a) : lg_crf_atanh(a);
+}
+__device__ float crf_double(int fn, float x)
+{
+    return fn == 0   ? (float)exp((double)x)
+           : fn == 1 ? (float)log((double)x)
+           : fn == 2 ? (float)atan((double)x)
+                     : (float)atanh((double)x);
+}
+
+// bit patterns lo + 2 i (the pair: lo + 2i, lo + 2i + 1) below hi; counts
+// lanes whose bits differ from the double evaluation (NaN equal to NaN),
+// and keeps the first few
+__global__ void lg_crf_sweep_kernel(int fn, unsigned long long lo, unsigned long long hi,
+                                    unsigned long long* __restrict__ bad, unsigned* __restrict__ first, int nfirst)
+{
+    const unsigned long long stride = 2ull * gridDim.x * blockDim.x;
+    unsigned long long nbad = 0;
+    for (unsigned long long u = lo + 2ull * (blockIdx.x * (unsigned long long)blockDim.x + threadIdx.x); u < hi;
+         u += stride) {
+        const float x0 = __uint_as_float((unsigned)u);
+        const float x1 = __uint_as_float((unsigned)(u + 1 < hi ? u + 1 : u));
+        const float2 r = crf_pair(fn, make_float2(x0, x1));
+        const float w0 = crf_double(fn, x0), w1 = crf_double(fn, x1);
+        const bool ok0 = __float_as_uint(r.x) == __float_as_uint(w0) || (r.x != r.x && w0 != w0);
+        const bool ok1 = __float_as_uint(r.y) == __float_as_uint(w1) || (r.y != r.y && w1 != w1);
+        if (!ok0 || !ok1) {
+            nbad += (!ok0) + (!ok1);
+            const unsigned long long k = atomicAdd(bad + 1, 1ull);
+            if (k < (unsigned long long)nfirst) first[k] = ok0 ? (unsigned)(u + 1) : (unsigned)u;
+        }
+    }
+    if (nbad) atomicAdd(bad, nbad);
+}
 
 __global__ void lg_pair_math_kernel(int fn, const float* __restrict__ x, int n, float* __restrict__ out)
 {
@@ -21,7 +63,8 @@ __global__ void lg_pair_math_kernel(int fn, const float* __restrict__ x, int n, 
                       : fn == 2 ? sqrtf(a)
                       : fn == 3 ? 1.0f / a
                       : fn == 4 ? atanf(a)
-                                : atanhf(a);
+                      : fn == 5 ? atanhf(a)
+                                : lg_pair{crf_pair(fn - 6, a.v)};
     out[i] = r.v.x;
     if (i + 1 < n) out[i + 1] = r.v.y;
 }
@@ -30,7 +73,7 @@ __global__ void lg_pair_math_kernel(int fn, const float* __restrict__ x, int n, 
 
 extern "C" int lg_probe_pair_math(int device, int fn, const float* x, int n, float* out)
 {
-    if (!x || !out || n < 0 || fn < 0 || fn > 5) return LG_ERR_INPUT;
+    if (!x || !out || n < 0 || fn < 0 || fn > 9) return LG_ERR_INPUT;
     if (n == 0) return LG_OK;
     auto fail = [](cudaError_t e) {
         lg::set_global_error(cudaGetErrorString(e));
@@ -55,4 +98,41 @@ extern "C" int lg_probe_pair_math(int device, int fn, const float* x, int n, flo
     cudaFree(dx);
     cudaFree(dy);
     return e == cudaSuccess ? LG_OK : fail(e);
+}
+
+extern "C" int lg_probe_crf_sweep(int device, int fn, unsigned long long lo, unsigned long long hi,
+                                  unsigned long long* mismatches, unsigned* first, int nfirst)
+{
+    if (fn < 0 || fn > 3 || lo > hi || hi > (1ull << 32) || !mismatches || nfirst < 0 || (nfirst && !first))
+        return LG_ERR_INPUT;
+    auto fail = [](cudaError_t e) {
+        lg::set_global_error(cudaGetErrorString(e));
+        return LG_ERR_CUDA;
+    };
+    cudaError_t e = cudaSetDevice(device);
+    if (e != cudaSuccess) return fail(e);
+    unsigned long long* d_bad = nullptr;
+    unsigned* d_first = nullptr;
+    if ((e = cudaMalloc((void**)&d_bad, 2 * sizeof(unsigned long long))) != cudaSuccess) return fail(e);
+    if ((e = cudaMalloc((void**)&d_first, (nfirst ? nfirst : 1) * sizeof(unsigned))) != cudaSuccess) {
+        cudaFree(d_bad);
+        return fail(e);
+    }
+    e = cudaMemset(d_bad, 0, 2 * sizeof(unsigned long long));
+    if (e == cudaSuccess && hi > lo) {
+        int sms = 0;
+        cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, device);
+        lg_crf_sweep_kernel<<<sms * 8, 256>>>(fn, lo, hi, d_bad, d_first, nfirst);
+        e = cudaGetLastError();
+    }
+    unsigned long long h[2] = {0, 0};
+    if (e == cudaSuccess) e = cudaMemcpy(h, d_bad, sizeof h, cudaMemcpyDeviceToHost);
+    if (e == cudaSuccess && nfirst)
+        e = cudaMemcpy(first, d_first, (size_t)(h[1] < (unsigned long long)nfirst ? h[1] : nfirst) * sizeof(unsigned),
+                       cudaMemcpyDeviceToHost);
+    cudaFree(d_bad);
+    cudaFree(d_first);
+    if (e != cudaSuccess) return fail(e);
+    *mismatches = h[0];
+    return LG_OK;
 }

@@ -195,22 +195,36 @@ void emit_set_params(std::ostringstream& o, const Model& m)
     o << "    default: break;\n    }\n}\n\n";
 }
 
+const char* mode_name(Fp mode) { return mode == Fp::FAST ? "fast" : (mode == Fp::EXACT ? "exact" : "strict"); }
+
+// The prelude and the elementary-function layer of a module: the set_params
+// module and the strict and exact evaluation modules map the plugins'
+// float functions to the double-evaluated ones; the exact modules add the
+// correctly rounded single-precision functions and their ray-pair overloads.
+void emit_prelude(std::ostringstream& o, Fp mode, bool set)
+{
+    if (!set && mode == Fp::EXACT) o << "#define LG_EXACT 1\n";
+    o << "\n" << prelude_source() << "\n";
+    if (set || mode != Fp::FAST) o << crmath_source() << "\n";
+    if (!set && mode == Fp::EXACT) o << crf_source() << "\n" << exact_pair_source() << "\n";
+}
+
 }  // namespace
 
-std::string compose_source(const Model& m, const Shape& s, bool strict, Part part)
+std::string compose_source(const Model& m, const Shape& s, Fp mode, Part part)
 {
     const bool set = part == Part::SET;
+    const bool strict = mode == Fp::STRICT;
     std::ostringstream o;
     o << "// Lensed likelihood program (" << (set ? "set_params" : "evaluation") << " module) composed for:";
     for (const auto& ob : m.objs) o << " " << ob.id << "=" << ob.plugin->name;
     o << "\n// image " << m.width << "x" << m.height << ", rule " << m.rule->name << " (" << m.rule->size
-      << " points), PSF " << m.psfw << "x" << m.psfh << (strict ? ", strict FP" : "") << "\n\n";
+      << " points), PSF " << m.psfw << "x" << m.psfh << ", " << mode_name(mode) << " FP\n\n";
     o << "#define LG_RT " << s.rt << "\n#define LG_RPPT " << s.rppt << "\n#define LG_QS " << s.qs << "\n";
     o << "#define LG_CTX " << s.ctx << "\n#define LG_CTY " << s.cty << "\n#define LG_CR " << s.cr << "\n";
-    // fast mode with a PSF up to 49 wide pairs rows unless the shape says not
+    // the paired modes with a PSF up to 49 wide pair rows unless the shape says not
     if (!strict && !s.pair_rows && m.psfw <= 49) o << "#define LG_CONV_SINGLE 1\n";
-    o << "\n" << prelude_source() << "\n";
-    if (set || strict) o << crmath_source() << "\n";
+    emit_prelude(o, mode, set);
     std::set<std::string> done;
     for (const auto& ob : m.objs) emit_plugin(o, ob.plugin, done);
 
@@ -266,17 +280,16 @@ std::string compose_source(const Model& m, const Shape& s, bool strict, Part par
 }
 
 std::string compose_multi_source(const Model& m, const std::vector<std::pair<int, int>>& psf_shapes,
-                                 const Shape& s, bool strict)
+                                 const Shape& s, Fp mode)
 {
+    const bool strict = mode == Fp::STRICT;
     std::ostringstream o;
     o << "// Lensed likelihood program (multi-system evaluation module) composed for:";
     for (const auto& ob : m.objs) o << " " << ob.id << "=" << ob.plugin->name;
-    o << "\n// rule " << m.rule->name << " (" << m.rule->size << " points)" << (strict ? ", strict FP" : "")
-      << "\n\n";
+    o << "\n// rule " << m.rule->name << " (" << m.rule->size << " points), " << mode_name(mode) << " FP\n\n";
     o << "#define LG_RT " << s.rt << "\n#define LG_RPPT " << s.rppt << "\n#define LG_QS " << s.qs << "\n";
-    o << "#define LG_CTX " << s.ctx << "\n#define LG_CTY " << s.cty << "\n#define LG_CR " << s.cr << "\n\n";
-    o << prelude_source() << "\n";
-    if (strict) o << crmath_source() << "\n";
+    o << "#define LG_CTX " << s.ctx << "\n#define LG_CTY " << s.cty << "\n#define LG_CR " << s.cr << "\n";
+    emit_prelude(o, mode, false);
     std::set<std::string> done;
     for (const auto& ob : m.objs) emit_plugin(o, ob.plugin, done);
     o << "// ---- model section\n#define LG_NPARS " << m.pars.size() << "\n";

@@ -24,6 +24,8 @@ const char* kernels_source() { return LG_EMBED_KERNELS; }
 const char* set_kernel_source() { return LG_EMBED_SET_KERNEL; }
 const char* crmath_source() { return LG_EMBED_CRMATH; }
 const char* multi_kernels_source() { return LG_EMBED_MULTI; }
+const char* crf_source() { return LG_EMBED_CRF; }
+const char* exact_pair_source() { return LG_EMBED_EXACT_PAIR; }
 
 namespace {
 

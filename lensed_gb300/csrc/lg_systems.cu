@@ -112,8 +112,8 @@ struct lg_systems {
 
 namespace {
 
-bool sys_strict(const lg_systems* S) { return (S->flags & LG_FLAG_STRICT_FP) != 0; }
-bool sys_ieee(const lg_systems* S) { return sys_strict(S) || (S->flags & LG_FLAG_IEEE_DIV); }
+lg::Fp sys_mode(const lg_systems* S) { return lg::fp_mode(S->flags); }
+bool sys_ieee(const lg_systems* S) { return lg::fp_ieee(S->flags); }
 
 // Distinct PSF shapes of the batch: each gets its own convolution code.
 std::vector<std::pair<int, int>> psf_shapes(const lg_systems* S)
@@ -126,24 +126,24 @@ std::vector<std::pair<int, int>> psf_shapes(const lg_systems* S)
 
 std::string multi_source(const lg_systems* S, const lg::Shape& sh)
 {
-    return lg::compose_multi_source(S->models[0], psf_shapes(S), sh, sys_strict(S));
+    return lg::compose_multi_source(S->models[0], psf_shapes(S), sh, sys_mode(S));
 }
 
 int compile_multi(lg_systems* S, const lg::Shape& sh, std::vector<char>& cubin)
 {
     std::string log;
-    int rc = lg::compile_program(multi_source(S, sh), !sys_strict(S), cubin, log, sys_ieee(S));
+    int rc = lg::compile_program(multi_source(S, sh), lg::fp_fmad(sys_mode(S)), cubin, log, sys_ieee(S));
     return rc ? S->fail(rc, log) : LG_OK;
 }
 
 // Launch shapes of the multi-system kernels: cty counts thread rows (a
 // paired-row unit covers 2 cty rows), and cr is a multiple of 8 so that
 // both unit kinds compile.
-std::string check_multi_shape(const lg::Shape& s, bool strict)
+std::string check_multi_shape(const lg::Shape& s, lg::Fp mode)
 {
     lg::Shape t = s;
     t.pair_rows = false;
-    std::string why = lg::check_shape(t, strict, true, 0);
+    std::string why = lg::check_shape(t, mode, true, 0);
     if (why.empty() && s.pair_rows) why = "the multi-system kernels choose paired rows per system";
     if (why.empty() && s.cr % 8) why = "multi-system convolution needs cr % 8 == 0";
     return why;
@@ -162,7 +162,7 @@ int apply_shape(lg_systems* S, const lg::Shape& sh, const std::vector<char>& cub
     cudaFree(S->d_partials);
     S->d_partials = nullptr;
     S->shape = sh;
-    const bool strict = sys_strict(S);
+    const bool strict = sys_mode(S) == lg::Fp::STRICT;
     long long part = 0;
     int csmem = 0;
     S->part0.clear();
@@ -170,8 +170,8 @@ int apply_shape(lg_systems* S, const lg::Shape& sh, const std::vector<char>& cub
         const lg::Model& m = S->models[s];
         SysInfo& I = S->info[s];
         I.rtiles = (I.N + sh.rtile() - 1) / sh.rtile();
-        // fast mode, PSF up to 49 wide: paired-row units of 2 * cty rows, as
-        // the single-system context tiles them
+        // fast and exact modes, PSF up to 49 wide: paired-row units of
+        // 2 * cty rows, as the single-system context tiles them
         const bool paired = S->psf && !strict && m.psfw <= 49;
         const int cty = paired ? 2 * sh.cty : sh.cty;
         I.ctiles_x = (I.W + sh.ctx - 1) / sh.ctx;
@@ -293,7 +293,7 @@ int create_systems(lg_systems* S, const lg_image_desc* images, int nsys, const l
 
     // static layout: images, PSFs and raw models by capacity; the tiles
     // and partial sums depend on the launch shape (apply_shape)
-    const bool strict = (S->flags & LG_FLAG_STRICT_FP) != 0;
+    const lg::Fp mode = lg::fp_mode(S->flags);
     long long img = 0, raw = 0;
     int psf_off = 0;
     for (int s = 0; s < nsys; ++s) {
@@ -325,7 +325,7 @@ int create_systems(lg_systems* S, const lg_image_desc* images, int nsys, const l
     // set_params module
     std::vector<char> cubin_set;
     std::string log;
-    rc = lg::compile_program(lg::compose_source(m0, S->shape, strict, lg::Part::SET), false, cubin_set, log);
+    rc = lg::compile_program(lg::compose_source(m0, S->shape, mode, lg::Part::SET), false, cubin_set, log);
     if (rc) return S->fail(rc, log);
     if ((rc = S->cuda(cudaSetDevice(S->device), "cudaSetDevice")) || (rc = S->cuda(cudaFree(nullptr), "context")))
         return rc;
@@ -497,15 +497,15 @@ int time_systems(lg_systems* S, double* render_ms, double* conv_ms)
 // of each are combined (cached per program, device, capacity and flags).
 int autotune_systems(lg_systems* S)
 {
-    const bool strict = sys_strict(S);
+    const lg::Fp mode = sys_mode(S);
     const lg::Shape base = S->shape;
     std::string caps;
     for (int c : S->cap) caps += std::to_string(c) + ",";
     const std::string key = lg::tune_key(multi_source(S, base) + caps, S->device, S->max_total,
-                                         S->flags & (LG_FLAG_STRICT_FP | LG_FLAG_IEEE_DIV));
+                                         S->flags & (LG_FLAG_STRICT_FP | LG_FLAG_IEEE_DIV | LG_FLAG_FAST_MATH));
     int rc;
     lg::Shape chosen;
-    if (lg::tune_cache_get(key, chosen) && check_multi_shape(chosen, strict).empty()) {
+    if (lg::tune_cache_get(key, chosen) && check_multi_shape(chosen, mode).empty()) {
         std::vector<char> cubin;
         if ((rc = compile_multi(S, chosen, cubin)) || (rc = apply_shape(S, chosen, cubin))) return rc;
         S->tune_report = "cached " + key + ": " + chosen.str() + "\n";
@@ -521,11 +521,11 @@ int autotune_systems(lg_systems* S)
     }
     std::vector<lg::Shape> cand;
     std::vector<int> is_render;
-    for (const lg::Shape& s : lg::render_candidates(base, strict))
-        if (check_multi_shape(s, strict).empty()) cand.push_back(s), is_render.push_back(1);
+    for (const lg::Shape& s : lg::render_candidates(base, mode))
+        if (check_multi_shape(s, mode).empty()) cand.push_back(s), is_render.push_back(1);
     if (S->psf)
         for (const lg::Shape& s : lg::conv_candidates(base, true)) {
-            if (!check_multi_shape(s, strict).empty()) continue;
+            if (!check_multi_shape(s, mode).empty()) continue;
             bool dup = false;
             for (const lg::Shape& t : cand) dup = dup || t == s;
             if (!dup) cand.push_back(s), is_render.push_back(0);
@@ -535,7 +535,7 @@ int autotune_systems(lg_systems* S)
     std::vector<std::vector<char>> cubins;
     std::vector<int> rcs;
     std::vector<std::string> logs;
-    lg::compile_parallel(srcs, !strict, sys_ieee(S), cubins, rcs, logs);
+    lg::compile_parallel(srcs, lg::fp_fmad(mode), sys_ieee(S), cubins, rcs, logs);
     std::ostringstream rep;
     double best_r = 1e30, best_c = 1e30;
     lg::Shape br = base, bc = base;
@@ -635,7 +635,7 @@ int lg_systems_set_launch_shape(lg_systems* S, const int shape[7])
     s.cty = shape[4];
     s.cr = shape[5];
     s.pair_rows = shape[6] != 0;
-    const std::string why = check_multi_shape(s, sys_strict(S));
+    const std::string why = check_multi_shape(s, sys_mode(S));
     if (!why.empty()) return S->fail(LG_ERR_INPUT, "launch shape: " + why);
     int rc;
     if ((rc = S->cuda(cudaSetDevice(S->device), "cudaSetDevice"))) return rc;

@@ -48,16 +48,30 @@ std::string Shape::str() const
     return o.str();
 }
 
-std::vector<Shape> render_candidates(const Shape& base, bool strict)
+Fp fp_mode(int flags)
 {
-    // (threads, pixels per group, quadrature split)
+    if (flags & LG_FLAG_STRICT_FP) return Fp::STRICT;
+    if (flags & LG_FLAG_FAST_MATH) return Fp::FAST;
+    return Fp::EXACT;
+}
+
+bool fp_ieee(int flags) { return fp_mode(flags) != Fp::FAST || (flags & LG_FLAG_IEEE_DIV); }
+
+std::vector<Shape> render_candidates(const Shape& base, Fp mode)
+{
+    // (threads, pixels per group, quadrature split); the exact and strict
+    // modes keep the quadrature sum in order (split 1)
     static const int fast[][3] = {{128, 2, 1}, {256, 2, 1}, {64, 2, 1}, {128, 4, 1}, {128, 2, 2}, {256, 2, 2},
                                   {128, 2, 4}, {128, 2, 8}};
+    static const int exact[][3] = {{128, 2, 1}, {256, 2, 1}, {64, 2, 1}, {128, 4, 1}, {64, 4, 1}};
     static const int scalar[][3] = {{128, 2, 1}, {256, 2, 1}, {64, 2, 1}, {128, 1, 1}, {128, 4, 1}};
+    const int(*tab)[3] = mode == Fp::FAST ? fast : (mode == Fp::EXACT ? exact : scalar);
+    const int n = mode == Fp::FAST ? (int)(sizeof fast / sizeof fast[0])
+                                   : (mode == Fp::EXACT ? (int)(sizeof exact / sizeof exact[0])
+                                                        : (int)(sizeof scalar / sizeof scalar[0]));
     std::vector<Shape> out;
-    const int n = strict ? (int)(sizeof scalar / sizeof scalar[0]) : (int)(sizeof fast / sizeof fast[0]);
     for (int i = 0; i < n; ++i) {
-        const int* c = strict ? scalar[i] : fast[i];
+        const int* c = tab[i];
         Shape s = base;
         s.rt = c[0];
         s.rppt = c[1];
@@ -103,16 +117,17 @@ std::vector<Shape> conv_candidates(const Shape& base, bool multi)
     return out;
 }
 
-std::string check_shape(const Shape& s, bool strict, bool psf, int psfw)
+std::string check_shape(const Shape& s, Fp mode, bool psf, int psfw)
 {
+    const bool strict = mode == Fp::STRICT;
     if (s.rt < 32 || s.rt > 1024 || s.rt % 32) return "render threads must be a multiple of 32 in [32, 1024]";
     if (s.rppt < 1 || s.rppt > 8) return "pixels per thread group must be in [1, 8]";
     if (s.qs != 1 && s.qs != 2 && s.qs != 4 && s.qs != 8) return "quadrature split must be 1, 2, 4 or 8";
-    if (strict && s.qs != 1) return "strict mode keeps the quadrature sum in order (split 1)";
+    if (mode != Fp::FAST && s.qs != 1) return "the exact and strict modes keep the quadrature sum in order (split 1)";
     if (!psf) return "";
     if (s.cr != 4 && s.cr != 8 && s.cr != 16) return "convolution outputs per thread must be 4, 8 or 16";
     if (s.ctx < s.cr || s.ctx % s.cr || s.ctx > 256) return "convolution tile width must be a multiple of cr";
-    if (s.pair_rows && (strict || psfw > 49)) return "paired rows need fast mode and a PSF up to 49 wide";
+    if (s.pair_rows && (strict || psfw > 49)) return "paired rows need the fast or exact mode and a PSF up to 49 wide";
     if (s.pair_rows && (s.cr % 8 || s.cty % 2)) return "paired rows need cr % 8 == 0 and an even tile height";
     if (s.cty < 1 || s.cty > 256) return "convolution tile height must be in [1, 256]";
     const int threads = (s.ctx / s.cr) * s.conv_block_y();

@@ -1,0 +1,529 @@
+// Correctly rounded single-precision exp, log, atan and atanh computed in
+// single-precision arithmetic, for the exact evaluation modules.
+//
+// The likelihood's FP32 semantics (the oracle's, and the strict modules')
+// takes every elementary function as its value evaluated in double and
+// rounded once to float.  GB300 executes FP64 at a small fraction of its
+// FP32 rate, so per ray these functions are computed here instead with
+// "double-word" arithmetic -- a value carried as an unevaluated sum hi + lo
+// of two floats, with exact products and sums from fma (Dekker 1971, "A
+// floating-point technique for extending the available precision") -- after
+// table-driven argument reductions (Tang 1989, "Table-driven implementation
+// of the exponential function in IEEE floating-point arithmetic"; Tang 1990,
+// "... of the logarithm function").  The double-word result is within about
+// 2^-42 of the true value (relative); Ziv's rounding test (Ziv 1991, "Fast
+// evaluation of elementary mathematical functions with correctly rounded
+// last bit") then rounds both ends of that error interval, and if they round
+// to the same float, that float is the correctly rounded result -- which is
+// also what the double evaluation rounds to, its own error being far smaller
+// than the interval.  Otherwise (about one call in 2^16) the lane evaluates
+// the function in double and rounds once, exactly as the strict modules do.
+// So each function returns the double-then-round value for every input.
+//
+// The functions are written once over a lane type F: float (one value;
+// also compiled for the host, with LG_CRF_HOST, for the CPU tests) or
+// float2 (two rays, with the paired f32x2 instructions).  Every operation is
+// a single IEEE round-to-nearest operation (no contraction is left to the
+// compiler).  Tables: lg_crf_tables.cuh, generated by make_crf_tables.py.
+
+#ifdef LG_CRF_HOST
+#include <cmath>
+#include <cstdint>
+#include <cstring>
+#define LG_CRF_DEV static inline
+#define LG_CRF_COLD static
+#define LG_CRF_TABLE(type, name, n) static const type name[n]
+struct float2 {
+    float x, y;
+};
+struct float4 {
+    float x, y, z, w;
+};
+#else
+#define LG_CRF_DEV static __device__ __forceinline__
+#define LG_CRF_COLD static __device__ __noinline__
+#define LG_CRF_TABLE(type, name, n) __device__ const type name[n]
+#endif
+
+// ------------------------------------------------------------- primitives --
+#ifdef LG_CRF_HOST
+LG_CRF_DEV float crf_add(float a, float b) { return a + b; }
+LG_CRF_DEV float crf_sub(float a, float b) { return a - b; }
+LG_CRF_DEV float crf_mul(float a, float b) { return a * b; }
+LG_CRF_DEV float crf_fma(float a, float b, float c) { return std::fma(a, b, c); }
+LG_CRF_DEV int crf_bits(float a)
+{
+    int i;
+    std::memcpy(&i, &a, 4);
+    return i;
+}
+LG_CRF_DEV float crf_from_bits(int i)
+{
+    float a;
+    std::memcpy(&a, &i, 4);
+    return a;
+}
+// reciprocal estimate: any value within a few ulp of 1/a serves (the
+// double-word steps correct it); the host uses the IEEE quotient
+LG_CRF_DEV float crf_rcp(float a) { return 1.0f / a; }
+// (a test build may count the lanes that take the double path)
+#ifndef LG_CRF_SLOW_COUNT
+#define LG_CRF_SLOW_COUNT()
+#endif
+LG_CRF_DEV float crf_slow_exp(float x) { LG_CRF_SLOW_COUNT(); return (float)std::exp((double)x); }
+LG_CRF_DEV float crf_slow_log(float x) { LG_CRF_SLOW_COUNT(); return (float)std::log((double)x); }
+LG_CRF_DEV float crf_slow_atan(float x) { LG_CRF_SLOW_COUNT(); return (float)std::atan((double)x); }
+LG_CRF_DEV float crf_slow_atanh(float x) { LG_CRF_SLOW_COUNT(); return (float)std::atanh((double)x); }
+#else
+LG_CRF_DEV float crf_add(float a, float b) { return __fadd_rn(a, b); }
+LG_CRF_DEV float crf_sub(float a, float b) { return __fsub_rn(a, b); }
+LG_CRF_DEV float crf_mul(float a, float b) { return __fmul_rn(a, b); }
+LG_CRF_DEV float crf_fma(float a, float b, float c) { return __fmaf_rn(a, b, c); }
+LG_CRF_DEV float2 crf_add(float2 a, float2 b) { return __fadd2_rn(a, b); }
+LG_CRF_DEV float2 crf_sub(float2 a, float2 b) { return __fadd2_rn(a, make_float2(-b.x, -b.y)); }
+LG_CRF_DEV float2 crf_mul(float2 a, float2 b) { return __fmul2_rn(a, b); }
+LG_CRF_DEV float2 crf_fma(float2 a, float2 b, float2 c) { return __ffma2_rn(a, b, c); }
+LG_CRF_DEV int crf_bits(float a) { return __float_as_int(a); }
+LG_CRF_DEV float crf_from_bits(int i) { return __int_as_float(i); }
+// PTX rcp.approx (within about 1 ulp; subnormal results flushed, which
+// the callers tolerate: see each use)
+LG_CRF_DEV float crf_rcp(float a)
+{
+    float r;
+    asm("rcp.approx.ftz.f32 %0, %1;" : "=f"(r) : "f"(a));
+    return r;
+}
+// the lanes the double-word path cannot decide: the function in double,
+// rounded once (out of line: a cold path)
+LG_CRF_COLD float crf_slow_exp(float x) { return (float)exp((double)x); }
+LG_CRF_COLD float crf_slow_log(float x) { return (float)log((double)x); }
+LG_CRF_COLD float crf_slow_atan(float x) { return (float)atan((double)x); }
+LG_CRF_COLD float crf_slow_atanh(float x) { return (float)atanh((double)x); }
+LG_CRF_DEV float crf_get(float2 v, int i) { return i ? v.y : v.x; }
+LG_CRF_DEV void crf_set(float2& v, int i, float s)
+{
+    if (i)
+        v.y = s;
+    else
+        v.x = s;
+}
+template <class T> LG_CRF_DEV T crf_ldg(const T* p) { return __ldg(p); }
+#endif
+
+#ifdef LG_CRF_HOST
+template <class T> LG_CRF_DEV T crf_ldg(const T* p) { return *p; }
+LG_CRF_DEV float crf_fabsf(float a) { return std::fabs(a); }
+#else
+LG_CRF_DEV float crf_fabsf(float a) { return fabsf(a); }
+#endif
+LG_CRF_DEV float crf_get(float v, int) { return v; }
+LG_CRF_DEV void crf_set(float& v, int, float s) { v = s; }
+
+template <class F> struct crf_lanes;
+template <> struct crf_lanes<float> { static const int n = 1; };
+template <> struct crf_lanes<float2> { static const int n = 2; };
+
+LG_CRF_DEV void crf_fill(float& v, float s) { v = s; }
+LG_CRF_DEV void crf_fill(float2& v, float s)
+{
+    v.x = s;
+    v.y = s;
+}
+// s in every lane
+template <class F>
+LG_CRF_DEV F crf_bc(float s)
+{
+    F v;
+    crf_fill(v, s);
+    return v;
+}
+LG_CRF_DEV float crf_neg(float a) { return -a; }
+LG_CRF_DEV float2 crf_neg(float2 a)
+{
+    float2 v;
+    v.x = -a.x;
+    v.y = -a.y;
+    return v;
+}
+LG_CRF_DEV float crf_abs(float a) { return crf_fabsf(a); }
+LG_CRF_DEV float2 crf_abs(float2 a)
+{
+    float2 v;
+    v.x = crf_fabsf(a.x);
+    v.y = crf_fabsf(a.y);
+    return v;
+}
+
+// (the library embeds the tables here for NVRTC, which has no include path)
+#ifndef LG_CRF_TABLES_INLINE
+#include "lg_crf_tables.cuh"
+#endif
+
+// Relative half-width of Ziv's interval: the double-word results of the
+// functions below are within 2^-42 of the true value (bound from the
+// error analysis in each function; tests/test_crfloat.py measures it over
+// all or dense samples of the inputs), so a margin of 2^-40 leaves a factor
+// of 4.
+#ifndef LG_CRF_ZIV
+#define LG_CRF_ZIV (0x1p-40f)
+#endif
+
+// Both ends of [hi + lo - d, hi + lo + d] rounded: equal means the result.
+template <class F>
+LG_CRF_DEV void crf_ziv(F hi, F lo, F& z1, F& z2)
+{
+    const F d = crf_mul(crf_abs(hi), crf_bc<F>(LG_CRF_ZIV));
+    z1 = crf_add(hi, crf_add(lo, d));
+    z2 = crf_add(hi, crf_sub(lo, d));
+}
+
+// ---------------------------------------------------------------------- exp --
+// x = k ln2/64 + r, |r| <= ln2/128 (k = m 64 + j); e^x = 2^m 2^(j/64) e^r.
+// r = x - k L_hi exactly (an fma: the difference is a multiple of 2^-31
+// below 2^-7 in magnitude) minus k L_lo; e^r = 1 + r + r^2/2 + r^3 (1/6 +
+// r/24 + r^2/120) with r = rh + rl, the square of rh exact (fma), rl to
+// first order (it reaches 2^-22), the cubic tail in float.
+// Error: k L_lo rounding and the L_hi + L_lo split (2^-46 at |k| <= 9600),
+// truncation r^6/720 (2^-54), table pairs (2^-48), evaluation (2^-47).
+// Results below 2^-126 are rounded to the subnormal grid from the
+// double-word value directly; e^x rounds to 0 for x <= LG_CRF_EXP_ZERO.
+LG_CRF_COLD float crf_exp_low(float x, float yh0, float yl0, int m)
+{
+    // renormalise the pair (yl0 reaches a few ulp of yh0): |yl| <= ulp(yh)/2
+    const float yh = crf_add(yh0, yl0);
+    const float yl = crf_sub(yl0, crf_sub(yh, yh0));
+    // the result y 2^m with m <= -126 and y < 2^(-126 - m): round y to the
+    // grid g = 2^(-149 - m) with the magic number M = 2^(-126 - m), for
+    // which M + y lies in [M, 2M) where floats are spaced by g
+    const float M = crf_from_bits((1 - m) << 23);
+    const float g = crf_mul(M, 0x1p-23f), h = crf_mul(g, 0.5f);
+    const float a = crf_add(M, yh);
+    const float base = crf_sub(a, M);   // exact
+    const float ea = crf_sub(yh, base);  // exact
+    const float rho = crf_add(ea, yl);
+    const float dd = crf_add(crf_mul(yh, LG_CRF_ZIV), crf_mul(h, 0x1p-22f));
+    const float ar = crf_fabsf(rho);
+    float q;
+    if (ar < crf_sub(h, dd))
+        q = base;
+    else if (ar > crf_add(h, dd))
+        q = crf_add(base, rho > 0.0f ? g : crf_neg(g));
+    else
+        return crf_slow_exp(x);
+    // q 2^m, exactly, in two power-of-two steps (m + 64 >= -87)
+    return crf_mul(crf_mul(q, crf_from_bits((m + 64 + 127) << 23)), 0x1p-64f);
+}
+
+// The double-word e^x 2^-m as yh + yl, and big = k + 1.5 2^23.
+template <class F>
+LG_CRF_DEV void crf_exp_core(F x, F& big, F& yh, F& yl)
+{
+    const F S = crf_bc<F>(0x1.8p23f);
+    big = crf_fma(x, crf_bc<F>(LG_CRF_EXP_INVL), S);  // k + 1.5 2^23 (|k| < 2^22)
+    const F kf = crf_sub(big, S);
+    const F rh = crf_fma(crf_neg(kf), crf_bc<F>(LG_CRF_EXP_LHI), x);
+    const F rl = crf_mul(crf_neg(kf), crf_bc<F>(LG_CRF_EXP_LLO));
+    const F sh = crf_mul(rh, rh);
+    const F sl = crf_fma(rh, rh, crf_neg(sh));
+    const F p3 = crf_fma(crf_fma(rh, crf_bc<F>(0x1.111112p-7f), crf_bc<F>(0x1.555556p-5f)), rh,
+                         crf_bc<F>(0x1.555556p-3f));
+    const F t = crf_mul(crf_mul(sh, rh), p3);
+    const F h = crf_mul(sh, crf_bc<F>(0.5f));
+    // first order in rl (up to 2^-22 at large |k|): rl (1 + rh + rh^2/2)
+    const F small = crf_add(crf_fma(sl, crf_bc<F>(0.5f), crf_fma(h, rl, crf_fma(rh, rl, rl))), t);
+    const F uh = crf_add(rh, h);  // |rh| >= rh^2 / 2: fast two-sum
+    const F ul = crf_add(crf_sub(h, crf_sub(uh, rh)), small);
+    F th, tl;
+#pragma unroll
+    for (int i = 0; i < crf_lanes<F>::n; ++i) {
+        const int k = crf_bits(crf_get(big, i)) - 0x4b400000;
+        const float2 T = crf_ldg(lg_crf_exp_tab + (k & 63));
+        crf_set(th, i, T.x);
+        crf_set(tl, i, T.y);
+    }
+    // T (1 + u) = T + T uh + (T ul + tl uh + tl)
+    const F ph = crf_mul(th, uh);
+    const F pl = crf_fma(th, uh, crf_neg(ph));
+    const F e = crf_add(crf_fma(th, ul, crf_fma(tl, uh, tl)), pl);
+    yh = crf_add(th, ph);  // |th| >= 1 > |ph|: fast two-sum
+    yl = crf_add(crf_sub(ph, crf_sub(yh, th)), e);
+}
+
+template <class F>
+LG_CRF_DEV F lg_crf_exp(F x)
+{
+    F big, yh, yl, z1, z2;
+    crf_exp_core(x, big, yh, yl);
+    crf_ziv(yh, yl, z1, z2);
+    F out;
+#pragma unroll
+    for (int i = 0; i < crf_lanes<F>::n; ++i) {
+        const float xi = crf_get(x, i);
+        float r;
+        if (xi <= 88.0f && xi > LG_CRF_EXP_ZERO) {
+            const int k = crf_bits(crf_get(big, i)) - 0x4b400000;
+            const int m = k >> 6;
+            const float a = crf_get(z1, i);
+            if (m >= -125 || (m == -126 && a >= 1.0f))
+                r = a == crf_get(z2, i) ? crf_from_bits(crf_bits(a) + m * 0x800000) : crf_slow_exp(xi);
+            else
+                r = crf_exp_low(xi, crf_get(yh, i), crf_get(yl, i), m);
+        } else {
+            r = xi <= LG_CRF_EXP_ZERO ? 0.0f : crf_slow_exp(xi);  // NaN, x > 88: in double
+        }
+        crf_set(out, i, r);
+    }
+    return out;
+}
+
+// ---------------------------------------------------------------------- log --
+// log1p of the double-word r = rh + rl (|r| <= 2^-10): r - r^2/2 + r^3
+// (1/3 - r/4 + r^2/5), the square exact; truncation r^6/6 (relative 2^-52
+// where the result is r itself), the cubic term in float (relative to r,
+// 3 roundings of a term below 2^-21.6: 2^-44).  Out: uh + ul.
+template <class F>
+LG_CRF_DEV void crf_log1p_dw(F rh, F rl, F& uh, F& ul)
+{
+    const F sh = crf_mul(rh, rh);
+    const F sl = crf_fma(rh, rh, crf_neg(sh));
+    const F P = crf_fma(crf_fma(rh, crf_bc<F>(0x1.99999ap-3f), crf_bc<F>(-0.25f)), rh, crf_bc<F>(0x1.555556p-2f));
+    const F t = crf_mul(crf_mul(sh, rh), P);
+    // r_lo - r_h r_lo - s_lo / 2 + t
+    const F small = crf_add(crf_fma(crf_neg(rh), rl, rl), crf_fma(sl, crf_bc<F>(-0.5f), t));
+    const F h = crf_mul(sh, crf_bc<F>(-0.5f));
+    uh = crf_add(rh, h);  // |rh| >= rh^2 / 2: fast two-sum
+    ul = crf_add(crf_sub(h, crf_sub(uh, rh)), small);
+}
+
+// ln(u), u = uh + ul > 0 (uh normal, |ul| <= ulp(uh)): u = 2^e m (m in
+// [0.75, 1.5)) and m c_j = 1 + r with c_j from the table of the interval of
+// m (|r| <= 2^-10), so ln u = e ln2 - ln(c_j) + log1p(r).  r = m c_j - 1 is exact as
+// (m_hi c_j - 1) + (the product's rounding error) + m_lo c_j (the first term
+// exactly by Sterbenz); c_j = 1 next to 1, so small logarithms keep their
+// relative accuracy.  Sum: e ln2 as an exact product pair plus e LN2_LO,
+// then two fast two-sums (|e ln2| >= |ln c_j| >= |log1p(r)| or the larger
+// term is zero).  Out: hi + lo.
+template <class F, bool DW>
+LG_CRF_DEV void crf_log_dw(F uh, F ul, F& hi, F& lo)
+{
+    F m, c, Lh, Ll, ef, ml;
+#pragma unroll
+    for (int i = 0; i < crf_lanes<F>::n; ++i) {
+        const int b = crf_bits(crf_get(uh, i));
+        const int t = b - 0x3f400000;
+        const int e = t >> 23;
+        crf_set(m, i, crf_from_bits(b - e * 0x800000));
+        const float4 T = crf_ldg(lg_crf_log_tab + ((t >> 13) & 1023));
+        crf_set(c, i, T.x);
+        crf_set(Lh, i, T.y);
+        crf_set(Ll, i, T.z);
+        // e as float: e + 1.5 2^23 has the bits 0x4b400000 + e
+        crf_set(ef, i, crf_from_bits(0x4b400000 + e) - 0x1.8p23f);
+        if (DW) crf_set(ml, i, crf_get(ul, i) * crf_from_bits((127 - e) << 23));  // exact: ul 2^-e
+    }
+    const F ph = crf_mul(m, c);
+    const F pl = crf_fma(m, c, crf_neg(ph));
+    F rh = crf_sub(ph, crf_bc<F>(1.0f));  // exact
+    F rl;
+    if (DW) {
+        // + m_lo c, then renormalise (two-sum: m_lo can exceed rh)
+        const F q = crf_fma(ml, c, pl);
+        const F s = crf_add(rh, q);
+        const F bb = crf_sub(s, rh);
+        rl = crf_add(crf_sub(rh, crf_sub(s, bb)), crf_sub(q, bb));
+        rh = s;
+    } else {
+        // renormalise: pl (up to 2^-25) would otherwise dominate the
+        // rounding errors of small r (fast two-sum: rh = 0 or |rh| >= 2^-24)
+        const F s = crf_add(rh, pl);
+        rl = crf_sub(pl, crf_sub(s, rh));
+        rh = s;
+    }
+    F vh, vl;
+    crf_log1p_dw(rh, rl, vh, vl);
+    const F a1 = crf_mul(ef, crf_bc<F>(LG_CRF_LN2_HI));
+    const F a1l = crf_fma(ef, crf_bc<F>(LG_CRF_LN2_HI), crf_neg(a1));
+    const F a1l2 = crf_mul(ef, crf_bc<F>(LG_CRF_LN2_LO));
+    const F s1 = crf_add(a1, Lh);
+    const F e1 = crf_sub(Lh, crf_sub(s1, a1));
+    hi = crf_add(s1, vh);
+    const F e2 = crf_sub(vh, crf_sub(hi, s1));
+    lo = crf_add(crf_add(e1, e2), crf_add(crf_add(a1l, a1l2), crf_add(Ll, vl)));
+}
+
+template <class F>
+LG_CRF_DEV F lg_crf_log(F x)
+{
+    F hi, lo, z1, z2;
+    crf_log_dw<F, false>(x, x, hi, lo);
+    crf_ziv(hi, lo, z1, z2);
+    F out;
+#pragma unroll
+    for (int i = 0; i < crf_lanes<F>::n; ++i) {
+        const float xi = crf_get(x, i);
+        // normal, positive, finite x; zero, negative, subnormal, infinite
+        // and NaN x in double
+        const bool common = xi >= 0x1p-126f && xi <= 0x1.fffffep127f;
+        const float a = crf_get(z1, i);
+        crf_set(out, i, common && a == crf_get(z2, i) ? a : crf_slow_log(xi));
+    }
+    return out;
+}
+
+// --------------------------------------------------------------------- atan --
+// a = |z|; t = a, or 1/a (as rcp(a) plus one Newton correction, a double
+// word) for a > 1.  With t_j = j/512 nearest t, atan t = atan t_j +
+// atan(delta), delta = (t - t_j) / (1 + t t_j) as a double word (numerator
+// exact by Sterbenz; denominator 1 + t t_j from an exact product; quotient
+// from rcp plus one correction step), |delta| <= 2^-10, atan(delta) = delta
+// + delta^3 (-1/3 + delta^2/5), truncation delta^7/7 (relative 2^-62), the
+// cubic term in float (relative to delta 2^-44).  For a > 1 the result is
+// pi/2 - that.  Error about 2^-44.
+template <class F>
+LG_CRF_DEV F lg_crf_atan(F z)
+{
+    const F a = crf_abs(z);
+    F r0, rd, th, tl, Ah, Al;
+    bool inv[2];
+#pragma unroll
+    for (int i = 0; i < crf_lanes<F>::n; ++i) {
+        inv[i] = crf_get(a, i) > 1.0f;
+        // 1/a for a > 1 (a > 2^126 flushes to 0; atan is then RN(pi/2))
+        crf_set(r0, i, inv[i] ? crf_rcp(crf_get(a, i)) : 1.0f);
+    }
+    const F rho = crf_fma(crf_neg(r0), a, crf_bc<F>(1.0f));
+    const F r1 = crf_mul(rho, r0);
+#pragma unroll
+    for (int i = 0; i < crf_lanes<F>::n; ++i) {
+        crf_set(th, i, inv[i] ? crf_get(r0, i) : crf_get(a, i));
+        crf_set(tl, i, inv[i] ? crf_get(r1, i) : 0.0f);
+    }
+    const F S = crf_bc<F>(0x1.8p23f);
+    const F big = crf_fma(th, crf_bc<F>(512.0f), S);
+    const F tj = crf_mul(crf_sub(big, S), crf_bc<F>(0x1p-9f));
+#pragma unroll
+    for (int i = 0; i < crf_lanes<F>::n; ++i) {
+        int j = crf_bits(crf_get(big, i)) - 0x4b400000;
+        j = j < 0 ? 0 : (j > 512 ? 512 : j);  // (in range for every finite t in [0, 1])
+        const float2 A = crf_ldg(lg_crf_atan_tab + j);
+        crf_set(Ah, i, A.x);
+        crf_set(Al, i, A.y);
+    }
+    const F nh = crf_sub(th, tj);  // exact
+    const F qh = crf_mul(th, tj);
+    const F ql = crf_fma(th, tj, crf_neg(qh));
+    const F dh = crf_add(crf_bc<F>(1.0f), qh);  // 1 >= qh: fast two-sum
+    const F dl = crf_add(crf_sub(qh, crf_sub(dh, crf_bc<F>(1.0f))), crf_fma(tl, tj, ql));
+#pragma unroll
+    for (int i = 0; i < crf_lanes<F>::n; ++i) crf_set(rd, i, crf_rcp(crf_get(dh, i)));  // dh in [1, 2]
+    const F d0 = crf_mul(nh, rd);
+    const F res = crf_add(crf_fma(crf_neg(d0), dh, nh), crf_fma(crf_neg(d0), dl, tl));
+    const F d1 = crf_mul(res, rd);
+    const F s = crf_mul(d0, d0);
+    const F P = crf_fma(s, crf_bc<F>(0x1.99999ap-3f), crf_bc<F>(-0x1.555556p-2f));
+    const F cub = crf_mul(crf_mul(s, d0), P);
+    const F s1 = crf_add(Ah, d0);  // |atan t_j| >= |delta| or t_j = 0
+    const F e1 = crf_sub(d0, crf_sub(s1, Ah));
+    const F lo = crf_add(crf_add(e1, Al), crf_add(d1, cub));
+    // pi/2 - (s1 + lo)
+    const F ph = crf_sub(crf_bc<F>(LG_CRF_PIO2_HI), s1);
+    const F pe = crf_sub(crf_sub(crf_bc<F>(LG_CRF_PIO2_HI), ph), s1);
+    const F plo = crf_add(pe, crf_sub(crf_bc<F>(LG_CRF_PIO2_LO), lo));
+    F hi2, lo2;
+#pragma unroll
+    for (int i = 0; i < crf_lanes<F>::n; ++i) {
+        crf_set(hi2, i, inv[i] ? crf_get(ph, i) : crf_get(s1, i));
+        crf_set(lo2, i, inv[i] ? crf_get(plo, i) : crf_get(lo, i));
+    }
+    F z1, z2;
+    crf_ziv(hi2, lo2, z1, z2);
+    F out;
+#pragma unroll
+    for (int i = 0; i < crf_lanes<F>::n; ++i) {
+        const float zi = crf_get(z, i);
+        const float w = crf_get(z1, i);
+        // finite z; infinite and NaN z in double
+        const bool ok = crf_fabsf(zi) <= 0x1.fffffep127f && w == crf_get(z2, i);
+        crf_set(out, i, ok ? (zi < 0.0f ? -w : (zi > 0.0f ? w : zi)) : crf_slow_atan(zi));
+    }
+    return out;
+}
+
+// -------------------------------------------------------------------- atanh --
+// atanh v = sign(v) atanh(a), a = |v| < 1, by two formulas:
+//  * a <= 1/16: the odd series a + a^3 (1/3 + a^2/5 + ... + a^8/11),
+//    truncation a^13/13 (relative 2^-51); the cubic term (up to 2^-9.6 of
+//    the result) as a double word: a^3 from exact products, 1/3 as a pair;
+//  * a > 1/16: ln(1 + w) / 2 with w = 2a / (1 - a) >= 1/8 as a double word
+//    (1 - a exact by a fast two-sum, the quotient from rcp plus one
+//    correction step), 1 + w as a two-sum, then the double-word logarithm:
+//    1 + w carries about 2^-49 absolute error, 2^-46 of the result here.
+// Each branch runs only where a lane of the pair needs it (neighbouring
+// rays mostly fall on the same side of 1/16).
+template <class F>
+LG_CRF_DEV F lg_crf_atanh(F v)
+{
+    const F a = crf_abs(v);
+    const F one = crf_bc<F>(1.0f);
+    bool small[2];
+    bool any_small = false, any_large = false;
+#pragma unroll
+    for (int i = 0; i < crf_lanes<F>::n; ++i) {
+        small[i] = crf_get(a, i) <= 0.0625f;
+        any_small = any_small || small[i];
+        any_large = any_large || !small[i];
+    }
+    F hs = a, ls = a, hl = a, ll = a;
+    if (any_small) {
+        const F sh = crf_mul(a, a);
+        const F sl = crf_fma(a, a, crf_neg(sh));
+        const F c3h = crf_mul(sh, a);
+        const F c3l = crf_fma(sl, a, crf_fma(sh, a, crf_neg(c3h)));
+        const F Q = crf_mul(sh, crf_fma(crf_fma(crf_fma(sh, crf_bc<F>(0x1.745d18p-4f), crf_bc<F>(0x1.c71c72p-4f)), sh,
+                                                crf_bc<F>(0x1.24924ap-3f)),
+                                        sh, crf_bc<F>(0x1.99999ap-3f)));
+        // 1/3 = 0x1.555556p-2 - 0x1.555556p-27 (to 2^-50)
+        const F pl = crf_add(crf_bc<F>(-0x1.555556p-27f), Q);
+        const F ch = crf_mul(c3h, crf_bc<F>(0x1.555556p-2f));
+        const F cl = crf_add(crf_fma(c3h, crf_bc<F>(0x1.555556p-2f), crf_neg(ch)),
+                             crf_fma(c3h, pl, crf_mul(c3l, crf_bc<F>(0x1.555556p-2f))));
+        hs = crf_add(a, ch);  // a >= a^3/3: fast two-sum
+        ls = crf_add(crf_sub(ch, crf_sub(hs, a)), cl);
+    }
+    if (any_large) {
+        const F dh = crf_sub(one, a);
+        const F dl = crf_sub(crf_sub(one, dh), a);  // exact (1 >= a)
+        const F n = crf_add(a, a);
+        F rd;
+#pragma unroll
+        for (int i = 0; i < crf_lanes<F>::n; ++i) crf_set(rd, i, crf_rcp(crf_get(dh, i)));  // dh >= 2^-24
+        const F w0 = crf_mul(n, rd);
+        const F res = crf_fma(crf_neg(w0), dl, crf_fma(crf_neg(w0), dh, n));
+        const F w1 = crf_mul(res, rd);
+        // 1 + w0 (two-sum: w0 may exceed 1), + w1
+        const F uh = crf_add(one, w0);
+        const F bb = crf_sub(uh, one);
+        const F ul = crf_add(crf_add(crf_sub(one, crf_sub(uh, bb)), crf_sub(w0, bb)), w1);
+        crf_log_dw<F, true>(uh, ul, hl, ll);
+        hl = crf_mul(hl, crf_bc<F>(0.5f));
+        ll = crf_mul(ll, crf_bc<F>(0.5f));
+    }
+    F hi, lo;
+#pragma unroll
+    for (int i = 0; i < crf_lanes<F>::n; ++i) {
+        crf_set(hi, i, small[i] ? crf_get(hs, i) : crf_get(hl, i));
+        crf_set(lo, i, small[i] ? crf_get(ls, i) : crf_get(ll, i));
+    }
+    F z1, z2;
+    crf_ziv(hi, lo, z1, z2);
+    F out;
+#pragma unroll
+    for (int i = 0; i < crf_lanes<F>::n; ++i) {
+        const float vi = crf_get(v, i);
+        const float w = crf_get(z1, i);
+        // |v| < 1; |v| >= 1 and NaN v in double
+        const bool ok = crf_fabsf(vi) < 1.0f && w == crf_get(z2, i);
+        crf_set(out, i, ok ? (vi < 0.0f ? -w : (vi > 0.0f ? w : vi)) : crf_slow_atanh(vi));
+    }
+    return out;
+}

@@ -296,10 +296,11 @@ LG_DEV double lg_conv_out(int b, int gy, int gx0, const float* acc, float* __res
 }
 
 #if defined(LG_PAIRED) && LG_PSF_W <= 49 && !defined(LG_CONV_SINGLE)
-// Paired rows (fast mode, PSFs up to 49 pixels wide, unless the launch shape
-// asks for single rows -- small tiles for small batches): a thread computes LG_CR columns of two output
-// rows, y and y + LG_CTY/2, with f32x2 fmas, every lane in the scalar
-// kernel's order.  The halo tile holds each input row together with the row
+// Paired rows (fast and exact modes, PSFs up to 49 pixels wide, unless the
+// launch shape asks for single rows -- small tiles for small batches): a
+// thread computes LG_CR columns of two output rows, y and y + LG_CTY/2, with
+// f32x2 instructions (fmas in the fast mode, a product then a sum in the
+// exact mode), every lane in the scalar kernel's order.  The halo tile holds each input row together with the row
 // LG_CTY/2 below it as float2 pairs; pair column c of a row sits at float
 // offset 2c + 4 floor(c/8) and the row pitch is 16 (mod 32) words, so the
 // float4 loads of a quarter warp (four column groups of two rows) fall in
@@ -355,7 +356,7 @@ LG_DEV void lg_conv_tile(const float* __restrict__ raw, float* __restrict__ out,
         for (int i = 0; i < LG_PSF_W; ++i) {
             const float2 p = make_float2(prow[i], prow[i]);
 #pragma unroll
-            for (int o = 0; o < LG_CR; ++o) acc[o] = __ffma2_rn(p, win[o + LG_PSF_W - 1 - i], acc[o]);
+            for (int o = 0; o < LG_CR; ++o) acc[o] = lg_pp_fma(p, win[o + LG_PSF_W - 1 - i], acc[o]);
         }
     }
     float a0[LG_CR], a1[LG_CR];

@@ -320,7 +320,7 @@ LG_DEV double lg_multi_conv_unit_pair(const float* __restrict__ src, const float
         for (int i = 0; i < PW; ++i) {
             const float2 p = make_float2(prow[i], prow[i]);
 #pragma unroll
-            for (int o = 0; o < LG_CR; ++o) acc[o] = __ffma2_rn(p, win[o + PW - 1 - i], acc[o]);
+            for (int o = 0; o < LG_CR; ++o) acc[o] = lg_pp_fma(p, win[o + PW - 1 - i], acc[o]);
         }
     }
     double s0 = 0.0, s1 = 0.0;

@@ -125,6 +125,14 @@ LG_DEV void lg_deflect(float2& y, float2 a)
 struct lg_pair {
     float2 v;  // (ray 0, ray 1)
 };
+// a + b c for a pending product: fused into one fma in the fast mode (as
+// the scalar build contracts it); in the exact mode (LG_EXACT) the product
+// is rounded first, as the reference's operation order without contraction
+#ifdef LG_EXACT
+LG_DEV float2 lg_pp_fma(float2 b, float2 c, float2 a) { return __fadd2_rn(__fmul2_rn(b, c), a); }
+#else
+LG_DEV float2 lg_pp_fma(float2 b, float2 c, float2 a) { return __ffma2_rn(b, c, a); }
+#endif
 // a pending product a * b, fused into an fma by a following + or -
 struct lg_pair_prod {
     float2 a, b;
@@ -157,21 +165,21 @@ LG_DEV lg_pair_prod operator*(lg_pair_prod a, lg_pair_prod b) { return {__fmul2_
 LG_DEV lg_pair operator+(lg_pair a, lg_pair b) { return {__fadd2_rn(a.v, b.v)}; }
 LG_DEV lg_pair operator+(lg_pair a, float b) { return {__fadd2_rn(a.v, lg_bc(b))}; }
 LG_DEV lg_pair operator+(float a, lg_pair b) { return {__fadd2_rn(lg_bc(a), b.v)}; }
-LG_DEV lg_pair operator+(lg_pair_prod p, lg_pair c) { return {__ffma2_rn(p.a, p.b, c.v)}; }
-LG_DEV lg_pair operator+(lg_pair c, lg_pair_prod p) { return {__ffma2_rn(p.a, p.b, c.v)}; }
-LG_DEV lg_pair operator+(lg_pair_prod p, float c) { return {__ffma2_rn(p.a, p.b, lg_bc(c))}; }
-LG_DEV lg_pair operator+(float c, lg_pair_prod p) { return {__ffma2_rn(p.a, p.b, lg_bc(c))}; }
-LG_DEV lg_pair operator+(lg_pair_prod p, lg_pair_prod q) { return {__ffma2_rn(p.a, p.b, __fmul2_rn(q.a, q.b))}; }
+LG_DEV lg_pair operator+(lg_pair_prod p, lg_pair c) { return {lg_pp_fma(p.a, p.b, c.v)}; }
+LG_DEV lg_pair operator+(lg_pair c, lg_pair_prod p) { return {lg_pp_fma(p.a, p.b, c.v)}; }
+LG_DEV lg_pair operator+(lg_pair_prod p, float c) { return {lg_pp_fma(p.a, p.b, lg_bc(c))}; }
+LG_DEV lg_pair operator+(float c, lg_pair_prod p) { return {lg_pp_fma(p.a, p.b, lg_bc(c))}; }
+LG_DEV lg_pair operator+(lg_pair_prod p, lg_pair_prod q) { return {lg_pp_fma(p.a, p.b, __fmul2_rn(q.a, q.b))}; }
 LG_DEV lg_pair operator-(lg_pair a) { return {lg_neg2(a.v)}; }
 LG_DEV lg_pair_prod operator-(lg_pair_prod p) { return {lg_neg2(p.a), p.b}; }
 LG_DEV lg_pair operator-(lg_pair a, lg_pair b) { return {__ffma2_rn(b.v, lg_bc(-1.0f), a.v)}; }
 LG_DEV lg_pair operator-(lg_pair a, float b) { return {__fadd2_rn(a.v, lg_bc(-b))}; }
 LG_DEV lg_pair operator-(float a, lg_pair b) { return {__ffma2_rn(b.v, lg_bc(-1.0f), lg_bc(a))}; }
-LG_DEV lg_pair operator-(lg_pair_prod p, lg_pair c) { return {__ffma2_rn(p.a, p.b, lg_neg2(c.v))}; }
-LG_DEV lg_pair operator-(lg_pair c, lg_pair_prod p) { return {__ffma2_rn(lg_neg2(p.a), p.b, c.v)}; }
-LG_DEV lg_pair operator-(lg_pair_prod p, float c) { return {__ffma2_rn(p.a, p.b, lg_bc(-c))}; }
-LG_DEV lg_pair operator-(float c, lg_pair_prod p) { return {__ffma2_rn(lg_neg2(p.a), p.b, lg_bc(c))}; }
-LG_DEV lg_pair operator-(lg_pair_prod p, lg_pair_prod q) { return {__ffma2_rn(p.a, p.b, lg_neg2(__fmul2_rn(q.a, q.b)))}; }
+LG_DEV lg_pair operator-(lg_pair_prod p, lg_pair c) { return {lg_pp_fma(p.a, p.b, lg_neg2(c.v))}; }
+LG_DEV lg_pair operator-(lg_pair c, lg_pair_prod p) { return {lg_pp_fma(lg_neg2(p.a), p.b, c.v)}; }
+LG_DEV lg_pair operator-(lg_pair_prod p, float c) { return {lg_pp_fma(p.a, p.b, lg_bc(-c))}; }
+LG_DEV lg_pair operator-(float c, lg_pair_prod p) { return {lg_pp_fma(lg_neg2(p.a), p.b, lg_bc(c))}; }
+LG_DEV lg_pair operator-(lg_pair_prod p, lg_pair_prod q) { return {lg_pp_fma(p.a, p.b, lg_neg2(__fmul2_rn(q.a, q.b)))}; }
 // quotients: a times the SFU reciprocal of b (PTX rcp.approx, the
 // definition of div.approx: within 2 ulp for 2^-126 <= |b| <= 2^126)
 LG_DEV float lg_sfu_rcp(float x)
@@ -409,6 +417,7 @@ LG_DEV void lg_deflect(lg_pair2& y, lg_pair2 a)
 // reference's atan2 and sincos to within rounding), phi = 0 at the origin.
 // The one-ray version, which follows the reference's calls, sits with the
 // plugin that uses it (after the strict mode's function mapping).
+#ifndef LG_EXACT
 LG_DEV void lg_polar(lg_pair2 x, lg_pair* r, lg_pair* c, lg_pair* s, lg_pair* c2, lg_pair* s2)
 {
     *r = length(x);
@@ -421,6 +430,7 @@ LG_DEV void lg_polar(lg_pair2 x, lg_pair* r, lg_pair* c, lg_pair* s, lg_pair* c2
     *c2 = cc * cc - ss * ss;
     *s2 = 2.0f * ss * cc;
 }
+#endif  // LG_EXACT (the exact modules follow the reference's atan2 and sincos, objects/epl.cuh)
 
 #endif  // LG_HOST_SET
 

@@ -39,6 +39,14 @@ LG_DEV void lg_polar(float2 x, float* r, float* c, float* s, float* c2, float* s
     sincosf(phi, s, c);
     sincosf(2 * phi, s2, c2);
 }
+#if defined(LG_EXACT) && !defined(LG_HOST_SET)
+// the exact modules trace ray pairs with the one-ray calls, lane by lane
+LG_DEV void lg_polar(lg_pair2 x, lg_pair* r, lg_pair* c, lg_pair* s, lg_pair* c2, lg_pair* s2)
+{
+    lg_polar(lg_lane(x, 0), &r->v.x, &c->v.x, &s->v.x, &c2->v.x, &s2->v.x);
+    lg_polar(lg_lane(x, 1), &r->v.y, &c->v.y, &s->v.y, &c2->v.y, &s2->v.y);
+}
+#endif
 template <class V>
 LG_DEV V lg_epl_frame(const lg_data_epl* __restrict__ o, V x)
 {

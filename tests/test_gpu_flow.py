@@ -226,3 +226,30 @@ def test_gpu_ellipsoid_draws_are_uniform(native):
     x = _draw([([0.05, 0.5, 0.5], np.eye(d) * 0.01, 1.0)], 100000, wrap=[1, 0, 0], seed=5)
     assert np.all((x >= 0) & (x <= 1))
     assert abs(np.mean(x[:, 0] > 0.5) - 5 / 32) < 0.006, np.mean(x[:, 0] > 0.5)
+
+
+def test_tensor_core_inverse_timeout_is_reported_and_survived(native):
+    """wait_tries < 0: every bounded mbarrier wait of the tensor-core inverse
+    gives up at once.  The kernel flags the error and returns (after its own
+    copies and MMA work in flight complete and its tensor memory is freed),
+    with no hang: a retraining reports LG_ERR_TIMEOUT, the same flow then
+    trains normally with the default budget, and a sampler whose flows all
+    time out drops them and finishes on the ellipsoid with the right
+    evidence."""
+    rng = np.random.Generator(np.random.PCG64(3))
+    pts = rng.normal(size=(600, 6))
+    flow = dict(layers=4, width=64, epochs=5)
+    with pytest.raises(lg.LensedError) as e:
+        lg.flow_fit(pts, wait_tries=-1, **flow)
+    assert e.value.code == -5  # LG_ERR_TIMEOUT
+    hist, eff = lg.flow_fit(pts, **flow)  # the device and the library stay usable
+    assert np.all(np.isfinite(hist)) and eff > 0
+    d = 4
+    exact = 2 * math.log(2 * math.pi * 0.15 * 0.01)
+    common = dict(nlive=300, batch=512, seed=9, tol=0.1)
+    r = lg.nested_sample_flow(banana, d, flow_every=300, flow=dict(wait_tries=-1, **flow), **common)
+    plain = lg.nested_sample(banana, d, **common)
+    print(f"timeouts: flow proposals {r['n_flow_proposals']}, lnZ {r['logz']:.3f}+-{r['logz_err']:.3f} "
+          f"(plain {plain['logz']:.3f}, exact {exact:.3f})")
+    assert r["n_flow_proposals"] == 0
+    assert abs(r["logz"] - exact) < 4 * r["logz_err"] + 0.1

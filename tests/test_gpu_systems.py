@@ -45,7 +45,7 @@ def test_systems_reject_bad_counts(native):
 
 def test_systems_with_paired_and_single_row_units(native):
     """PSFs on both sides of the paired-row limit (49 pixels) in one batch:
-    each system still equals its own context, in fast and strict mode."""
+    each system still equals its own context, in every mode."""
     base = _systems(3)
     widths = [15, 51, 25]
     syst = []
@@ -53,7 +53,7 @@ def test_systems_with_paired_and_single_row_units(native):
         psf = workloads.psf_gauss_wings(w, 2.0)
         syst.append((s, psf))
     objs = base[0].objects
-    for flags in (0, lg.LG_FLAG_STRICT_FP):
+    for flags in (0, lg.LG_FLAG_STRICT_FP, lg.LG_FLAG_FAST_MATH):
         S = lg.Systems([(s.image, s.weight, psf, None) for s, psf in syst], objs, capacity=[3] * 3, rule="g3k7",
                        flags=flags)
         params = []

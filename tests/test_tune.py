@@ -22,13 +22,24 @@ def _compile_all(shapes, **kw):
 
 def test_fast_mode_candidates_with_psf_compile(native):
     psf = workloads.psf_gauss_wings(11, 2.0)
-    shapes = lg.tune_candidates(96, 72, OBJS, psf=psf, rule="sub5")
+    fast = lg.LG_FLAG_FAST_MATH
+    shapes = lg.tune_candidates(96, 72, OBJS, psf=psf, rule="sub5", flags=fast)
     render = {(s["rt"], s["rppt"], s["qs"]) for s in shapes}
     conv = {(s["ctx"], s["cty"], s["cr"]) for s in shapes}
     assert (128, 2, 1) in render and any(q > 1 for _, _, q in render)  # quadrature split candidates
     assert len(conv) >= 4 and sum(s["pair_rows"] == 1 for s in shapes) >= 7
     # single-row tiles of four outputs per thread for small batches
     assert any(s["pair_rows"] == 0 and s["cr"] == 4 for s in shapes)
+    _compile_all(shapes, psf=psf, rule="sub5", flags=fast)
+
+
+def test_exact_mode_candidates_pair_rays_and_keep_the_quadrature_order(native):
+    """The default (exact) mode: paired rays and paired convolution rows,
+    but the quadrature sum in the reference's order (split 1)."""
+    psf = workloads.psf_gauss_wings(11, 2.0)
+    shapes = lg.tune_candidates(96, 72, OBJS, psf=psf, rule="sub5")
+    assert shapes and all(s["qs"] == 1 for s in shapes)
+    assert sum(s["pair_rows"] == 1 for s in shapes) >= 5
     _compile_all(shapes, psf=psf, rule="sub5")
 
 
@@ -48,7 +59,8 @@ def test_no_psf_candidates_are_render_only(native):
 
 @pytest.mark.parametrize("bad,flags,psfw", [
     (dict(qs=2), lg.LG_FLAG_STRICT_FP, 11),    # strict mode keeps the quadrature sum in order
-    (dict(qs=3), 0, 11),                        # split of 1, 2, 4 or 8 threads
+    (dict(qs=2), 0, 11),                        # so does the exact mode
+    (dict(qs=3), lg.LG_FLAG_FAST_MATH, 11),     # split of 1, 2, 4 or 8 threads
     (dict(rt=100), 0, 11),                      # whole warps
     (dict(rppt=0), 0, 11),
     (dict(cr=8, ctx=36), 0, 11),                # tile width a multiple of cr
