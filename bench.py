@@ -391,6 +391,7 @@ def main():
     ap.add_argument("--flags", type=int, default=0,
                     help="lg_options.flags: 0 exact (default), 1 strict, 16 fast, 16|4 fast with IEEE div/sqrt")
     ap.add_argument("--no-fast", action="store_true", help="do not time the fast mode beside the exact one")
+    ap.add_argument("--no-plain", action="store_true", help="skip the one-candidate-per-call measurement")
     ap.add_argument("--parity-n", type=int, default=128,
                     help="timed candidates checked against the FP32 oracle (CPU) for the parity block")
     ap.add_argument("--flow-layers", type=int, default=8)
@@ -504,7 +505,7 @@ def main():
     # flow, e.g. MultiNest's callback), on a context created for it
     # (max_batch = 1; its launch shape tuned for one candidate)
     plain, plain_shape, plain_loglike = None, None, None
-    if rank == 0:
+    if rank == 0 and not args.no_plain:
         ctx1 = lg.Context(s.image, s.weight, s.objects, psf=s.psf, rule=s.rule, device=local, max_batch=1,
                           flags=args.flags | (0 if args.no_autotune else lg.LG_FLAG_AUTOTUNE))
         plain_shape = ctx1.launch_shape

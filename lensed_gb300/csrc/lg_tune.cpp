@@ -59,11 +59,13 @@ bool fp_ieee(int flags) { return fp_mode(flags) != Fp::FAST || (flags & LG_FLAG_
 
 std::vector<Shape> render_candidates(const Shape& base, Fp mode)
 {
-    // (threads, pixels per group, quadrature split); the exact and strict
-    // modes keep the quadrature sum in order (split 1)
+    // (threads, pixels per group, quadrature split); the strict mode keeps
+    // one quadrature point per step (split 1); the exact mode splits with an
+    // ordered sum
     static const int fast[][3] = {{128, 2, 1}, {256, 2, 1}, {64, 2, 1}, {128, 4, 1}, {128, 2, 2}, {256, 2, 2},
                                   {128, 2, 4}, {128, 2, 8}};
-    static const int exact[][3] = {{128, 2, 1}, {256, 2, 1}, {64, 2, 1}, {128, 4, 1}, {64, 4, 1}};
+    static const int exact[][3] = {{128, 2, 1}, {256, 2, 1}, {64, 2, 1}, {128, 4, 1}, {128, 2, 2}, {128, 2, 4},
+                                   {128, 2, 8}};
     static const int scalar[][3] = {{128, 2, 1}, {256, 2, 1}, {64, 2, 1}, {128, 1, 1}, {128, 4, 1}};
     const int(*tab)[3] = mode == Fp::FAST ? fast : (mode == Fp::EXACT ? exact : scalar);
     const int n = mode == Fp::FAST ? (int)(sizeof fast / sizeof fast[0])
@@ -123,7 +125,9 @@ std::string check_shape(const Shape& s, Fp mode, bool psf, int psfw)
     if (s.rt < 32 || s.rt > 1024 || s.rt % 32) return "render threads must be a multiple of 32 in [32, 1024]";
     if (s.rppt < 1 || s.rppt > 8) return "pixels per thread group must be in [1, 8]";
     if (s.qs != 1 && s.qs != 2 && s.qs != 4 && s.qs != 8) return "quadrature split must be 1, 2, 4 or 8";
-    if (mode != Fp::FAST && s.qs != 1) return "the exact and strict modes keep the quadrature sum in order (split 1)";
+    if (strict && s.qs != 1) return "strict mode keeps the quadrature sum in order (split 1)";
+    if (mode == Fp::EXACT && s.qs != 1 && s.rppt % 2)
+        return "the exact mode splits the quadrature of pixel pairs only (even pixels per group)";
     if (!psf) return "";
     if (s.cr != 4 && s.cr != 8 && s.cr != 16) return "convolution outputs per thread must be 4, 8 or 16";
     if (s.ctx < s.cr || s.ctx % s.cr || s.ctx > 256) return "convolution tile width must be a multiple of cr";

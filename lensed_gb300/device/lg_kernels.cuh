@@ -28,8 +28,9 @@
 #define LG_RPPT 2
 #endif
 // quadrature split: LG_QS adjacent threads share a thread's pixels, each
-// taking every LG_QS-th quadrature point (fast mode only: the split changes
-// the order of the quadrature sum)
+// taking every LG_QS-th quadrature point (fast mode: partial sums combined
+// by a butterfly, which reorders the quadrature sum; exact mode: the values
+// gathered and summed in the rule's order)
 #ifndef LG_QS
 #define LG_QS 1
 #endif
@@ -152,6 +153,31 @@ LG_DEV void lg_render_tile(const lg_model* __restrict__ models, float* __restric
         pv[j] = lg_pair_of(0.0f);
         pe[j] = lg_pair_of(0.0f);
     }
+#if defined(LG_EXACT) && LG_QS > 1
+    // exact mode with a quadrature split: the threads of a group evaluate
+    // every LG_QS-th point, the values meet in shared memory, and every
+    // lane of the group sums all of them in the rule's order -- the sum the
+    // unsplit kernel forms, bit for bit
+    __shared__ float2 lg_fq[LG_RT][(LG_Q + LG_QS - 1) / LG_QS][LG_RPPT / 2];
+#pragma unroll 1
+    for (int n = sub, kq = 0; n < LG_Q; n += LG_QS, ++kq) {
+        const float2 q = lg_qq[n];
+#pragma unroll
+        for (int j = 0; j < LG_RPPT / 2; ++j) lg_fq[threadIdx.x][kq][j] = lg_compute2(m, lg_pair2{px[j] + q.x, py[j] + q.y}).v;
+    }
+    __syncwarp();
+#pragma unroll 1
+    for (int n = 0; n < LG_Q; ++n) {
+        const float2 w = lg_ww[n];
+        const int src = grp * LG_QS + n % LG_QS;
+#pragma unroll
+        for (int j = 0; j < LG_RPPT / 2; ++j) {
+            const lg_pair f = {lg_fq[src][n / LG_QS][j]};
+            pv[j] += w.x * f;
+            if (MODE == 2) pe[j] += w.y * f;
+        }
+    }
+#else
 #pragma unroll 1
     for (int n = sub; n < LG_Q; n += LG_QS) {
         const float2 q = lg_qq[n];
@@ -163,6 +189,7 @@ LG_DEV void lg_render_tile(const lg_model* __restrict__ models, float* __restric
             if (MODE == 2) pe[j] += w.y * f;
         }
     }
+#endif
 #pragma unroll
     for (int j = 0; j < LG_RPPT / 2; ++j) {
         v[2 * j] = pv[j].v.x;
@@ -183,6 +210,7 @@ LG_DEV void lg_render_tile(const lg_model* __restrict__ models, float* __restric
         }
     }
 #endif
+#ifndef LG_EXACT
     if (LG_QS > 1) {
 #pragma unroll
         for (int j = 0; j < LG_RPPT; ++j) {
@@ -190,6 +218,7 @@ LG_DEV void lg_render_tile(const lg_model* __restrict__ models, float* __restric
             if (MODE == 2) e[j] = lg_qs_sum(e[j]);
         }
     }
+#endif
     if (MODE == 1) {
         __shared__ double red[LG_RT / 32];
         double s = 0.0;

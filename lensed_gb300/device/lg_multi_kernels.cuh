@@ -138,6 +138,27 @@ LG_DEV void lg_multi_render_body(const lg_model* __restrict__ models, const lg_s
             py[j] = lg_pair_of(xp[2 * j].y, xp[2 * j + 1].y);
             pv[j] = lg_pair_of(0.0f);
         }
+#if defined(LG_EXACT) && LG_QS > 1
+        // exact mode with a quadrature split: values gathered in shared
+        // memory and summed in the rule's order (as the single-system kernel)
+        __shared__ float2 lg_fq[LG_RT][(LG_Q + LG_QS - 1) / LG_QS][LG_RPPT / 2];
+        __syncwarp();  // the previous unit's reads of lg_fq are done
+#pragma unroll 1
+        for (int n = sub, kq = 0; n < LG_Q; n += LG_QS, ++kq) {
+            const float2 q = lg_qq[n];
+#pragma unroll
+            for (int j = 0; j < LG_RPPT / 2; ++j)
+                lg_fq[threadIdx.x][kq][j] = lg_compute2(m, lg_pair2{px[j] + q.x, py[j] + q.y}).v;
+        }
+        __syncwarp();
+#pragma unroll 1
+        for (int n = 0; n < LG_Q; ++n) {
+            const float2 w = lg_ww[n];
+            const int src = grp * LG_QS + n % LG_QS;
+#pragma unroll
+            for (int j = 0; j < LG_RPPT / 2; ++j) pv[j] += w.x * lg_pair{lg_fq[src][n / LG_QS][j]};
+        }
+#else
 #pragma unroll 1
         for (int n = sub; n < LG_Q; n += LG_QS) {
             const float2 q = lg_qq[n];
@@ -145,6 +166,7 @@ LG_DEV void lg_multi_render_body(const lg_model* __restrict__ models, const lg_s
 #pragma unroll
             for (int j = 0; j < LG_RPPT / 2; ++j) pv[j] += w.x * lg_compute2(m, lg_pair2{px[j] + q.x, py[j] + q.y});
         }
+#endif
 #pragma unroll
         for (int j = 0; j < LG_RPPT / 2; ++j) {
             v[2 * j] = pv[j].v.x;
@@ -159,10 +181,12 @@ LG_DEV void lg_multi_render_body(const lg_model* __restrict__ models, const lg_s
             for (int j = 0; j < LG_RPPT; ++j) v[j] += w.x * lg_compute(m, xp[j] + q);
         }
 #endif
+#ifndef LG_EXACT
         if (LG_QS > 1) {
 #pragma unroll
             for (int j = 0; j < LG_RPPT; ++j) v[j] = lg_qs_sum(v[j]);
         }
+#endif
         if (WITH_PSF) {
 #pragma unroll
             for (int j = 0; j < LG_RPPT; ++j) {

@@ -456,6 +456,25 @@ def test_host_set_params_match_the_set_module(native):
         ctx.close()
 
 
+def test_host_set_params_on_many_prior_draws(native):
+    """10^4 unit-cube draws of the benchmarked model: small batches (object
+    data and prior transform on the host, the C library's double functions)
+    against the batched path (set_params kernel, CUDA's double functions).
+    The two round each elementary function's double value to float, so they
+    can differ only where that value lies within about 2^-52 of a float
+    rounding boundary; the test counts such candidates (expected none)."""
+    s = workloads.config2()
+    ctx = lg.Context(s.image, s.weight, s.objects, psf=s.psf, rule=s.rule, max_batch=1024)
+    assert ctx.host_set
+    cube = np.random.Generator(np.random.PCG64(31)).random((10000, ctx.ndims))
+    batch = np.concatenate([ctx.eval_cube(cube[i:i + 1024])[0] for i in range(0, 10000, 1024)])
+    small = np.concatenate([ctx.eval_cube(cube[i:i + 4])[0] for i in range(0, 10000, 4)])
+    same = (batch == small) | (np.isnan(batch) & np.isnan(small))
+    print(f"host vs kernel set_params: {int((~same).sum())} of 10000 prior draws differ")
+    assert same.all()
+    ctx.close()
+
+
 def test_cube_transform_and_reference_callback(native):
     s = workloads.small()
     ctx = lg.Context(s.image, s.weight, s.objects, rule=s.rule, max_batch=16)

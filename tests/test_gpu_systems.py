@@ -66,3 +66,41 @@ def test_systems_with_paired_and_single_row_units(native):
             ctx = lg.Context(s.image, s.weight, s.objects, psf=psf, rule="g3k7", max_batch=3, flags=flags)
             assert np.array_equal(g, ctx.eval_batch(p)), (s.name, flags)
             ctx.close()
+
+
+@pytest.mark.parametrize("flags", [0, lg.LG_FLAG_FAST_MATH])
+def test_systems_full_size_against_the_oracle(native, flags):
+    """The uneven multi-system workload at full size (16 systems of 64^2 to
+    512^2, EPL + shear with slopes t in [0.8, 1.2], Sersic, sky, odd PSFs of
+    15 to 31 pixels, 49-point g3k7 rule), two candidates per system through
+    the persistent multi-system launch, against the FP32 oracle of each
+    system: |dlogL| <= 1e-3 in the default (exact) mode, the fast mode's
+    widened bound 1e-3 + 2e-6 |logL| with LG_FLAG_FAST_MATH; the distance to
+    the FP64 oracle is printed."""
+    from lensed_gb300 import quadrature
+    from oracle.oracle import Oracle
+
+    syst = workloads.systems()
+    S = lg.Systems([(s.image, s.weight, s.psf, None) for s in syst], syst[0].objects, capacity=[2] * len(syst),
+                   rule="g3k7", flags=flags)
+    cands, params = [], []
+    for k, s in enumerate(syst):
+        ctx = lg.Context(s.image, s.weight, s.objects, psf=s.psf, rule=s.rule, max_batch=2, flags=flags)
+        c = workloads.draw_candidates(s, 2, seed=40 + k)
+        cands.append(c)
+        params.append(ctx.to_map_order(c))
+        ctx.close()
+    got = S.eval(params)
+    worst = 0.0
+    for s, c, g in zip(syst, cands, got):
+        kw = dict(psf=s.psf, image=s.image, weight=s.weight, threads=16)
+        w32 = Oracle(s.plugins, s.width, s.height, quadrature.rule(s.rule), precision=32, **kw).loglike(c)
+        w64 = Oracle(s.plugins, s.width, s.height, quadrature.rule(s.rule), precision=64, **kw).loglike(c)
+        d = np.abs(g - w32)
+        tol = 1e-3 if not flags else 1e-3 + 2e-6 * np.abs(w32)
+        print(f"{s.name}: |dlogL| vs FP32 oracle {np.array2string(d, precision=2)}, vs FP64 "
+              f"{np.array2string(np.abs(g - w64), precision=2)}, FP32 oracle vs FP64 "
+              f"{np.array2string(np.abs(w32 - w64), precision=2)}")
+        assert np.all(d <= tol), (s.name, d)
+        worst = max(worst, d.max())
+    print(f"16 systems, {'fast' if flags else 'exact'} mode: max |dlogL| vs FP32 oracle {worst:.3g}")

@@ -11,9 +11,10 @@ sky; 96x72 image so that tiles are ragged in both directions; 11x11 PSF;
   * with a quadrature split (fast mode only) the FP32 quadrature sum is
     reordered: images within 1e-5 relative and logL within the fast-mode
     tolerance of the FP32 oracle (1e-3 + 2e-6 |logL|);
-  * exact (default) and strict modes: every candidate gives images identical
-    to the oracle-pinned default, and the exact mode's equal the strict
-    mode's;
+  * exact (default) and strict modes: every candidate (the exact mode's
+    quadrature splits included: they sum in the rule's order) gives images
+    identical to the oracle-pinned default, and the exact mode's equal the
+    strict mode's;
   * the autotuner picks one of its candidates, caches the choice in the
     process and in the LG_TUNE_CACHE file, and its results meet the same
     tolerances; the multi-system kernels likewise.
@@ -111,6 +112,8 @@ def test_every_exact_and_strict_candidate_shape(native, flags):
         strict.close()
     shapes = lg.tune_candidates(W, H, objs, psf=psf, rule="sub5", flags=flags)
     assert len(shapes) >= 5
+    if not flags:
+        assert any(s["qs"] > 1 for s in shapes)  # ordered splits: still identical images
     for s in shapes:
         ctx.set_launch_shape(**s)
         model, raw, err = ctx.render(p[0])
@@ -118,7 +121,7 @@ def test_every_exact_and_strict_candidate_shape(native, flags):
         assert np.array_equal(model, base_model), s
         assert np.allclose(ctx.eval_batch(p), base_logl, rtol=1e-12, atol=0), s
     with pytest.raises(lg.LensedError):
-        ctx.set_launch_shape(qs=2)  # the exact and strict modes keep the quadrature order
+        ctx.set_launch_shape(qs=2, rppt=1)  # no split of single pixels (exact), no split at all (strict)
     assert ctx.launch_shape == shapes[-1]  # unchanged by the rejected call
 
 
@@ -187,8 +190,8 @@ MULTI_CONV = [(32, 32, 8), (32, 16, 8), (64, 32, 8), (64, 16, 8), (32, 32, 16), 
 
 
 def test_systems_shapes_and_autotune(native):
-    """Fast mode (where the quadrature split exists); the tuned exact
-    systems keep the quadrature order and match the untuned ones."""
+    """Fast mode (quadrature splits reorder the sum); the tuned exact
+    systems (ordered splits) match the untuned ones bit for bit."""
     syst = workloads.systems(count=4)
     objs = syst[0].objects
     S = lg.Systems([(s.image, s.weight, s.psf, None) for s in syst], objs, capacity=[6] * 4, rule="g3k7",
@@ -218,7 +221,6 @@ def test_systems_shapes_and_autotune(native):
     E = lg.Systems([(s.image, s.weight, s.psf, None) for s in syst], objs, capacity=[6] * 4, rule="g3k7")
     TE = lg.Systems([(s.image, s.weight, s.psf, None) for s in syst], objs, capacity=[6] * 4, rule="g3k7",
                     flags=lg.LG_FLAG_AUTOTUNE)
-    assert TE.launch_shape["qs"] == 1
     ex = np.concatenate(E.eval(params))
     assert np.allclose(np.concatenate(TE.eval(params)), ex, rtol=1e-12, atol=0)
     with pytest.raises(lg.LensedError):

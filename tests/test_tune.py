@@ -34,11 +34,11 @@ def test_fast_mode_candidates_with_psf_compile(native):
 
 
 def test_exact_mode_candidates_pair_rays_and_keep_the_quadrature_order(native):
-    """The default (exact) mode: paired rays and paired convolution rows,
-    but the quadrature sum in the reference's order (split 1)."""
+    """The default (exact) mode: paired rays and paired convolution rows;
+    quadrature splits sum the gathered values in the rule's order."""
     psf = workloads.psf_gauss_wings(11, 2.0)
     shapes = lg.tune_candidates(96, 72, OBJS, psf=psf, rule="sub5")
-    assert shapes and all(s["qs"] == 1 for s in shapes)
+    assert shapes and any(s["qs"] > 1 for s in shapes) and all(s["rppt"] % 2 == 0 for s in shapes if s["qs"] > 1)
     assert sum(s["pair_rows"] == 1 for s in shapes) >= 5
     _compile_all(shapes, psf=psf, rule="sub5")
 
@@ -59,7 +59,7 @@ def test_no_psf_candidates_are_render_only(native):
 
 @pytest.mark.parametrize("bad,flags,psfw", [
     (dict(qs=2), lg.LG_FLAG_STRICT_FP, 11),    # strict mode keeps the quadrature sum in order
-    (dict(qs=2), 0, 11),                        # so does the exact mode
+    (dict(qs=2, rppt=1), 0, 11),                # the exact mode splits pixel pairs only
     (dict(qs=3), lg.LG_FLAG_FAST_MATH, 11),     # split of 1, 2, 4 or 8 threads
     (dict(rt=100), 0, 11),                      # whole warps
     (dict(rppt=0), 0, 11),
