@@ -104,9 +104,10 @@ std::vector<Shape> conv_candidates(const Shape& base, bool multi)
         out.push_back(s);
     }
     if (!multi && base.pair_rows) {
-        // single-row tiles of four outputs per thread: the most threads for a
-        // batch of one or a few candidates (same per-pixel arithmetic)
-        static const int small[][3] = {{32, 16, 4}, {16, 16, 4}};
+        // single-row tiles of two or four outputs per thread: the most
+        // threads for a batch of one or a few candidates (same per-pixel
+        // arithmetic)
+        static const int small[][3] = {{32, 16, 4}, {16, 16, 4}, {32, 8, 2}, {16, 16, 2}};
         for (const auto& c : small) {
             Shape s = base;
             s.ctx = c[0];
@@ -129,7 +130,7 @@ std::string check_shape(const Shape& s, Fp mode, bool psf, int psfw)
     if (mode == Fp::EXACT && s.qs != 1 && s.rppt % 2)
         return "the exact mode splits the quadrature of pixel pairs only (even pixels per group)";
     if (!psf) return "";
-    if (s.cr != 4 && s.cr != 8 && s.cr != 16) return "convolution outputs per thread must be 4, 8 or 16";
+    if (s.cr != 2 && s.cr != 4 && s.cr != 8 && s.cr != 16) return "convolution outputs per thread must be 2, 4, 8 or 16";
     if (s.ctx < s.cr || s.ctx % s.cr || s.ctx > 256) return "convolution tile width must be a multiple of cr";
     if (s.pair_rows && (strict || psfw > 49)) return "paired rows need the fast or exact mode and a PSF up to 49 wide";
     if (s.pair_rows && (s.cr % 8 || s.cty % 2)) return "paired rows need cr % 8 == 0 and an even tile height";

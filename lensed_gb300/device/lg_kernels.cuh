@@ -404,7 +404,15 @@ LG_DEV void lg_conv_tile(const float* __restrict__ raw, float* __restrict__ out,
     }
 }
 #else
-#define LG_WIN4 ((LG_CR + LG_PSF_W - 1 + 3) / 4 * 4)
+// a thread's window of LG_CR + PW - 1 inputs is read as float4 (LG_CR a
+// multiple of 4) or float2 (LG_CR = 2: a thread's first input sits at an
+// even offset, 8-byte aligned)
+#if LG_CR % 4 == 0
+#define LG_WVEC 4
+#else
+#define LG_WVEC 2
+#endif
+#define LG_WIN4 ((LG_CR + LG_PSF_W - 1 + LG_WVEC - 1) / LG_WVEC * LG_WVEC)
 #define LG_TW_NEED (LG_CTX - LG_CR + LG_WIN4)
 // row pitch = 4 (mod 32) words: the float4 loads of a quarter warp (two
 // rows of four threads) then fall in distinct banks
@@ -439,8 +447,9 @@ LG_DEV void lg_conv_tile(const float* __restrict__ raw, float* __restrict__ out,
     for (int o = 0; o < LG_CR; ++o) acc[o] = 0.0f;
 #pragma unroll 1
     for (int j = 0; j < LG_PSF_H; ++j) {
-        const float4* row = reinterpret_cast<const float4*>(tile + (ly + LG_PSF_H - 1 - j) * LG_TWP + lx0);
         float win[LG_WIN4];
+#if LG_WVEC == 4
+        const float4* row = reinterpret_cast<const float4*>(tile + (ly + LG_PSF_H - 1 - j) * LG_TWP + lx0);
 #pragma unroll
         for (int t = 0; t < LG_WIN4 / 4; ++t) {
             const float4 q = row[t];
@@ -449,6 +458,15 @@ LG_DEV void lg_conv_tile(const float* __restrict__ raw, float* __restrict__ out,
             win[4 * t + 2] = q.z;
             win[4 * t + 3] = q.w;
         }
+#else
+        const float2* row = reinterpret_cast<const float2*>(tile + (ly + LG_PSF_H - 1 - j) * LG_TWP + lx0);
+#pragma unroll
+        for (int t = 0; t < LG_WIN4 / 2; ++t) {
+            const float2 q = row[t];
+            win[2 * t + 0] = q.x;
+            win[2 * t + 1] = q.y;
+        }
+#endif
         const float* prow = lg_psf + j * LG_PSF_W;
 #pragma unroll
         for (int i = 0; i < LG_PSF_W; ++i) {

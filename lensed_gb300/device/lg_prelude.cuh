@@ -4,9 +4,9 @@
 // It provides the vocabulary the plugins are written in: float2 arithmetic,
 // the 2x2 matrix type and its product (kernel/constants.cl:23-35), the
 // OpenCL-style vector helpers dot/length/normalize, and the constants of
-// kernel/constants.cl:6-13.  Arithmetic is IEEE single precision with
-// correctly rounded division and square root; the build enables FMA
-// contraction unless the context asks for strict parity mode.
+// kernel/constants.cl:6-13.  Arithmetic is IEEE single precision; the fast
+// mode's build enables FMA contraction and hardware-approximate division and
+// square root, the exact and strict modes' builds neither.
 
 #define LG_LENS 'L'
 #define LG_SOURCE 'S'
@@ -114,14 +114,15 @@ LG_DEV void lg_deflect(float2& y, float2 a)
 
 #ifndef LG_HOST_SET
 // ------------------------------------------------------------ ray pairs --
-// The evaluation module of the fast mode traces two rays per thread at once
-// with Blackwell's paired single-precision instructions (add/mul/fma on
-// f32x2): lg_pair holds the value of one scalar for both rays, lg_pair2 a
-// 2-vector for both rays.  Each lane is computed exactly as the scalar code
-// computes it (the same IEEE operations; a product followed by a sum is
-// fused into one fma, as the scalar build contracts it).  The plugins'
-// evaluation functions are templates over the vector type V (float2 or
-// lg_pair2) and are written once for both.
+// The evaluation modules of the fast and exact modes trace two rays per
+// thread at once with Blackwell's paired single-precision instructions
+// (add/mul/fma on f32x2): lg_pair holds the value of one scalar for both
+// rays, lg_pair2 a 2-vector for both rays.  Each lane is computed exactly as
+// the scalar code of the same mode computes it (the same IEEE operations; a
+// product followed by a sum is fused into one fma in the fast mode, as its
+// scalar build contracts it, and rounded before the sum in the exact mode).
+// The plugins' evaluation functions are templates over the vector type V
+// (float2 or lg_pair2) and are written once for both.
 struct lg_pair {
     float2 v;  // (ray 0, ray 1)
 };
