@@ -28,18 +28,19 @@ __device__ float crf_double(int fn, float x)
                      : (float)atanh((double)x);
 }
 
-// bit patterns lo + 2 i (the pair: lo + 2i, lo + 2i + 1) below hi; counts
-// lanes whose bits differ from the double evaluation (NaN equal to NaN),
-// and keeps the first few
+// every bit pattern u in [lo, hi) as lane 0 of a pair whose lane 1 is an
+// unrelated input (u times an odd constant, a bijection of the 32-bit
+// patterns), so that the lanes of a pair take different paths and table
+// entries; counts lanes whose bits differ from the double evaluation (NaN
+// equal to NaN), and keeps the first few
 __global__ void lg_crf_sweep_kernel(int fn, unsigned long long lo, unsigned long long hi,
                                     unsigned long long* __restrict__ bad, unsigned* __restrict__ first, int nfirst)
 {
-    const unsigned long long stride = 2ull * gridDim.x * blockDim.x;
+    const unsigned long long stride = (unsigned long long)gridDim.x * blockDim.x;
     unsigned long long nbad = 0;
-    for (unsigned long long u = lo + 2ull * (blockIdx.x * (unsigned long long)blockDim.x + threadIdx.x); u < hi;
-         u += stride) {
+    for (unsigned long long u = lo + blockIdx.x * (unsigned long long)blockDim.x + threadIdx.x; u < hi; u += stride) {
         const float x0 = __uint_as_float((unsigned)u);
-        const float x1 = __uint_as_float((unsigned)(u + 1 < hi ? u + 1 : u));
+        const float x1 = __uint_as_float((unsigned)u * 0x9E3779B1u);
         const float2 r = crf_pair(fn, make_float2(x0, x1));
         const float w0 = crf_double(fn, x0), w1 = crf_double(fn, x1);
         const bool ok0 = __float_as_uint(r.x) == __float_as_uint(w0) || (r.x != r.x && w0 != w0);
@@ -47,7 +48,7 @@ __global__ void lg_crf_sweep_kernel(int fn, unsigned long long lo, unsigned long
         if (!ok0 || !ok1) {
             nbad += (!ok0) + (!ok1);
             const unsigned long long k = atomicAdd(bad + 1, 1ull);
-            if (k < (unsigned long long)nfirst) first[k] = ok0 ? (unsigned)(u + 1) : (unsigned)u;
+            if (k < (unsigned long long)nfirst) first[k] = ok0 ? __float_as_uint(x1) : (unsigned)u;
         }
     }
     if (nbad) atomicAdd(bad, nbad);

@@ -64,12 +64,33 @@ LG_CRF_DEV float crf_from_bits(int i)
     return a;
 }
 // reciprocal estimate: any value within a few ulp of 1/a serves (the
-// double-word steps correct it); the host uses the IEEE quotient
-LG_CRF_DEV float crf_rcp(float a) { return 1.0f / a; }
+// double-word steps correct it); the host uses the IEEE quotient unless a
+// test build substitutes a perturbed one (to stand in for the device's
+// approximate reciprocal)
+#ifndef LG_CRF_HOST_RCP
+#define LG_CRF_HOST_RCP(a) (1.0f / (a))
+#endif
+LG_CRF_DEV float crf_rcp(float a) { return LG_CRF_HOST_RCP(a); }
 // (a test build may count the lanes that take the double path)
 #ifndef LG_CRF_SLOW_COUNT
 #define LG_CRF_SLOW_COUNT()
 #endif
+// integer fields of the arguments' bit patterns (see the device versions)
+LG_CRF_DEV void crf_log_fields(int b, int& e, int& j, int& mb)
+{
+    const int t = b - 0x3f400000;
+    e = t >> 23;
+    j = (t >> 13) & 1023;
+    mb = b - e * 0x800000;
+}
+LG_CRF_DEV void crf_exp_fields(int bits, int& j, int& m)
+{
+    const int k = bits - 0x4b400000;
+    j = k & 63;
+    m = k >> 6;
+}
+LG_CRF_DEV int crf_pow2_bits(int e) { return (e + 127) * 0x800000; }   // bits of 2^e (normal e)
+LG_CRF_DEV int crf_add_exp(int bits, int m) { return bits + m * 0x800000; }
 LG_CRF_DEV float crf_slow_exp(float x) { LG_CRF_SLOW_COUNT(); return (float)std::exp((double)x); }
 LG_CRF_DEV float crf_slow_log(float x) { LG_CRF_SLOW_COUNT(); return (float)std::log((double)x); }
 LG_CRF_DEV float crf_slow_atan(float x) { LG_CRF_SLOW_COUNT(); return (float)std::atan((double)x); }
@@ -79,9 +100,13 @@ LG_CRF_DEV float crf_add(float a, float b) { return __fadd_rn(a, b); }
 LG_CRF_DEV float crf_sub(float a, float b) { return __fsub_rn(a, b); }
 LG_CRF_DEV float crf_mul(float a, float b) { return __fmul_rn(a, b); }
 LG_CRF_DEV float crf_fma(float a, float b, float c) { return __fmaf_rn(a, b, c); }
+// paired operations: add and fma on f32x2; products lane by lane, because
+// with CUDA 13.0 the assembler fused an f32x2 multiply into the following
+// f32x2 add (scalar round-to-nearest multiplies are never fused), and the
+// double-word steps are written for separately rounded products
 LG_CRF_DEV float2 crf_add(float2 a, float2 b) { return __fadd2_rn(a, b); }
 LG_CRF_DEV float2 crf_sub(float2 a, float2 b) { return __fadd2_rn(a, make_float2(-b.x, -b.y)); }
-LG_CRF_DEV float2 crf_mul(float2 a, float2 b) { return __fmul2_rn(a, b); }
+LG_CRF_DEV float2 crf_mul(float2 a, float2 b) { return make_float2(__fmul_rn(a.x, b.x), __fmul_rn(a.y, b.y)); }
 LG_CRF_DEV float2 crf_fma(float2 a, float2 b, float2 c) { return __ffma2_rn(a, b, c); }
 LG_CRF_DEV int crf_bits(float a) { return __float_as_int(a); }
 LG_CRF_DEV float crf_from_bits(int i) { return __int_as_float(i); }
@@ -91,6 +116,39 @@ LG_CRF_DEV float crf_rcp(float a)
 {
     float r;
     asm("rcp.approx.ftz.f32 %0, %1;" : "=f"(r) : "f"(a));
+    return r;
+}
+// Integer fields of the arguments' bit patterns, in inline PTX: with CUDA
+// 13.0 the optimizer was seen to miscompute such per-lane shifts of paired
+// values (a lane's t >> 23 came out as t), and an asm block is opaque to it.
+//   log: t = b - bits(0.75); e = t >> 23 (arithmetic); j = (t >> 13) & 1023;
+//        mb = b - e 2^23 (the mantissa scaled into [0.75, 1.5))
+LG_CRF_DEV void crf_log_fields(int b, int& e, int& j, int& mb)
+{
+    asm("{\n.reg .s32 t, x;\nsub.s32 t, %3, 0x3f400000;\nshr.s32 %0, t, 23;\nshr.s32 x, t, 13;\n"
+        "and.b32 %1, x, 1023;\nshl.b32 x, %0, 23;\nsub.s32 %2, %3, x;\n}"
+        : "=r"(e), "=r"(j), "=r"(mb)
+        : "r"(b));
+}
+//   exp: k = bits - bits(1.5 2^23); j = k & 63; m = k >> 6 (arithmetic)
+LG_CRF_DEV void crf_exp_fields(int bits, int& j, int& m)
+{
+    asm("{\n.reg .s32 k;\nsub.s32 k, %2, 0x4b400000;\nand.b32 %0, k, 63;\nshr.s32 %1, k, 6;\n}"
+        : "=r"(j), "=r"(m)
+        : "r"(bits));
+}
+// bits of 2^e for a normal power of two, and bits + m 2^23 (a float scaled
+// by 2^m while it stays normal)
+LG_CRF_DEV int crf_pow2_bits(int e)
+{
+    int r;
+    asm("{\n.reg .s32 x;\nadd.s32 x, %1, 127;\nshl.b32 %0, x, 23;\n}" : "=r"(r) : "r"(e));
+    return r;
+}
+LG_CRF_DEV int crf_add_exp(int bits, int m)
+{
+    int r;
+    asm("{\n.reg .s32 x;\nshl.b32 x, %2, 23;\nadd.s32 %0, %1, x;\n}" : "=r"(r) : "r"(bits), "r"(m));
     return r;
 }
 // the lanes the double-word path cannot decide: the function in double,
@@ -195,7 +253,7 @@ LG_CRF_COLD float crf_exp_low(float x, float yh0, float yl0, int m)
     // the result y 2^m with m <= -126 and y < 2^(-126 - m): round y to the
     // grid g = 2^(-149 - m) with the magic number M = 2^(-126 - m), for
     // which M + y lies in [M, 2M) where floats are spaced by g
-    const float M = crf_from_bits((1 - m) << 23);
+    const float M = crf_from_bits(crf_pow2_bits(-126 - m));
     const float g = crf_mul(M, 0x1p-23f), h = crf_mul(g, 0.5f);
     const float a = crf_add(M, yh);
     const float base = crf_sub(a, M);   // exact
@@ -211,7 +269,7 @@ LG_CRF_COLD float crf_exp_low(float x, float yh0, float yl0, int m)
     else
         return crf_slow_exp(x);
     // q 2^m, exactly, in two power-of-two steps (m + 64 >= -87)
-    return crf_mul(crf_mul(q, crf_from_bits((m + 64 + 127) << 23)), 0x1p-64f);
+    return crf_mul(crf_mul(q, crf_from_bits(crf_pow2_bits(m + 64))), 0x1p-64f);
 }
 
 // The double-word e^x 2^-m as yh + yl, and big = k + 1.5 2^23.
@@ -236,8 +294,9 @@ LG_CRF_DEV void crf_exp_core(F x, F& big, F& yh, F& yl)
     F th, tl;
 #pragma unroll
     for (int i = 0; i < crf_lanes<F>::n; ++i) {
-        const int k = crf_bits(crf_get(big, i)) - 0x4b400000;
-        const float2 T = crf_ldg(lg_crf_exp_tab + (k & 63));
+        int j, m;
+        crf_exp_fields(crf_bits(crf_get(big, i)), j, m);
+        const float2 T = crf_ldg(lg_crf_exp_tab + j);
         crf_set(th, i, T.x);
         crf_set(tl, i, T.y);
     }
@@ -261,11 +320,11 @@ LG_CRF_DEV F lg_crf_exp(F x)
         const float xi = crf_get(x, i);
         float r;
         if (xi <= 88.0f && xi > LG_CRF_EXP_ZERO) {
-            const int k = crf_bits(crf_get(big, i)) - 0x4b400000;
-            const int m = k >> 6;
+            int j, m;
+            crf_exp_fields(crf_bits(crf_get(big, i)), j, m);
             const float a = crf_get(z1, i);
             if (m >= -125 || (m == -126 && a >= 1.0f))
-                r = a == crf_get(z2, i) ? crf_from_bits(crf_bits(a) + m * 0x800000) : crf_slow_exp(xi);
+                r = a == crf_get(z2, i) ? crf_from_bits(crf_add_exp(crf_bits(a), m)) : crf_slow_exp(xi);
             else
                 r = crf_exp_low(xi, crf_get(yh, i), crf_get(yl, i), m);
         } else {
@@ -309,17 +368,16 @@ LG_CRF_DEV void crf_log_dw(F uh, F ul, F& hi, F& lo)
     F m, c, Lh, Ll, ef, ml;
 #pragma unroll
     for (int i = 0; i < crf_lanes<F>::n; ++i) {
-        const int b = crf_bits(crf_get(uh, i));
-        const int t = b - 0x3f400000;
-        const int e = t >> 23;
-        crf_set(m, i, crf_from_bits(b - e * 0x800000));
-        const float4 T = crf_ldg(lg_crf_log_tab + ((t >> 13) & 1023));
+        int e, j, mb;
+        crf_log_fields(crf_bits(crf_get(uh, i)), e, j, mb);
+        crf_set(m, i, crf_from_bits(mb));
+        const float4 T = crf_ldg(lg_crf_log_tab + j);
         crf_set(c, i, T.x);
         crf_set(Lh, i, T.y);
         crf_set(Ll, i, T.z);
         // e as float: e + 1.5 2^23 has the bits 0x4b400000 + e
         crf_set(ef, i, crf_from_bits(0x4b400000 + e) - 0x1.8p23f);
-        if (DW) crf_set(ml, i, crf_get(ul, i) * crf_from_bits((127 - e) << 23));  // exact: ul 2^-e
+        if (DW) crf_set(ml, i, crf_get(ul, i) * crf_from_bits(crf_pow2_bits(-e)));  // exact: ul 2^-e
     }
     const F ph = crf_mul(m, c);
     const F pl = crf_fma(m, c, crf_neg(ph));

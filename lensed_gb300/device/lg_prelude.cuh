@@ -126,18 +126,33 @@ LG_DEV void lg_deflect(float2& y, float2 a)
 struct lg_pair {
     float2 v;  // (ray 0, ray 1)
 };
+// Paired single-precision add, multiply and fma.  In the exact modules a
+// product must be rounded before the sum that uses it; with CUDA 13.0 the
+// assembler fused an f32x2 multiply into the following f32x2 add (the
+// intrinsics and explicit-rounding PTX alike, also without contraction
+// enabled), while scalar round-to-nearest multiplies are never fused.  So
+// the exact modules multiply lane by lane (__fmul_rn) and keep the paired
+// add and fma; the fast modules use the paired intrinsics throughout.
+#ifdef LG_EXACT
+LG_DEV float2 lg_mul2(float2 a, float2 b) { return make_float2(__fmul_rn(a.x, b.x), __fmul_rn(a.y, b.y)); }
+#else
+LG_DEV float2 lg_mul2(float2 a, float2 b) { return __fmul2_rn(a, b); }
+#endif
+LG_DEV float2 lg_add2(float2 a, float2 b) { return __fadd2_rn(a, b); }
+LG_DEV float2 lg_fma2(float2 a, float2 b, float2 c) { return __ffma2_rn(a, b, c); }
+
 // a + b c for a pending product: fused into one fma in the fast mode (as
 // the scalar build contracts it); in the exact mode (LG_EXACT) the product
 // is rounded first, as the reference's operation order without contraction
 #ifdef LG_EXACT
-LG_DEV float2 lg_pp_fma(float2 b, float2 c, float2 a) { return __fadd2_rn(__fmul2_rn(b, c), a); }
+LG_DEV float2 lg_pp_fma(float2 b, float2 c, float2 a) { return lg_add2(lg_mul2(b, c), a); }
 #else
-LG_DEV float2 lg_pp_fma(float2 b, float2 c, float2 a) { return __ffma2_rn(b, c, a); }
+LG_DEV float2 lg_pp_fma(float2 b, float2 c, float2 a) { return lg_fma2(b, c, a); }
 #endif
 // a pending product a * b, fused into an fma by a following + or -
 struct lg_pair_prod {
     float2 a, b;
-    LG_DEV_MEMBER operator lg_pair() const { return lg_pair{__fmul2_rn(a, b)}; }
+    LG_DEV_MEMBER operator lg_pair() const { return lg_pair{lg_mul2(a, b)}; }
 };
 struct lg_pair2 {
     lg_pair x, y;
@@ -157,30 +172,30 @@ LG_DEV float2 lg_neg2(float2 a) { return make_float2(-a.x, -a.y); }
 LG_DEV lg_pair_prod operator*(lg_pair a, lg_pair b) { return {a.v, b.v}; }
 LG_DEV lg_pair_prod operator*(float a, lg_pair b) { return {lg_bc(a), b.v}; }
 LG_DEV lg_pair_prod operator*(lg_pair a, float b) { return {a.v, lg_bc(b)}; }
-LG_DEV lg_pair_prod operator*(lg_pair_prod a, lg_pair b) { return {__fmul2_rn(a.a, a.b), b.v}; }
-LG_DEV lg_pair_prod operator*(lg_pair a, lg_pair_prod b) { return {a.v, __fmul2_rn(b.a, b.b)}; }
-LG_DEV lg_pair_prod operator*(lg_pair_prod a, float b) { return {__fmul2_rn(a.a, a.b), lg_bc(b)}; }
-LG_DEV lg_pair_prod operator*(float a, lg_pair_prod b) { return {lg_bc(a), __fmul2_rn(b.a, b.b)}; }
-LG_DEV lg_pair_prod operator*(lg_pair_prod a, lg_pair_prod b) { return {__fmul2_rn(a.a, a.b), __fmul2_rn(b.a, b.b)}; }
+LG_DEV lg_pair_prod operator*(lg_pair_prod a, lg_pair b) { return {lg_mul2(a.a, a.b), b.v}; }
+LG_DEV lg_pair_prod operator*(lg_pair a, lg_pair_prod b) { return {a.v, lg_mul2(b.a, b.b)}; }
+LG_DEV lg_pair_prod operator*(lg_pair_prod a, float b) { return {lg_mul2(a.a, a.b), lg_bc(b)}; }
+LG_DEV lg_pair_prod operator*(float a, lg_pair_prod b) { return {lg_bc(a), lg_mul2(b.a, b.b)}; }
+LG_DEV lg_pair_prod operator*(lg_pair_prod a, lg_pair_prod b) { return {lg_mul2(a.a, a.b), lg_mul2(b.a, b.b)}; }
 // sums and differences (a product on either side is fused)
-LG_DEV lg_pair operator+(lg_pair a, lg_pair b) { return {__fadd2_rn(a.v, b.v)}; }
-LG_DEV lg_pair operator+(lg_pair a, float b) { return {__fadd2_rn(a.v, lg_bc(b))}; }
-LG_DEV lg_pair operator+(float a, lg_pair b) { return {__fadd2_rn(lg_bc(a), b.v)}; }
+LG_DEV lg_pair operator+(lg_pair a, lg_pair b) { return {lg_add2(a.v, b.v)}; }
+LG_DEV lg_pair operator+(lg_pair a, float b) { return {lg_add2(a.v, lg_bc(b))}; }
+LG_DEV lg_pair operator+(float a, lg_pair b) { return {lg_add2(lg_bc(a), b.v)}; }
 LG_DEV lg_pair operator+(lg_pair_prod p, lg_pair c) { return {lg_pp_fma(p.a, p.b, c.v)}; }
 LG_DEV lg_pair operator+(lg_pair c, lg_pair_prod p) { return {lg_pp_fma(p.a, p.b, c.v)}; }
 LG_DEV lg_pair operator+(lg_pair_prod p, float c) { return {lg_pp_fma(p.a, p.b, lg_bc(c))}; }
 LG_DEV lg_pair operator+(float c, lg_pair_prod p) { return {lg_pp_fma(p.a, p.b, lg_bc(c))}; }
-LG_DEV lg_pair operator+(lg_pair_prod p, lg_pair_prod q) { return {lg_pp_fma(p.a, p.b, __fmul2_rn(q.a, q.b))}; }
+LG_DEV lg_pair operator+(lg_pair_prod p, lg_pair_prod q) { return {lg_pp_fma(p.a, p.b, lg_mul2(q.a, q.b))}; }
 LG_DEV lg_pair operator-(lg_pair a) { return {lg_neg2(a.v)}; }
 LG_DEV lg_pair_prod operator-(lg_pair_prod p) { return {lg_neg2(p.a), p.b}; }
-LG_DEV lg_pair operator-(lg_pair a, lg_pair b) { return {__ffma2_rn(b.v, lg_bc(-1.0f), a.v)}; }
-LG_DEV lg_pair operator-(lg_pair a, float b) { return {__fadd2_rn(a.v, lg_bc(-b))}; }
-LG_DEV lg_pair operator-(float a, lg_pair b) { return {__ffma2_rn(b.v, lg_bc(-1.0f), lg_bc(a))}; }
+LG_DEV lg_pair operator-(lg_pair a, lg_pair b) { return {lg_fma2(b.v, lg_bc(-1.0f), a.v)}; }
+LG_DEV lg_pair operator-(lg_pair a, float b) { return {lg_add2(a.v, lg_bc(-b))}; }
+LG_DEV lg_pair operator-(float a, lg_pair b) { return {lg_fma2(b.v, lg_bc(-1.0f), lg_bc(a))}; }
 LG_DEV lg_pair operator-(lg_pair_prod p, lg_pair c) { return {lg_pp_fma(p.a, p.b, lg_neg2(c.v))}; }
 LG_DEV lg_pair operator-(lg_pair c, lg_pair_prod p) { return {lg_pp_fma(lg_neg2(p.a), p.b, c.v)}; }
 LG_DEV lg_pair operator-(lg_pair_prod p, float c) { return {lg_pp_fma(p.a, p.b, lg_bc(-c))}; }
 LG_DEV lg_pair operator-(float c, lg_pair_prod p) { return {lg_pp_fma(lg_neg2(p.a), p.b, lg_bc(c))}; }
-LG_DEV lg_pair operator-(lg_pair_prod p, lg_pair_prod q) { return {lg_pp_fma(p.a, p.b, lg_neg2(__fmul2_rn(q.a, q.b)))}; }
+LG_DEV lg_pair operator-(lg_pair_prod p, lg_pair_prod q) { return {lg_pp_fma(p.a, p.b, lg_neg2(lg_mul2(q.a, q.b)))}; }
 // quotients: a times the SFU reciprocal of b (PTX rcp.approx, the
 // definition of div.approx: within 2 ulp for 2^-126 <= |b| <= 2^126)
 LG_DEV float lg_sfu_rcp(float x)
@@ -208,9 +223,9 @@ LG_DEV lg_pair operator/(lg_pair a, lg_pair b) { return {make_float2(a.v.x / b.v
 LG_DEV lg_pair operator/(lg_pair a, float b) { return {make_float2(a.v.x / b, a.v.y / b)}; }
 LG_DEV lg_pair operator/(float a, lg_pair b) { return {make_float2(a / b.v.x, a / b.v.y)}; }
 #else
-LG_DEV lg_pair operator/(lg_pair a, lg_pair b) { return {__fmul2_rn(a.v, lg_rcp(b).v)}; }
-LG_DEV lg_pair operator/(lg_pair a, float b) { return {__fmul2_rn(a.v, lg_bc(lg_sfu_rcp(b)))}; }
-LG_DEV lg_pair operator/(float a, lg_pair b) { return {__fmul2_rn(lg_bc(a), lg_rcp(b).v)}; }
+LG_DEV lg_pair operator/(lg_pair a, lg_pair b) { return {lg_mul2(a.v, lg_rcp(b).v)}; }
+LG_DEV lg_pair operator/(lg_pair a, float b) { return {lg_mul2(a.v, lg_bc(lg_sfu_rcp(b)))}; }
+LG_DEV lg_pair operator/(float a, lg_pair b) { return {lg_mul2(lg_bc(a), lg_rcp(b).v)}; }
 #endif
 LG_DEV lg_pair operator/(lg_pair_prod a, lg_pair b) { return lg_pair(a) / b; }
 LG_DEV lg_pair operator/(lg_pair_prod a, float b) { return lg_pair(a) / b; }
@@ -272,10 +287,10 @@ LG_DEV float lg_exp_pick(float t, float p, float r) { return fabsf(t) < 128.0f ?
 LG_DEV lg_pair expf(lg_pair x)
 {
     const float2 L = lg_bc(0x1.715476p+0f), Llo = lg_bc(0x1.4ae0c0p-26f);
-    const float2 t = __fmul2_rn(x.v, L);
-    const float2 c = __ffma2_rn(x.v, Llo, __ffma2_rn(x.v, L, lg_neg2(t)));
+    const float2 t = lg_mul2(x.v, L);
+    const float2 c = lg_fma2(x.v, Llo, lg_fma2(x.v, L, lg_neg2(t)));
     const float2 p = make_float2(lg_sfu_ex2(t.x), lg_sfu_ex2(t.y));
-    const float2 r = __ffma2_rn(p, __fmul2_rn(c, lg_bc(0x1.62e430p-1f)), p);
+    const float2 r = lg_fma2(p, lg_mul2(c, lg_bc(0x1.62e430p-1f)), p);
     return {make_float2(lg_exp_pick(t.x, p.x, r.x), lg_exp_pick(t.y, p.y, r.y))};
 }
 LG_DEV lg_pair expf(lg_pair_prod x) { return expf(lg_pair(x)); }
@@ -289,8 +304,8 @@ LG_DEV lg_pair logf(lg_pair x)
 {
     const float2 y = make_float2(lg_sfu_lg2(x.v.x), lg_sfu_lg2(x.v.y));
     const float2 s = make_float2(lg_sfu_ex2(-y.x), lg_sfu_ex2(-y.y));
-    const float2 u = __fmul2_rn(y, lg_bc(0x1.62e430p-1f));
-    const float2 r = __ffma2_rn(y, lg_bc(0x1.62e430p-1f), __ffma2_rn(x.v, s, lg_bc(-1.0f)));
+    const float2 u = lg_mul2(y, lg_bc(0x1.62e430p-1f));
+    const float2 r = lg_fma2(y, lg_bc(0x1.62e430p-1f), lg_fma2(x.v, s, lg_bc(-1.0f)));
     return {make_float2(fabsf(y.x) < 120.0f ? r.x : u.x, fabsf(y.y) < 120.0f ? r.y : u.y)};
 }
 LG_DEV lg_pair logf(lg_pair_prod x) { return logf(lg_pair(x)); }
@@ -330,18 +345,18 @@ LG_DEV lg_pair atanf(lg_pair z)
     const float2 a = lg_abs2(z.v);
     const bool b0 = a.x > 1.0f, b1 = a.y > 1.0f;
     const float2 r = make_float2(b0 ? lg_sfu_rcp(a.x) : a.x, b1 ? lg_sfu_rcp(a.y) : a.y);
-    const float2 s = __fmul2_rn(r, r);
+    const float2 s = lg_mul2(r, r);
     float2 p = lg_bc(-0x1.cbc208p-10f);
-    p = __ffma2_rn(p, s, lg_bc(0x1.5f7ca4p-7f));
-    p = __ffma2_rn(p, s, lg_bc(-0x1.f8b096p-6f));
-    p = __ffma2_rn(p, s, lg_bc(0x1.d775dep-5f));
-    p = __ffma2_rn(p, s, lg_bc(-0x1.57220ap-4f));
-    p = __ffma2_rn(p, s, lg_bc(0x1.c02f58p-4f));
-    p = __ffma2_rn(p, s, lg_bc(-0x1.241596p-3f));
-    p = __ffma2_rn(p, s, lg_bc(0x1.999082p-3f));
-    p = __ffma2_rn(p, s, lg_bc(-0x1.555534p-2f));
-    p = __ffma2_rn(__fmul2_rn(p, s), r, r);  // r + r s P'(s)
-    const float2 q = __ffma2_rn(p, lg_bc(-1.0f), lg_bc(LG_PI_HALF));
+    p = lg_fma2(p, s, lg_bc(0x1.5f7ca4p-7f));
+    p = lg_fma2(p, s, lg_bc(-0x1.f8b096p-6f));
+    p = lg_fma2(p, s, lg_bc(0x1.d775dep-5f));
+    p = lg_fma2(p, s, lg_bc(-0x1.57220ap-4f));
+    p = lg_fma2(p, s, lg_bc(0x1.c02f58p-4f));
+    p = lg_fma2(p, s, lg_bc(-0x1.241596p-3f));
+    p = lg_fma2(p, s, lg_bc(0x1.999082p-3f));
+    p = lg_fma2(p, s, lg_bc(-0x1.555534p-2f));
+    p = lg_fma2(lg_mul2(p, s), r, r);  // r + r s P'(s)
+    const float2 q = lg_fma2(p, lg_bc(-1.0f), lg_bc(LG_PI_HALF));
     return {lg_copysign2(make_float2(b0 ? q.x : p.x, b1 ? q.y : p.y), z.v)};
 }
 LG_DEV lg_pair atanf(lg_pair_prod z) { return atanf(lg_pair(z)); }
@@ -360,20 +375,20 @@ LG_DEV lg_pair atanhf(lg_pair v)
     const bool small0 = a.x <= 0.5f, small1 = a.y <= 0.5f;
     float2 p = a, h = a;
     if (small0 || small1) {
-        const float2 s = __fmul2_rn(a, a);
+        const float2 s = lg_mul2(a, a);
         p = lg_bc(0x1.6dad62p-3f);
-        p = __ffma2_rn(p, s, lg_bc(0x1.986234p-5f));
-        p = __ffma2_rn(p, s, lg_bc(0x1.e6379cp-4f));
-        p = __ffma2_rn(p, s, lg_bc(0x1.2323c0p-3f));
-        p = __ffma2_rn(p, s, lg_bc(0x1.99a96cp-3f));
-        p = __ffma2_rn(p, s, lg_bc(0x1.555534p-2f));
-        p = __ffma2_rn(__fmul2_rn(p, s), a, a);  // a + a s Q'(s)
+        p = lg_fma2(p, s, lg_bc(0x1.986234p-5f));
+        p = lg_fma2(p, s, lg_bc(0x1.e6379cp-4f));
+        p = lg_fma2(p, s, lg_bc(0x1.2323c0p-3f));
+        p = lg_fma2(p, s, lg_bc(0x1.99a96cp-3f));
+        p = lg_fma2(p, s, lg_bc(0x1.555534p-2f));
+        p = lg_fma2(lg_mul2(p, s), a, a);  // a + a s Q'(s)
     }
     if (!(small0 && small1)) {
-        const float2 num = __fadd2_rn(lg_bc(1.0f), a);
-        const float2 den = __ffma2_rn(a, lg_bc(-1.0f), lg_bc(1.0f));
-        const lg_pair l = logf(lg_pair{__fmul2_rn(num, make_float2(lg_sfu_rcp(den.x), lg_sfu_rcp(den.y)))});
-        h = __fmul2_rn(l.v, lg_bc(0.5f));
+        const float2 num = lg_add2(lg_bc(1.0f), a);
+        const float2 den = lg_fma2(a, lg_bc(-1.0f), lg_bc(1.0f));
+        const lg_pair l = logf(lg_pair{lg_mul2(num, make_float2(lg_sfu_rcp(den.x), lg_sfu_rcp(den.y)))});
+        h = lg_mul2(l.v, lg_bc(0.5f));
     }
     return {lg_copysign2(make_float2(small0 ? p.x : h.x, small1 ? p.y : h.y), v.v)};
 }

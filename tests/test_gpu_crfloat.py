@@ -1,9 +1,14 @@
 """The correctly rounded exp, log, atan and atanh of the exact evaluation
 modules on the GPU, as ray pairs (f32x2 instructions, rcp.approx
-estimates): for every one of the 2^32 float inputs the result equals the
-function evaluated in double on the device and rounded once (NaN matches
-NaN) -- the strict modules' per-ray semantics, which the exact modules must
-reproduce bit for bit."""
+estimates): for every one of the 2^32 float inputs, paired with an
+unrelated second input (so that the two lanes take different paths and
+table entries), the result equals the function evaluated in double on the
+device and rounded once (NaN matches NaN) -- the strict modules' per-ray
+semantics, which the exact modules must reproduce bit for bit.  The count
+is over both lanes; the double evaluation itself is within 1-2 double ulp,
+so a handful of inputs whose exact value lies within about 2^-51 of a float
+rounding boundary could differ without either side being wrong: the test
+allows none, and reports any."""
 import ctypes as C
 
 import numpy as np

@@ -310,9 +310,9 @@ def test_loglike_config2_fast_ieee_division(native):
 
 @pytest.mark.parametrize("name", ["small", "config2"])
 def test_loglike_exact_equals_strict(native, name):
-    """The exact and strict modes give the same logL bit for bit (their
-    images are identical and so is the summation), within 1e-6 of the
-    oracle's (FP64 summation order only)."""
+    """The exact and strict modes give the same images, so their logL differ
+    only by the grouping of the FP64 partial sums of their launch shapes
+    (about 1e-15 relative), and lie within 1e-6 of the oracle's."""
     s = getattr(workloads, name)()
     cand = workloads.draw_candidates(s, 8, seed=5)
     o = Oracle(s.plugins, s.width, s.height, quadrature.rule(s.rule), psf=s.psf, image=s.image, weight=s.weight,
@@ -325,7 +325,7 @@ def test_loglike_exact_equals_strict(native, name):
         d = _report(f"{name} {mode}", got[mode], want, want)
         assert d.max() <= 1e-6
         ctx.close()
-    assert np.array_equal(got["exact"], got["strict"])
+    assert np.allclose(got["exact"], got["strict"], rtol=1e-12, atol=0)
 
 
 def test_batch_equals_single_and_is_deterministic(native):

@@ -108,7 +108,7 @@ def test_every_exact_and_strict_candidate_shape(native, flags):
         s_model, s_raw, s_err = strict.render(p[0])
         assert np.array_equal(base_raw, s_raw) and np.array_equal(base_err, s_err)
         assert np.array_equal(base_model, s_model)
-        assert np.array_equal(base_logl, strict.eval_batch(p))
+        assert np.allclose(base_logl, strict.eval_batch(p), rtol=1e-12, atol=0)  # FP64 summation grouping
         strict.close()
     shapes = lg.tune_candidates(W, H, objs, psf=psf, rule="sub5", flags=flags)
     assert len(shapes) >= 5
