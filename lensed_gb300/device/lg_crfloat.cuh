@@ -171,8 +171,10 @@ template <class T> LG_CRF_DEV T crf_ldg(const T* p) { return __ldg(p); }
 #ifdef LG_CRF_HOST
 template <class T> LG_CRF_DEV T crf_ldg(const T* p) { return *p; }
 LG_CRF_DEV float crf_fabsf(float a) { return std::fabs(a); }
+LG_CRF_DEV float crf_copysignf(float a, float b) { return std::copysign(a, b); }
 #else
 LG_CRF_DEV float crf_fabsf(float a) { return fabsf(a); }
+LG_CRF_DEV float crf_copysignf(float a, float b) { return copysignf(a, b); }
 #endif
 LG_CRF_DEV float crf_get(float v, int) { return v; }
 LG_CRF_DEV void crf_set(float& v, int, float s) { v = s; }
@@ -226,13 +228,25 @@ LG_CRF_DEV float2 crf_abs(float2 a)
 #define LG_CRF_ZIV (0x1p-40f)
 #endif
 
-// Both ends of [hi + lo - d, hi + lo + d] rounded: equal means the result.
+// Both ends of [hi + lo - d, hi + lo + d], d = |hi| 2^-40, rounded: equal
+// means the result.  (lo +- hi 2^-40 from an fma: the product is exact, a
+// power-of-two scaling; for negative hi the two ends swap, which the
+// equality test does not mind.)
 template <class F>
 LG_CRF_DEV void crf_ziv(F hi, F lo, F& z1, F& z2)
 {
-    const F d = crf_mul(crf_abs(hi), crf_bc<F>(LG_CRF_ZIV));
-    z1 = crf_add(hi, crf_add(lo, d));
-    z2 = crf_add(hi, crf_sub(lo, d));
+    z1 = crf_add(hi, crf_fma(hi, crf_bc<F>(LG_CRF_ZIV), lo));
+    z2 = crf_add(hi, crf_fma(hi, crf_bc<F>(-LG_CRF_ZIV), lo));
+}
+
+// every lane of v satisfies ok
+template <class F>
+LG_CRF_DEV bool crf_all(const bool (&ok)[2])
+{
+    bool a = true;
+#pragma unroll
+    for (int i = 0; i < crf_lanes<F>::n; ++i) a = a && ok[i];
+    return a;
 }
 
 // ---------------------------------------------------------------------- exp --
@@ -272,9 +286,9 @@ LG_CRF_COLD float crf_exp_low(float x, float yh0, float yl0, int m)
     return crf_mul(crf_mul(q, crf_from_bits(crf_pow2_bits(m + 64))), 0x1p-64f);
 }
 
-// The double-word e^x 2^-m as yh + yl, and big = k + 1.5 2^23.
+// The double-word e^x 2^-m as yh + yl, big = k + 1.5 2^23, and m per lane.
 template <class F>
-LG_CRF_DEV void crf_exp_core(F x, F& big, F& yh, F& yl)
+LG_CRF_DEV void crf_exp_core(F x, F& big, F& yh, F& yl, int (&mm)[2])
 {
     const F S = crf_bc<F>(0x1.8p23f);
     big = crf_fma(x, crf_bc<F>(LG_CRF_EXP_INVL), S);  // k + 1.5 2^23 (|k| < 2^22)
@@ -294,8 +308,8 @@ LG_CRF_DEV void crf_exp_core(F x, F& big, F& yh, F& yl)
     F th, tl;
 #pragma unroll
     for (int i = 0; i < crf_lanes<F>::n; ++i) {
-        int j, m;
-        crf_exp_fields(crf_bits(crf_get(big, i)), j, m);
+        int j;
+        crf_exp_fields(crf_bits(crf_get(big, i)), j, mm[i]);
         const float2 T = crf_ldg(lg_crf_exp_tab + j);
         crf_set(th, i, T.x);
         crf_set(tl, i, T.y);
@@ -312,21 +326,34 @@ template <class F>
 LG_CRF_DEV F lg_crf_exp(F x)
 {
     F big, yh, yl, z1, z2;
-    crf_exp_core(x, big, yh, yl);
+    int m[2];
+    crf_exp_core(x, big, yh, yl, m);
     crf_ziv(yh, yl, z1, z2);
     F out;
+    // the common case for the whole pair: x in [-87, 88] (a normal result,
+    // so m >= -125 or m = -126 with z1 >= 1) and the rounding decided
+    bool ok[2];
+#pragma unroll
+    for (int i = 0; i < crf_lanes<F>::n; ++i) {
+        const float xi = crf_get(x, i);
+        ok[i] = xi >= -87.0f && xi <= 88.0f && crf_get(z1, i) == crf_get(z2, i);
+    }
+    if (crf_all<F>(ok)) {
+#pragma unroll
+        for (int i = 0; i < crf_lanes<F>::n; ++i)
+            crf_set(out, i, crf_from_bits(crf_add_exp(crf_bits(crf_get(z1, i)), m[i])));
+        return out;
+    }
 #pragma unroll
     for (int i = 0; i < crf_lanes<F>::n; ++i) {
         const float xi = crf_get(x, i);
         float r;
         if (xi <= 88.0f && xi > LG_CRF_EXP_ZERO) {
-            int j, m;
-            crf_exp_fields(crf_bits(crf_get(big, i)), j, m);
             const float a = crf_get(z1, i);
-            if (m >= -125 || (m == -126 && a >= 1.0f))
-                r = a == crf_get(z2, i) ? crf_from_bits(crf_add_exp(crf_bits(a), m)) : crf_slow_exp(xi);
+            if (m[i] >= -125 || (m[i] == -126 && a >= 1.0f))
+                r = a == crf_get(z2, i) ? crf_from_bits(crf_add_exp(crf_bits(a), m[i])) : crf_slow_exp(xi);
             else
-                r = crf_exp_low(xi, crf_get(yh, i), crf_get(yl, i), m);
+                r = crf_exp_low(xi, crf_get(yh, i), crf_get(yl, i), m[i]);
         } else {
             r = xi <= LG_CRF_EXP_ZERO ? 0.0f : crf_slow_exp(xi);  // NaN, x > 88: in double
         }
@@ -415,16 +442,18 @@ LG_CRF_DEV F lg_crf_log(F x)
     F hi, lo, z1, z2;
     crf_log_dw<F, false>(x, x, hi, lo);
     crf_ziv(hi, lo, z1, z2);
-    F out;
+    // normal, positive, finite x with the rounding decided; zero, negative,
+    // subnormal, infinite and NaN x in double
+    bool ok[2];
 #pragma unroll
     for (int i = 0; i < crf_lanes<F>::n; ++i) {
         const float xi = crf_get(x, i);
-        // normal, positive, finite x; zero, negative, subnormal, infinite
-        // and NaN x in double
-        const bool common = xi >= 0x1p-126f && xi <= 0x1.fffffep127f;
-        const float a = crf_get(z1, i);
-        crf_set(out, i, common && a == crf_get(z2, i) ? a : crf_slow_log(xi));
+        ok[i] = xi >= 0x1p-126f && xi <= 0x1.fffffep127f && crf_get(z1, i) == crf_get(z2, i);
     }
+    if (crf_all<F>(ok)) return z1;
+    F out;
+#pragma unroll
+    for (int i = 0; i < crf_lanes<F>::n; ++i) crf_set(out, i, ok[i] ? crf_get(z1, i) : crf_slow_log(crf_get(x, i)));
     return out;
 }
 
@@ -495,15 +524,20 @@ LG_CRF_DEV F lg_crf_atan(F z)
     }
     F z1, z2;
     crf_ziv(hi2, lo2, z1, z2);
+    // finite z with the rounding decided; infinite and NaN z in double.  The
+    // sign of z on |result| (z = +-0 gives +-0: the result is 0 there).
+    bool ok[2];
     F out;
 #pragma unroll
     for (int i = 0; i < crf_lanes<F>::n; ++i) {
         const float zi = crf_get(z, i);
-        const float w = crf_get(z1, i);
-        // finite z; infinite and NaN z in double
-        const bool ok = crf_fabsf(zi) <= 0x1.fffffep127f && w == crf_get(z2, i);
-        crf_set(out, i, ok ? (zi < 0.0f ? -w : (zi > 0.0f ? w : zi)) : crf_slow_atan(zi));
+        ok[i] = crf_fabsf(zi) <= 0x1.fffffep127f && crf_get(z1, i) == crf_get(z2, i);
+        crf_set(out, i, crf_copysignf(crf_get(z1, i), zi));
     }
+    if (crf_all<F>(ok)) return out;
+#pragma unroll
+    for (int i = 0; i < crf_lanes<F>::n; ++i)
+        if (!ok[i]) crf_set(out, i, crf_slow_atan(crf_get(z, i)));
     return out;
 }
 
@@ -574,14 +608,19 @@ LG_CRF_DEV F lg_crf_atanh(F v)
     }
     F z1, z2;
     crf_ziv(hi, lo, z1, z2);
+    // |v| < 1 with the rounding decided; |v| >= 1 and NaN v in double.  The
+    // sign of v on |result| (v = +-0 gives +-0).
+    bool ok2[2];
     F out;
 #pragma unroll
     for (int i = 0; i < crf_lanes<F>::n; ++i) {
         const float vi = crf_get(v, i);
-        const float w = crf_get(z1, i);
-        // |v| < 1; |v| >= 1 and NaN v in double
-        const bool ok = crf_fabsf(vi) < 1.0f && w == crf_get(z2, i);
-        crf_set(out, i, ok ? (vi < 0.0f ? -w : (vi > 0.0f ? w : vi)) : crf_slow_atanh(vi));
+        ok2[i] = crf_fabsf(vi) < 1.0f && crf_get(z1, i) == crf_get(z2, i);
+        crf_set(out, i, crf_copysignf(crf_get(z1, i), vi));
     }
+    if (crf_all<F>(ok2)) return out;
+#pragma unroll
+    for (int i = 0; i < crf_lanes<F>::n; ++i)
+        if (!ok2[i]) crf_set(out, i, crf_slow_atanh(crf_get(v, i)));
     return out;
 }
