@@ -20,6 +20,10 @@ __device__ float2 crf_pair(int fn, float2 a)
 {
     return fn == 0 ? lg_crf_exp(a) : fn == 1 ? lg_crf_log(a) : fn == 2 ? lg_crf_atan(a) : lg_crf_atanh(a);
 }
+__device__ float crf_scalar(int fn, float x)
+{
+    return fn == 0 ? lg_crf_exp(x) : fn == 1 ? lg_crf_log(x) : fn == 2 ? lg_crf_atan(x) : lg_crf_atanh(x);
+}
 __device__ float crf_double(int fn, float x)
 {
     return fn == 0   ? (float)exp((double)x)
@@ -31,8 +35,9 @@ __device__ float crf_double(int fn, float x)
 // every bit pattern u in [lo, hi) as lane 0 of a pair whose lane 1 is an
 // unrelated input (u times an odd constant, a bijection of the 32-bit
 // patterns), so that the lanes of a pair take different paths and table
-// entries; counts lanes whose bits differ from the double evaluation (NaN
-// equal to NaN), and keeps the first few
+// entries, and through the one-lane version; counts inputs whose bits
+// differ from the double evaluation in either (NaN equal to NaN), and
+// keeps the first few
 __global__ void lg_crf_sweep_kernel(int fn, unsigned long long lo, unsigned long long hi,
                                     unsigned long long* __restrict__ bad, unsigned* __restrict__ first, int nfirst)
 {
@@ -43,7 +48,10 @@ __global__ void lg_crf_sweep_kernel(int fn, unsigned long long lo, unsigned long
         const float x1 = __uint_as_float((unsigned)u * 0x9E3779B1u);
         const float2 r = crf_pair(fn, make_float2(x0, x1));
         const float w0 = crf_double(fn, x0), w1 = crf_double(fn, x1);
-        const bool ok0 = __float_as_uint(r.x) == __float_as_uint(w0) || (r.x != r.x && w0 != w0);
+        // the one-lane version (what the exact render calls) on x0 too
+        const float r0 = crf_scalar(fn, x0);
+        const bool ok0 = (__float_as_uint(r.x) == __float_as_uint(w0) || (r.x != r.x && w0 != w0)) &&
+                         (__float_as_uint(r0) == __float_as_uint(w0) || (r0 != r0 && w0 != w0));
         const bool ok1 = __float_as_uint(r.y) == __float_as_uint(w1) || (r.y != r.y && w1 != w1);
         if (!ok0 || !ok1) {
             nbad += (!ok0) + (!ok1);

@@ -253,10 +253,10 @@ LG_CRF_DEV bool crf_all(const bool (&ok)[2])
 // x = k ln2/64 + r, |r| <= ln2/128 (k = m 64 + j); e^x = 2^m 2^(j/64) e^r.
 // r = x - k L_hi exactly (an fma: the difference is a multiple of 2^-31
 // below 2^-7 in magnitude) minus k L_lo; e^r = 1 + r + r^2/2 + r^3 (1/6 +
-// r/24 + r^2/120) with r = rh + rl, the square of rh exact (fma), rl to
-// first order (it reaches 2^-22), the cubic tail in float.
+// r/24) with r = rh + rl, the square of rh exact (fma), rl to first order
+// (it reaches 2^-22), the cubic tail in float.
 // Error: k L_lo rounding and the L_hi + L_lo split (2^-46 at |k| <= 9600),
-// truncation r^6/720 (2^-54), table pairs (2^-48), evaluation (2^-47).
+// truncation r^5/120 (2^-44.6), table pairs (2^-48), evaluation (2^-47).
 // Results below 2^-126 are rounded to the subnormal grid from the
 // double-word value directly; e^x rounds to 0 for x <= LG_CRF_EXP_ZERO.
 LG_CRF_COLD float crf_exp_low(float x, float yh0, float yl0, int m)
@@ -297,12 +297,10 @@ LG_CRF_DEV void crf_exp_core(F x, F& big, F& yh, F& yl, int (&mm)[2])
     const F rl = crf_mul(crf_neg(kf), crf_bc<F>(LG_CRF_EXP_LLO));
     const F sh = crf_mul(rh, rh);
     const F sl = crf_fma(rh, rh, crf_neg(sh));
-    const F p3 = crf_fma(crf_fma(rh, crf_bc<F>(0x1.111112p-7f), crf_bc<F>(0x1.555556p-5f)), rh,
-                         crf_bc<F>(0x1.555556p-3f));
-    const F t = crf_mul(crf_mul(sh, rh), p3);
+    const F p3 = crf_fma(rh, crf_bc<F>(0x1.555556p-5f), crf_bc<F>(0x1.555556p-3f));
     const F h = crf_mul(sh, crf_bc<F>(0.5f));
     // first order in rl (up to 2^-22 at large |k|): rl (1 + rh + rh^2/2)
-    const F small = crf_add(crf_fma(sl, crf_bc<F>(0.5f), crf_fma(h, rl, crf_fma(rh, rl, rl))), t);
+    const F small = crf_fma(crf_mul(sh, rh), p3, crf_fma(sl, crf_bc<F>(0.5f), crf_fma(h, rl, crf_fma(rh, rl, rl))));
     const F uh = crf_add(rh, h);  // |rh| >= rh^2 / 2: fast two-sum
     const F ul = crf_add(crf_sub(h, crf_sub(uh, rh)), small);
     F th, tl;

@@ -8,14 +8,17 @@
 //
 // exp, log, atan and atanh (the functions of the SIE family, the Sersic,
 // exponential, Gaussian and de Vaucouleurs profiles) come from
-// lg_crfloat.cuh, in single-precision arithmetic with paired instructions;
+// lg_crfloat.cuh, in single-precision arithmetic;
 // the others (those of the EPL lens: atan2, sincos, pow; and the rest of the
 // mapped library) are evaluated lane by lane in double.
 
-LG_DEV lg_pair lg_cr_expf(lg_pair a) { return {lg_crf_exp(a.v)}; }
-LG_DEV lg_pair lg_cr_logf(lg_pair a) { return {lg_crf_log(a.v)}; }
-LG_DEV lg_pair lg_cr_atanf(lg_pair a) { return {lg_crf_atan(a.v)}; }
-LG_DEV lg_pair lg_cr_atanhf(lg_pair a) { return {lg_crf_atanh(a.v)}; }
+// one lane at a time: these functions are bound by instruction issue, and
+// their per-lane parts (bit fields, tests, table loads) outweigh what f32x2
+// instructions save in the double-word steps (measured 5-7% faster per lane)
+LG_DEV lg_pair lg_cr_expf(lg_pair a) { return {make_float2(lg_crf_exp(a.v.x), lg_crf_exp(a.v.y))}; }
+LG_DEV lg_pair lg_cr_logf(lg_pair a) { return {make_float2(lg_crf_log(a.v.x), lg_crf_log(a.v.y))}; }
+LG_DEV lg_pair lg_cr_atanf(lg_pair a) { return {make_float2(lg_crf_atan(a.v.x), lg_crf_atan(a.v.y))}; }
+LG_DEV lg_pair lg_cr_atanhf(lg_pair a) { return {make_float2(lg_crf_atanh(a.v.x), lg_crf_atanh(a.v.y))}; }
 LG_DEV lg_pair lg_cr_expf(lg_pair_prod a) { return lg_cr_expf(lg_pair(a)); }
 LG_DEV lg_pair lg_cr_logf(lg_pair_prod a) { return lg_cr_logf(lg_pair(a)); }
 LG_DEV lg_pair lg_cr_atanf(lg_pair_prod a) { return lg_cr_atanf(lg_pair(a)); }
