@@ -58,6 +58,11 @@ UNIT = "evals/s"
 # (268 MB algorithmic; about 60 MB are still in L2 when it ends) and the
 # convolution reads them once (268 MB) -- no re-reads.
 MEASURED_TRAFFIC = {("config2", 1024, "render"): 208.45e6, ("config2", 1024, "convolve"): 269.2e6}
+# Thread instructions per ray of the render kernel (ncu smsp__inst_executed.sum
+# x 32 / rays of the launch) per floating-point mode, config2 workload: the
+# render is bound by instruction issue (4 warp instructions per SM and cycle),
+# so its issue rate against that peak is the second roofline it reports.
+MEASURED_INSTR_PER_RAY = {("config2", "exact"): 445.7, ("config2", "fast"): 90.8}
 
 RAY_FLOPS = {
     "sis": 12, "sis_plus_shear": 20, "nsis": 10, "sie": 26, "sie_plus_shear": 34, "nsie": 30,
@@ -504,11 +509,10 @@ def main():
     # plain mode: one candidate per call with a host sync (the reference
     # flow, e.g. MultiNest's callback), on a context created for it
     # (max_batch = 1; its launch shape tuned for one candidate)
-    plain, plain_shape, plain_loglike = None, None, None
-    if rank == 0 and not args.no_plain:
+    def plain_leg(flags):
         ctx1 = lg.Context(s.image, s.weight, s.objects, psf=s.psf, rule=s.rule, device=local, max_batch=1,
-                          flags=args.flags | (0 if args.no_autotune else lg.LG_FLAG_AUTOTUNE))
-        plain_shape = ctx1.launch_shape
+                          flags=flags | (0 if args.no_autotune else lg.LG_FLAG_AUTOTUNE))
+        shape = ctx1.launch_shape
         # through the C ABI as a C caller makes it (lg_eval_batch, B = 1),
         # the argument pointers prepared once
         import ctypes as C
@@ -525,7 +529,7 @@ def main():
         t0 = time.perf_counter()
         for i in range(n1):
             call(ctx1.h, ptrs[i % len(ptrs)], 1, pone)
-        plain = n1 / (time.perf_counter() - t0)
+        rate = n1 / (time.perf_counter() - t0)
         if not np.isfinite(one[0]):
             raise SystemExit("non-finite plain logL")
         # the reference-signature callback loglike(cube, ndim, npar, lnew,
@@ -545,8 +549,16 @@ def main():
         for i in range(n1):
             work[:] = cubes[i % 64]
             cb(pw, C.byref(nd), C.byref(npar), C.byref(lnew), ctx1.h)
-        plain_loglike = n1 / (time.perf_counter() - t0)
+        rate_cb = n1 / (time.perf_counter() - t0)
         ctx1.close()
+        return rate, shape, rate_cb
+
+    plain, plain_shape, plain_loglike = None, None, None
+    fast_plain = None
+    if rank == 0 and not args.no_plain:
+        plain, plain_shape, plain_loglike = plain_leg(args.flags)
+        if fast is not None:
+            fast_plain = plain_leg(lg.LG_FLAG_FAST_MATH)
 
     # roofline of the dominant kernel (headline mode)
     N, Q = s.width * s.height, len(lg.quad_rules()[s.rule][1])
@@ -576,6 +588,16 @@ def main():
                          "finish": float(stage[3])},
             "convolve_tflops": (conv_flops / (stage[2] * 1e-3) / 1e12) if stage[2] > 0 else None,
             "rays_per_s": B * N * Q / (stage[1] * 1e-3)}
+    ipr = MEASURED_INSTR_PER_RAY.get((args.workload, mode_name(args.flags)))
+    if dom == "render" and ipr and clk and clk.get("sm_mhz"):
+        # issue roofline: thread instructions per second against 152 SMs x 4
+        # warp instructions x 32 threads per cycle at the sampled SM clock
+        ach_i = ipr * B * N * Q / (stage[1] * 1e-3) / 1e12
+        peak_i = 152 * 4 * 32 * clk["sm_mhz"] * 1e6 / 1e12
+        roof["issue"] = {"thread_instructions_per_ray": ipr, "achieved": ach_i, "peak": peak_i,
+                         "unit": "T thread-instructions/s", "frac": ach_i / peak_i,
+                         "source": "instructions per ray from ncu smsp__inst_executed.sum (one launch, "
+                                   "this workload and mode); time from this run's render stage"}
 
     config = describe(s, B)
     config["fp_mode"] = mode_name(args.flags)
@@ -594,6 +616,9 @@ def main():
                              "flags": "LG_FLAG_FAST_MATH",
                              "stage_ms": {"set_params": float(fst[0]), "render": float(fst[1]),
                                           "convolve": float(fst[2]), "finish": float(fst[3])}}
+        if fast_plain:
+            line["fast_mode"].update({"plain_evals_per_s": fast_plain[0], "plain_launch_shape": fast_plain[1],
+                                      "plain_loglike_callback_per_s": fast_plain[2]})
     if clk:
         line["clocks"] = clk
     if rank == 0 and world == 1 and not args.no_cpu_baseline:

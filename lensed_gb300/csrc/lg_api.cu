@@ -210,14 +210,18 @@ struct lg_ctx {
         return mark(4);
     }
 
+    // every captured graph (they hold the evaluation module's kernels)
+    void drop_graphs()
+    {
+        for (auto* m : {&graphs, &cube_graphs, &hgraphs}) {
+            for (auto& g : *m) cudaGraphExecDestroy(g.second);
+            m->clear();
+        }
+    }
+
     void release()
     {
-        for (auto& g : graphs) cudaGraphExecDestroy(g.second);
-        graphs.clear();
-        for (auto& g : cube_graphs) cudaGraphExecDestroy(g.second);
-        cube_graphs.clear();
-        for (auto& g : hgraphs) cudaGraphExecDestroy(g.second);
-        hgraphs.clear();
+        drop_graphs();
         cudaFreeHost(z_models);
         z_models = nullptr;
         cudaFree(d_priors);
@@ -376,10 +380,7 @@ int load_eval(lg_ctx* c, const lg::Shape& s, const std::vector<char>& cubin)
 {
     int rc;
     if (c->stream && (rc = c->cuda(cudaStreamSynchronize(c->stream), "synchronize"))) return rc;
-    for (auto& g : c->graphs) cudaGraphExecDestroy(g.second);
-    c->graphs.clear();
-    for (auto& g : c->cube_graphs) cudaGraphExecDestroy(g.second);
-    c->cube_graphs.clear();
+    c->drop_graphs();
     if (c->mod) c->drv->moduleUnload(c->mod);
     c->mod = nullptr;
     cudaFree(c->d_partials);

@@ -145,6 +145,30 @@ def test_autotune_picks_a_candidate_and_caches_it(native):
     assert other.tune_report.startswith("tuned")
 
 
+def test_shape_change_after_small_batch_calls(native):
+    """A launch-shape change replaces the evaluation module: the graphs
+    captured for earlier calls (batches through the host object data
+    included) are released with it, and later calls of every batch size
+    capture new ones and give the same logL."""
+    psf, image, weight, objs, cand = _setup()
+    ctx = _ctx(objs, image, weight, psf, max_batch=16)
+    p = ctx.to_map_order(cand)
+    before = [ctx.eval_batch(p[:1]), ctx.eval_batch(p[:3]), ctx.eval_batch(p)]
+    cube = np.full((1, ctx.ndims), 0.4)
+    cb, _ = ctx.eval_cube(cube)
+    base = ctx.launch_shape
+    other = dict(rt=64, rppt=2, qs=1, ctx=32, cty=16, cr=4, pair_rows=0)
+    assert other != base
+    ctx.set_launch_shape(**other)
+    after = [ctx.eval_batch(p[:1]), ctx.eval_batch(p[:3]), ctx.eval_batch(p)]
+    ca, _ = ctx.eval_cube(cube)
+    for x, y in zip(before, after):
+        np.testing.assert_allclose(x, y, rtol=1e-12, atol=0)
+    np.testing.assert_allclose(ca, cb, rtol=1e-12, atol=0)
+    ctx.set_launch_shape(**base)
+    assert np.array_equal(ctx.eval_batch(p[:1]), before[0])
+
+
 def test_autotune_file_cache_across_processes(native, tmp_path):
     cache = tmp_path / "tune.txt"
     script = textwrap.dedent(f"""
