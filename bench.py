@@ -397,6 +397,7 @@ def main():
                     help="lg_options.flags: 0 exact (default), 1 strict, 16 fast, 16|4 fast with IEEE div/sqrt")
     ap.add_argument("--no-fast", action="store_true", help="do not time the fast mode beside the exact one")
     ap.add_argument("--no-plain", action="store_true", help="skip the one-candidate-per-call measurement")
+    ap.add_argument("--plain-only", action="store_true", help="only the one-candidate-per-call measurement")
     ap.add_argument("--parity-n", type=int, default=128,
                     help="timed candidates checked against the FP32 oracle (CPU) for the parity block")
     ap.add_argument("--flow-layers", type=int, default=8)
@@ -486,26 +487,6 @@ def main():
                 "t_create": t_create}
 
     # the headline: the default (exact) mode unless --flags asks otherwise
-    head = timed(args.flags, Clocks(local))
-    ctx, cand, value, ms, clk, logL_gpu, stage, t_create = (head[k] for k in (
-        "ctx", "cand", "value", "ms", "clocks", "logL", "stage", "t_create"))
-    # the fast mode beside it (hardware-approximate functions, FMA contraction)
-    fast = None
-    if args.flags == 0 and not args.no_fast:
-        fast = timed(lg.LG_FLAG_FAST_MATH)
-        fast["ctx"].close()
-
-    # end to end through the public C ABI with host buffers
-    hp = np.ascontiguousarray(cand)
-    for _ in range(2):
-        ctx.eval_batch(hp)
-    ne2e = max(3, min(args.steps, 50))
-    t0 = time.perf_counter()
-    for _ in range(ne2e):
-        ll_host = ctx.eval_batch(hp)
-    e2e_dt = (time.perf_counter() - t0) / ne2e
-    e2e = replicas.aggregate(B, replicas.max_over_ranks(e2e_dt, dist, device=f"cuda:{local}"), world)
-
     # plain mode: one candidate per call with a host sync (the reference
     # flow, e.g. MultiNest's callback), on a context created for it
     # (max_batch = 1; its launch shape tuned for one candidate)
@@ -517,7 +498,8 @@ def main():
         # the argument pointers prepared once
         import ctypes as C
 
-        rows = [np.ascontiguousarray(hp[i:i + 1]) for i in range(min(B, 64))]
+        hp1 = ctx1.to_map_order(cand_obj[:64])
+        rows = [np.ascontiguousarray(hp1[i:i + 1]) for i in range(len(hp1))]
         ptrs = [r.ctypes.data_as(C.POINTER(C.c_double)) for r in rows]
         one = np.zeros(1)
         pone = one.ctypes.data_as(C.POINTER(C.c_double))
@@ -552,6 +534,37 @@ def main():
         rate_cb = n1 / (time.perf_counter() - t0)
         ctx1.close()
         return rate, shape, rate_cb
+
+    if args.plain_only:
+        # one-candidate calls alone (for profiling the plain path)
+        if rank == 0:
+            r = plain_leg(args.flags)
+            line = {"metric": METRIC + " (one candidate per call)", "value": r[0], "unit": UNIT,
+                    "n_gpus": 1, "higher_is_better": True, "data": "synthetic", "config": describe(s, 1),
+                    "fp_mode": mode_name(args.flags), "plain_launch_shape": r[1],
+                    "plain_loglike_callback_per_s": r[2]}
+            print(json.dumps(line), flush=True)
+        return
+
+    head = timed(args.flags, Clocks(local))
+    ctx, cand, value, ms, clk, logL_gpu, stage, t_create = (head[k] for k in (
+        "ctx", "cand", "value", "ms", "clocks", "logL", "stage", "t_create"))
+    # the fast mode beside it (hardware-approximate functions, FMA contraction)
+    fast = None
+    if args.flags == 0 and not args.no_fast:
+        fast = timed(lg.LG_FLAG_FAST_MATH)
+        fast["ctx"].close()
+
+    # end to end through the public C ABI with host buffers
+    hp = np.ascontiguousarray(cand)
+    for _ in range(2):
+        ctx.eval_batch(hp)
+    ne2e = max(3, min(args.steps, 50))
+    t0 = time.perf_counter()
+    for _ in range(ne2e):
+        ll_host = ctx.eval_batch(hp)
+    e2e_dt = (time.perf_counter() - t0) / ne2e
+    e2e = replicas.aggregate(B, replicas.max_over_ranks(e2e_dt, dist, device=f"cuda:{local}"), world)
 
     plain, plain_shape, plain_loglike = None, None, None
     fast_plain = None
