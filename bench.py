@@ -189,6 +189,42 @@ def run_flow_inverse(args):
     print(json.dumps(line), flush=True)
 
 
+def run_flow_train(args):
+    """Training steps of the learned proposal's flow (d = 13, 8 coupling
+    layers, width 128, 2 hidden layers) on minibatches of `--batch` rows
+    (default 256, the sampler's) of 1024 points with random weights: device
+    time per step (forward + backward + Adam) of the tcgen05 step and of the
+    FP32-weight step (CUDA events, 50 steps after warm-up), and the
+    tensor-core step's dense FLOPs per second (forward, recomputed forward
+    and the two backward products of every dense)."""
+    import ctypes as C
+
+    import lensed_gb300 as lg
+
+    d, layers, width, hidden = 13, 8, 128, 2
+    batch = args.batch or 256
+    n = max(1024, batch)
+    rng = np.random.Generator(np.random.PCG64(7))
+    npar = lg.lib().lg_flow_nparams(d, layers, width, hidden)
+    params = (rng.normal(size=npar) * 0.05).astype(np.float32)
+    x = rng.normal(size=(n, d)).astype(np.float32)
+    P = lambda a: a.ctypes.data_as(C.POINTER(C.c_float))
+    out = {}
+    for tc in (1, 0):
+        ms = np.zeros(1, np.float32)
+        rc = lg.lib().lg_flow_train_time(0, d, layers, width, hidden, tc, P(params), P(x), n, batch, 50, P(ms))
+        out["tc" if tc else "fp32"] = {"rc": rc, "ms": float(ms[0])}
+    # dense multiply-adds per row and layer: 16 x 128 + 128 x 128 + 128 x 16
+    # (K and N padded to 16); 4 passes (forward, recomputed forward, dX, dW)
+    flop = 2.0 * (16 * width + width * width + width * 16) * layers * 4
+    line = {"metric": "learned-proposal training step", "batch": batch, "flow": [d, layers, width, hidden],
+            "ms_per_step": {k: v["ms"] for k, v in out.items()},
+            "rows_per_s": {k: batch / (v["ms"] * 1e-3) for k, v in out.items() if v["ms"] > 0},
+            "tc_tflops": batch * flop / (out["tc"]["ms"] * 1e-3) / 1e12 if out["tc"]["ms"] > 0 else None,
+            "rc": {k: v["rc"] for k, v in out.items()}}
+    print(json.dumps(line), flush=True)
+
+
 def run_systems(args):
     """16 systems of uneven sizes, 256 candidates each, one batch per step
     through lg_systems_eval (host buffers in and out: value = e2e)."""
@@ -420,6 +456,8 @@ def main():
         return run_sampler(args)
     if args.workload == "flow-inverse":
         return run_flow_inverse(args)
+    if args.workload == "flow-train":
+        return run_flow_train(args)
 
     import torch
 

@@ -437,11 +437,16 @@ typedef struct {
                          128^2 image with a 9-point rule): the flow is used when its volume times
                          1 + draw_cost x latent draws per proposal is below the ellipsoids' volume;
                          0 for expensive likelihoods.  A fixed number, so that runs repeat */
-    int wait_tries;   /* polls of each bounded wait of the tensor-core inverse before it gives up
-                         (0: the default 2^20; negative: none -- every wait gives up at once, which
-                         exercises the timeout path: the kernel flags the error, lets its own copies
-                         and tensor-core work in flight complete, frees its tensor memory and
-                         returns, and the sampler drops that flow) */
+    int wait_tries;   /* polls of each bounded wait of the tensor-core kernels (inverse and
+                         training step) before it gives up (0: the default 2^20; negative: none --
+                         every wait gives up at once, which exercises the timeout path: the kernel
+                         flags the error, lets its own copies and tensor-core work in flight
+                         complete, frees its tensor memory and returns, and the sampler drops that
+                         flow) */
+    int train_tc;     /* 1: training steps on the tensor cores (lg_flow_step_tc: BF16 weights,
+                         conditioner inputs and activations, FP32 accumulators in tensor memory)
+                         when the shape allows it (width 128, two hidden layers, d <= 16, sm_100+);
+                         0: the FP32-weight training kernels */
 } lg_flow_options;
 
 typedef int (*lg_batch_loglike)(void* user, const double* cube, int B, double* logL);
@@ -451,8 +456,9 @@ lg_flow_options lg_flow_defaults(void);
 int lg_nested_sample(int ndims, lg_batch_loglike fn, void* user, const lg_nested_options* opts,
                      lg_nested_result* result);
 /* Loss and gradient of a flow with the given parameters on n points
- * (standardised coordinates), for gradient checks; bf16 = 0 keeps hidden
- * activations in FP32. */
+ * (standardised coordinates), for gradient checks: bf16 = 0 the FP32
+ * training kernel with FP32 hidden activations, 1 the same with BF16 hidden
+ * activations, 2 the tensor-core training step (lg_flow_options.train_tc). */
 long lg_flow_nparams(int d, int layers, int width, int hidden);
 int lg_flow_loss_grad(int device, int d, int layers, int width, int hidden, int bf16, const float* params,
                       const float* x, int n, float* loss, float* grad);
@@ -469,6 +475,12 @@ int lg_flow_inverse_check(int device, int d, int layers, int width, int hidden, 
    events on the launching stream; *ms = milliseconds per launch. */
 int lg_flow_inverse_time(int device, int d, int layers, int width, int hidden, int tc, const float* params,
                          const float* z, int M, int reps, float* ms);
+/* Device time of flow training steps (forward + backward of `batch` rows
+   of the n points, then the Adam step): tc = 1 the tensor-core step, 0 the
+   FP32-weight step (BF16 activations); reps steps after two warm-up steps,
+   CUDA events on the launching stream; *ms = milliseconds per step. */
+int lg_flow_train_time(int device, int d, int layers, int width, int hidden, int tc, const float* params,
+                       const float* x, int n, int batch, int reps, float* ms);
 /* One retraining of the learned proposal on n points (n x d, row-major),
  * as the sampler does it on its live points: history receives the held-out
  * loss before training and after each epoch (NaN past the last epoch run);

@@ -73,7 +73,7 @@ class NestedResult(C.Structure):
 class FlowOptions(C.Structure):
     _fields_ = [("layers", C.c_int), ("width", C.c_int), ("hidden", C.c_int), ("epochs", C.c_int),
                 ("batch", C.c_int), ("lr", C.c_double), ("expand", C.c_double), ("patience", C.c_int),
-                ("lag", C.c_int), ("draw_cost", C.c_double), ("wait_tries", C.c_int)]
+                ("lag", C.c_int), ("draw_cost", C.c_double), ("wait_tries", C.c_int), ("train_tc", C.c_int)]
 
 
 BATCH_LOGLIKE = C.CFUNCTYPE(C.c_int, C.c_void_p, C.POINTER(C.c_double), C.c_int, C.POINTER(C.c_double))
@@ -158,6 +158,7 @@ def lib():
         "lg_flow_nparams": (C.c_long, [C.c_int, C.c_int, C.c_int, C.c_int]),
         "lg_flow_inverse_check": (C.c_int, [C.c_int] * 7 + [fp, fp, C.c_int, fp, fp]),
         "lg_flow_inverse_time": (C.c_int, [C.c_int] * 6 + [fp, fp, C.c_int, C.c_int, fp]),
+        "lg_flow_train_time": (C.c_int, [C.c_int] * 6 + [fp, fp, C.c_int, C.c_int, C.c_int, fp]),
         "lg_ellipsoid_draw_check": (C.c_int, [C.c_int, C.c_int, C.c_int, dp, dp, ip, dp, C.c_int, C.c_ulonglong]),
         "lg_flow_fit": (C.c_int, [C.c_int, C.c_int, C.POINTER(FlowOptions), dp, C.c_int, fp, C.c_int, dp]),
         "lg_flow_loss_grad": (C.c_int, [C.c_int, C.c_int, C.c_int, C.c_int, C.c_int, C.c_int, fp, fp, C.c_int,

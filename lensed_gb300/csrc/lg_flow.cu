@@ -475,26 +475,6 @@ __global__ void __launch_bounds__(FT)
     }
 }
 
-// Gradient = sum of the blocks' slices in block order; then (adam) an Adam
-// step with bias corrections c1, c2 of this step.
-__global__ void __launch_bounds__(256)
-    lg_flow_adam(float* __restrict__ P, const float* __restrict__ gpart, int nparts, long n, float* __restrict__ G,
-                 float* __restrict__ m1, float* __restrict__ m2, int adam, float lr, float b1, float b2, float c1,
-                 float c2, const int* __restrict__ stop)
-{
-    if (stop && *stop) return;
-    const long i = (long)blockIdx.x * blockDim.x + threadIdx.x;
-    if (i >= n) return;
-    float g = 0.0f;
-    for (int c = 0; c < nparts; ++c) g += gpart[(size_t)c * n + i];
-    if (G) G[i] = g;
-    if (!adam) return;
-    const float a = b1 * m1[i] + (1 - b1) * g, b = b2 * m2[i] + (1 - b2) * g * g;
-    m1[i] = a;
-    m2[i] = b;
-    P[i] -= lr * (a / c1) / (sqrtf(b / c2) + 1e-8f);
-}
-
 // Early stopping on the device.  state: [0] best held-out loss, [1] epochs
 // since the best (as float), [2] last held-out loss, [3] training epochs
 // completed (counted when epoch = 1), [4] 1 if the last check improved,
@@ -755,6 +735,52 @@ __global__ void __launch_bounds__(256)
     }
 }
 
+// Library index i of a weight -> its position in the packed BF16 operands
+// (lg_flow_pack's layout); -1 for a bias.
+__device__ long lg_packed_index(const FlowDims& f, const TcDims& t, long i)
+{
+    for (int l = 0; l < f.L; ++l)
+        for (int k = 0; k <= f.NH; ++k) {
+            const int K = f.kin(l, k), N = f.kout(l, k);
+            const long nw = (long)K * N;
+            if (i < nw) {
+                const int kk = (int)(i / N), n = (int)(i - (long)kk * N);
+                const long at = (long)l * t.sl + (k == 0 ? 0 : t.s0 + (long)(k - 1) * t.sh);
+                return at + lg_core_off(n, kk, k == 0 ? t.kp0 : f.W);
+            }
+            i -= nw;
+            if (i < N) return -1;
+            i -= N;
+        }
+    return -1;
+}
+
+// Gradient = sum of the blocks' slices in block order; then (adam) an Adam
+// step with bias corrections c1, c2 of this step, and (packed) the updated
+// weight's BF16 copy in the tensor-core operands.
+__global__ void __launch_bounds__(256)
+    lg_flow_adam(float* __restrict__ P, const float* __restrict__ gpart, int nparts, long n, float* __restrict__ G,
+                 float* __restrict__ m1, float* __restrict__ m2, int adam, float lr, float b1, float b2, float c1,
+                 float c2, const int* __restrict__ stop, FlowDims f, __nv_bfloat16* __restrict__ packed)
+{
+    if (stop && *stop) return;
+    const long i = (long)blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    float g = 0.0f;
+    for (int c = 0; c < nparts; ++c) g += gpart[(size_t)c * n + i];
+    if (G) G[i] = g;
+    if (!adam) return;
+    const float a = b1 * m1[i] + (1 - b1) * g, b = b2 * m2[i] + (1 - b2) * g * g;
+    m1[i] = a;
+    m2[i] = b;
+    const float p = P[i] - lr * (a / c1) / (sqrtf(b / c2) + 1e-8f);
+    P[i] = p;
+    if (packed) {
+        const long q = lg_packed_index(f, TcDims(f), i);
+        if (q >= 0) packed[q] = __float2bfloat16_rn(p);
+    }
+}
+
 // Shared-memory layout of lg_flow_inverse_tc (bytes): one layer's weights,
 // the conditioner input and one hidden activation tile (each epilogue
 // overwrites the tile its MMA chain has finished reading), so that two
@@ -970,6 +996,464 @@ __global__ void __launch_bounds__(256, 2)
     asm volatile("tcgen05.fence::before_thread_sync;");
     __syncthreads();
     if (w == 0) asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" ::"r"(tmem), "r"(tcols));
+}
+
+// ------------------------------------------------- tensor-core training --
+// A training step (or a forward pass) of the flow on the tensor cores, for
+// the conditioner shape the proposal uses (width 128, two hidden layers): a
+// block takes 128 minibatch rows (the MMA's M) forward through every
+// coupling layer and back.  The forward denses are the inverse's (BF16
+// weights and conditioner input, BF16 hidden activations, FP32 accumulators
+// in tensor memory), so training and proposals run the same network.  The
+// backward products read the same shared-memory tiles transposed: a K-major
+// tile of X (rows r, columns k) is, described MN-major, the tile of X^T, so
+//   dW_out = H1^T dO,   dH1 = dO W_out      (dO: 128 x 16, BF16)
+//   dW1    = H0^T dY1,  dH0 = dY1 W1        (dY1 = dH1 [H1 > 0], in place of H1)
+//   dW0^T  = dY0^T A0,  dA0 = dY0 W0        (dY0 = dH0 [H0 > 0], in place of H0)
+// each a chain of tcgen05.mma with both operands in shared memory and no
+// transposed copies (the packed weights serve the forward products as
+// K-major and the backward ones as MN-major operands).  Weight gradients go
+// from tensor memory into the block's slice of the partial-gradient buffer
+// (summed in block order by lg_flow_adam, which also refreshes the packed
+// BF16 weights); bias gradients are column sums in a fixed order.  A
+// layer's hidden activations are recomputed in the backward pass (all
+// layers' would need 512 KB); the layer inputs u_l stay in shared memory
+// (FP32).  Every mbarrier wait is bounded as in the inverse; a wait that
+// runs out sets *err and the early-stop flag, lets the block's copies and
+// MMA chains in flight complete, frees the tensor memory and returns.
+
+// Shared-memory layout of lg_flow_step_tc (bytes).
+struct TcStepSmem {
+    int wbuf, a0, h0, h1, dob, us, ob, dv, du, ld, cs, bias, stg, bar, total;
+    __host__ __device__ explicit TcStepSmem(const FlowDims& f)
+    {
+        const TcDims t(f);
+        int q = 0;
+        auto take = [&](int bytes) {
+            const int at = q;
+            q += (bytes + 127) / 128 * 128;
+            return at;
+        };
+        wbuf = take(2 * t.sl);
+        a0 = take(128 * t.kp0 * 2);
+        h0 = take(128 * f.W * 2);
+        h1 = take(128 * f.W * 2);
+        dob = take(128 * t.np * 2);
+        us = take((f.L + 1) * 128 * f.d * 4);
+        ob = take(128 * t.np * 4);
+        dv = take(128 * f.d * 4);
+        du = take(128 * f.d * 4);
+        ld = take(128 * 4);
+        cs = take(2 * f.W * 4);
+        bias = take((2 * f.W + t.np) * 4);
+        stg = take(128 * 16 * 4);
+        bar = take(64);
+        total = q;
+    }
+};
+
+// Two floats as BF16 (round to nearest even), the first in the low half.
+__device__ __forceinline__ uint32_t lg_pack_bf16(float lo, float hi)
+{
+    return (uint32_t)__bfloat16_as_ushort(__float2bfloat16_rn(lo)) |
+           ((uint32_t)__bfloat16_as_ushort(__float2bfloat16_rn(hi)) << 16);
+}
+
+// Instruction descriptor with operand majors: amaj / bmaj = 1 for an
+// MN-major (transposed) A / B.
+__device__ __forceinline__ uint32_t lg_umma_idesc_t(int M, int N, int amaj, int bmaj)
+{
+    return lg_umma_idesc(M, N) | ((uint32_t)amaj << 15) | ((uint32_t)bmaj << 16);
+}
+
+__global__ void __launch_bounds__(256, 1)
+    lg_flow_step_tc(FlowDims f, const float* __restrict__ P, const __nv_bfloat16* __restrict__ packed,
+                    const float* __restrict__ X, const int* __restrict__ idx, int row0, int M, int grad,
+                    float* __restrict__ loss, float* __restrict__ znorm2, float* __restrict__ gpart, long nparams,
+                    int* __restrict__ stop, int* __restrict__ err, long tries)
+{
+    // (read once per block: another block of this launch may set it)
+    __shared__ int stopped;
+    if (threadIdx.x == 0) stopped = stop ? *(volatile int*)stop : 0;
+    __syncthreads();
+    if (stopped) return;
+    extern __shared__ __align__(1024) unsigned char smem[];
+    const TcDims td(f);
+    const TcStepSmem L(f);
+    const int t = threadIdx.x, w = t / 32, lane = t % 32;
+    const int d = f.d, W = f.W, kp0 = td.kp0, np = td.np;
+    unsigned char* wb = smem + L.wbuf;
+    __nv_bfloat16* A0 = reinterpret_cast<__nv_bfloat16*>(smem + L.a0);
+    __nv_bfloat16* H0 = reinterpret_cast<__nv_bfloat16*>(smem + L.h0);
+    __nv_bfloat16* H1 = reinterpret_cast<__nv_bfloat16*>(smem + L.h1);
+    __nv_bfloat16* DO = reinterpret_cast<__nv_bfloat16*>(smem + L.dob);
+    float* Us = reinterpret_cast<float*>(smem + L.us);
+    float* ob = reinterpret_cast<float*>(smem + L.ob);
+    float* dv = reinterpret_cast<float*>(smem + L.dv);
+    float* du = reinterpret_cast<float*>(smem + L.du);
+    float* ld = reinterpret_cast<float*>(smem + L.ld);
+    float* cs = reinterpret_cast<float*>(smem + L.cs);
+    float* bs = reinterpret_cast<float*>(smem + L.bias);  // the layer's biases: dense 0, dense 1, output
+    float* stg = reinterpret_cast<float*>(smem + L.stg);  // 128 x 16 weight-gradient columns on their way out
+    uint64_t* bars = reinterpret_cast<uint64_t*>(smem + L.bar);       // [0] MMA, [1] weights
+    uint32_t* misc = reinterpret_cast<uint32_t*>(smem + L.bar + 32);  // [0] TMEM base, [1] abort flag
+    const uint32_t lbytes = 2u * td.sl;
+    // tensor-memory columns: the row-indexed accumulator (forward denses,
+    // dH1, dH0), dW1, the output dense, dW_out, dW0^T, dA0
+    constexpr uint32_t kCols = 512, cD = 0, cW1 = 128, cO = 256, cWo = 272, cW0 = 288, cX0 = 304;
+    if (w == 0) {
+        asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;" ::"r"(lg_saddr(misc)),
+                     "r"(kCols));
+        asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;");
+    }
+    if (t == 0) {
+        for (int i = 0; i < 2; ++i)
+            asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" ::"r"(lg_saddr(bars + i)), "r"(1));
+        asm volatile("fence.mbarrier_init.release.cluster;");
+        misc[1] = 0;
+    }
+    // rows beyond M are zero inputs; their loss and gradient are dropped
+    const int base = blockIdx.x * 128;
+    for (int e = t; e < 128 * d; e += 256) {
+        const int r = e / d, j = e - r * d, m = base + r;
+        Us[e] = m < M ? X[(size_t)(idx ? idx[row0 + m] : row0 + m) * d + j] : 0.0f;
+    }
+    if (t < 128) ld[t] = 0.0f;
+    asm volatile("tcgen05.fence::before_thread_sync;");
+    __syncthreads();
+    asm volatile("tcgen05.fence::after_thread_sync;");
+    const uint32_t tmem = misc[0];
+    const uint32_t sA0 = lg_saddr(A0), sH0 = lg_saddr(H0), sH1 = lg_saddr(H1), sDO = lg_saddr(DO);
+    const uint32_t sW0 = lg_saddr(wb), sW1 = sW0 + 2u * td.s0, sWo = sW1 + 2u * td.sh;
+
+    int issued = 0, waited = 0;
+    auto issue_weights = [&](int l) {
+        if (t == 0) {
+            void* bar = bars + 1;
+            asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(lg_saddr(bar)), "r"(lbytes)
+                         : "memory");
+            asm volatile(
+                "cp.async.bulk.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1], %2, [%3];" ::"r"(
+                    lg_saddr(wb)),
+                "l"(packed + (size_t)l * td.sl), "r"(lbytes), "r"(lg_saddr(bar))
+                : "memory");
+        }
+        ++issued;
+    };
+    // wait for the last weight copy issued (every thread)
+    auto wait_weights = [&]() {
+        if (t == 0 && !lg_mbar_wait(bars + 1, (uint32_t)waited & 1u, tries)) misc[1] = 1;
+        __syncthreads();
+        if (misc[1]) return false;
+        ++waited;
+        return true;
+    };
+    uint32_t mma_phase = 0;
+    bool mma_pending = false;
+    uint32_t pending_parity = 0;
+    // one MMA chain D[col] (+)= A . B^T over `steps` K-steps of 16, from
+    // start addresses, leading / stride byte offsets and per-step advances
+    auto chain = [&](uint32_t col, uint32_t a, uint32_t alb, uint32_t asb, uint32_t ast, uint32_t b, uint32_t blb,
+                     uint32_t bsb, uint32_t bst, int steps, uint32_t id) {
+        if (t == 0)
+            for (int ks = 0; ks < steps; ++ks)
+                lg_mma(tmem + col, lg_umma_desc(a + ks * ast, alb, asb), lg_umma_desc(b + ks * bst, blb, bsb), id,
+                       ks > 0);
+    };
+    // descriptors of a tile with C columns stored K-major (rows r): as a
+    // K-major operand (reduction over its columns) ...
+    auto KM = [](int C, uint32_t& lbo, uint32_t& sbo, uint32_t& st) {
+        lbo = 128;
+        sbo = (uint32_t)C * 16;
+        st = 256;
+    };
+    // ... and as an MN-major operand (reduction over its rows): the K
+    // direction's core-matrix stride in the leading byte offset, the MN
+    // direction's in the stride byte offset
+    auto MN = [](int C, uint32_t& lbo, uint32_t& sbo, uint32_t& st) {
+        lbo = (uint32_t)C * 16;
+        sbo = 128;
+        st = (uint32_t)C * 32;
+    };
+    auto begin_mma = [&]() {
+        if (t == 0) asm volatile("tcgen05.fence::after_thread_sync;");
+    };
+    auto commit_wait = [&]() {
+        if (t == 0) {
+            lg_mma_commit(bars);
+            if (!lg_mbar_wait(bars, mma_phase, tries)) {
+                misc[1] = 1;
+                mma_pending = true;
+                pending_parity = mma_phase;
+            }
+        }
+        mma_phase ^= 1u;
+        __syncthreads();
+        asm volatile("tcgen05.fence::after_thread_sync;");
+        return misc[1] == 0;
+    };
+    auto publish = [&]() {  // shared-memory tiles written by threads -> visible to the MMAs
+        asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
+        asm volatile("tcgen05.fence::before_thread_sync;");
+        __syncthreads();
+    };
+    // tensor-memory lane group and column half of this warp
+    const int m = 32 * (w % 4) + lane, half = w / 4;
+    const uint32_t tlane = tmem + ((uint32_t)(32 * (w % 4)) << 16);
+    // hidden epilogue: columns [0, W) + bias, ReLU, BF16 into dst
+    auto hidden_epilogue = [&](const float* bias, __nv_bfloat16* dst) {
+        for (int n0 = half * (W / 2); n0 < (half + 1) * (W / 2); n0 += 16) {
+            float v[16];
+            lg_tmem_ld16(tlane + cD + n0, v);
+            uint32_t h[8];
+#pragma unroll
+            for (int j = 0; j < 8; ++j) {
+                const float x0 = v[2 * j] + bias[n0 + 2 * j], x1 = v[2 * j + 1] + bias[n0 + 2 * j + 1];
+                h[j] = lg_pack_bf16(x0 > 0.0f ? x0 : 0.0f, x1 > 0.0f ? x1 : 0.0f);
+            }
+            uint4* q = reinterpret_cast<uint4*>(dst + lg_core_off(m, n0, W));
+            q[0] = make_uint4(h[0], h[1], h[2], h[3]);
+            q[8] = make_uint4(h[4], h[5], h[6], h[7]);
+        }
+        publish();
+    };
+    // backward epilogue: dst (holding the activations H) <- D [H > 0], BF16
+    auto mask_epilogue = [&](__nv_bfloat16* dst) {
+        for (int n0 = half * (W / 2); n0 < (half + 1) * (W / 2); n0 += 16) {
+            float v[16];
+            lg_tmem_ld16(tlane + cD + n0, v);
+            uint4* q = reinterpret_cast<uint4*>(dst + lg_core_off(m, n0, W));
+            const uint4 a = q[0], b = q[8];
+            const uint32_t hin[8] = {a.x, a.y, a.z, a.w, b.x, b.y, b.z, b.w};
+            uint32_t h[8];
+#pragma unroll
+            for (int j = 0; j < 8; ++j)  // a BF16 activation is > 0 iff its sign bit is clear and it is not zero
+                h[j] = lg_pack_bf16((hin[j] & 0x8000u) == 0 && (hin[j] & 0x7FFFu) != 0 ? v[2 * j] : 0.0f,
+                                    (hin[j] >> 31) == 0 && (hin[j] & 0x7FFF0000u) != 0 ? v[2 * j + 1] : 0.0f);
+            q[0] = make_uint4(h[0], h[1], h[2], h[3]);
+            q[8] = make_uint4(h[4], h[5], h[6], h[7]);
+        }
+        publish();
+    };
+    // out[n] = sum over the 128 rows of the BF16 tile T (W columns), fixed order
+    auto colsum = [&](const __nv_bfloat16* T, float* __restrict__ out) {
+        const int n = t % 128, hh = t / 128;
+        float s = 0.0f;
+        for (int r = hh * 64; r < hh * 64 + 64; ++r) s += __bfloat162float(T[lg_core_off(r, n, W)]);
+        cs[hh * 128 + n] = s;
+        __syncthreads();
+        if (t < 128) out[t] = cs[t] + cs[128 + t];
+        __syncthreads();
+    };
+    // parameter offsets of layer l (library layout)
+    auto layer_offset = [&](int l) {
+        long o = 0;
+        for (int ll = 0; ll < l; ++ll)
+            for (int kk = 0; kk <= f.NH; ++kk) o += (long)f.kin(ll, kk) * f.kout(ll, kk) + f.kout(ll, kk);
+        return o;
+    };
+    // forward of layer l up to the conditioner output o = D_out + b_out in
+    // ob (FP32, 128 x np, zero past 2 db); the layer's weights resident
+    auto conditioner = [&](int l, long woff, bool next_weights) {
+        const int da = f.da(l), db = f.db(l), a0 = f.a0(l);
+        const float* u = Us + (size_t)l * 128 * d;
+        for (int e = t; e < 128 * kp0; e += 256) {
+            const int r = e / kp0, k = e - r * kp0;
+            A0[lg_core_off(r, k, kp0)] = __float2bfloat16_rn(k < da ? u[r * d + a0 + k] : 0.0f);
+        }
+        publish();
+        uint32_t al, as, at;
+        const long ob0 = woff + (long)da * W, ob1 = ob0 + W + (long)W * W,
+                   obo = ob1 + W + (long)W * 2 * db;
+        for (int e = t; e < 2 * W + np; e += 256)
+            bs[e] = e < W ? P[ob0 + e] : (e < 2 * W ? P[ob1 + e - W] : (e - 2 * W < 2 * db ? P[obo + e - 2 * W] : 0.0f));
+        begin_mma();
+        KM(kp0, al, as, at);
+        chain(cD, sA0, al, as, at, sW0, al, as, at, kp0 / 16, lg_umma_idesc(128, W));
+        if (!commit_wait()) return false;
+        hidden_epilogue(bs, H0);
+        begin_mma();
+        KM(W, al, as, at);
+        chain(cD, sH0, al, as, at, sW1, al, as, at, W / 16, lg_umma_idesc(128, W));
+        if (!commit_wait()) return false;
+        hidden_epilogue(bs + W, H1);
+        begin_mma();
+        chain(cO, sH1, al, as, at, sWo, al, as, at, W / 16, lg_umma_idesc(128, np));
+        if (!commit_wait()) return false;
+        if (next_weights) issue_weights(l + 1);  // the buffer is free: the next layer's copy runs under the coupling
+        if (w < 4) {
+            for (int n0 = 0; n0 < np; n0 += 16) {
+                float v[16];
+                lg_tmem_ld16(tlane + cO + n0, v);
+#pragma unroll
+                for (int j = 0; j < 16; ++j) {
+                    const int n = n0 + j;
+                    ob[m * np + n] = v[j] + bs[2 * W + n];
+                }
+            }
+        }
+        asm volatile("tcgen05.fence::before_thread_sync;");
+        __syncthreads();
+        return true;
+    };
+
+    bool ok = true;
+    issue_weights(0);
+    // ---- forward
+    for (int l = 0; l < f.L && ok; ++l) {
+        if (!(ok = wait_weights())) break;
+        if (!(ok = conditioner(l, layer_offset(l), l + 1 < f.L))) break;
+        const int db = f.db(l), b0 = f.b0(l);
+        const float* u = Us + (size_t)l * 128 * d;
+        float* v = Us + (size_t)(l + 1) * 128 * d;
+        if (t < 128) {
+            for (int j = 0; j < d; ++j) v[t * d + j] = u[t * d + j];
+            float acc = 0.0f;
+            for (int j = 0; j < db; ++j) {
+                const float s = LG_FLOW_CLAMP * tanhf(ob[t * np + j] / LG_FLOW_CLAMP);
+                v[t * d + b0 + j] = u[t * d + b0 + j] * expf(s) + ob[t * np + db + j];
+                acc += s;
+            }
+            ld[t] += acc;
+        }
+        __syncthreads();
+    }
+    // ---- loss: 0.5 |z|^2 - logdet per row
+    const float* z = Us + (size_t)f.L * 128 * d;
+    if (ok && t < 128) {
+        float q = 0.0f;
+        for (int j = 0; j < d; ++j) q += z[t * d + j] * z[t * d + j];
+        if (base + t < M) {
+            loss[base + t] = 0.5f * q - ld[t];
+            if (znorm2) znorm2[base + t] = q;
+        }
+    }
+    if (ok && grad) {
+        // ---- backward: dz = z / M, dlogdet = -1 / M (mean loss)
+        for (int e = t; e < 128 * d; e += 256) dv[e] = (base + e / d < M) ? z[e] / M : 0.0f;
+        __syncthreads();
+        float* gp = gpart + (size_t)blockIdx.x * nparams;
+        for (int l = f.L - 1; l >= 0 && ok; --l) {
+            const int da = f.da(l), db = f.db(l), a0 = f.a0(l), b0 = f.b0(l);
+            const long woff = layer_offset(l), ob0 = woff + (long)da * W, ow1 = ob0 + W, ob1 = ow1 + (long)W * W,
+                       owo = ob1 + W, obo = owo + (long)W * 2 * db;
+            // the layer's conditioner again (the last layer's is still there)
+            if (l < f.L - 1) {
+                if (!(ok = wait_weights())) break;
+                if (!(ok = conditioner(l, woff, false))) break;
+            }
+            // coupling backward: dO = (ds (1 - th^2), g) into ob (FP32) and DO
+            // (BF16), du = dv with du_B = g e^s
+            const float* u = Us + (size_t)l * 128 * d;
+            if (t < 128) {
+                for (int j = 0; j < d; ++j) du[t * d + j] = dv[t * d + j];
+                const float dlog = base + t < M ? -1.0f / M : 0.0f;
+                for (int j = 0; j < db; ++j) {
+                    const float th = tanhf(ob[t * np + j] / LG_FLOW_CLAMP);
+                    const float es = expf(LG_FLOW_CLAMP * th);
+                    const float g = dv[t * d + b0 + j];
+                    const float ds = g * u[t * d + b0 + j] * es + dlog;
+                    ob[t * np + j] = ds * (1.0f - th * th);
+                    ob[t * np + db + j] = g;
+                    du[t * d + b0 + j] = g * es;
+                }
+                for (int n = 0; n < np; ++n) DO[lg_core_off(t, n, np)] = __float2bfloat16_rn(ob[t * np + n]);
+            }
+            publish();
+            uint32_t al, as, at, bl, bs, bt;
+            // dW_out = H1^T dO (lanes k, 16 columns n); dH1 = dO W_out (lanes r)
+            begin_mma();
+            MN(W, al, as, at);
+            MN(np, bl, bs, bt);
+            chain(cWo, sH1, al, as, at, sDO, bl, bs, bt, 128 / 16, lg_umma_idesc_t(128, np, 1, 1));
+            KM(np, al, as, at);
+            MN(W, bl, bs, bt);
+            chain(cD, sDO, al, as, at, sWo, bl, bs, bt, np / 16, lg_umma_idesc_t(128, W, 0, 1));
+            // output bias gradient (FP32 dO, rows in order) under the MMAs
+            if (t < 2 * db) {
+                float s = 0.0f;
+                for (int r = 0; r < 128; ++r) s += ob[r * np + t];
+                gp[obo + t] = s;
+            }
+            if (!(ok = commit_wait())) break;
+            if (w < 4) {
+                float v[16];
+                lg_tmem_ld16(tlane + cWo, v);
+#pragma unroll
+                for (int n = 0; n < 16; ++n)
+                    if (n < 2 * db) gp[owo + (long)m * 2 * db + n] = v[n];
+            }
+            mask_epilogue(H1);  // dY1 in place of H1
+            // dW1 = H0^T dY1 (lanes k, columns n); dH0 = dY1 W1 (lanes r)
+            begin_mma();
+            MN(W, al, as, at);
+            chain(cW1, sH0, al, as, at, sH1, al, as, at, 128 / 16, lg_umma_idesc_t(128, W, 1, 1));
+            KM(W, al, as, at);
+            MN(W, bl, bs, bt);
+            chain(cD, sH1, al, as, at, sW1, bl, bs, bt, W / 16, lg_umma_idesc_t(128, W, 0, 1));
+            colsum(H1, gp + ob1);  // dense 1 bias gradient, under the MMAs
+            if (!(ok = commit_wait())) break;
+            // 16 columns at a time through shared memory, so that
+            // consecutive threads write consecutive gradient entries
+            for (int n0 = 0; n0 < W; n0 += 16) {
+                if (w < 4) {
+                    float v[16];
+                    lg_tmem_ld16(tlane + cW1 + n0, v);
+                    float4* q = reinterpret_cast<float4*>(stg + m * 16);
+#pragma unroll
+                    for (int j = 0; j < 4; ++j) q[j] = make_float4(v[4 * j], v[4 * j + 1], v[4 * j + 2], v[4 * j + 3]);
+                }
+                __syncthreads();
+#pragma unroll
+                for (int i = 0; i < 8; ++i) {
+                    const int e = t + 256 * i, k = e / 16, j = e % 16;
+                    gp[ow1 + (long)k * W + n0 + j] = stg[e];
+                }
+                __syncthreads();
+            }
+            mask_epilogue(H0);  // dY0 in place of H0
+            // dW0^T = dY0^T A0 (lanes n, columns k); dA0 = dY0 W0 (lanes r)
+            begin_mma();
+            MN(W, al, as, at);
+            MN(kp0, bl, bs, bt);
+            chain(cW0, sH0, al, as, at, sA0, bl, bs, bt, 128 / 16, lg_umma_idesc_t(128, kp0, 1, 1));
+            KM(W, al, as, at);
+            MN(kp0, bl, bs, bt);
+            chain(cX0, sH0, al, as, at, sW0, bl, bs, bt, W / 16, lg_umma_idesc_t(128, kp0, 0, 1));
+            colsum(H0, gp + ob0);  // dense 0 bias gradient, under the MMAs
+            if (!(ok = commit_wait())) break;
+            if (l > 0) issue_weights(l - 1);  // the buffer is free
+            {
+                float v[16];
+                if (w < 4) {
+                    lg_tmem_ld16(tlane + cW0, v);  // lanes n: dW0[k][n]
+#pragma unroll
+                    for (int k = 0; k < 16; ++k)
+                        if (k < da) gp[woff + (long)k * W + m] = v[k];
+                } else {
+                    lg_tmem_ld16(tlane + cX0, v);  // lanes r: dA0[r][k]
+#pragma unroll
+                    for (int k = 0; k < 16; ++k)
+                        if (k < da) du[m * d + a0 + k] += v[k];
+                }
+            }
+            asm volatile("tcgen05.fence::before_thread_sync;");
+            __syncthreads();
+            for (int e = t; e < 128 * d; e += 256) dv[e] = du[e];
+            __syncthreads();
+        }
+    }
+    if (!ok && t == 0) {
+        atomicExch(err, 1);
+        if (stop) atomicExch(stop, 1);
+        // what is still in flight completes before the tensor memory is
+        // freed and the block exits (waits with the full budget)
+        if (mma_pending) lg_mbar_wait(bars, pending_parity);
+        for (; waited < issued; ++waited) lg_mbar_wait(bars + 1, (uint32_t)waited & 1u);
+    }
+    asm volatile("tcgen05.fence::before_thread_sync;");
+    __syncthreads();
+    if (w == 0) asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" ::"r"(tmem), "r"(kCols));
 }
 
 // Counter-based uniforms in (0, 1): splitmix64 finaliser of (key, counter),
@@ -1211,8 +1695,13 @@ public:
     FlowDims f{};
     bool bf16 = true;
     bool tc = false;  // proposals' inverse on the tensor cores (BF16 activations, width % 32 == 0)
+    // training steps on the tensor cores (lg_flow_step_tc): asked for by the
+    // owner before init, on when the shape allows it
+    bool want_tct = false, tct = false;
     size_t nparams = 0;
     DevBuf<float> P, G, M1, M2, gpart, loss, znorm;
+    DevBuf<__nv_bfloat16> tpack;  // packed BF16 copy of P for lg_flow_step_tc (refreshed by the Adam steps)
+    DevBuf<int> terr;             // set when a bounded wait of lg_flow_step_tc ran out
     std::vector<float> mean, sdev;
     long step = 0;
     cudaStream_t stream = nullptr;
@@ -1231,7 +1720,7 @@ public:
         return n;
     }
 
-    int rows() const { return bf16 ? FR : FR32; }  // minibatch rows per training block
+    int rows() const { return tct ? 128 : (bf16 ? FR : FR32); }  // minibatch rows per training block
     int step_smem() const { return StepSmem(f, rows(), bf16 ? 2 : 4).total; }
     int inverse_smem() const { return InvSmem(f, FRI, bf16 ? 2 : 4).total; }
 
@@ -1259,6 +1748,13 @@ public:
         tc = bf16 && cc >= 10 && width % 32 == 0 && width <= 256 && TcDims(f).np <= width &&
              TcSmem(f).total <= optin && !std::getenv("LG_FLOW_NO_TC");
         if (tc) cudaFuncSetAttribute(lg_flow_inverse_tc, cudaFuncAttributeMaxDynamicSharedMemorySize, TcSmem(f).total);
+        // tensor-core training: width 128, two hidden layers, at most 8
+        // transformed dimensions (one 16-wide K block for the input dense,
+        // one 16-wide N block for the output dense)
+        tct = want_tct && tc && width == 128 && hidden == 2 && TcDims(f).kp0 == 16 && TcDims(f).np == 16 &&
+              TcStepSmem(f).total <= optin;
+        if (tct)
+            cudaFuncSetAttribute(lg_flow_step_tc, cudaFuncAttributeMaxDynamicSharedMemorySize, TcStepSmem(f).total);
         // the highest stream priority: training launches are small and
         // run beside the likelihood's large grids, whose blocks they then
         // pass in the queue as SMs free up
@@ -1295,6 +1791,11 @@ public:
                 o += nw + f.kout(l, k);
             }
         cudaMemcpy(P.p, host.data(), nparams * 4, cudaMemcpyHostToDevice);
+        if (tct) {
+            if (!tpack.ensure(packed_size()) || !terr.ensure(1)) return false;
+            cudaMemset(terr.p, 0, sizeof(int));
+            if (!repack(stream)) return false;
+        }
         cudaMemset(M1.p, 0, nparams * 4);
         cudaMemset(M2.p, 0, nparams * 4);
         step = 0;
@@ -1312,11 +1813,17 @@ public:
     // Enqueue one forward (+ backward) pass over rows [row0, row0 + M) of
     // the index list (or of X when idx is NULL): per-row losses in loss,
     // |z|^2 in znorm (when asked), partial gradients in gpart.
-    bool pass(const float* X, const int* idx, int row0, int M, bool grad, bool want_z, const int* stop)
+    bool pass(const float* X, const int* idx, int row0, int M, bool grad, bool want_z, int* stop)
     {
         const int blocks = (M + rows() - 1) / rows();
         if (!loss.ensure(M) || (want_z && !znorm.ensure(M)) || (grad && !gpart.ensure((size_t)blocks * nparams)))
             return false;
+        if (tct) {
+            lg_flow_step_tc<<<blocks, 256, TcStepSmem(f).total, stream>>>(
+                f, P.p, tpack.p, X, idx, row0, M, grad, loss.p, want_z ? znorm.p : nullptr, gpart.p, (long)nparams,
+                stop, terr.p, wait_tries);
+            return cudaGetLastError() == cudaSuccess;
+        }
         const int sm = step_smem();
         if (bf16)
             lg_flow_step<FR, __nv_bfloat16><<<blocks, FT, sm, stream>>>(f, P.p, X, idx, row0, M, grad, loss.p,
@@ -1341,9 +1848,13 @@ public:
         }
         lg_flow_adam<<<(unsigned)((nparams + 255) / 256), 256, 0, stream>>>(
             P.p, gpart.p, blocks, (long)nparams, adam ? nullptr : G.p, M1.p, M2.p, adam ? 1 : 0, lr, 0.9f, 0.999f,
-            c1, c2, stop);
+            c1, c2, stop, f, adam && tct ? tpack.p : nullptr);
         return cudaGetLastError() == cudaSuccess;
     }
+
+    // the training kernel's packed weights from P (after P was set from
+    // outside the Adam steps)
+    bool repack(cudaStream_t st) { return !tct || pack(P.p, tpack.p, st); }
 
     size_t packed_size() const { return (size_t)f.L * TcDims(f).sl; }
 
@@ -1485,8 +1996,9 @@ public:
         if (pending) finish();
         if (flow.f.d != d) {
             flow.bf16 = true;
-            if (!flow.init(d, opt.layers, opt.width, opt.hidden, seed)) return LG_ERR_INPUT;
+            flow.want_tct = opt.train_tc != 0;
             flow.wait_tries = opt.wait_tries == 0 ? kMbarTries : (opt.wait_tries < 0 ? 0 : opt.wait_tries);
+            if (!flow.init(d, opt.layers, opt.width, opt.hidden, seed)) return LG_ERR_INPUT;
         }
         if (!ps && cudaStreamCreateWithFlags(&ps, cudaStreamNonBlocking) != cudaSuccess) return fail_cuda();
         if (!done && cudaEventCreate(&done) != cudaSuccess) return fail_cuda();
@@ -1526,7 +2038,7 @@ public:
         const size_t nidx = (size_t)nval + (size_t)epochs * ntr, nst = 8 + LG_FLOW_HISTORY;
         if (!hx.ensure((size_t)n * d + 2 * (size_t)d) || !hidx.ensure(nidx) || !dx.ensure((size_t)n * d) ||
             !didx.ensure(nidx) || !best.ensure(flow.nparams) || !state.ensure(nst) || !dstop.ensure(1) ||
-            !hstate.ensure(nst) || !hinit.ensure(nst) || !hres.ensure(4) || !Puse[pslot].ensure(flow.nparams) ||
+            !hstate.ensure(nst) || !hinit.ensure(nst) || !hres.ensure(5) || !Puse[pslot].ensure(flow.nparams) ||
             !dmean[pslot].ensure(d) || !dsdev[pslot].ensure(d) || !dres[pslot].ensure(3) || !flow.reserve(n, Mb) ||
             !cz.ensure((size_t)16384 * d) || !cu.ensure((size_t)16384 * d) || !cld.ensure(16384) ||
             !dtcerr.ensure(2) || (flow.tc && !dpack[pslot].ensure(flow.packed_size())))
@@ -1567,7 +2079,10 @@ public:
             // timeout flags: [0] this stream's calibration, [1] the proposal
             // stream's inverses (cleared there when a flow takes over)
             cudaMemsetAsync(dtcerr.p, 0, (ntrain == 1 ? 2 : 1) * sizeof(int), s) ||
-            cudaEventRecord(started, s))
+            (flow.tct && cudaMemsetAsync(flow.terr.p, 0, sizeof(int), s)) || cudaEventRecord(started, s) ||
+            // the training kernel's packed weights (P may have been set from
+            // the best weights of the previous retraining)
+            !flow.repack(s))
             return fail_cuda();
         // the whole retraining is enqueued at once: the held-out check stops
         // it on the device, keeping the best weights
@@ -1588,7 +2103,7 @@ public:
         // best weights: the training state and the proposal slot
         if (!ok || cudaMemcpyAsync(flow.P.p, best.p, flow.nparams * 4, cudaMemcpyDeviceToDevice, s) ||
             cudaMemcpyAsync(Puse[pslot].p, best.p, flow.nparams * 4, cudaMemcpyDeviceToDevice, s) ||
-            (flow.tc && !flow.pack(Puse[pslot].p, dpack[pslot].p, s)))
+            (flow.tc && !flow.pack(Puse[pslot].p, dpack[pslot].p, s)) || !flow.repack(s))
             return fail_cuda();
         // latent radius of the live points: max |z|^2 over all of them
         if (!flow.pass(dx.p, nullptr, 0, n, false, true, nullptr)) return fail_cuda();
@@ -1601,8 +2116,10 @@ public:
         if (!flow.inverse(Puse[pslot].p, dpack[pslot].p, cz.p, Mc, cu.p, cld.p, s, dtcerr.p)) return fail_cuda();
         lg_flow_max<<<1, 1024, 0, s>>>(cld.p, Mc, -INFINITY, r + 1);
         lg_flow_expsum<<<1, 1024, 0, s>>>(cld.p, Mc, r + 1);
+        hres.p[4] = 0;  // (no retraining is pending: nothing writes hres now)
         if (cudaMemcpyAsync(hres.p, r, 3 * sizeof(double), cudaMemcpyDeviceToHost, s) ||
             cudaMemcpyAsync(hres.p + 3, dtcerr.p, sizeof(int), cudaMemcpyDeviceToHost, s) ||
+            (flow.tct && cudaMemcpyAsync(hres.p + 4, flow.terr.p, sizeof(int), cudaMemcpyDeviceToHost, s)) ||
             cudaMemcpyAsync(hstate.p, state.p, nst * sizeof(float), cudaMemcpyDeviceToHost, s) ||
             cudaEventRecord(done, s))
             return fail_cuda();
@@ -1634,11 +2151,13 @@ public:
         const double mx = hres.p[1];
         wnorm[k] = mx + 1.0;
         efficiency[k] = hres.p[2] * std::exp(-1.0) / 16384;  // mean exp(w - wnorm)
-        int tcerr = 0;
+        int tcerr = 0, trerr = 0;
         std::memcpy(&tcerr, hres.p + 3, sizeof tcerr);
+        std::memcpy(&trerr, hres.p + 4, sizeof trerr);
         usable[k] = std::isfinite(radius[k]) && radius[k] > 0 && std::isfinite(mx) && efficiency[k] >= kMinKept &&
-                    tcerr == 0;
+                    tcerr == 0 && trerr == 0;
         if (tcerr) std::fprintf(stderr, "lensed_gb300: flow inverse: a bounded wait ran out; flow not used\n");
+        if (trerr) std::fprintf(stderr, "lensed_gb300: flow training: a bounded wait ran out; flow not used\n");
         act = usable[k] ? k : -1;
         ++gen[k];
         kept_frac[k] = efficiency[k];
@@ -1910,6 +2429,7 @@ lg_flow_options lg_flow_defaults(void)
     o.lag = 800;
     o.draw_cost = 0.005;
     o.wait_tries = 0;
+    o.train_tc = 1;
     return o;
 }
 
@@ -1939,8 +2459,13 @@ int lg_flow_fit(int device, int d, const lg_flow_options* opts, const double* pt
     p->finish();
     for (int i = 0; i < max_history && history; ++i) history[i] = i < LG_FLOW_HISTORY ? p->hstate.p[8 + i] : NAN;
     if (efficiency) *efficiency = p->efficiency[p->pslot];
-    int tcerr = 0;
+    int tcerr = 0, trerr = 0;
     std::memcpy(&tcerr, p->hres.p + 3, sizeof tcerr);
+    std::memcpy(&trerr, p->hres.p + 4, sizeof trerr);
+    if (trerr) {
+        lg::set_global_error("flow fit: a bounded wait of the tensor-core training step ran out");
+        return LG_ERR_TIMEOUT;
+    }
     if (tcerr) {
         lg::set_global_error("flow fit: a bounded wait of the tensor-core inverse ran out (calibration)");
         return LG_ERR_TIMEOUT;
@@ -2034,6 +2559,55 @@ int lg_flow_inverse_time(int device, int d, int layers, int width, int hidden, i
     return herr ? LG_ERR_TIMEOUT : LG_OK;
 }
 
+// Device time of training steps (forward + backward of a minibatch of
+// `batch` rows, then the Adam step) on n points uploaded once: tc = 1 the
+// tensor-core step, 0 the FP32-weight step with BF16 activations; reps
+// steps after two warm-up steps, CUDA events on the launching stream; *ms =
+// milliseconds per step (both launches).
+int lg_flow_train_time(int device, int d, int layers, int width, int hidden, int tc, const float* params,
+                       const float* x, int n, int batch, int reps, float* ms)
+{
+    if (!params || !x || !ms || n <= 0 || batch <= 0 || batch > n || reps <= 0) return LG_ERR_INPUT;
+    if (cudaSetDevice(device) != cudaSuccess) return LG_ERR_CUDA;
+    lg::Flow f;
+    f.bf16 = true;
+    f.want_tct = tc != 0;
+    if (!f.init(d, layers, width, hidden, 1)) {
+        lg::set_global_error(f.err.c_str());
+        return f.err.empty() ? LG_ERR_ALLOC : LG_ERR_INPUT;
+    }
+    if (tc && !f.tct) {
+        lg::set_global_error("flow training timing: the tensor-core step needs width 128, two hidden layers, d <= 16 "
+                             "and sm_100+");
+        return LG_ERR_UNSUPPORTED;
+    }
+    lg::DevBuf<float> dx;
+    if (!dx.ensure((size_t)n * d) || !f.reserve(n, batch)) return LG_ERR_ALLOC;
+    cudaEvent_t e0 = nullptr, e1 = nullptr;
+    if (cudaMemcpy(f.P.p, params, f.nparams * 4, cudaMemcpyHostToDevice) ||
+        cudaMemcpy(dx.p, x, (size_t)n * d * 4, cudaMemcpyHostToDevice) || !f.repack(f.stream) ||
+        cudaEventCreate(&e0) || cudaEventCreate(&e1))
+        return LG_ERR_CUDA;
+    const int nb = n / batch;
+    auto step = [&](int i) {
+        return f.pass(dx.p, nullptr, (i % nb) * batch, batch, true, false, nullptr) &&
+               f.update(batch, true, 1e-4f, nullptr);
+    };
+    bool ok = step(0) && step(1);
+    ok = ok && cudaEventRecord(e0, f.stream) == cudaSuccess;
+    for (int i = 0; i < reps && ok; ++i) ok = step(i);
+    int herr = 0;
+    float t = 0;
+    ok = ok && cudaEventRecord(e1, f.stream) == cudaSuccess &&
+         (!f.tct || cudaMemcpyAsync(&herr, f.terr.p, sizeof(int), cudaMemcpyDeviceToHost, f.stream) == cudaSuccess) &&
+         cudaStreamSynchronize(f.stream) == cudaSuccess && cudaEventElapsedTime(&t, e0, e1) == cudaSuccess;
+    cudaEventDestroy(e0);
+    cudaEventDestroy(e1);
+    if (!ok) return LG_ERR_CUDA;
+    *ms = t / reps;
+    return herr ? LG_ERR_TIMEOUT : LG_OK;
+}
+
 // Loss and gradient of the flow on n points (standardised space, host
 // arrays), for gradient checks against the CPU restatement: params in,
 // loss (mean over the points) and grad out.  bf16 = 0 keeps activations in
@@ -2045,20 +2619,34 @@ int lg_flow_loss_grad(int device, int d, int layers, int width, int hidden, int 
     if (cudaSetDevice(device) != cudaSuccess) return LG_ERR_CUDA;
     lg::Flow f;
     f.bf16 = bf16 != 0;
+    f.want_tct = bf16 == 2;
     if (!f.init(d, layers, width, hidden, 1)) {
         lg::set_global_error(f.err.c_str());
         return f.err.empty() ? LG_ERR_ALLOC : LG_ERR_INPUT;
+    }
+    if (bf16 == 2 && !f.tct) {
+        lg::set_global_error("flow loss/grad: the tensor-core training step needs width 128, two hidden layers, "
+                             "d <= 16 and sm_100+");
+        return LG_ERR_UNSUPPORTED;
     }
     cudaMemcpy(f.P.p, params, f.nparams * 4, cudaMemcpyHostToDevice);
     lg::DevBuf<float> dx;
     if (!dx.ensure((size_t)n * d)) return LG_ERR_ALLOC;
     cudaMemcpy(dx.p, x, (size_t)n * d * 4, cudaMemcpyHostToDevice);
-    if (!f.pass(dx.p, nullptr, 0, n, true, false, nullptr) || !f.update(n, false, 0.0f, nullptr)) return LG_ERR_CUDA;
+    if (!f.repack(f.stream) || !f.pass(dx.p, nullptr, 0, n, true, false, nullptr) ||
+        !f.update(n, false, 0.0f, nullptr))
+        return LG_ERR_CUDA;
     std::vector<float> per(n);
+    int herr = 0;
     if (cudaMemcpyAsync(per.data(), f.loss.p, (size_t)n * 4, cudaMemcpyDeviceToHost, f.stream) ||
         cudaMemcpyAsync(grad, f.G.p, f.nparams * 4, cudaMemcpyDeviceToHost, f.stream) ||
+        (f.tct && cudaMemcpyAsync(&herr, f.terr.p, sizeof(int), cudaMemcpyDeviceToHost, f.stream)) ||
         cudaStreamSynchronize(f.stream))
         return LG_ERR_CUDA;
+    if (herr) {
+        lg::set_global_error("flow loss/grad: a bounded wait of the tensor-core training step ran out");
+        return LG_ERR_TIMEOUT;
+    }
     double s = 0;
     for (float v : per) s += v;
     *loss = (float)(s / n);

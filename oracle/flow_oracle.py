@@ -90,6 +90,66 @@ def bf16(a):
     return bits.astype(np.uint32).view(np.float32).astype(np.float64)
 
 
+def loss_grad_tc(params, x, d, layers, width, hidden):
+    """loss_grad with the rounding points of the tensor-core training step
+    (lg_flow_step_tc): weights, conditioner input and hidden activations in
+    bfloat16 (forward), the output-layer gradient dO and the masked hidden
+    gradients dY rounded to bfloat16 before they enter the products;
+    dense-layer bias gradients summed from the rounded dY, the output bias
+    gradient from the unrounded dO.  Float64 arithmetic otherwise."""
+    L, n = layout(d, layers, width, hidden)
+    p = np.asarray(params, np.float64)
+    M = x.shape[0]
+    grad = np.zeros_like(p)
+    us, caches = [np.asarray(x, np.float64)], []
+    logdet = np.zeros(M)
+    for (da, db, a0, b0, dense) in L:
+        u = us[-1]
+        acts = [bf16(u[:, a0:a0 + da])]
+        for k, (w0, kin, kout, b) in enumerate(dense):
+            W = bf16(p[w0:w0 + kin * kout].reshape(kin, kout))
+            z = acts[-1] @ W + p[b:b + kout]
+            acts.append(bf16(np.maximum(z, 0)) if k < len(dense) - 1 else z)
+        o = acts[-1]
+        sr, t = o[:, :db], o[:, db:]
+        s = CLAMP * np.tanh(sr / CLAMP)
+        v = u.copy()
+        v[:, b0:b0 + db] = u[:, b0:b0 + db] * np.exp(s) + t
+        logdet += s.sum(1)
+        caches.append((acts, sr, s))
+        us.append(v)
+    z = us[-1]
+    loss = np.mean(0.5 * np.sum(z * z, 1) - logdet)
+    dv = z / M
+    for li in range(len(L) - 1, -1, -1):
+        da, db, a0, b0, dense = L[li]
+        acts, sr, s = caches[li]
+        u = us[li]
+        g = dv[:, b0:b0 + db]
+        es = np.exp(s)
+        ds = g * u[:, b0:b0 + db] * es - 1.0 / M
+        th = np.tanh(sr / CLAMP)
+        dout = np.concatenate([ds * (1 - th * th), g], axis=1)
+        du = dv.copy()
+        du[:, b0:b0 + db] = g * es
+        w0, kin, kout, b = dense[-1]
+        grad[b:b + kout] = dout.sum(0)
+        dcur = bf16(dout)
+        for k in range(len(dense) - 1, -1, -1):
+            w0, kin, kout, b = dense[k]
+            W = bf16(p[w0:w0 + kin * kout].reshape(kin, kout))
+            grad[w0:w0 + kin * kout] = (acts[k].T @ dcur).ravel()
+            if k < len(dense) - 1:
+                grad[b:b + kout] = dcur.sum(0)
+            dprev = dcur @ W.T
+            if k > 0:
+                dprev = bf16(dprev * (acts[k] > 0))
+            dcur = dprev
+        du[:, a0:a0 + da] += dcur
+        dv = du
+    return loss, grad
+
+
 def inverse(params, z, d, layers, width, hidden, mode="fp32"):
     """Inverse flow z -> u and log|det du/dz| in float64, with the rounding
     points of the library's kernels: mode "fp32" none, "bf16" hidden

@@ -43,6 +43,76 @@ def test_flow_gradients_bf16_activations(native):
     assert err <= 5e-2, err
 
 
+def _tc_case(n, seed=1, d=13, layers=4):
+    import ctypes as C
+
+    width, hidden = 128, 2
+    rng = np.random.Generator(np.random.PCG64(seed))
+    npar = lg.lib().lg_flow_nparams(d, layers, width, hidden)
+    params = (rng.normal(size=npar) * 0.05).astype(np.float32)
+    x = rng.normal(size=(n, d)).astype(np.float32)
+    loss = C.c_float()
+    grad = np.zeros(npar, np.float32)
+    rc = lg.lib().lg_flow_loss_grad(0, d, layers, width, hidden, 2, params.ctypes.data_as(C.POINTER(C.c_float)),
+                                    x.ctypes.data_as(C.POINTER(C.c_float)), n, C.byref(loss),
+                                    grad.ctypes.data_as(C.POINTER(C.c_float)))
+    assert rc == 0, lg.lib().lg_last_error(None)
+    return params, x, loss.value, grad
+
+
+@pytest.mark.parametrize("n", [128, 200, 256])
+def test_flow_gradients_tensor_core_training_step(native, n):
+    """lg_flow_step_tc (tcgen05: BF16 operands, FP32 accumulators in tensor
+    memory, transposed operands for the backward products) against the CPU
+    restatement with the same rounding points; one, two ragged and two full
+    128-row blocks.  Against the FP32 restatement the BF16 rounding moves
+    the gradient by under 1%."""
+    d, layers, width, hidden = 13, 4, 128, 2
+    params, x, l, g = _tc_case(n)
+    wl, wg = flow_oracle.loss_grad_tc(params.astype(np.float64), x.astype(np.float64), d, layers, width, hidden)
+    err = np.abs(g - wg).max() / np.abs(wg).max()
+    print(f"n {n}: loss {l:.6f} vs {wl:.6f}; max grad error {err:.2e} of the largest component")
+    assert abs(l - wl) <= 1e-4 * abs(wl)
+    assert err <= 2e-3, err
+    fl, fg = flow_oracle.loss_grad(params.astype(np.float64), x.astype(np.float64), d, layers, width, hidden)
+    assert np.abs(g - fg).max() / np.abs(fg).max() <= 2e-2
+    # deterministic: the same bits again
+    _, _, l2, g2 = _tc_case(n)
+    assert l2 == l and np.array_equal(g2, g)
+
+
+def test_tensor_core_training_matches_fp32_training(native):
+    """A retraining with tensor-core steps lowers the held-out loss about as
+    far as one with the FP32-weight steps (same points, epochs and early
+    stopping)."""
+    rng = np.random.Generator(np.random.PCG64(4))
+    base = rng.normal(size=(1000, 8))
+    pts = np.column_stack([base[:, :4], base[:, 4:] * 0.2 + 0.5 * base[:, :4] ** 2])
+    flow = dict(layers=8, width=128, hidden=2, epochs=60)
+    h_tc, e_tc = lg.flow_fit(pts, train_tc=1, **flow)
+    h_32, e_32 = lg.flow_fit(pts, train_tc=0, **flow)
+    best_tc, best_32 = np.nanmin(h_tc), np.nanmin(h_32)
+    print(f"held-out loss: start {h_tc[0]:.4f}; best tensor-core {best_tc:.4f} ({np.sum(np.isfinite(h_tc)) - 1} "
+          f"epochs, kept {e_tc:.3f}); best FP32 {best_32:.4f} ({np.sum(np.isfinite(h_32)) - 1} epochs, kept {e_32:.3f})")
+    assert best_tc < h_tc[0] - 0.2 and best_32 < h_32[0] - 0.2
+    assert abs(best_tc - best_32) < 0.15 * abs(h_tc[0] - best_32)
+
+
+def test_tensor_core_training_timeout_is_reported_and_survived(native):
+    """wait_tries < 0 with the tensor-core training step (width 128, two
+    hidden layers): its first bounded wait gives up, the kernel flags the
+    error and stops the retraining, and the fit reports LG_ERR_TIMEOUT; the
+    next fit with the default budget trains normally."""
+    rng = np.random.Generator(np.random.PCG64(5))
+    pts = rng.normal(size=(600, 6))
+    flow = dict(layers=4, width=128, hidden=2, epochs=5)
+    with pytest.raises(lg.LensedError) as e:
+        lg.flow_fit(pts, wait_tries=-1, **flow)
+    assert e.value.code == -5  # LG_ERR_TIMEOUT
+    hist, eff = lg.flow_fit(pts, **flow)
+    assert np.all(np.isfinite(hist[:2])) and eff > 0
+
+
 def banana(x):
     """Three curved ridges: x_{2i+1} ~ 0.3 + 1.5 (x_{2i} - 0.5)^2 +- 0.01."""
     ll = np.zeros(x.shape[0])
