@@ -103,6 +103,8 @@ def run_sampler(args):
     out = {}
     seeds = [11 + 7 * k for k in range(max(1, args.sampler_seeds))]
     flow = {"layers": args.flow_layers, "width": args.flow_width, "epochs": args.flow_epochs}
+    if args.train_tc >= 0:
+        flow["train_tc"] = args.train_tc
     arms = [("plain", {}), ("flow", {"proposal": lg.PROPOSAL_FLOW, "flow_every": 1000})]
     if args.max_ellipsoids > 1:
         arms.append(("plain_multi", {"max_ellipsoids": args.max_ellipsoids}))
@@ -439,6 +441,8 @@ def main():
     ap.add_argument("--flow-layers", type=int, default=8)
     ap.add_argument("--flow-width", type=int, default=128)
     ap.add_argument("--flow-epochs", type=int, default=200)
+    ap.add_argument("--train-tc", type=int, default=-1,
+                    help="sampler workload: 1 tensor-core training steps, 0 the FP32-weight ones (-1: the default)")
     ap.add_argument("--skip-plain", action="store_true")
     ap.add_argument("--sampler-seeds", type=int, default=16,
                     help="sampler workload: runs (seeds) per sampler (one run's ln Z scatters by about 0.2)")

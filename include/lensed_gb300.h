@@ -446,7 +446,7 @@ typedef struct {
     int train_tc;     /* 1: training steps on the tensor cores (lg_flow_step_tc: BF16 weights,
                          conditioner inputs and activations, FP32 accumulators in tensor memory)
                          when the shape allows it (width 128, two hidden layers, d <= 16, sm_100+);
-                         0: the FP32-weight training kernels */
+                         0 (default): the FP32-weight training kernels (BF16 activations) */
 } lg_flow_options;
 
 typedef int (*lg_batch_loglike)(void* user, const double* cube, int B, double* logL);

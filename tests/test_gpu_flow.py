@@ -105,12 +105,26 @@ def test_tensor_core_training_timeout_is_reported_and_survived(native):
     next fit with the default budget trains normally."""
     rng = np.random.Generator(np.random.PCG64(5))
     pts = rng.normal(size=(600, 6))
-    flow = dict(layers=4, width=128, hidden=2, epochs=5)
+    flow = dict(layers=4, width=128, hidden=2, epochs=5, train_tc=1)
     with pytest.raises(lg.LensedError) as e:
         lg.flow_fit(pts, wait_tries=-1, **flow)
     assert e.value.code == -5  # LG_ERR_TIMEOUT
+    assert "training step" in str(e.value)
     hist, eff = lg.flow_fit(pts, **flow)
     assert np.all(np.isfinite(hist[:2])) and eff > 0
+
+
+def test_learned_sampler_with_tensor_core_training(native):
+    """The sampler with the learned proposal trained by the tensor-core
+    steps reaches the closed-form evidence of the curved posterior."""
+    d = 4
+    exact = 2 * math.log(2 * math.pi * 0.15 * 0.01)
+    r = lg.nested_sample_flow(banana, d, nlive=400, batch=512, seed=7, tol=0.1, flow_every=400,
+                              flow=dict(layers=8, width=128, hidden=2, train_tc=1))
+    print(f"tensor-core training: lnZ {r['logz']:.3f} +- {r['logz_err']:.3f} (exact {exact:.3f}), "
+          f"{r['ncall']} calls, {r['n_flow_proposals']} from the flow")
+    assert r["n_flow_proposals"] > 0
+    assert abs(r["logz"] - exact) < 4 * r["logz_err"] + 0.1
 
 
 def banana(x):
