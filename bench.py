@@ -57,7 +57,8 @@ UNIT = "evals/s"
 # matched the bench's CUDA events): the render writes the raw models
 # (268 MB algorithmic; about 60 MB are still in L2 when it ends) and the
 # convolution reads them once (268 MB) -- no re-reads.
-MEASURED_TRAFFIC = {("config2", 1024, "render"): 208.45e6, ("config2", 1024, "convolve"): 269.2e6}
+MEASURED_TRAFFIC = {("config2", 1024, "render", "fast"): 208.45e6, ("config2", 1024, "convolve", "fast"): 269.2e6,
+                    ("config2", 1024, "render", "exact"): 210.09e6, ("config2", 1024, "convolve", "exact"): 270.17e6}
 # Thread instructions per ray of the render kernel (ncu smsp__inst_executed.sum
 # x 32 / rays of the launch) per floating-point mode, config2 workload: the
 # render is bound by instruction issue (4 warp instructions per SM and cycle),
@@ -635,9 +636,9 @@ def main():
             "bound": "fp32", "achieved": ach, "peak": peak, "unit": "TFLOP/s", "frac": ach / peak,
             "peak_source": "measured FP32 FMA probe (lg_measure_fp32_peak) on this GPU" if peak_fp32 else
                            "nominal 152 SM x 128 lanes x 2 flop x 2070 MHz",
-            "nominal_peak": nominal, "traffic": MEASURED_TRAFFIC.get((args.workload, B, dom)),
-            "traffic_source": "ncu dram__bytes_read.sum + dram__bytes_write.sum, one launch of this workload"
-                              if (args.workload, B, dom) in MEASURED_TRAFFIC else None,
+            "nominal_peak": nominal, "traffic": MEASURED_TRAFFIC.get((args.workload, B, dom, mode_name(args.flags))),
+            "traffic_source": "ncu dram__bytes_read.sum + dram__bytes_write.sum, one launch of this workload and mode"
+                              if (args.workload, B, dom, mode_name(args.flags)) in MEASURED_TRAFFIC else None,
             "algorithmic_flops_per_launch": render_flops if dom == "render" else conv_flops,
             "stage_ms": {"set_params": float(stage[0]), "render": float(stage[1]), "convolve": float(stage[2]),
                          "finish": float(stage[3])},

@@ -781,13 +781,20 @@ __global__ void __launch_bounds__(256)
     }
 }
 
+// Two floats as BF16 (round to nearest even), the first in the low half.
+__device__ __forceinline__ uint32_t lg_pack_bf16(float lo, float hi)
+{
+    return (uint32_t)__bfloat16_as_ushort(__float2bfloat16_rn(lo)) |
+           ((uint32_t)__bfloat16_as_ushort(__float2bfloat16_rn(hi)) << 16);
+}
+
 // Shared-memory layout of lg_flow_inverse_tc (bytes): one layer's weights,
 // the conditioner input and one hidden activation tile (each epilogue
 // overwrites the tile its MMA chain has finished reading), so that two
 // blocks fit on an SM and one block's epilogues overlap the other's MMAs
 // and weight copies.
 struct TcSmem {
-    int wbuf, a0, a1, cur, obuf, ld, bar, total;
+    int wbuf, a0, a1, cur, obuf, ld, bias, bar, total;
     __host__ __device__ explicit TcSmem(const FlowDims& f)
     {
         const TcDims t(f);
@@ -803,6 +810,7 @@ struct TcSmem {
         cur = take(128 * f.d * 4);
         obuf = take(128 * t.np * 4);
         ld = take(128 * 4);
+        bias = take((f.NH * f.W + t.np) * 4);
         bar = take(64);
         total = q;
     }
@@ -824,6 +832,7 @@ __global__ void __launch_bounds__(256, 2)
     float* cur = reinterpret_cast<float*>(smem + L.cur);
     float* ob = reinterpret_cast<float*>(smem + L.obuf);
     float* ld = reinterpret_cast<float*>(smem + L.ld);
+    float* bsm = reinterpret_cast<float*>(smem + L.bias);  // the layer's biases: hidden denses, output
     uint64_t* bars = reinterpret_cast<uint64_t*>(smem + L.bar);  // [0] MMA, [1] weights
     uint32_t* misc = reinterpret_cast<uint32_t*>(smem + L.bar + 32);  // [0] TMEM base, [1] abort flag
     const uint32_t lbytes = 2u * td.sl;
@@ -893,21 +902,21 @@ __global__ void __launch_bounds__(256, 2)
     // into A1 (128 x W core matrices; the chain that read A1 has completed);
     // warp w reads lanes of w % 4, warps 0-3 the first half of the columns,
     // 4-7 the second
-    auto hidden_epilogue = [&](const float* __restrict__ bias) {
+    auto hidden_epilogue = [&](const float* bias) {
         const int m = 32 * (w % 4) + lane, half = w / 4;
         const uint32_t taddr = tmem + ((uint32_t)(32 * (w % 4)) << 16);
         for (int n0 = half * (W / 2); n0 < (half + 1) * (W / 2); n0 += 16) {
             float v[16];
             lg_tmem_ld16(taddr + n0, v);
-            __align__(16) __nv_bfloat16 h[16];
+            uint32_t h[8];
 #pragma unroll
-            for (int j = 0; j < 16; ++j) {
-                const float x = v[j] + __ldg(bias + n0 + j);
-                h[j] = __float2bfloat16_rn(x > 0.0f ? x : 0.0f);
+            for (int j = 0; j < 8; ++j) {
+                const float x0 = v[2 * j] + bias[n0 + 2 * j], x1 = v[2 * j + 1] + bias[n0 + 2 * j + 1];
+                h[j] = lg_pack_bf16(x0 > 0.0f ? x0 : 0.0f, x1 > 0.0f ? x1 : 0.0f);
             }
             uint4* dst = reinterpret_cast<uint4*>(A1 + lg_core_off(m, n0, W));
-            dst[0] = reinterpret_cast<const uint4*>(h)[0];
-            dst[8] = reinterpret_cast<const uint4*>(h)[1];  // next core matrix along K: +64 elements
+            dst[0] = make_uint4(h[0], h[1], h[2], h[3]);
+            dst[8] = make_uint4(h[4], h[5], h[6], h[7]);  // next core matrix along K: +64 elements
         }
         asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
         asm volatile("tcgen05.fence::before_thread_sync;");
@@ -919,6 +928,14 @@ __global__ void __launch_bounds__(256, 2)
         long woff = 0;
         for (int ll = 0; ll < l; ++ll)
             for (int kk = 0; kk <= NH; ++kk) woff += (long)f.kin(ll, kk) * f.kout(ll, kk) + f.kout(ll, kk);
+        // the layer's biases into shared memory (read by every epilogue)
+        for (int e = t; e < NH * W + td.np; e += 256) {
+            long o = woff;
+            const int kk = e < NH * W ? e / W : NH, n = e < NH * W ? e - kk * W : e - NH * W;
+            for (int j = 0; j < kk; ++j) o += (long)f.kin(l, j) * f.kout(l, j) + f.kout(l, j);
+            o += (long)f.kin(l, kk) * f.kout(l, kk);
+            bsm[e] = n < f.kout(l, kk) ? P[o + n] : 0.0f;
+        }
         // the conditioning half as BF16 A0 (zero padding to kp0)
         for (int e = t; e < 128 * td.kp0; e += 256) {
             const int m = e / td.kp0, k = e - m * td.kp0;
@@ -935,20 +952,19 @@ __global__ void __launch_bounds__(256, 2)
         // input dense
         long bo = woff + (long)f.kin(l, 0) * f.kout(l, 0);
         if (!(ok = gemm(A0, wb, td.kp0, W))) break;
-        hidden_epilogue(P + bo);
+        hidden_epilogue(bsm);
         long wo = bo + f.kout(l, 0);
         // hidden denses, in place in A1
         for (int k = 1; k < NH && ok; ++k) {
             ok = gemm(A1, wb + 2 * (td.s0 + (size_t)(k - 1) * td.sh), W, W);
             if (!ok) break;
             bo = wo + (long)f.kin(l, k) * f.kout(l, k);
-            hidden_epilogue(P + bo);
+            hidden_epilogue(bsm + k * W);
             wo = bo + f.kout(l, k);
         }
         if (!ok) break;
         // output dense
         if (!(ok = gemm(A1, wb + 2 * (td.s0 + (size_t)(NH - 1) * td.sh), W, td.np))) break;
-        const float* obias = P + wo + (long)f.kin(l, NH) * f.kout(l, NH);
         // this layer's weights are consumed: the next layer's copy runs
         // under the output epilogue and the coupling
         if (l - 1 >= 0) {
@@ -971,8 +987,8 @@ __global__ void __launch_bounds__(256, 2)
         if (t < 128) {
             float acc = 0.0f;
             for (int j = 0; j < db; ++j) {
-                const float sr = ob[t * td.np + j] + __ldg(obias + j);
-                const float tt = ob[t * td.np + db + j] + __ldg(obias + db + j);
+                const float sr = ob[t * td.np + j] + bsm[NH * W + j];
+                const float tt = ob[t * td.np + db + j] + bsm[NH * W + db + j];
                 const float s = LG_FLOW_CLAMP * tanhf(sr / LG_FLOW_CLAMP);
                 cur[t * d + b0 + j] = (cur[t * d + b0 + j] - tt) * expf(-s);
                 acc -= s;
@@ -1051,13 +1067,6 @@ struct TcStepSmem {
         total = q;
     }
 };
-
-// Two floats as BF16 (round to nearest even), the first in the low half.
-__device__ __forceinline__ uint32_t lg_pack_bf16(float lo, float hi)
-{
-    return (uint32_t)__bfloat16_as_ushort(__float2bfloat16_rn(lo)) |
-           ((uint32_t)__bfloat16_as_ushort(__float2bfloat16_rn(hi)) << 16);
-}
 
 // Instruction descriptor with operand majors: amaj / bmaj = 1 for an
 // MN-major (transposed) A / B.
