@@ -301,11 +301,14 @@ int lg_compile_check_shape(const lg_image_desc* image, const lg_object_desc* obj
 int lg_probe_pair_math(int device, int fn, const float* x, int n, float* out);
 
 /* Diagnostic: compares the exact modules' correctly rounded exp (fn = 0),
- * log (1), atan (2) or atanh (3), on ray pairs, with the function evaluated
- * in double and rounded once, for every float whose bit pattern lies in
- * [lo, hi) (hi <= 2^32), on a device.  *mismatches receives the number of
- * inputs whose results differ (NaN matches NaN); the first nfirst of their
- * bit patterns go to first. */
+ * log (1), atan (2) or atanh (3), on ray pairs, or sin (4), cos (5),
+ * pow(x, Y[u % 16]) (6: sixteen fixed exponents, those of the EPL lens among
+ * them), atan2(x, p) (7) or pow(|x|, p) (8), with p the float of bit pattern
+ * u * 0x9E3779B1, one value at a time, with the function evaluated in double
+ * and rounded once, for every float x whose bit pattern u lies in [lo, hi)
+ * (hi <= 2^32), on a device.  *mismatches receives the number of inputs
+ * whose results differ (NaN matches NaN); the first nfirst of their bit
+ * patterns go to first. */
 int lg_probe_crf_sweep(int device, int fn, unsigned long long lo, unsigned long long hi,
                        unsigned long long* mismatches, unsigned* first, int nfirst);
 

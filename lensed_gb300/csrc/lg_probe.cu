@@ -32,6 +32,35 @@ __device__ float crf_double(int fn, float x)
                      : (float)atanh((double)x);
 }
 
+// the EPL lens's functions, one value: fn 4 sin, 5 cos, 6 pow(x, Y[u % 16])
+// with the lens's exponents and others, 7 atan2(x, p), 8 pow(|x|, p), p the
+// float of bit pattern u * 0x9E3779B1 (the second argument swept too)
+__constant__ float lg_probe_y[16] = {-1.2f, -1.0f, -0.8f, -0.5f, 0.5f, -0.25f, 0.2f, 1.0f / 3,
+                                     2.5f, -2.2f, 0.999f, 1.5f, -0.1f, 3.7f, 0.05f, -7.5f};
+__device__ float crf_two(int fn, float x, unsigned u)
+{
+    const float p = __uint_as_float(u * 0x9E3779B1u);
+    float s, c;
+    switch (fn) {
+    case 4: lg_crf_sincos(x, &s, &c); return s;
+    case 5: lg_crf_sincos(x, &s, &c); return c;
+    case 6: return lg_crf_pow(x, lg_probe_y[u % 16]);
+    case 7: return lg_crf_atan2(x, p);
+    default: return lg_crf_pow(fabsf(x), p);
+    }
+}
+__device__ float crf_two_double(int fn, float x, unsigned u)
+{
+    const float p = __uint_as_float(u * 0x9E3779B1u);
+    switch (fn) {
+    case 4: return (float)sin((double)x);
+    case 5: return (float)cos((double)x);
+    case 6: return (float)pow((double)x, (double)lg_probe_y[u % 16]);
+    case 7: return (float)atan2((double)x, (double)p);
+    default: return (float)pow((double)fabsf(x), (double)p);
+    }
+}
+
 // every bit pattern u in [lo, hi) as lane 0 of a pair whose lane 1 is an
 // unrelated input (u times an odd constant, a bijection of the 32-bit
 // patterns), so that the lanes of a pair take different paths and table
@@ -45,6 +74,15 @@ __global__ void lg_crf_sweep_kernel(int fn, unsigned long long lo, unsigned long
     unsigned long long nbad = 0;
     for (unsigned long long u = lo + blockIdx.x * (unsigned long long)blockDim.x + threadIdx.x; u < hi; u += stride) {
         const float x0 = __uint_as_float((unsigned)u);
+        if (fn >= 4) {
+            const float r0 = crf_two(fn, x0, (unsigned)u), w0 = crf_two_double(fn, x0, (unsigned)u);
+            if (!(__float_as_uint(r0) == __float_as_uint(w0) || (r0 != r0 && w0 != w0))) {
+                ++nbad;
+                const unsigned long long k = atomicAdd(bad + 1, 1ull);
+                if (k < (unsigned long long)nfirst) first[k] = (unsigned)u;
+            }
+            continue;
+        }
         const float x1 = __uint_as_float((unsigned)u * 0x9E3779B1u);
         const float2 r = crf_pair(fn, make_float2(x0, x1));
         const float w0 = crf_double(fn, x0), w1 = crf_double(fn, x1);
@@ -112,7 +150,7 @@ extern "C" int lg_probe_pair_math(int device, int fn, const float* x, int n, flo
 extern "C" int lg_probe_crf_sweep(int device, int fn, unsigned long long lo, unsigned long long hi,
                                   unsigned long long* mismatches, unsigned* first, int nfirst)
 {
-    if (fn < 0 || fn > 3 || lo > hi || hi > (1ull << 32) || !mismatches || nfirst < 0 || (nfirst && !first))
+    if (fn < 0 || fn > 8 || lo > hi || hi > (1ull << 32) || !mismatches || nfirst < 0 || (nfirst && !first))
         return LG_ERR_INPUT;
     auto fail = [](cudaError_t e) {
         lg::set_global_error(cudaGetErrorString(e));

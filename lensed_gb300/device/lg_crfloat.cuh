@@ -95,6 +95,14 @@ LG_CRF_DEV float crf_slow_exp(float x) { LG_CRF_SLOW_COUNT(); return (float)std:
 LG_CRF_DEV float crf_slow_log(float x) { LG_CRF_SLOW_COUNT(); return (float)std::log((double)x); }
 LG_CRF_DEV float crf_slow_atan(float x) { LG_CRF_SLOW_COUNT(); return (float)std::atan((double)x); }
 LG_CRF_DEV float crf_slow_atanh(float x) { LG_CRF_SLOW_COUNT(); return (float)std::atanh((double)x); }
+LG_CRF_DEV float crf_slow_sin(float x) { LG_CRF_SLOW_COUNT(); return (float)std::sin((double)x); }
+LG_CRF_DEV float crf_slow_cos(float x) { LG_CRF_SLOW_COUNT(); return (float)std::cos((double)x); }
+LG_CRF_DEV float crf_slow_pow(float x, float y) { LG_CRF_SLOW_COUNT(); return (float)std::pow((double)x, (double)y); }
+LG_CRF_DEV float crf_slow_atan2(float y, float x)
+{
+    LG_CRF_SLOW_COUNT();
+    return (float)std::atan2((double)y, (double)x);
+}
 #else
 LG_CRF_DEV float crf_add(float a, float b) { return __fadd_rn(a, b); }
 LG_CRF_DEV float crf_sub(float a, float b) { return __fsub_rn(a, b); }
@@ -157,6 +165,10 @@ LG_CRF_COLD float crf_slow_exp(float x) { return (float)exp((double)x); }
 LG_CRF_COLD float crf_slow_log(float x) { return (float)log((double)x); }
 LG_CRF_COLD float crf_slow_atan(float x) { return (float)atan((double)x); }
 LG_CRF_COLD float crf_slow_atanh(float x) { return (float)atanh((double)x); }
+LG_CRF_COLD float crf_slow_sin(float x) { return (float)sin((double)x); }
+LG_CRF_COLD float crf_slow_cos(float x) { return (float)cos((double)x); }
+LG_CRF_COLD float crf_slow_pow(float x, float y) { return (float)pow((double)x, (double)y); }
+LG_CRF_COLD float crf_slow_atan2(float y, float x) { return (float)atan2((double)y, (double)x); }
 LG_CRF_DEV float crf_get(float2 v, int i) { return i ? v.y : v.x; }
 LG_CRF_DEV void crf_set(float2& v, int i, float s)
 {
@@ -286,15 +298,11 @@ LG_CRF_COLD float crf_exp_low(float x, float yh0, float yl0, int m)
     return crf_mul(crf_mul(q, crf_from_bits(crf_pow2_bits(m + 64))), 0x1p-64f);
 }
 
-// The double-word e^x 2^-m as yh + yl, big = k + 1.5 2^23, and m per lane.
+// e^r 2^(j/64) as yh + yl for r = rh + rl (|rh| <= ln2/128 + 2^-17, rl to
+// first order) and j, m (k = 64 m + j) from big = k + 1.5 2^23, per lane.
 template <class F>
-LG_CRF_DEV void crf_exp_core(F x, F& big, F& yh, F& yl, int (&mm)[2])
+LG_CRF_DEV void crf_exp_tail(F big, F rh, F rl, F& yh, F& yl, int (&mm)[2])
 {
-    const F S = crf_bc<F>(0x1.8p23f);
-    big = crf_fma(x, crf_bc<F>(LG_CRF_EXP_INVL), S);  // k + 1.5 2^23 (|k| < 2^22)
-    const F kf = crf_sub(big, S);
-    const F rh = crf_fma(crf_neg(kf), crf_bc<F>(LG_CRF_EXP_LHI), x);
-    const F rl = crf_mul(crf_neg(kf), crf_bc<F>(LG_CRF_EXP_LLO));
     const F sh = crf_mul(rh, rh);
     const F sl = crf_fma(rh, rh, crf_neg(sh));
     const F p3 = crf_fma(rh, crf_bc<F>(0x1.555556p-5f), crf_bc<F>(0x1.555556p-3f));
@@ -318,6 +326,18 @@ LG_CRF_DEV void crf_exp_core(F x, F& big, F& yh, F& yl, int (&mm)[2])
     const F e = crf_add(crf_fma(th, ul, crf_fma(tl, uh, tl)), pl);
     yh = crf_add(th, ph);  // |th| >= 1 > |ph|: fast two-sum
     yl = crf_add(crf_sub(ph, crf_sub(yh, th)), e);
+}
+
+// The double-word e^x 2^-m as yh + yl, big = k + 1.5 2^23, and m per lane.
+template <class F>
+LG_CRF_DEV void crf_exp_core(F x, F& big, F& yh, F& yl, int (&mm)[2])
+{
+    const F S = crf_bc<F>(0x1.8p23f);
+    big = crf_fma(x, crf_bc<F>(LG_CRF_EXP_INVL), S);  // k + 1.5 2^23 (|k| < 2^22)
+    const F kf = crf_sub(big, S);
+    const F rh = crf_fma(crf_neg(kf), crf_bc<F>(LG_CRF_EXP_LHI), x);
+    const F rl = crf_mul(crf_neg(kf), crf_bc<F>(LG_CRF_EXP_LLO));
+    crf_exp_tail(big, rh, rl, yh, yl, mm);
 }
 
 template <class F>
@@ -464,25 +484,11 @@ LG_CRF_DEV F lg_crf_log(F x)
 // + delta^3 (-1/3 + delta^2/5), truncation delta^7/7 (relative 2^-62), the
 // cubic term in float (relative to delta 2^-44).  For a > 1 the result is
 // pi/2 - that.  Error about 2^-44.
+// atan t for t = th + tl in [0, 1] (tl a few ulp of th at most) as s1 + lo.
 template <class F>
-LG_CRF_DEV F lg_crf_atan(F z)
+LG_CRF_DEV void crf_atan_core(F th, F tl, F& s1, F& lo)
 {
-    const F a = crf_abs(z);
-    F r0, rd, th, tl, Ah, Al;
-    bool inv[2];
-#pragma unroll
-    for (int i = 0; i < crf_lanes<F>::n; ++i) {
-        inv[i] = crf_get(a, i) > 1.0f;
-        // 1/a for a > 1 (a > 2^126 flushes to 0; atan is then RN(pi/2))
-        crf_set(r0, i, inv[i] ? crf_rcp(crf_get(a, i)) : 1.0f);
-    }
-    const F rho = crf_fma(crf_neg(r0), a, crf_bc<F>(1.0f));
-    const F r1 = crf_mul(rho, r0);
-#pragma unroll
-    for (int i = 0; i < crf_lanes<F>::n; ++i) {
-        crf_set(th, i, inv[i] ? crf_get(r0, i) : crf_get(a, i));
-        crf_set(tl, i, inv[i] ? crf_get(r1, i) : 0.0f);
-    }
+    F rd, Ah, Al;
     const F S = crf_bc<F>(0x1.8p23f);
     const F big = crf_fma(th, crf_bc<F>(512.0f), S);
     const F tj = crf_mul(crf_sub(big, S), crf_bc<F>(0x1p-9f));
@@ -507,9 +513,32 @@ LG_CRF_DEV F lg_crf_atan(F z)
     const F s = crf_mul(d0, d0);
     const F P = crf_fma(s, crf_bc<F>(0x1.99999ap-3f), crf_bc<F>(-0x1.555556p-2f));
     const F cub = crf_mul(crf_mul(s, d0), P);
-    const F s1 = crf_add(Ah, d0);  // |atan t_j| >= |delta| or t_j = 0
+    s1 = crf_add(Ah, d0);  // |atan t_j| >= |delta| or t_j = 0
     const F e1 = crf_sub(d0, crf_sub(s1, Ah));
-    const F lo = crf_add(crf_add(e1, Al), crf_add(d1, cub));
+    lo = crf_add(crf_add(e1, Al), crf_add(d1, cub));
+}
+
+template <class F>
+LG_CRF_DEV F lg_crf_atan(F z)
+{
+    const F a = crf_abs(z);
+    F r0, th, tl;
+    bool inv[2];
+#pragma unroll
+    for (int i = 0; i < crf_lanes<F>::n; ++i) {
+        inv[i] = crf_get(a, i) > 1.0f;
+        // 1/a for a > 1 (a > 2^126 flushes to 0; atan is then RN(pi/2))
+        crf_set(r0, i, inv[i] ? crf_rcp(crf_get(a, i)) : 1.0f);
+    }
+    const F rho = crf_fma(crf_neg(r0), a, crf_bc<F>(1.0f));
+    const F r1 = crf_mul(rho, r0);
+#pragma unroll
+    for (int i = 0; i < crf_lanes<F>::n; ++i) {
+        crf_set(th, i, inv[i] ? crf_get(r0, i) : crf_get(a, i));
+        crf_set(tl, i, inv[i] ? crf_get(r1, i) : 0.0f);
+    }
+    F s1, lo;
+    crf_atan_core(th, tl, s1, lo);
     // pi/2 - (s1 + lo)
     const F ph = crf_sub(crf_bc<F>(LG_CRF_PIO2_HI), s1);
     const F pe = crf_sub(crf_sub(crf_bc<F>(LG_CRF_PIO2_HI), ph), s1);
@@ -621,4 +650,177 @@ LG_CRF_DEV F lg_crf_atanh(F v)
     for (int i = 0; i < crf_lanes<F>::n; ++i)
         if (!ok2[i]) crf_set(out, i, crf_slow_atanh(crf_get(v, i)));
     return out;
+}
+
+// ------------------------------------------------- sincos, pow, atan2 (scalar) --
+// The EPL lens's functions, one value at a time (the exact render calls the
+// correctly rounded functions lane by lane).
+
+LG_CRF_DEV void crf_two_sum(float a, float b, float& s, float& e)
+{
+    s = crf_add(a, b);
+    const float bb = crf_sub(s, a);
+    e = crf_add(crf_sub(a, crf_sub(s, bb)), crf_sub(b, bb));
+}
+
+// Ziv's test with the margin |hi| 2^-40 + floor (floor: an absolute error
+// bound of results near zero); z the rounded result when it holds
+LG_CRF_DEV bool crf_ziv1(float hi, float lo, float floor_, float& z)
+{
+    const float m = crf_fma(crf_fabsf(hi), LG_CRF_ZIV, floor_);
+    const float z1 = crf_add(hi, crf_add(lo, m)), z2 = crf_add(hi, crf_sub(lo, m));
+    z = z1;
+    return z1 == z2;
+}
+
+// sin x and cos x.  x = k pi/2 + r with k = rint(x 2/pi) (|x| <= 128, so
+// |k| < 2^7) and r = ((x - k P1) - k P2) - k P3 as a double word: k P1 and
+// k P2 exact (P1, P2 of 17 significant bits), the first difference exact by
+// Sterbenz, the second by a two-sum, pi/2 - P1 - P2 - P3 below 2^-59, so
+// |error| <= 2^-51 (none for k = 0).  r = a + s with a = j/256 nearest r
+// (s exact, |s| <= 2^-9): sin r = sin a cos s + cos a sin s, cos r = cos a
+// cos s - sin a sin s with sin a, cos a as table pairs (2^-48), sin s = s -
+// s^3/6 + s^5/120 (truncation 2^-65), cos s - 1 = -s^2/2 + s^4/24 - s^6/720
+// with s^2 exact; the leading products exact (fma), the sums by two-sums.
+// Relative error about 2^-46 plus the reduction's 2^-51 absolute: the
+// rounding test takes an absolute floor of 2^-46 when k != 0.  |x| > 128,
+// infinite and NaN x, and undecided roundings in double.
+LG_CRF_DEV void lg_crf_sincos(float x, float* sp, float* cp)
+{
+    const bool inr = crf_fabsf(x) <= 128.0f;
+    const float xr = inr ? x : 0.0f;
+    const float S = 0x1.8p23f;
+    const float big = crf_fma(xr, LG_CRF_INV_PIO2, S);
+    const float kf = crf_sub(big, S);
+    const int k = crf_bits(big) - 0x4b400000;
+    const float r1 = crf_fma(-kf, LG_CRF_PIO2_1, xr);  // exact
+    float rh, e;
+    crf_two_sum(r1, crf_mul(-kf, LG_CRF_PIO2_2), rh, e);
+    const float rl = crf_fma(-kf, LG_CRF_PIO2_3, e);
+    const float bj = crf_fma(rh, 256.0f, S);
+    const int j = crf_bits(bj) - 0x4b400000;  // |j| <= 201
+    const float a = crf_mul(crf_sub(bj, S), 0x1p-8f);
+    const float s0 = crf_sub(rh, a);  // exact
+    const float4 T = crf_ldg(lg_crf_sc_tab + (j + 201));
+    const float sah = T.x, sal = T.y, cah = T.z, cal = T.w;
+    // sin s = s0 + Sl; cos s - 1 = Ch + Cl
+    const float s2 = crf_mul(s0, s0);
+    const float s2l = crf_fma(crf_add(s0, s0), rl, crf_fma(s0, s0, -s2));
+    const float Sl = crf_fma(crf_mul(s2, s0), crf_fma(s2, 0x1.111112p-7f, -0x1.555556p-3f), rl);
+    const float Ch = crf_mul(s2, -0.5f);  // exact
+    const float Cl = crf_fma(crf_mul(s2, s2), crf_fma(s2, -0x1.6c16c2p-10f, 0x1.555556p-5f), crf_mul(s2l, -0.5f));
+    // sin r = sa + ca s0 + sa Ch + (sa Cl + ca Sl + cal s0 + sal)
+    const float p1 = crf_mul(cah, s0), e1 = crf_fma(cah, s0, -p1);
+    const float p2 = crf_mul(sah, Ch), e2 = crf_fma(sah, Ch, -p2);
+    float u, eu;
+    crf_two_sum(sah, p1, u, eu);
+    const float sh = crf_add(u, p2);  // |u| >= |p2|: fast two-sum
+    const float ev = crf_sub(p2, crf_sub(sh, u));
+    const float sl = crf_add(crf_add(ev, eu),
+                             crf_add(crf_add(e1, e2), crf_fma(sah, Cl, crf_fma(cah, Sl, crf_fma(cal, s0, sal)))));
+    // cos r = ca - sa s0 + ca Ch + (ca Cl - sa Sl - sal s0 + cal)
+    const float p3 = crf_mul(sah, s0), e3 = crf_fma(sah, s0, -p3);
+    const float p4 = crf_mul(cah, Ch), e4 = crf_fma(cah, Ch, -p4);
+    float u2, eu2;
+    crf_two_sum(cah, -p3, u2, eu2);
+    const float ch = crf_add(u2, p4);  // |u2| >= 1/2 >= |p4|: fast two-sum
+    const float ev2 = crf_sub(p4, crf_sub(ch, u2));
+    const float cl = crf_add(crf_add(ev2, eu2),
+                             crf_add(crf_sub(e4, e3), crf_fma(cah, Cl, crf_fma(-sah, Sl, crf_fma(-sal, s0, cal)))));
+    // quadrant: sin x = (sin r, cos r, -sin r, -cos r)[k & 3], cos x = (cos r,
+    // -sin r, -cos r, sin r)[k & 3]
+    const int q = k & 3;
+    const bool swap = q & 1, sneg = q >= 2, cneg = q == 1 || q == 2;
+    float xsh = swap ? ch : sh, xsl = swap ? cl : sl, xch = swap ? sh : ch, xcl = swap ? sl : cl;
+    if (sneg) {
+        xsh = -xsh;
+        xsl = -xsl;
+    }
+    if (cneg) {
+        xch = -xch;
+        xcl = -xcl;
+    }
+    const float fl = k != 0 ? 0x1p-46f : 0.0f;
+    float zs, zc;
+    const bool oks = crf_ziv1(xsh, xsl, fl, zs) && inr, okc = crf_ziv1(xch, xcl, fl, zc) && inr;
+    *sp = oks ? (x == 0.0f ? x : zs) : crf_slow_sin(x);  // (sin of -0 is -0)
+    *cp = okc ? zc : crf_slow_cos(x);
+}
+
+// x^y = e^(y ln x): ln x as a double word (crf_log_dw, relative error below
+// 2^-42), t = y ln x as a double word (the product exact by an fma), e^t
+// from the exp tail with the low part of t added to the reduced argument by
+// a two-sum.  Relative error below about |t| 2^-42 + 2^-42, so the rounding
+// test's margin grows with |t|.  Positive normal x with t in [-87, 88] (a
+// normal result) and the rounding decided; everything else in double.
+LG_CRF_DEV float lg_crf_pow(float x, float y)
+{
+    const bool xin = x >= 0x1p-126f && x <= 0x1.fffffep127f;
+    const float xr = xin ? x : 1.0f;
+    float lh, ll;
+    crf_log_dw<float, false>(xr, xr, lh, ll);
+    const float th = crf_mul(y, lh);
+    const float tl = crf_fma(y, ll, crf_fma(y, lh, -th));
+    const bool tin = th >= -87.0f && th <= 88.0f;  // (false for NaN)
+    const float t = tin ? th : 0.0f, tlo = tin ? tl : 0.0f;
+    const float S = 0x1.8p23f;
+    const float big = crf_fma(t, LG_CRF_EXP_INVL, S);
+    const float kf = crf_sub(big, S);
+    const float r0 = crf_fma(-kf, LG_CRF_EXP_LHI, t);  // exact
+    float rh, e;
+    crf_two_sum(r0, tlo, rh, e);
+    const float rl = crf_fma(-kf, LG_CRF_EXP_LLO, e);
+    float yh, yl;
+    int m[2];
+    crf_exp_tail(big, rh, rl, yh, yl, m);
+    const float mrel = crf_fma(crf_fabsf(t), 0x1p-41f, LG_CRF_ZIV);
+    const float mg = crf_mul(crf_fabsf(yh), mrel);
+    const float z1 = crf_add(yh, crf_add(yl, mg)), z2 = crf_add(yh, crf_sub(yl, mg));
+    if (xin && tin && z1 == z2) return crf_from_bits(crf_add_exp(crf_bits(z1), m[0]));
+    return crf_slow_pow(x, y);
+}
+
+// atan2(y, x): q = min(|x|, |y|) / max(|x|, |y|) in [0, 1] as a double word
+// (rcp plus one correction step, relative error 2^-46), atan q from the atan
+// core, then pi/2 - that where |y| > |x| and pi - that where x < 0 (double-
+// word constants; fast two-sums, the constant being the larger), the sign
+// of y.  Relative error about 2^-44.  min(|x|, |y|) >= 2^-100, max(|x|, |y|)
+// < 2^126, a quotient above 2^-100 (so the result is normal) and the
+// rounding decided; zeros, infinities, NaN, tiny or huge arguments and the
+// rest in double.
+LG_CRF_DEV float lg_crf_atan2(float y, float x)
+{
+    const float ax = crf_fabsf(x), ay = crf_fabsf(y);
+    const bool swap = ay > ax;
+    float num = swap ? ax : ay, den = swap ? ay : ax;
+    // the quotient's remainder exact (no underflow: num >= 2^-100), the
+    // reciprocal normal (den < 2^126) and the quotient above 2^-100
+    const bool in = den < 0x1p126f && num >= 0x1p-100f && num >= crf_mul(den, 0x1p-100f);
+    if (!in) {
+        num = 1.0f;
+        den = 1.0f;
+    }
+    const float rd = crf_rcp(den);
+    const float q0 = crf_mul(num, rd);
+    const float res = crf_fma(-q0, den, num);  // exact
+    const float q1 = crf_mul(res, rd);
+    float s1, lo;
+    crf_atan_core(q0, q1, s1, lo);
+    float hi = s1;
+    if (swap) {  // pi/2 - (s1 + lo)
+        const float ph = crf_sub(LG_CRF_PIO2_HI, s1);
+        const float pe = crf_sub(crf_sub(LG_CRF_PIO2_HI, ph), s1);
+        lo = crf_add(pe, crf_sub(LG_CRF_PIO2_LO, lo));
+        hi = ph;
+    }
+    if (x < 0.0f) {  // pi - (hi + lo)
+        const float PIH = crf_mul(LG_CRF_PIO2_HI, 2.0f), PIL = crf_mul(LG_CRF_PIO2_LO, 2.0f);
+        const float ph = crf_sub(PIH, hi);
+        const float pe = crf_sub(crf_sub(PIH, ph), hi);
+        lo = crf_add(pe, crf_sub(PIL, lo));
+        hi = ph;
+    }
+    float z;
+    if (in && crf_ziv1(hi, lo, 0.0f, z)) return crf_copysignf(z, y);
+    return crf_slow_atan2(y, x);
 }

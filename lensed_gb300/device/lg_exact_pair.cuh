@@ -7,10 +7,10 @@
 // evaluated in double and rounded once.
 //
 // exp, log, atan and atanh (the functions of the SIE family, the Sersic,
-// exponential, Gaussian and de Vaucouleurs profiles) come from
-// lg_crfloat.cuh, in single-precision arithmetic;
-// the others (those of the EPL lens: atan2, sincos, pow; and the rest of the
-// mapped library) are evaluated lane by lane in double.
+// exponential, Gaussian and de Vaucouleurs profiles) and atan2, sincos and
+// pow (the EPL lens) come from lg_crfloat.cuh, in single-precision
+// arithmetic; the rest of the mapped library is evaluated lane by lane in
+// double.
 
 // one lane at a time: these functions are bound by instruction issue, and
 // their per-lane parts (bit fields, tests, table loads) outweigh what f32x2
@@ -49,18 +49,31 @@ LG_EXACT_LANES1(lg_cr_tgammaf)
 LG_EXACT_LANES1(lg_cr_lgammaf)
 #undef LG_EXACT_LANES1
 
-LG_DEV lg_pair lg_cr_powf(lg_pair a, float b) { return {make_float2(lg_cr_powf(a.v.x, b), lg_cr_powf(a.v.y, b))}; }
-LG_DEV lg_pair lg_cr_powf(lg_pair_prod a, float b) { return lg_cr_powf(lg_pair(a), b); }
-LG_DEV lg_pair lg_cr_powf(lg_pair a, lg_pair b)
+// the EPL lens's atan2, sincos and pow: correctly rounded in single
+// precision too (lg_crfloat.cuh), one lane at a time; the strict mapping's
+// names are rebound to them for the plugins of this module (scalar calls
+// included: the exact EPL polar frame runs per lane)
+LG_DEV float lg_crx_powf(float a, float b) { return lg_crf_pow(a, b); }
+LG_DEV lg_pair lg_crx_powf(lg_pair a, float b) { return {make_float2(lg_crf_pow(a.v.x, b), lg_crf_pow(a.v.y, b))}; }
+LG_DEV lg_pair lg_crx_powf(lg_pair_prod a, float b) { return lg_crx_powf(lg_pair(a), b); }
+LG_DEV lg_pair lg_crx_powf(lg_pair a, lg_pair b)
 {
-    return {make_float2(lg_cr_powf(a.v.x, b.v.x), lg_cr_powf(a.v.y, b.v.y))};
+    return {make_float2(lg_crf_pow(a.v.x, b.v.x), lg_crf_pow(a.v.y, b.v.y))};
 }
-LG_DEV lg_pair lg_cr_atan2f(lg_pair y, lg_pair x)
+LG_DEV float lg_crx_atan2f(float y, float x) { return lg_crf_atan2(y, x); }
+LG_DEV lg_pair lg_crx_atan2f(lg_pair y, lg_pair x)
 {
-    return {make_float2(lg_cr_atan2f(y.v.x, x.v.x), lg_cr_atan2f(y.v.y, x.v.y))};
+    return {make_float2(lg_crf_atan2(y.v.x, x.v.x), lg_crf_atan2(y.v.y, x.v.y))};
 }
-LG_DEV void lg_cr_sincosf(lg_pair a, lg_pair* s, lg_pair* c)
+LG_DEV void lg_crx_sincosf(float a, float* s, float* c) { lg_crf_sincos(a, s, c); }
+LG_DEV void lg_crx_sincosf(lg_pair a, lg_pair* s, lg_pair* c)
 {
-    lg_cr_sincosf(a.v.x, &s->v.x, &c->v.x);
-    lg_cr_sincosf(a.v.y, &s->v.y, &c->v.y);
+    lg_crf_sincos(a.v.x, &s->v.x, &c->v.x);
+    lg_crf_sincos(a.v.y, &s->v.y, &c->v.y);
 }
+#undef powf
+#undef atan2f
+#undef sincosf
+#define powf(x, y) lg_crx_powf(x, y)
+#define atan2f(y, x) lg_crx_atan2f(y, x)
+#define sincosf(x, s, c) lg_crx_sincosf(x, s, c)

@@ -11,6 +11,7 @@ hi = RN(v) and lo = RN(v - hi).
         (c = 1 for the two intervals next to 1) and -ln(c_j) as (hi, lo)
         (Tang 1990)
   atan  atan(j/512), j = 0..512, as (hi, lo)
+  sin/cos  sin(j/256) and cos(j/256), j = -201..201, as (hi, lo) pairs
 
 Run:  python lensed_gb300/device/make_crf_tables.py
 """
@@ -79,6 +80,14 @@ def main():
         hi, lo = split(mp.atan(mp.mpf(j) / 512))
         rows.append(f"{{{lit(hi)}, {lit(lo)}}}")
     out.append("LG_CRF_TABLE(float2, lg_crf_atan_tab, 513) = {\n    " + ",\n    ".join(rows) + "};")
+    # sin / cos(j/256), j = -201..201, as (sin hi, sin lo, cos hi, cos lo)
+    rows = []
+    for j in range(-201, 202):
+        a = mp.mpf(j) / 256
+        sh, sl = split(mp.sin(a))
+        ch, cl = split(mp.cos(a))
+        rows.append(f"{{{lit(sh)}, {lit(sl)}, {lit(ch)}, {lit(cl)}}}")
+    out.append("LG_CRF_TABLE(float4, lg_crf_sc_tab, 403) = {\n    " + ",\n    ".join(rows) + "};")
     # split constants
     consts = {}
     l64 = mp.log(2) / 64
@@ -86,6 +95,14 @@ def main():
     consts["LG_CRF_EXP_LHI"], consts["LG_CRF_EXP_LLO"] = split(l64)
     consts["LG_CRF_LN2_HI"], consts["LG_CRF_LN2_LO"] = split(mp.log(2))
     consts["LG_CRF_PIO2_HI"], consts["LG_CRF_PIO2_LO"] = split(mp.pi / 2)
+    # sin / cos argument reduction: 2/pi, and pi/2 = P1 + P2 + P3 with P1
+    # and P2 of 17 significant bits (k P1, k P2 exact for |k| < 2^7)
+    consts["LG_CRF_INV_PIO2"] = rn(2 / mp.pi)
+    p1 = mp.floor(mp.pi / 2 * 2 ** 16 + mp.mpf(0.5)) / 2 ** 16
+    p2 = mp.floor((mp.pi / 2 - p1) * 2 ** 33 + mp.mpf(0.5)) / 2 ** 33
+    consts["LG_CRF_PIO2_1"], consts["LG_CRF_PIO2_2"] = rn(p1), rn(p2)
+    assert mp.mpf(rn(p1)) == p1 and mp.mpf(rn(p2)) == p2
+    consts["LG_CRF_PIO2_3"] = rn(mp.pi / 2 - p1 - p2)
     # exp(x) rounds to 0 for x <= LG_CRF_EXP_ZERO (e^x <= 2^-150, the tie at
     # 2^-150 going to the even value 0): the largest such float
     t = mp.log(mp.mpf(2) ** -150)

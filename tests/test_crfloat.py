@@ -1,5 +1,5 @@
-"""The correctly rounded single-precision exp, log, atan and atanh of the
-exact evaluation modules, on the CPU.
+"""The correctly rounded single-precision exp, log, atan, atanh, sin, cos,
+pow and atan2 of the exact evaluation modules, on the CPU.
 
 lensed_gb300/device/lg_crfloat.cuh computes each function in
 single-precision double-word arithmetic and rounds with Ziv's test, falling
@@ -9,9 +9,10 @@ result must equal the function evaluated in double and rounded once --
 the oracle's semantics -- bit for bit.  Checked here on a stride through
 all 2^32 bit patterns plus dense windows where the algorithms switch paths
 (subnormal exp results, logarithms near 1, the two atanh formulas, atan
-near 1); the whole range of all four functions was swept without a
-mismatch when the code was written, and the GPU tests sweep it on the
-device (test_gpu_crfloat.py).  The share of in-range inputs that need the
+near 1, sin and cos near multiples of pi/2, pow near 1); the whole range of
+every function (for pow and atan2 every first argument, with a second
+argument derived from it) was swept without a mismatch when the code was
+written, and the GPU tests sweep it on the device (test_gpu_crfloat.py).  The share of in-range inputs that need the
 double path is bounded too (about 2^-15 to 2^-19).
 """
 import os
@@ -45,13 +46,19 @@ def sweep(tmp_path_factory):
     return run
 
 
-@pytest.mark.parametrize("fn,name", [(0, "exp"), (1, "log"), (2, "atan"), (3, "atanh")])
-def test_stride_through_all_floats(sweep, fn, name):
-    n, bad, nin, slow, err = sweep(fn, 0, 1 << 32, 257)
+# (fn, name, bound on the share of in-range inputs through double: pow's
+# rounding-test margin grows with |y ln x|)
+FUNCTIONS = [(0, "exp", -13), (1, "log", -13), (2, "atan", -13), (3, "atanh", -13), (4, "sin", -13),
+             (5, "cos", -13), (6, "pow(x, fixed y)", -10), (7, "atan2(x, p)", -13), (8, "pow(|x|, p)", -10)]
+
+
+@pytest.mark.parametrize("fn,name,slow_bound", FUNCTIONS)
+def test_stride_through_all_floats(sweep, fn, name, slow_bound):
+    n, bad, nin, slow, err = sweep(fn, 0, 1 << 32, 257 if fn < 4 else 1031)
     print(f"{name}: {n} inputs, {bad} mismatches, {slow} of {nin} in range through double "
           f"({slow / max(nin, 1):.2g})")
     assert bad == 0, err
-    assert slow <= 2.0 ** -13 * nin
+    assert slow <= 2.0 ** slow_bound * nin
 
 
 WINDOWS = [
@@ -65,6 +72,14 @@ WINDOWS = [
     (3, bits(0.05), bits(0.08)),              # atanh at the switch between its two formulas
     (3, bits(1e-4), bits(3e-3)),              # atanh: small arguments
     (3, bits(0.99), bits(1.0)),               # atanh near 1
+    (4, bits(1e-4), bits(0.02)),              # sin: small arguments, the first table intervals
+    (4, bits(3.13), bits(3.16)),              # sin near pi (results near zero, k = 2)
+    (5, bits(1.56), bits(1.58)),              # cos near pi/2
+    (5, bits(127.0), bits(128.5)),            # cos at the end of the reduced range
+    (6, bits(0.999), bits(1.001)),            # pow near x = 1 (y ln x near zero)
+    (6, bits(1e-3), bits(200.0)),             # pow over the EPL lens's radii
+    (7, bits(0.5), bits(2.0)),                # atan2 with arguments of similar size
+    (8, bits(0.9), bits(1.1)),                # pow(|x|, p) near |x| = 1
 ]
 
 

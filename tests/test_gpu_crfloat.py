@@ -1,8 +1,10 @@
 """The correctly rounded exp, log, atan and atanh of the exact evaluation
 modules on the GPU, as ray pairs (f32x2 instructions, rcp.approx
-estimates): for every one of the 2^32 float inputs, paired with an
-unrelated second input (so that the two lanes take different paths and
-table entries), the result equals the function evaluated in double on the
+estimates), and the EPL lens's sin, cos, pow and atan2 one value at a time
+(pow with sixteen fixed exponents and with a second argument derived from
+the first, atan2 likewise): for every one of the 2^32 float inputs, paired
+with an unrelated second input (so that the two lanes take different paths
+and table entries), the result equals the function evaluated in double on the
 device and rounded once (NaN matches NaN) -- the strict modules' per-ray
 semantics, which the exact modules must reproduce bit for bit.  The count
 is over both lanes; the double evaluation itself is within 1-2 double ulp,
@@ -28,7 +30,8 @@ def sweep(fn, lo=0, hi=1 << 32):
     return bad.value, xs
 
 
-@pytest.mark.parametrize("fn,name", [(0, "exp"), (1, "log"), (2, "atan"), (3, "atanh")])
+@pytest.mark.parametrize("fn,name", [(0, "exp"), (1, "log"), (2, "atan"), (3, "atanh"), (4, "sin"), (5, "cos"),
+                                     (6, "pow(x, fixed y)"), (7, "atan2(x, p)"), (8, "pow(|x|, p)")])
 def test_every_float_input(native, fn, name):
     bad, xs = sweep(fn)
     print(f"{name}: {bad} of 2^32 inputs differ from the double evaluation {xs}")
