@@ -278,9 +278,12 @@ LG_DEV float lg_sfu_lg2(float x)
 }
 
 // e^x for two rays: 2^t * 2^c with t = fl(x log2(e)) and c the rest of
-// x log2(e) (the product's rounding error, exact through an fma, plus x
-// times the rounding error of the constant); 2^t from the SFU, 2^c as
-// 1 + c ln 2 (|c| <= 2^-24 |t|).  Within the SFU's few-ulp error of e^x;
+// x log2(e) (the product's rounding error, exact through an fma -- Dekker's
+// exact product (Dekker 1971) -- plus x times the rounding error of the
+// constant, log2(e) split into two floats as in Cody and Waite's argument
+// reduction (Cody & Waite 1980, "Software Manual for the Elementary
+// Functions")); 2^t from the SFU, 2^c as 1 + c ln 2, the first-order term
+// of its series (|c| <= 2^-24 |t|).  Within the SFU's few-ulp error of e^x;
 // results below 2^-126 are flushed to zero; for |t| >= 128 (where 2^t is 0
 // or overflows, and for infinite x) and NaN x the result is 2^t itself.
 LG_DEV float lg_exp_pick(float t, float p, float r) { return fabsf(t) < 128.0f ? r : p; }
@@ -296,8 +299,9 @@ LG_DEV lg_pair expf(lg_pair x)
 LG_DEV lg_pair expf(lg_pair_prod x) { return expf(lg_pair(x)); }
 
 // ln x for two rays: y ln 2 + (x 2^-y - 1) with y = lg2(x) from the SFU; the
-// second term removes the error of y to first order, leaving an absolute
-// error of about 2^-22 (the SFU's 2^-y).  Outside |y| < 120 (where 2^-y
+// second term is one Newton step for u in e^u = x from u0 = y ln 2 (u1 = u0
+// + x e^-u0 - 1, here with e^-u0 = 2^-y), which removes the error of y to
+// first order, leaving an absolute error of about 2^-22 (the SFU's 2^-y).  Outside |y| < 120 (where 2^-y
 // would leave the normal range), and for zero, infinite, negative or NaN x,
 // the result is y ln 2 (subnormal x is flushed: -inf).
 LG_DEV lg_pair logf(lg_pair x)
