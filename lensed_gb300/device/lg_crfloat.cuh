@@ -570,44 +570,63 @@ LG_CRF_DEV F lg_crf_atan(F z)
 
 // -------------------------------------------------------------------- atanh --
 // atanh v = sign(v) atanh(a), a = |v| < 1, by two formulas:
-//  * a <= 1/16: the odd series a + a^3 (1/3 + a^2/5 + ... + a^8/11),
-//    truncation a^13/13 (relative 2^-51); the cubic term (up to 2^-9.6 of
-//    the result) as a double word: a^3 from exact products, 1/3 as a pair;
-//  * a > 1/16: ln(1 + w) / 2 with w = 2a / (1 - a) >= 1/8 as a double word
-//    (1 - a exact by a fast two-sum, the quotient from rcp plus one
-//    correction step), 1 + w as a two-sum, then the double-word logarithm:
-//    1 + w carries about 2^-49 absolute error, 2^-46 of the result here.
-// Each branch runs only where a lane of the pair needs it (neighbouring
-// rays mostly fall on the same side of 1/16).
+//  * a <= 0.9: with t_j = j/512 nearest a, atanh a = atanh t_j +
+//    atanh(delta), delta = (a - t_j) / (1 - a t_j) as a double word
+//    (numerator exact; denominator from an exact product and a fast
+//    two-sum, at least 0.19; quotient from rcp plus one correction step),
+//    |delta| <= 2^-7.6, atanh(delta) = delta + delta^3 (1/3 + delta^2/5),
+//    truncation delta^7/7 (relative 2^-48), the cubic term in float;
+//    table pairs atanh t_j (2^-48).  Error about 2^-45;
+//  * a > 0.9: ln(1 + w) / 2 with w = 2a / (1 - a) as a double word (1 - a
+//    exact by a fast two-sum, the quotient from rcp plus one correction
+//    step), 1 + w as a two-sum, then the double-word logarithm: 1 + w
+//    carries about 2^-49 absolute error, 2^-46 of the result here.
+// The SIE family's arguments stay below sqrt(1 - q^2), so its rays take the
+// first formula unless q < 0.44; each branch runs only where a lane of the
+// pair needs it.
 template <class F>
 LG_CRF_DEV F lg_crf_atanh(F v)
 {
     const F a = crf_abs(v);
     const F one = crf_bc<F>(1.0f);
-    bool small[2];
-    bool any_small = false, any_large = false;
+    bool tab[2];
+    bool any_tab = false, any_large = false;
 #pragma unroll
     for (int i = 0; i < crf_lanes<F>::n; ++i) {
-        small[i] = crf_get(a, i) <= 0.0625f;
-        any_small = any_small || small[i];
-        any_large = any_large || !small[i];
+        tab[i] = crf_get(a, i) <= 0.9f;
+        any_tab = any_tab || tab[i];
+        any_large = any_large || !tab[i];
     }
     F hs = a, ls = a, hl = a, ll = a;
-    if (any_small) {
-        const F sh = crf_mul(a, a);
-        const F sl = crf_fma(a, a, crf_neg(sh));
-        const F c3h = crf_mul(sh, a);
-        const F c3l = crf_fma(sl, a, crf_fma(sh, a, crf_neg(c3h)));
-        const F Q = crf_mul(sh, crf_fma(crf_fma(crf_fma(sh, crf_bc<F>(0x1.745d18p-4f), crf_bc<F>(0x1.c71c72p-4f)), sh,
-                                                crf_bc<F>(0x1.24924ap-3f)),
-                                        sh, crf_bc<F>(0x1.99999ap-3f)));
-        // 1/3 = 0x1.555556p-2 - 0x1.555556p-27 (to 2^-50)
-        const F pl = crf_add(crf_bc<F>(-0x1.555556p-27f), Q);
-        const F ch = crf_mul(c3h, crf_bc<F>(0x1.555556p-2f));
-        const F cl = crf_add(crf_fma(c3h, crf_bc<F>(0x1.555556p-2f), crf_neg(ch)),
-                             crf_fma(c3h, pl, crf_mul(c3l, crf_bc<F>(0x1.555556p-2f))));
-        hs = crf_add(a, ch);  // a >= a^3/3: fast two-sum
-        ls = crf_add(crf_sub(ch, crf_sub(hs, a)), cl);
+    if (any_tab) {
+        const F S = crf_bc<F>(0x1.8p23f);
+        const F big = crf_fma(a, crf_bc<F>(512.0f), S);
+        const F tj = crf_mul(crf_sub(big, S), crf_bc<F>(0x1p-9f));
+        F Ah, Al, rd;
+#pragma unroll
+        for (int i = 0; i < crf_lanes<F>::n; ++i) {
+            int j = crf_bits(crf_get(big, i)) - 0x4b400000;
+            j = j < 0 ? 0 : (j > 461 ? 461 : j);  // (in range for a <= 0.9; the other lanes are not used)
+            const float2 A = crf_ldg(lg_crf_atanh_tab + j);
+            crf_set(Ah, i, A.x);
+            crf_set(Al, i, A.y);
+        }
+        const F nh = crf_sub(a, tj);  // exact
+        const F qh = crf_mul(a, tj);
+        const F ql = crf_fma(a, tj, crf_neg(qh));
+        const F dh = crf_sub(one, qh);  // 1 >= qh: fast two-sum
+        const F dl = crf_sub(crf_sub(crf_sub(one, dh), qh), ql);
+#pragma unroll
+        for (int i = 0; i < crf_lanes<F>::n; ++i) crf_set(rd, i, crf_rcp(crf_get(dh, i)));  // dh in [0.19, 1]
+        const F d0 = crf_mul(nh, rd);
+        const F res = crf_fma(crf_neg(d0), dl, crf_fma(crf_neg(d0), dh, nh));
+        const F d1 = crf_mul(res, rd);
+        const F s = crf_mul(d0, d0);
+        const F P = crf_fma(s, crf_bc<F>(0x1.99999ap-3f), crf_bc<F>(0x1.555556p-2f));
+        const F cub = crf_mul(crf_mul(s, d0), P);
+        hs = crf_add(Ah, d0);  // |atanh t_j| >= |delta| or t_j = 0: fast two-sum
+        const F e1 = crf_sub(d0, crf_sub(hs, Ah));
+        ls = crf_add(crf_add(e1, Al), crf_add(d1, cub));
     }
     if (any_large) {
         const F dh = crf_sub(one, a);
@@ -630,8 +649,8 @@ LG_CRF_DEV F lg_crf_atanh(F v)
     F hi, lo;
 #pragma unroll
     for (int i = 0; i < crf_lanes<F>::n; ++i) {
-        crf_set(hi, i, small[i] ? crf_get(hs, i) : crf_get(hl, i));
-        crf_set(lo, i, small[i] ? crf_get(ls, i) : crf_get(ll, i));
+        crf_set(hi, i, tab[i] ? crf_get(hs, i) : crf_get(hl, i));
+        crf_set(lo, i, tab[i] ? crf_get(ls, i) : crf_get(ll, i));
     }
     F z1, z2;
     crf_ziv(hi, lo, z1, z2);

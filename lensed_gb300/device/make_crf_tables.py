@@ -11,6 +11,7 @@ hi = RN(v) and lo = RN(v - hi).
         (c = 1 for the two intervals next to 1) and -ln(c_j) as (hi, lo)
         (Tang 1990)
   atan  atan(j/512), j = 0..512, as (hi, lo)
+  atanh atanh(j/512), j = 0..461, as (hi, lo)
   sin/cos  sin(j/256) and cos(j/256), j = -201..201, as (hi, lo) pairs
 
 Run:  python lensed_gb300/device/make_crf_tables.py
@@ -80,6 +81,12 @@ def main():
         hi, lo = split(mp.atan(mp.mpf(j) / 512))
         rows.append(f"{{{lit(hi)}, {lit(lo)}}}")
     out.append("LG_CRF_TABLE(float2, lg_crf_atan_tab, 513) = {\n    " + ",\n    ".join(rows) + "};")
+    # atanh(j/512), j = 0..461, as (hi, lo)
+    rows = []
+    for j in range(462):
+        hi, lo = split(mp.atanh(mp.mpf(j) / 512))
+        rows.append(f"{{{lit(hi)}, {lit(lo)}}}")
+    out.append("LG_CRF_TABLE(float2, lg_crf_atanh_tab, 462) = {\n    " + ",\n    ".join(rows) + "};")
     # sin / cos(j/256), j = -201..201, as (sin hi, sin lo, cos hi, cos lo)
     rows = []
     for j in range(-201, 202):

@@ -72,6 +72,7 @@ WINDOWS = [
     (3, bits(0.05), bits(0.08)),              # atanh at the switch between its two formulas
     (3, bits(1e-4), bits(3e-3)),              # atanh: small arguments
     (3, bits(0.99), bits(1.0)),               # atanh near 1
+    (3, bits(0.89), bits(0.91)),              # atanh at the switch from the table to the logarithm
     (4, bits(1e-4), bits(0.02)),              # sin: small arguments, the first table intervals
     (4, bits(3.13), bits(3.16)),              # sin near pi (results near zero, k = 2)
     (5, bits(1.56), bits(1.58)),              # cos near pi/2
