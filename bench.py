@@ -63,7 +63,7 @@ MEASURED_TRAFFIC = {("config2", 1024, "render", "fast"): 208.45e6, ("config2", 1
 # x 32 / rays of the launch) per floating-point mode, config2 workload: the
 # render is bound by instruction issue (4 warp instructions per SM and cycle),
 # so its issue rate against that peak is the second roofline it reports.
-MEASURED_INSTR_PER_RAY = {("config2", "exact"): 445.7, ("config2", "fast"): 90.8}
+MEASURED_INSTR_PER_RAY = {("config2", "exact"): 406.5, ("config2", "fast"): 90.8}
 
 RAY_FLOPS = {
     "sis": 12, "sis_plus_shear": 20, "nsis": 10, "sie": 26, "sie_plus_shear": 34, "nsie": 30,
