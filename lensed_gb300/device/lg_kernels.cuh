@@ -257,13 +257,21 @@ LG_DEV void lg_render_tile(const lg_model* __restrict__ models, float* __restric
     }
 }
 
-extern "C" __global__ void __launch_bounds__(LG_RT) lg_render_raw(const lg_model* __restrict__ models,
-                                                                  float* __restrict__ raw)
+// exact modules: 1024 resident threads per SM (64 registers a thread) --
+// the correctly rounded functions are issue-bound, and the extra warps hide
+// their latencies better than the 80 registers the compiler would use
+#if defined(LG_EXACT)
+#define LG_RENDER_MINB (1024 / LG_RT)
+#else
+#define LG_RENDER_MINB 1
+#endif
+extern "C" __global__ void __launch_bounds__(LG_RT, LG_RENDER_MINB) lg_render_raw(const lg_model* __restrict__ models,
+                                                                                  float* __restrict__ raw)
 {
     lg_render_tile<0>(models, raw, nullptr, nullptr, nullptr, nullptr, nullptr, nullptr);
 }
 
-extern "C" __global__ void __launch_bounds__(LG_RT)
+extern "C" __global__ void __launch_bounds__(LG_RT, LG_RENDER_MINB)
     lg_render_chi2(const lg_model* __restrict__ models, const float* __restrict__ image,
                    const float* __restrict__ weight, double* __restrict__ partials, unsigned* __restrict__ counters,
                    double* __restrict__ logL)
