@@ -209,14 +209,22 @@ LG_DEV void lg_multi_render_body(const lg_model* __restrict__ models, const lg_s
     }
 }
 
-extern "C" __global__ void __launch_bounds__(LG_RT)
+// exact modules: 64 registers a thread, as the single-system render
+#ifndef LG_RENDER_MINB
+#if defined(LG_EXACT)
+#define LG_RENDER_MINB (1024 / LG_RT)
+#else
+#define LG_RENDER_MINB 1
+#endif
+#endif
+extern "C" __global__ void __launch_bounds__(LG_RT, LG_RENDER_MINB)
     lg_multi_render_raw(const lg_model* __restrict__ models, const lg_sysinfo* __restrict__ info,
                         const lg_sysplan* __restrict__ plan, const long long* __restrict__ hdr, float* __restrict__ raw)
 {
     lg_multi_render_body<true>(models, info, plan, hdr, raw, nullptr, nullptr, nullptr);
 }
 
-extern "C" __global__ void __launch_bounds__(LG_RT)
+extern "C" __global__ void __launch_bounds__(LG_RT, LG_RENDER_MINB)
     lg_multi_render_chi2(const lg_model* __restrict__ models, const lg_sysinfo* __restrict__ info,
                          const lg_sysplan* __restrict__ plan, const long long* __restrict__ hdr,
                          const float* __restrict__ images, const float* __restrict__ weights,
