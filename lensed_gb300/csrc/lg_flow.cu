@@ -42,7 +42,7 @@
 // uniform in the image of the ball; draws outside the cube are dropped.  The
 // flow is trained with a held-out split and early stopping so that it stays
 // smooth; a flow whose calibrated kept fraction is below 0.2% is not used.
-// Every kept draw is then judged by the exact likelihood in the sampler.
+// Every kept draw is then evaluated by the exact likelihood in the sampler.
 
 #include <cuda_bf16.h>
 #include <cuda_runtime.h>

@@ -14,7 +14,7 @@
 // The evidence is accumulated as a log-sum-exp in double precision, with
 // Skilling's information H and the error sqrt(H / nlive).  A learned
 // proposal (lg_flow.cu) can replace the ellipsoid; the ellipsoid remains the
-// fallback and the judge of the learned sampler.
+// fallback and the yardstick of the learned sampler.
 
 #include <algorithm>
 #include <chrono>

@@ -245,13 +245,13 @@ public:
             lg_ell_draw<<<(M + 127) / 128, 128, 0, s>>>(seed + 0x632BE59BD9B4E019ull * (uint64_t)round, M, T, dw, dX.p,
                                                          dflag.p);
             lg_ell_compact<<<1, 1024, 0, s>>>(dflag.p, M, dX.p, d, need, dout.p + (size_t)got * d, dcnt.p);
-            // the counts and the room for this round's points in one wait
+            // the counts and the room for this pass's points in one wait
             if (cudaMemcpyAsync(hcnt.p, dcnt.p, 2 * sizeof(int), cudaMemcpyDeviceToHost, s) ||
                 cudaMemcpyAsync(hout.p + (size_t)got * d, dout.p + (size_t)got * d, (size_t)need * d * sizeof(double),
                                 cudaMemcpyDeviceToHost, s) ||
                 cudaStreamSynchronize(s))
                 return -1;
-            // kept fraction of all draws of this round
+            // kept fraction of all draws of this pass
             accept = 0.5 * accept + 0.5 * std::max((double)hcnt.p[1] / M, 1e-6);
             got += hcnt.p[0];
         }

@@ -1,5 +1,5 @@
 """The CPU restatement of the flow loss: its analytic gradient agrees with
-central finite differences (so it can judge the CUDA training kernels)."""
+central finite differences (so it can check the CUDA training kernels)."""
 import numpy as np
 
 from oracle import flow_oracle as F
