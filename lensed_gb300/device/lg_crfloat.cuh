@@ -522,32 +522,41 @@ template <class F>
 LG_CRF_DEV F lg_crf_atan(F z)
 {
     const F a = crf_abs(z);
-    F r0, th, tl;
+    F th = a, tl = crf_bc<F>(0.0f);
     bool inv[2];
+    bool any_inv = false;
 #pragma unroll
     for (int i = 0; i < crf_lanes<F>::n; ++i) {
         inv[i] = crf_get(a, i) > 1.0f;
-        // 1/a for a > 1 (a > 2^126 flushes to 0; atan is then RN(pi/2))
-        crf_set(r0, i, inv[i] ? crf_rcp(crf_get(a, i)) : 1.0f);
+        any_inv = any_inv || inv[i];
     }
-    const F rho = crf_fma(crf_neg(r0), a, crf_bc<F>(1.0f));
-    const F r1 = crf_mul(rho, r0);
+    // the reciprocal and pi/2 - ... only where a lane needs them (the SIE
+    // family's arguments rarely exceed 1)
+    if (any_inv) {
+        F r0;
 #pragma unroll
-    for (int i = 0; i < crf_lanes<F>::n; ++i) {
-        crf_set(th, i, inv[i] ? crf_get(r0, i) : crf_get(a, i));
-        crf_set(tl, i, inv[i] ? crf_get(r1, i) : 0.0f);
+        for (int i = 0; i < crf_lanes<F>::n; ++i)  // 1/a for a > 1 (a > 2^126 flushes to 0; atan is then RN(pi/2))
+            crf_set(r0, i, inv[i] ? crf_rcp(crf_get(a, i)) : 1.0f);
+        const F rho = crf_fma(crf_neg(r0), a, crf_bc<F>(1.0f));
+        const F r1 = crf_mul(rho, r0);
+#pragma unroll
+        for (int i = 0; i < crf_lanes<F>::n; ++i) {
+            crf_set(th, i, inv[i] ? crf_get(r0, i) : crf_get(a, i));
+            crf_set(tl, i, inv[i] ? crf_get(r1, i) : 0.0f);
+        }
     }
     F s1, lo;
     crf_atan_core(th, tl, s1, lo);
-    // pi/2 - (s1 + lo)
-    const F ph = crf_sub(crf_bc<F>(LG_CRF_PIO2_HI), s1);
-    const F pe = crf_sub(crf_sub(crf_bc<F>(LG_CRF_PIO2_HI), ph), s1);
-    const F plo = crf_add(pe, crf_sub(crf_bc<F>(LG_CRF_PIO2_LO), lo));
-    F hi2, lo2;
+    F hi2 = s1, lo2 = lo;
+    if (any_inv) {  // pi/2 - (s1 + lo)
+        const F ph = crf_sub(crf_bc<F>(LG_CRF_PIO2_HI), s1);
+        const F pe = crf_sub(crf_sub(crf_bc<F>(LG_CRF_PIO2_HI), ph), s1);
+        const F plo = crf_add(pe, crf_sub(crf_bc<F>(LG_CRF_PIO2_LO), lo));
 #pragma unroll
-    for (int i = 0; i < crf_lanes<F>::n; ++i) {
-        crf_set(hi2, i, inv[i] ? crf_get(ph, i) : crf_get(s1, i));
-        crf_set(lo2, i, inv[i] ? crf_get(plo, i) : crf_get(lo, i));
+        for (int i = 0; i < crf_lanes<F>::n; ++i) {
+            crf_set(hi2, i, inv[i] ? crf_get(ph, i) : crf_get(s1, i));
+            crf_set(lo2, i, inv[i] ? crf_get(plo, i) : crf_get(lo, i));
+        }
     }
     F z1, z2;
     crf_ziv(hi2, lo2, z1, z2);
