@@ -1760,8 +1760,9 @@ public:
         // tensor-core training: width 128, two hidden layers, at most 8
         // transformed dimensions (one 16-wide K block for the input dense,
         // one 16-wide N block for the output dense)
+        // (plus 1 KB of static shared memory: the block's stop flag, aligned)
         tct = want_tct && tc && width == 128 && hidden == 2 && TcDims(f).kp0 == 16 && TcDims(f).np == 16 &&
-              TcStepSmem(f).total <= optin;
+              TcStepSmem(f).total + 1024 <= optin;
         if (tct)
             cudaFuncSetAttribute(lg_flow_step_tc, cudaFuncAttributeMaxDynamicSharedMemorySize, TcStepSmem(f).total);
         // the highest stream priority: training launches are small and
