@@ -1729,8 +1729,11 @@ public:
         return n;
     }
 
-    int rows() const { return tct ? 128 : (bf16 ? FR : FR32); }  // minibatch rows per training block
-    int step_smem() const { return StepSmem(f, rows(), bf16 ? 2 : 4).total; }
+    // rows per block and shared memory of the FP32-weight step kernel (also
+    // the forward passes that track the live points between trainings)
+    int simt_rows() const { return bf16 ? FR : FR32; }
+    int step_smem() const { return StepSmem(f, simt_rows(), bf16 ? 2 : 4).total; }
+    int rows() const { return tct ? 128 : simt_rows(); }  // minibatch rows per training block
     int inverse_smem() const { return InvSmem(f, FRI, bf16 ? 2 : 4).total; }
 
     bool init(int dim, int layers, int width, int hidden, uint64_t seed)
@@ -2310,7 +2313,7 @@ public:
                 hlive.p[(size_t)i * d + a] = (float)((live[(size_t)i * d + a] - hmean[k][a]) / hsdev[k][a]);
         if (cudaMemcpyAsync(dlive.p, hlive.p, (size_t)n * d * sizeof(float), cudaMemcpyHostToDevice, ps)) return;
         // the live points' latent radii through the active weights
-        const int blocks = (n + flow.rows() - 1) / flow.rows(), sm = flow.step_smem();
+        const int blocks = (n + flow.simt_rows() - 1) / flow.simt_rows(), sm = flow.step_smem();
         if (flow.bf16)
             lg_flow_step<FR, __nv_bfloat16><<<blocks, FT, sm, ps>>>(flow.f, Puse[k].p, dlive.p, nullptr, 0, n, 0,
                                                                     dtl.p, dtz.p, nullptr, (long)flow.nparams,
@@ -2318,6 +2321,7 @@ public:
         else
             lg_flow_step<FR32, float><<<blocks, FT, sm, ps>>>(flow.f, Puse[k].p, dlive.p, nullptr, 0, n, 0, dtl.p,
                                                             dtz.p, nullptr, (long)flow.nparams, nullptr);
+        if (cudaGetLastError() != cudaSuccess) return;  // (no update of the ball then)
         lg_flow_max<<<1, 1024, 0, ps>>>(dtz.p, n, -INFINITY, dtrack.p);
         // the weight bound of that ball, calibrated as at training
         const uint64_t key = seed * 0x9E3779B97F4A7C15ull + 0xD1B54A32D192ED03ull * (uint64_t)(++ntrack);
@@ -2439,9 +2443,10 @@ lg_flow_options lg_flow_defaults(void)
     o.lag = 800;
     o.draw_cost = 0.005;
     o.wait_tries = 0;
-    // the FP32-weight training kernels: on the sampler workload their flows
-    // propose better (16 seeds: 788 k likelihood calls against 1.08 M with
-    // the tensor-core steps, whose training step is 28% faster)
+    // the FP32-weight training kernels; the tensor-core steps (train_tc = 1)
+    // train flows that propose as well (16 seeds of the sampler workload:
+    // 785 k likelihood calls against 788 k) in steps 28% faster, a few
+    // hundredths of a second of a run
     o.train_tc = 0;
     return o;
 }
