@@ -488,7 +488,8 @@ int lg_flow_train_time(int device, int d, int layers, int width, int hidden, int
  * as the sampler does it on its live points: history receives the held-out
  * loss before training and after each epoch (NaN past the last epoch run);
  * returns the epochs run (negative: error; LG_ERR_TIMEOUT when a bounded
- * wait of the calibration's tensor-core inverse ran out, see wait_tries);
+ * wait of the tensor-core training step or of the calibration's
+ * tensor-core inverse ran out, see wait_tries; lg_last_error says which);
  * *efficiency = calibrated kept fraction of latent draws. */
 int lg_flow_fit(int device, int d, const lg_flow_options* opts, const double* pts, int n, float* history,
                 int max_history, double* efficiency);

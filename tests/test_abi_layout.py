@@ -51,3 +51,12 @@ def test_python_mirror_matches_the_header(c_layout, cname):
     assert c_layout[(cname, "size")] == lg.C.sizeof(py), cname
     for fname, _ in py._fields_:
         assert c_layout[(cname, fname)] == getattr(py, fname).offset, (cname, fname)
+
+
+def test_flow_defaults():
+    """lg_flow_defaults: the documented defaults of the learned proposal
+    (FP32-weight training steps, the default wait budget)."""
+    o = lg.lib().lg_flow_defaults()
+    assert (o.layers, o.width, o.hidden, o.epochs, o.batch) == (8, 128, 2, 200, 256)
+    assert o.wait_tries == 0 and o.train_tc == 0
+    assert o.lr == 1e-3 and o.patience == 4 and o.lag == 800
