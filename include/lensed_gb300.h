@@ -64,9 +64,11 @@ extern "C" {
  *                      correctly rounded (its value in double, rounded once):
  *                      model images and logL identical to the oracle's and to
  *                      the strict mode's.  Rays are traced in pairs with
- *                      f32x2 instructions; exp, log, atan and atanh are
- *                      computed in single-precision double-word arithmetic,
- *                      the others in double.
+ *                      f32x2 instructions; exp, log, atan, atanh, sin, cos,
+ *                      pow and atan2 are computed in single-precision
+ *                      double-word arithmetic (Ziv's rounding test, double
+ *                      where it cannot decide), the other functions in
+ *                      double.
  *   LG_FLAG_STRICT_FP  the same results one ray at a time with every
  *                      elementary function evaluated in double (the
  *                      definition the default mode reproduces; slow on
@@ -74,8 +76,8 @@ extern "C" {
  *   LG_FLAG_FAST_MATH  ray pairs with FMA contraction and hardware-
  *                      approximate functions (a few ulp each; what the
  *                      reference's -cl-fast-relaxed-math build allows):
- *                      about twice the default's throughput, logL within
- *                      about 1e-3 + 2e-6 |logL| of the oracle's */
+ *                      about three times the default's throughput, logL
+ *                      within about 1e-3 + 2e-6 |logL| of the oracle's */
 #define LG_FLAG_STRICT_FP 1  /* strict mode (above) */
 #define LG_FLAG_NO_GRAPH 2   /* launch kernels directly instead of graph replay */
 #define LG_FLAG_IEEE_DIV 4   /* fast mode with IEEE division and square root per ray */
