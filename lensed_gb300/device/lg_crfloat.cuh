@@ -1,5 +1,6 @@
-// Correctly rounded single-precision exp, log, atan and atanh computed in
-// single-precision arithmetic, for the exact evaluation modules.
+// Correctly rounded single-precision exp, log, atan, atanh, sin, cos, pow
+// and atan2 computed in single-precision arithmetic, for the exact
+// evaluation modules.
 //
 // The likelihood's FP32 semantics (the oracle's, and the strict modules')
 // takes every elementary function as its value evaluated in double and
